@@ -1,0 +1,318 @@
+"""Traversal benchmark: closest-hit Mrays/s of the GB300 LBVH path.
+
+Workload (the reference's traversal micro-benchmark configuration):
+1,048,576 FP32 triangles with seeded centroids uniform in the unit cube and
+vertices offset by U[-0.01, 0.01]; 16,777,216 rays with origins uniform in
+[-0.2, 1.2]^3 and directions uniform on the sphere, tmax unbounded.  One
+step = one closest-hit pass over all rays (Accelerator::intersect
+semantics, bit-exact IDs/t/uv).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbrt|reference]
+
+`value`: rays/s with rays resident in HBM (CUDA events on the launching
+stream).  `e2e`: the same through the host-buffer C ABI entry
+(gbrt_trace_closest_host) with rays in pinned host memory, the upload and
+the hit download inside the timed region.  The rays (512 MiB) exceed L2
+(129 MB), so no explicit flush is done between steps.
+Under torchrun each rank traces its own 16,777,216 rays on its own GPU
+(weak scaling, no collective on the data path); value sums over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_TRI = 1 << 20
+N_RAY = 1 << 24
+ALG_BYTES_PER_RAY = 32 + 16          # ray record in + hit record out
+ALG_BYTES_PER_TRI = 36               # three FP32 vertices, read once per pass
+FALLBACK_HBM_GBS = 6800.0
+METRIC = "Mrays/s closest-hit (1M-triangle traversal micro-benchmark)"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic_per_ray():
+    """DRAM bytes per ray of the closest-hit kernel from the committed ncu
+    summary (a line 'dram_bytes_per_ray: X'), or None."""
+    p = os.path.join(ROOT, "profiles", "traverse_closest_1M.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_ray:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1])); mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(verts, faces, rays, budget_s=12.0, threads=None):
+    """Oracle port (CPU restatement, front-to-back BVH, all host threads) on a
+    bounded sample of the same rays.  Returns rays/s and details."""
+    from oracle import orc
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    scene = orc.OracleScene(verts, faces)
+    build_s = time.perf_counter() - t0
+    probe = rays[: 20000 * threads]
+    t0 = time.perf_counter(); scene.trace(probe, 0, threads=threads); dt = time.perf_counter() - t0
+    n = int(min(len(rays), max(len(probe), len(probe) * budget_s / max(dt, 1e-6))))
+    sample = rays[len(probe):len(probe) + n] if len(probe) + n <= len(rays) else rays[:n]
+    t0 = time.perf_counter(); scene.trace(sample, 0, threads=threads); dt = time.perf_counter() - t0
+    return len(sample) / dt, {"cores": threads, "rays": len(sample), "seconds": dt, "build_s": build_s}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the CPU restatement of the reference's traversal
+    (kind 'port'; the reference's own kd-tree is not compiled on this host)
+    timed on all host threads, each step a bounded sample of the workload."""
+    if rank != 0:
+        return
+    from libyafaray_gb300 import scenes
+    from oracle import orc
+    threads = os.cpu_count() or 1
+    verts, faces = scenes.random_triangles(N_TRI, seed=1)
+    scene = orc.OracleScene(verts, faces)
+    sample = max(20000, 40000 * threads)
+    rays = scenes.random_rays(sample * 2, seed=2)
+    for _ in range(args.warmup):
+        scene.trace(rays[:sample], 0, threads=threads)
+    times = []
+    for k in range(args.steps):
+        chunk = rays[(k % 2) * sample:(k % 2 + 1) * sample]
+        t0 = time.perf_counter(); scene.trace(chunk, 0, threads=threads); times.append(time.perf_counter() - t0)
+    per_step = float(np.mean(times))
+    v = sample / per_step / 1e6
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+           "config": {"workload": "traversal micro-benchmark: 1,048,576 triangles, incoherent rays, closest hit",
+                      "triangles": N_TRI, "rays_per_step": sample, "sample_of": N_RAY},
+           "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                            "sample": f"{sample} of the {N_RAY} rays per step"},
+           "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbrt", choices=["gbrt", "reference"])
+    ap.add_argument("--rays", type=int, default=N_RAY)
+    ap.add_argument("--tris", type=int, default=N_TRI)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    from libyafaray_gb300 import gbrt, scenes
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    gbrt.load()
+
+    verts, faces = scenes.random_triangles(args.tris, seed=1)
+    rays_np = scenes.random_rays(args.rays, seed=2 + 1000 * rank)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    v_d = torch.from_numpy(verts).cuda()
+    f_d = torch.from_numpy(faces.view(np.int32)).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bvh = gbrt.Bvh.build_device(v_d.data_ptr(), len(verts), f_d.data_ptr(), len(faces), stream=sp)
+    build_s = time.perf_counter() - t0
+    info = bvh.info()
+    rays_d = torch.from_numpy(rays_np).cuda()
+    hits_d = torch.empty((args.rays, 4), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        bvh.trace_closest_device(rays_d.data_ptr(), args.rays, hits_d.data_ptr(), stream=sp)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for k in range(args.steps):
+            bvh.trace_closest_device(rays_d.data_ptr(), args.rays, hits_d.data_ptr(), stream=sp)
+            ev[k + 1].record(stream)
+        torch.cuda.synchronize()
+    launch_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[-1])
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    per_step_s = total_ms / 1e3 / args.steps
+    value = args.rays * world / per_step_s / 1e6
+    hits_np = hits_d[:, 0].cpu().numpy().view(np.int32)
+    hit_frac = float((hits_np >= 0).mean())
+
+    # any-hit pass over the same rays (reported beside the headline)
+    occ_d = torch.empty(args.rays, dtype=torch.int32, device="cuda")
+    bvh.trace_shadow_device(rays_d.data_ptr(), args.rays, occ_d.data_ptr(), stream=sp)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(3):
+        bvh.trace_shadow_device(rays_d.data_ptr(), args.rays, occ_d.data_ptr(), stream=sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    anyhit_mrays = args.rays * 3 / (e0.elapsed_time(e1) / 1e3) / 1e6
+
+    e2e = None
+    if not args.no_e2e:
+        rays_pin = torch.from_numpy(rays_np).pin_memory()
+        hits_pin = torch.empty((args.rays, 4), dtype=torch.float32).pin_memory()
+        rp, hp = rays_pin.numpy(), hits_pin.numpy()
+        import ctypes
+        L = gbrt.load()
+
+        def e2e_step():
+            gbrt.check(L.gbrt_trace_closest_host(bvh.handle, ctypes.c_void_p(rp.ctypes.data), args.rays,
+                                                 ctypes.c_void_p(hp.ctypes.data)))
+        for _ in range(2):
+            e2e_step()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        if dist:
+            t = torch.tensor([e2e_s], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        assert np.array_equal(hp[:, 0].view(np.int32), hits_np), "host path disagrees with device path"
+        e2e = {"value": args.rays * world / e2e_s / 1e6, "unit": "Mrays/s",
+               "h2d_bytes_per_step": int(rp.nbytes), "d2h_bytes_per_step": int(hp.nbytes),
+               "ms_per_step": e2e_s * 1e3, "gpu_launches_per_step": (args.rays + (1 << 21) - 1) >> 21}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    peak, peak_kind = peaks()
+    avg_launch_s = float(np.mean(launch_ms)) / 1e3
+    alg_bytes = args.rays * ALG_BYTES_PER_RAY + args.tris * ALG_BYTES_PER_TRI
+    achieved = alg_bytes / avg_launch_s / 1e9
+    tpr = ncu_traffic_per_ray()
+    cpu = None
+    if not args.no_cpu_baseline:
+        cv, cinfo = cpu_baseline(verts, faces, rays_np)
+        cpu = {"value": cv / 1e6, "unit": "Mrays/s", "cores": cinfo["cores"], "kind": "port",
+               "sample": f"{cinfo['rays']} of the {args.rays} rays on the same scene "
+                         f"({cinfo['seconds']:.1f} s, CPU restatement with a front-to-back BVH)"}
+    out = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per_step_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": "traversal micro-benchmark: 1,048,576 triangles (centroids U[0,1]^3, vertex offsets "
+                               "U[-0.01,0.01]), 16,777,216 incoherent rays (origins U[-0.2,1.2]^3, directions "
+                               "uniform on S^2), closest hit",
+                   "triangles": args.tris, "rays_per_gpu": args.rays, "l2": "inputs (512 MiB rays) larger than L2; no flush",
+                   "max_leaf_size": 4, "hit_fraction": hit_frac, "bvh_build_s": build_s,
+                   "bvh_nodes": info["n_nodes"], "bvh_depth": info["max_depth"], "bvh_sah": info["sah_cost"]},
+        "gpu_launches": args.steps,
+        "anyhit_mrays_s": anyhit_mrays,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": f"{peak_kind} (HBM copy bandwidth)",
+                     "traffic": (tpr * args.rays) if tpr is not None else None,
+                     "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_launch_s * 1e3},
+        "clocks": clocks.summary(),
+    }
+    if e2e:
+        out["e2e"] = e2e
+    if cpu:
+        out["cpu_baseline"] = cpu
+    print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,134 @@
+/*
+ * gbrt.h — C ABI of the GB300 (sm_103a) ray-tracing kernels behind
+ * libyafaray_gb300.  Plain C, no CUDA or torch types: device buffers are
+ * passed as plain pointers, streams as `void *` (a cudaStream_t, NULL for the
+ * legacy default stream).
+ *
+ * Conventions
+ *   - Every entry point returns an int status: GBRT_OK (0) or a negative
+ *     GBRT_ERR_* code; gbrt_last_error() gives the message of the calling
+ *     thread's last failure.  Nothing aborts or traps.
+ *   - Create calls allocate device memory and own it until the matching
+ *     destroy call; inputs are borrowed; outputs are caller-allocated.
+ *   - Calls taking `_dev` buffers are asynchronous on the given stream; calls
+ *     taking host buffers (`_host`) copy in, compute and copy out, and return
+ *     when the result is in host memory.
+ *   - A handle may be used from several host threads at once for queries;
+ *     build/destroy of one handle must not overlap other calls on it.
+ *
+ * Primitive layout (mirrors MeshObject faces, src/geometry/object/object_mesh.cc:96-112):
+ *   vertices : float[3 * n_vertices]
+ *   faces    : uint32[4 * n_faces]; faces[4*i+3] == GBRT_TRIANGLE marks a
+ *              triangle, otherwise the face is a quad and stays ONE primitive
+ *              (its two triangles are tested as in shape_polygon.h:126-176).
+ *   The primitive ID of face i is i (the order Scene::preprocess collects
+ *   primitives in, src/scene/scene.cc:320-341).
+ */
+#ifndef GBRT_H
+#define GBRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBRT_TRIANGLE 0xFFFFFFFFu
+
+enum {
+	GBRT_OK = 0,
+	GBRT_ERR_INVALID = -1,    /* bad argument (null pointer, bad index, size) */
+	GBRT_ERR_CUDA = -2,       /* a CUDA runtime call failed */
+	GBRT_ERR_OOM = -3,        /* device allocation failed */
+	GBRT_ERR_TIMEOUT = -4,    /* a device-side iteration budget ran out */
+	GBRT_ERR_CAPACITY = -5,   /* a size exceeds a fixed capacity */
+	GBRT_ERR_NO_DEVICE = -6   /* no CUDA device visible */
+};
+
+/* Ray record, 32 bytes: Ray::from_, tmin_, dir_, tmax_ (include/geometry/ray.h:46-49).
+ * tmax < 0 means unbounded, as in Accelerator::intersect (accelerator.h:91). */
+typedef struct gbrt_ray {
+	float org[3];
+	float tmin;
+	float dir[3];
+	float tmax;
+} gbrt_ray;
+
+/* Hit record, 16 bytes: the primitive ID (-1 = miss), t and the (u,v) that
+ * IntersectData carries (src/accelerator/intersect_data.h:30-39). */
+typedef struct gbrt_hit {
+	int32_t prim;
+	float t;
+	float u;
+	float v;
+} gbrt_hit;
+
+typedef struct gbrt_build_params {
+	uint32_t max_leaf_size;   /* 1..16; 0 = default (4) */
+	float traversal_cost;     /* SAH cost of a node visit; 0 = default (1.0) */
+	float intersect_cost;     /* SAH cost of a primitive test; 0 = default (1.0) */
+	uint32_t flags;           /* reserved, 0 */
+} gbrt_build_params;
+
+typedef struct gbrt_bvh_info {
+	uint32_t n_prims;
+	uint32_t n_nodes;         /* internal nodes actually referenced */
+	uint32_t n_leaves;
+	uint32_t max_depth;
+	float sah_cost;
+	float bound[6];           /* reference tree bound: lo xyz, hi xyz */
+	uint64_t device_bytes;    /* device memory held by the handle */
+} gbrt_bvh_info;
+
+typedef struct gbrt_bvh gbrt_bvh;
+
+/* Library / device ---------------------------------------------------- */
+const char *gbrt_last_error(void);
+int gbrt_version(void);
+int gbrt_device_count(int *count);
+
+/* BVH build.  Replaces the kd-tree construction that Accelerator::factory
+ * runs from Scene::preprocess (src/scene/scene.cc:347,
+ * src/accelerator/accelerator.cc:44-55, accelerator_kdtree_original.cc:65-141).
+ * LBVH: Morton codes, radix sort, Karras hierarchy, bottom-up refit with an
+ * SAH leaf-collapse.  Device-resident inputs. */
+int gbrt_bvh_build(const float *vertices_dev, uint32_t n_vertices,
+                   const uint32_t *faces_dev, uint32_t n_faces,
+                   const gbrt_build_params *params, void *stream, gbrt_bvh **out);
+
+/* Same from host arrays (copied to the device inside the call). */
+int gbrt_bvh_build_host(const float *vertices, uint32_t n_vertices,
+                        const uint32_t *faces, uint32_t n_faces,
+                        const gbrt_build_params *params, gbrt_bvh **out);
+
+int gbrt_bvh_destroy(gbrt_bvh *bvh);
+
+/* Accelerator::getBound (accelerator.h:53): the primitive bound grown by
+ * 0.1 % per axis (accelerator_kdtree_original.cc:99-103).  Synchronises. */
+int gbrt_bvh_get_bound(const gbrt_bvh *bvh, float bound_out[6]);
+int gbrt_bvh_get_info(const gbrt_bvh *bvh, gbrt_bvh_info *info);
+
+/* Closest hit for n rays: Accelerator::intersect(ray, camera)
+ * (accelerator.h:89-101 -> kdtree::intersect<Nearest>,
+ * accelerator_kdtree_common.h:108-255), same acceptance rule and dynamic ray
+ * bias.  Device buffers, async on stream. */
+int gbrt_trace_closest(const gbrt_bvh *bvh, const gbrt_ray *rays_dev, uint32_t n,
+                       gbrt_hit *hits_dev, void *stream);
+
+/* Any hit for n shadow rays: Accelerator::isShadowed (accelerator.h:103-111
+ * -> kdtree::intersect<Shadow>).  occluder_dev[i] = ID of an occluding
+ * primitive or -1.  Device buffers, async on stream. */
+int gbrt_trace_shadow(const gbrt_bvh *bvh, const gbrt_ray *rays_dev, uint32_t n,
+                      int32_t *occluder_dev, void *stream);
+
+/* Host-buffer variants: copy rays in, trace, copy results out, synchronise.
+ * These are what a host Accelerator::intersect batch path binds. */
+int gbrt_trace_closest_host(const gbrt_bvh *bvh, const gbrt_ray *rays, uint32_t n, gbrt_hit *hits);
+int gbrt_trace_shadow_host(const gbrt_bvh *bvh, const gbrt_ray *rays, uint32_t n, int32_t *occluder);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBRT_H */

@@ -1,0 +1,80 @@
+// Internal definitions shared by the gbrt translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "gbrt.h"
+
+// Leaf child reference: bit 31 set, bits 27..30 = count-1, bits 0..26 = first
+// primitive slot.  Internal child reference: node index (bit 31 clear).
+#define GBRT_LEAF_BIT 0x80000000u
+#define GBRT_LEAF_MAX_SLOTS (1u << 27)
+#define GBRT_LEAF_MAX_COUNT 16u
+#define GBRT_QUAD_BIT 0x80000000u
+
+__host__ __device__ inline uint32_t gbrt_leaf_ref(uint32_t first, uint32_t count)
+{
+	return GBRT_LEAF_BIT | ((count - 1u) << 27) | first;
+}
+
+// Device memory of a built hierarchy.
+//   nodes : 4 float4 per internal node (both children's boxes + refs):
+//           [0] c0.lo.x c0.hi.x c0.lo.y c0.hi.y
+//           [1] c1.lo.x c1.hi.x c1.lo.y c1.hi.y
+//           [2] c0.lo.z c0.hi.z c1.lo.z c1.hi.z
+//           [3] ref0 ref1 (uint bits) 0 0
+//   tris  : 3 float4 per primitive slot, leaf order:
+//           [0] v0.xyz e3.x   [1] e1.xyz e3.y   [2] e2.xyz e3.z
+//           (e_k = v_k - v0 in float, exactly as shape_polygon.h:130-131,155)
+//   ids   : primitive ID per slot, GBRT_QUAD_BIT set for quads
+//   meta  : float bound[6] (reference tree bound) + build scratch words
+struct gbrt_bvh {
+	int device = 0;
+	uint32_t n_prims = 0;
+	uint32_t n_node_slots = 0;
+	float4 *nodes = nullptr;
+	float4 *tris = nullptr;
+	uint32_t *ids = nullptr;
+	float *meta = nullptr;
+	uint64_t bytes = 0;
+	gbrt_build_params params{};
+	float host_bound[6]{};
+	bool host_bound_valid = false;
+	// Staging for the host-buffer entry points: two device slots of
+	// kStageRays rays each, two streams, grown on first use, guarded by mu.
+	void *stage_mu = nullptr;          // std::mutex*, kept opaque here
+	cudaStream_t stage_stream[2]{};
+	void *stage_rays[2]{};
+	void *stage_out[2]{};
+};
+
+// meta word offsets
+enum : int {
+	GBRT_META_BOUND = 0,        // 6 floats: reference tree bound
+	GBRT_META_CLO = 6,          // 3 floats: centroid bound lo
+	GBRT_META_CINV = 9,         // 3 floats: 1 / centroid extent (0 if flat)
+	GBRT_META_ORD = 12,         // 12 uints: ordered-int reduction scratch
+	GBRT_META_ERR = 24,         // 1 uint: build error flag (bad vertex index)
+	GBRT_META_WORDS = 32
+};
+
+int gbrt_set_error(int code, const char *fmt, ...);
+
+#define GBRT_CK(call)                                                                             \
+	do {                                                                                          \
+		cudaError_t gbrt_e_ = (call);                                                             \
+		if(gbrt_e_ != cudaSuccess)                                                                \
+			return gbrt_set_error(gbrt_e_ == cudaErrorMemoryAllocation ? GBRT_ERR_OOM : GBRT_ERR_CUDA, \
+			                      "%s: %s", #call, cudaGetErrorString(gbrt_e_));                  \
+	} while(0)
+
+// Launchers implemented in traverse.cu
+int gbrt_launch_closest(const gbrt_bvh *bvh, const gbrt_ray *rays, uint32_t n, gbrt_hit *hits, cudaStream_t s);
+int gbrt_launch_shadow(const gbrt_bvh *bvh, const gbrt_ray *rays, uint32_t n, int32_t *occ, cudaStream_t s);
+// Implemented in bvh_build.cu
+int gbrt_build_impl(const float *verts, uint32_t nv, const uint32_t *faces, uint32_t nf,
+                    const gbrt_build_params *params, cudaStream_t s, gbrt_bvh **out);

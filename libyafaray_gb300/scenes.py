@@ -1,0 +1,125 @@
+"""Seeded synthetic workloads (numpy PCG64 generators).
+
+Each generator returns plain arrays in the layout the C ABI takes:
+vertices float32 [nv,3]; faces uint32 [nf,4] with column 3 == 0xFFFFFFFF for
+a triangle (a quad keeps 4 indices and stays ONE primitive, as in
+src/geometry/object/object_mesh.cc:96-112); rays float32 [n,8] =
+(ox, oy, oz, dx, dy, dz, tmin, tmax) with tmax < 0 meaning unbounded
+(include/geometry/ray.h:43-48, accelerator.h:91).
+"""
+import math
+
+import numpy as np
+
+TRI = 0xFFFFFFFF
+
+
+def random_triangles(n, seed=1, spread=0.01):
+    """Triangle soup: centroids uniform in the unit cube, each vertex offset
+    from its centroid by U[-spread, spread] per axis (1,048,576 triangles in
+    the traversal micro-benchmark)."""
+    rng = np.random.default_rng(seed)
+    c = rng.random((n, 1, 3), dtype=np.float64)
+    off = rng.uniform(-spread, spread, size=(n, 3, 3))
+    verts = (c + off).astype(np.float32).reshape(-1, 3)
+    faces = np.empty((n, 4), np.uint32)
+    faces[:, :3] = np.arange(3 * n, dtype=np.uint32).reshape(n, 3)
+    faces[:, 3] = TRI
+    return verts, faces
+
+
+def random_rays(n, seed=2, lo=-0.2, hi=1.2, tmin=0.0, tmax=-1.0):
+    """Incoherent rays: origins uniform in [lo,hi]^3, directions uniform on
+    the sphere (z = 1-2u, phi = 2 pi v)."""
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(lo, hi, size=(n, 3))
+    u = rng.random(n)
+    v = rng.random(n)
+    z = 1.0 - 2.0 * u
+    r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+    phi = 2.0 * math.pi * v
+    d = np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=1)
+    rays = np.empty((n, 8), np.float32)
+    rays[:, 0:3] = o
+    rays[:, 3:6] = d
+    rays[:, 6] = tmin
+    rays[:, 7] = tmax
+    return rays
+
+
+def _box_quads(corner_lo, corner_hi, yaw_deg=0.0, center=None):
+    """Axis-aligned (optionally yawed about +y) box as 6 quads."""
+    x0, y0, z0 = corner_lo
+    x1, y1, z1 = corner_hi
+    p = np.array([[x0, y0, z0], [x1, y0, z0], [x1, y1, z0], [x0, y1, z0],
+                  [x0, y0, z1], [x1, y0, z1], [x1, y1, z1], [x0, y1, z1]], np.float64)
+    if yaw_deg:
+        cx = center if center is not None else p.mean(axis=0)
+        a = math.radians(yaw_deg)
+        R = np.array([[math.cos(a), 0, math.sin(a)], [0, 1, 0], [-math.sin(a), 0, math.cos(a)]])
+        p = (p - cx) @ R.T + cx
+    q = [[0, 3, 2, 1], [4, 5, 6, 7], [0, 1, 5, 4], [3, 7, 6, 2], [0, 4, 7, 3], [1, 2, 6, 5]]
+    return p, np.array(q, np.uint32)
+
+
+def cornell_mesh(as_quads=True):
+    """Cornell-style box [-1,1]x[0,2]x[-1,1] (floor, ceiling, back, left, right
+    walls) with two yawed boxes (0.6 m at +17 deg, 1.2 m at -20 deg).
+    Returns (verts, faces, face_group) with groups 0 grey walls, 1 red,
+    2 green, 3 short box, 4 tall box."""
+    V, F, G = [], [], []
+
+    def add(pts, quads, g):
+        base = sum(len(v) for v in V)
+        V.append(np.asarray(pts, np.float64))
+        for q in quads:
+            if as_quads:
+                F.append([base + q[0], base + q[1], base + q[2], base + q[3]]); G.append(g)
+            else:
+                F.append([base + q[0], base + q[1], base + q[2], TRI]); G.append(g)
+                F.append([base + q[0], base + q[2], base + q[3], TRI]); G.append(g)
+
+    walls = {
+        "floor": ([[-1, 0, -1], [1, 0, -1], [1, 0, 1], [-1, 0, 1]], 0),
+        "ceiling": ([[-1, 2, -1], [-1, 2, 1], [1, 2, 1], [1, 2, -1]], 0),
+        "back": ([[-1, 0, -1], [-1, 2, -1], [1, 2, -1], [1, 0, -1]], 0),
+        "left": ([[-1, 0, -1], [-1, 0, 1], [-1, 2, 1], [-1, 2, -1]], 1),
+        "right": ([[1, 0, -1], [1, 2, -1], [1, 2, 1], [1, 0, 1]], 2),
+    }
+    for pts, g in walls.values():
+        add(pts, [[0, 1, 2, 3]], g)
+    p, q = _box_quads((0.05, 0.0, -0.05), (0.65, 0.6, 0.55), 17.0)
+    add(p, q, 3)
+    p, q = _box_quads((-0.7, 0.0, -0.7), (-0.1, 1.2, -0.1), -20.0)
+    add(p, q, 4)
+    verts = np.concatenate(V).astype(np.float32)
+    faces = np.array(F, np.uint32)
+    return verts, faces, np.array(G, np.int32)
+
+
+def camera_rays(width, height, eye, target, up=(0.0, 1.0, 0.0), fov_deg=40.0, seed=None):
+    """Pinhole primary rays through pixel centres (or jittered when seed is
+    given), one per pixel, row-major from the top-left."""
+    eye = np.asarray(eye, np.float64)
+    w = np.asarray(target, np.float64) - eye
+    w /= np.linalg.norm(w)
+    r = np.cross(w, np.asarray(up, np.float64)); r /= np.linalg.norm(r)
+    u = np.cross(r, w)
+    th = math.tan(math.radians(fov_deg) * 0.5)
+    aspect = height / width
+    jy, jx = np.mgrid[0:height, 0:width].astype(np.float64)
+    if seed is not None:
+        rng = np.random.default_rng(seed)
+        jx += rng.random(jx.shape); jy += rng.random(jy.shape)
+    else:
+        jx += 0.5; jy += 0.5
+    px = (2.0 * jx / width - 1.0) * th
+    py = (1.0 - 2.0 * jy / height) * th * aspect
+    d = w[None, None, :] + px[..., None] * r[None, None, :] + py[..., None] * u[None, None, :]
+    d /= np.linalg.norm(d, axis=-1, keepdims=True)
+    rays = np.empty((height * width, 8), np.float32)
+    rays[:, 0:3] = eye
+    rays[:, 3:6] = d.reshape(-1, 3)
+    rays[:, 6] = 0.0
+    rays[:, 7] = -1.0
+    return rays

@@ -1,0 +1,125 @@
+"""TEST ORACLE bindings (test infrastructure, never the product path).
+
+``OracleScene`` wraps liborc.so, the C restatement of libYafaRay's
+ray/primitive acceleration semantics (oracle/traverse_oracle.c).
+``run_reference_kdtree`` drives oracle/_ref/kdtree_dump, the reference's own
+kd-tree (src/accelerator/accelerator_kdtree_original.cc) compiled from its
+sources by oracle/ref/Makefile; it exists only where the reference sources
+were available at build time and is used to make and check golden vectors.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module.
+"""
+import ctypes
+import os
+import struct
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liborc.so")
+REF_KDTREE = os.path.join(HERE, "_ref", "kdtree_dump")
+TRI_MARK = 0xFFFFFFFF
+
+_lib = None
+
+
+def build():
+    """Compile liborc.so (plain C, gcc)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        fp = ctypes.POINTER(ctypes.c_float)
+        up = ctypes.POINTER(ctypes.c_uint32)
+        ip = ctypes.POINTER(ctypes.c_int32)
+        L.orc_scene_create.restype = ctypes.c_void_p
+        L.orc_scene_create.argtypes = [fp, ctypes.c_uint32, up, ctypes.c_uint32]
+        L.orc_scene_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_scene_bound.argtypes = [ctypes.c_void_p, fp]
+        L.orc_trace.argtypes = [ctypes.c_void_p, fp, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ip, fp, fp, fp]
+        L.orc_mt_intersect.restype = ctypes.c_float
+        L.orc_mt_intersect.argtypes = [fp, ctypes.c_int, fp, fp, fp, fp]
+        L.orc_bound_cross.restype = ctypes.c_int
+        L.orc_bound_cross.argtypes = [fp, fp, fp, ctypes.c_float, fp, fp]
+        _lib = L
+    return _lib
+
+
+def _f(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class OracleScene:
+    """CPU restatement of an accelerator over one mesh (faces: uint32 [n,4],
+    column 3 == 0xFFFFFFFF for triangles)."""
+
+    def __init__(self, verts, faces):
+        self.verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+        self.faces = np.ascontiguousarray(faces, dtype=np.uint32).reshape(-1, 4)
+        L = lib()
+        self._h = L.orc_scene_create(_f(self.verts), len(self.verts),
+                                     self.faces.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                     len(self.faces))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_scene_destroy(self._h)
+            self._h = None
+
+    def bound(self):
+        out = np.zeros(6, np.float32)
+        lib().orc_scene_bound(self._h, _f(out))
+        return out
+
+    def trace(self, rays, mode=0, bruteforce=False, threads=None):
+        """rays: float32 [n,8] (ox oy oz dx dy dz tmin tmax).  mode 0 closest
+        (Accelerator::intersect), 1 shadow (Accelerator::isShadowed).
+        Returns (prim int32, t, u, v)."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        n = len(rays)
+        prim = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        u = np.empty(n, np.float32)
+        v = np.empty(n, np.float32)
+        if threads is None:
+            threads = os.cpu_count() or 1
+        lib().orc_trace(self._h, _f(rays), n, int(mode), int(bool(bruteforce)), int(threads),
+                        prim.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _f(t), _f(u), _f(v))
+        return prim, t, u, v
+
+
+def reference_available():
+    return os.path.exists(REF_KDTREE)
+
+
+def run_reference_kdtree(verts, faces, rays, mode=0, accel="yafaray-kdtree-original"):
+    """Run the compiled reference kd-tree ray by ray.  Returns
+    (bound[6], build_s, trace_s, prim, t, u, v)."""
+    verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+    faces = np.ascontiguousarray(faces, dtype=np.uint32).reshape(-1, 4)
+    rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
+        with open(fin, "wb") as f:
+            f.write(b"GBRTKD01")
+            f.write(struct.pack("<I", len(verts))); f.write(verts.tobytes())
+            f.write(struct.pack("<I", len(faces))); f.write(faces.tobytes())
+            f.write(struct.pack("<I", len(rays))); f.write(rays.tobytes())
+            f.write(struct.pack("<I", mode))
+            a = accel.encode()
+            f.write(struct.pack("<I", len(a))); f.write(a)
+        subprocess.run([REF_KDTREE, fin, fout], check=True, stdout=subprocess.DEVNULL)
+        raw = open(fout, "rb").read()
+    bound = np.frombuffer(raw[:24], np.float32).copy()
+    build_s, trace_s = struct.unpack("<dd", raw[24:40])
+    rec = np.frombuffer(raw[40:], dtype=np.dtype([("id", "<i4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")]))
+    return bound, build_s, trace_s, rec["id"].copy(), rec["t"].copy(), rec["u"].copy(), rec["v"].copy()

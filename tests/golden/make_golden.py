@@ -1,0 +1,105 @@
+"""Generates the traversal golden vectors in tests/golden/*.npz by running the
+reference libYafaRay kd-tree itself (oracle/_ref/kdtree_dump, built from the
+reference sources by oracle/ref/Makefile) ray by ray.
+
+    make -C oracle/ref -j8 && python tests/golden/make_golden.py
+
+Each file holds the scene (vertices, faces), the rays, and what the reference
+returned: closest hit (Accelerator::intersect) prim/t/u/v and shadow
+occlusion (Accelerator::isShadowed) as a hit flag, plus the tree bound.
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import orc  # noqa: E402
+from libyafaray_gb300 import scenes  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def edge_rays(verts, faces, n, seed):
+    """Rays aimed at face vertices and edge midpoints (shared-edge cases) and
+    axis-aligned rays (zero direction components)."""
+    rng = np.random.default_rng(seed)
+    lo, hi = verts.min(0), verts.max(0)
+    ext = hi - lo
+    rays = np.zeros((n, 8), np.float32)
+    for i in range(n):
+        f = faces[rng.integers(len(faces))]
+        nv = 3 if f[3] == scenes.TRI else 4
+        a, b = rng.choice(nv, 2, replace=False)
+        target = 0.5 * (verts[f[a]].astype(np.float64) + verts[f[b]]) if i % 2 else verts[f[a]].astype(np.float64)
+        o = lo - 0.3 * ext + rng.random(3) * 1.6 * ext
+        if i % 7 == 0:  # axis-aligned
+            ax = rng.integers(3)
+            o = target.copy(); o[ax] = lo[ax] - 0.5 * ext[ax] if rng.random() < 0.5 else hi[ax] + 0.5 * ext[ax]
+        d = target - o
+        d /= np.linalg.norm(d)
+        rays[i, :3] = o; rays[i, 3:6] = d; rays[i, 6] = 0.0; rays[i, 7] = -1.0
+    return rays
+
+
+def bounded_rays(rays, seed):
+    """Copies with tmin > 0 and finite tmax (shadow-ray style segments)."""
+    rng = np.random.default_rng(seed)
+    r = rays.copy()
+    r[:, 6] = rng.choice([0.0, 1e-4, 5e-4, 0.01], len(r)).astype(np.float32)
+    r[:, 7] = np.where(rng.random(len(r)) < 0.3, -1.0, rng.uniform(0.05, 2.0, len(r))).astype(np.float32)
+    return r
+
+
+def run_case(name, verts, faces, rays):
+    b0, bs, ts, p0, t0, u0, v0 = orc.run_reference_kdtree(verts, faces, rays, 0)
+    b1, _, _, p1, _, _, _ = orc.run_reference_kdtree(verts, faces, rays, 1)
+    assert np.array_equal(b0, b1)
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), vertices=verts, faces=faces, rays=rays, bound=b0,
+                        closest_prim=p0, closest_t=t0, closest_u=u0, closest_v=v0,
+                        shadow_hit=(p1 >= 0).astype(np.uint8))
+    print(f"{name}: {len(faces)} faces, {len(rays)} rays, {int((p0 >= 0).sum())} closest hits, "
+          f"{int((p1 >= 0).sum())} occluded, kd build {bs:.3f}s trace {ts:.3f}s")
+
+
+def main():
+    if not orc.reference_available():
+        sys.exit("oracle/_ref/kdtree_dump missing: run make -C oracle/ref first")
+    # 1. triangle soup, the traversal micro-benchmark's distribution, small
+    v, f = scenes.random_triangles(4096, seed=1)
+    r = scenes.random_rays(4096, seed=2)
+    run_case("tri_soup_4k", v, f, r)
+    # 1b. denser soup (larger triangles, many overlaps), incl. bounded segments
+    v, f = scenes.random_triangles(4096, seed=12, spread=0.06)
+    r = scenes.random_rays(6144, seed=13)
+    r = np.concatenate([r, bounded_rays(scenes.random_rays(2048, seed=14), seed=15)])
+    run_case("tri_soup_dense", v, f, r)
+    # 2. Cornell box, quads (one primitive per quad, shared edges)
+    v, f, _ = scenes.cornell_mesh(as_quads=True)
+    cam = scenes.camera_rays(48, 48, (0.0, 1.0, 3.7), (0.0, 1.0, 0.0), seed=5)
+    inside = scenes.random_rays(2048, seed=6, lo=-0.95, hi=0.95)
+    inside[:, 1] += 1.0
+    er = edge_rays(v, f, 1024, seed=7)
+    r = np.concatenate([cam, inside, er, bounded_rays(inside, seed=8)])
+    run_case("cornell_quads", v, f, r)
+    # 3. Cornell box as triangles
+    v, f, _ = scenes.cornell_mesh(as_quads=False)
+    er = edge_rays(v, f, 1024, seed=9)
+    r = np.concatenate([cam, inside, er, bounded_rays(inside, seed=10)])
+    run_case("cornell_tris", v, f, r)
+    # 4. one triangle, incl. degenerate neighbours (zero area)
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.5, 0.5, 0], [0.5, 0.5, 0], [0.2, 0.2, 0]], np.float32)
+    f = np.array([[0, 1, 2, scenes.TRI], [3, 4, 5, scenes.TRI]], np.uint32)
+    rng = np.random.default_rng(11)
+    r = np.zeros((512, 8), np.float32)
+    r[:, 0:2] = rng.uniform(-0.2, 1.2, (512, 2)); r[:, 2] = 1.0
+    r[:, 5] = -1.0; r[:, 7] = -1.0
+    r[::3, 5] = 1.0   # pointing away
+    r[::5, 2] = 0.0; r[::5, 3] = 1.0; r[::5, 5] = 0.0  # in-plane rays
+    run_case("single_tri", v, f, r)
+
+
+if __name__ == "__main__":
+    main()

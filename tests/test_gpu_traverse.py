@@ -1,0 +1,142 @@
+"""GPU traversal parity: the sm_103a LBVH build + closest/any-hit kernels,
+called through the C ABI, against the golden vectors of the reference
+kd-tree and against the oracle (same tie rule, so bit-exact)."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import orc
+from tests import parity
+from libyafaray_gb300 import gbrt, scenes
+
+pytestmark = pytest.mark.gpu
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+@pytest.fixture(scope="module")
+def dev(cuda_device):
+    return cuda_device
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_gpu_closest_vs_reference_golden(dev, path):
+    g = np.load(path)
+    bvh = gbrt.Bvh.build_host(g["vertices"], g["faces"])
+    assert np.array_equal(bvh.bound(), g["bound"])
+    got = bvh.trace_closest_host(g["rays"])
+    ref = (g["closest_prim"], g["closest_t"], g["closest_u"], g["closest_v"])
+    r = parity.compare_closest(g["vertices"], g["faces"], g["rays"], got, ref)
+    print(os.path.basename(path), r["mismatch"], "mismatches:", r["edge"], "on edges,", r["tie"], "exact ties")
+    assert not r["bad"], f"unexplained mismatches at {r['bad'][:10]}"
+    assert r["t_exact"] and r["uv_ok"]
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_gpu_shadow_vs_reference_golden(dev, path):
+    g = np.load(path)
+    bvh = gbrt.Bvh.build_host(g["vertices"], g["faces"])
+    occ = bvh.trace_shadow_host(g["rays"])
+    r = parity.compare_shadow(g["vertices"], g["faces"], g["rays"], occ, g["shadow_hit"])
+    assert not r["bad"], f"unexplained shadow mismatches at {r['bad'][:10]}"
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+@pytest.mark.parametrize("leaf", [1, 4, 16])
+def test_gpu_bitexact_vs_oracle_golden_scenes(dev, path, leaf):
+    g = np.load(path)
+    s = orc.OracleScene(g["vertices"], g["faces"])
+    bvh = gbrt.Bvh.build_host(g["vertices"], g["faces"], max_leaf_size=leaf)
+    got = bvh.trace_closest_host(g["rays"])
+    exp = s.trace(g["rays"], 0)
+    for a, b in zip(got, exp):
+        assert np.array_equal(a, b)
+    occ = bvh.trace_shadow_host(g["rays"])
+    occ_o, _, _, _ = s.trace(g["rays"], 1)
+    assert np.array_equal(occ >= 0, occ_o >= 0)
+
+
+@pytest.mark.parametrize("n_tri,n_ray,spread", [(100_000, 400_000, 0.01), (200_000, 200_000, 0.03)])
+def test_gpu_bitexact_vs_oracle_random(dev, n_tri, n_ray, spread):
+    v, f = scenes.random_triangles(n_tri, seed=31, spread=spread)
+    r = scenes.random_rays(n_ray, seed=32)
+    s = orc.OracleScene(v, f)
+    bvh = gbrt.Bvh.build_host(v, f)
+    got = bvh.trace_closest_host(r)
+    exp = s.trace(r, 0)
+    assert (exp[0] >= 0).sum() > n_ray // 20
+    for a, b in zip(got, exp):
+        assert np.array_equal(a, b)
+    occ = bvh.trace_shadow_host(r)
+    assert np.array_equal(occ >= 0, exp[0] >= 0)  # unbounded segments: occluded iff closest hit exists
+
+
+def test_gpu_device_pointer_path_matches_host_path(dev):
+    torch = pytest.importorskip("torch")
+    v, f = scenes.random_triangles(50_000, seed=41)
+    r = scenes.random_rays(100_000, seed=42)
+    vt = torch.from_numpy(v).cuda(); ft = torch.from_numpy(f.view(np.int32)).cuda()
+    rt = torch.from_numpy(r).cuda()
+    stream = torch.cuda.current_stream()
+    bvh = gbrt.Bvh.build_device(vt.data_ptr(), len(v), ft.data_ptr(), len(f), stream=stream.cuda_stream)
+    hits = torch.empty((len(r), 4), dtype=torch.float32, device="cuda")
+    bvh.trace_closest_device(rt.data_ptr(), len(r), hits.data_ptr(), stream=stream.cuda_stream)
+    occ = torch.empty(len(r), dtype=torch.int32, device="cuda")
+    bvh.trace_shadow_device(rt.data_ptr(), len(r), occ.data_ptr(), stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    h = hits.cpu().numpy()
+    p2, t2, u2, v2 = gbrt.Bvh.build_host(v, f).trace_closest_host(r)
+    assert np.array_equal(h[:, 0].view(np.int32), p2) and np.array_equal(h[:, 1], t2)
+    assert np.array_equal(occ.cpu().numpy() >= 0, p2 >= 0)
+
+
+def test_gpu_empty_and_single(dev):
+    r = scenes.random_rays(1000, seed=51)
+    bvh = gbrt.Bvh.build_host(np.zeros((0, 3), np.float32), np.zeros((0, 4), np.uint32))
+    p, t, u, v = bvh.trace_closest_host(r)
+    assert (p == -1).all() and (t == 0).all()
+    assert (bvh.trace_shadow_host(r) == -1).all()
+    assert np.array_equal(bvh.bound(), np.zeros(6, np.float32))
+    v1 = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    f1 = np.array([[0, 1, 2, scenes.TRI]], np.uint32)
+    rays = np.zeros((3, 8), np.float32)
+    rays[:, 0:3] = [[0.25, 0.25, 1.0], [0.9, 0.9, 1.0], [0.25, 0.25, -1.0]]
+    rays[:, 5] = -1.0; rays[:, 7] = -1.0
+    p, t, _, _ = gbrt.Bvh.build_host(v1, f1).trace_closest_host(rays)
+    assert list(p) == [0, -1, -1] and t[0] == 1.0
+
+
+def test_gpu_invalid_input_is_an_error(dev):
+    v = np.zeros((3, 3), np.float32)
+    f = np.array([[0, 1, 7, scenes.TRI]], np.uint32)
+    with pytest.raises(gbrt.GbrtError) as e:
+        gbrt.Bvh.build_host(v, f)
+    assert e.value.code == -1
+    with pytest.raises(gbrt.GbrtError):
+        gbrt.Bvh.build_host(v, np.zeros((1, 4), np.uint32), max_leaf_size=17)
+
+
+def test_gpu_full_size_properties(dev):
+    """1,048,576 triangles x 16,777,216 rays (the traversal benchmark):
+    a seeded subset of rays is checked ray by ray against the oracle, and
+    closest/any-hit agree on every ray."""
+    torch = pytest.importorskip("torch")
+    v, f = scenes.random_triangles(1 << 20, seed=1)
+    r = scenes.random_rays(1 << 24, seed=2)
+    bvh = gbrt.Bvh.build_host(v, f)
+    info = bvh.info()
+    assert info["n_prims"] == 1 << 20 and info["max_depth"] < 64
+    rt = torch.from_numpy(r).cuda()
+    hits = torch.empty((len(r), 4), dtype=torch.float32, device="cuda")
+    occ = torch.empty(len(r), dtype=torch.int32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    bvh.trace_closest_device(rt.data_ptr(), len(r), hits.data_ptr(), stream=s)
+    bvh.trace_shadow_device(rt.data_ptr(), len(r), occ.data_ptr(), stream=s)
+    torch.cuda.synchronize()
+    h = hits.cpu().numpy()
+    prim = h[:, 0].view(np.int32)
+    assert np.array_equal(prim >= 0, occ.cpu().numpy() >= 0)
+    sel = np.random.default_rng(3).choice(len(r), 200_000, replace=False)
+    exp = orc.OracleScene(v, f).trace(r[sel], 0)
+    assert np.array_equal(prim[sel], exp[0]) and np.array_equal(h[sel, 1], exp[1])
