@@ -109,6 +109,14 @@ int gbrt_bvh_destroy(gbrt_bvh *bvh);
 int gbrt_bvh_get_bound(const gbrt_bvh *bvh, float bound_out[6]);
 int gbrt_bvh_get_info(const gbrt_bvh *bvh, gbrt_bvh_info *info);
 
+/* Copies the device hierarchy to host buffers (for validation tools):
+ * nodes: 64 bytes per node slot (gbrt_bvh_info.n_nodes counts the reachable
+ * ones; the slot count is max(n_prims - 1, 1)), prims: 48 bytes and ids: 4
+ * bytes per primitive slot.  Any pointer may be NULL to skip that array.
+ * Layout: see libyafaray_gb300/csrc/gbrt_internal.cuh.  Synchronises. */
+int gbrt_bvh_export(const gbrt_bvh *bvh, void *nodes, size_t nodes_bytes, void *prims, size_t prims_bytes,
+                    uint32_t *ids, size_t ids_bytes);
+
 /* Closest hit for n rays: Accelerator::intersect(ray, camera)
  * (accelerator.h:89-101 -> kdtree::intersect<Nearest>,
  * accelerator_kdtree_common.h:108-255), same acceptance rule and dynamic ray

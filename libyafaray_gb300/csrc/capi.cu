@@ -199,6 +199,19 @@ int gbrt_bvh_get_info(const gbrt_bvh *b, gbrt_bvh_info *info)
 	return GBRT_OK;
 }
 
+int gbrt_bvh_export(const gbrt_bvh *b, void *nodes, size_t nodes_bytes, void *prims, size_t prims_bytes,
+                    uint32_t *ids, size_t ids_bytes)
+{
+	if(!b) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_bvh_export: NULL handle");
+	const size_t nb = 64ull * b->n_node_slots, pb = 48ull * b->n_prims, ib = 4ull * b->n_prims;
+	if((nodes && nodes_bytes < nb) || (prims && prims_bytes < pb) || (ids && ids_bytes < ib))
+		return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_bvh_export: buffers too small (need %zu/%zu/%zu bytes)", nb, pb, ib);
+	if(nodes) GBRT_CK(cudaMemcpy(nodes, b->nodes, nb, cudaMemcpyDeviceToHost));
+	if(prims && pb) GBRT_CK(cudaMemcpy(prims, b->tris, pb, cudaMemcpyDeviceToHost));
+	if(ids && ib) GBRT_CK(cudaMemcpy(ids, b->ids, ib, cudaMemcpyDeviceToHost));
+	return GBRT_OK;
+}
+
 int gbrt_trace_closest(const gbrt_bvh *b, const gbrt_ray *rays_dev, uint32_t n, gbrt_hit *hits_dev, void *stream)
 {
 	if(!b) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_trace_closest: NULL handle");

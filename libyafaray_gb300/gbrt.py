@@ -47,6 +47,7 @@ SIGNATURES = {
     "gbrt_bvh_destroy": (_I, [_VP]),
     "gbrt_bvh_get_bound": (_I, [_VP, ctypes.POINTER(ctypes.c_float)]),
     "gbrt_bvh_get_info": (_I, [_VP, ctypes.POINTER(BvhInfo)]),
+    "gbrt_bvh_export": (_I, [_VP, _VP, ctypes.c_size_t, _VP, ctypes.c_size_t, _VP, ctypes.c_size_t]),
     "gbrt_trace_closest": (_I, [_VP, _VP, _U32, _VP, _VP]),
     "gbrt_trace_shadow": (_I, [_VP, _VP, _U32, _VP, _VP]),
     "gbrt_trace_closest_host": (_I, [_VP, _VP, _U32, _VP]),
@@ -132,6 +133,17 @@ class Bvh:
         return {"n_prims": inf.n_prims, "n_nodes": inf.n_nodes, "n_leaves": inf.n_leaves,
                 "max_depth": inf.max_depth, "sah_cost": inf.sah_cost, "bound": list(inf.bound),
                 "device_bytes": inf.device_bytes}
+
+    def export(self):
+        """(nodes float32 [slots,16], prims float32 [n,12], ids uint32 [n])."""
+        inf = self.info()
+        n = inf["n_prims"]
+        slots = max(n - 1, 1)
+        nodes = np.empty((slots, 16), np.float32)
+        prims = np.empty((max(n, 1), 12), np.float32)
+        ids = np.empty(max(n, 1), np.uint32)
+        check(load().gbrt_bvh_export(self._h, _ptr(nodes), nodes.nbytes, _ptr(prims), prims.nbytes, _ptr(ids), ids.nbytes))
+        return nodes, prims[:n], ids[:n]
 
     def trace_closest_host(self, rays):
         r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)

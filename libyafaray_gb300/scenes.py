@@ -3,9 +3,9 @@
 Each generator returns plain arrays in the layout the C ABI takes:
 vertices float32 [nv,3]; faces uint32 [nf,4] with column 3 == 0xFFFFFFFF for
 a triangle (a quad keeps 4 indices and stays ONE primitive, as in
-src/geometry/object/object_mesh.cc:96-112); rays float32 [n,8] =
-(ox, oy, oz, dx, dy, dz, tmin, tmax) with tmax < 0 meaning unbounded
-(include/geometry/ray.h:43-48, accelerator.h:91).
+src/geometry/object/object_mesh.cc:96-112); rays float32 [n,8] in the
+gbrt_ray layout (ox, oy, oz, tmin, dx, dy, dz, tmax) with tmax < 0 meaning
+unbounded (include/geometry/ray.h:43-48, accelerator.h:91).
 """
 import math
 
@@ -41,8 +41,8 @@ def random_rays(n, seed=2, lo=-0.2, hi=1.2, tmin=0.0, tmax=-1.0):
     d = np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=1)
     rays = np.empty((n, 8), np.float32)
     rays[:, 0:3] = o
-    rays[:, 3:6] = d
-    rays[:, 6] = tmin
+    rays[:, 3] = tmin
+    rays[:, 4:7] = d
     rays[:, 7] = tmax
     return rays
 
@@ -119,7 +119,7 @@ def camera_rays(width, height, eye, target, up=(0.0, 1.0, 0.0), fov_deg=40.0, se
     d /= np.linalg.norm(d, axis=-1, keepdims=True)
     rays = np.empty((height * width, 8), np.float32)
     rays[:, 0:3] = eye
-    rays[:, 3:6] = d.reshape(-1, 3)
-    rays[:, 6] = 0.0
+    rays[:, 3] = 0.0
+    rays[:, 4:7] = d.reshape(-1, 3)
     rays[:, 7] = -1.0
     return rays

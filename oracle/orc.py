@@ -81,7 +81,7 @@ class OracleScene:
         return out
 
     def trace(self, rays, mode=0, bruteforce=False, threads=None):
-        """rays: float32 [n,8] (ox oy oz dx dy dz tmin tmax).  mode 0 closest
+        """rays: float32 [n,8] (ox oy oz tmin dx dy dz tmax).  mode 0 closest
         (Accelerator::intersect), 1 shadow (Accelerator::isShadowed).
         Returns (prim int32, t, u, v)."""
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)

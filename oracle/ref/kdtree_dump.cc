@@ -8,7 +8,7 @@
 //   char[8]  "GBRTKD01"
 //   u32 nv;  f32 v[nv][3]
 //   u32 nf;  u32 f[nf][4]        (f[3] == 0xFFFFFFFF marks a triangle)
-//   u32 nr;  f32 r[nr][8]        (ox oy oz dx dy dz tmin tmax)
+//   u32 nr;  f32 r[nr][8]        (ox oy oz tmin dx dy dz tmax)
 //   u32 mode                     0 closest (Accelerator::intersect(ray, camera) t_max rule)
 //                                1 shadow  (Accelerator::isShadowed wrapper)
 //   u32 len; char accel_type[len]
@@ -94,7 +94,7 @@ int main(int argc, char **argv)
 	for(uint32_t i = 0; i < nr; ++i)
 	{
 		const float *r = &rays[8ull * i];
-		yafaray::Ray ray{{{r[0], r[1], r[2]}}, {{r[3], r[4], r[5]}}, 0.f, r[6], r[7]};
+		yafaray::Ray ray{{{r[0], r[1], r[2]}}, {{r[4], r[5], r[6]}}, 0.f, r[3], r[7]};
 		yafaray::IntersectData d;
 		if(mode == 0)
 		{

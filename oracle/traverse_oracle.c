@@ -337,8 +337,8 @@ static inline int slab(const box *b, const float *o, const float *inv, float t0,
 static void query(const orc_scene *s, const float *r, int mode, int bruteforce, int32_t *prim, float *tout, float *uout, float *vout)
 {
 	float from[3] = {r[0], r[1], r[2]};
-	const float dir[3] = {r[3], r[4], r[5]};
-	const float tmin = r[6], tmax = r[7];
+	const float dir[3] = {r[4], r[5], r[6]};
+	const float tmin = r[3], tmax = r[7];
 	float t_max;
 	if(mode == 0) t_max = (tmax >= 0.f) ? tmax : FLT_MAX;
 	else
@@ -420,7 +420,8 @@ static void *worker(void *p)
 	return NULL;
 }
 
-/* rays: 8 floats each (ox oy oz dx dy dz tmin tmax).  threads <= 1: serial. */
+/* rays: 8 floats each (ox oy oz tmin dx dy dz tmax), the gbrt_ray layout.
+ * threads <= 1: serial. */
 void orc_trace(const orc_scene *s, const float *rays, uint32_t n, int mode, int bruteforce, int threads,
                int32_t *prim, float *t, float *u, float *v)
 {

@@ -40,7 +40,7 @@ def edge_rays(verts, faces, n, seed):
             o = target.copy(); o[ax] = lo[ax] - 0.5 * ext[ax] if rng.random() < 0.5 else hi[ax] + 0.5 * ext[ax]
         d = target - o
         d /= np.linalg.norm(d)
-        rays[i, :3] = o; rays[i, 3:6] = d; rays[i, 6] = 0.0; rays[i, 7] = -1.0
+        rays[i, :3] = o; rays[i, 3] = 0.0; rays[i, 4:7] = d; rays[i, 7] = -1.0
     return rays
 
 
@@ -48,7 +48,7 @@ def bounded_rays(rays, seed):
     """Copies with tmin > 0 and finite tmax (shadow-ray style segments)."""
     rng = np.random.default_rng(seed)
     r = rays.copy()
-    r[:, 6] = rng.choice([0.0, 1e-4, 5e-4, 0.01], len(r)).astype(np.float32)
+    r[:, 3] = rng.choice([0.0, 1e-4, 5e-4, 0.01], len(r)).astype(np.float32)
     r[:, 7] = np.where(rng.random(len(r)) < 0.3, -1.0, rng.uniform(0.05, 2.0, len(r))).astype(np.float32)
     return r
 
@@ -95,9 +95,9 @@ def main():
     rng = np.random.default_rng(11)
     r = np.zeros((512, 8), np.float32)
     r[:, 0:2] = rng.uniform(-0.2, 1.2, (512, 2)); r[:, 2] = 1.0
-    r[:, 5] = -1.0; r[:, 7] = -1.0
-    r[::3, 5] = 1.0   # pointing away
-    r[::5, 2] = 0.0; r[::5, 3] = 1.0; r[::5, 5] = 0.0  # in-plane rays
+    r[:, 6] = -1.0; r[:, 7] = -1.0
+    r[::3, 6] = 1.0   # pointing away
+    r[::5, 2] = 0.0; r[::5, 4] = 1.0; r[::5, 6] = 0.0  # in-plane rays
     run_case("single_tri", v, f, r)
 
 

@@ -40,7 +40,7 @@ def near_edge(verts, faces, ray, prim, t):
     if prim < 0:
         return False
     o = ray[:3].astype(np.float64)
-    d = ray[3:6].astype(np.float64)
+    d = ray[4:7].astype(np.float64)
     p = o + float(t) * d
     scale = max(1.0, float(np.abs(p).max()))
     slack = 8.0 * float(np.finfo(np.float32).eps) * abs(float(t)) * float(np.linalg.norm(d))
@@ -76,9 +76,9 @@ def _segment_edge_hit(verts, faces, ray):
     import ctypes
     from oracle import orc
     L = orc.lib()
-    o = ray[:3].astype(np.float32) + ray[3:6].astype(np.float32) * np.float32(ray[6])
-    d = ray[3:6].astype(np.float32)
-    t_max = np.float32(ray[7] - 2 * ray[6]) if ray[7] >= 0 else np.float32(np.finfo(np.float32).max)
+    o = ray[:3].astype(np.float32) + ray[4:7].astype(np.float32) * np.float32(ray[3])
+    d = ray[4:7].astype(np.float32)
+    t_max = np.float32(ray[7] - 2 * ray[3]) if ray[7] >= 0 else np.float32(np.finfo(np.float32).max)
     fp = ctypes.POINTER(ctypes.c_float)
     u = ctypes.c_float(); v = ctypes.c_float()
     for k, f in enumerate(faces):

@@ -102,7 +102,7 @@ def test_gpu_empty_and_single(dev):
     f1 = np.array([[0, 1, 2, scenes.TRI]], np.uint32)
     rays = np.zeros((3, 8), np.float32)
     rays[:, 0:3] = [[0.25, 0.25, 1.0], [0.9, 0.9, 1.0], [0.25, 0.25, -1.0]]
-    rays[:, 5] = -1.0; rays[:, 7] = -1.0
+    rays[:, 6] = -1.0; rays[:, 7] = -1.0
     p, t, _, _ = gbrt.Bvh.build_host(v1, f1).trace_closest_host(rays)
     assert list(p) == [0, -1, -1] and t[0] == 1.0
 
@@ -140,3 +140,21 @@ def test_gpu_full_size_properties(dev):
     sel = np.random.default_rng(3).choice(len(r), 200_000, replace=False)
     exp = orc.OracleScene(v, f).trace(r[sel], 0)
     assert np.array_equal(prim[sel], exp[0]) and np.array_equal(h[sel, 1], exp[1])
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_gpu_bvh_structure(dev, path):
+    from tests.bvh_check import check_bvh
+    g = np.load(path)
+    bvh = gbrt.Bvh.build_host(g["vertices"], g["faces"])
+    nodes, prims, ids = bvh.export()
+    assert check_bvh(nodes, prims, ids, g["vertices"], g["faces"]) == []
+
+
+def test_gpu_bvh_structure_random(dev):
+    from tests.bvh_check import check_bvh
+    v, f = scenes.random_triangles(30_000, seed=61)
+    for leaf in (1, 4, 16):
+        bvh = gbrt.Bvh.build_host(v, f, max_leaf_size=leaf)
+        nodes, prims, ids = bvh.export()
+        assert check_bvh(nodes, prims, ids, v, f) == []
