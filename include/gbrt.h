@@ -104,6 +104,38 @@ int gbrt_bvh_build_host(const float *vertices, uint32_t n_vertices,
 
 int gbrt_bvh_destroy(gbrt_bvh *bvh);
 
+/* Largest face count gbrt_bvh_build_static accepts. */
+#define GBRT_STATIC_MAX_FACES 65536u
+
+/* BVH build that allocates nothing.  This entry point has no counterpart in
+ * the reference: it exists for callers that must not allocate device memory
+ * at build time — a render loop that rebuilds small per-object hierarchies
+ * every frame cannot afford cudaMalloc/cudaFree (they synchronise the whole
+ * device and can fail under memory pressure), and a host application that
+ * budgets GPU memory itself (through its own pool) hands out only the
+ * output buffers.
+ *
+ * Same inputs and results as gbrt_bvh_build, written into caller buffers in
+ * the layout gbrt_bvh_export produces: nodes 64 bytes x max(n_faces-1, 1),
+ * prims 48 bytes x n_faces, ids 4 bytes x n_faces (device memory), and the
+ * tree bound into bound_out (host memory, 6 floats).
+ *
+ * The build's temporary arrays live in one fixed device array inside the
+ * library, sized for GBRT_STATIC_MAX_FACES faces (about 7 MB, held on every
+ * GPU that loads the library until the process exits).  More faces return
+ * GBRT_ERR_CAPACITY.  The first call on a device looks up that array's
+ * device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  Every call, on every stream, shares the array: calls that
+ * overlap on the GPU race and corrupt each other's result, so serialise
+ * them.  Synchronises `stream` before returning. */
+int gbrt_bvh_build_static(const float *vertices_dev, uint32_t n_vertices,
+                          const uint32_t *faces_dev, uint32_t n_faces,
+                          const gbrt_build_params *params,
+                          void *nodes_dev, size_t nodes_bytes,
+                          void *prims_dev, size_t prims_bytes,
+                          uint32_t *ids_dev, size_t ids_bytes,
+                          float bound_out[6], void *stream);
+
 /* Accelerator::getBound (accelerator.h:53): the primitive bound grown by
  * 0.1 % per axis (accelerator_kdtree_original.cc:99-103).  Synchronises. */
 int gbrt_bvh_get_bound(const gbrt_bvh *bvh, float bound_out[6]);

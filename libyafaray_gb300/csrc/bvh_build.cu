@@ -19,6 +19,8 @@
 
 #include <cfloat>
 #include <cmath>
+#include <cstring>
+#include <mutex>
 
 namespace {
 
@@ -539,5 +541,159 @@ int gbrt_build_impl(const float *verts, uint32_t nv, const uint32_t *faces, uint
 	}
 	if((e = cudaGetLastError()) != cudaSuccess) return fail(gbrt_set_error(GBRT_ERR_CUDA, "build launch: %s", cudaGetErrorString(e)));
 	*out = b;
+	return GBRT_OK;
+}
+
+// ---- build without device allocation -------------------------------------
+// gbrt_bvh_build_static runs the same kernels as gbrt_build_impl, with its
+// temporaries carved from one file-scope device array instead of a
+// stream-ordered allocation.
+namespace {
+
+constexpr size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct StaticLayout {
+	size_t blo, bhi, k0, k1, v0, v1, hist, child, range, pint, pleaf, nlo, nhi, flags, coll, meta, total;
+};
+
+constexpr StaticLayout static_layout(uint64_t nf)
+{
+	const uint64_t n_int = nf > 1 ? nf - 1 : 1;
+	const uint64_t nblk = (nf + kSortTile - 1) / kSortTile;
+	StaticLayout L{};
+	size_t o = 0;
+	L.blo = o; o += round256(16 * nf);
+	L.bhi = o; o += round256(16 * nf);
+	L.k0 = o; o += round256(4 * nf);
+	L.k1 = o; o += round256(4 * nf);
+	L.v0 = o; o += round256(4 * nf);
+	L.v1 = o; o += round256(4 * nf);
+	L.hist = o; o += round256(4 * 256 * nblk);
+	L.child = o; o += round256(8 * n_int);
+	L.range = o; o += round256(8 * n_int);
+	L.pint = o; o += round256(4 * n_int);
+	L.pleaf = o; o += round256(4 * nf);
+	L.nlo = o; o += round256(16 * n_int);
+	L.nhi = o; o += round256(16 * n_int);
+	L.flags = o; o += round256(4 * n_int);
+	L.coll = o; o += round256(n_int);
+	L.meta = o; o += round256(4 * GBRT_META_WORDS);
+	L.total = o;
+	return L;
+}
+
+constexpr size_t kStaticScratchBytes = static_layout(GBRT_STATIC_MAX_FACES).total;
+
+// Shared by every call on a device; see gbrt_bvh_build_static in gbrt.h.
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+unsigned char *g_static_addr[kMaxDevices] = {};
+
+// Device address of g_static_scratch on the current device, looked up once
+// per device (host code must not use the symbol itself as a pointer).
+int static_scratch_address(int dev, unsigned char **out)
+{
+	if(dev < 0 || dev >= kMaxDevices) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_bvh_build_static: device %d out of range", dev);
+	std::lock_guard<std::mutex> g(g_static_mu);
+	if(!g_static_addr[dev])
+	{
+		void *p = nullptr;
+		const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+		if(e != cudaSuccess || !p)
+			return gbrt_set_error(GBRT_ERR_CUDA, "gbrt_bvh_build_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+		g_static_addr[dev] = static_cast<unsigned char *>(p);
+	}
+	*out = g_static_addr[dev];
+	return GBRT_OK;
+}
+
+} // namespace
+
+extern "C" int gbrt_bvh_build_static(const float *verts, uint32_t nv, const uint32_t *faces, uint32_t nf,
+                                     const gbrt_build_params *params, void *nodes_dev, size_t nodes_bytes,
+                                     void *prims_dev, size_t prims_bytes, uint32_t *ids_dev, size_t ids_bytes,
+                                     float bound_out[6], void *stream)
+{
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	if(nf > GBRT_STATIC_MAX_FACES)
+		return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_bvh_build_static: %u faces exceed the fixed scratch capacity of %u faces",
+		                      nf, GBRT_STATIC_MAX_FACES);
+	if(nf > 0 && (!verts || !faces)) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_bvh_build_static: NULL vertex or face buffer");
+	if(!bound_out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_bvh_build_static: bound_out is NULL");
+	const uint32_t n_int = nf > 1 ? nf - 1 : 1;
+	if(!nodes_dev || nodes_bytes < 64ull * n_int || (nf && (!prims_dev || prims_bytes < 48ull * nf || !ids_dev || ids_bytes < 4ull * nf)))
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_bvh_build_static: output buffers missing or too small (need %llu/%llu/%llu bytes)",
+		                      64ull * n_int, 48ull * nf, 4ull * nf);
+	gbrt_build_params p{};
+	if(params) p = *params;
+	if(p.max_leaf_size == 0) p.max_leaf_size = 4;
+	if(p.max_leaf_size > GBRT_LEAF_MAX_COUNT) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_bvh_build_static: max_leaf_size %u > %u", p.max_leaf_size, GBRT_LEAF_MAX_COUNT);
+	if(!(p.traversal_cost > 0.f)) p.traversal_cost = 1.f;
+	if(!(p.intersect_cost > 0.f)) p.intersect_cost = 1.f;
+	int dev = 0;
+	GBRT_CK(cudaGetDevice(&dev));
+	unsigned char *base = nullptr;
+	if(int rc = static_scratch_address(dev, &base)) return rc;
+
+	const StaticLayout L = static_layout(nf);
+	float *meta = reinterpret_cast<float *>(base + L.meta);
+	float4 *nodes = static_cast<float4 *>(nodes_dev);
+	k_init_meta<<<1, 32, 0, s>>>(meta);
+	if(nf == 0)
+	{
+		k_finalize<<<1, 32, 0, s>>>(meta, 0);
+		GBRT_CK(cudaMemsetAsync(nodes_dev, 0, 64ull * n_int, s));
+	}
+	else
+	{
+		float4 *blo = reinterpret_cast<float4 *>(base + L.blo), *bhi = reinterpret_cast<float4 *>(base + L.bhi);
+		uint32_t *k0 = reinterpret_cast<uint32_t *>(base + L.k0), *k1 = reinterpret_cast<uint32_t *>(base + L.k1);
+		uint32_t *v0 = reinterpret_cast<uint32_t *>(base + L.v0), *v1 = reinterpret_cast<uint32_t *>(base + L.v1);
+		uint32_t *hist = reinterpret_cast<uint32_t *>(base + L.hist);
+		uint2 *child = reinterpret_cast<uint2 *>(base + L.child), *range = reinterpret_cast<uint2 *>(base + L.range);
+		uint32_t *pint = reinterpret_cast<uint32_t *>(base + L.pint), *pleaf = reinterpret_cast<uint32_t *>(base + L.pleaf);
+		float4 *nlo = reinterpret_cast<float4 *>(base + L.nlo), *nhi = reinterpret_cast<float4 *>(base + L.nhi);
+		uint32_t *flags = reinterpret_cast<uint32_t *>(base + L.flags);
+		uint8_t *coll = reinterpret_cast<uint8_t *>(base + L.coll);
+		float4 *tris = static_cast<float4 *>(prims_dev);
+		k_setup<<<blocks_for(nf, 256), 256, 0, s>>>(verts, nv, faces, nf, blo, bhi, meta);
+		k_finalize<<<1, 32, 0, s>>>(meta, nf);
+		if(nf == 1)
+		{
+			k_emit_single<<<1, 1, 0, s>>>(blo, bhi, meta, nodes);
+			k_emit_prims<<<1, 32, 0, s>>>(verts, faces, nullptr, 1, meta, tris, ids_dev);
+		}
+		else
+		{
+			const uint32_t nblk = blocks_for(nf, kSortTile);
+			k_morton<<<blocks_for(nf, 256), 256, 0, s>>>(blo, bhi, nf, meta, k0, v0);
+			uint32_t *kin = k0, *kout = k1, *vin = v0, *vout = v1;
+			for(int shift = 0; shift < 30; shift += 8)
+			{
+				k_hist<<<nblk, kSortThreads, 0, s>>>(kin, nf, shift, hist, nblk);
+				k_scan<<<1, 1024, 0, s>>>(hist, 256u * nblk);
+				k_scatter<<<nblk, kSortThreads, 0, s>>>(kin, vin, nf, shift, hist, nblk, kout, vout);
+				std::swap(kin, kout); std::swap(vin, vout);
+			}
+			// the array keeps the previous call's contents: reset parents and arrival counters
+			GBRT_CK(cudaMemsetAsync(pint, 0xFF, 4ull * n_int, s));
+			GBRT_CK(cudaMemsetAsync(flags, 0, 4ull * n_int, s));
+			k_karras<<<blocks_for(n_int, 256), 256, 0, s>>>(kin, static_cast<int>(nf), child, range, pint, pleaf);
+			k_refit<<<blocks_for(nf, 256), 256, 0, s>>>(vin, static_cast<int>(nf), blo, bhi, child, pint, pleaf, nlo, nhi, flags, coll,
+			                                            p.max_leaf_size, p.traversal_cost, p.intersect_cost);
+			k_emit_nodes<<<blocks_for(n_int, 256), 256, 0, s>>>(static_cast<int>(n_int), vin, blo, bhi, child, range, nlo, nhi, coll, meta, nodes);
+			k_emit_prims<<<blocks_for(nf, 256), 256, 0, s>>>(verts, faces, vin, nf, meta, tris, ids_dev);
+		}
+	}
+	GBRT_CK(cudaGetLastError());
+	float m[GBRT_META_WORDS];
+	GBRT_CK(cudaMemcpyAsync(m, meta, sizeof(m), cudaMemcpyDeviceToHost, s));
+	GBRT_CK(cudaStreamSynchronize(s));
+	uint32_t err;
+	std::memcpy(&err, &m[GBRT_META_ERR], 4);
+	if(err) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_bvh_build_static: a face references a vertex index >= %u", nv);
+	std::memcpy(bound_out, &m[GBRT_META_BOUND], 6 * sizeof(float));
 	return GBRT_OK;
 }

@@ -48,6 +48,8 @@ SIGNATURES = {
     "gbrt_bvh_get_bound": (_I, [_VP, ctypes.POINTER(ctypes.c_float)]),
     "gbrt_bvh_get_info": (_I, [_VP, ctypes.POINTER(BvhInfo)]),
     "gbrt_bvh_export": (_I, [_VP, _VP, ctypes.c_size_t, _VP, ctypes.c_size_t, _VP, ctypes.c_size_t]),
+    "gbrt_bvh_build_static": (_I, [_VP, _U32, _VP, _U32, ctypes.POINTER(BuildParams), _VP, ctypes.c_size_t, _VP,
+                                   ctypes.c_size_t, _VP, ctypes.c_size_t, ctypes.POINTER(ctypes.c_float), _VP]),
     "gbrt_trace_closest": (_I, [_VP, _VP, _U32, _VP, _VP]),
     "gbrt_trace_shadow": (_I, [_VP, _VP, _U32, _VP, _VP]),
     "gbrt_trace_closest_host": (_I, [_VP, _VP, _U32, _VP]),
