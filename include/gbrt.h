@@ -167,6 +167,103 @@ int gbrt_trace_shadow(const gbrt_bvh *bvh, const gbrt_ray *rays_dev, uint32_t n,
 int gbrt_trace_closest_host(const gbrt_bvh *bvh, const gbrt_ray *rays, uint32_t n, gbrt_hit *hits);
 int gbrt_trace_shadow_host(const gbrt_bvh *bvh, const gbrt_ray *rays, uint32_t n, int32_t *occluder);
 
+
+/* ---- wavefront path tracer (the `pathtracing` integrator) ---------------
+ * Replaces PathIntegrator::integrate and MonteCarloIntegrator's light
+ * estimation (src/integrator/surface/integrator_path_tracer.cc:138-314,
+ * integrator_montecarlo.cc:92-440) run per pixel sample by
+ * TiledIntegrator::renderTile (integrator_tiled.cc:253-395), with the film
+ * accumulation of ImageFilm::addSample for a box filter of width 1
+ * (imagefilm.cc:771-822). */
+
+enum {
+	GBRT_MAT_SHINYDIFFUSE = 0,   /* "shinydiffusemat": color, params[0] = diffuse_reflect (0 -> 1) */
+	GBRT_MAT_LIGHT = 1,          /* "light_mat": color, power, params[0] = double_sided (0/1) */
+	GBRT_MAT_GLOSSY = 2,         /* "glossy" (not yet supported by gbrt_scene_create) */
+	GBRT_MAT_ROUGH_GLASS = 3,    /* "rough_glass" (not yet supported) */
+	GBRT_MAT_GLASS = 4           /* "glass" (not yet supported) */
+};
+enum { GBRT_LIGHT_AREA = 0, GBRT_LIGHT_POINT = 1 };
+enum { GBRT_PT_FP64_FILM = 1 };
+
+typedef struct gbrt_material_desc {
+	uint32_t type;
+	float color[3];
+	float color2[3];
+	float power;
+	float params[6];
+} gbrt_material_desc;
+
+/* "arealight": corner, point1, point2, color, power, samples
+ * (include/light/light_area.h:51-58). */
+typedef struct gbrt_light_desc {
+	uint32_t type;
+	float corner[3], point1[3], point2[3];
+	float color[3];
+	float power;
+	int32_t samples;
+} gbrt_light_desc;
+
+/* "perspective" camera: from, to, up (a point), resx, resy, focal
+ * (include/camera/camera.h, camera_perspective.h); aperture 0. */
+typedef struct gbrt_camera_desc {
+	float from[3], to[3], up[3];
+	int32_t resx, resy;
+	float focal;
+} gbrt_camera_desc;
+
+/* pathtracing / film parameters with the reference's names:
+ * AA_minsamples (spp, one pass), path_samples, bounces,
+ * russian_roulette_min_bounces, adv_base_sampling_offset. */
+typedef struct gbrt_pt_params {
+	int32_t spp;
+	int32_t path_samples;
+	int32_t bounces;
+	int32_t russian_roulette_min_bounces;
+	uint32_t base_sampling_offset;
+	uint32_t seed;              /* random stream of Russian roulette / light choice */
+	uint32_t flags;             /* GBRT_PT_FP64_FILM: accumulate in double */
+	uint32_t wave_paths;        /* paths per wavefront wave; 0 = 4 Mi */
+} gbrt_pt_params;
+
+typedef struct gbrt_pt_stats {
+	uint64_t camera_samples;
+	uint64_t extension_rays;    /* camera + path continuation rays traced */
+	uint64_t shadow_rays;       /* shadow rays traced */
+	float ms;                   /* device time of the render (CUDA events) */
+} gbrt_pt_stats;
+
+typedef struct gbrt_scene gbrt_scene;
+
+/* Scene for rendering over a built BVH (borrowed; must outlive the scene).
+ * vertices/faces are the host arrays the BVH was built from (geometric
+ * normals are taken from them); face_material[i] indexes `materials`. */
+int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_vertices,
+                      const uint32_t *faces, uint32_t n_faces, const int32_t *face_material,
+                      const gbrt_material_desc *materials, uint32_t n_materials,
+                      const gbrt_light_desc *lights, uint32_t n_lights, gbrt_scene **out);
+int gbrt_scene_destroy(gbrt_scene *scene);
+
+/* Renders spp samples per pixel and ADDS each pixel's sample sum (RGB,
+ * resx*resy*3, row-major from the top-left) to film_dev (float) or
+ * film64_dev (double, when not NULL).  Asynchronous on `stream` unless
+ * `stats` is given (then it synchronises to read the ray counts). */
+int gbrt_pt_render(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params,
+                   float *film_dev, double *film64_dev, gbrt_pt_stats *stats, void *stream);
+
+/* Same into a host image of per-pixel means (sum / spp), resx*resy*3 floats. */
+int gbrt_pt_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params,
+                        float *image_out, gbrt_pt_stats *stats);
+
+/* Diagnostics: evaluates one of the path tracer's sampling primitives on n
+ * inputs, on the device (on_device != 0) or with the host build of the same
+ * code.  kind: 0 Halton::lowDiscrepancySampling(dim, x) (halton.cc:419-439),
+ * 1 sample::riVdC, 2 riLp, 3 riS, 4 fnv32ABuf (sample.h:100-148), 5/6
+ * Halton base 2/3 radical inverse of x (halton.h:59-85), 7 FAST_TRIG
+ * math::sin (dim 0) or math::cos (dim 1) of the float with bits x
+ * (math.h:228-265). */
+int gbrt_sampler_eval(int kind, int dim, const uint32_t *input, uint32_t n, double *out, int on_device);
+
 #ifdef __cplusplus
 }
 #endif

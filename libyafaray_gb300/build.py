@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbrt.so")
 
-SOURCES = ["capi.cu", "bvh_build.cu", "traverse.cu"]
+SOURCES = ["capi.cu", "bvh_build.cu", "traverse.cu", "pathtrace.cu"]
 EXACT_FP = {"traverse.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -34,7 +34,7 @@ def nvcc():
 
 def _compile(src):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
            "-I", os.path.join(ROOT, "include"), "-I", CSRC, "-c", os.path.join(CSRC, src), "-o", obj]
     if src in EXACT_FP:
         cmd.insert(1, "--fmad=false")

@@ -1,0 +1,971 @@
+// Wavefront path tracer: the `pathtracing` integrator's per-sample work
+// (PathIntegrator::integrate, src/integrator/surface/integrator_path_tracer.cc:138-314,
+// with MonteCarloIntegrator's light estimation, integrator_montecarlo.cc:92-440)
+// as a sequence of kernels over queues:
+//
+//   k_camera  camera rays (TiledIntegrator::renderTile sample positions,
+//             integrator_tiled.cc:296-325; PerspectiveCamera::shootRay,
+//             camera_perspective.cc:165-180)
+//   k_extend  closest hit of every queued ray (traverse_core.cuh)
+//   k_shade   one path vertex: emission, light estimation (shadow rays are
+//             appended to the shadow queue with their would-be contribution),
+//             Russian roulette and BSDF sampling of the continuation ray
+//             (appended to the next ray queue, warp-ballot compacted)
+//   k_shadow  any hit of every shadow ray; unoccluded ones add their
+//             contribution to the film (ImageFilm::addSample with a box
+//             filter of width 1, imagefilm.cc:771-822)
+//
+// The vertex logic, sample dimensions and weights follow the reference
+// line by line (cited at each step); quirks are kept, e.g. the first-bounce
+// vertex adds emission unconditionally, later vertices use the first-bounce
+// material's flags (integrator_path_tracer.cc:214-283), light sampling uses
+// an area of 1 (light_area.h:79) and the 0.99 pdf + 0.01 weight
+// (material_shiny_diffuse.cc:432).
+#include "traverse_core.cuh"
+#include "sampling.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+namespace {
+
+using gbrt::xa;
+using gbrt::xm;
+using gbrt::xs;
+
+// BsdfFlags subset (include/material/material.h), own bit assignment.
+enum : uint32_t {
+	BF_SPECULAR = 1u, BF_GLOSSY = 2u, BF_DIFFUSE = 4u, BF_DISPERSIVE = 8u, BF_REFLECT = 16u,
+	BF_TRANSMIT = 32u, BF_FILTER = 64u, BF_EMIT = 128u, BF_ALL = 255u
+};
+
+struct DevMaterial {
+	uint32_t type;
+	uint32_t flags;
+	float col[3];      // shinydiffuse diffuse colour x diffuse strength; light_mat colour x power
+	float extra[5];
+};
+
+struct DevLight {
+	float c[3], tx[3], ty[3], nflip[3], col[3];   // area light (light_area.h:70-78)
+	float e1[3], e2[3], e3[3];                    // quad edges from the corner, for intersect
+	int samples;
+	float pad[2];
+};
+
+constexpr int kThreads = 128;
+constexpr uint32_t kDead = 0xFFFFFFFFu;
+constexpr float kRayMinDist = 0.00005f;   // Accelerator::min_raydist_ (accelerator.h:85)
+constexpr float kShadowBias = 0.0005f;    // Accelerator::shadow_bias_ (accelerator.h:86)
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kInvPi = 0.31830988618379067154f;
+
+struct Camera {
+	float from[3], vright[3], vup[3], vto[3];
+	int resx, resy;
+};
+
+struct Params {
+	int spp, path_samples, bounces, rr_min;
+	uint32_t base_offset, seed;
+	uint32_t wave_start, wave_n;
+	float d1;
+	uint32_t n_lights;
+	int fp64;
+};
+
+struct Work {
+	uint32_t *p_pixel, *p_si, *p_state;
+	float4 *p_thr;
+	float4 *q_ray[2];
+	uint32_t *q_path[2];
+	float4 *hits;
+	float4 *s_ray;
+	float4 *s_col;
+	uint32_t *s_pix;
+	uint32_t *count;            // [0],[1] ray queues, [2] shadow queue
+	unsigned long long *stats;  // [0] extension rays, [1] shadow rays traced
+};
+
+struct SceneDev {
+	gbrt::BvhView bv;
+	const float4 *prim_ng;      // geometric normal xyz, material index in w (bits)
+	const DevMaterial *mats;
+	const DevLight *lights;
+	gbrt::LdsTables lds;
+};
+
+__device__ __forceinline__ float dot3(const float a[3], const float b[3]) { return xa(xa(xm(a[0], b[0]), xm(a[1], b[1])), xm(a[2], b[2])); }
+
+__device__ __forceinline__ uint32_t hash32(uint32_t x)
+{
+	x ^= x >> 16; x *= 0x7feb352du;
+	x ^= x >> 15; x *= 0x846ca68bu;
+	x ^= x >> 16;
+	return x;
+}
+__device__ __forceinline__ float rng01(uint32_t a, uint32_t b, uint32_t c, uint32_t seed)
+{
+	const uint32_t h = hash32(a ^ hash32(b ^ hash32(c ^ hash32(seed))));
+	return static_cast<float>(h >> 8) * (1.f / 16777216.f);
+}
+
+// Vec3::createCoordsSystem (include/geometry/vector.h:399-420)
+__device__ __forceinline__ void coords_system(const float n[3], float u[3], float v[3])
+{
+	if(n[0] == 0.f && n[1] == 0.f)
+	{
+		u[0] = n[2] < 0.f ? -1.f : 1.f; u[1] = 0.f; u[2] = 0.f;
+		v[0] = 0.f; v[1] = 1.f; v[2] = 0.f;
+		return;
+	}
+	const float d = __fdiv_rn(1.f, sqrtf(xa(xm(n[1], n[1]), xm(n[0], n[0]))));
+	u[0] = xm(n[1], d); u[1] = xm(-n[0], d); u[2] = 0.f;
+	v[0] = xs(xm(n[1], u[2]), xm(n[2], u[1]));
+	v[1] = xs(xm(n[2], u[0]), xm(n[0], u[2]));
+	v[2] = xs(xm(n[0], u[1]), xm(n[1], u[0]));
+}
+
+// sample::cosHemisphere (include/sampler/sample.h:43-52) with FAST_TRIG.
+__device__ __forceinline__ void cos_hemisphere(const float n[3], const float u[3], const float v[3], float s1, float s2, float out[3])
+{
+	if(s1 >= 1.f) { out[0] = n[0]; out[1] = n[1]; out[2] = n[2]; return; }
+	const float z2 = xm(s2, 6.28318530717958647692f);
+	const float cz = gbrt::fast_cos(z2), sz = gbrt::fast_sin(z2);
+	const float a = sqrtf(xs(1.f, s1)), b = sqrtf(s1);
+	for(int k = 0; k < 3; ++k) out[k] = xa(xm(xa(xm(u[k], cz), xm(v[k], sz)), a), xm(n[k], b));
+}
+
+struct Surface {
+	float p[3], ng[3], n[3], u[3], v[3];
+	const DevMaterial *m;
+};
+
+// SurfacePoint::normalFaceForward (include/geometry/surface.h:202-205)
+__device__ __forceinline__ void face_forward(const Surface &s, const float wo[3], float out[3])
+{
+	const bool flip = dot3(s.ng, wo) < 0.f;
+	for(int k = 0; k < 3; ++k) out[k] = flip ? -s.n[k] : s.n[k];
+}
+
+// ShinyDiffuseMaterial::eval, diffuse component (material_shiny_diffuse.cc:297-337).
+__device__ __forceinline__ void mat_eval(const Surface &s, const float wo[3], const float wl[3], float out[3])
+{
+	out[0] = out[1] = out[2] = 0.f;
+	if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return;
+	float n[3];
+	face_forward(s, wo, n);
+	if(dot3(n, wl) < 0.f) return;
+	for(int k = 0; k < 3; ++k) out[k] = s.m->col[k];
+}
+
+// ShinyDiffuseMaterial::pdf (material_shiny_diffuse.cc:443-484), lambertian part.
+__device__ __forceinline__ float mat_pdf(const Surface &s, const float wo[3], const float wi[3])
+{
+	if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return 0.f;
+	float n[3];
+	face_forward(s, wo, n);
+	return fabsf(dot3(wi, n));
+}
+
+// ShinyDiffuseMaterial::sample (material_shiny_diffuse.cc:346-440), diffuse
+// reflection branch; light_mat returns pdf 0 (material_light.cc:75-80).
+__device__ __forceinline__ bool mat_sample(const Surface &s, const float wo[3], float s1, float s2, uint32_t req_flags,
+                                           float wi[3], float col[3], float &w, float &pdf, uint32_t &sampled)
+{
+	col[0] = col[1] = col[2] = 0.f;
+	w = 0.f; pdf = 0.f; sampled = 0u;
+	if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return false;
+	const uint32_t cflags = BF_DIFFUSE | BF_REFLECT;
+	if((req_flags & cflags) != cflags) return false;
+	float n[3];
+	face_forward(s, wo, n);
+	cos_hemisphere(n, s.u, s.v, s1, s2, wi);
+	const float cos_ng_wo = dot3(s.ng, wo);
+	if(xm(cos_ng_wo, dot3(s.ng, wi)) > 0.f)
+		for(int k = 0; k < 3; ++k) col[k] = s.m->col[k];
+	pdf = fabsf(dot3(wi, n));
+	w = __fdiv_rn(fabsf(dot3(wi, s.n)), xa(xm(pdf, 0.99f), 0.01f));
+	sampled = cflags;
+	return true;
+}
+
+// LightMaterial::emit (material_light.cc:82-87)
+__device__ __forceinline__ bool mat_emit(const Surface &s, const float wo[3], float out[3])
+{
+	if(s.m->type != GBRT_MAT_LIGHT) return false;
+	if(dot3(wo, s.n) <= 0.f && !(s.m->extra[0] > 0.5f)) return false;
+	for(int k = 0; k < 3; ++k) out[k] = s.m->col[k];
+	return true;
+}
+
+__device__ __forceinline__ void film_add(float *film, double *film64, uint32_t pixel, float r, float g, float b)
+{
+	if(film64)
+	{
+		atomicAdd(film64 + 3ull * pixel, static_cast<double>(r));
+		atomicAdd(film64 + 3ull * pixel + 1, static_cast<double>(g));
+		atomicAdd(film64 + 3ull * pixel + 2, static_cast<double>(b));
+	}
+	else
+	{
+		atomicAdd(film + 3ull * pixel, r);
+		atomicAdd(film + 3ull * pixel + 1, g);
+		atomicAdd(film + 3ull * pixel + 2, b);
+	}
+}
+
+// Writes a lane's reserved run of shadow-queue slots; unused slots are
+// marked dead so the shadow kernel skips them.
+struct ShadowWriter {
+	float4 *ray;
+	float4 *col;
+	uint32_t *pix;
+	uint32_t slot, end;
+	__device__ void put(const float o[3], float tmin, const float d[3], float tmax, uint32_t pixel, const float c[3])
+	{
+		if(slot >= end) return;
+		ray[2ull * slot] = make_float4(o[0], o[1], o[2], tmin);
+		ray[2ull * slot + 1] = make_float4(d[0], d[1], d[2], tmax);
+		col[slot] = make_float4(c[0], c[1], c[2], 0.f);
+		pix[slot] = pixel;
+		++slot;
+	}
+	__device__ void close()
+	{
+		for(; slot < end; ++slot) pix[slot] = kDead;
+	}
+};
+
+// MonteCarloIntegrator::doLightEstimation for an area light
+// (integrator_montecarlo.cc:417-440): num_samples light samples
+// (areaLightSampleLight, :192-330) and num_samples BSDF samples that hit the
+// light (areaLightSampleMaterial, :332-415), power-heuristic MIS, Halton
+// bases 2/3 from offs = num_samples * sample + pixel offset + loffs * 4567.
+__device__ void light_estimation(const SceneDev &sc, const Surface &s, const float wo[3], uint32_t li, uint32_t loffs,
+                                 uint32_t sample_, uint32_t offset_, const float weight[3], uint32_t pixel, ShadowWriter &sw)
+{
+	const DevLight &L = sc.lights[li];
+	const int ns = L.samples;
+	const float inv_ns = __fdiv_rn(1.f, static_cast<float>(ns));
+	const uint32_t offs = static_cast<uint32_t>(ns) * sample_ + offset_ + loffs * 4567u;
+	const float plen = sqrtf(dot3(s.p, s.p));
+	const float sbias = xm(kShadowBias, fmaxf(1.f, plen));
+	const float rbias = xm(kRayMinDist, fmaxf(1.f, plen));
+	for(int i = 0; i < ns; ++i)
+	{
+		const float s1 = gbrt::radical_inverse(offs + static_cast<uint32_t>(i), 2);
+		const float s2 = gbrt::radical_inverse(offs + static_cast<uint32_t>(i), 3);
+		// light sample (AreaLight::illumSample, light_area.cc:99-124)
+		{
+			float lp[3], ldir[3];
+			for(int k = 0; k < 3; ++k) lp[k] = xa(xa(L.c[k], xm(s1, L.tx[k])), xm(s2, L.ty[k]));
+			for(int k = 0; k < 3; ++k) ldir[k] = xs(lp[k], s.p[k]);
+			const float dist_sqr = dot3(ldir, ldir);
+			const float dist = sqrtf(dist_sqr);
+			if(dist > 0.f)
+			{
+				const float invd = __fdiv_rn(1.f, dist);
+				for(int k = 0; k < 3; ++k) ldir[k] = xm(ldir[k], invd);
+				const float cos_angle = dot3(ldir, L.nflip);
+				if(cos_angle > 0.f)
+				{
+					const float pdf = __fdiv_rn(xm(dist_sqr, kPi), xm(1.f, cos_angle));
+					if(pdf > 1e-6f)
+					{
+						float surf[3];
+						mat_eval(s, wo, ldir, surf);
+						const float angle = fabsf(dot3(s.n, ldir));
+						float w = 1.f;
+						const float m_pdf = mat_pdf(s, wo, ldir);
+						if(m_pdf > 1e-6f)
+						{
+							const float l2 = xm(pdf, pdf), m2 = xm(m_pdf, m_pdf);
+							w = __fdiv_rn(l2, xa(l2, m2));
+						}
+						float c[3];
+						for(int k = 0; k < 3; ++k)
+							c[k] = xm(xm(__fdiv_rn(xm(xm(xm(surf[k], L.col[k]), angle), w), pdf), inv_ns), weight[k]);
+						if(c[0] != 0.f || c[1] != 0.f || c[2] != 0.f) sw.put(s.p, sbias, ldir, dist, pixel, c);
+					}
+				}
+			}
+		}
+		// BSDF sample towards the light (Material::sample + AreaLight::intersect, light_area.cc:146-155)
+		{
+			float wi[3], scol[3], W, spdf;
+			uint32_t sflags;
+			mat_sample(s, wo, s1, s2, BF_GLOSSY | BF_DIFFUSE | BF_DISPERSIVE | BF_REFLECT | BF_TRANSMIT, wi, scol, W, spdf, sflags);
+			const float cos_angle = dot3(wi, L.nflip);
+			if(cos_angle > 0.f && spdf > 1e-6f)
+			{
+				const float4 A = make_float4(L.c[0], L.c[1], L.c[2], L.e3[0]);
+				const float4 B = make_float4(L.e1[0], L.e1[1], L.e1[2], L.e3[1]);
+				const float4 C = make_float4(L.e2[0], L.e2[1], L.e2[2], L.e3[2]);
+				float u, v;
+				const float t = gbrt::mt_intersect(A, B, C, true, s.p, wi, u, v);
+				if(t > 0.f)
+				{
+					const float ipdf = xm(xm(xm(__fdiv_rn(1.f, xm(t, t)), 1.f), cos_angle), kInvPi);
+					if(ipdf > 1e-6f)
+					{
+						const float l_pdf = __fdiv_rn(1.f, ipdf);
+						const float l2 = xm(l_pdf, l_pdf), m2 = xm(spdf, spdf);
+						const float w = __fdiv_rn(m2, xa(l2, m2));
+						float c[3];
+						for(int k = 0; k < 3; ++k) c[k] = xm(xm(xm(xm(xm(scol[k], L.col[k]), w), W), inv_ns), weight[k]);
+						if(c[0] != 0.f || c[1] != 0.f || c[2] != 0.f) sw.put(s.p, rbias, wi, t, pixel, c);
+					}
+				}
+			}
+		}
+	}
+}
+
+__device__ __forceinline__ uint32_t pixel_offset(uint32_t pixel, int resx)
+{
+	const uint32_t x = pixel % static_cast<uint32_t>(resx), y = pixel / static_cast<uint32_t>(resx);
+	return gbrt::fnv32(y * gbrt::fnv32(x));      // integrator_tiled.cc:297
+}
+
+__global__ void __launch_bounds__(kThreads) k_camera(Camera cam, Params P, Work W)
+{
+	const uint32_t per_pixel = static_cast<uint32_t>(P.spp * P.path_samples);
+	for(uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < P.wave_n; s += gridDim.x * blockDim.x)
+	{
+		const uint32_t g = P.wave_start + s;
+		const uint32_t pixel = g / per_pixel, si = g % per_pixel;
+		const uint32_t sample = si / static_cast<uint32_t>(P.path_samples);
+		const uint32_t offset_ = pixel_offset(pixel, cam.resx);
+		float dx = 0.5f, dy = 0.5f;
+		if(P.spp > 1)
+		{
+			dx = xm(xa(0.5f, static_cast<float>(sample)), P.d1);
+			dy = gbrt::ri_lp(sample + offset_);
+		}
+		const float px = xa(static_cast<float>(pixel % static_cast<uint32_t>(cam.resx)), dx);
+		const float py = xa(static_cast<float>(pixel / static_cast<uint32_t>(cam.resx)), dy);
+		float d[3];
+		for(int k = 0; k < 3; ++k) d[k] = xa(xa(xm(cam.vright[k], px), xm(cam.vup[k], py)), cam.vto[k]);
+		const float l2 = dot3(d, d);
+		if(l2 != 0.f)
+		{
+			const float inv = __fdiv_rn(1.f, sqrtf(l2));
+			for(int k = 0; k < 3; ++k) d[k] = xm(d[k], inv);
+		}
+		W.p_pixel[s] = pixel;
+		W.p_si[s] = si;
+		W.p_thr[s] = make_float4(1.f, 1.f, 1.f, 0.f);
+		W.p_state[s] = 0u;
+		W.q_ray[0][2ull * s] = make_float4(cam.from[0], cam.from[1], cam.from[2], 0.f);
+		W.q_ray[0][2ull * s + 1] = make_float4(d[0], d[1], d[2], -1.f);
+		W.q_path[0][s] = s;
+	}
+	if(blockIdx.x == 0 && threadIdx.x == 0)
+	{
+		W.count[0] = P.wave_n;
+		atomicAdd(W.stats, static_cast<unsigned long long>(P.wave_n));
+	}
+}
+
+__global__ void __launch_bounds__(kThreads) k_extend(gbrt::BvhView bv, const float4 *__restrict__ rays, const uint32_t *__restrict__ count,
+                                                     float4 *__restrict__ hits)
+{
+	const uint32_t n = *count;
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	{
+		const float4 a = rays[2ull * i], b = rays[2ull * i + 1];
+		const gbrt::Hit h = gbrt::trace_ray<false>(bv, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w);
+		hits[i] = make_float4(__int_as_float(h.prim), h.t, h.u, h.v);
+	}
+}
+
+__global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work W, int cur, int resx, uint32_t shadow_cap,
+                                                    float *film, double *film64)
+{
+	const uint32_t n = W.count[cur];
+	const int nxt = cur ^ 1;
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t lt_mask = (1u << lane) - 1u;
+	for(uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x)
+	{
+		const uint32_t q = base + threadIdx.x;
+		const bool live = q < n;
+		bool cont = false;
+		float nray[8];
+		uint32_t path = 0, n_shadow = 0;
+		Surface s;
+		float wo[3] = {0.f, 0.f, 0.f}, thr[3] = {0.f, 0.f, 0.f};
+		uint32_t pixel = 0, sample_ = 0, offset_ = 0, sub = 0, k = 0, mat1 = 0, caustic = 0;
+		bool hit = false;
+		if(live)
+		{
+			path = W.q_path[cur][q];
+			const float4 h = W.hits[q];
+			const int32_t prim = __float_as_int(h.x);
+			if(prim >= 0)
+			{
+				hit = true;
+				const float4 ra = W.q_ray[cur][2ull * q], rb = W.q_ray[cur][2ull * q + 1];
+				const float dir[3] = {rb.x, rb.y, rb.z};
+				s.p[0] = xa(ra.x, xm(h.y, dir[0])); s.p[1] = xa(ra.y, xm(h.y, dir[1])); s.p[2] = xa(ra.z, xm(h.y, dir[2]));
+				const float4 ng = __ldg(sc.prim_ng + prim);
+				s.ng[0] = ng.x; s.ng[1] = ng.y; s.ng[2] = ng.z;
+				s.n[0] = ng.x; s.n[1] = ng.y; s.n[2] = ng.z;
+				s.m = sc.mats + __float_as_uint(ng.w);
+				coords_system(s.n, s.u, s.v);
+				wo[0] = -dir[0]; wo[1] = -dir[1]; wo[2] = -dir[2];
+				pixel = W.p_pixel[path];
+				const uint32_t si = W.p_si[path];
+				sub = si % static_cast<uint32_t>(P.path_samples);
+				sample_ = P.base_offset + si / static_cast<uint32_t>(P.path_samples);
+				offset_ = pixel_offset(pixel, resx);
+				const uint32_t st = W.p_state[path];
+				k = st & 0xffu; mat1 = (st >> 8) & 0xffu; caustic = (st >> 16) & 1u;
+				const float4 t4 = W.p_thr[path];
+				thr[0] = t4.x; thr[1] = t4.y; thr[2] = t4.z;
+			}
+		}
+		// --- decide this vertex's work, count its shadow rays -----------------
+		bool do_nee_all = false, do_nee_one = false, rr_dead = false;
+		float nee_weight[3] = {0.f, 0.f, 0.f};
+		uint32_t nee_light = 0;
+		if(hit)
+		{
+			if(k == 0)
+			{
+				float e[3];
+				if((s.m->flags & BF_EMIT) && sub == 0 && mat_emit(s, wo, e)) film_add(film, film64, pixel, e[0], e[1], e[2]);
+				do_nee_all = (s.m->flags & BF_DIFFUSE) && sub == 0;
+				nee_weight[0] = nee_weight[1] = nee_weight[2] = 1.f;
+				if(do_nee_all)
+					for(uint32_t l = 0; l < P.n_lights; ++l) n_shadow += 2u * static_cast<uint32_t>(sc.lights[l].samples);
+			}
+			else
+			{
+				if(k == 1) mat1 = s.m->flags;
+				if(k >= 2 && static_cast<int>(k) - 1 > P.rr_min)   // integrator_path_tracer.cc:267-273
+				{
+					const float r = rng01(pixel, sample_ * 64u + sub, k, P.seed);
+					const float prob = fmaxf(thr[0], fmaxf(thr[1], thr[2]));
+					if(prob <= 0.f || prob < r) rr_dead = true;
+					else { const float ip = __fdiv_rn(1.f, prob); for(int c = 0; c < 3; ++c) thr[c] = xm(thr[c], ip); }
+				}
+				if(!rr_dead)
+				{
+					do_nee_one = P.n_lights > 0 && (k == 1 || (mat1 & BF_DIFFUSE));
+					if(do_nee_one)
+					{
+						const float r = rng01(pixel, sample_ * 64u + sub, k, P.seed ^ 0x9e3779b9u);
+						nee_light = min(static_cast<uint32_t>(r * static_cast<float>(P.n_lights)), P.n_lights - 1u);
+						for(int c = 0; c < 3; ++c) nee_weight[c] = xm(thr[c], static_cast<float>(P.n_lights));
+						n_shadow = 2u * static_cast<uint32_t>(sc.lights[nee_light].samples);
+					}
+					float e[3];
+					if((k == 1 && (s.m->flags & BF_EMIT)) || (k >= 2 && (mat1 & BF_EMIT) && caustic))
+						if(mat_emit(s, wo, e)) film_add(film, film64, pixel, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
+				}
+			}
+		}
+		// --- reserve shadow-queue slots for the warp (prefix sum of counts) ---
+		uint32_t incl = n_shadow;
+		for(int off = 1; off < 32; off <<= 1)
+		{
+			const uint32_t v = __shfl_up_sync(0xffffffffu, incl, off);
+			if(lane >= static_cast<uint32_t>(off)) incl += v;
+		}
+		const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+		uint32_t wbase = 0;
+		if(lane == 31 && total) wbase = atomicAdd(W.count + 2, total);
+		wbase = __shfl_sync(0xffffffffu, wbase, 31);
+		ShadowWriter sw{W.s_ray, W.s_col, W.s_pix, wbase + incl - n_shadow, wbase + incl};
+		if(sw.end > shadow_cap) sw.end = sw.slot > shadow_cap ? sw.slot : shadow_cap;
+		if(do_nee_all)
+			for(uint32_t l = 0; l < P.n_lights; ++l) light_estimation(sc, s, wo, l, l, sample_, offset_, nee_weight, pixel, sw);
+		if(do_nee_one) light_estimation(sc, s, wo, nee_light, nee_light, sample_, offset_, nee_weight, pixel, sw);
+		sw.close();
+		// --- continuation ray ----------------------------------------------
+		if(hit && !rr_dead)
+		{
+			float s1 = -1.f, s2 = 0.f;
+			uint32_t req = BF_ALL;
+			if(k == 0)
+			{
+				if(s.m->flags & BF_DIFFUSE)    // path_flags = Diffuse (integrator_path_tracer.cc:178-190)
+				{
+					const uint32_t offs = static_cast<uint32_t>(P.path_samples) * sample_ + offset_ + sub;
+					s1 = gbrt::ri_vdc(offs);
+					s2 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 2, offs));
+					req = BF_DIFFUSE | BF_REFLECT | BF_TRANSMIT;
+				}
+			}
+			else if(static_cast<int>(k) < P.bounces)
+			{
+				const uint32_t offs = static_cast<uint32_t>(P.path_samples) * sample_ + offset_ + sub;
+				const int d4 = 4 * static_cast<int>(k);
+				if(d4 + 4 < gbrt::kLdsDims)
+				{
+					s1 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d4 + 3, offs));
+					s2 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d4 + 4, offs));
+				}
+				else
+				{
+					s1 = rng01(pixel, sample_ * 64u + sub, 1000u + k, P.seed);
+					s2 = rng01(pixel, sample_ * 64u + sub, 2000u + k, P.seed);
+				}
+			}
+			if(s1 >= 0.f)
+			{
+				float wi[3], scol[3], w, pdf;
+				uint32_t sflags;
+				mat_sample(s, wo, s1, s2, req, wi, scol, w, pdf, sflags);
+				float nt[3];
+				for(int c = 0; c < 3; ++c) nt[c] = xm(thr[c], xm(scol[c], w));
+				if(k == 0)
+				{
+					const float inv_ps = __fdiv_rn(1.f, static_cast<float>(P.path_samples));
+					for(int c = 0; c < 3; ++c) nt[c] = xm(nt[c], inv_ps);
+				}
+				if(nt[0] != 0.f || nt[1] != 0.f || nt[2] != 0.f)
+				{
+					cont = true;
+					caustic = (sflags & (BF_SPECULAR | BF_GLOSSY | BF_FILTER)) ? 1u : 0u;
+					W.p_thr[path] = make_float4(nt[0], nt[1], nt[2], 0.f);
+					W.p_state[path] = (k + 1u) | (mat1 << 8) | (caustic << 16);
+					nray[0] = s.p[0]; nray[1] = s.p[1]; nray[2] = s.p[2]; nray[3] = kRayMinDist;
+					nray[4] = wi[0]; nray[5] = wi[1]; nray[6] = wi[2]; nray[7] = -1.f;
+				}
+			}
+		}
+		const uint32_t ballot = __ballot_sync(0xffffffffu, cont);
+		if(ballot)
+		{
+			uint32_t qbase = 0;
+			const uint32_t leader = __ffs(ballot) - 1u;
+			if(lane == leader) qbase = atomicAdd(W.count + nxt, static_cast<uint32_t>(__popc(ballot)));
+			qbase = __shfl_sync(0xffffffffu, qbase, leader);
+			if(cont)
+			{
+				const uint32_t slot = qbase + __popc(ballot & lt_mask);
+				W.q_ray[nxt][2ull * slot] = make_float4(nray[0], nray[1], nray[2], nray[3]);
+				W.q_ray[nxt][2ull * slot + 1] = make_float4(nray[4], nray[5], nray[6], nray[7]);
+				W.q_path[nxt][slot] = path;
+			}
+			if(lane == leader) atomicAdd(W.stats, static_cast<unsigned long long>(__popc(ballot)));
+		}
+	}
+}
+
+__global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Work W, uint32_t shadow_cap, float *film, double *film64)
+{
+	const uint32_t n = min(W.count[2], shadow_cap);
+	uint32_t traced = 0;
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	{
+		const uint32_t pixel = W.s_pix[i];
+		if(pixel == kDead) continue;
+		const float4 a = W.s_ray[2ull * i], b = W.s_ray[2ull * i + 1];
+		const gbrt::Hit h = gbrt::trace_ray<true>(bv, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w);
+		++traced;
+		if(h.prim < 0)
+		{
+			const float4 c = W.s_col[i];
+			film_add(film, film64, pixel, c.x, c.y, c.z);
+		}
+	}
+	for(int off = 16; off > 0; off >>= 1) traced += __shfl_xor_sync(0xffffffffu, traced, off);
+	if((threadIdx.x & 31u) == 0 && traced) atomicAdd(W.stats + 1, static_cast<unsigned long long>(traced));
+}
+
+__global__ void k_reset(uint32_t *count, int which) { count[which] = 0u; count[2] = 0u; }
+
+__global__ void k_mean(const float *sum, const double *sum64, float *out, size_t n, float inv)
+{
+	for(size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
+		out[i] = sum64 ? static_cast<float>(sum64[i] * static_cast<double>(inv)) : sum[i] * inv;
+}
+
+// kind: 0 lowDiscrepancySampling(dim, x), 1 riVdC, 2 riLp, 3 riS, 4 fnv32ABuf,
+// 5 radical inverse base 2, 6 radical inverse base 3, 7 FAST_TRIG sin and
+// cos of the float whose bits are x (sin in the value, cos via dim = 1).
+__host__ __device__ inline double sampler_value(const gbrt::LdsTables &t, int kind, int dim, uint32_t x)
+{
+	switch(kind)
+	{
+		case 0: return gbrt::low_discrepancy(t, dim, x);
+		case 1: return gbrt::ri_vdc(x);
+		case 2: return gbrt::ri_lp(x);
+		case 3: return gbrt::ri_s(x);
+		case 4: return static_cast<double>(gbrt::fnv32(x));
+		case 5: return gbrt::radical_inverse(x, 2);
+		case 6: return gbrt::radical_inverse(x, 3);
+		default:
+		{
+			float f;
+			memcpy(&f, &x, 4);
+			return dim == 1 ? gbrt::fast_cos(f) : gbrt::fast_sin(f);
+		}
+	}
+}
+
+__global__ void k_sampler(gbrt::LdsTables t, int kind, int dim, const uint32_t *in, uint32_t n, double *out)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n) out[i] = sampler_value(t, kind, dim, in[i]);
+}
+
+} // namespace
+
+struct gbrt_scene {
+	const gbrt_bvh *bvh = nullptr;
+	int device = 0;
+	int n_sm = 0;
+	uint32_t n_prims = 0, n_mats = 0, n_lights = 0;
+	float4 *prim_ng = nullptr;
+	DevMaterial *mats = nullptr;
+	DevLight *lights = nullptr;
+	uint16_t *lds_perm = nullptr;
+	uint32_t *lds_off = nullptr, *lds_base = nullptr;
+	double *lds_inv = nullptr;
+	// work buffers (grown on demand)
+	size_t cap_paths = 0, cap_shadow = 0;
+	void *work = nullptr;
+	Work w{};
+	std::mutex mu;
+};
+
+namespace {
+
+int alloc_work(gbrt_scene *S, size_t paths, size_t shadow)
+{
+	if(paths <= S->cap_paths && shadow <= S->cap_shadow) return GBRT_OK;
+	if(S->work) { cudaFree(S->work); S->work = nullptr; }
+	size_t off = 0;
+	auto carve = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
+	const size_t o_pix = carve(4 * paths), o_si = carve(4 * paths), o_st = carve(4 * paths), o_thr = carve(16 * paths);
+	const size_t o_qr0 = carve(32 * paths), o_qr1 = carve(32 * paths), o_qp0 = carve(4 * paths), o_qp1 = carve(4 * paths);
+	const size_t o_hit = carve(16 * paths);
+	const size_t o_sr = carve(32 * shadow), o_sc = carve(16 * shadow), o_sp = carve(4 * shadow);
+	const size_t o_cnt = carve(64), o_stats = carve(64);
+	cudaError_t e = cudaMalloc(&S->work, off);
+	if(e != cudaSuccess) { S->work = nullptr; S->cap_paths = S->cap_shadow = 0; return gbrt_set_error(GBRT_ERR_OOM, "path tracer work buffers (%zu bytes): %s", off, cudaGetErrorString(e)); }
+	char *b = static_cast<char *>(S->work);
+	Work &w = S->w;
+	w.p_pixel = reinterpret_cast<uint32_t *>(b + o_pix);
+	w.p_si = reinterpret_cast<uint32_t *>(b + o_si);
+	w.p_state = reinterpret_cast<uint32_t *>(b + o_st);
+	w.p_thr = reinterpret_cast<float4 *>(b + o_thr);
+	w.q_ray[0] = reinterpret_cast<float4 *>(b + o_qr0);
+	w.q_ray[1] = reinterpret_cast<float4 *>(b + o_qr1);
+	w.q_path[0] = reinterpret_cast<uint32_t *>(b + o_qp0);
+	w.q_path[1] = reinterpret_cast<uint32_t *>(b + o_qp1);
+	w.hits = reinterpret_cast<float4 *>(b + o_hit);
+	w.s_ray = reinterpret_cast<float4 *>(b + o_sr);
+	w.s_col = reinterpret_cast<float4 *>(b + o_sc);
+	w.s_pix = reinterpret_cast<uint32_t *>(b + o_sp);
+	w.count = reinterpret_cast<uint32_t *>(b + o_cnt);
+	w.stats = reinterpret_cast<unsigned long long *>(b + o_stats);
+	S->cap_paths = paths;
+	S->cap_shadow = shadow;
+	return GBRT_OK;
+}
+
+// Camera::Camera axes (camera.cc:96-103) and PerspectiveCamera::setAxis
+// (camera_perspective.cc:97-111), in float like the reference.
+Camera make_camera(const gbrt_camera_desc &c)
+{
+	auto sub = [](const float *a, const float *b, float *o) { for(int k = 0; k < 3; ++k) o[k] = a[k] - b[k]; };
+	auto cross = [](const float *a, const float *b, float *o) {
+		o[0] = a[1] * b[2] - a[2] * b[1]; o[1] = a[2] * b[0] - a[0] * b[2]; o[2] = a[0] * b[1] - a[1] * b[0];
+	};
+	auto normalize = [](float *v) {
+		const float l2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+		if(l2 != 0.f) { const float inv = 1.f / std::sqrt(l2); for(int k = 0; k < 3; ++k) v[k] *= inv; }
+	};
+	float cy[3], cz[3], cx[3];
+	sub(c.up, c.from, cy);
+	sub(c.to, c.from, cz);
+	cross(cz, cy, cx);
+	cross(cz, cx, cy);
+	normalize(cx); normalize(cy); normalize(cz);
+	const float aspect = 1.f * static_cast<float>(c.resy) / static_cast<float>(c.resx);
+	Camera cam{};
+	for(int k = 0; k < 3; ++k)
+	{
+		cam.from[k] = c.from[k];
+		cam.vright[k] = cx[k];
+		cam.vup[k] = aspect * cy[k];
+	}
+	for(int k = 0; k < 3; ++k) cam.vto[k] = (cz[k] * c.focal) - 0.5f * (cam.vup[k] + cam.vright[k]);
+	for(int k = 0; k < 3; ++k) { cam.vup[k] /= static_cast<float>(c.resy); cam.vright[k] /= static_cast<float>(c.resx); }
+	cam.resx = c.resx;
+	cam.resy = c.resy;
+	return cam;
+}
+
+unsigned grid_for(size_t n, int n_sm)
+{
+	const size_t want = (n + kThreads - 1) / kThreads;
+	const size_t cap = static_cast<size_t>(n_sm > 0 ? n_sm : 148) * 16;
+	return static_cast<unsigned>(std::max<size_t>(1, std::min(want, cap)));
+}
+
+} // namespace
+
+extern "C" {
+
+int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_vertices, const uint32_t *faces, uint32_t n_faces,
+                      const int32_t *face_material, const gbrt_material_desc *materials, uint32_t n_materials,
+                      const gbrt_light_desc *lights, uint32_t n_lights, gbrt_scene **out)
+{
+	if(!out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: out is NULL");
+	*out = nullptr;
+	if(!bvh || (n_faces && (!vertices || !faces || !face_material)) || (n_materials && !materials) || (n_lights && !lights))
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: NULL argument");
+	gbrt_bvh_info info{};
+	if(int rc = gbrt_bvh_get_info(bvh, &info)) return rc;
+	if(info.n_prims != n_faces) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: %u faces but the BVH holds %u", n_faces, info.n_prims);
+	// materials
+	std::vector<DevMaterial> mats(n_materials);
+	for(uint32_t i = 0; i < n_materials; ++i)
+	{
+		const gbrt_material_desc &m = materials[i];
+		DevMaterial &d = mats[i];
+		std::memset(&d, 0, sizeof(d));
+		d.type = m.type;
+		if(m.type == GBRT_MAT_SHINYDIFFUSE)
+		{
+			const float strength = m.params[0] > 0.f ? m.params[0] : 1.f;   // diffuse_reflect
+			d.flags = strength * 1.f > 0.00001f ? (BF_DIFFUSE | BF_REFLECT) : 0u;
+			for(int k = 0; k < 3; ++k) d.col[k] = m.color[k] * strength;
+		}
+		else if(m.type == GBRT_MAT_LIGHT)
+		{
+			d.flags = BF_EMIT;
+			for(int k = 0; k < 3; ++k) d.col[k] = m.color[k] * m.power;    // light_col_ = color * power
+			d.extra[0] = m.params[0];                                      // double_sided
+		}
+		else return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: material %u has unsupported type %u", i, m.type);
+	}
+	// lights
+	std::vector<DevLight> ls(n_lights);
+	for(uint32_t i = 0; i < n_lights; ++i)
+	{
+		const gbrt_light_desc &L = lights[i];
+		if(L.type != GBRT_LIGHT_AREA) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: light %u has unsupported type %u", i, L.type);
+		if(L.samples < 1) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: light %u has %d samples", i, L.samples);
+		DevLight &d = ls[i];
+		std::memset(&d, 0, sizeof(d));
+		float tx[3], ty[3];
+		for(int k = 0; k < 3; ++k) { d.c[k] = L.corner[k]; tx[k] = L.point1[k] - L.corner[k]; ty[k] = L.point2[k] - L.corner[k]; }
+		for(int k = 0; k < 3; ++k) { d.tx[k] = tx[k]; d.ty[k] = ty[k]; }
+		// normal_flipped_ = (point2 - corner) ^ (point1 - corner), not normalised (light_area.h:75)
+		d.nflip[0] = ty[1] * tx[2] - ty[2] * tx[1];
+		d.nflip[1] = ty[2] * tx[0] - ty[0] * tx[2];
+		d.nflip[2] = ty[0] * tx[1] - ty[1] * tx[0];
+		for(int k = 0; k < 3; ++k) d.col[k] = L.color[k] * L.power * 3.14159265358979323846f;   // light_area.h:78
+		// area_quad_ = {corner, point1, point1 + point2 - corner, point2} (light_area.h:72)
+		for(int k = 0; k < 3; ++k)
+		{
+			const float v2 = (L.point1[k] + L.point2[k]) - L.corner[k];
+			d.e1[k] = L.point1[k] - L.corner[k];
+			d.e2[k] = v2 - L.corner[k];
+			d.e3[k] = L.point2[k] - L.corner[k];
+		}
+		d.samples = L.samples;
+	}
+	// per-primitive geometric normal ((v1-v0) ^ (v2-v0)).normalize(), shape_polygon.h:58-62
+	std::vector<float4> ng(n_faces ? n_faces : 1);
+	for(uint32_t i = 0; i < n_faces; ++i)
+	{
+		const uint32_t *f = faces + 4ull * i;
+		for(int k = 0; k < 3; ++k)
+			if(f[k] >= n_vertices) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: face %u references vertex %u >= %u", i, f[k], n_vertices);
+		if(face_material[i] < 0 || static_cast<uint32_t>(face_material[i]) >= n_materials)
+			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: face %u has material %d of %u", i, face_material[i], n_materials);
+		const float *v0 = vertices + 3ull * f[0], *v1 = vertices + 3ull * f[1], *v2 = vertices + 3ull * f[2];
+		const float a[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
+		const float b[3] = {v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2]};
+		float n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+		const float l2 = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+		if(l2 != 0.f) { const float inv = 1.f / std::sqrt(l2); for(int k = 0; k < 3; ++k) n[k] *= inv; }
+		uint32_t mi = static_cast<uint32_t>(face_material[i]);
+		float w;
+		std::memcpy(&w, &mi, 4);
+		ng[i] = make_float4(n[0], n[1], n[2], w);
+	}
+	gbrt_scene *S = new gbrt_scene();
+	S->bvh = bvh;
+	S->n_prims = n_faces; S->n_mats = n_materials; S->n_lights = n_lights;
+	auto fail = [&](int rc) { gbrt_scene_destroy(S); return rc; };
+	cudaError_t e;
+	if((e = cudaGetDevice(&S->device)) != cudaSuccess) return fail(gbrt_set_error(GBRT_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e)));
+	cudaDeviceGetAttribute(&S->n_sm, cudaDevAttrMultiProcessorCount, S->device);
+	const auto T = gbrt::make_lds_tables();
+	struct Up { void **dst; const void *src; size_t bytes; };
+	const Up ups[] = {
+		{reinterpret_cast<void **>(&S->prim_ng), ng.data(), ng.size() * sizeof(float4)},
+		{reinterpret_cast<void **>(&S->mats), mats.data(), std::max<size_t>(1, mats.size()) * sizeof(DevMaterial)},
+		{reinterpret_cast<void **>(&S->lights), ls.data(), std::max<size_t>(1, ls.size()) * sizeof(DevLight)},
+		{reinterpret_cast<void **>(&S->lds_perm), T.perm.data(), T.perm.size() * sizeof(uint16_t)},
+		{reinterpret_cast<void **>(&S->lds_off), T.offset.data(), T.offset.size() * sizeof(uint32_t)},
+		{reinterpret_cast<void **>(&S->lds_base), T.base.data(), T.base.size() * sizeof(uint32_t)},
+		{reinterpret_cast<void **>(&S->lds_inv), T.inv.data(), T.inv.size() * sizeof(double)},
+	};
+	for(const Up &u : ups)
+	{
+		if((e = cudaMalloc(u.dst, u.bytes)) != cudaSuccess) return fail(gbrt_set_error(GBRT_ERR_OOM, "gbrt_scene_create: %s", cudaGetErrorString(e)));
+		const size_t src_bytes = u.bytes;
+		if(u.src && (e = cudaMemcpy(*u.dst, u.src, src_bytes, cudaMemcpyHostToDevice)) != cudaSuccess)
+			return fail(gbrt_set_error(GBRT_ERR_CUDA, "gbrt_scene_create: %s", cudaGetErrorString(e)));
+	}
+	*out = S;
+	return GBRT_OK;
+}
+
+int gbrt_scene_destroy(gbrt_scene *S)
+{
+	if(!S) return GBRT_OK;
+	void *ptrs[] = {S->prim_ng, S->mats, S->lights, S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->work};
+	for(void *p : ptrs) if(p) cudaFree(p);
+	delete S;
+	return GBRT_OK;
+}
+
+int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, float *film_dev, double *film64_dev,
+                   gbrt_pt_stats *stats, void *stream)
+{
+	if(!S || !camera || !params) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: NULL argument");
+	if(!film_dev && !film64_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: no film buffer");
+	const gbrt_pt_params &pp = *params;
+	if(camera->resx <= 0 || camera->resy <= 0 || pp.spp <= 0 || pp.path_samples <= 0 || pp.bounces < 0 || pp.path_samples > 64)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: bad resolution or sampling parameters");
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	std::lock_guard<std::mutex> lock(S->mu);
+	const uint64_t total = static_cast<uint64_t>(camera->resx) * camera->resy * pp.spp * pp.path_samples;
+	if(total >= (1ull << 32)) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_pt_render: %llu paths exceed 2^32", static_cast<unsigned long long>(total));
+	const uint64_t wave = std::min<uint64_t>(total, pp.wave_paths ? pp.wave_paths : (1ull << 22));
+	uint32_t max_shadow = 0;
+	{
+		std::vector<DevLight> ls(S->n_lights);
+		if(S->n_lights) GBRT_CK(cudaMemcpy(ls.data(), S->lights, ls.size() * sizeof(DevLight), cudaMemcpyDeviceToHost));
+		uint32_t all = 0, one = 0;
+		for(const auto &l : ls) { all += 2u * l.samples; one = std::max(one, 2u * static_cast<uint32_t>(l.samples)); }
+		max_shadow = std::max(all, one);
+	}
+	const size_t shadow_cap = std::max<size_t>(1, wave * max_shadow);
+	if(int rc = alloc_work(S, wave, shadow_cap)) return rc;
+	Camera cam = make_camera(*camera);
+	SceneDev sc{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv}};
+	Params P{};
+	P.spp = pp.spp; P.path_samples = pp.path_samples; P.bounces = pp.bounces; P.rr_min = pp.russian_roulette_min_bounces;
+	P.base_offset = pp.base_sampling_offset; P.seed = pp.seed;
+	P.d1 = 1.f / static_cast<float>(pp.spp);
+	P.n_lights = S->n_lights;
+	float *film = film64_dev ? nullptr : film_dev;
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	if(stats)
+	{
+		GBRT_CK(cudaEventCreate(&e0)); GBRT_CK(cudaEventCreate(&e1));
+		GBRT_CK(cudaEventRecord(e0, s));
+	}
+	GBRT_CK(cudaMemsetAsync(S->w.stats, 0, 2 * sizeof(unsigned long long), s));
+	for(uint64_t start = 0; start < total; start += wave)
+	{
+		P.wave_start = static_cast<uint32_t>(start);
+		P.wave_n = static_cast<uint32_t>(std::min<uint64_t>(wave, total - start));
+		k_camera<<<grid_for(P.wave_n, S->n_sm), kThreads, 0, s>>>(cam, P, S->w);
+		int cur = 0;
+		for(int vtx = 0; vtx <= pp.bounces; ++vtx)
+		{
+			k_reset<<<1, 1, 0, s>>>(S->w.count, cur ^ 1);
+			k_extend<<<grid_for(P.wave_n, S->n_sm), kThreads, 0, s>>>(sc.bv, S->w.q_ray[cur], S->w.count + cur, S->w.hits);
+			k_shade<<<grid_for(P.wave_n, S->n_sm), kThreads, 0, s>>>(sc, P, S->w, cur, camera->resx, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+			k_shadow<<<grid_for(shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, S->w, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+			cur ^= 1;
+		}
+	}
+	GBRT_CK(cudaGetLastError());
+	if(stats)
+	{
+		GBRT_CK(cudaEventRecord(e1, s));
+		unsigned long long st[2];
+		GBRT_CK(cudaMemcpyAsync(st, S->w.stats, sizeof(st), cudaMemcpyDeviceToHost, s));
+		GBRT_CK(cudaStreamSynchronize(s));
+		float ms = 0.f;
+		cudaEventElapsedTime(&ms, e0, e1);
+		cudaEventDestroy(e0); cudaEventDestroy(e1);
+		stats->camera_samples = total / pp.path_samples;
+		stats->extension_rays = st[0];
+		stats->shadow_rays = st[1];
+		stats->ms = ms;
+	}
+	return GBRT_OK;
+}
+
+int gbrt_pt_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, float *image_out, gbrt_pt_stats *stats)
+{
+	if(!S || !camera || !params || !image_out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_host: NULL argument");
+	const size_t n = 3ull * camera->resx * camera->resy;
+	const bool fp64 = (params->flags & GBRT_PT_FP64_FILM) != 0;
+	void *sum = nullptr, *mean = nullptr;
+	GBRT_CK(cudaMalloc(&sum, n * (fp64 ? 8 : 4)));
+	cudaError_t e = cudaMalloc(&mean, n * 4);
+	if(e != cudaSuccess) { cudaFree(sum); return gbrt_set_error(GBRT_ERR_OOM, "gbrt_pt_render_host: %s", cudaGetErrorString(e)); }
+	int rc = GBRT_OK;
+	if((e = cudaMemset(sum, 0, n * (fp64 ? 8 : 4))) != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+	if(!rc) rc = gbrt_pt_render(S, camera, params, fp64 ? nullptr : static_cast<float *>(sum), fp64 ? static_cast<double *>(sum) : nullptr, stats, nullptr);
+	if(!rc)
+	{
+		k_mean<<<grid_for(n, S->n_sm), kThreads>>>(fp64 ? nullptr : static_cast<float *>(sum), fp64 ? static_cast<double *>(sum) : nullptr,
+		                                           static_cast<float *>(mean), n, 1.f / static_cast<float>(params->spp));
+		if((e = cudaMemcpy(image_out, mean, n * 4, cudaMemcpyDeviceToHost)) != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "copy: %s", cudaGetErrorString(e));
+	}
+	cudaFree(sum);
+	cudaFree(mean);
+	return rc;
+}
+
+// Diagnostics: evaluates one sampling primitive on n inputs, on the device
+// (on_device != 0) or with the host build of the same code.
+int gbrt_sampler_eval(int kind, int dim, const uint32_t *input, uint32_t n, double *out, int on_device)
+{
+	if(!input || !out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_sampler_eval: NULL buffer");
+	if(kind < 0 || kind > 7 || (kind == 0 && (dim < 1 || dim >= gbrt::kLdsDims)))
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_sampler_eval: bad kind %d / dim %d", kind, dim);
+	const auto T = gbrt::make_lds_tables();
+	if(!on_device)
+	{
+		const gbrt::LdsTables t{T.perm.data(), T.offset.data(), T.base.data(), T.inv.data()};
+		for(uint32_t i = 0; i < n; ++i) out[i] = sampler_value(t, kind, dim, input[i]);
+		return GBRT_OK;
+	}
+	if(n == 0) return GBRT_OK;
+	void *d_perm = nullptr, *d_off = nullptr, *d_base = nullptr, *d_inv = nullptr, *d_in = nullptr, *d_out = nullptr;
+	int rc = GBRT_OK;
+	cudaError_t e = cudaSuccess;
+	struct Up { void **dst; const void *src; size_t bytes; };
+	const Up ups[] = {{&d_perm, T.perm.data(), T.perm.size() * 2}, {&d_off, T.offset.data(), T.offset.size() * 4},
+	                  {&d_base, T.base.data(), T.base.size() * 4}, {&d_inv, T.inv.data(), T.inv.size() * 8},
+	                  {&d_in, input, 4ull * n}, {&d_out, nullptr, 8ull * n}};
+	for(const Up &u : ups)
+	{
+		if(e == cudaSuccess) e = cudaMalloc(u.dst, u.bytes);
+		if(e == cudaSuccess && u.src) e = cudaMemcpy(*u.dst, u.src, u.bytes, cudaMemcpyHostToDevice);
+	}
+	if(e == cudaSuccess)
+	{
+		const gbrt::LdsTables t{static_cast<uint16_t *>(d_perm), static_cast<uint32_t *>(d_off), static_cast<uint32_t *>(d_base), static_cast<double *>(d_inv)};
+		k_sampler<<<(n + 127) / 128, 128>>>(t, kind, dim, static_cast<const uint32_t *>(d_in), n, static_cast<double *>(d_out));
+		e = cudaGetLastError();
+		if(e == cudaSuccess) e = cudaMemcpy(out, d_out, 8ull * n, cudaMemcpyDeviceToHost);
+	}
+	if(e != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "gbrt_sampler_eval: %s", cudaGetErrorString(e));
+	for(void *p : {d_perm, d_off, d_base, d_inv, d_in, d_out}) if(p) cudaFree(p);
+	return rc;
+}
+
+} // extern "C"

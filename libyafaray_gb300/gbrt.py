@@ -36,6 +36,36 @@ class BvhInfo(ctypes.Structure):
                 ("device_bytes", ctypes.c_uint64)]
 
 
+class MaterialDesc(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_uint32), ("color", ctypes.c_float * 3), ("color2", ctypes.c_float * 3),
+                ("power", ctypes.c_float), ("params", ctypes.c_float * 6)]
+
+
+class LightDesc(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_uint32), ("corner", ctypes.c_float * 3), ("point1", ctypes.c_float * 3),
+                ("point2", ctypes.c_float * 3), ("color", ctypes.c_float * 3), ("power", ctypes.c_float),
+                ("samples", ctypes.c_int32)]
+
+
+class CameraDesc(ctypes.Structure):
+    _fields_ = [("from_", ctypes.c_float * 3), ("to", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("resx", ctypes.c_int32), ("resy", ctypes.c_int32), ("focal", ctypes.c_float)]
+
+
+class PtParams(ctypes.Structure):
+    _fields_ = [("spp", ctypes.c_int32), ("path_samples", ctypes.c_int32), ("bounces", ctypes.c_int32),
+                ("russian_roulette_min_bounces", ctypes.c_int32), ("base_sampling_offset", ctypes.c_uint32),
+                ("seed", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("wave_paths", ctypes.c_uint32)]
+
+
+class PtStats(ctypes.Structure):
+    _fields_ = [("camera_samples", ctypes.c_uint64), ("extension_rays", ctypes.c_uint64),
+                ("shadow_rays", ctypes.c_uint64), ("ms", ctypes.c_float)]
+
+
+MAT_TYPES = {"shinydiffusemat": 0, "light_mat": 1, "glossy": 2, "rough_glass": 3, "glass": 4}
+PT_FP64_FILM = 1
+
 # Every symbol include/gbrt.h declares, with its ctypes signature.
 _VP, _U32, _I, _F = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_float
 SIGNATURES = {
@@ -54,6 +84,14 @@ SIGNATURES = {
     "gbrt_trace_shadow": (_I, [_VP, _VP, _U32, _VP, _VP]),
     "gbrt_trace_closest_host": (_I, [_VP, _VP, _U32, _VP]),
     "gbrt_trace_shadow_host": (_I, [_VP, _VP, _U32, _VP]),
+    "gbrt_scene_create": (_I, [_VP, _VP, _U32, _VP, _U32, _VP, ctypes.POINTER(MaterialDesc), _U32,
+                               ctypes.POINTER(LightDesc), _U32, ctypes.POINTER(_VP)]),
+    "gbrt_scene_destroy": (_I, [_VP]),
+    "gbrt_sampler_eval": (_I, [_I, _I, _VP, _U32, _VP, _I]),
+    "gbrt_pt_render": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP, _VP,
+                            ctypes.POINTER(PtStats), _VP]),
+    "gbrt_pt_render_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP,
+                                 ctypes.POINTER(PtStats)]),
 }
 
 _lib = None
@@ -167,3 +205,106 @@ class Bvh:
     def trace_shadow_device(self, rays_ptr, n, occ_ptr, stream=0):
         check(load().gbrt_trace_shadow(self._h, ctypes.c_void_p(rays_ptr), n, ctypes.c_void_p(occ_ptr),
                                        ctypes.c_void_p(stream)))
+
+
+def _material_desc(m):
+    d = MaterialDesc()
+    kind = m[0]
+    d.type = MAT_TYPES[kind]
+    if kind == "shinydiffusemat":
+        d.color[:] = [float(x) for x in m[1]]
+    elif kind == "light_mat":
+        d.color[:] = [float(x) for x in m[1]]
+        d.power = float(m[2])
+    else:
+        vals = [float(x) for x in m[1]]
+        d.color[:] = vals[0:3]
+        d.params[:len(vals[3:9])] = vals[3:9]
+    return d
+
+
+class Renderer:
+    """A scene dict (libyafaray_gb300.scenes) on the GPU: BVH + materials +
+    lights, rendered by the wavefront path tracer (gbrt_pt_render)."""
+
+    def __init__(self, scene):
+        from . import scenes as _scenes
+        self.scene = scene
+        self.vertices, self.faces, self.face_mat, self.mat_names = _scenes.flatten(scene)
+        self.bvh = Bvh.build_host(self.vertices, self.faces)
+        mats = (MaterialDesc * max(1, len(self.mat_names)))()
+        for i, name in enumerate(self.mat_names):
+            mats[i] = _material_desc(scene["materials"][name])
+        lights = (LightDesc * max(1, len(scene["lights"])))()
+        for i, L in enumerate(scene["lights"]):
+            if L["type"] != "arealight":
+                raise ValueError("only arealight is supported by this renderer")
+            lights[i].type = 0
+            lights[i].corner[:] = [float(x) for x in L["corner"]]
+            lights[i].point1[:] = [float(x) for x in L["point1"]]
+            lights[i].point2[:] = [float(x) for x in L["point2"]]
+            lights[i].color[:] = [float(x) for x in L["color"]]
+            lights[i].power = float(L["power"])
+            lights[i].samples = int(L["samples"])
+        h = ctypes.c_void_p()
+        fm = np.ascontiguousarray(self.face_mat, np.int32)
+        check(load().gbrt_scene_create(self.bvh.handle, _ptr(self.vertices), len(self.vertices), _ptr(self.faces),
+                                       len(self.faces), _ptr(fm), mats, len(self.mat_names), lights,
+                                       len(scene["lights"]), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().gbrt_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def camera_desc(self):
+        c = self.scene["camera"]
+        d = CameraDesc()
+        d.from_[:] = [float(x) for x in c["from"]]
+        d.to[:] = [float(x) for x in c["to"]]
+        d.up[:] = [float(x) for x in c["up"]]
+        d.resx, d.resy, d.focal = int(c["resx"]), int(c["resy"]), float(c["focal"])
+        return d
+
+    def params(self, spp, base_offset=0, seed=1, fp64=False, wave_paths=0):
+        it = self.scene["integrator"]
+        return PtParams(int(spp), int(it.get("path_samples", 1)), int(it.get("bounces", 5)),
+                        int(it.get("russian_roulette_min_bounces", 0)), int(base_offset), int(seed),
+                        PT_FP64_FILM if fp64 else 0, int(wave_paths))
+
+    def render(self, spp, base_offset=0, seed=1, fp64=False):
+        """Per-pixel mean image [resy, resx, 3] and stats dict."""
+        cam = self.camera_desc()
+        p = self.params(spp, base_offset, seed, fp64)
+        img = np.empty((cam.resy, cam.resx, 3), np.float32)
+        st = PtStats()
+        check(load().gbrt_pt_render_host(self._h, ctypes.byref(cam), ctypes.byref(p), _ptr(img), ctypes.byref(st)))
+        return img, {"camera_samples": st.camera_samples, "extension_rays": st.extension_rays,
+                     "shadow_rays": st.shadow_rays, "ms": st.ms}
+
+    def render_device(self, spp, film_ptr, film64_ptr=0, base_offset=0, seed=1, stream=0, stats=False, wave_paths=0):
+        """Adds sample sums into a device film (float or double RGB)."""
+        cam = self.camera_desc()
+        p = self.params(spp, base_offset, seed, bool(film64_ptr), wave_paths)
+        st = PtStats()
+        check(load().gbrt_pt_render(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.c_void_p(film_ptr or None),
+                                    ctypes.c_void_p(film64_ptr or None), ctypes.byref(st) if stats else None,
+                                    ctypes.c_void_p(stream)))
+        if stats:
+            return {"camera_samples": st.camera_samples, "extension_rays": st.extension_rays,
+                    "shadow_rays": st.shadow_rays, "ms": st.ms}
+        return None
+
+
+def sampler_eval(kind, dim, inputs, on_device):
+    x = np.ascontiguousarray(inputs, np.uint32)
+    out = np.empty(len(x), np.float64)
+    check(load().gbrt_sampler_eval(int(kind), int(dim), _ptr(x), len(x), _ptr(out), int(bool(on_device))))
+    return out

@@ -123,3 +123,64 @@ def camera_rays(width, height, eye, target, up=(0.0, 1.0, 0.0), fov_deg=40.0, se
     rays[:, 4:7] = d.reshape(-1, 3)
     rays[:, 7] = -1.0
     return rays
+
+
+# ---- scene descriptions for the renderers -------------------------------
+# A scene is a plain dict: materials (ordered), objects (name, material,
+# vertices, faces), lights, camera and integrator parameters, in the
+# vocabulary of the reference's ParamMaps (shinydiffusemat "color",
+# light_mat "color"/"power", arealight "corner"/"point1"/"point2"/"color"/
+# "power"/"samples", perspective camera "from"/"to"/"up"/"focal",
+# pathtracing "path_samples"/"bounces"/"russian_roulette_min_bounces").
+
+def cornell_scene(res=512, light_samples=4, bounces=5, rr_min=3, path_samples=1):
+    """The Cornell-box configuration: 34 triangles of walls and boxes
+    (shinydiffuse, grey 0.75 / red / green), a 0.5 x 0.5 m ceiling area light
+    of colour (17,12,4) at y = 1.999 with a 2-triangle light_mat emitter,
+    40-degree pinhole camera (focal 1.3737) from (0,1,3.7)."""
+    verts, faces, groups = cornell_mesh(as_quads=False)
+    mats = {"grey": ("shinydiffusemat", (0.75, 0.75, 0.75)),
+            "red": ("shinydiffusemat", (0.63, 0.065, 0.05)),
+            "green": ("shinydiffusemat", (0.14, 0.45, 0.09)),
+            "emitter": ("light_mat", (17.0, 12.0, 4.0), 1.0)}
+    gmat = {0: "grey", 1: "red", 2: "green", 3: "grey", 4: "grey"}
+    objects = []
+    for g in sorted(set(groups.tolist())):
+        sel = np.where(groups == g)[0]
+        f = faces[sel]
+        used = np.unique(f[:, :3])
+        remap = {int(u): i for i, u in enumerate(used)}
+        ff = np.array([[remap[int(x)] for x in row[:3]] + [TRI] for row in f], np.uint32)
+        objects.append({"name": f"group{g}", "material": gmat[g], "vertices": verts[used], "faces": ff})
+    c = np.array([-0.25, 1.999, -0.25])
+    x = np.array([0.5, 0.0, 0.0])
+    z = np.array([0.0, 0.0, 0.5])
+    lv = np.array([c, c + x, c + x + z, c + z], np.float32)
+    objects.append({"name": "lamp", "material": "emitter", "vertices": lv,
+                    "faces": np.array([[0, 1, 2, TRI], [0, 2, 3, TRI]], np.uint32)})
+    lights = [{"type": "arealight", "corner": tuple(c), "point1": tuple(c + x), "point2": tuple(c + z),
+               "color": (17.0, 12.0, 4.0), "power": 1.0, "samples": light_samples}]
+    camera = {"from": (0.0, 1.0, 3.7), "to": (0.0, 1.0, 0.0), "up": (0.0, 2.0, 3.7),
+              "resx": res, "resy": res, "focal": 1.3737}
+    integ = {"type": "pathtracing", "path_samples": path_samples, "bounces": bounces,
+             "russian_roulette_min_bounces": rr_min}
+    return {"materials": mats, "objects": objects, "lights": lights, "camera": camera, "integrator": integ}
+
+
+def flatten(scene):
+    """Concatenate objects in order into one mesh: (vertices, faces,
+    per-face material index, material names).  Face order = primitive IDs
+    (objects in creation order, faces in insertion order)."""
+    names = list(scene["materials"].keys())
+    V, F, M = [], [], []
+    base = 0
+    for o in scene["objects"]:
+        v = np.asarray(o["vertices"], np.float32)
+        f = np.asarray(o["faces"], np.uint32).copy()
+        tri = f[:, 3] == TRI
+        f[:, :3] += base
+        f[~tri, 3] += base
+        V.append(v); F.append(f)
+        M.append(np.full(len(f), names.index(o["material"]), np.int32))
+        base += len(v)
+    return np.concatenate(V), np.concatenate(F), np.concatenate(M), names

@@ -123,3 +123,55 @@ def run_reference_kdtree(verts, faces, rays, mode=0, accel="yafaray-kdtree-origi
     build_s, trace_s = struct.unpack("<dd", raw[24:40])
     rec = np.frombuffer(raw[40:], dtype=np.dtype([("id", "<i4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")]))
     return bound, build_s, trace_s, rec["id"].copy(), rec["t"].copy(), rec["u"].copy(), rec["v"].copy()
+
+
+REF_RENDER = os.path.join(HERE, "_ref", "render_dump")
+
+
+def reference_scene_text(scene, spp, batches, threads=-1):
+    """Scene dict (libyafaray_gb300.scenes) -> render_dump input text."""
+    out = []
+    for name, m in scene["materials"].items():
+        t = m[0]
+        if t == "shinydiffusemat":
+            out.append(f"material {name} shinydiffusemat {m[1][0]!r} {m[1][1]!r} {m[1][2]!r}")
+        elif t == "light_mat":
+            out.append(f"material {name} light_mat {m[1][0]!r} {m[1][1]!r} {m[1][2]!r} {m[2]!r}")
+        else:
+            out.append(f"material {name} {t} " + " ".join(repr(float(x)) for x in m[1]))
+    for o in scene["objects"]:
+        v = np.asarray(o["vertices"], np.float32)
+        f = np.asarray(o["faces"], np.uint32)
+        out.append(f"object {o['name']} {o['material']} {len(v)} {len(f)}")
+        out += [f"{float(a)!r} {float(b)!r} {float(c)!r}" for a, b, c in v]
+        out += [" ".join(str(int(x)) for x in (row[:3] if row[3] == TRI_MARK else row)) for row in f]
+    for L in scene["lights"]:
+        if L["type"] == "arealight":
+            vals = [*L["corner"], *L["point1"], *L["point2"], *L["color"], L["power"]]
+            out.append("arealight " + " ".join(repr(float(x)) for x in vals) + f" {int(L['samples'])}")
+        elif L["type"] == "pointlight":
+            vals = [*L["from"], *L["color"], L["power"]]
+            out.append("pointlight " + " ".join(repr(float(x)) for x in vals))
+    c = scene["camera"]
+    vals = [*c["from"], *c["to"], *c["up"]]
+    out.append("camera " + " ".join(repr(float(x)) for x in vals) + f" {c['resx']} {c['resy']} {float(c['focal'])!r}")
+    integ = dict(scene["integrator"])
+    t = integ.pop("type")
+    out.append(f"integrator {t} " + " ".join(f"{k}={str(v).lower() if isinstance(v, bool) else v}" for k, v in integ.items()))
+    out.append(f"render {spp} {batches} {threads}")
+    return "\n".join(out) + "\n"
+
+
+def run_reference_render(scene, spp, batches, threads=-1):
+    """Render with the compiled reference; returns (rgb [K,H,W,3] float32,
+    seconds per batch)."""
+    text = reference_scene_text(scene, spp, batches, threads)
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout = os.path.join(d, "scene.txt"), os.path.join(d, "out.bin")
+        open(fin, "w").write(text)
+        subprocess.run([REF_RENDER, fin, fout], check=True, stdout=subprocess.DEVNULL)
+        raw = open(fout, "rb").read()
+    K, H, W = struct.unpack("<iii", raw[:12])
+    secs = np.frombuffer(raw[12:12 + 8 * K], np.float64).copy()
+    rgb = np.frombuffer(raw[12 + 8 * K:], np.float32).reshape(K, H, W, 3).copy()
+    return rgb, secs

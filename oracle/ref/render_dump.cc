@@ -1,0 +1,234 @@
+// Test-oracle harness: renders a scene with the reference libYafaRay through
+// its public C API (yafaray_c_api.h) and dumps the "combined" layer of K
+// independent batches (distinct adv_base_sampling_offset values,
+// imagefilm.h:194) so per-pixel means and standard errors can be formed.
+// Box filter of width 1 (imagefilm.cc:252) makes each sample land in its own
+// pixel, so a batch's pixel value is the plain mean of its spp samples.
+// Only tests/golden/make_render_golden.py runs it.
+//
+// Input: a text scene, one statement per line (# comments):
+//   material NAME shinydiffusemat R G B
+//   material NAME light_mat R G B POWER
+//   material NAME glossy R G B  SR SG SB  EXPONENT  GLOSSY_REFLECT  DIFFUSE_REFLECT
+//   material NAME rough_glass IOR ALPHA  FR FG FB
+//   material NAME glass IOR  FR FG FB
+//   object NAME MATERIAL NV NF   then NV lines "x y z", NF lines "a b c" or "a b c d"
+//   arealight CX CY CZ  P1X P1Y P1Z  P2X P2Y P2Z  R G B  POWER SAMPLES
+//   pointlight X Y Z  R G B  POWER
+//   camera FX FY FZ  TX TY TZ  UX UY UZ  RESX RESY FOCAL
+//   integrator TYPE key=value ...      (ints/floats/bools/strings by key)
+//   render SPP BATCHES THREADS
+// Output (binary): i32 K, H, W; f64 seconds[K]; f32 rgb[K][H][W][3]
+#include "yafaray_c_api.h"
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+namespace {
+struct Film { int w = 0, h = 0; std::vector<float> rgb; };
+
+void putPixel(const char *layer, int x, int y, float r, float g, float b, float a, void *data)
+{
+	(void)a;
+	auto *f = static_cast<Film *>(data);
+	if(std::strcmp(layer, "combined") != 0 || x < 0 || y < 0 || x >= f->w || y >= f->h) return;
+	float *p = &f->rgb[3ull * (static_cast<size_t>(y) * f->w + x)];
+	p[0] = r; p[1] = g; p[2] = b;
+}
+
+void setTyped(yafaray_ParamMap *pm, const std::string &key, const std::string &val)
+{
+	if(val == "true" || val == "false") { yafaray_setParamMapBool(pm, key.c_str(), val == "true" ? YAFARAY_BOOL_TRUE : YAFARAY_BOOL_FALSE); return; }
+	char *end = nullptr;
+	const long iv = std::strtol(val.c_str(), &end, 10);
+	if(end && *end == '\0') { yafaray_setParamMapInt(pm, key.c_str(), static_cast<int>(iv)); return; }
+	const double dv = std::strtod(val.c_str(), &end);
+	if(end && *end == '\0') { yafaray_setParamMapFloat(pm, key.c_str(), dv); return; }
+	yafaray_setParamMapString(pm, key.c_str(), val.c_str());
+}
+} // namespace
+
+int main(int argc, char **argv)
+{
+	if(argc != 3) { fprintf(stderr, "usage: %s scene.txt out.bin\n", argv[0]); return 2; }
+	std::ifstream in(argv[1]);
+	if(!in) { perror("scene"); return 2; }
+	yafaray_Logger *logger = yafaray_createLogger("oracle", nullptr, nullptr, YAFARAY_DISPLAY_CONSOLE_HIDDEN);
+	yafaray_Scene *scene = yafaray_createScene(logger, "scene");
+	yafaray_ParamMap *pm = yafaray_createParamMap();
+	yafaray_ParamMapList *pml = yafaray_createParamMapList();
+	yafaray_SurfaceIntegrator *integrator = nullptr;
+	yafaray_ParamMap *camera = yafaray_createParamMap();
+	int resx = 0, resy = 0, spp = 1, batches = 1, threads = -1;
+	std::string line;
+	while(std::getline(in, line))
+	{
+		std::istringstream ss(line);
+		std::string kw;
+		if(!(ss >> kw) || kw[0] == '#') continue;
+		yafaray_clearParamMap(pm);
+		if(kw == "material")
+		{
+			std::string name, type;
+			ss >> name >> type;
+			yafaray_setParamMapString(pm, "type", type.c_str());
+			if(type == "shinydiffusemat") { double r, g, b; ss >> r >> g >> b; yafaray_setParamMapColor(pm, "color", r, g, b, 1.0); }
+			else if(type == "light_mat") { double r, g, b, p; ss >> r >> g >> b >> p; yafaray_setParamMapColor(pm, "color", r, g, b, 1.0); yafaray_setParamMapFloat(pm, "power", p); }
+			else if(type == "glossy")
+			{
+				double r, g, b, sr, sg, sb, e, gr, dr; ss >> r >> g >> b >> sr >> sg >> sb >> e >> gr >> dr;
+				yafaray_setParamMapColor(pm, "diffuse_color", r, g, b, 1.0);
+				yafaray_setParamMapColor(pm, "color", sr, sg, sb, 1.0);
+				yafaray_setParamMapFloat(pm, "exponent", e);
+				yafaray_setParamMapFloat(pm, "glossy_reflect", gr);
+				yafaray_setParamMapFloat(pm, "diffuse_reflect", dr);
+			}
+			else if(type == "rough_glass")
+			{
+				double ior, a, r, g, b; ss >> ior >> a >> r >> g >> b;
+				yafaray_setParamMapFloat(pm, "IOR", ior); yafaray_setParamMapFloat(pm, "alpha", a);
+				yafaray_setParamMapColor(pm, "filter_color", r, g, b, 1.0);
+			}
+			else if(type == "glass")
+			{
+				double ior, r, g, b; ss >> ior >> r >> g >> b;
+				yafaray_setParamMapFloat(pm, "IOR", ior);
+				yafaray_setParamMapColor(pm, "filter_color", r, g, b, 1.0);
+			}
+			size_t id;
+			yafaray_createMaterial(scene, &id, name.c_str(), pm, pml);
+		}
+		else if(kw == "object")
+		{
+			std::string name, mat; size_t nv, nf;
+			ss >> name >> mat >> nv >> nf;
+			size_t mat_id = 0;
+			yafaray_getMaterialId(scene, &mat_id, mat.c_str());
+			yafaray_setParamMapString(pm, "type", "mesh");
+			size_t obj;
+			yafaray_createObject(scene, &obj, name.c_str(), pm);
+			for(size_t i = 0; i < nv; ++i)
+			{
+				std::getline(in, line); std::istringstream vs(line);
+				double x, y, z; vs >> x >> y >> z;
+				yafaray_addVertex(scene, obj, x, y, z);
+			}
+			for(size_t i = 0; i < nf; ++i)
+			{
+				std::getline(in, line); std::istringstream fs(line);
+				std::vector<size_t> ix; size_t k;
+				while(fs >> k) ix.push_back(k);
+				if(ix.size() == 3) yafaray_addTriangle(scene, obj, ix[0], ix[1], ix[2], mat_id);
+				else if(ix.size() == 4) yafaray_addQuad(scene, obj, ix[0], ix[1], ix[2], ix[3], mat_id);
+			}
+			yafaray_initObject(scene, obj, mat_id);
+		}
+		else if(kw == "arealight")
+		{
+			double c[3], p1[3], p2[3], col[3], power; int samples;
+			ss >> c[0] >> c[1] >> c[2] >> p1[0] >> p1[1] >> p1[2] >> p2[0] >> p2[1] >> p2[2] >> col[0] >> col[1] >> col[2] >> power >> samples;
+			yafaray_setParamMapString(pm, "type", "arealight");
+			yafaray_setParamMapVector(pm, "corner", c[0], c[1], c[2]);
+			yafaray_setParamMapVector(pm, "point1", p1[0], p1[1], p1[2]);
+			yafaray_setParamMapVector(pm, "point2", p2[0], p2[1], p2[2]);
+			yafaray_setParamMapColor(pm, "color", col[0], col[1], col[2], 1.0);
+			yafaray_setParamMapFloat(pm, "power", power);
+			yafaray_setParamMapInt(pm, "samples", samples);
+			static int n = 0;
+			const std::string name = "area" + std::to_string(n++);
+			yafaray_createLight(scene, name.c_str(), pm);
+		}
+		else if(kw == "pointlight")
+		{
+			double p[3], col[3], power;
+			ss >> p[0] >> p[1] >> p[2] >> col[0] >> col[1] >> col[2] >> power;
+			yafaray_setParamMapString(pm, "type", "pointlight");
+			yafaray_setParamMapVector(pm, "from", p[0], p[1], p[2]);
+			yafaray_setParamMapColor(pm, "color", col[0], col[1], col[2], 1.0);
+			yafaray_setParamMapFloat(pm, "power", power);
+			static int n = 0;
+			const std::string name = "point" + std::to_string(n++);
+			yafaray_createLight(scene, name.c_str(), pm);
+		}
+		else if(kw == "camera")
+		{
+			double f[3], t[3], u[3], focal;
+			ss >> f[0] >> f[1] >> f[2] >> t[0] >> t[1] >> t[2] >> u[0] >> u[1] >> u[2] >> resx >> resy >> focal;
+			yafaray_clearParamMap(camera);
+			yafaray_setParamMapString(camera, "type", "perspective");
+			yafaray_setParamMapInt(camera, "resx", resx);
+			yafaray_setParamMapInt(camera, "resy", resy);
+			yafaray_setParamMapFloat(camera, "focal", focal);
+			yafaray_setParamMapVector(camera, "from", f[0], f[1], f[2]);
+			yafaray_setParamMapVector(camera, "to", t[0], t[1], t[2]);
+			yafaray_setParamMapVector(camera, "up", u[0], u[1], u[2]);
+		}
+		else if(kw == "integrator")
+		{
+			std::string type; ss >> type;
+			yafaray_setParamMapString(pm, "type", type.c_str());
+			std::string kv;
+			while(ss >> kv)
+			{
+				const auto eq = kv.find('=');
+				if(eq != std::string::npos) setTyped(pm, kv.substr(0, eq), kv.substr(eq + 1));
+			}
+			integrator = yafaray_createSurfaceIntegrator(logger, "integrator", pm);
+		}
+		else if(kw == "render") ss >> spp >> batches >> threads;
+	}
+	if(!integrator || resx <= 0 || resy <= 0) { fprintf(stderr, "scene lacks integrator or camera\n"); return 2; }
+	yafaray_clearParamMap(pm);
+	yafaray_setParamMapString(pm, "type", "yafaray-kdtree-original");
+	yafaray_setSceneAcceleratorParams(scene, pm);
+
+	std::vector<double> secs;
+	std::vector<float> all;
+	for(int k = 0; k < batches; ++k)
+	{
+		yafaray_clearParamMap(pm);
+		yafaray_setParamMapInt(pm, "width", resx);
+		yafaray_setParamMapInt(pm, "height", resy);
+		yafaray_setParamMapInt(pm, "threads", threads);
+		yafaray_setParamMapInt(pm, "AA_passes", 1);
+		yafaray_setParamMapInt(pm, "AA_minsamples", spp);
+		yafaray_setParamMapString(pm, "filter_type", "box");
+		yafaray_setParamMapFloat(pm, "AA_pixelwidth", 1.0);
+		yafaray_setParamMapInt(pm, "adv_base_sampling_offset", k * spp);
+		yafaray_Film *film = yafaray_createFilm(logger, integrator, "film", pm);
+		yafaray_defineCamera(film, camera);
+		Film f; f.w = resx; f.h = resy; f.rgb.assign(3ull * resx * resy, 0.f);
+		yafaray_setPutPixelCallback(film, putPixel, &f);
+		yafaray_RenderControl *rc = yafaray_createRenderControl();
+		yafaray_RenderMonitor *rm = yafaray_createRenderMonitor(nullptr, nullptr, YAFARAY_DISPLAY_CONSOLE_HIDDEN);
+		yafaray_setRenderControlForNormalStart(rc);
+		const auto flags = yafaray_checkAndClearSceneModifiedFlags(scene);
+		const auto t0 = std::chrono::steady_clock::now();
+		yafaray_preprocessScene(scene, rc, flags);
+		yafaray_preprocessSurfaceIntegrator(rm, integrator, rc, scene);
+		yafaray_render(rc, rm, integrator, film);
+		secs.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+		all.insert(all.end(), f.rgb.begin(), f.rgb.end());
+		yafaray_destroyRenderMonitor(rm);
+		yafaray_destroyRenderControl(rc);
+		yafaray_destroyFilm(film);
+	}
+	FILE *fo = fopen(argv[2], "wb");
+	if(!fo) { perror("out"); return 2; }
+	const int hdr[3] = {batches, resy, resx};
+	fwrite(hdr, 4, 3, fo);
+	fwrite(secs.data(), 8, secs.size(), fo);
+	fwrite(all.data(), 4, all.size(), fo);
+	fclose(fo);
+	yafaray_destroySurfaceIntegrator(integrator);
+	yafaray_destroyParamMap(camera);
+	yafaray_destroyParamMap(pm);
+	yafaray_destroyParamMapList(pml);
+	yafaray_destroyScene(scene);
+	yafaray_destroyLogger(logger);
+	return 0;
+}

@@ -1,0 +1,74 @@
+"""Generates render and sampler golden fixtures from the compiled reference
+(oracle/_ref/render_dump and oracle/_ref/sampler_dump, built from the
+reference sources by oracle/ref/Makefile).
+
+    make -C oracle/ref -j8 && python tests/golden/make_render_golden.py
+
+cornell_64_render.npz: the Cornell-box configuration at 64x64, `pathtracing`
+(path_samples 1, bounces 5, russian_roulette_min_bounces 3), 16 spp per
+batch, 32 batches with distinct adv_base_sampling_offset; per-pixel mean and
+standard error of the batch means.
+sampler.npz: the reference's lowDiscrepancySampling / riVdC / riLp / riS /
+fnv32ABuf / Halton(2,3) / FAST_TRIG sin and cos on a fixed input grid.
+"""
+import os
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import orc  # noqa: E402
+from libyafaray_gb300 import scenes  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+SAMPLER = os.path.join(ROOT, "oracle", "_ref", "sampler_dump")
+
+
+def sampler_golden():
+    with tempfile.TemporaryDirectory() as d:
+        fo = os.path.join(d, "s.bin")
+        subprocess.run([SAMPLER, fo], check=True)
+        raw = open(fo, "rb").read()
+    nd, ni = struct.unpack("<ii", raw[:8])
+    o = 8
+    lds = np.frombuffer(raw, np.float64, nd * ni, o).reshape(nd, ni); o += 8 * nd * ni
+    vdc = np.frombuffer(raw, np.float32, ni, o); o += 4 * ni
+    lp = np.frombuffer(raw, np.float32, ni, o); o += 4 * ni
+    ss = np.frombuffer(raw, np.float32, ni, o); o += 4 * ni
+    fnv = np.frombuffer(raw, np.uint32, ni, o); o += 4 * ni
+    h2 = np.frombuffer(raw, np.float32, ni, o); o += 4 * ni
+    h3 = np.frombuffer(raw, np.float32, ni, o); o += 4 * ni
+    na = struct.unpack("<i", raw[o:o + 4])[0]; o += 4
+    ang = np.frombuffer(raw, np.float32, na, o); o += 4 * na
+    sn = np.frombuffer(raw, np.float32, na, o); o += 4 * na
+    cs = np.frombuffer(raw, np.float32, na, o)
+    k = 512
+    np.savez_compressed(os.path.join(OUT, "sampler.npz"),
+                        lds=lds[:, :k].copy(), lds_index_mult=np.uint32(7919),
+                        vdc=vdc[:1024].copy(), lp=lp[:1024].copy(), s=ss[:1024].copy(), fnv=fnv[:1024].copy(),
+                        seq_index_mult=np.uint32(2654435761), h2=h2[:1024].copy(), h3=h3[:1024].copy(),
+                        halton_start=np.uint32(1000), angle=ang[::4].copy(), sin=sn[::4].copy(), cos=cs[::4].copy())
+    print("sampler.npz written")
+
+
+def render_golden(res=64, spp=16, batches=32):
+    sc = scenes.cornell_scene(res=res)
+    rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
+    mean = rgb.mean(0)
+    se = rgb.std(0, ddof=1) / np.sqrt(batches)
+    np.savez_compressed(os.path.join(OUT, f"cornell_{res}_render.npz"), mean=mean.astype(np.float32),
+                        se=se.astype(np.float32), batches=np.int32(batches), spp=np.int32(spp),
+                        seconds=secs)
+    print(f"cornell_{res}_render.npz: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
+
+
+if __name__ == "__main__":
+    if not os.path.exists(SAMPLER) or not os.path.exists(orc.REF_RENDER):
+        sys.exit("reference harnesses missing: run make -C oracle/ref first")
+    sampler_golden()
+    render_golden()

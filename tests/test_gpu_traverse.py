@@ -12,7 +12,8 @@ from tests import parity
 from libyafaray_gb300 import gbrt, scenes
 
 pytestmark = pytest.mark.gpu
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+TRAVERSAL_CASES = ["cornell_quads", "cornell_tris", "single_tri", "tri_soup_4k", "tri_soup_dense"]
+GOLDEN = [os.path.join(os.path.dirname(__file__), "golden", n + ".npz") for n in TRAVERSAL_CASES]
 
 
 @pytest.fixture(scope="module")

@@ -9,7 +9,8 @@ import pytest
 from oracle import orc
 from tests import parity
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+TRAVERSAL_CASES = ["cornell_quads", "cornell_tris", "single_tri", "tri_soup_4k", "tri_soup_dense"]
+GOLDEN = [os.path.join(os.path.dirname(__file__), "golden", n + ".npz") for n in TRAVERSAL_CASES]
 
 
 def test_golden_present():
