@@ -179,7 +179,8 @@ int gbrt_trace_shadow_host(const gbrt_bvh *bvh, const gbrt_ray *rays, uint32_t n
 enum {
 	GBRT_MAT_SHINYDIFFUSE = 0,   /* "shinydiffusemat": color, params[0] = diffuse_reflect (0 -> 1) */
 	GBRT_MAT_LIGHT = 1,          /* "light_mat": color, power, params[0] = double_sided (0/1) */
-	GBRT_MAT_GLOSSY = 2,         /* "glossy" (not yet supported by gbrt_scene_create) */
+	GBRT_MAT_GLOSSY = 2,         /* "glossy": color (glossy colour), color2 (diffuse_color), params =
+	                                {exponent, glossy_reflect, diffuse_reflect, as_diffuse (1)} */
 	GBRT_MAT_ROUGH_GLASS = 3,    /* "rough_glass" (not yet supported) */
 	GBRT_MAT_GLASS = 4           /* "glass" (not yet supported) */
 };
@@ -261,7 +262,8 @@ int gbrt_pt_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const
  * 1 sample::riVdC, 2 riLp, 3 riS, 4 fnv32ABuf (sample.h:100-148), 5/6
  * Halton base 2/3 radical inverse of x (halton.h:59-85), 7 FAST_TRIG
  * math::sin (dim 0) or math::cos (dim 1) of the float with bits x
- * (math.h:228-265). */
+ * (math.h:228-265), 8 FAST_MATH math::pow(a, b) with a = float bits of x
+ * and b = float bits of dim (math.h:116-146). */
 int gbrt_sampler_eval(int kind, int dim, const uint32_t *input, uint32_t n, double *out, int on_device);
 
 #ifdef __cplusplus

@@ -45,8 +45,10 @@ enum : uint32_t {
 struct DevMaterial {
 	uint32_t type;
 	uint32_t flags;
-	float col[3];      // shinydiffuse diffuse colour x diffuse strength; light_mat colour x power
-	float extra[5];
+	float col[3];      // shinydiffuse: colour x diffuse strength; light_mat: colour x power; glossy: glossy colour
+	float col2[3];     // glossy: diffuse colour
+	float exponent, m_glossy, m_diffuse, p_diffuse;
+	uint32_t as_diffuse, with_diffuse, double_sided, pad;
 };
 
 struct DevLight {
@@ -151,10 +153,171 @@ __device__ __forceinline__ void face_forward(const Surface &s, const float wo[3]
 	for(int k = 0; k < 3; ++k) out[k] = flip ? -s.n[k] : s.n[k];
 }
 
-// ShinyDiffuseMaterial::eval, diffuse component (material_shiny_diffuse.cc:297-337).
+__device__ __forceinline__ void normalize3(float v[3])
+{
+	const float l2 = dot3(v, v);
+	if(l2 != 0.f)
+	{
+		const float inv = __fdiv_rn(1.f, sqrtf(l2));
+		for(int k = 0; k < 3; ++k) v[k] = xm(v[k], inv);
+	}
+}
+
+// microfacet helpers (include/material/material_utils_microfacet.h:26-34, 87-104, 181-198)
+__device__ __forceinline__ float blinn_d(float cos_h, float e) { return xm(xa(e, 1.f), gbrt::fast_pow(cos_h, e)); }
+__device__ __forceinline__ float pdf_divisor(float c) { return xm(xm(8.f, kPi), xa(xm(c, 0.99f), 0.04f)); }
+__device__ __forceinline__ float blinn_pdf(float cos_theta, float cos_w_h, float e) { return __fdiv_rn(blinn_d(cos_theta, e), pdf_divisor(cos_w_h)); }
+__device__ __forceinline__ float as_divisor(float c1, float ci, float co)
+{
+	return xm(xm(8.f, kPi), xa(xm(xm(c1, fmaxf(ci, co)), 0.99f), 0.04f));
+}
+__device__ __forceinline__ float schlick(float c, float r)
+{
+	const float c1 = xs(1.f, c), c2 = xm(c1, c1);
+	return xa(r, xm(xm(xm(xs(1.f, r), c1), c2), c2));
+}
+__device__ __forceinline__ float diffuse_reflect_factor(float wi_n, float wo_n, float glossy, float diffuse)
+{
+	float f_wi = xs(1.f, xm(0.5f, wi_n));
+	float t = xm(f_wi, f_wi);
+	f_wi = xm(xm(t, t), f_wi);
+	float f_wo = xs(1.f, xm(0.5f, wo_n));
+	t = xm(f_wo, f_wo);
+	f_wo = xm(xm(t, t), f_wo);
+	const double r = 0.387507688 * diffuse * static_cast<double>(xs(1.f, glossy)) * static_cast<double>(xs(1.f, f_wi)) * static_cast<double>(xs(1.f, f_wo));
+	return static_cast<float>(r);
+}
+
+// GlossyMaterial::eval (material_glossy.cc:200-242)
+__device__ __forceinline__ void glossy_eval(const Surface &s, const float wo[3], const float wl[3], uint32_t bsdfs, float out[3])
+{
+	const DevMaterial &m = *s.m;
+	out[0] = out[1] = out[2] = 0.f;
+	if(!(bsdfs & BF_DIFFUSE) || xm(dot3(s.ng, wl), dot3(s.ng, wo)) < 0.f) return;
+	const bool diffuse_flag = (bsdfs & BF_DIFFUSE) != 0u;
+	float n[3];
+	face_forward(s, wo, n);
+	const float wi_n = fabsf(dot3(wl, n)), wo_n = fabsf(dot3(wo, n));
+	if((m.as_diffuse && diffuse_flag) || (!m.as_diffuse && (bsdfs & BF_GLOSSY)))
+	{
+		float h[3] = {xa(wo[0], wl[0]), xa(wo[1], wl[1]), xa(wo[2], wl[2])};
+		normalize3(h);
+		const float cos_wi_h = fmaxf(0.f, dot3(wl, h));
+		const float glossy = __fdiv_rn(xm(blinn_d(dot3(h, n), m.exponent), schlick(cos_wi_h, m.m_glossy)), as_divisor(cos_wi_h, wo_n, wi_n));
+		for(int k = 0; k < 3; ++k) out[k] = xm(glossy, m.col[k]);
+	}
+	if(m.with_diffuse && diffuse_flag)
+		for(int k = 0; k < 3; ++k) out[k] = xa(out[k], xm(xm(m.m_diffuse, xs(1.f, m.m_glossy)), m.col2[k]));
+}
+
+// GlossyMaterial::pdf (material_glossy.cc:404-444)
+__device__ __forceinline__ float glossy_pdf(const Surface &s, const float wo[3], const float wi[3], uint32_t flags)
+{
+	const DevMaterial &m = *s.m;
+	if(xm(dot3(s.ng, wo), dot3(s.ng, wi)) < 0.f) return 0.f;
+	float n[3];
+	face_forward(s, wo, n);
+	const float pd = m.p_diffuse;
+	const bool use_glossy = m.as_diffuse ? (flags & BF_DIFFUSE) != 0u : (flags & BF_GLOSSY) != 0u;
+	const bool use_diffuse = m.with_diffuse && (flags & BF_DIFFUSE);
+	float h[3] = {xa(wi[0], wo[0]), xa(wi[1], wo[1]), xa(wi[2], wo[2])};
+	normalize3(h);
+	if(use_diffuse)
+	{
+		float pdf = fabsf(dot3(wi, n));
+		if(use_glossy) pdf = xa(xm(pdf, pd), xm(blinn_pdf(dot3(n, h), dot3(wo, h), m.exponent), xs(1.f, pd)));
+		return pdf;
+	}
+	if(use_glossy) return blinn_pdf(dot3(n, h), dot3(wo, h), m.exponent);
+	return 0.f;
+}
+
+// GlossyMaterial::sample (material_glossy.cc:245-402), isotropic Blinn.
+__device__ __forceinline__ void glossy_sample(const Surface &s, const float wo[3], float s1, float s2, uint32_t flags,
+                                              float wi[3], float col[3], float &w, float &pdf, uint32_t &sampled)
+{
+	const DevMaterial &m = *s.m;
+	const float cos_ng_wo = dot3(s.ng, wo);
+	float n[3];
+	face_forward(s, wo, n);
+	pdf = 0.f;
+	float wi_n = 0.f;
+	const float wo_n = fabsf(dot3(wo, n));
+	col[0] = col[1] = col[2] = 0.f;
+	sampled = 0u;
+	wi[0] = n[0]; wi[1] = n[1]; wi[2] = n[2];
+	const float pd = m.p_diffuse;
+	const bool use_glossy = m.as_diffuse ? (flags & BF_DIFFUSE) != 0u : (flags & BF_GLOSSY) != 0u;
+	const bool use_diffuse = m.with_diffuse && (flags & BF_DIFFUSE);
+	if(use_diffuse)
+	{
+		const float s_pd = use_glossy ? pd : 1.f;
+		if(s1 < s_pd)
+		{
+			s1 = __fdiv_rn(s1, s_pd);
+			cos_hemisphere(n, s.u, s.v, s1, s2, wi);
+			if(xm(dot3(s.ng, wi), cos_ng_wo) < 0.f) { w = 0.f; return; }
+			wi_n = fabsf(dot3(wi, n));
+			pdf = wi_n;
+			float glossy = 0.f;
+			if(use_glossy)
+			{
+				float h[3] = {xa(wi[0], wo[0]), xa(wi[1], wo[1]), xa(wi[2], wo[2])};
+				normalize3(h);
+				const float cos_wo_h = dot3(wo, h), cos_wi_h = fabsf(dot3(wi, h)), cos_n_h = dot3(n, h);
+				pdf = xa(xm(pdf, pd), xm(blinn_pdf(cos_n_h, cos_wo_h, m.exponent), xs(1.f, pd)));
+				glossy = __fdiv_rn(xm(blinn_d(cos_n_h, m.exponent), schlick(cos_wi_h, m.m_glossy)), as_divisor(cos_wi_h, wo_n, wi_n));
+			}
+			sampled = BF_DIFFUSE | BF_REFLECT;
+			if(!(flags & BF_REFLECT)) { w = 0.f; return; }
+			const float dr = diffuse_reflect_factor(wi_n, wo_n, m.m_glossy, m.m_diffuse);
+			for(int k = 0; k < 3; ++k) col[k] = xa(xm(glossy, m.col[k]), xm(dr, m.col2[k]));
+			w = __fdiv_rn(wi_n, xa(xm(pdf, 0.99f), 0.01f));
+			return;
+		}
+		s1 = __fdiv_rn(xs(s1, pd), xs(1.f, pd));
+	}
+	if(use_glossy)
+	{
+		// microfacet::blinnSample (material_utils_microfacet.h:96-104)
+		const float cos_theta = gbrt::fast_pow(xs(1.f, s2), __fdiv_rn(1.f, xa(m.exponent, 1.f)));
+		const float sin_theta = sqrtf(xs(1.f, xm(cos_theta, cos_theta)));
+		const float phi = xm(s1, 6.28318530717958647692f);
+		const float hs[3] = {xm(sin_theta, gbrt::fast_cos(phi)), xm(sin_theta, gbrt::fast_sin(phi)), cos_theta};
+		float h[3];
+		for(int k = 0; k < 3; ++k) h[k] = xa(xa(xm(hs[0], s.u[k]), xm(hs[1], s.v[k])), xm(hs[2], n[k]));
+		float cos_wo_h = dot3(wo, h);
+		if(cos_wo_h < 0.f)
+		{
+			const float vn = xm(2.f, dot3(h, n));   // Vec::reflect (vector.h:358-362)
+			for(int k = 0; k < 3; ++k) h[k] = xs(xm(vn, n[k]), h[k]);
+			cos_wo_h = dot3(wo, h);
+		}
+		const float vn = dot3(wo, h);               // Vec::reflectDir (vector.h:391-396)
+		for(int k = 0; k < 3; ++k) wi[k] = vn < 0.f ? -wo[k] : xs(xm(xm(2.f, vn), h[k]), wo[k]);
+		if(xm(cos_ng_wo, dot3(s.ng, wi)) < 0.f) { w = 0.f; return; }
+		wi_n = fabsf(dot3(wi, n));
+		const float cos_hn = dot3(h, n);
+		pdf = blinn_pdf(cos_hn, cos_wo_h, m.exponent);
+		const float glossy = __fdiv_rn(xm(blinn_d(cos_hn, m.exponent), schlick(cos_wo_h, m.m_glossy)), as_divisor(cos_wo_h, wo_n, wi_n));
+		for(int k = 0; k < 3; ++k) col[k] = xm(glossy, m.col[k]);
+		sampled = m.as_diffuse ? (BF_DIFFUSE | BF_REFLECT) : (BF_GLOSSY | BF_REFLECT);
+	}
+	if(use_diffuse)
+	{
+		const float dr = diffuse_reflect_factor(wi_n, wo_n, m.m_glossy, m.m_diffuse);
+		for(int k = 0; k < 3; ++k) col[k] = xa(col[k], xm(dr, m.col2[k]));
+		pdf = xa(xm(wi_n, pd), xm(pdf, xs(1.f, pd)));
+	}
+	w = __fdiv_rn(wi_n, xa(xm(pdf, 0.99f), 0.01f));
+}
+
+// Material::eval dispatch; ShinyDiffuseMaterial::eval diffuse component
+// (material_shiny_diffuse.cc:297-337).
 __device__ __forceinline__ void mat_eval(const Surface &s, const float wo[3], const float wl[3], float out[3])
 {
 	out[0] = out[1] = out[2] = 0.f;
+	if(s.m->type == GBRT_MAT_GLOSSY) { glossy_eval(s, wo, wl, BF_ALL, out); return; }
 	if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return;
 	float n[3];
 	face_forward(s, wo, n);
@@ -162,22 +325,31 @@ __device__ __forceinline__ void mat_eval(const Surface &s, const float wo[3], co
 	for(int k = 0; k < 3; ++k) out[k] = s.m->col[k];
 }
 
-// ShinyDiffuseMaterial::pdf (material_shiny_diffuse.cc:443-484), lambertian part.
+// Material::pdf dispatch; ShinyDiffuseMaterial::pdf lambertian part
+// (material_shiny_diffuse.cc:443-484).  Flags of the MIS calls:
+// Glossy | Diffuse | Dispersive | Reflect | Transmit.
 __device__ __forceinline__ float mat_pdf(const Surface &s, const float wo[3], const float wi[3])
 {
+	if(s.m->type == GBRT_MAT_GLOSSY) return glossy_pdf(s, wo, wi, BF_GLOSSY | BF_DIFFUSE | BF_DISPERSIVE | BF_REFLECT | BF_TRANSMIT);
 	if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return 0.f;
 	float n[3];
 	face_forward(s, wo, n);
 	return fabsf(dot3(wi, n));
 }
 
-// ShinyDiffuseMaterial::sample (material_shiny_diffuse.cc:346-440), diffuse
-// reflection branch; light_mat returns pdf 0 (material_light.cc:75-80).
+// Material::sample dispatch; ShinyDiffuseMaterial::sample diffuse reflection
+// branch (material_shiny_diffuse.cc:346-440); light_mat returns pdf 0
+// (material_light.cc:75-80).
 __device__ __forceinline__ bool mat_sample(const Surface &s, const float wo[3], float s1, float s2, uint32_t req_flags,
                                            float wi[3], float col[3], float &w, float &pdf, uint32_t &sampled)
 {
 	col[0] = col[1] = col[2] = 0.f;
 	w = 0.f; pdf = 0.f; sampled = 0u;
+	if(s.m->type == GBRT_MAT_GLOSSY)
+	{
+		glossy_sample(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
+		return sampled != 0u;
+	}
 	if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return false;
 	const uint32_t cflags = BF_DIFFUSE | BF_REFLECT;
 	if((req_flags & cflags) != cflags) return false;
@@ -197,7 +369,7 @@ __device__ __forceinline__ bool mat_sample(const Surface &s, const float wo[3], 
 __device__ __forceinline__ bool mat_emit(const Surface &s, const float wo[3], float out[3])
 {
 	if(s.m->type != GBRT_MAT_LIGHT) return false;
-	if(dot3(wo, s.n) <= 0.f && !(s.m->extra[0] > 0.5f)) return false;
+	if(dot3(wo, s.n) <= 0.f && !s.m->double_sided) return false;
 	for(int k = 0; k < 3; ++k) out[k] = s.m->col[k];
 	return true;
 }
@@ -602,6 +774,14 @@ __host__ __device__ inline double sampler_value(const gbrt::LdsTables &t, int ki
 		case 4: return static_cast<double>(gbrt::fnv32(x));
 		case 5: return gbrt::radical_inverse(x, 2);
 		case 6: return gbrt::radical_inverse(x, 3);
+		case 8:
+		{
+			// FAST_MATH pow: base = float bits of x, exponent = float bits of dim
+			float f, e;
+			memcpy(&f, &x, 4);
+			memcpy(&e, &dim, 4);
+			return gbrt::fast_pow(f, e);
+		}
 		default:
 		{
 			float f;
@@ -746,7 +926,21 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 		{
 			d.flags = BF_EMIT;
 			for(int k = 0; k < 3; ++k) d.col[k] = m.color[k] * m.power;    // light_col_ = color * power
-			d.extra[0] = m.params[0];                                      // double_sided
+			d.double_sided = m.params[0] > 0.5f ? 1u : 0u;
+		}
+		else if(m.type == GBRT_MAT_GLOSSY)
+		{
+			// GlossyMaterial ctor and initBsdf (material_glossy.cc:128-148); params:
+			// exponent, glossy_reflect, diffuse_reflect, as_diffuse (1 = default)
+			d.exponent = m.params[0] > 0.f ? m.params[0] : 50.f;
+			d.m_glossy = m.params[1];
+			d.m_diffuse = m.params[2];
+			d.as_diffuse = m.params[3] < 0.5f ? 0u : 1u;
+			d.with_diffuse = d.m_diffuse > 0.f ? 1u : 0u;
+			d.flags = (d.with_diffuse ? (BF_DIFFUSE | BF_REFLECT) : 0u) | (d.as_diffuse ? (BF_DIFFUSE | BF_REFLECT) : (BF_GLOSSY | BF_REFLECT));
+			d.p_diffuse = std::min(0.6f, 1.f - (d.m_glossy / (d.m_glossy + (1.f - d.m_glossy) * d.m_diffuse)));
+			for(int k = 0; k < 3; ++k) { d.col[k] = m.color[k]; d.col2[k] = m.color2[k]; }
+			if(!d.as_diffuse) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: glossy material %u with as_diffuse = false needs the recursive glossy tracer (not built)", i);
 		}
 		else return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: material %u has unsupported type %u", i, m.type);
 	}
@@ -934,7 +1128,7 @@ int gbrt_pt_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbr
 int gbrt_sampler_eval(int kind, int dim, const uint32_t *input, uint32_t n, double *out, int on_device)
 {
 	if(!input || !out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_sampler_eval: NULL buffer");
-	if(kind < 0 || kind > 7 || (kind == 0 && (dim < 1 || dim >= gbrt::kLdsDims)))
+	if(kind < 0 || kind > 8 || (kind == 0 && (dim < 1 || dim >= gbrt::kLdsDims)))
 		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_sampler_eval: bad kind %d / dim %d", kind, dim);
 	const auto T = gbrt::make_lds_tables();
 	if(!on_device)

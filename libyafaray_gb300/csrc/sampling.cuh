@@ -14,6 +14,7 @@
 
 #include <cstdint>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #if defined(__CUDACC__)
@@ -176,6 +177,53 @@ GBRT_HD float fast_sin(float x)
 	return r;
 }
 GBRT_HD float fast_cos(float x) { return fast_sin(fadd(x, 1.57079632679489661923f)); }
+
+// FAST_MATH pow (include/math/math.h:116-146, 177-183): exp2(log2(a) * b)
+// with fifth-degree polynomial approximations of exp2 on the fractional part
+// and of log2 on the mantissa (exponent bits taken directly).
+GBRT_HD float bits_to_float(int32_t i)
+{
+#if defined(__CUDA_ARCH__)
+	return __int_as_float(i);
+#else
+	float f;
+	std::memcpy(&f, &i, 4);
+	return f;
+#endif
+}
+GBRT_HD int32_t float_to_bits(float f)
+{
+#if defined(__CUDA_ARCH__)
+	return __float_as_int(f);
+#else
+	int32_t i;
+	std::memcpy(&i, &f, 4);
+	return i;
+#endif
+}
+GBRT_HD float poly_exp2(float x)
+{
+	return fadd(fmul(x, fadd(fmul(x, fadd(fmul(x, fadd(fmul(x, fadd(fmul(x, 1.8775767e-3f), 8.9893397e-3f)), 5.5826318e-2f)), 2.4015361e-1f)), 6.9315308e-1f)), 9.9999994e-1f);
+}
+GBRT_HD float fast_exp2(float x)
+{
+	const float xl = fmaxf(fminf(x, 129.00000f), -126.99999f);
+	const int32_t ipart = static_cast<int32_t>(fsub(xl, 0.5f));
+	const float fpart = fsub(xl, static_cast<float>(ipart));
+	return fmul(bits_to_float((ipart + 127) << 23), poly_exp2(fpart));
+}
+GBRT_HD float poly_log2(float x)
+{
+	return fadd(fmul(x, fadd(fmul(x, fadd(fmul(x, fadd(fmul(x, fadd(fmul(x, -3.4436006e-2f), 3.1821337e-1f)), -1.2315303f)), 2.5988452f)), -3.3241990f)), 3.1157899f);
+}
+GBRT_HD float fast_log2(float x)
+{
+	const int32_t i = float_to_bits(x);
+	const float m = bits_to_float((i & 0x7FFFFF) | float_to_bits(1.f));
+	const float e = static_cast<float>(((i & 0x7F800000) >> 23) - 127);
+	return fadd(fmul(poly_log2(m), fsub(m, 1.f)), e);
+}
+GBRT_HD float fast_pow(float a, float b) { return fast_exp2(fmul(fast_log2(a), b)); }
 
 // ---- host-side table construction -------------------------------------------
 inline std::vector<uint32_t> lds_bases()

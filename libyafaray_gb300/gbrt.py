@@ -216,6 +216,11 @@ def _material_desc(m):
     elif kind == "light_mat":
         d.color[:] = [float(x) for x in m[1]]
         d.power = float(m[2])
+    elif kind == "glossy":
+        _, dc, gc, e, gr, dr = m
+        d.color[:] = [float(x) for x in gc]
+        d.color2[:] = [float(x) for x in dc]
+        d.params[:4] = [float(e), float(gr), float(dr), 1.0]
     else:
         vals = [float(x) for x in m[1]]
         d.color[:] = vals[0:3]

@@ -133,17 +133,34 @@ def camera_rays(width, height, eye, target, up=(0.0, 1.0, 0.0), fov_deg=40.0, se
 # "power"/"samples", perspective camera "from"/"to"/"up"/"focal",
 # pathtracing "path_samples"/"bounces"/"russian_roulette_min_bounces").
 
-def cornell_scene(res=512, light_samples=4, bounces=5, rr_min=3, path_samples=1):
+def glossy_material(diffuse_color, glossy_color=(0.9, 0.9, 0.9), exponent=100.0, glossy_reflect=0.5,
+                    diffuse_reflect=1.0):
+    """A "glossy" material tuple: (type, diffuse_color, color, exponent,
+    glossy_reflect, diffuse_reflect); as_diffuse keeps its default (true)."""
+    return ("glossy", tuple(diffuse_color), tuple(glossy_color), float(exponent), float(glossy_reflect),
+            float(diffuse_reflect))
+
+
+def cornell_scene(res=512, light_samples=4, bounces=5, rr_min=3, path_samples=1, glossy=False):
     """The Cornell-box configuration: 34 triangles of walls and boxes
     (shinydiffuse, grey 0.75 / red / green), a 0.5 x 0.5 m ceiling area light
     of colour (17,12,4) at y = 1.999 with a 2-triangle light_mat emitter,
-    40-degree pinhole camera (focal 1.3737) from (0,1,3.7)."""
+    40-degree pinhole camera (focal 1.3737) from (0,1,3.7).  glossy=True
+    makes the tall box glossy (exponent 100) and the floor glossy (exponent 20)."""
     verts, faces, groups = cornell_mesh(as_quads=False)
     mats = {"grey": ("shinydiffusemat", (0.75, 0.75, 0.75)),
             "red": ("shinydiffusemat", (0.63, 0.065, 0.05)),
             "green": ("shinydiffusemat", (0.14, 0.45, 0.09)),
             "emitter": ("light_mat", (17.0, 12.0, 4.0), 1.0)}
     gmat = {0: "grey", 1: "red", 2: "green", 3: "grey", 4: "grey"}
+    if glossy:
+        mats["glossy_box"] = glossy_material((0.75, 0.75, 0.75), exponent=100.0)
+        mats["glossy_floor"] = glossy_material((0.75, 0.75, 0.75), exponent=20.0, glossy_reflect=0.4)
+        gmat[4] = "glossy_box"
+    if glossy:
+        groups = groups.copy()
+        groups[0:2] = 5          # the floor's two triangles get their own object
+        gmat[5] = "glossy_floor"
     objects = []
     for g in sorted(set(groups.tolist())):
         sel = np.where(groups == g)[0]

@@ -137,6 +137,10 @@ def reference_scene_text(scene, spp, batches, threads=-1):
             out.append(f"material {name} shinydiffusemat {m[1][0]!r} {m[1][1]!r} {m[1][2]!r}")
         elif t == "light_mat":
             out.append(f"material {name} light_mat {m[1][0]!r} {m[1][1]!r} {m[1][2]!r} {m[2]!r}")
+        elif t == "glossy":
+            _, dc, gc, e, gr, dr = m
+            vals = [*dc, *gc, e, gr, dr]
+            out.append(f"material {name} glossy " + " ".join(repr(float(x)) for x in vals))
         else:
             out.append(f"material {name} {t} " + " ".join(repr(float(x)) for x in m[1]))
     for o in scene["objects"]:

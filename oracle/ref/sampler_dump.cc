@@ -9,6 +9,7 @@
 //   u32 fnv[n_idx]                                            fnv32ABuf(n * 2654435761u)
 //   f32 h2[n_idx], h3[n_idx]                                  Halton(2/3, start=1000).getNext() x n_idx
 //   i32 n_ang; f32 ang[n_ang], sin[n_ang], cos[n_ang]          math::sin / math::cos (FAST_TRIG)
+//   i32 n_pow; f32 base[n_pow], expo[n_pow], pow[n_pow]        math::pow (FAST_MATH exp2(log2(a) * b))
 #include "sampler/halton.h"
 #include "sampler/sample.h"
 #include "math/random.h"
@@ -59,6 +60,17 @@ int main(int argc, char **argv)
 		co[i] = math::cos(ang[i]);
 	}
 	fwrite(ang.data(), 4, n_ang, f); fwrite(s.data(), 4, n_ang, f); fwrite(co.data(), 4, n_ang, f);
+	const int n_pow = 8192;
+	fwrite(&n_pow, 4, 1, f);
+	std::vector<float> pb(n_pow), pe(n_pow), pv(n_pow);
+	for(int i = 0; i < n_pow; ++i)
+	{
+		pb[i] = -0.2f + 1.2f * static_cast<float>(i % 1024) / 1023.f;
+		const float exps[8] = {1.f / 51.f, 1.f / 101.f, 1.f / 501.f, 0.5f, 50.f, 100.f, 500.f, 3.3f};
+		pe[i] = exps[i / 1024];
+		pv[i] = math::pow(pb[i], pe[i]);
+	}
+	fwrite(pb.data(), 4, n_pow, f); fwrite(pe.data(), 4, n_pow, f); fwrite(pv.data(), 4, n_pow, f);
 	fclose(f);
 	return 0;
 }

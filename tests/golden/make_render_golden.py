@@ -46,29 +46,40 @@ def sampler_golden():
     na = struct.unpack("<i", raw[o:o + 4])[0]; o += 4
     ang = np.frombuffer(raw, np.float32, na, o); o += 4 * na
     sn = np.frombuffer(raw, np.float32, na, o); o += 4 * na
-    cs = np.frombuffer(raw, np.float32, na, o)
+    cs = np.frombuffer(raw, np.float32, na, o); o += 4 * na
+    npow = struct.unpack("<i", raw[o:o + 4])[0]; o += 4
+    pb = np.frombuffer(raw, np.float32, npow, o); o += 4 * npow
+    pe = np.frombuffer(raw, np.float32, npow, o); o += 4 * npow
+    pv = np.frombuffer(raw, np.float32, npow, o)
     k = 512
     np.savez_compressed(os.path.join(OUT, "sampler.npz"),
                         lds=lds[:, :k].copy(), lds_index_mult=np.uint32(7919),
                         vdc=vdc[:1024].copy(), lp=lp[:1024].copy(), s=ss[:1024].copy(), fnv=fnv[:1024].copy(),
                         seq_index_mult=np.uint32(2654435761), h2=h2[:1024].copy(), h3=h3[:1024].copy(),
-                        halton_start=np.uint32(1000), angle=ang[::4].copy(), sin=sn[::4].copy(), cos=cs[::4].copy())
+                        halton_start=np.uint32(1000), angle=ang[::4].copy(), sin=sn[::4].copy(), cos=cs[::4].copy(),
+                        pow_base=pb.copy(), pow_exp=pe.copy(), pow=pv.copy())
     print("sampler.npz written")
 
 
-def render_golden(res=64, spp=16, batches=32):
-    sc = scenes.cornell_scene(res=res)
+def render_golden(res=64, spp=16, batches=32, glossy=False):
+    sc = scenes.cornell_scene(res=res, glossy=glossy)
     rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
     mean = rgb.mean(0)
     se = rgb.std(0, ddof=1) / np.sqrt(batches)
-    np.savez_compressed(os.path.join(OUT, f"cornell_{res}_render.npz"), mean=mean.astype(np.float32),
+    name = f"cornell_{'glossy_' if glossy else ''}{res}_render.npz"
+    np.savez_compressed(os.path.join(OUT, name), mean=mean.astype(np.float32),
                         se=se.astype(np.float32), batches=np.int32(batches), spp=np.int32(spp),
                         seconds=secs)
-    print(f"cornell_{res}_render.npz: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
+    print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
 
 
 if __name__ == "__main__":
     if not os.path.exists(SAMPLER) or not os.path.exists(orc.REF_RENDER):
         sys.exit("reference harnesses missing: run make -C oracle/ref first")
-    sampler_golden()
-    render_golden()
+    what = sys.argv[1:] or ["sampler", "cornell"]
+    if "sampler" in what:
+        sampler_golden()
+    if "cornell" in what:
+        render_golden()
+    if "cornell_glossy" in what or "cornell" in what:
+        render_golden(glossy=True)

@@ -39,4 +39,11 @@ def check_sampler(on_device):
         got = gbrt.sampler_eval(7, dim, bits, on_device).astype(np.float32)
         if (got != g[key]).any():
             mismatches[key] = int((got != g[key]).sum())
+    pb = g["pow_base"].view(np.uint32)
+    for e in np.unique(g["pow_exp"]):
+        sel = g["pow_exp"] == e
+        got = gbrt.sampler_eval(8, int(np.float32(e).view(np.int32)), pb[sel], on_device).astype(np.float32)
+        bad = int((got.view(np.uint32) != g["pow"][sel].view(np.uint32)).sum())
+        if bad:
+            mismatches[f"pow{e}"] = bad
     return mismatches

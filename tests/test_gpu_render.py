@@ -66,3 +66,14 @@ def test_gpu_render_accumulates_and_counts_rays(cuda_device):
     img64, _ = r.render(8, fp64=True)
     img32, _ = r.render(8)
     assert np.allclose(img64, img32, rtol=1e-4, atol=1e-5)
+
+
+def test_gpu_cornell_glossy_matches_reference(cuda_device):
+    g = np.load(os.path.join(GOLD, "cornell_glossy_64_render.npz"))
+    sc = scenes.cornell_scene(res=64, glossy=True)
+    r = gbrt.Renderer(sc)
+    gb = batches(r, int(g["spp"]), int(g["batches"]))
+    frac, relmse, m = parity(gb, g["mean"], g["se"])
+    print(f"cornell glossy 64x64: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
+          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
+    assert frac >= 0.995
