@@ -201,3 +201,87 @@ def flatten(scene):
         M.append(np.full(len(f), names.index(o["material"]), np.int32))
         base += len(v)
     return np.concatenate(V), np.concatenate(F), np.concatenate(M), names
+
+
+def _box_tris(center, size, yaw):
+    """12 triangles of a yawed box (outward-facing)."""
+    hx, hy, hz = 0.5 * np.asarray(size, np.float64)
+    p = np.array([[-hx, -hy, -hz], [hx, -hy, -hz], [hx, hy, -hz], [-hx, hy, -hz],
+                  [-hx, -hy, hz], [hx, -hy, hz], [hx, hy, hz], [-hx, hy, hz]])
+    c, s = math.cos(yaw), math.sin(yaw)
+    R = np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])
+    p = p @ R.T + np.asarray(center, np.float64)
+    quads = [[0, 3, 2, 1], [4, 5, 6, 7], [0, 1, 5, 4], [3, 7, 6, 2], [0, 4, 7, 3], [1, 2, 6, 5]]
+    tris = []
+    for q in quads:
+        tris.append([q[0], q[1], q[2]]); tris.append([q[0], q[2], q[3]])
+    return p, np.array(tris)
+
+
+def indoor_scene(n_boxes=16_667, res=(960, 540), seed=5, bounces=12, rr_min=4, light_samples=2):
+    """Indoor scene lit through a gap: a closed 10 x 4 x 6 m room whose
+    1 x 2 m door (in the wall z = 6, x in [4.5, 5.5]) stands ajar by 0.1 m,
+    an outdoor 2 x 2 m area light of radiance 200 facing the door 3 m beyond
+    it (z = 9), and n_boxes seeded furniture boxes (12 triangles each;
+    16,667 boxes = 200,004 triangles) with shinydiffuse albedo U[0.2, 0.8]
+    per channel (palette of 32) or, for 20 % of the boxes, glossy exponent 100
+    (palette of 8).  Camera inside looking at the door wall; max depth 12."""
+    rng = np.random.default_rng(seed)
+    mats = {}
+    for i in range(32):
+        mats[f"diff{i}"] = ("shinydiffusemat", tuple(float(x) for x in rng.uniform(0.2, 0.8, 3)))
+    for i in range(8):
+        mats[f"glossy{i}"] = glossy_material(tuple(float(x) for x in rng.uniform(0.2, 0.8, 3)), exponent=100.0)
+    mats["wall"] = ("shinydiffusemat", (0.7, 0.7, 0.7))
+    mats["emitter"] = ("light_mat", (1.0, 1.0, 1.0), 200.0)
+    objects = []
+
+    def quad_obj(name, mat, pts):
+        objects.append({"name": name, "material": mat, "vertices": np.asarray(pts, np.float32),
+                        "faces": np.array([[0, 1, 2, TRI], [0, 2, 3, TRI]], np.uint32)})
+
+    W, H, D = 10.0, 4.0, 6.0
+    quad_obj("floor", "wall", [[0, 0, 0], [0, 0, D], [W, 0, D], [W, 0, 0]])
+    quad_obj("ceiling", "wall", [[0, H, 0], [W, H, 0], [W, H, D], [0, H, D]])
+    quad_obj("wall_front", "wall", [[0, 0, 0], [W, 0, 0], [W, H, 0], [0, H, 0]])
+    quad_obj("wall_left", "wall", [[0, 0, 0], [0, H, 0], [0, H, D], [0, 0, D]])
+    quad_obj("wall_right", "wall", [[W, 0, 0], [W, 0, D], [W, H, D], [W, H, 0]])
+    # back wall z = D with a 1 x 2 m door opening at x in [4.5, 5.5]
+    quad_obj("wall_back_l", "wall", [[0, 0, D], [0, H, D], [4.5, H, D], [4.5, 0, D]])
+    quad_obj("wall_back_r", "wall", [[5.5, 0, D], [5.5, H, D], [W, H, D], [W, 0, D]])
+    quad_obj("wall_back_t", "wall", [[4.5, 2, D], [4.5, H, D], [5.5, H, D], [5.5, 2, D]])
+    # door leaf hinged at x = 4.5, opened outwards so its free edge leaves a 0.1 m gap
+    ang = math.asin(0.1)
+    ex, ez = 4.5 + math.cos(ang), D + math.sin(ang)
+    quad_obj("door", "wall", [[4.5, 0, D], [4.5, 2, D], [ex, 2, ez], [ex, 0, ez]])
+    # furniture boxes, kept out of the door's light path
+    V, F, M = [], [], []
+    names_d = [f"diff{i}" for i in range(32)]
+    names_g = [f"glossy{i}" for i in range(8)]
+    for b in range(n_boxes):
+        size = rng.uniform(0.05, 0.35, 3)
+        while True:
+            c = np.array([rng.uniform(0.3, W - 0.3), rng.uniform(0.0, 3.2), rng.uniform(0.3, D - 0.4)])
+            if not (3.5 < c[0] < 6.5 and c[2] > 4.2):
+                break
+        c[1] += 0.5 * size[1]
+        p, t = _box_tris(c, size, rng.uniform(0, 2 * math.pi))
+        V.append(p); F.append(t)
+        M.append(names_g[rng.integers(8)] if rng.random() < 0.2 else names_d[rng.integers(32)])
+    by_mat = {}
+    for v, f, m in zip(V, F, M):
+        by_mat.setdefault(m, []).append((v, f))
+    for m, lst in sorted(by_mat.items()):
+        vv = np.concatenate([v for v, _ in lst]).astype(np.float32)
+        ff = np.concatenate([f + 8 * i for i, (_, f) in enumerate(lst)]).astype(np.uint32)
+        faces = np.empty((len(ff), 4), np.uint32); faces[:, :3] = ff; faces[:, 3] = TRI
+        objects.append({"name": f"boxes_{m}", "material": m, "vertices": vv, "faces": faces})
+    # outdoor light 3 m beyond the gap, facing -z, with its light_mat emitter
+    c = (4.0, 0.0, D + 3.0)
+    lights = [{"type": "arealight", "corner": c, "point1": (4.0, 2.0, D + 3.0), "point2": (6.0, 0.0, D + 3.0),
+               "color": (1.0, 1.0, 1.0), "power": 200.0, "samples": light_samples}]
+    quad_obj("lamp", "emitter", [[4, 0, D + 3], [4, 2, D + 3], [6, 2, D + 3], [6, 0, D + 3]])
+    camera = {"from": (5.0, 1.6, 0.4), "to": (5.0, 1.1, 6.0), "up": (5.0, 2.6, 0.4),
+              "resx": res[0], "resy": res[1], "focal": 1.0}
+    integ = {"type": "pathtracing", "path_samples": 1, "bounces": bounces, "russian_roulette_min_bounces": rr_min}
+    return {"materials": mats, "objects": objects, "lights": lights, "camera": camera, "integrator": integ}

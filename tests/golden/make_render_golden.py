@@ -73,6 +73,16 @@ def render_golden(res=64, spp=16, batches=32, glossy=False):
     print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
 
 
+def indoor_golden(spp=16, batches=24):
+    sc = scenes.indoor_scene(n_boxes=400, res=(96, 54))
+    rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
+    mean = rgb.mean(0)
+    se = rgb.std(0, ddof=1) / np.sqrt(batches)
+    np.savez_compressed(os.path.join(OUT, "indoor_small_render.npz"), mean=mean.astype(np.float32),
+                        se=se.astype(np.float32), batches=np.int32(batches), spp=np.int32(spp), seconds=secs)
+    print(f"indoor_small_render.npz: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
+
+
 if __name__ == "__main__":
     if not os.path.exists(SAMPLER) or not os.path.exists(orc.REF_RENDER):
         sys.exit("reference harnesses missing: run make -C oracle/ref first")
@@ -83,3 +93,5 @@ if __name__ == "__main__":
         render_golden()
     if "cornell_glossy" in what or "cornell" in what:
         render_golden(glossy=True)
+    if "indoor" in what:
+        indoor_golden()

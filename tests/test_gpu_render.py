@@ -77,3 +77,16 @@ def test_gpu_cornell_glossy_matches_reference(cuda_device):
     print(f"cornell glossy 64x64: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
           f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
     assert frac >= 0.995
+
+
+def test_gpu_indoor_small_matches_reference(cuda_device):
+    """Indoor scene (door ajar, outdoor light, glossy and diffuse boxes), 400
+    boxes at 96x54, depth 12 with Russian roulette."""
+    g = np.load(os.path.join(GOLD, "indoor_small_render.npz"))
+    sc = scenes.indoor_scene(n_boxes=400, res=(96, 54))
+    r = gbrt.Renderer(sc)
+    gb = batches(r, int(g["spp"]), int(g["batches"]))
+    frac, relmse, m = parity(gb, g["mean"], g["se"])
+    print(f"indoor small: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
+          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
+    assert frac >= 0.995
