@@ -185,7 +185,10 @@ enum {
 	GBRT_MAT_GLASS = 4           /* "glass" (not yet supported) */
 };
 enum { GBRT_LIGHT_AREA = 0, GBRT_LIGHT_POINT = 1 };
-enum { GBRT_PT_FP64_FILM = 1 };
+enum {
+	GBRT_PT_FP64_FILM = 1,        /* accumulate the film in double */
+	GBRT_PT_GUIDE_RADIANCE = 2    /* train the guide on incident radiance alone (default: radiance x BSDF cosine) */
+};
 
 typedef struct gbrt_material_desc {
 	uint32_t type;
@@ -216,6 +219,8 @@ typedef struct gbrt_camera_desc {
 /* pathtracing / film parameters with the reference's names:
  * AA_minsamples (spp, one pass), path_samples, bounces,
  * russian_roulette_min_bounces, adv_base_sampling_offset. */
+typedef struct gbrt_guide gbrt_guide;
+
 typedef struct gbrt_pt_params {
 	int32_t spp;
 	int32_t path_samples;
@@ -224,7 +229,12 @@ typedef struct gbrt_pt_params {
 	uint32_t base_sampling_offset;
 	uint32_t seed;              /* random stream of Russian roulette / light choice */
 	uint32_t flags;             /* GBRT_PT_FP64_FILM: accumulate in double */
-	uint32_t wave_paths;        /* paths per wavefront wave; 0 = 4 Mi */
+	uint32_t wave_paths;        /* paths per wavefront wave; 0 = 4 Mi (1 Mi while recording) */
+	gbrt_guide *guide;          /* path-guiding network, or NULL for plain path tracing */
+	float guide_alpha;          /* probability of sampling the guide (one-sample MIS); 0 = plain */
+	uint32_t guide_train_steps; /* Adam steps on this render's own records after each wave; 0 = none */
+	uint32_t guide_batch;       /* records per step; 0 = 65536 */
+	uint32_t guide_max_vertex;  /* guide (and record) only vertices 0 .. guide_max_vertex - 1; 0 = all */
 } gbrt_pt_params;
 
 typedef struct gbrt_pt_stats {
@@ -255,6 +265,44 @@ int gbrt_pt_render(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt
 /* Same into a host image of per-pixel means (sum / spp), resx*resy*3 floats. */
 int gbrt_pt_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params,
                         float *image_out, gbrt_pt_stats *stats);
+
+
+/* ---- path-guiding network (no counterpart in the reference) -------------
+ * q(w | x): 8-lobe von Mises-Fisher mixture over incident direction,
+ * predicted from the hit position by a 16-level x 2-feature hash-grid
+ * encoding (2^log2_table entries per level) and an MLP 32 -> 64 -> 64 -> 40.
+ * Trained online on records {position xyz, sampled direction xyz,
+ * weight = luminance(incident radiance) / sampling pdf, pad} (8 floats),
+ * minimising the Monte-Carlo KL divergence  -sum c log q / sum c  with Adam. */
+typedef struct gbrt_guide_params {
+	uint32_t log2_table;        /* 0 -> 19 */
+	float base_resolution;      /* 0 -> 16 */
+	float max_resolution;       /* 0 -> 2048 */
+	float learning_rate;        /* 0 -> 5e-3 */
+	uint32_t seed;
+} gbrt_guide_params;
+
+int gbrt_guide_create(const float bound[6], const gbrt_guide_params *params, gbrt_guide **out);
+int gbrt_guide_destroy(gbrt_guide *guide);
+int gbrt_guide_info(const gbrt_guide *guide, uint32_t *n_mlp_params, uint64_t *n_table_params);
+/* Copy parameters out / in (host buffers; either pointer may be NULL).
+ * MLP layout: W1[64][32] b1[64] W2[64][64] b2[64] W3[40][64] b3[40];
+ * table: [16 levels][2^log2_table][2 features]. */
+int gbrt_guide_get_params(const gbrt_guide *guide, float *mlp, float *table);
+int gbrt_guide_set_params(gbrt_guide *guide, const float *mlp, const float *table);
+/* Mixture parameters for n positions (device, 3 floats each): 40 floats per
+ * position, per lobe {mu xyz, kappa, weight}. */
+int gbrt_guide_eval(gbrt_guide *guide, const float *pos_dev, uint32_t n, float *lobes_dev, void *stream);
+/* Loss gradient of n records (device) into the guide's gradient buffers;
+ * loss_out (host, optional) receives the batch loss (synchronises). */
+int gbrt_guide_grad(gbrt_guide *guide, const float *records_dev, uint32_t n, float *loss_out, void *stream);
+int gbrt_guide_get_grads(const gbrt_guide *guide, float *mlp_grad, float *table_grad);
+/* The same forward pass on the host (no CUDA calls), from explicit
+ * parameters in the gbrt_guide_get_params layout: lobes for n positions. */
+int gbrt_guide_forward_host(const float bound[6], const gbrt_guide_params *params, const float *mlp, const float *table,
+                            const float *pos, uint32_t n, float *lobes);
+/* gbrt_guide_grad followed by one Adam step (gradients are cleared). */
+int gbrt_guide_step(gbrt_guide *guide, const float *records_dev, uint32_t n, float *loss_out, void *stream);
 
 /* Diagnostics: evaluates one of the path tracer's sampling primitives on n
  * inputs, on the device (on_device != 0) or with the host build of the same

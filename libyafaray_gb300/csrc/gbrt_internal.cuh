@@ -75,6 +75,8 @@ int gbrt_set_error(int code, const char *fmt, ...);
 // Launchers implemented in traverse.cu
 int gbrt_launch_closest(const gbrt_bvh *bvh, const gbrt_ray *rays, uint32_t n, gbrt_hit *hits, cudaStream_t s);
 int gbrt_launch_shadow(const gbrt_bvh *bvh, const gbrt_ray *rays, uint32_t n, int32_t *occ, cudaStream_t s);
+// Implemented in guiding.cu
+int gbrt_guide_eval_queue(gbrt_guide *G, const float *pos_dev, uint32_t cap, const uint32_t *count_dev, float *lobes_dev, cudaStream_t s);
 // Implemented in bvh_build.cu
 int gbrt_build_impl(const float *verts, uint32_t nv, const uint32_t *faces, uint32_t nf,
                     const gbrt_build_params *params, cudaStream_t s, gbrt_bvh **out);

@@ -1,0 +1,554 @@
+// Path-guiding network (no counterpart in the reference; the benchmark spec's
+// learned part): hash-grid encoding + MLP + 8-lobe vMF mixture head, trained
+// online on the tracer's own radiance samples.
+//
+//   k_guide_eval   position -> mixture parameters (mu, kappa, weight per lobe)
+//   k_guide_grad   forward + KL-divergence gradient + backward for a batch of
+//                  (position, sampled direction, weight L/pdf) records;
+//                  weight gradients per block, hash-grid gradients by atomics
+//   k_reduce       per-block weight gradients -> one gradient
+//   k_adam         Adam step on the MLP and the touched hash-grid entries
+//
+// The training objective is the Monte-Carlo estimate of the KL divergence
+// from the incident-radiance distribution to q:  -sum_j c_j log q(w_j | x_j)
+// with c_j = luminance(L_j) / p_j (p_j the pdf w_j was sampled with),
+// normalised by sum_j c_j.
+#include "gbrt_internal.cuh"
+#include "guide_common.cuh"
+#include "guide_device.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+namespace {
+
+using namespace gbrt;
+
+constexpr int kEvalThreads = 128;
+constexpr int kGradThreads = 64;       // one record per thread, 64 records per chunk
+constexpr int kGradChunks = 16;        // chunks per block -> 1024 records per block
+
+GBRT_GHD float2 load_feat(const float *table, size_t off)
+{
+#if defined(__CUDA_ARCH__)
+	return __ldg(reinterpret_cast<const float2 *>(table) + off);
+#else
+	return make_float2(table[2 * off], table[2 * off + 1]);
+#endif
+}
+
+GBRT_GHD void encode(const GuideGrid &g, const float *__restrict__ table, const float p[3], float e[kGuideIn],
+                                       uint32_t *corner_idx, float *corner_w)
+{
+	float x[3];
+	for(int a = 0; a < 3; ++a) x[a] = fminf(fmaxf((p[a] - g.lo[a]) * g.inv_ext[a], 0.f), 1.f);
+#pragma unroll 1
+	for(int l = 0; l < kGuideLevels; ++l)
+	{
+		const float r = g.res[l];
+		float fx[3];
+		uint32_t ix[3];
+		for(int a = 0; a < 3; ++a)
+		{
+			const float s = x[a] * r;
+			const float fl = fminf(floorf(s), r - 1.f);
+			ix[a] = static_cast<uint32_t>(fl);
+			fx[a] = s - fl;
+		}
+		float f0 = 0.f, f1 = 0.f;
+		for(int c = 0; c < 8; ++c)
+		{
+			const uint32_t dx = c & 1, dy = (c >> 1) & 1, dz = (c >> 2) & 1;
+			const float w = (dx ? fx[0] : 1.f - fx[0]) * (dy ? fx[1] : 1.f - fx[1]) * (dz ? fx[2] : 1.f - fx[2]);
+			const uint32_t idx = grid_index(g, l, ix[0] + dx, ix[1] + dy, ix[2] + dz);
+			const size_t off = (static_cast<size_t>(l) << g.log2_table) + idx;
+			const float2 v = load_feat(table, off);
+			f0 += w * v.x;
+			f1 += w * v.y;
+			if(corner_idx) { corner_idx[l * 8 + c] = static_cast<uint32_t>(off); corner_w[l * 8 + c] = w; }
+		}
+		e[2 * l] = f0;
+		e[2 * l + 1] = f1;
+	}
+}
+
+// MLP forward from smem weights; returns raw outputs.
+GBRT_GHD void mlp_forward(const float *__restrict__ W, const float e[kGuideIn], float h1[kGuideHidden],
+                                            float h2[kGuideHidden], float o[kGuideOut])
+{
+	for(int j = 0; j < kGuideHidden; ++j)
+	{
+		float acc = W[kOffB1 + j];
+		const float *w = W + kOffW1 + j * kGuideIn;
+#pragma unroll
+		for(int i = 0; i < kGuideIn; ++i) acc += w[i] * e[i];
+		h1[j] = fmaxf(acc, 0.f);
+	}
+	for(int j = 0; j < kGuideHidden; ++j)
+	{
+		float acc = W[kOffB2 + j];
+		const float *w = W + kOffW2 + j * kGuideHidden;
+#pragma unroll 16
+		for(int i = 0; i < kGuideHidden; ++i) acc += w[i] * h1[i];
+		h2[j] = fmaxf(acc, 0.f);
+	}
+	for(int j = 0; j < kGuideOut; ++j)
+	{
+		float acc = W[kOffB3 + j];
+		const float *w = W + kOffW3 + j * kGuideHidden;
+#pragma unroll 16
+		for(int i = 0; i < kGuideHidden; ++i) acc += w[i] * h2[i];
+		o[j] = acc;
+	}
+}
+
+__global__ void __launch_bounds__(kEvalThreads) k_guide_eval(GuideGrid g, const float *__restrict__ table, const float *__restrict__ mlp,
+                                                             const float *__restrict__ pos, uint32_t n, const uint32_t *__restrict__ n_dev,
+                                                             float *__restrict__ lobes)
+{
+	__shared__ float W[kMlpParams];
+	for(int i = threadIdx.x; i < kMlpParams; i += blockDim.x) W[i] = mlp[i];
+	__syncthreads();
+	const uint32_t count = n_dev ? min(*n_dev, n) : n;
+	for(uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < count; s += gridDim.x * blockDim.x)
+	{
+		const float p[3] = {pos[3ull * s], pos[3ull * s + 1], pos[3ull * s + 2]};
+		float e[kGuideIn], h1[kGuideHidden], h2[kGuideHidden], o[kGuideOut];
+		encode(g, table, p, e, nullptr, nullptr);
+		mlp_forward(W, e, h1, h2, o);
+		float lo[kGuideOut];
+		raw_to_lobes(o, lo);
+		float4 *out = reinterpret_cast<float4 *>(lobes + static_cast<size_t>(kGuideOut) * s);
+		for(int k = 0; k < kGuideOut / 4; ++k) out[k] = make_float4(lo[4 * k], lo[4 * k + 1], lo[4 * k + 2], lo[4 * k + 3]);
+	}
+}
+
+// d(-log q(w))/d(raw outputs), scaled by c.
+__device__ __forceinline__ float head_grad(const float o[kGuideOut], const float w[3], float c, float d[kGuideOut])
+{
+	float lob[kGuideOut];
+	raw_to_lobes(o, lob);
+	float logf_k[kGuideLobes], lmax = -1e30f;
+	for(int k = 0; k < kGuideLobes; ++k)
+	{
+		logf_k[k] = logf(lob[5 * k + 4]) + vmf_log_pdf(&lob[5 * k], lob[5 * k + 3], w);
+		lmax = fmaxf(lmax, logf_k[k]);
+	}
+	float sum = 0.f;
+	for(int k = 0; k < kGuideLobes; ++k) sum += expf(logf_k[k] - lmax);
+	const float logq = lmax + logf(sum);
+	for(int k = 0; k < kGuideLobes; ++k)
+	{
+		const float r = expf(logf_k[k] - logq);          // responsibility
+		const float wk = lob[5 * k + 4];
+		const float kap = lob[5 * k + 3];
+		const float *mu = &lob[5 * k];
+		const float mw = mu[0] * w[0] + mu[1] * w[1] + mu[2] * w[2];
+		d[5 * k + 4] = c * (wk - r);
+		const float e2 = expf(-2.f * kap);
+		const float dlogf_dk = 1.f / kap - 2.f * e2 / (1.f - e2) + (mw - 1.f);
+		const float a = o[5 * k + 3];
+		const float sp = softplus(a) + kKappaMin;
+		const float dk_da = sp < kKappaMax ? 1.f / (1.f + expf(-a)) : 0.f;
+		d[5 * k + 3] = -c * r * dlogf_dk * dk_da;
+		const float m0 = o[5 * k], m1 = o[5 * k + 1], m2 = o[5 * k + 2];
+		const float len = sqrtf(m0 * m0 + m1 * m1 + m2 * m2);
+		if(len > 1e-20f)
+		{
+			const float s = -c * r * kap / len;
+			d[5 * k + 0] = s * (w[0] - mw * mu[0]);
+			d[5 * k + 1] = s * (w[1] - mw * mu[1]);
+			d[5 * k + 2] = s * (w[2] - mw * mu[2]);
+		}
+		else d[5 * k + 0] = d[5 * k + 1] = d[5 * k + 2] = 0.f;
+	}
+	return -c * logq;
+}
+
+// One block: kGradChunks chunks of 64 records.  Weight gradients accumulate
+// in shared memory (each entry owned by one thread) and are written once per
+// block; hash-grid gradients are scattered with atomics.
+__global__ void __launch_bounds__(kGradThreads) k_guide_grad(GuideGrid g, const float *__restrict__ table, const float *__restrict__ mlp,
+                                                             const float *__restrict__ rec, uint32_t n, const float *__restrict__ wsum,
+                                                             float *__restrict__ partial, float *__restrict__ grid_grad,
+                                                             float *__restrict__ loss_out)
+{
+	extern __shared__ float sm[];
+	float *W = sm;                                        // kMlpParams
+	float *G = W + kMlpParams;                            // kMlpParams, block gradient
+	float *E = G + kMlpParams;                            // [64][32]
+	float *H1 = E + kGradThreads * kGuideIn;              // [64][64]
+	float *H2 = H1 + kGradThreads * kGuideHidden;         // [64][64]
+	float *D1 = H2 + kGradThreads * kGuideHidden;         // [64][64] dL/d(pre-act 1)
+	float *D2 = D1 + kGradThreads * kGuideHidden;         // [64][64]
+	float *D3 = D2 + kGradThreads * kGuideHidden;         // [64][40]
+	const int t = threadIdx.x;
+	const float inv_norm = *wsum > 0.f ? 1.f / *wsum : 0.f;
+	for(int i = t; i < kMlpParams; i += blockDim.x) { W[i] = mlp[i]; G[i] = 0.f; }
+	__syncthreads();
+	float loss = 0.f;
+	for(int chunk = 0; chunk < kGradChunks; ++chunk)
+	{
+		const uint32_t r = (blockIdx.x * kGradChunks + chunk) * kGradThreads + t;
+		const bool live = r < n;
+		float e[kGuideIn], h1[kGuideHidden], h2[kGuideHidden], o[kGuideOut], d3[kGuideOut];
+		uint32_t cidx[kGuideLevels * 8];
+		float cw[kGuideLevels * 8];
+		if(live)
+		{
+			const float *q = rec + 8ull * r;   // pos xyz, dir xyz, weight, pad
+			const float p[3] = {q[0], q[1], q[2]};
+			const float w[3] = {q[3], q[4], q[5]};
+			encode(g, table, p, e, cidx, cw);
+			mlp_forward(W, e, h1, h2, o);
+			loss += head_grad(o, w, q[6] * inv_norm, d3);
+		}
+		else
+		{
+			for(int i = 0; i < kGuideIn; ++i) e[i] = 0.f;
+			for(int i = 0; i < kGuideHidden; ++i) h1[i] = h2[i] = 0.f;
+			for(int i = 0; i < kGuideOut; ++i) d3[i] = 0.f;
+		}
+		// backward through the MLP
+		float d2[kGuideHidden], d1[kGuideHidden];
+		for(int i = 0; i < kGuideHidden; ++i)
+		{
+			float acc = 0.f;
+			for(int j = 0; j < kGuideOut; ++j) acc += W[kOffW3 + j * kGuideHidden + i] * d3[j];
+			d2[i] = h2[i] > 0.f ? acc : 0.f;
+		}
+		for(int i = 0; i < kGuideHidden; ++i)
+		{
+			float acc = 0.f;
+			for(int j = 0; j < kGuideHidden; ++j) acc += W[kOffW2 + j * kGuideHidden + i] * d2[j];
+			d1[i] = h1[i] > 0.f ? acc : 0.f;
+		}
+		if(live)
+		{
+			// encoding gradient -> hash grid (trilinear weights)
+			for(int l = 0; l < kGuideLevels; ++l)
+			{
+				float de0 = 0.f, de1 = 0.f;
+				for(int j = 0; j < kGuideHidden; ++j)
+				{
+					de0 += W[kOffW1 + j * kGuideIn + 2 * l] * d1[j];
+					de1 += W[kOffW1 + j * kGuideIn + 2 * l + 1] * d1[j];
+				}
+				for(int c = 0; c < 8; ++c)
+				{
+					const float wc = cw[l * 8 + c];
+					const size_t off = cidx[l * 8 + c];
+					atomicAdd(grid_grad + 2 * off, wc * de0);
+					atomicAdd(grid_grad + 2 * off + 1, wc * de1);
+				}
+			}
+		}
+		for(int i = 0; i < kGuideIn; ++i) E[t * kGuideIn + i] = e[i];
+		for(int i = 0; i < kGuideHidden; ++i)
+		{
+			H1[t * kGuideHidden + i] = h1[i]; H2[t * kGuideHidden + i] = h2[i];
+			D1[t * kGuideHidden + i] = d1[i]; D2[t * kGuideHidden + i] = d2[i];
+		}
+		for(int i = 0; i < kGuideOut; ++i) D3[t * kGuideOut + i] = d3[i];
+		__syncthreads();
+		// weight gradients: sum over the 64 records of the chunk
+		for(int idx = t; idx < kMlpParams; idx += kGradThreads)
+		{
+			float acc = 0.f;
+			if(idx < kOffB1)      { const int j = idx / kGuideIn, i = idx % kGuideIn; for(int s = 0; s < kGradThreads; ++s) acc += D1[s * kGuideHidden + j] * E[s * kGuideIn + i]; }
+			else if(idx < kOffW2) { const int j = idx - kOffB1; for(int s = 0; s < kGradThreads; ++s) acc += D1[s * kGuideHidden + j]; }
+			else if(idx < kOffB2) { const int k = idx - kOffW2, j = k / kGuideHidden, i = k % kGuideHidden; for(int s = 0; s < kGradThreads; ++s) acc += D2[s * kGuideHidden + j] * H1[s * kGuideHidden + i]; }
+			else if(idx < kOffW3) { const int j = idx - kOffB2; for(int s = 0; s < kGradThreads; ++s) acc += D2[s * kGuideHidden + j]; }
+			else if(idx < kOffB3) { const int k = idx - kOffW3, j = k / kGuideHidden, i = k % kGuideHidden; for(int s = 0; s < kGradThreads; ++s) acc += D3[s * kGuideOut + j] * H2[s * kGuideHidden + i]; }
+			else                  { const int j = idx - kOffB3; for(int s = 0; s < kGradThreads; ++s) acc += D3[s * kGuideOut + j]; }
+			G[idx] += acc;
+		}
+		__syncthreads();
+	}
+	for(int i = t; i < kMlpParams; i += blockDim.x) partial[static_cast<size_t>(blockIdx.x) * kMlpParams + i] = G[i];
+	for(int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
+	if((t & 31) == 0) atomicAdd(loss_out, loss);
+}
+
+__global__ void k_weight_sum(const float *__restrict__ rec, uint32_t n, float *__restrict__ out)
+{
+	float acc = 0.f;
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) acc += rec[8ull * i + 6];
+	for(int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+	if((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
+__global__ void k_reduce(const float *__restrict__ partial, int nblk, float *__restrict__ grad)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= kMlpParams) return;
+	float acc = 0.f;
+	for(int b = 0; b < nblk; ++b) acc += partial[static_cast<size_t>(b) * kMlpParams + i];
+	grad[i] = acc;
+}
+
+__global__ void k_adam(float *__restrict__ p, float *__restrict__ g, float *__restrict__ m, float *__restrict__ v, size_t n,
+                       float lr, float b1, float b2, float eps, float c1, float c2, int sparse)
+{
+	for(size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
+	{
+		const float gi = g[i];
+		if(sparse && gi == 0.f) continue;     // untouched hash entries keep their moments
+		const float mi = b1 * m[i] + (1.f - b1) * gi;
+		const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+		m[i] = mi; v[i] = vi;
+		p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+		g[i] = 0.f;
+	}
+}
+
+} // namespace
+
+struct gbrt_guide {
+	int device = 0;
+	GuideGrid grid{};
+	gbrt_guide_params params{};
+	size_t table_floats = 0;
+	float *table = nullptr, *table_g = nullptr, *table_m = nullptr, *table_v = nullptr;
+	float *mlp = nullptr, *mlp_g = nullptr, *mlp_m = nullptr, *mlp_v = nullptr;
+	float *partial = nullptr;
+	size_t partial_blocks = 0;
+	float *loss = nullptr;    // [0] loss, [1] record weight sum
+	int step = 0;
+	int n_sm = 0;
+};
+
+namespace {
+
+int guide_alloc(gbrt_guide *G)
+{
+	const size_t T = G->table_floats;
+	float **bufs[] = {&G->table, &G->table_g, &G->table_m, &G->table_v};
+	for(float **b : bufs) GBRT_CK(cudaMalloc(b, T * sizeof(float)));
+	float **mb[] = {&G->mlp, &G->mlp_g, &G->mlp_m, &G->mlp_v};
+	for(float **b : mb) GBRT_CK(cudaMalloc(b, kMlpParams * sizeof(float)));
+	GBRT_CK(cudaMalloc(&G->loss, 2 * sizeof(float)));
+	return GBRT_OK;
+}
+
+size_t grad_smem_bytes()
+{
+	return sizeof(float) * (2 * kMlpParams + kGradThreads * (kGuideIn + 4 * kGuideHidden + kGuideOut));
+}
+
+} // namespace
+
+namespace {
+GuideGrid make_grid(const float bound[6], const gbrt_guide_params &p);
+gbrt_guide_params defaults(const gbrt_guide_params *params);
+} // namespace
+
+extern "C" {
+
+int gbrt_guide_create(const float bound[6], const gbrt_guide_params *params, gbrt_guide **out)
+{
+	if(!out || !bound) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_create: NULL argument");
+	*out = nullptr;
+	const gbrt_guide_params p = defaults(params);
+	if(p.log2_table < 8 || p.log2_table > 24) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_create: log2_table %u out of [8, 24]", p.log2_table);
+	gbrt_guide *G = new gbrt_guide();
+	G->params = p;
+	G->grid = make_grid(bound, p);
+	G->table_floats = static_cast<size_t>(kGuideLevels) * kGuideFeatures << p.log2_table;
+	cudaGetDevice(&G->device);
+	cudaDeviceGetAttribute(&G->n_sm, cudaDevAttrMultiProcessorCount, G->device);
+	if(int rc = guide_alloc(G)) { gbrt_guide_destroy(G); return rc; }
+	// init: table U[-1e-4, 1e-4], MLP uniform(+-sqrt(6/fan_in)) (He), zero biases
+	std::mt19937 rng(p.seed ? p.seed : 1234u);
+	std::vector<float> tab(G->table_floats);
+	std::uniform_real_distribution<float> ut(-1e-4f, 1e-4f);
+	for(auto &x : tab) x = ut(rng);
+	std::vector<float> w(kMlpParams, 0.f);
+	auto fill = [&](int off, int rows, int cols, float scale) {
+		std::uniform_real_distribution<float> u(-scale, scale);
+		for(int i = 0; i < rows * cols; ++i) w[off + i] = u(rng);
+	};
+	fill(kOffW1, kGuideHidden, kGuideIn, std::sqrt(6.f / kGuideIn));
+	fill(kOffW2, kGuideHidden, kGuideHidden, std::sqrt(6.f / kGuideHidden));
+	fill(kOffW3, kGuideOut, kGuideHidden, 0.5f * std::sqrt(6.f / kGuideHidden));
+	// mean-direction biases spread over the sphere, small kappa, equal weights
+	for(int k = 0; k < kGuideLobes; ++k)
+	{
+		const float z = 1.f - 2.f * (k + 0.5f) / kGuideLobes, phi = 2.399963f * k, r = std::sqrt(std::max(0.f, 1.f - z * z));
+		w[kOffB3 + 5 * k + 0] = r * std::cos(phi);
+		w[kOffB3 + 5 * k + 1] = r * std::sin(phi);
+		w[kOffB3 + 5 * k + 2] = z;
+	}
+	cudaError_t e;
+	if((e = cudaMemcpy(G->table, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess ||
+	   (e = cudaMemcpy(G->mlp, w.data(), kMlpParams * 4, cudaMemcpyHostToDevice)) != cudaSuccess ||
+	   (e = cudaMemset(G->table_g, 0, G->table_floats * 4)) != cudaSuccess || (e = cudaMemset(G->table_m, 0, G->table_floats * 4)) != cudaSuccess ||
+	   (e = cudaMemset(G->table_v, 0, G->table_floats * 4)) != cudaSuccess || (e = cudaMemset(G->mlp_g, 0, kMlpParams * 4)) != cudaSuccess ||
+	   (e = cudaMemset(G->mlp_m, 0, kMlpParams * 4)) != cudaSuccess || (e = cudaMemset(G->mlp_v, 0, kMlpParams * 4)) != cudaSuccess)
+	{
+		gbrt_guide_destroy(G);
+		return gbrt_set_error(GBRT_ERR_CUDA, "gbrt_guide_create: %s", cudaGetErrorString(e));
+	}
+	*out = G;
+	return GBRT_OK;
+}
+
+int gbrt_guide_destroy(gbrt_guide *G)
+{
+	if(!G) return GBRT_OK;
+	void *ptrs[] = {G->table, G->table_g, G->table_m, G->table_v, G->mlp, G->mlp_g, G->mlp_m, G->mlp_v, G->partial, G->loss};
+	for(void *p : ptrs) if(p) cudaFree(p);
+	delete G;
+	return GBRT_OK;
+}
+
+int gbrt_guide_get_params(const gbrt_guide *G, float *mlp_out, float *table_out)
+{
+	if(!G) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_get_params: NULL");
+	if(mlp_out) GBRT_CK(cudaMemcpy(mlp_out, G->mlp, kMlpParams * 4, cudaMemcpyDeviceToHost));
+	if(table_out) GBRT_CK(cudaMemcpy(table_out, G->table, G->table_floats * 4, cudaMemcpyDeviceToHost));
+	return GBRT_OK;
+}
+
+int gbrt_guide_set_params(gbrt_guide *G, const float *mlp, const float *table)
+{
+	if(!G) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_set_params: NULL");
+	if(mlp) GBRT_CK(cudaMemcpy(G->mlp, mlp, kMlpParams * 4, cudaMemcpyHostToDevice));
+	if(table) GBRT_CK(cudaMemcpy(G->table, table, G->table_floats * 4, cudaMemcpyHostToDevice));
+	return GBRT_OK;
+}
+
+int gbrt_guide_eval(gbrt_guide *G, const float *pos_dev, uint32_t n, float *lobes_dev, void *stream)
+{
+	if(!G || (n && (!pos_dev || !lobes_dev))) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_eval: NULL argument");
+	if(n == 0) return GBRT_OK;
+	const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + kEvalThreads - 1) / kEvalThreads, static_cast<size_t>(G->n_sm) * 8));
+	k_guide_eval<<<grid, kEvalThreads, 0, static_cast<cudaStream_t>(stream)>>>(G->grid, G->table, G->mlp, pos_dev, n, nullptr, lobes_dev);
+	GBRT_CK(cudaGetLastError());
+	return GBRT_OK;
+}
+
+// Gradient of the batch loss into the gradient buffers (no update).
+int gbrt_guide_grad(gbrt_guide *G, const float *records_dev, uint32_t n, float *loss_out, void *stream)
+{
+	if(!G || (n && !records_dev)) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_grad: NULL argument");
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	const size_t per_block = static_cast<size_t>(kGradThreads) * kGradChunks;
+	const size_t nblk = std::max<size_t>(1, (n + per_block - 1) / per_block);
+	if(nblk > G->partial_blocks)
+	{
+		if(G->partial) cudaFree(G->partial);
+		GBRT_CK(cudaMalloc(&G->partial, nblk * kMlpParams * sizeof(float)));
+		G->partial_blocks = nblk;
+	}
+	static bool attr = false;
+	if(!attr) { cudaFuncSetAttribute(k_guide_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(grad_smem_bytes())); attr = true; }
+	GBRT_CK(cudaMemsetAsync(G->loss, 0, 2 * sizeof(float), s));
+	k_weight_sum<<<std::max(1, std::min(G->n_sm * 4, static_cast<int>((n + 255) / 256))), 256, 0, s>>>(records_dev, n, G->loss + 1);
+	k_guide_grad<<<static_cast<unsigned>(nblk), kGradThreads, grad_smem_bytes(), s>>>(G->grid, G->table, G->mlp, records_dev, n, G->loss + 1,
+	                                                                                  G->partial, G->table_g, G->loss);
+	k_reduce<<<(kMlpParams + 255) / 256, 256, 0, s>>>(G->partial, static_cast<int>(nblk), G->mlp_g);
+	GBRT_CK(cudaGetLastError());
+	if(loss_out)
+	{
+		GBRT_CK(cudaMemcpyAsync(loss_out, G->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+		GBRT_CK(cudaStreamSynchronize(s));
+	}
+	return GBRT_OK;
+}
+
+int gbrt_guide_get_grads(const gbrt_guide *G, float *mlp_grad, float *table_grad)
+{
+	if(!G) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_get_grads: NULL");
+	if(mlp_grad) GBRT_CK(cudaMemcpy(mlp_grad, G->mlp_g, kMlpParams * 4, cudaMemcpyDeviceToHost));
+	if(table_grad) GBRT_CK(cudaMemcpy(table_grad, G->table_g, G->table_floats * 4, cudaMemcpyDeviceToHost));
+	return GBRT_OK;
+}
+
+int gbrt_guide_step(gbrt_guide *G, const float *records_dev, uint32_t n, float *loss_out, void *stream)
+{
+	if(int rc = gbrt_guide_grad(G, records_dev, n, loss_out, stream)) return rc;
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	G->step += 1;
+	const float b1 = 0.9f, b2 = 0.99f;
+	const float c1 = 1.f - std::pow(b1, static_cast<float>(G->step)), c2 = 1.f - std::pow(b2, static_cast<float>(G->step));
+	const float lr = G->params.learning_rate;
+	k_adam<<<64, 256, 0, s>>>(G->mlp, G->mlp_g, G->mlp_m, G->mlp_v, kMlpParams, lr, b1, b2, 1e-8f, c1, c2, 0);
+	const unsigned gblocks = static_cast<unsigned>(std::min<size_t>((G->table_floats + 255) / 256, static_cast<size_t>(G->n_sm) * 16));
+	k_adam<<<gblocks, 256, 0, s>>>(G->table, G->table_g, G->table_m, G->table_v, G->table_floats, lr, b1, b2, 1e-15f, c1, c2, 1);
+	GBRT_CK(cudaGetLastError());
+	return GBRT_OK;
+}
+
+int gbrt_guide_info(const gbrt_guide *G, uint32_t *n_mlp_params, uint64_t *n_table_params)
+{
+	if(!G) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_info: NULL");
+	if(n_mlp_params) *n_mlp_params = kMlpParams;
+	if(n_table_params) *n_table_params = G->table_floats;
+	return GBRT_OK;
+}
+
+} // extern "C"
+
+// Host build of the same forward pass (no CUDA calls): tests compare it with
+// the FP64 oracle without a GPU, and with the device kernel on one.
+namespace {
+GuideGrid make_grid(const float bound[6], const gbrt_guide_params &p)
+{
+	GuideGrid g{};
+	for(int a = 0; a < 3; ++a)
+	{
+		const float ext = bound[3 + a] - bound[a];
+		g.lo[a] = bound[a];
+		g.inv_ext[a] = ext > 0.f ? 1.f / ext : 0.f;
+	}
+	g.log2_table = p.log2_table;
+	const double b = std::exp((std::log(static_cast<double>(p.max_resolution)) - std::log(static_cast<double>(p.base_resolution))) / (kGuideLevels - 1));
+	for(int l = 0; l < kGuideLevels; ++l)
+	{
+		g.res[l] = std::floor(static_cast<float>(static_cast<double>(p.base_resolution) * std::pow(b, l)));
+		const double cells = std::pow(g.res[l] + 1.0, 3.0);
+		g.dense[l] = cells <= static_cast<double>(1u << p.log2_table) ? 1u : 0u;
+	}
+	return g;
+}
+gbrt_guide_params defaults(const gbrt_guide_params *params)
+{
+	gbrt_guide_params p{};
+	if(params) p = *params;
+	if(p.log2_table == 0) p.log2_table = 19;
+	if(p.base_resolution <= 0.f) p.base_resolution = 16.f;
+	if(p.max_resolution <= 0.f) p.max_resolution = 2048.f;
+	if(p.learning_rate <= 0.f) p.learning_rate = 5e-3f;
+	return p;
+}
+} // namespace
+
+extern "C" int gbrt_guide_forward_host(const float bound[6], const gbrt_guide_params *params, const float *mlp, const float *table,
+                                       const float *pos, uint32_t n, float *lobes)
+{
+	if(!bound || !mlp || !table || (n && (!pos || !lobes))) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_forward_host: NULL argument");
+	const gbrt_guide_params p = defaults(params);
+	if(p.log2_table < 8 || p.log2_table > 24) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_forward_host: log2_table out of range");
+	const GuideGrid g = make_grid(bound, p);
+	for(uint32_t s = 0; s < n; ++s)
+	{
+		float e[kGuideIn], h1[kGuideHidden], h2[kGuideHidden], o[kGuideOut];
+		encode(g, table, pos + 3ull * s, e, nullptr, nullptr);
+		mlp_forward(mlp, e, h1, h2, o);
+		raw_to_lobes(o, lobes + static_cast<size_t>(kGuideOut) * s);
+	}
+	return GBRT_OK;
+}
+
+// Used by the path tracer: lobes for the hit points of a queue.
+int gbrt_guide_eval_queue(gbrt_guide *G, const float *pos_dev, uint32_t cap, const uint32_t *count_dev, float *lobes_dev, cudaStream_t s)
+{
+	const unsigned grid = static_cast<unsigned>(std::min<size_t>((cap + kEvalThreads - 1) / kEvalThreads, static_cast<size_t>(G->n_sm) * 8));
+	k_guide_eval<<<std::max(1u, grid), kEvalThreads, 0, s>>>(G->grid, G->table, G->mlp, pos_dev, cap, count_dev, lobes_dev);
+	GBRT_CK(cudaGetLastError());
+	return GBRT_OK;
+}

@@ -23,6 +23,7 @@
 // (material_shiny_diffuse.cc:432).
 #include "traverse_core.cuh"
 #include "sampling.cuh"
+#include "guide_device.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -60,6 +61,7 @@ struct DevLight {
 
 constexpr int kThreads = 128;
 constexpr uint32_t kDead = 0xFFFFFFFFu;
+constexpr uint32_t kMaxBatch = 1u << 18;   // largest guide training batch
 constexpr float kRayMinDist = 0.00005f;   // Accelerator::min_raydist_ (accelerator.h:85)
 constexpr float kShadowBias = 0.0005f;    // Accelerator::shadow_bias_ (accelerator.h:86)
 constexpr float kPi = 3.14159265358979323846f;
@@ -77,6 +79,11 @@ struct Params {
 	float d1;
 	uint32_t n_lights;
 	int fp64;
+	int guiding;          // sample continuation directions with the guide (one-sample MIS)
+	float alpha;          // probability of the guide technique
+	int record;           // write training records
+	uint32_t rec_stride;  // record slots per path (= bounces)
+	int radiance_target;  // train on incident radiance instead of the product with the BSDF
 };
 
 struct Work {
@@ -88,8 +95,20 @@ struct Work {
 	float4 *s_ray;
 	float4 *s_col;
 	uint32_t *s_pix;
-	uint32_t *count;            // [0],[1] ray queues, [2] shadow queue
+	uint32_t *s_path;
+	uint32_t *count;            // [0],[1] ray queues, [2] shadow queue, [3] training records
 	unsigned long long *stats;  // [0] extension rays, [1] shadow rays traced
+	// path guiding (allocated only when a guide is attached)
+	float *hitpos;              // [queue][3] hit points for the network
+	float *lobes;               // [queue][40] mixture parameters
+	float4 *p_sum;              // [path] contributions added so far (recording)
+	float4 *r_pos;              // [path * stride + vertex] position xyz, mixture pdf
+	float4 *r_dir;              // direction xyz
+	float4 *r_thr;              // throughput after sampling
+	float4 *r_pre;              // contributions before the next vertex
+	uint32_t *r_valid;
+	float *train;               // [n][8] training records
+	uint32_t train_cap;
 };
 
 struct SceneDev {
@@ -365,6 +384,72 @@ __device__ __forceinline__ bool mat_sample(const Surface &s, const float wo[3], 
 	return true;
 }
 
+// Sample colour x weight that Material::sample would return for a given
+// direction wi (both sampling branches of glossy give the same function of
+// wi), used for directions drawn from the guide.
+__device__ __forceinline__ void bsdf_eval_at(const Surface &s, const float wo[3], const float wi[3], uint32_t flags, float fw[3])
+{
+	fw[0] = fw[1] = fw[2] = 0.f;
+	float n[3];
+	face_forward(s, wo, n);
+	if(dot3(wi, n) <= 0.f) return;
+	const float cos_ng_wo = dot3(s.ng, wo), cos_ng_wi = dot3(s.ng, wi);
+	if(s.m->type == GBRT_MAT_SHINYDIFFUSE)
+	{
+		if(!(xm(cos_ng_wo, cos_ng_wi) > 0.f)) return;
+		const float pdf = fabsf(dot3(wi, n));
+		const float w = __fdiv_rn(fabsf(dot3(wi, s.n)), xa(xm(pdf, 0.99f), 0.01f));
+		for(int k = 0; k < 3; ++k) fw[k] = xm(s.m->col[k], w);
+		return;
+	}
+	if(s.m->type != GBRT_MAT_GLOSSY || xm(cos_ng_wo, cos_ng_wi) < 0.f) return;
+	const DevMaterial &m = *s.m;
+	const float pd = m.p_diffuse;
+	const bool use_glossy = m.as_diffuse ? (flags & BF_DIFFUSE) != 0u : (flags & BF_GLOSSY) != 0u;
+	const bool use_diffuse = m.with_diffuse && (flags & BF_DIFFUSE);
+	const float wi_n = fabsf(dot3(wi, n)), wo_n = fabsf(dot3(wo, n));
+	float h[3] = {xa(wi[0], wo[0]), xa(wi[1], wo[1]), xa(wi[2], wo[2])};
+	normalize3(h);
+	const float cos_wo_h = dot3(wo, h), cos_wi_h = fabsf(dot3(wi, h)), cos_n_h = dot3(n, h);
+	float pdf = use_diffuse ? wi_n : 0.f, glossy = 0.f;
+	if(use_glossy)
+	{
+		const float bp = blinn_pdf(cos_n_h, cos_wo_h, m.exponent);
+		pdf = use_diffuse ? xa(xm(pdf, pd), xm(bp, xs(1.f, pd))) : bp;
+		glossy = __fdiv_rn(xm(blinn_d(cos_n_h, m.exponent), schlick(cos_wi_h, m.m_glossy)), as_divisor(cos_wi_h, wo_n, wi_n));
+	}
+	const float dr = use_diffuse ? diffuse_reflect_factor(wi_n, wo_n, m.m_glossy, m.m_diffuse) : 0.f;
+	const float w = __fdiv_rn(wi_n, xa(xm(pdf, 0.99f), 0.01f));
+	for(int k = 0; k < 3; ++k) fw[k] = xm(xa(xm(glossy, m.col[k]), xm(dr, m.col2[k])), w);
+}
+
+// Solid-angle density of the directions Material::sample draws: cosine
+// hemisphere (1/pi normalised) and, for glossy, the Blinn half-vector
+// density (e+1)/(2 pi) cos^e / (4 |wo.h|), mixed by the diffuse pick
+// probability.
+__device__ __forceinline__ float bsdf_true_pdf(const Surface &s, const float wo[3], const float wi[3], uint32_t flags)
+{
+	float n[3];
+	face_forward(s, wo, n);
+	const float c = dot3(wi, n);
+	if(c <= 0.f) return 0.f;
+	if(s.m->type == GBRT_MAT_SHINYDIFFUSE) return c * kInvPi;
+	if(s.m->type != GBRT_MAT_GLOSSY) return 0.f;
+	const DevMaterial &m = *s.m;
+	const bool use_glossy = m.as_diffuse ? (flags & BF_DIFFUSE) != 0u : (flags & BF_GLOSSY) != 0u;
+	const bool use_diffuse = m.with_diffuse && (flags & BF_DIFFUSE);
+	const float pd = use_diffuse ? (use_glossy ? m.p_diffuse : 1.f) : 0.f;
+	float pg = 0.f;
+	if(use_glossy)
+	{
+		float h[3] = {wi[0] + wo[0], wi[1] + wo[1], wi[2] + wo[2]};
+		normalize3(h);
+		const float ch = dot3(h, n), woh = dot3(wo, h);
+		if(ch > 0.f && woh > 0.f) pg = (m.exponent + 1.f) * (0.5f * kInvPi) * powf(ch, m.exponent) / (4.f * woh);
+	}
+	return pd * c * kInvPi + (1.f - pd) * pg;
+}
+
 // LightMaterial::emit (material_light.cc:82-87)
 __device__ __forceinline__ bool mat_emit(const Surface &s, const float wo[3], float out[3])
 {
@@ -372,6 +457,12 @@ __device__ __forceinline__ bool mat_emit(const Surface &s, const float wo[3], fl
 	if(dot3(wo, s.n) <= 0.f && !s.m->double_sided) return false;
 	for(int k = 0; k < 3; ++k) out[k] = s.m->col[k];
 	return true;
+}
+
+__device__ __forceinline__ void path_sum_add(const Work &W, uint32_t path, float r, float g, float b)
+{
+	float *p = reinterpret_cast<float *>(W.p_sum + path);
+	atomicAdd(p, r); atomicAdd(p + 1, g); atomicAdd(p + 2, b);
 }
 
 __device__ __forceinline__ void film_add(float *film, double *film64, uint32_t pixel, float r, float g, float b)
@@ -396,6 +487,8 @@ struct ShadowWriter {
 	float4 *ray;
 	float4 *col;
 	uint32_t *pix;
+	uint32_t *pth;
+	uint32_t path;
 	uint32_t slot, end;
 	__device__ void put(const float o[3], float tmin, const float d[3], float tmax, uint32_t pixel, const float c[3])
 	{
@@ -404,6 +497,7 @@ struct ShadowWriter {
 		ray[2ull * slot + 1] = make_float4(d[0], d[1], d[2], tmax);
 		col[slot] = make_float4(c[0], c[1], c[2], 0.f);
 		pix[slot] = pixel;
+		pth[slot] = path;
 		++slot;
 	}
 	__device__ void close()
@@ -532,6 +626,11 @@ __global__ void __launch_bounds__(kThreads) k_camera(Camera cam, Params P, Work 
 		W.p_si[s] = si;
 		W.p_thr[s] = make_float4(1.f, 1.f, 1.f, 0.f);
 		W.p_state[s] = 0u;
+		if(W.p_sum)
+		{
+			W.p_sum[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+			for(uint32_t k = 0; k < P.rec_stride; ++k) W.r_valid[static_cast<size_t>(s) * P.rec_stride + k] = 0u;
+		}
 		W.q_ray[0][2ull * s] = make_float4(cam.from[0], cam.from[1], cam.from[2], 0.f);
 		W.q_ray[0][2ull * s + 1] = make_float4(d[0], d[1], d[2], -1.f);
 		W.q_path[0][s] = s;
@@ -544,7 +643,7 @@ __global__ void __launch_bounds__(kThreads) k_camera(Camera cam, Params P, Work 
 }
 
 __global__ void __launch_bounds__(kThreads) k_extend(gbrt::BvhView bv, const float4 *__restrict__ rays, const uint32_t *__restrict__ count,
-                                                     float4 *__restrict__ hits)
+                                                     float4 *__restrict__ hits, float *__restrict__ hitpos)
 {
 	const uint32_t n = *count;
 	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -552,6 +651,12 @@ __global__ void __launch_bounds__(kThreads) k_extend(gbrt::BvhView bv, const flo
 		const float4 a = rays[2ull * i], b = rays[2ull * i + 1];
 		const gbrt::Hit h = gbrt::trace_ray<false>(bv, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w);
 		hits[i] = make_float4(__int_as_float(h.prim), h.t, h.u, h.v);
+		if(hitpos)
+		{
+			hitpos[3ull * i] = xa(a.x, xm(h.t, b.x));
+			hitpos[3ull * i + 1] = xa(a.y, xm(h.t, b.y));
+			hitpos[3ull * i + 2] = xa(a.z, xm(h.t, b.z));
+		}
 	}
 }
 
@@ -601,6 +706,14 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				thr[0] = t4.x; thr[1] = t4.y; thr[2] = t4.z;
 			}
 		}
+		// the previous vertex's record: incident radiance along its sampled
+		// direction = what the path adds from here on
+		if(hit && W.p_sum && k >= 1 && k - 1 < P.rec_stride && W.r_valid[static_cast<size_t>(path) * P.rec_stride + (k - 1)] == 2u)
+		{
+			const size_t slot = static_cast<size_t>(path) * P.rec_stride + (k - 1);
+			W.r_pre[slot] = W.p_sum[path];
+			W.r_valid[slot] = 1u;     // complete
+		}
 		// --- decide this vertex's work, count its shadow rays -----------------
 		bool do_nee_all = false, do_nee_one = false, rr_dead = false;
 		float nee_weight[3] = {0.f, 0.f, 0.f};
@@ -610,7 +723,11 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 			if(k == 0)
 			{
 				float e[3];
-				if((s.m->flags & BF_EMIT) && sub == 0 && mat_emit(s, wo, e)) film_add(film, film64, pixel, e[0], e[1], e[2]);
+				if((s.m->flags & BF_EMIT) && sub == 0 && mat_emit(s, wo, e))
+				{
+					film_add(film, film64, pixel, e[0], e[1], e[2]);
+					if(W.p_sum) path_sum_add(W, path, e[0], e[1], e[2]);
+				}
 				do_nee_all = (s.m->flags & BF_DIFFUSE) && sub == 0;
 				nee_weight[0] = nee_weight[1] = nee_weight[2] = 1.f;
 				if(do_nee_all)
@@ -638,7 +755,11 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 					}
 					float e[3];
 					if((k == 1 && (s.m->flags & BF_EMIT)) || (k >= 2 && (mat1 & BF_EMIT) && caustic))
-						if(mat_emit(s, wo, e)) film_add(film, film64, pixel, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
+						if(mat_emit(s, wo, e))
+						{
+							film_add(film, film64, pixel, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
+							if(W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
+						}
 				}
 			}
 		}
@@ -653,7 +774,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 		uint32_t wbase = 0;
 		if(lane == 31 && total) wbase = atomicAdd(W.count + 2, total);
 		wbase = __shfl_sync(0xffffffffu, wbase, 31);
-		ShadowWriter sw{W.s_ray, W.s_col, W.s_pix, wbase + incl - n_shadow, wbase + incl};
+		ShadowWriter sw{W.s_ray, W.s_col, W.s_pix, W.s_path, path, wbase + incl - n_shadow, wbase + incl};
 		if(sw.end > shadow_cap) sw.end = sw.slot > shadow_cap ? sw.slot : shadow_cap;
 		if(do_nee_all)
 			for(uint32_t l = 0; l < P.n_lights; ++l) light_estimation(sc, s, wo, l, l, sample_, offset_, nee_weight, pixel, sw);
@@ -693,9 +814,50 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 			{
 				float wi[3], scol[3], w, pdf;
 				uint32_t sflags;
-				mat_sample(s, wo, s1, s2, req, wi, scol, w, pdf, sflags);
+				float mult[3], mpdf = 0.f, hf = 0.f;
+				const bool guidable = s.m->type == GBRT_MAT_SHINYDIFFUSE || s.m->type == GBRT_MAT_GLOSSY;
+				if(P.guiding && guidable)
+				{
+					// one-sample MIS of the guide mixture q and the BSDF sampler
+					// (true density p): weight = h(w) / (alpha q(w) + (1 - alpha) p(w)),
+					// h(w) = (sample colour x weight)(w) * p(w), the integrand the
+					// plain estimator targets, so guided and plain converge alike.
+					const float *lob = W.lobes + static_cast<size_t>(gbrt::kGuideOut) * q;
+					const uint32_t key = sample_ * 64u + sub;
+					const float u = rng01(pixel, key, k, P.seed ^ 0x51ed270bu);
+					float fw[3], ptrue;
+					if(u < P.alpha)
+					{
+						gbrt::mixture_sample(lob, rng01(pixel, key, k, P.seed ^ 0x2545f491u), rng01(pixel, key, k, P.seed ^ 0x6c8e9cf5u),
+						                     rng01(pixel, key, k, P.seed ^ 0x1b873593u), wi);
+						bsdf_eval_at(s, wo, wi, req, fw);
+						ptrue = bsdf_true_pdf(s, wo, wi, req);
+						sflags = BF_DIFFUSE | BF_REFLECT;
+					}
+					else
+					{
+						mat_sample(s, wo, s1, s2, req, wi, scol, w, pdf, sflags);
+						for(int c = 0; c < 3; ++c) fw[c] = xm(scol[c], w);
+						ptrue = bsdf_true_pdf(s, wo, wi, req);
+					}
+					const float qp = gbrt::mixture_pdf(lob, wi);
+					mpdf = P.alpha * qp + (1.f - P.alpha) * ptrue;
+					const float f = mpdf > 0.f ? ptrue / mpdf : 0.f;
+					for(int c = 0; c < 3; ++c) mult[c] = fw[c] * f;
+					hf = (0.2126f * fw[0] + 0.7152f * fw[1] + 0.0722f * fw[2]) * ptrue;
+				}
+				else
+				{
+					mat_sample(s, wo, s1, s2, req, wi, scol, w, pdf, sflags);
+					for(int c = 0; c < 3; ++c) mult[c] = xm(scol[c], w);
+					if(P.record && guidable)
+					{
+						mpdf = bsdf_true_pdf(s, wo, wi, req);
+						hf = (0.2126f * mult[0] + 0.7152f * mult[1] + 0.0722f * mult[2]) * mpdf;
+					}
+				}
 				float nt[3];
-				for(int c = 0; c < 3; ++c) nt[c] = xm(thr[c], xm(scol[c], w));
+				for(int c = 0; c < 3; ++c) nt[c] = xm(thr[c], mult[c]);
 				if(k == 0)
 				{
 					const float inv_ps = __fdiv_rn(1.f, static_cast<float>(P.path_samples));
@@ -704,6 +866,14 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				if(nt[0] != 0.f || nt[1] != 0.f || nt[2] != 0.f)
 				{
 					cont = true;
+					if(P.record && mpdf > 0.f && k < P.rec_stride)
+					{
+						const size_t slot = static_cast<size_t>(path) * P.rec_stride + k;
+						W.r_pos[slot] = make_float4(s.p[0], s.p[1], s.p[2], mpdf);
+						W.r_dir[slot] = make_float4(wi[0], wi[1], wi[2], hf);
+						W.r_thr[slot] = make_float4(nt[0], nt[1], nt[2], 0.f);
+						W.r_valid[slot] = 2u;     // waiting for the next vertex
+					}
 					caustic = (sflags & (BF_SPECULAR | BF_GLOSSY | BF_FILTER)) ? 1u : 0u;
 					W.p_thr[path] = make_float4(nt[0], nt[1], nt[2], 0.f);
 					W.p_state[path] = (k + 1u) | (mat1 << 8) | (caustic << 16);
@@ -746,10 +916,71 @@ __global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Work W, u
 		{
 			const float4 c = W.s_col[i];
 			film_add(film, film64, pixel, c.x, c.y, c.z);
+			if(W.p_sum) path_sum_add(W, W.s_path[i], c.x, c.y, c.z);
 		}
 	}
 	for(int off = 16; off > 0; off >>= 1) traced += __shfl_xor_sync(0xffffffffu, traced, off);
 	if((threadIdx.x & 31u) == 0 && traced) atomicAdd(W.stats + 1, static_cast<unsigned long long>(traced));
+}
+
+// Records of a finished wave -> training records {pos, dir, c, 0} with
+// c = luminance(incident radiance) x h / mixture pdf, where h is the BSDF x
+// cosine factor of the estimator (the guide learns the product), incident
+// radiance = (path total - contributions before the next vertex) /
+// throughput after sampling.
+__global__ void k_make_records(Work W, uint32_t n_paths, uint32_t stride, int radiance_target)
+{
+	const uint32_t lane = threadIdx.x & 31u;
+	const size_t total = static_cast<size_t>(n_paths) * stride;
+	for(size_t base = blockIdx.x * static_cast<size_t>(blockDim.x); base < total; base += static_cast<size_t>(gridDim.x) * blockDim.x)
+	{
+		const size_t slot = base + threadIdx.x;
+		bool ok = false;
+		float4 pos = make_float4(0.f, 0.f, 0.f, 0.f), dir = pos;
+		float c = 0.f;
+		if(slot < total && W.r_valid[slot] == 1u)
+		{
+			const uint32_t path = static_cast<uint32_t>(slot / stride);
+			const float4 sum = W.p_sum[path], pre = W.r_pre[slot], thr = W.r_thr[slot];
+			pos = W.r_pos[slot];
+			dir = W.r_dir[slot];
+			const float L[3] = {thr.x > 0.f ? (sum.x - pre.x) / thr.x : 0.f, thr.y > 0.f ? (sum.y - pre.y) / thr.y : 0.f,
+			                    thr.z > 0.f ? (sum.z - pre.z) / thr.z : 0.f};
+			// target density ~ incident radiance x (BSDF x cosine): c = L h / m
+			const float lum = fmaxf(0.f, 0.2126f * L[0] + 0.7152f * L[1] + 0.0722f * L[2]);
+			c = pos.w > 0.f ? lum * (radiance_target ? 1.f : fmaxf(dir.w, 0.f)) / pos.w : 0.f;
+			ok = c > 0.f && isfinite(c);
+			c = fminf(c, 1e4f);
+		}
+		const uint32_t ballot = __ballot_sync(0xffffffffu, ok);
+		if(!ballot) continue;
+		const uint32_t leader = __ffs(ballot) - 1u;
+		uint32_t b = 0;
+		if(lane == leader) b = atomicAdd(W.count + 3, static_cast<uint32_t>(__popc(ballot)));
+		b = __shfl_sync(0xffffffffu, b, leader);
+		if(ok)
+		{
+			const uint32_t i = b + __popc(ballot & ((1u << lane) - 1u));
+			if(i < W.train_cap)
+			{
+				float4 *o = reinterpret_cast<float4 *>(W.train + 8ull * i);
+				o[0] = make_float4(pos.x, pos.y, pos.z, dir.x);
+				o[1] = make_float4(dir.y, dir.z, c, 0.f);
+			}
+		}
+	}
+}
+
+// A training batch of `batch` records drawn uniformly (with replacement)
+// from the n records of the wave, so a step sees the whole image.
+__global__ void k_gather_batch(const float4 *__restrict__ rec, uint32_t n, uint32_t batch, uint32_t seed, float4 *__restrict__ out)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < batch; i += gridDim.x * blockDim.x)
+	{
+		const uint32_t j = hash32(i * 0x9e3779b9u ^ hash32(seed)) % n;
+		out[2ull * i] = rec[2ull * j];
+		out[2ull * i + 1] = rec[2ull * j + 1];
+	}
 }
 
 __global__ void k_reset(uint32_t *count, int which) { count[which] = 0u; count[2] = 0u; }
@@ -811,7 +1042,7 @@ struct gbrt_scene {
 	uint32_t *lds_off = nullptr, *lds_base = nullptr;
 	double *lds_inv = nullptr;
 	// work buffers (grown on demand)
-	size_t cap_paths = 0, cap_shadow = 0;
+	size_t cap_paths = 0, cap_shadow = 0, cap_stride = 0;
 	void *work = nullptr;
 	Work w{};
 	std::mutex mu;
@@ -819,21 +1050,33 @@ struct gbrt_scene {
 
 namespace {
 
-int alloc_work(gbrt_scene *S, size_t paths, size_t shadow)
+int alloc_work(gbrt_scene *S, size_t paths, size_t shadow, size_t stride)
 {
-	if(paths <= S->cap_paths && shadow <= S->cap_shadow) return GBRT_OK;
+	if(paths <= S->cap_paths && shadow <= S->cap_shadow && stride <= S->cap_stride) return GBRT_OK;
+	paths = std::max(paths, S->cap_paths);
+	shadow = std::max(shadow, S->cap_shadow);
+	stride = std::max(stride, S->cap_stride);
 	if(S->work) { cudaFree(S->work); S->work = nullptr; }
 	size_t off = 0;
 	auto carve = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
 	const size_t o_pix = carve(4 * paths), o_si = carve(4 * paths), o_st = carve(4 * paths), o_thr = carve(16 * paths);
 	const size_t o_qr0 = carve(32 * paths), o_qr1 = carve(32 * paths), o_qp0 = carve(4 * paths), o_qp1 = carve(4 * paths);
 	const size_t o_hit = carve(16 * paths);
-	const size_t o_sr = carve(32 * shadow), o_sc = carve(16 * shadow), o_sp = carve(4 * shadow);
+	const size_t o_sr = carve(32 * shadow), o_sc = carve(16 * shadow), o_sp = carve(4 * shadow), o_spath = carve(4 * shadow);
 	const size_t o_cnt = carve(64), o_stats = carve(64);
+	size_t o_hp = 0, o_lob = 0, o_psum = 0, o_rpos = 0, o_rdir = 0, o_rthr = 0, o_rpre = 0, o_rval = 0, o_train = 0;
+	const size_t recs = paths * stride;
+	if(stride)
+	{
+		o_hp = carve(12 * paths); o_lob = carve(4ull * gbrt::kGuideOut * paths); o_psum = carve(16 * paths);
+		o_rpos = carve(16 * recs); o_rdir = carve(16 * recs); o_rthr = carve(16 * recs); o_rpre = carve(16 * recs);
+		o_rval = carve(4 * recs); o_train = carve(32 * (recs + kMaxBatch));
+	}
 	cudaError_t e = cudaMalloc(&S->work, off);
-	if(e != cudaSuccess) { S->work = nullptr; S->cap_paths = S->cap_shadow = 0; return gbrt_set_error(GBRT_ERR_OOM, "path tracer work buffers (%zu bytes): %s", off, cudaGetErrorString(e)); }
+	if(e != cudaSuccess) { S->work = nullptr; S->cap_paths = S->cap_shadow = S->cap_stride = 0; return gbrt_set_error(GBRT_ERR_OOM, "path tracer work buffers (%zu bytes): %s", off, cudaGetErrorString(e)); }
 	char *b = static_cast<char *>(S->work);
 	Work &w = S->w;
+	w = Work{};
 	w.p_pixel = reinterpret_cast<uint32_t *>(b + o_pix);
 	w.p_si = reinterpret_cast<uint32_t *>(b + o_si);
 	w.p_state = reinterpret_cast<uint32_t *>(b + o_st);
@@ -846,10 +1089,25 @@ int alloc_work(gbrt_scene *S, size_t paths, size_t shadow)
 	w.s_ray = reinterpret_cast<float4 *>(b + o_sr);
 	w.s_col = reinterpret_cast<float4 *>(b + o_sc);
 	w.s_pix = reinterpret_cast<uint32_t *>(b + o_sp);
+	w.s_path = reinterpret_cast<uint32_t *>(b + o_spath);
 	w.count = reinterpret_cast<uint32_t *>(b + o_cnt);
 	w.stats = reinterpret_cast<unsigned long long *>(b + o_stats);
+	if(stride)
+	{
+		w.hitpos = reinterpret_cast<float *>(b + o_hp);
+		w.lobes = reinterpret_cast<float *>(b + o_lob);
+		w.p_sum = reinterpret_cast<float4 *>(b + o_psum);
+		w.r_pos = reinterpret_cast<float4 *>(b + o_rpos);
+		w.r_dir = reinterpret_cast<float4 *>(b + o_rdir);
+		w.r_thr = reinterpret_cast<float4 *>(b + o_rthr);
+		w.r_pre = reinterpret_cast<float4 *>(b + o_rpre);
+		w.r_valid = reinterpret_cast<uint32_t *>(b + o_rval);
+		w.train = reinterpret_cast<float *>(b + o_train);
+		w.train_cap = static_cast<uint32_t>(std::min<size_t>(recs + kMaxBatch, 0xFFFFFFFFull));
+	}
 	S->cap_paths = paths;
 	S->cap_shadow = shadow;
+	S->cap_stride = stride;
 	return GBRT_OK;
 }
 
@@ -1041,7 +1299,11 @@ int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 	std::lock_guard<std::mutex> lock(S->mu);
 	const uint64_t total = static_cast<uint64_t>(camera->resx) * camera->resy * pp.spp * pp.path_samples;
 	if(total >= (1ull << 32)) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_pt_render: %llu paths exceed 2^32", static_cast<unsigned long long>(total));
-	const uint64_t wave = std::min<uint64_t>(total, pp.wave_paths ? pp.wave_paths : (1ull << 22));
+	gbrt_guide *guide = pp.guide;
+	if(pp.guide_batch > kMaxBatch) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_pt_render: guide_batch %u > %u", pp.guide_batch, kMaxBatch);
+	const bool guiding = guide && pp.guide_alpha > 0.f;
+	const bool record = guide && pp.guide_train_steps > 0;
+	const uint64_t wave = std::min<uint64_t>(total, pp.wave_paths ? pp.wave_paths : (record ? (1ull << 20) : (1ull << 22)));
 	uint32_t max_shadow = 0;
 	{
 		std::vector<DevLight> ls(S->n_lights);
@@ -1051,7 +1313,8 @@ int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 		max_shadow = std::max(all, one);
 	}
 	const size_t shadow_cap = std::max<size_t>(1, wave * max_shadow);
-	if(int rc = alloc_work(S, wave, shadow_cap)) return rc;
+	const uint32_t stride = static_cast<uint32_t>(std::max(1, pp.bounces));
+	if(int rc = alloc_work(S, wave, shadow_cap, guide ? stride : 0)) return rc;
 	Camera cam = make_camera(*camera);
 	SceneDev sc{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv}};
 	Params P{};
@@ -1059,6 +1322,12 @@ int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 	P.base_offset = pp.base_sampling_offset; P.seed = pp.seed;
 	P.d1 = 1.f / static_cast<float>(pp.spp);
 	P.n_lights = S->n_lights;
+	P.guiding = guiding ? 1 : 0;
+	P.alpha = guiding ? std::min(1.f, pp.guide_alpha) : 0.f;
+	P.record = record ? 1 : 0;
+	P.rec_stride = stride;
+	Work W = S->w;
+	if(!record) W.p_sum = nullptr;
 	float *film = film64_dev ? nullptr : film_dev;
 	cudaEvent_t e0 = nullptr, e1 = nullptr;
 	if(stats)
@@ -1071,15 +1340,47 @@ int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 	{
 		P.wave_start = static_cast<uint32_t>(start);
 		P.wave_n = static_cast<uint32_t>(std::min<uint64_t>(wave, total - start));
-		k_camera<<<grid_for(P.wave_n, S->n_sm), kThreads, 0, s>>>(cam, P, S->w);
+		k_camera<<<grid_for(P.wave_n, S->n_sm), kThreads, 0, s>>>(cam, P, W);
 		int cur = 0;
 		for(int vtx = 0; vtx <= pp.bounces; ++vtx)
 		{
-			k_reset<<<1, 1, 0, s>>>(S->w.count, cur ^ 1);
-			k_extend<<<grid_for(P.wave_n, S->n_sm), kThreads, 0, s>>>(sc.bv, S->w.q_ray[cur], S->w.count + cur, S->w.hits);
-			k_shade<<<grid_for(P.wave_n, S->n_sm), kThreads, 0, s>>>(sc, P, S->w, cur, camera->resx, static_cast<uint32_t>(shadow_cap), film, film64_dev);
-			k_shadow<<<grid_for(shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, S->w, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+			// guide only the first guide_max_vertex vertex levels (a wavefront
+			// level holds the paths' vertex vtx, so the network runs only there)
+			const bool level_guided = guiding && (pp.guide_max_vertex == 0 || vtx < static_cast<int>(pp.guide_max_vertex));
+			P.guiding = level_guided ? 1 : 0;
+			P.record = (record && (pp.guide_max_vertex == 0 || vtx < static_cast<int>(pp.guide_max_vertex))) ? 1 : 0;
+			k_reset<<<1, 1, 0, s>>>(W.count, cur ^ 1);
+			k_extend<<<grid_for(P.wave_n, S->n_sm), kThreads, 0, s>>>(sc.bv, W.q_ray[cur], W.count + cur, W.hits, level_guided ? W.hitpos : nullptr);
+			if(level_guided)
+				if(int rc = gbrt_guide_eval_queue(guide, W.hitpos, P.wave_n, W.count + cur, W.lobes, s)) return rc;
+			k_shade<<<grid_for(P.wave_n, S->n_sm), kThreads, 0, s>>>(sc, P, W, cur, camera->resx, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+			k_shadow<<<grid_for(shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, W, static_cast<uint32_t>(shadow_cap), film, film64_dev);
 			cur ^= 1;
+		}
+		if(record)
+		{
+			GBRT_CK(cudaMemsetAsync(W.count + 3, 0, sizeof(uint32_t), s));
+			k_make_records<<<grid_for(static_cast<size_t>(P.wave_n) * stride, S->n_sm), kThreads, 0, s>>>(W, P.wave_n, stride,
+			                                                                                             (pp.flags & GBRT_PT_GUIDE_RADIANCE) ? 1 : 0);
+			uint32_t n_rec = 0;
+			GBRT_CK(cudaMemcpyAsync(&n_rec, W.count + 3, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+			GBRT_CK(cudaStreamSynchronize(s));
+			n_rec = std::min(n_rec, W.train_cap);
+			const uint32_t batch = pp.guide_batch ? pp.guide_batch : 65536u;
+			if(n_rec > 0)
+				for(uint32_t st = 0; st < pp.guide_train_steps; ++st)
+				{
+					float *bbuf = W.train + 8ull * W.train_cap - 8ull * batch;   // batch area at the end of the buffer
+					if(static_cast<uint64_t>(n_rec) + batch > W.train_cap)
+					{
+						n_rec = W.train_cap > batch ? W.train_cap - batch : 0;
+						if(n_rec == 0) break;
+					}
+					k_gather_batch<<<grid_for(batch, S->n_sm), kThreads, 0, s>>>(reinterpret_cast<const float4 *>(W.train), n_rec, batch,
+					                                                          pp.seed * 7919u + static_cast<uint32_t>(start) + st * 131u,
+					                                                          reinterpret_cast<float4 *>(bbuf));
+					if(int rc = gbrt_guide_step(guide, bbuf, batch, nullptr, s)) return rc;
+				}
 		}
 	}
 	GBRT_CK(cudaGetLastError());

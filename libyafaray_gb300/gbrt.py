@@ -55,7 +55,9 @@ class CameraDesc(ctypes.Structure):
 class PtParams(ctypes.Structure):
     _fields_ = [("spp", ctypes.c_int32), ("path_samples", ctypes.c_int32), ("bounces", ctypes.c_int32),
                 ("russian_roulette_min_bounces", ctypes.c_int32), ("base_sampling_offset", ctypes.c_uint32),
-                ("seed", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("wave_paths", ctypes.c_uint32)]
+                ("seed", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("wave_paths", ctypes.c_uint32),
+                ("guide", ctypes.c_void_p), ("guide_alpha", ctypes.c_float), ("guide_train_steps", ctypes.c_uint32),
+                ("guide_batch", ctypes.c_uint32), ("guide_max_vertex", ctypes.c_uint32)]
 
 
 class PtStats(ctypes.Structure):
@@ -63,8 +65,14 @@ class PtStats(ctypes.Structure):
                 ("shadow_rays", ctypes.c_uint64), ("ms", ctypes.c_float)]
 
 
+class GuideParams(ctypes.Structure):
+    _fields_ = [("log2_table", ctypes.c_uint32), ("base_resolution", ctypes.c_float),
+                ("max_resolution", ctypes.c_float), ("learning_rate", ctypes.c_float), ("seed", ctypes.c_uint32)]
+
+
 MAT_TYPES = {"shinydiffusemat": 0, "light_mat": 1, "glossy": 2, "rough_glass": 3, "glass": 4}
 PT_FP64_FILM = 1
+PT_GUIDE_RADIANCE = 2
 
 # Every symbol include/gbrt.h declares, with its ctypes signature.
 _VP, _U32, _I, _F = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_float
@@ -88,6 +96,16 @@ SIGNATURES = {
                                ctypes.POINTER(LightDesc), _U32, ctypes.POINTER(_VP)]),
     "gbrt_scene_destroy": (_I, [_VP]),
     "gbrt_sampler_eval": (_I, [_I, _I, _VP, _U32, _VP, _I]),
+    "gbrt_guide_create": (_I, [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(GuideParams), ctypes.POINTER(_VP)]),
+    "gbrt_guide_destroy": (_I, [_VP]),
+    "gbrt_guide_info": (_I, [_VP, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint64)]),
+    "gbrt_guide_get_params": (_I, [_VP, _VP, _VP]),
+    "gbrt_guide_set_params": (_I, [_VP, _VP, _VP]),
+    "gbrt_guide_eval": (_I, [_VP, _VP, _U32, _VP, _VP]),
+    "gbrt_guide_grad": (_I, [_VP, _VP, _U32, ctypes.POINTER(ctypes.c_float), _VP]),
+    "gbrt_guide_get_grads": (_I, [_VP, _VP, _VP]),
+    "gbrt_guide_step": (_I, [_VP, _VP, _U32, ctypes.POINTER(ctypes.c_float), _VP]),
+    "gbrt_guide_forward_host": (_I, [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(GuideParams), _VP, _VP, _VP, _U32, _VP]),
     "gbrt_pt_render": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP, _VP,
                             ctypes.POINTER(PtStats), _VP]),
     "gbrt_pt_render_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP,
@@ -269,6 +287,10 @@ class Renderer:
         except Exception:
             pass
 
+    def make_guide(self, **kw):
+        """A guiding network over this scene's tree bound."""
+        return Guide(self.bvh.bound(), **kw)
+
     def camera_desc(self):
         c = self.scene["camera"]
         d = CameraDesc()
@@ -278,26 +300,33 @@ class Renderer:
         d.resx, d.resy, d.focal = int(c["resx"]), int(c["resy"]), float(c["focal"])
         return d
 
-    def params(self, spp, base_offset=0, seed=1, fp64=False, wave_paths=0):
+    def params(self, spp, base_offset=0, seed=1, fp64=False, wave_paths=0, guide=None, alpha=0.0, train_steps=0,
+               batch=0, max_vertex=0):
         it = self.scene["integrator"]
         return PtParams(int(spp), int(it.get("path_samples", 1)), int(it.get("bounces", 5)),
                         int(it.get("russian_roulette_min_bounces", 0)), int(base_offset), int(seed),
-                        PT_FP64_FILM if fp64 else 0, int(wave_paths))
+                        PT_FP64_FILM if fp64 else 0, int(wave_paths), guide.handle if guide is not None else None,
+                        float(alpha), int(train_steps), int(batch), int(max_vertex))
 
-    def render(self, spp, base_offset=0, seed=1, fp64=False):
+    def render(self, spp, base_offset=0, seed=1, fp64=False, guide=None, alpha=0.0, train_steps=0, batch=0,
+               max_vertex=0):
         """Per-pixel mean image [resy, resx, 3] and stats dict."""
         cam = self.camera_desc()
-        p = self.params(spp, base_offset, seed, fp64)
+        p = self.params(spp, base_offset, seed, fp64, 0, guide, alpha, train_steps, batch, max_vertex)
         img = np.empty((cam.resy, cam.resx, 3), np.float32)
         st = PtStats()
         check(load().gbrt_pt_render_host(self._h, ctypes.byref(cam), ctypes.byref(p), _ptr(img), ctypes.byref(st)))
         return img, {"camera_samples": st.camera_samples, "extension_rays": st.extension_rays,
                      "shadow_rays": st.shadow_rays, "ms": st.ms}
 
-    def render_device(self, spp, film_ptr, film64_ptr=0, base_offset=0, seed=1, stream=0, stats=False, wave_paths=0):
+    def render_device(self, spp, film_ptr, film64_ptr=0, base_offset=0, seed=1, stream=0, stats=False, wave_paths=0,
+                      guide=None, alpha=0.0, train_steps=0, batch=0, max_vertex=0, radiance_target=False):
         """Adds sample sums into a device film (float or double RGB)."""
         cam = self.camera_desc()
-        p = self.params(spp, base_offset, seed, bool(film64_ptr), wave_paths)
+        p = self.params(spp, base_offset, seed, bool(film64_ptr), wave_paths, guide, alpha, train_steps, batch,
+                        max_vertex)
+        if radiance_target:
+            p.flags |= PT_GUIDE_RADIANCE
         st = PtStats()
         check(load().gbrt_pt_render(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.c_void_p(film_ptr or None),
                                     ctypes.c_void_p(film64_ptr or None), ctypes.byref(st) if stats else None,
@@ -312,4 +341,76 @@ def sampler_eval(kind, dim, inputs, on_device):
     x = np.ascontiguousarray(inputs, np.uint32)
     out = np.empty(len(x), np.float64)
     check(load().gbrt_sampler_eval(int(kind), int(dim), _ptr(x), len(x), _ptr(out), int(bool(on_device))))
+    return out
+
+
+class Guide:
+    """Path-guiding network handle (gbrt_guide)."""
+
+    def __init__(self, bound, log2_table=19, base_resolution=16.0, max_resolution=2048.0, learning_rate=5e-3, seed=1):
+        b = (ctypes.c_float * 6)(*[float(x) for x in bound])
+        p = GuideParams(log2_table, base_resolution, max_resolution, learning_rate, seed)
+        h = ctypes.c_void_p()
+        check(load().gbrt_guide_create(b, ctypes.byref(p), ctypes.byref(h)))
+        self._h = h
+        n_mlp, n_tab = ctypes.c_uint32(), ctypes.c_uint64()
+        check(load().gbrt_guide_info(h, ctypes.byref(n_mlp), ctypes.byref(n_tab)))
+        self.n_mlp, self.n_table = n_mlp.value, n_tab.value
+        self.log2_table = log2_table
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().gbrt_guide_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self):
+        mlp = np.empty(self.n_mlp, np.float32)
+        tab = np.empty(self.n_table, np.float32)
+        check(load().gbrt_guide_get_params(self._h, _ptr(mlp), _ptr(tab)))
+        return mlp, tab.reshape(16, 1 << self.log2_table, 2)
+
+    def set_params(self, mlp=None, table=None):
+        m = None if mlp is None else np.ascontiguousarray(mlp, np.float32)
+        t = None if table is None else np.ascontiguousarray(table, np.float32)
+        check(load().gbrt_guide_set_params(self._h, _ptr(m), _ptr(t)))
+
+    def grads(self):
+        mlp = np.empty(self.n_mlp, np.float32)
+        tab = np.empty(self.n_table, np.float32)
+        check(load().gbrt_guide_get_grads(self._h, _ptr(mlp), _ptr(tab)))
+        return mlp, tab.reshape(16, 1 << self.log2_table, 2)
+
+    def eval_device(self, pos_ptr, n, lobes_ptr, stream=0):
+        check(load().gbrt_guide_eval(self._h, ctypes.c_void_p(pos_ptr), n, ctypes.c_void_p(lobes_ptr), ctypes.c_void_p(stream)))
+
+    def grad_device(self, rec_ptr, n, stream=0):
+        loss = ctypes.c_float()
+        check(load().gbrt_guide_grad(self._h, ctypes.c_void_p(rec_ptr), n, ctypes.byref(loss), ctypes.c_void_p(stream)))
+        return loss.value
+
+    def step_device(self, rec_ptr, n, stream=0):
+        loss = ctypes.c_float()
+        check(load().gbrt_guide_step(self._h, ctypes.c_void_p(rec_ptr), n, ctypes.byref(loss), ctypes.c_void_p(stream)))
+        return loss.value
+
+
+def guide_forward_host(bound, mlp, table, pos, log2_table=19, base_resolution=16.0, max_resolution=2048.0):
+    """Host build of the guide's forward pass: lobes [n, 40]."""
+    b = (ctypes.c_float * 6)(*[float(x) for x in bound])
+    p = GuideParams(log2_table, base_resolution, max_resolution, 0.0, 0)
+    m = np.ascontiguousarray(mlp, np.float32)
+    t = np.ascontiguousarray(table, np.float32)
+    x = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    out = np.empty((len(x), 40), np.float32)
+    check(load().gbrt_guide_forward_host(b, ctypes.byref(p), _ptr(m), _ptr(t), _ptr(x), len(x), _ptr(out)))
     return out

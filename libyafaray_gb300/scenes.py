@@ -203,29 +203,43 @@ def flatten(scene):
     return np.concatenate(V), np.concatenate(F), np.concatenate(M), names
 
 
-def _box_tris(center, size, yaw):
-    """12 triangles of a yawed box (outward-facing)."""
-    hx, hy, hz = 0.5 * np.asarray(size, np.float64)
-    p = np.array([[-hx, -hy, -hz], [hx, -hy, -hz], [hx, hy, -hz], [-hx, hy, -hz],
-                  [-hx, -hy, hz], [hx, -hy, hz], [hx, hy, hz], [-hx, hy, hz]])
+def _box_tris(center, size, yaw, subdiv=1):
+    """Triangles of a yawed box, each face subdivided into subdiv x subdiv
+    quads (2 triangles each), outward-facing.  Returns (vertices, tri indices)."""
+    h = 0.5 * np.asarray(size, np.float64)
     c, s = math.cos(yaw), math.sin(yaw)
     R = np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])
-    p = p @ R.T + np.asarray(center, np.float64)
-    quads = [[0, 3, 2, 1], [4, 5, 6, 7], [0, 1, 5, 4], [3, 7, 6, 2], [0, 4, 7, 3], [1, 2, 6, 5]]
-    tris = []
-    for q in quads:
-        tris.append([q[0], q[1], q[2]]); tris.append([q[0], q[2], q[3]])
-    return p, np.array(tris)
+    # (origin corner, u edge, v edge) per face with u x v pointing outwards
+    faces = [((-1, -1, -1), (0, 2, 0), (2, 0, 0)), ((-1, -1, 1), (2, 0, 0), (0, 2, 0)),
+             ((-1, -1, -1), (2, 0, 0), (0, 0, 2)), ((-1, 1, -1), (0, 0, 2), (2, 0, 0)),
+             ((-1, -1, -1), (0, 0, 2), (0, 2, 0)), ((1, -1, -1), (0, 2, 0), (0, 0, 2))]
+    V, T = [], []
+    n = subdiv
+    g = np.linspace(0.0, 1.0, n + 1)
+    for o, u, v in faces:
+        o, u, v = (np.asarray(x, np.float64) * h for x in (o, u, v))
+        base = len(V) * 0
+        pts = o[None, None, :] + g[:, None, None] * u[None, None, :] + g[None, :, None] * v[None, None, :]
+        off = sum(len(x) for x in V)
+        V.append(pts.reshape(-1, 3))
+        for i in range(n):
+            for j in range(n):
+                a = off + i * (n + 1) + j
+                b, cc, d = a + (n + 1), a + (n + 1) + 1, a + 1
+                T.append([a, b, cc]); T.append([a, cc, d])
+    P = np.concatenate(V) @ R.T + np.asarray(center, np.float64)
+    return P, np.array(T)
 
 
-def indoor_scene(n_boxes=16_667, res=(960, 540), seed=5, bounces=12, rr_min=4, light_samples=2):
+def indoor_scene(n_boxes=463, subdiv=6, res=(960, 540), seed=5, bounces=12, rr_min=4, light_samples=2):
     """Indoor scene lit through a gap: a closed 10 x 4 x 6 m room whose
     1 x 2 m door (in the wall z = 6, x in [4.5, 5.5]) stands ajar by 0.1 m,
     an outdoor 2 x 2 m area light of radiance 200 facing the door 3 m beyond
-    it (z = 9), and n_boxes seeded furniture boxes (12 triangles each;
-    16,667 boxes = 200,004 triangles) with shinydiffuse albedo U[0.2, 0.8]
-    per channel (palette of 32) or, for 20 % of the boxes, glossy exponent 100
-    (palette of 8).  Camera inside looking at the door wall; max depth 12."""
+    it (z = 9), and n_boxes seeded furniture boxes (edges U[0.1, 0.6] m,
+    faces tessellated subdiv x subdiv: 463 boxes x 432 = 200,016 triangles)
+    with shinydiffuse albedo U[0.2, 0.8] per channel (palette of 32) or, for
+    20 % of the boxes, glossy exponent 100 (palette of 8).  Camera inside
+    looking at the door wall; max depth 12."""
     rng = np.random.default_rng(seed)
     mats = {}
     for i in range(32):
@@ -259,13 +273,13 @@ def indoor_scene(n_boxes=16_667, res=(960, 540), seed=5, bounces=12, rr_min=4, l
     names_d = [f"diff{i}" for i in range(32)]
     names_g = [f"glossy{i}" for i in range(8)]
     for b in range(n_boxes):
-        size = rng.uniform(0.05, 0.35, 3)
+        size = rng.uniform(0.1, 0.6, 3)
         while True:
             c = np.array([rng.uniform(0.3, W - 0.3), rng.uniform(0.0, 3.2), rng.uniform(0.3, D - 0.4)])
             if not (3.5 < c[0] < 6.5 and c[2] > 4.2):
                 break
         c[1] += 0.5 * size[1]
-        p, t = _box_tris(c, size, rng.uniform(0, 2 * math.pi))
+        p, t = _box_tris(c, size, rng.uniform(0, 2 * math.pi), subdiv)
         V.append(p); F.append(t)
         M.append(names_g[rng.integers(8)] if rng.random() < 0.2 else names_d[rng.integers(32)])
     by_mat = {}
@@ -273,7 +287,8 @@ def indoor_scene(n_boxes=16_667, res=(960, 540), seed=5, bounces=12, rr_min=4, l
         by_mat.setdefault(m, []).append((v, f))
     for m, lst in sorted(by_mat.items()):
         vv = np.concatenate([v for v, _ in lst]).astype(np.float32)
-        ff = np.concatenate([f + 8 * i for i, (_, f) in enumerate(lst)]).astype(np.uint32)
+        offs = np.cumsum([0] + [len(v) for v, _ in lst[:-1]])
+        ff = np.concatenate([f + o for o, (_, f) in zip(offs, lst)]).astype(np.uint32)
         faces = np.empty((len(ff), 4), np.uint32); faces[:, :3] = ff; faces[:, 3] = TRI
         objects.append({"name": f"boxes_{m}", "material": m, "vertices": vv, "faces": faces})
     # outdoor light 3 m beyond the gap, facing -z, with its light_mat emitter

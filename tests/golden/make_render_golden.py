@@ -74,7 +74,7 @@ def render_golden(res=64, spp=16, batches=32, glossy=False):
 
 
 def indoor_golden(spp=16, batches=24):
-    sc = scenes.indoor_scene(n_boxes=400, res=(96, 54))
+    sc = scenes.indoor_scene(n_boxes=120, subdiv=1, res=(96, 54))
     rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
     mean = rgb.mean(0)
     se = rgb.std(0, ddof=1) / np.sqrt(batches)

@@ -80,10 +80,10 @@ def test_gpu_cornell_glossy_matches_reference(cuda_device):
 
 
 def test_gpu_indoor_small_matches_reference(cuda_device):
-    """Indoor scene (door ajar, outdoor light, glossy and diffuse boxes), 400
-    boxes at 96x54, depth 12 with Russian roulette."""
+    """Indoor scene (door ajar, outdoor light, glossy and diffuse boxes), 120
+    untessellated boxes at 96x54, depth 12 with Russian roulette."""
     g = np.load(os.path.join(GOLD, "indoor_small_render.npz"))
-    sc = scenes.indoor_scene(n_boxes=400, res=(96, 54))
+    sc = scenes.indoor_scene(n_boxes=120, subdiv=1, res=(96, 54))
     r = gbrt.Renderer(sc)
     gb = batches(r, int(g["spp"]), int(g["batches"]))
     frac, relmse, m = parity(gb, g["mean"], g["se"])
