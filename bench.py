@@ -163,6 +163,55 @@ def run_reference(args, rank, world):
     print(json.dumps(out))
 
 
+def render_sections(args):
+    """Cornell path tracing throughput and the guided-vs-plain time to
+    relMSE 0.01 on the indoor scene (against an FP64-accumulated plain
+    render of args.ref_spp samples per pixel)."""
+    import torch
+    from libyafaray_gb300 import convergence, gbrt, scenes
+    out = {}
+    # Cornell box, 512x512, 16 spp, path_samples 1, bounces 5, RR from 3
+    r = gbrt.Renderer(scenes.cornell_scene(res=512))
+    film = torch.zeros(512 * 512 * 3, dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        r.render_device(16, film.data_ptr())
+    best = None
+    for k in range(5):
+        st = r.render_device(16, film.data_ptr(), base_offset=16 * k, stats=True)
+        if best is None or st["ms"] < best["ms"]:
+            best = st
+    rays = best["extension_rays"] + best["shadow_rays"]
+    out["pathtracing_cornell"] = {
+        "workload": "Cornell box 34 triangles + emitter, 512x512, 16 spp, pathtracing path_samples 1 bounces 5 rr_min 3",
+        "ms_per_frame": best["ms"], "mrays_s": rays / best["ms"] / 1e3,
+        "msamples_s": best["camera_samples"] / best["ms"] / 1e3,
+        "rays_per_frame": rays, "reference_cpu_note": "reference renders this frame in 3.37 s on 8 x86 threads"}
+    del r
+    # indoor scene lit through a door gap: guided vs plain time to relMSE 0.01
+    r = gbrt.Renderer(scenes.indoor_scene())
+    t0 = time.perf_counter()
+    ref = convergence.reference_image(r, spp=args.ref_spp)
+    ref_s = time.perf_counter() - t0
+    plain = convergence.time_to_relmse(r, ref, target=0.01, spp_pass=16, max_time=90)
+    guide = r.make_guide()
+    guided = convergence.time_to_relmse(r, ref, target=0.01, spp_pass=4, max_time=90, guide=guide, alpha=0.5,
+                                        train_fraction=0.25, train_steps=16, batch=65536, max_vertex=0,
+                                        expected_time=plain["time_s"])
+    out["guided_vs_plain"] = {
+        "workload": "indoor room 10x4x6 m, door ajar 0.1 m, outdoor 2x2 m light radiance 200, 200,036 triangles, "
+                    "960x540, bounces 12",
+        "reference": {"spp": args.ref_spp, "accumulation": "fp64", "seconds": ref_s},
+        "target_relmse": 0.01, "relmse": "mean (x - r)^2 / (r^2 + 1e-2) over pixels and RGB",
+        "plain": {k: plain[k] for k in ("time_s", "spp", "relmse", "reached")},
+        "guided": {k: guided[k] for k in ("time_s", "spp", "relmse", "reached")},
+        "guided_settings": {"alpha": 0.5, "train_fraction_of_plain_time": 0.25, "adam_steps_per_pass": 16,
+                            "batch": 65536, "target": "incident radiance x BSDF cosine", "guided_vertices": "all"},
+        "speedup_wall_time": plain["time_s"] / guided["time_s"] if guided["reached"] and plain["reached"] else None,
+        "speedup_samples": plain["spp"] / guided["spp"] if guided["reached"] and plain["reached"] else None,
+    }
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -173,6 +222,8 @@ def main():
     ap.add_argument("--tris", type=int, default=N_TRI)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-render", action="store_true", help="skip the path-tracing and guided-vs-plain sections")
+    ap.add_argument("--ref-spp", type=int, default=16384, help="spp of the FP64 reference of the guided-vs-plain run")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -271,6 +322,8 @@ def main():
                "h2d_bytes_per_step": int(rp.nbytes), "d2h_bytes_per_step": int(hp.nbytes),
                "ms_per_step": e2e_s * 1e3, "gpu_launches_per_step": (args.rays + (1 << 21) - 1) >> 21}
 
+    render = None if args.no_render else render_sections(args)
+
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -309,6 +362,8 @@ def main():
         out["e2e"] = e2e
     if cpu:
         out["cpu_baseline"] = cpu
+    if render:
+        out.update(render)
     print(json.dumps(out))
     if dist:
         dist.destroy_process_group()

@@ -293,6 +293,19 @@ int gbrt_guide_set_params(gbrt_guide *guide, const float *mlp, const float *tabl
 /* Mixture parameters for n positions (device, 3 floats each): 40 floats per
  * position, per lobe {mu xyz, kappa, weight}. */
 int gbrt_guide_eval(gbrt_guide *guide, const float *pos_dev, uint32_t n, float *lobes_dev, void *stream);
+/* Units that run the forward pass (gbrt_guide_eval and the path tracer's
+ * per-vertex evaluation): tensor cores (tcgen05, BF16 operands, FP32
+ * accumulation; the default) or FP32 CUDA cores. */
+enum { GBRT_GUIDE_EVAL_TENSOR = 0, GBRT_GUIDE_EVAL_FP32 = 1 };
+int gbrt_guide_set_eval_mode(gbrt_guide *guide, int mode);
+/* Reads and clears the guide's device status flags (synchronous):
+ * bit 0 = a tensor-core MMA completion wait timed out (that kernel stopped
+ * early and its outputs are incomplete). */
+int gbrt_guide_status(gbrt_guide *guide, uint32_t *flags);
+/* Diagnostic: D[128][N] = A[128][K] * B[N][K]^T (host FP32 arrays) computed
+ * by one tcgen05 MMA chain with BF16 operands (rounded to nearest) and FP32
+ * accumulation; N and K multiples of 16 in [16, 64]. */
+int gbrt_tc_selftest(const float *A, const float *B, uint32_t N, uint32_t K, float *D);
 /* Loss gradient of n records (device) into the guide's gradient buffers;
  * loss_out (host, optional) receives the batch loss (synchronises). */
 int gbrt_guide_grad(gbrt_guide *guide, const float *records_dev, uint32_t n, float *loss_out, void *stream);

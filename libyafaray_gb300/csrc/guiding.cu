@@ -16,6 +16,7 @@
 #include "gbrt_internal.cuh"
 #include "guide_common.cuh"
 #include "guide_device.cuh"
+#include "tc_sm100.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -305,6 +306,200 @@ __global__ void k_adam(float *__restrict__ p, float *__restrict__ g, float *__re
 	}
 }
 
+
+// ---- tensor-core forward pass ------------------------------------------------
+// One CTA (4 warps) evaluates tiles of 128 positions: the encoding (hash-grid
+// gathers, one position per thread) is written as BF16 into shared memory,
+// then each layer is one tcgen05 MMA chain (M = 128, N = 64 / 64 / 48,
+// K = 32 / 64 / 64) into TMEM, and the epilogue (bias, ReLU, BF16) reads each
+// thread's TMEM lane and writes the next layer's operand.
+constexpr int kTcThreads = 128;
+constexpr uint32_t kTcCols = 128;              // TMEM columns: D1 [0,64), D2 [64,128), D3 reuses [0,48)
+constexpr uint32_t kTcWaitIters = 1u << 24;    // bounded mbarrier wait
+constexpr uint32_t kSmA0 = 0, kSmA1 = 16384, kSmB1 = 32768, kSmB2 = 36864, kSmB3 = 45056, kSmBias = 51200;
+constexpr uint32_t kSmMbar = 51904, kSmSlot = 51912, kSmTotal = 51968;
+
+__device__ __forceinline__ void tc_load_weights(const float *__restrict__ mlp, uint8_t *smem, float *bias)
+{
+	for(int i = threadIdx.x; i < kGuideHidden * kGuideIn; i += blockDim.x)
+	{
+		const int r = i / kGuideIn, k = i % kGuideIn;
+		*reinterpret_cast<__nv_bfloat16 *>(smem + kSmB1 + tc::kmajor_offset(r, k, kGuideIn)) = __float2bfloat16_rn(mlp[kOffW1 + i]);
+	}
+	for(int i = threadIdx.x; i < kGuideHidden * kGuideHidden; i += blockDim.x)
+	{
+		const int r = i / kGuideHidden, k = i % kGuideHidden;
+		*reinterpret_cast<__nv_bfloat16 *>(smem + kSmB2 + tc::kmajor_offset(r, k, kGuideHidden)) = __float2bfloat16_rn(mlp[kOffW2 + i]);
+	}
+	for(int i = threadIdx.x; i < kGuideOutPad * kGuideHidden; i += blockDim.x)
+	{
+		const int r = i / kGuideHidden, k = i % kGuideHidden;
+		const float w = r < kGuideOut ? mlp[kOffW3 + r * kGuideHidden + k] : 0.f;
+		*reinterpret_cast<__nv_bfloat16 *>(smem + kSmB3 + tc::kmajor_offset(r, k, kGuideHidden)) = __float2bfloat16_rn(w);
+	}
+	for(int i = threadIdx.x; i < 2 * kGuideHidden + kGuideOutPad; i += blockDim.x)
+	{
+		float b;
+		if(i < kGuideHidden) b = mlp[kOffB1 + i];
+		else if(i < 2 * kGuideHidden) b = mlp[kOffB2 + i - kGuideHidden];
+		else b = (i - 2 * kGuideHidden) < kGuideOut ? mlp[kOffB3 + i - 2 * kGuideHidden] : 0.f;
+		bias[i] = b;
+	}
+}
+
+// Issue a K-chain of MMAs (K/16 instructions) and commit to the mbarrier.
+__device__ __forceinline__ void tc_layer(uint32_t d_tmem, uint32_t a_saddr, uint32_t b_saddr, uint32_t K, uint32_t N, uint64_t *mbar)
+{
+	const uint32_t sbo = (K / 8) * 128u;
+	const uint32_t idesc = tc::idesc_bf16(128, N);
+	for(uint32_t kk = 0; kk < K / 16; ++kk)
+		tc::mma_bf16(d_tmem, tc::smem_desc(a_saddr + kk * 256u, 128u, sbo), tc::smem_desc(b_saddr + kk * 256u, 128u, sbo), idesc, kk > 0 ? 1u : 0u);
+	tc::mma_commit(mbar);
+}
+
+__global__ void __launch_bounds__(kTcThreads) k_guide_eval_tc(GuideGrid g, const float *__restrict__ table, const float *__restrict__ mlp,
+                                                              const float *__restrict__ pos, uint32_t n, const uint32_t *__restrict__ n_dev,
+                                                              float *__restrict__ lobes, uint32_t *__restrict__ err)
+{
+	extern __shared__ __align__(1024) uint8_t smem[];
+	float *bias = reinterpret_cast<float *>(smem + kSmBias);
+	uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + kSmMbar);
+	uint32_t *slot = reinterpret_cast<uint32_t *>(smem + kSmSlot);
+	const int t = threadIdx.x, warp = t >> 5;
+	tc_load_weights(mlp, smem, bias);
+	if(t == 0) { tc::mbar_init(mbar, 1); tc::fence_mbar_init(); }
+	if(warp == 0) tc::tmem_alloc(slot, kTcCols);
+	tc::fence_smem_async();
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+	const uint32_t tbase = *slot;
+	const uint32_t lane_addr = tbase + (static_cast<uint32_t>(warp * 32) << 16);
+	const uint32_t sA0 = tc::smem_addr(smem + kSmA0), sA1 = tc::smem_addr(smem + kSmA1);
+	const uint32_t sB1 = tc::smem_addr(smem + kSmB1), sB2 = tc::smem_addr(smem + kSmB2), sB3 = tc::smem_addr(smem + kSmB3);
+	const uint32_t count = n_dev ? min(*n_dev, n) : n;
+	uint32_t phase = 0;
+	bool ok = true;
+	for(uint32_t tile = blockIdx.x; tile * 128u < count; tile += gridDim.x)
+	{
+		const uint32_t s = tile * 128u + t;
+		const bool live = s < count;
+		float v[kGuideOutPad];
+		if(live)
+		{
+			const float p[3] = {pos[3ull * s], pos[3ull * s + 1], pos[3ull * s + 2]};
+			encode(g, table, p, v, nullptr, nullptr);
+		}
+		else
+			for(int i = 0; i < kGuideIn; ++i) v[i] = 0.f;
+		tc::store_bf16_row(smem + kSmA0, t, kGuideIn, v, 0, kGuideIn);
+		tc::fence_smem_async();
+		__syncthreads();
+		// layer 1: D1 = E W1^T
+		if(t == 0) { tc::fence_after_sync(); tc_layer(tbase, sA0, sB1, kGuideIn, kGuideHidden, mbar); }
+		ok = __syncthreads_and(tc::mbar_wait(mbar, phase, kTcWaitIters));
+		phase ^= 1u;
+		if(!ok) break;
+		tc::fence_after_sync();
+		for(int c = 0; c < kGuideHidden / 16; ++c)
+		{
+			tc::tmem_ld16(lane_addr + 16u * c, v);
+			for(int i = 0; i < 16; ++i) v[i] = fmaxf(v[i] + bias[16 * c + i], 0.f);
+			tc::store_bf16_row(smem + kSmA1, t, kGuideHidden, v, 16u * c, 16);
+		}
+		tc::fence_before_sync();
+		tc::fence_smem_async();
+		__syncthreads();
+		// layer 2: D2 = H1 W2^T
+		if(t == 0) { tc::fence_after_sync(); tc_layer(tbase + 64u, sA1, sB2, kGuideHidden, kGuideHidden, mbar); }
+		ok = __syncthreads_and(tc::mbar_wait(mbar, phase, kTcWaitIters));
+		phase ^= 1u;
+		if(!ok) break;
+		tc::fence_after_sync();
+		for(int c = 0; c < kGuideHidden / 16; ++c)
+		{
+			tc::tmem_ld16(lane_addr + 64u + 16u * c, v);
+			for(int i = 0; i < 16; ++i) v[i] = fmaxf(v[i] + bias[kGuideHidden + 16 * c + i], 0.f);
+			tc::store_bf16_row(smem + kSmA0, t, kGuideHidden, v, 16u * c, 16);
+		}
+		tc::fence_before_sync();
+		tc::fence_smem_async();
+		__syncthreads();
+		// layer 3: D3 = H2 W3^T (40 outputs padded to 48), into columns [0, 48)
+		if(t == 0) { tc::fence_after_sync(); tc_layer(tbase, sA0, sB3, kGuideHidden, kGuideOutPad, mbar); }
+		ok = __syncthreads_and(tc::mbar_wait(mbar, phase, kTcWaitIters));
+		phase ^= 1u;
+		if(!ok) break;
+		tc::fence_after_sync();
+		for(int c = 0; c < kGuideOutPad / 16; ++c)
+		{
+			tc::tmem_ld16(lane_addr + 16u * c, v + 16 * c);
+			for(int i = 0; i < 16; ++i) v[16 * c + i] += bias[2 * kGuideHidden + 16 * c + i];
+		}
+		if(live)
+		{
+			float lo[kGuideOut];
+			raw_to_lobes(v, lo);
+			float4 *out = reinterpret_cast<float4 *>(lobes + static_cast<size_t>(kGuideOut) * s);
+			for(int k = 0; k < kGuideOut / 4; ++k) out[k] = make_float4(lo[4 * k], lo[4 * k + 1], lo[4 * k + 2], lo[4 * k + 3]);
+		}
+		tc::fence_before_sync();
+		__syncthreads();
+	}
+	if(!ok)
+	{
+		if(t == 0) atomicOr(err, 1u);
+		tc::mbar_wait(mbar, phase ^ 1u, kTcWaitIters);   // the phase that timed out: let its MMAs finish before freeing TMEM
+	}
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+	if(warp == 0) tc::tmem_dealloc(tbase, kTcCols);
+}
+
+// Self-test of the tcgen05 path: D[128][N] = A[128][K] B[N][K]^T in BF16 with
+// FP32 accumulation, through the same layouts, descriptors and TMEM loads.
+__global__ void __launch_bounds__(kTcThreads) k_tc_selftest(const float *__restrict__ A, const float *__restrict__ B, uint32_t N, uint32_t K,
+                                                            float *__restrict__ D, uint32_t *__restrict__ err)
+{
+	extern __shared__ __align__(1024) uint8_t smem[];
+	uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + kSmMbar);
+	uint32_t *slot = reinterpret_cast<uint32_t *>(smem + kSmSlot);
+	const int t = threadIdx.x, warp = t >> 5;
+	for(uint32_t i = t; i < 128u * K; i += blockDim.x)
+		*reinterpret_cast<__nv_bfloat16 *>(smem + kSmA0 + tc::kmajor_offset(i / K, i % K, K)) = __float2bfloat16_rn(A[i]);
+	for(uint32_t i = t; i < N * K; i += blockDim.x)
+		*reinterpret_cast<__nv_bfloat16 *>(smem + kSmA1 + tc::kmajor_offset(i / K, i % K, K)) = __float2bfloat16_rn(B[i]);
+	if(t == 0) { tc::mbar_init(mbar, 1); tc::fence_mbar_init(); }
+	if(warp == 0) tc::tmem_alloc(slot, kTcCols);
+	tc::fence_smem_async();
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+	const uint32_t tbase = *slot;
+	if(t == 0) { tc::fence_after_sync(); tc_layer(tbase, tc::smem_addr(smem + kSmA0), tc::smem_addr(smem + kSmA1), K, N, mbar); }
+	const bool ok = __syncthreads_and(tc::mbar_wait(mbar, 0, kTcWaitIters));
+	tc::fence_after_sync();
+	if(ok)
+	{
+		float v[16];
+		for(uint32_t c = 0; c < N / 16; ++c)
+		{
+			tc::tmem_ld16(tbase + (static_cast<uint32_t>(warp * 32) << 16) + 16u * c, v);
+			for(int i = 0; i < 16; ++i) D[static_cast<size_t>(t) * N + 16u * c + i] = v[i];
+		}
+	}
+	else
+	{
+		if(t == 0) atomicOr(err, 1u);
+		tc::mbar_wait(mbar, 0, kTcWaitIters);
+	}
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+	if(warp == 0) tc::tmem_dealloc(tbase, kTcCols);
+}
+
 } // namespace
 
 struct gbrt_guide {
@@ -317,6 +512,8 @@ struct gbrt_guide {
 	float *partial = nullptr;
 	size_t partial_blocks = 0;
 	float *loss = nullptr;    // [0] loss, [1] record weight sum
+	uint32_t *tc_err = nullptr; // set by the tensor-core kernels when an MMA wait times out
+	int eval_mode = GBRT_GUIDE_EVAL_TENSOR;
 	int step = 0;
 	int n_sm = 0;
 };
@@ -331,6 +528,28 @@ int guide_alloc(gbrt_guide *G)
 	float **mb[] = {&G->mlp, &G->mlp_g, &G->mlp_m, &G->mlp_v};
 	for(float **b : mb) GBRT_CK(cudaMalloc(b, kMlpParams * sizeof(float)));
 	GBRT_CK(cudaMalloc(&G->loss, 2 * sizeof(float)));
+	GBRT_CK(cudaMalloc(&G->tc_err, sizeof(uint32_t)));
+	GBRT_CK(cudaMemset(G->tc_err, 0, sizeof(uint32_t)));
+	return GBRT_OK;
+}
+
+// Forward pass of a queue of positions on the selected units.
+int launch_eval(gbrt_guide *G, const float *pos, uint32_t cap, const uint32_t *count_dev, float *lobes, cudaStream_t s)
+{
+	if(G->eval_mode == GBRT_GUIDE_EVAL_TENSOR)
+	{
+		static bool attr = false;
+		if(!attr) { GBRT_CK(cudaFuncSetAttribute(k_guide_eval_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmTotal))); attr = true; }
+		const size_t tiles = (static_cast<size_t>(cap) + 127) / 128;
+		const unsigned grid = static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>(tiles, static_cast<size_t>(G->n_sm) * 4)));
+		k_guide_eval_tc<<<grid, kTcThreads, kSmTotal, s>>>(G->grid, G->table, G->mlp, pos, cap, count_dev, lobes, G->tc_err);
+	}
+	else
+	{
+		const unsigned grid = static_cast<unsigned>(std::min<size_t>((cap + kEvalThreads - 1) / kEvalThreads, static_cast<size_t>(G->n_sm) * 8));
+		k_guide_eval<<<std::max(1u, grid), kEvalThreads, 0, s>>>(G->grid, G->table, G->mlp, pos, cap, count_dev, lobes);
+	}
+	GBRT_CK(cudaGetLastError());
 	return GBRT_OK;
 }
 
@@ -399,7 +618,7 @@ int gbrt_guide_create(const float bound[6], const gbrt_guide_params *params, gbr
 int gbrt_guide_destroy(gbrt_guide *G)
 {
 	if(!G) return GBRT_OK;
-	void *ptrs[] = {G->table, G->table_g, G->table_m, G->table_v, G->mlp, G->mlp_g, G->mlp_m, G->mlp_v, G->partial, G->loss};
+	void *ptrs[] = {G->table, G->table_g, G->table_m, G->table_v, G->mlp, G->mlp_g, G->mlp_m, G->mlp_v, G->partial, G->loss, G->tc_err};
 	for(void *p : ptrs) if(p) cudaFree(p);
 	delete G;
 	return GBRT_OK;
@@ -425,9 +644,51 @@ int gbrt_guide_eval(gbrt_guide *G, const float *pos_dev, uint32_t n, float *lobe
 {
 	if(!G || (n && (!pos_dev || !lobes_dev))) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_eval: NULL argument");
 	if(n == 0) return GBRT_OK;
-	const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + kEvalThreads - 1) / kEvalThreads, static_cast<size_t>(G->n_sm) * 8));
-	k_guide_eval<<<grid, kEvalThreads, 0, static_cast<cudaStream_t>(stream)>>>(G->grid, G->table, G->mlp, pos_dev, n, nullptr, lobes_dev);
-	GBRT_CK(cudaGetLastError());
+	return launch_eval(G, pos_dev, n, nullptr, lobes_dev, static_cast<cudaStream_t>(stream));
+}
+
+int gbrt_guide_set_eval_mode(gbrt_guide *G, int mode)
+{
+	if(!G) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_set_eval_mode: NULL");
+	if(mode != GBRT_GUIDE_EVAL_TENSOR && mode != GBRT_GUIDE_EVAL_FP32)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_set_eval_mode: unknown mode %d", mode);
+	G->eval_mode = mode;
+	return GBRT_OK;
+}
+
+int gbrt_guide_status(gbrt_guide *G, uint32_t *flags)
+{
+	if(!G || !flags) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_status: NULL");
+	GBRT_CK(cudaMemcpy(flags, G->tc_err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+	GBRT_CK(cudaMemset(G->tc_err, 0, sizeof(uint32_t)));
+	return GBRT_OK;
+}
+
+int gbrt_tc_selftest(const float *A, const float *B, uint32_t N, uint32_t K, float *D)
+{
+	if(!A || !B || !D) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_tc_selftest: NULL argument");
+	if(N < 16 || N > 64 || N % 16 || K < 16 || K > 64 || K % 16)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_tc_selftest: N=%u K=%u (each a multiple of 16 in [16, 64])", N, K);
+	float *dA = nullptr, *dB = nullptr, *dD = nullptr;
+	uint32_t *dErr = nullptr, herr = 0;
+	cudaError_t e = cudaMalloc(&dA, 128ull * K * 4);
+	if(e == cudaSuccess) e = cudaMalloc(&dB, static_cast<size_t>(N) * K * 4);
+	if(e == cudaSuccess) e = cudaMalloc(&dD, 128ull * N * 4);
+	if(e == cudaSuccess) e = cudaMalloc(&dErr, 4);
+	if(e == cudaSuccess) e = cudaMemset(dErr, 0, 4);
+	if(e == cudaSuccess) e = cudaMemcpy(dA, A, 128ull * K * 4, cudaMemcpyHostToDevice);
+	if(e == cudaSuccess) e = cudaMemcpy(dB, B, static_cast<size_t>(N) * K * 4, cudaMemcpyHostToDevice);
+	if(e == cudaSuccess) e = cudaFuncSetAttribute(k_tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmTotal));
+	if(e == cudaSuccess)
+	{
+		k_tc_selftest<<<1, kTcThreads, kSmTotal>>>(dA, dB, N, K, dD, dErr);
+		e = cudaGetLastError();
+	}
+	if(e == cudaSuccess) e = cudaMemcpy(D, dD, 128ull * N * 4, cudaMemcpyDeviceToHost);
+	if(e == cudaSuccess) e = cudaMemcpy(&herr, dErr, 4, cudaMemcpyDeviceToHost);
+	cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(dErr);
+	if(e != cudaSuccess) return gbrt_set_error(GBRT_ERR_CUDA, "gbrt_tc_selftest: %s", cudaGetErrorString(e));
+	if(herr) return gbrt_set_error(GBRT_ERR_CUDA, "gbrt_tc_selftest: MMA completion wait timed out");
 	return GBRT_OK;
 }
 
@@ -547,8 +808,5 @@ extern "C" int gbrt_guide_forward_host(const float bound[6], const gbrt_guide_pa
 // Used by the path tracer: lobes for the hit points of a queue.
 int gbrt_guide_eval_queue(gbrt_guide *G, const float *pos_dev, uint32_t cap, const uint32_t *count_dev, float *lobes_dev, cudaStream_t s)
 {
-	const unsigned grid = static_cast<unsigned>(std::min<size_t>((cap + kEvalThreads - 1) / kEvalThreads, static_cast<size_t>(G->n_sm) * 8));
-	k_guide_eval<<<std::max(1u, grid), kEvalThreads, 0, s>>>(G->grid, G->table, G->mlp, pos_dev, cap, count_dev, lobes_dev);
-	GBRT_CK(cudaGetLastError());
-	return GBRT_OK;
+	return launch_eval(G, pos_dev, cap, count_dev, lobes_dev, s);
 }

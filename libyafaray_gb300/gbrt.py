@@ -106,6 +106,9 @@ SIGNATURES = {
     "gbrt_guide_get_grads": (_I, [_VP, _VP, _VP]),
     "gbrt_guide_step": (_I, [_VP, _VP, _U32, ctypes.POINTER(ctypes.c_float), _VP]),
     "gbrt_guide_forward_host": (_I, [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(GuideParams), _VP, _VP, _VP, _U32, _VP]),
+    "gbrt_guide_set_eval_mode": (_I, [_VP, ctypes.c_int]),
+    "gbrt_guide_status": (_I, [_VP, ctypes.POINTER(ctypes.c_uint32)]),
+    "gbrt_tc_selftest": (_I, [_VP, _VP, _U32, _U32, _VP]),
     "gbrt_pt_render": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP, _VP,
                             ctypes.POINTER(PtStats), _VP]),
     "gbrt_pt_render_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP,
@@ -390,6 +393,18 @@ class Guide:
         check(load().gbrt_guide_get_grads(self._h, _ptr(mlp), _ptr(tab)))
         return mlp, tab.reshape(16, 1 << self.log2_table, 2)
 
+    EVAL_TENSOR, EVAL_FP32 = 0, 1
+
+    def set_eval_mode(self, mode):
+        """EVAL_TENSOR (tcgen05, BF16 operands, the default) or EVAL_FP32."""
+        check(load().gbrt_guide_set_eval_mode(self._h, int(mode)))
+
+    def status(self):
+        """Reads and clears the device status flags (bit 0: an MMA wait timed out)."""
+        f = ctypes.c_uint32()
+        check(load().gbrt_guide_status(self._h, ctypes.byref(f)))
+        return f.value
+
     def eval_device(self, pos_ptr, n, lobes_ptr, stream=0):
         check(load().gbrt_guide_eval(self._h, ctypes.c_void_p(pos_ptr), n, ctypes.c_void_p(lobes_ptr), ctypes.c_void_p(stream)))
 
@@ -402,6 +417,18 @@ class Guide:
         loss = ctypes.c_float()
         check(load().gbrt_guide_step(self._h, ctypes.c_void_p(rec_ptr), n, ctypes.byref(loss), ctypes.c_void_p(stream)))
         return loss.value
+
+
+def tc_selftest(a, b):
+    """D = A B^T through one tcgen05 MMA chain (BF16 operands, FP32
+    accumulation); A [128, K], B [N, K]."""
+    A = np.ascontiguousarray(a, np.float32)
+    B = np.ascontiguousarray(b, np.float32)
+    n, k = B.shape
+    assert A.shape == (128, k)
+    D = np.empty((128, n), np.float32)
+    check(load().gbrt_tc_selftest(_ptr(A), _ptr(B), n, k, _ptr(D)))
+    return D
 
 
 def guide_forward_host(bound, mlp, table, pos, log2_table=19, base_resolution=16.0, max_resolution=2048.0):

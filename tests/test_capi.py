@@ -5,6 +5,8 @@ import os
 import re
 import subprocess
 
+import pytest
+
 from libyafaray_gb300 import gbrt
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -39,3 +41,17 @@ def test_null_arguments_are_errors_not_crashes(gbrt_lib):
     assert L.gbrt_trace_closest(None, None, 10, None, None) == -1
     assert L.gbrt_bvh_destroy(None) == 0
     assert L.gbrt_version() >= 1
+
+
+def test_guide_and_tensor_core_argument_checks(gbrt_lib):
+    """Argument errors are reported before any CUDA call."""
+    import numpy as np
+    from libyafaray_gb300 import gbrt
+    L = gbrt_lib
+    assert L.gbrt_guide_set_eval_mode(None, 0) == -1
+    assert L.gbrt_guide_status(None, None) == -1
+    a = np.zeros((128, 16), np.float32)
+    with pytest.raises(gbrt.GbrtError, match="multiple of 16"):
+        gbrt.tc_selftest(np.zeros((128, 8), np.float32), np.zeros((8, 8), np.float32))
+    with pytest.raises(gbrt.GbrtError, match="multiple of 16"):
+        gbrt.tc_selftest(a, np.zeros((80, 16), np.float32))

@@ -34,9 +34,77 @@ def _records(rng, n):
     return r
 
 
+def bf16(x):
+    """Round FP32 values to BF16 (nearest, ties to even), returned as FP32."""
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
+
+
+@pytest.mark.parametrize("n,k", [(16, 16), (64, 32), (48, 64), (64, 64)])
+def test_tcgen05_gemm_selftest(cuda_device, n, k):
+    """One tcgen05 MMA chain (operand layout, descriptors, TMEM loads) equals
+    the BF16-rounded product accumulated in FP64, up to FP32 summation."""
+    rng = np.random.default_rng(n * 100 + k)
+    a = rng.normal(size=(128, k)).astype(np.float32)
+    b = rng.normal(size=(n, k)).astype(np.float32)
+    d = gbrt.tc_selftest(a, b)
+    exp = bf16(a).astype(np.float64) @ bf16(b).astype(np.float64).T
+    scale = np.abs(bf16(a)).astype(np.float64) @ np.abs(bf16(b)).astype(np.float64).T
+    err = np.abs(d - exp) / np.maximum(scale, 1e-30)
+    assert err.max() < 1e-5, (err.max(), np.unravel_index(err.argmax(), err.shape))
+
+
+def _oracle_lobes(grid, mlp, tab, p, tensor):
+    """Oracle forward; tensor=True rounds the layer inputs and weights to
+    BF16 as the tensor-core path does (accumulation stays FP64)."""
+    e, _ = grid.encode(tab.astype(np.float64), p)
+    m = mlp.astype(np.float64)
+    if not tensor:
+        return go.lobes(go.mlp_forward(m, e)[2])
+    r = lambda x: bf16(np.asarray(x, np.float32)).astype(np.float64)
+    W1 = r(m[go.OFF_W1:go.OFF_B1]).reshape(go.HID, go.IN); b1 = m[go.OFF_B1:go.OFF_W2]
+    W2 = r(m[go.OFF_W2:go.OFF_B2]).reshape(go.HID, go.HID); b2 = m[go.OFF_B2:go.OFF_W3]
+    W3 = r(m[go.OFF_W3:go.OFF_B3]).reshape(go.OUT, go.HID); b3 = m[go.OFF_B3:go.N_MLP]
+    h1 = np.maximum(W1 @ r(e) + b1, 0)
+    h2 = np.maximum(W2 @ r(h1) + b2, 0)
+    return go.lobes(W3 @ r(h2) + b3)
+
+
+def test_guide_eval_tensor_cores_match_oracle(cuda_device):
+    """tcgen05 forward pass against the oracle with the same BF16 operand
+    rounding: >= 99 % of positions within rtol 1e-2 / atol 2e-3 (a BF16
+    rounding flip of one operand moves an output by ~1e-3 relative), all
+    within rtol 5e-2 / atol 1e-2; and against the exact FP64 forward within
+    BF16-level error on average."""
+    torch = pytest.importorskip("torch")
+    g, grid, mlp, tab, rng = _setup(seed=7)
+    n = 1000                                  # 8 tiles of 128, the last one ragged
+    rec = _records(rng, n)
+    pos = torch.from_numpy(np.ascontiguousarray(rec[:, :3])).cuda()
+    out = torch.full((n + 128, 40), -7.0, dtype=torch.float32, device="cuda")
+    g.set_eval_mode(gbrt.Guide.EVAL_TENSOR)
+    g.eval_device(pos.data_ptr(), n, out.data_ptr())
+    torch.cuda.synchronize()
+    assert g.status() == 0
+    got = out.cpu().numpy()
+    assert np.all(got[n:] == -7.0), "wrote past the last position"
+    tight, loose, dev = 0, True, []
+    for i in range(n):
+        exp = _oracle_lobes(grid, mlp, tab, rec[i, :3], tensor=True)
+        tight += np.allclose(got[i], exp, rtol=1e-2, atol=2e-3)
+        loose &= bool(np.allclose(got[i], exp, rtol=5e-2, atol=1e-2))
+        ex = _oracle_lobes(grid, mlp, tab, rec[i, :3], tensor=False)
+        dev.append(np.abs(got[i] - ex).mean())
+    print(f"tensor-core eval: {tight}/{n} rows tight, mean |dev| from FP64 {np.mean(dev):.2e}")
+    assert tight >= 0.99 * n and loose
+    assert np.mean(dev) < 1e-2
+
+
 def test_guide_eval_matches_oracle(cuda_device):
     torch = pytest.importorskip("torch")
     g, grid, mlp, tab, rng = _setup()
+    g.set_eval_mode(gbrt.Guide.EVAL_FP32)
     rec = _records(rng, 200)
     pos = torch.from_numpy(np.ascontiguousarray(rec[:, :3])).cuda()
     out = torch.empty((200, 40), dtype=torch.float32, device="cuda")
@@ -117,16 +185,18 @@ def test_guided_render_is_unbiased(cuda_device):
 
 
 def test_trained_guide_lowers_error_at_equal_samples(cuda_device):
-    """What the trained network gains: relMSE at 32 spp against an 8192-spp
-    plain reference, guided (after online training) vs plain."""
+    """What the trained network gains: relMSE at 64 spp against an 8192-spp
+    plain reference, guided (after online training) vs plain.  relMSE of a
+    64-spp image of this scene is heavy-tailed (rare long paths through the
+    door gap), so the comparison is of medians over 12 independent images."""
     r = gbrt.Renderer(_indoor_small())
     ref = np.mean([r.render(1024, base_offset=10_000_000 + b * 1024, seed=900 + b)[0] for b in range(8)], axis=0)
     guide = r.make_guide(log2_table=16, seed=4)
-    _train(r, guide, passes=12)
+    _train(r, guide, passes=24)
 
     def relmse(x):
         return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
-    ep = np.mean([relmse(r.render(32, base_offset=b * 32, seed=70 + b)[0]) for b in range(6)])
-    eg = np.mean([relmse(r.render(32, base_offset=b * 32, seed=70 + b, guide=guide, alpha=0.5)[0]) for b in range(6)])
-    print(f"relMSE at 32 spp: plain {ep:.4g}, guided {eg:.4g} (x{ep / eg:.2f})")
+    ep = np.median([relmse(r.render(64, base_offset=b * 64, seed=70 + b)[0]) for b in range(12)])
+    eg = np.median([relmse(r.render(64, base_offset=b * 64, seed=70 + b, guide=guide, alpha=0.5)[0]) for b in range(12)])
+    print(f"median relMSE at 64 spp: plain {ep:.4g}, guided {eg:.4g} (x{ep / eg:.2f})")
     assert eg < ep
