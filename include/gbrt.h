@@ -293,9 +293,10 @@ int gbrt_guide_set_params(gbrt_guide *guide, const float *mlp, const float *tabl
 /* Mixture parameters for n positions (device, 3 floats each): 40 floats per
  * position, per lobe {mu xyz, kappa, weight}. */
 int gbrt_guide_eval(gbrt_guide *guide, const float *pos_dev, uint32_t n, float *lobes_dev, void *stream);
-/* Units that run the forward pass (gbrt_guide_eval and the path tracer's
- * per-vertex evaluation): tensor cores (tcgen05, BF16 operands, FP32
- * accumulation; the default) or FP32 CUDA cores. */
+/* Units that run the network (gbrt_guide_eval, the path tracer's per-vertex
+ * evaluation, and the forward/backward pass of gbrt_guide_grad and
+ * gbrt_guide_step): tensor cores (tcgen05, BF16 operands and activations,
+ * FP32 accumulation; the default) or FP32 CUDA cores. */
 enum { GBRT_GUIDE_EVAL_TENSOR = 0, GBRT_GUIDE_EVAL_FP32 = 1 };
 int gbrt_guide_set_eval_mode(gbrt_guide *guide, int mode);
 /* Reads and clears the guide's device status flags (synchronous):

@@ -500,6 +500,289 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_selftest(const float *__restr
 	if(warp == 0) tc::tmem_dealloc(tbase, kTcCols);
 }
 
+// ---- tensor-core training step ----------------------------------------------
+// One CTA per SM, tiles of 128 records.  Per tile, six tcgen05 stages:
+//   L1..L3   forward (as in k_guide_eval_tc), activations kept in shared
+//            memory twice: [record][feature] (A operand of the next layer)
+//            and [feature][record] (operand of the weight-gradient GEMMs)
+//   dH2      dO  [128x48] . W3  -> ReLU mask -> dA2
+//   dH1      dA2 [128x64] . W2  -> ReLU mask -> dA1
+//   dE       dA1 [128x64] . W1  -> scattered into the hash-grid gradient
+// with the weight gradients accumulated in TMEM over all tiles of the CTA:
+//   G1 [128 x 112] += [dA2^T ; dA1^T] . [H1^T ; E^T ; 1]^T
+//        rows 0-63:  dW2 (cols 0-63), db2 (col 96)
+//        rows 64-127: dW1 (cols 64-95), db1 (col 96)
+//   G2 [128 x 48]  += [H2^T ; 1] . dO
+//        rows 0-63: dW3^T, rows 64-127: db3
+// The cross blocks of G1 (dA2^T E, dA1^T H1) are computed and ignored.
+constexpr uint32_t kTrThreads = 128;
+constexpr uint32_t kTrCols = 256;
+constexpr uint32_t kTrW1 = 0, kTrW2 = 4096, kTrW3 = 12288, kTrW3T = 18432, kTrW2T = 24576, kTrW1T = 32768;
+constexpr uint32_t kTrCH0 = 36864, kTrCH1 = 53248;                       // [128][<=64] chain operands
+constexpr uint32_t kTrH2T = 69632, kTrOne64 = 86016;                     // G2 A: rows 0-63, 64-127
+constexpr uint32_t kTrDA2T = 102400, kTrDA1T = 118784;                   // G1 A: rows 0-63, 64-127
+constexpr uint32_t kTrH1T = 135168, kTrET = 151552, kTrOne16 = 159744;   // G1 B: rows 0-63, 64-95, 96-111
+constexpr uint32_t kTrDOT = 163840;                                      // G2 B: rows 0-47 (40-47 zero)
+constexpr uint32_t kTrBias = 176128, kTrMbar = 176832, kTrSlot = 176840, kTrTotal = 176896;
+constexpr uint32_t kTrColG1 = 64, kTrColG2 = 192;                        // TMEM: scratch [0,64), G1, G2
+
+__device__ __forceinline__ void st_bf16(uint8_t *smem, uint32_t off, float x)
+{
+	*reinterpret_cast<__nv_bfloat16 *>(smem + off) = __float2bfloat16_rn(x);
+}
+
+// [feature][record] copy of one record's row (K = 128 records).
+__device__ __forceinline__ void store_bf16_col(uint8_t *base, uint32_t rec, const float *v, uint32_t nfeat)
+{
+	for(uint32_t f = 0; f < nfeat; ++f) st_bf16(base, tc::kmajor_offset(f, rec, 128), v[f]);
+}
+
+// Hash-grid gradient: corner weights x dL/de, as in encode.
+__device__ __forceinline__ void scatter_grid_grad(const GuideGrid &g, const float p[3], const float de[kGuideIn], float *__restrict__ grid_grad)
+{
+	float x[3];
+	for(int a = 0; a < 3; ++a) x[a] = fminf(fmaxf((p[a] - g.lo[a]) * g.inv_ext[a], 0.f), 1.f);
+#pragma unroll 1
+	for(int l = 0; l < kGuideLevels; ++l)
+	{
+		const float r = g.res[l];
+		float fx[3];
+		uint32_t ix[3];
+		for(int a = 0; a < 3; ++a)
+		{
+			const float s = x[a] * r;
+			const float fl = fminf(floorf(s), r - 1.f);
+			ix[a] = static_cast<uint32_t>(fl);
+			fx[a] = s - fl;
+		}
+		const float d0 = de[2 * l], d1 = de[2 * l + 1];
+		for(int c = 0; c < 8; ++c)
+		{
+			const uint32_t dx = c & 1, dy = (c >> 1) & 1, dz = (c >> 2) & 1;
+			const float w = (dx ? fx[0] : 1.f - fx[0]) * (dy ? fx[1] : 1.f - fx[1]) * (dz ? fx[2] : 1.f - fx[2]);
+			const size_t off = (static_cast<size_t>(l) << g.log2_table) + grid_index(g, l, ix[0] + dx, ix[1] + dy, ix[2] + dz);
+			atomicAdd(reinterpret_cast<float2 *>(grid_grad) + off, make_float2(w * d0, w * d1));
+		}
+	}
+}
+
+// A K-chain of MMAs (K/16 instructions) without commit; the operand row
+// strides are given separately for A and B (both K-major, no swizzle).
+__device__ __forceinline__ void tc_chain(uint32_t d_tmem, uint32_t a_saddr, uint32_t b_saddr, uint32_t K, uint32_t N, bool accumulate)
+{
+	const uint32_t sbo = (K / 8) * 128u;
+	const uint32_t idesc = tc::idesc_bf16(128, N);
+	for(uint32_t kk = 0; kk < K / 16; ++kk)
+		tc::mma_bf16(d_tmem, tc::smem_desc(a_saddr + kk * 256u, 128u, sbo), tc::smem_desc(b_saddr + kk * 256u, 128u, sbo), idesc,
+		             (accumulate || kk > 0) ? 1u : 0u);
+}
+
+__global__ void __launch_bounds__(kTrThreads, 1) k_guide_train_tc(GuideGrid g, const float *__restrict__ table, const float *__restrict__ mlp,
+                                                                  const float *__restrict__ rec, uint32_t n, const float *__restrict__ wsum,
+                                                                  float *__restrict__ partial, float *__restrict__ grid_grad,
+                                                                  float *__restrict__ loss_out, uint32_t *__restrict__ err)
+{
+	extern __shared__ __align__(1024) uint8_t smem[];
+	float *bias = reinterpret_cast<float *>(smem + kTrBias);
+	uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + kTrMbar);
+	uint32_t *slot = reinterpret_cast<uint32_t *>(smem + kTrSlot);
+	const int t = threadIdx.x, warp = t >> 5;
+	// weights in both orientations, biases, constant blocks
+	for(int i = t; i < kGuideHidden * kGuideIn; i += blockDim.x)
+	{
+		const int j = i / kGuideIn, f = i % kGuideIn;
+		st_bf16(smem, kTrW1 + tc::kmajor_offset(j, f, kGuideIn), mlp[kOffW1 + i]);
+		st_bf16(smem, kTrW1T + tc::kmajor_offset(f, j, kGuideHidden), mlp[kOffW1 + i]);
+	}
+	for(int i = t; i < kGuideHidden * kGuideHidden; i += blockDim.x)
+	{
+		const int j = i / kGuideHidden, k = i % kGuideHidden;
+		st_bf16(smem, kTrW2 + tc::kmajor_offset(j, k, kGuideHidden), mlp[kOffW2 + i]);
+		st_bf16(smem, kTrW2T + tc::kmajor_offset(k, j, kGuideHidden), mlp[kOffW2 + i]);
+	}
+	for(int i = t; i < kGuideOutPad * kGuideHidden; i += blockDim.x)
+	{
+		const int o = i / kGuideHidden, j = i % kGuideHidden;
+		const float w = o < kGuideOut ? mlp[kOffW3 + o * kGuideHidden + j] : 0.f;
+		st_bf16(smem, kTrW3 + tc::kmajor_offset(o, j, kGuideHidden), w);
+		st_bf16(smem, kTrW3T + tc::kmajor_offset(j, o, kGuideOutPad), w);
+	}
+	for(int i = t; i < 2 * kGuideHidden + kGuideOutPad; i += blockDim.x)
+	{
+		float b;
+		if(i < kGuideHidden) b = mlp[kOffB1 + i];
+		else if(i < 2 * kGuideHidden) b = mlp[kOffB2 + i - kGuideHidden];
+		else b = (i - 2 * kGuideHidden) < kGuideOut ? mlp[kOffB3 + i - 2 * kGuideHidden] : 0.f;
+		bias[i] = b;
+	}
+	{
+		const uint32_t one2 = 0x3F803F80u;   // two BF16 ones
+		uint32_t *o64 = reinterpret_cast<uint32_t *>(smem + kTrOne64), *o16 = reinterpret_cast<uint32_t *>(smem + kTrOne16);
+		uint32_t *dot = reinterpret_cast<uint32_t *>(smem + kTrDOT);
+		for(int i = t; i < 16384 / 4; i += blockDim.x) o64[i] = one2;
+		for(int i = t; i < 4096 / 4; i += blockDim.x) o16[i] = one2;
+		for(int i = t; i < 12288 / 4; i += blockDim.x) dot[i] = 0u;
+	}
+	if(t == 0) { tc::mbar_init(mbar, 1); tc::fence_mbar_init(); }
+	if(warp == 0) tc::tmem_alloc(slot, kTrCols);
+	tc::fence_smem_async();
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+	const uint32_t tbase = *slot;
+	const uint32_t lane_addr = tbase + (static_cast<uint32_t>(warp * 32) << 16);
+	const uint32_t s0 = tc::smem_addr(smem);
+	const float inv_norm = *wsum > 0.f ? 1.f / *wsum : 0.f;
+	const uint32_t ntiles = (n + 127u) / 128u;
+	uint32_t phase = 0;
+	bool ok = true, first = true;
+	float loss = 0.f;
+	// one MMA stage: make the shared-memory operands visible to the tensor
+	// core, issue from thread 0, wait (bounded) for completion
+	auto stage = [&](auto issue) -> bool {
+		tc::fence_smem_async();
+		tc::fence_before_sync();
+		__syncthreads();
+		if(t == 0) { tc::fence_after_sync(); issue(); tc::mma_commit(mbar); }
+		const bool done = __syncthreads_and(tc::mbar_wait(mbar, phase, kTcWaitIters));
+		phase ^= 1u;
+		tc::fence_after_sync();
+		return done;
+	};
+	for(uint32_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x)
+	{
+		const uint32_t r = tile * 128u + t;
+		const bool live = r < n;
+		float p[3] = {0.f, 0.f, 0.f}, w[3] = {0.f, 0.f, 1.f}, c = 0.f;
+		float v[kGuideHidden];
+		uint32_t m1lo = 0, m1hi = 0, m2lo = 0, m2hi = 0;   // ReLU masks
+		if(live)
+		{
+			const float4 a = *reinterpret_cast<const float4 *>(rec + 8ull * r);
+			const float4 b = *reinterpret_cast<const float4 *>(rec + 8ull * r + 4);
+			p[0] = a.x; p[1] = a.y; p[2] = a.z; w[0] = a.w; w[1] = b.x; w[2] = b.y;
+			c = b.z * inv_norm;
+			encode(g, table, p, v, nullptr, nullptr);
+		}
+		else
+			for(int i = 0; i < kGuideIn; ++i) v[i] = 0.f;
+		tc::store_bf16_row(smem + kTrCH0, t, kGuideIn, v, 0, kGuideIn);
+		store_bf16_col(smem + kTrET, t, v, kGuideIn);
+		// L1
+		if(!(ok = stage([&] { tc_chain(tbase, s0 + kTrCH0, s0 + kTrW1, kGuideIn, kGuideHidden, false); }))) break;
+		for(int cc = 0; cc < 4; ++cc) tc::tmem_ld16(lane_addr + 16u * cc, v + 16 * cc);
+		for(int i = 0; i < kGuideHidden; ++i)
+		{
+			const float a = v[i] + bias[i];
+			v[i] = fmaxf(a, 0.f);
+			if(a > 0.f) { if(i < 32) m1lo |= 1u << i; else m1hi |= 1u << (i - 32); }
+		}
+		tc::store_bf16_row(smem + kTrCH1, t, kGuideHidden, v, 0, kGuideHidden);
+		store_bf16_col(smem + kTrH1T, t, v, kGuideHidden);
+		// L2
+		if(!(ok = stage([&] { tc_chain(tbase, s0 + kTrCH1, s0 + kTrW2, kGuideHidden, kGuideHidden, false); }))) break;
+		for(int cc = 0; cc < 4; ++cc) tc::tmem_ld16(lane_addr + 16u * cc, v + 16 * cc);
+		for(int i = 0; i < kGuideHidden; ++i)
+		{
+			const float a = v[i] + bias[kGuideHidden + i];
+			v[i] = fmaxf(a, 0.f);
+			if(a > 0.f) { if(i < 32) m2lo |= 1u << i; else m2hi |= 1u << (i - 32); }
+		}
+		tc::store_bf16_row(smem + kTrCH0, t, kGuideHidden, v, 0, kGuideHidden);
+		store_bf16_col(smem + kTrH2T, t, v, kGuideHidden);
+		// L3 + loss head
+		if(!(ok = stage([&] { tc_chain(tbase, s0 + kTrCH0, s0 + kTrW3, kGuideHidden, kGuideOutPad, false); }))) break;
+		for(int cc = 0; cc < 3; ++cc) tc::tmem_ld16(lane_addr + 16u * cc, v + 16 * cc);
+		{
+			float o[kGuideOut], d3[kGuideOut];
+			for(int i = 0; i < kGuideOut; ++i) o[i] = v[i] + bias[2 * kGuideHidden + i];
+			if(live) loss += head_grad(o, w, c, d3);
+			else for(int i = 0; i < kGuideOut; ++i) d3[i] = 0.f;
+			for(int i = 0; i < kGuideOut; ++i) v[i] = d3[i];
+			for(int i = kGuideOut; i < kGuideOutPad; ++i) v[i] = 0.f;
+		}
+		tc::store_bf16_row(smem + kTrCH1, t, kGuideOutPad, v, 0, kGuideOutPad);
+		store_bf16_col(smem + kTrDOT, t, v, kGuideOut);
+		// dH2 = dO W3, ReLU mask of layer 2
+		if(!(ok = stage([&] { tc_chain(tbase, s0 + kTrCH1, s0 + kTrW3T, kGuideOutPad, kGuideHidden, false); }))) break;
+		for(int cc = 0; cc < 4; ++cc) tc::tmem_ld16(lane_addr + 16u * cc, v + 16 * cc);
+		for(int i = 0; i < kGuideHidden; ++i)
+			if(!(((i < 32 ? m2lo : m2hi) >> (i & 31)) & 1u)) v[i] = 0.f;
+		tc::store_bf16_row(smem + kTrCH0, t, kGuideHidden, v, 0, kGuideHidden);
+		store_bf16_col(smem + kTrDA2T, t, v, kGuideHidden);
+		// dH1 = dA2 W2, ReLU mask of layer 1
+		if(!(ok = stage([&] { tc_chain(tbase, s0 + kTrCH0, s0 + kTrW2T, kGuideHidden, kGuideHidden, false); }))) break;
+		for(int cc = 0; cc < 4; ++cc) tc::tmem_ld16(lane_addr + 16u * cc, v + 16 * cc);
+		for(int i = 0; i < kGuideHidden; ++i)
+			if(!(((i < 32 ? m1lo : m1hi) >> (i & 31)) & 1u)) v[i] = 0.f;
+		tc::store_bf16_row(smem + kTrCH1, t, kGuideHidden, v, 0, kGuideHidden);
+		store_bf16_col(smem + kTrDA1T, t, v, kGuideHidden);
+		// dE = dA1 W1, and the weight-gradient GEMMs of this tile
+		const bool acc = !first;
+		if(!(ok = stage([&] {
+			tc_chain(tbase, s0 + kTrCH1, s0 + kTrW1T, kGuideHidden, kGuideIn, false);
+			tc_chain(tbase + kTrColG1, s0 + kTrDA2T, s0 + kTrH1T, 128, 112, acc);
+			tc_chain(tbase + kTrColG2, s0 + kTrH2T, s0 + kTrDOT, 128, kGuideOutPad, acc);
+		}))) break;
+		first = false;
+		for(int cc = 0; cc < 2; ++cc) tc::tmem_ld16(lane_addr + 16u * cc, v + 16 * cc);
+		if(live) scatter_grid_grad(g, p, v, grid_grad);
+	}
+	float *out = partial + static_cast<size_t>(blockIdx.x) * kMlpParams;
+	if(!ok)
+	{
+		if(t == 0) atomicOr(err, 1u);
+		tc::mbar_wait(mbar, phase ^ 1u, kTcWaitIters);
+		for(int i = t; i < kMlpParams; i += blockDim.x) out[i] = 0.f;
+	}
+	else if(first)
+		for(int i = t; i < kMlpParams; i += blockDim.x) out[i] = 0.f;
+	else
+	{
+		float v[16];
+		if(warp < 2)
+		{
+			for(int cc = 0; cc < 4; ++cc)
+			{
+				tc::tmem_ld16(lane_addr + kTrColG1 + 16u * cc, v);
+				for(int i = 0; i < 16; ++i) out[kOffW2 + t * kGuideHidden + 16 * cc + i] = v[i];
+			}
+			tc::tmem_ld16(lane_addr + kTrColG1 + 96u, v);
+			out[kOffB2 + t] = v[0];
+			for(int cc = 0; cc < 3; ++cc)
+			{
+				tc::tmem_ld16(lane_addr + kTrColG2 + 16u * cc, v);
+				for(int i = 0; i < 16; ++i)
+					if(16 * cc + i < kGuideOut) out[kOffW3 + (16 * cc + i) * kGuideHidden + t] = v[i];
+			}
+		}
+		else
+		{
+			const int j = t - kGuideHidden;
+			for(int cc = 0; cc < 2; ++cc)
+			{
+				tc::tmem_ld16(lane_addr + kTrColG1 + 64u + 16u * cc, v);
+				for(int i = 0; i < 16; ++i) out[kOffW1 + j * kGuideIn + 16 * cc + i] = v[i];
+			}
+			tc::tmem_ld16(lane_addr + kTrColG1 + 96u, v);
+			out[kOffB1 + j] = v[0];
+			for(int cc = 0; cc < 3; ++cc)
+			{
+				tc::tmem_ld16(lane_addr + kTrColG2 + 16u * cc, v);
+				if(j == 0)
+					for(int i = 0; i < 16; ++i)
+						if(16 * cc + i < kGuideOut) out[kOffB3 + 16 * cc + i] = v[i];
+			}
+		}
+	}
+	for(int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
+	if((t & 31) == 0 && loss != 0.f) atomicAdd(loss_out, loss);
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+	if(warp == 0) tc::tmem_dealloc(tbase, kTrCols);
+}
+
 } // namespace
 
 struct gbrt_guide {
@@ -698,7 +981,7 @@ int gbrt_guide_grad(gbrt_guide *G, const float *records_dev, uint32_t n, float *
 	if(!G || (n && !records_dev)) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_guide_grad: NULL argument");
 	cudaStream_t s = static_cast<cudaStream_t>(stream);
 	const size_t per_block = static_cast<size_t>(kGradThreads) * kGradChunks;
-	const size_t nblk = std::max<size_t>(1, (n + per_block - 1) / per_block);
+	const size_t nblk = std::max<size_t>({1, (n + per_block - 1) / per_block, static_cast<size_t>(G->n_sm)});
 	if(nblk > G->partial_blocks)
 	{
 		if(G->partial) cudaFree(G->partial);
@@ -706,12 +989,28 @@ int gbrt_guide_grad(gbrt_guide *G, const float *records_dev, uint32_t n, float *
 		G->partial_blocks = nblk;
 	}
 	static bool attr = false;
-	if(!attr) { cudaFuncSetAttribute(k_guide_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(grad_smem_bytes())); attr = true; }
+	if(!attr)
+	{
+		GBRT_CK(cudaFuncSetAttribute(k_guide_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(grad_smem_bytes())));
+		GBRT_CK(cudaFuncSetAttribute(k_guide_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTrTotal)));
+		attr = true;
+	}
 	GBRT_CK(cudaMemsetAsync(G->loss, 0, 2 * sizeof(float), s));
 	k_weight_sum<<<std::max(1, std::min(G->n_sm * 4, static_cast<int>((n + 255) / 256))), 256, 0, s>>>(records_dev, n, G->loss + 1);
-	k_guide_grad<<<static_cast<unsigned>(nblk), kGradThreads, grad_smem_bytes(), s>>>(G->grid, G->table, G->mlp, records_dev, n, G->loss + 1,
-	                                                                                  G->partial, G->table_g, G->loss);
-	k_reduce<<<(kMlpParams + 255) / 256, 256, 0, s>>>(G->partial, static_cast<int>(nblk), G->mlp_g);
+	size_t used = nblk;
+	if(G->eval_mode == GBRT_GUIDE_EVAL_TENSOR)
+	{
+		// one CTA per SM (176 KB of shared memory, 256 TMEM columns each)
+		const size_t tiles = (static_cast<size_t>(n) + 127) / 128;
+		used = std::min<size_t>(tiles, static_cast<size_t>(G->n_sm));
+		if(used)
+			k_guide_train_tc<<<static_cast<unsigned>(used), kTrThreads, kTrTotal, s>>>(G->grid, G->table, G->mlp, records_dev, n, G->loss + 1,
+			                                                                          G->partial, G->table_g, G->loss, G->tc_err);
+	}
+	else
+		k_guide_grad<<<static_cast<unsigned>(nblk), kGradThreads, grad_smem_bytes(), s>>>(G->grid, G->table, G->mlp, records_dev, n, G->loss + 1,
+		                                                                                  G->partial, G->table_g, G->loss);
+	k_reduce<<<(kMlpParams + 255) / 256, 256, 0, s>>>(G->partial, static_cast<int>(used), G->mlp_g);
 	GBRT_CK(cudaGetLastError());
 	if(loss_out)
 	{

@@ -118,9 +118,68 @@ def test_guide_eval_matches_oracle(cuda_device):
         assert np.allclose(got[i], exp, rtol=2e-3, atol=2e-4), (i, got[i], exp)
 
 
+@pytest.mark.parametrize("n", [300, 3000])
+def test_guide_gradients_tensor_cores(cuda_device, n):
+    """tcgen05 forward + backward (BF16 operands and activations, FP32
+    accumulation) against the FP64 oracle (ragged last tiles of 44 and 56
+    records): loss within 1 %; MLP gradients within 3 % in relative L2 norm,
+    cosine >= 0.999; hash-grid gradients within 6 %, cosine >= 0.998.  The
+    grid tolerance is wider because each coarse-level entry sums the BF16
+    gradients of every record in its cell, and those cancel: the relative
+    error of the sum grows with the number of records (2.3 % at 300, 4.2 %
+    at 3000 records measured on a GB300)."""
+    torch = pytest.importorskip("torch")
+    g, grid, mlp, tab, rng = _setup(seed=5)
+    g.set_eval_mode(gbrt.Guide.EVAL_TENSOR)
+    rec = _records(rng, n)
+    rt = torch.from_numpy(rec).cuda()
+    loss = g.grad_device(rt.data_ptr(), len(rec))
+    assert g.status() == 0
+    gm, gt = g.grads()
+    eloss, em, et = go.loss_and_grads(grid, mlp, tab, rec.astype(np.float64))
+    rel_m = np.linalg.norm(gm - em) / np.linalg.norm(em)
+    rel_t = np.linalg.norm(gt - et) / np.linalg.norm(et)
+    cos_m = float(gm @ em / (np.linalg.norm(gm) * np.linalg.norm(em)))
+    cos_t = float(gt.ravel() @ et.ravel() / (np.linalg.norm(gt) * np.linalg.norm(et)))
+    print(f"n {n}: loss tc {loss:.6f} fp64 {eloss:.6f}; rel err mlp {rel_m:.2e} table {rel_t:.2e}; cos {cos_m:.6f} {cos_t:.6f}")
+    assert abs(loss - eloss) <= 1e-2 * abs(eloss) + 1e-4
+    assert rel_m < 3e-2 and cos_m > 0.999
+    assert rel_t < 6e-2 and cos_t > 0.998
+    for name, lo, hi in [("W1", go.OFF_W1, go.OFF_B1), ("b1", go.OFF_B1, go.OFF_W2), ("W2", go.OFF_W2, go.OFF_B2),
+                         ("b2", go.OFF_B2, go.OFF_W3), ("W3", go.OFF_W3, go.OFF_B3), ("b3", go.OFF_B3, go.N_MLP)]:
+        e = np.linalg.norm(gm[lo:hi] - em[lo:hi]) / max(np.linalg.norm(em[lo:hi]), 1e-30)
+        assert e < 5e-2, (name, e)
+
+
+def test_guide_gradients_tensor_cores_accumulate_over_tiles(cuda_device):
+    """40,000 records = 313 tiles of 128, more than one per CTA, so each CTA
+    accumulates weight gradients over several tiles in TMEM: the tensor-core
+    gradients match the FP32 CUDA-core kernel's (itself checked against the
+    FP64 oracle) within BF16 error."""
+    torch = pytest.importorskip("torch")
+    g, grid, mlp, tab, rng = _setup(seed=6)
+    rec = _records(rng, 40000)
+    rt = torch.from_numpy(rec).cuda()
+    g.set_eval_mode(gbrt.Guide.EVAL_FP32)
+    l32 = g.grad_device(rt.data_ptr(), len(rec))
+    m32, t32 = g.grads()
+    g2 = gbrt.Guide(BOUND, log2_table=12, seed=6)     # fresh gradient buffers, same parameters
+    g2.set_params(mlp, tab)
+    g2.set_eval_mode(gbrt.Guide.EVAL_TENSOR)
+    ltc = g2.grad_device(rt.data_ptr(), len(rec))
+    assert g2.status() == 0
+    mtc, ttc = g2.grads()
+    rel_m = np.linalg.norm(mtc - m32) / np.linalg.norm(m32)
+    rel_t = np.linalg.norm(ttc - t32) / np.linalg.norm(t32)
+    print(f"loss fp32 {l32:.6f} tc {ltc:.6f}; rel diff mlp {rel_m:.2e} table {rel_t:.2e}")
+    assert abs(ltc - l32) <= 1e-2 * abs(l32) + 1e-4
+    assert rel_m < 3e-2 and rel_t < 8e-2
+
+
 def test_guide_gradients_match_fp64_oracle(cuda_device):
     torch = pytest.importorskip("torch")
     g, grid, mlp, tab, rng = _setup(seed=5)
+    g.set_eval_mode(gbrt.Guide.EVAL_FP32)
     rec = _records(rng, 300)
     rt = torch.from_numpy(rec).cuda()
     loss = g.grad_device(rt.data_ptr(), len(rec))
