@@ -599,11 +599,14 @@ __device__ __forceinline__ uint32_t pixel_offset(uint32_t pixel, int resx)
 
 __global__ void __launch_bounds__(kThreads) k_camera(Camera cam, Params P, Work W)
 {
-	const uint32_t per_pixel = static_cast<uint32_t>(P.spp * P.path_samples);
+	// sample-major order: a wave holds whole sample indices of every pixel,
+	// so each wave (and each guide training batch drawn from it) covers the
+	// full image, and neighbouring threads shoot neighbouring pixels
+	const uint32_t n_pix = static_cast<uint32_t>(cam.resx) * static_cast<uint32_t>(cam.resy);
 	for(uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < P.wave_n; s += gridDim.x * blockDim.x)
 	{
 		const uint32_t g = P.wave_start + s;
-		const uint32_t pixel = g / per_pixel, si = g % per_pixel;
+		const uint32_t pixel = g % n_pix, si = g / n_pix;
 		const uint32_t sample = si / static_cast<uint32_t>(P.path_samples);
 		const uint32_t offset_ = pixel_offset(pixel, cam.resx);
 		float dx = 0.5f, dy = 0.5f;
