@@ -181,10 +181,13 @@ enum {
 	GBRT_MAT_LIGHT = 1,          /* "light_mat": color, power, params[0] = double_sided (0/1) */
 	GBRT_MAT_GLOSSY = 2,         /* "glossy": color (glossy colour), color2 (diffuse_color), params =
 	                                {exponent, glossy_reflect, diffuse_reflect, as_diffuse (1)} */
-	GBRT_MAT_ROUGH_GLASS = 3,    /* "rough_glass" (not yet supported) */
-	GBRT_MAT_GLASS = 4           /* "glass" (not yet supported) */
+	GBRT_MAT_ROUGH_GLASS = 3,    /* "rough_glass": color (filter_color), color2 (mirror_color), params =
+	                                {IOR (0 -> 1.4), transmit_filter, alpha (0 -> 0.5)} */
+	GBRT_MAT_GLASS = 4           /* "glass": color (filter_color), color2 (mirror_color), params =
+	                                {IOR (0 -> 1.4), transmit_filter} */
 };
-enum { GBRT_LIGHT_AREA = 0, GBRT_LIGHT_POINT = 1 };
+/* Every material: params[5] = additionaldepth (extra recursive ray levels). */
+enum { GBRT_LIGHT_AREA = 0, GBRT_LIGHT_POINT = 1 };   /* "pointlight": corner = from, color, power */
 enum {
 	GBRT_PT_FP64_FILM = 1,        /* accumulate the film in double */
 	GBRT_PT_GUIDE_RADIANCE = 2    /* train the guide on incident radiance alone (default: radiance x BSDF cosine) */
@@ -235,6 +238,8 @@ typedef struct gbrt_pt_params {
 	uint32_t guide_train_steps; /* Adam steps on this render's own records after each wave; 0 = none */
 	uint32_t guide_batch;       /* records per step; 0 = 65536 */
 	uint32_t guide_max_vertex;  /* guide (and record) only vertices 0 .. guide_max_vertex - 1; 0 = all */
+	int32_t raydepth;           /* "raydepth": last ray level of the recursive glossy / specular split
+	                               (MonteCarloIntegrator::recursiveRaytrace); 0 = 5 */
 } gbrt_pt_params;
 
 typedef struct gbrt_pt_stats {

@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <vector>
 
@@ -46,17 +47,21 @@ enum : uint32_t {
 struct DevMaterial {
 	uint32_t type;
 	uint32_t flags;
-	float col[3];      // shinydiffuse: colour x diffuse strength; light_mat: colour x power; glossy: glossy colour
-	float col2[3];     // glossy: diffuse colour
+	float col[3];      // shinydiffuse: colour x diffuse strength; light_mat: colour x power; glossy: glossy colour;
+	                   // glass, rough_glass: filter colour
+	float col2[3];     // glossy: diffuse colour; glass, rough_glass: mirror colour
 	float exponent, m_glossy, m_diffuse, p_diffuse;
-	uint32_t as_diffuse, with_diffuse, double_sided, pad;
+	uint32_t as_diffuse, with_diffuse, double_sided, addl_depth;
+	float ior, a2;     // glass, rough_glass: IOR; rough_glass: GGX alpha^2
+	float pad[2];
 };
 
 struct DevLight {
-	float c[3], tx[3], ty[3], nflip[3], col[3];   // area light (light_area.h:70-78)
+	float c[3], tx[3], ty[3], nflip[3], col[3];   // area light (light_area.h:70-78); point light: c = from, col
 	float e1[3], e2[3], e3[3];                    // quad edges from the corner, for intersect
 	int samples;
-	float pad[2];
+	uint32_t type;                                // GBRT_LIGHT_AREA / GBRT_LIGHT_POINT
+	float pad;
 };
 
 constexpr int kThreads = 128;
@@ -74,6 +79,7 @@ struct Camera {
 
 struct Params {
 	int spp, path_samples, bounces, rr_min;
+	int raydepth;         // MonteCarloIntegrator raydepth: last ray level of the recursive glossy / specular split
 	uint32_t base_offset, seed;
 	uint32_t wave_start, wave_n;
 	float d1;
@@ -89,6 +95,12 @@ struct Params {
 struct Work {
 	uint32_t *p_pixel, *p_si, *p_state;
 	float4 *p_thr;
+	uint4 *p_task;              // integrate() call of the path: {level | addl << 8 | division << 16, branch, deco1, deco2}
+	// spawned integrate() calls of the recursive split (5 float4 each:
+	// origin+tmin, dir+tmax, weight, {pixel, si, task.x, branch}, {deco1, deco2})
+	float4 *sp_out;
+	uint32_t *sp_count;
+	uint32_t sp_cap;
 	float4 *q_ray[2];
 	uint32_t *q_path[2];
 	float4 *hits;
@@ -331,6 +343,284 @@ __device__ __forceinline__ void glossy_sample(const Surface &s, const float wo[3
 	w = __fdiv_rn(wi_n, xa(xm(pdf, 0.99f), 0.01f));
 }
 
+// ---- glass and rough glass ---------------------------------------------------
+
+// Vec3::refract (include/geometry/vector.h:484-503): directions point away
+// from the surface; false on total internal reflection.
+__device__ __forceinline__ bool vec_refract(const float n_in[3], const float wi[3], float wo[3], float ior)
+{
+	float n[3] = {n_in[0], n_in[1], n_in[2]};
+	float eta, cos_v_n = dot3(wi, n);
+	if(cos_v_n < 0.f) { eta = ior; n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2]; cos_v_n = -cos_v_n; }
+	else eta = 1.f / ior;
+	const float k = 1.f - eta * eta * (1.f - cos_v_n * cos_v_n);
+	if(k <= 0.f) return false;
+	const float a = eta * cos_v_n - sqrtf(k);
+	for(int c = 0; c < 3; ++c) wo[c] = eta * -wi[c] + a * n[c];
+	normalize3(wo);
+	return true;
+}
+
+// Vec3::fresnel (vector.h:505-518)
+__device__ __forceinline__ void vec_fresnel(const float i[3], const float n[3], float ior, float &kr, float &kt)
+{
+	const float d = dot3(i, n);
+	const float c = d < 0.f ? -d : d;
+	float g = ior * ior + c * c - 1.f;
+	g = g <= 0.f ? 0.f : sqrtf(g);
+	const float aux = c * (g + c);
+	kr = ((0.5f * (g - c) * (g - c)) / ((g + c) * (g + c))) * (1.f + ((aux - 1.f) * (aux - 1.f)) / ((aux + 1.f) * (aux + 1.f)));
+	kt = kr < 1.f ? 1.f - kr : 0.f;
+}
+
+// Vec3::reflect: 2 (v.n) n - v (vector.h:358-362)
+__device__ __forceinline__ void vec_reflect(const float v[3], const float n[3], float out[3])
+{
+	const float vn = 2.f * dot3(v, n);
+	for(int c = 0; c < 3; ++c) out[c] = vn * n[c] - v[c];
+}
+
+// Normal used by GlassMaterial::sample / getSpecular (material_glass.cc:173-177,
+// 320-330): the shading normal, bent towards wo when it faces away.
+__device__ __forceinline__ void glass_normal(const Surface &s, const float wo[3], float n[3], bool &outside)
+{
+	outside = dot3(s.ng, wo) > 0.f;
+	const float c = dot3(s.n, wo);
+	if(outside ? c >= 0.f : c <= 0.f) { n[0] = s.n[0]; n[1] = s.n[1]; n[2] = s.n[2]; return; }
+	for(int k = 0; k < 3; ++k) n[k] = s.n[k] - (1.00001f * c) * wo[k];
+	normalize3(n);
+}
+
+// GlassMaterial::sample without dispersion (material_glass.cc:164-176, 235-300).
+// Note the weight: the chosen branch returns its colour with w = 1 (no
+// division by the branch probability).
+__device__ __forceinline__ bool glass_sample(const Surface &s, const float wo[3], float s1, uint32_t req, float wi[3], float col[3],
+                                             float &w, float &pdf, uint32_t &sampled)
+{
+	const DevMaterial &m = *s.m;
+	col[0] = col[1] = col[2] = 0.f; w = 0.f; pdf = 0.f; sampled = 0u;
+	if(!(req & BF_SPECULAR)) return false;
+	float n[3];
+	bool outside;
+	glass_normal(s, wo, n, outside);
+	pdf = 1.f;
+	float refdir[3];
+	if(vec_refract(n, wo, refdir, m.ior))
+	{
+		float kr, kt;
+		vec_fresnel(wo, n, m.ior, kr, kt);
+		const float p_kr = 0.01f + 0.99f * kr, p_kt = 0.01f + 0.99f * kt;
+		if(s1 < p_kt && (req & (BF_SPECULAR | BF_TRANSMIT)))
+		{
+			for(int k = 0; k < 3; ++k) { wi[k] = refdir[k]; col[k] = m.col[k]; }
+			pdf = p_kt; w = 1.f; sampled = BF_SPECULAR | BF_TRANSMIT;
+			return true;
+		}
+		if(req & (BF_SPECULAR | BF_REFLECT))
+		{
+			vec_reflect(wo, n, wi);
+			for(int k = 0; k < 3; ++k) col[k] = m.col2[k];
+			pdf = p_kr; w = 1.f; sampled = BF_SPECULAR | BF_REFLECT;
+			return true;
+		}
+	}
+	else if(req & (BF_SPECULAR | BF_REFLECT))   // total internal reflection
+	{
+		vec_reflect(wo, n, wi);
+		col[0] = col[1] = col[2] = 1.f;
+		w = 1.f; sampled = BF_SPECULAR | BF_REFLECT;
+		return true;
+	}
+	pdf = 0.f;
+	return false;
+}
+
+// GlassMaterial::getSpecular without dispersion (material_glass.cc:313-370):
+// refraction (kt x filter colour) and reflection (kr x mirror colour; for
+// rays leaving the glass only below ray level 3); TIR: mirror colour.
+__device__ __forceinline__ void glass_specular(const Surface &s, const float wo[3], int ray_level, bool &has_refract, float rdir[3],
+                                               float rcol[3], bool &has_reflect, float ldir[3], float lcol[3])
+{
+	const DevMaterial &m = *s.m;
+	float n[3];
+	bool outside;
+	glass_normal(s, wo, n, outside);
+	has_refract = has_reflect = false;
+	if(vec_refract(n, wo, rdir, m.ior))
+	{
+		float kr, kt;
+		vec_fresnel(wo, n, m.ior, kr, kt);
+		has_refract = true;
+		for(int k = 0; k < 3; ++k) rcol[k] = kt * m.col[k];
+		if(outside || ray_level < 3)
+		{
+			has_reflect = true;
+			vec_reflect(wo, n, ldir);
+			for(int k = 0; k < 3; ++k) lcol[k] = m.col2[k] * kr;
+		}
+	}
+	else
+	{
+		has_reflect = true;
+		vec_reflect(wo, n, ldir);
+		for(int k = 0; k < 3; ++k) lcol[k] = m.col2[k];
+	}
+}
+
+// GGX helpers (include/material/material_utils_microfacet.h:109-179)
+__device__ __forceinline__ void ggx_sample(float a2, float s1, float s2, float h[3])
+{
+	const float tan_theta_2 = a2 * (s1 / (1.00001f - s1));
+	const float cos_theta = 1.f / sqrtf(1.f + tan_theta_2);
+	const float sin_theta = sqrtf(1.00001f - cos_theta * cos_theta);
+	const float phi = 6.28318530717958647692f * s2;
+	h[0] = sin_theta * gbrt::fast_cos(phi); h[1] = sin_theta * gbrt::fast_sin(phi); h[2] = cos_theta;
+}
+__device__ __forceinline__ float ggx_d(float a2, float ct2, float tt2)
+{
+	const float ct4 = ct2 * ct2, a_tan = a2 + tt2;
+	return a2 / (kPi * ct4 * a_tan * a_tan);
+}
+__device__ __forceinline__ float ggx_g(float a2, float wo_n, float wi_n)
+{
+	const float wo2 = wo_n * wo_n, wi2 = wi_n * wi_n;
+	const float t1 = sqrtf(1.f + a2 * ((1.f - wo2) / wo2)), t2 = sqrtf(1.f + a2 * ((1.f - wi2) / wi2));
+	return (2.f / (1.f + t1)) * (2.f / (1.f + t2));
+}
+__device__ __forceinline__ float mf_fresnel(float wo_h, float ior)
+{
+	const float c = fabsf(wo_h);
+	float g = ior * ior - 1.f + c * c;
+	if(g > 0.f)
+	{
+		g = sqrtf(g);
+		const float a = (g - c) / (g + c), b = (c * (g + c) - 1.f) / (c * (g - c) + 1.f);
+		return 0.5f * a * a * (1.f + b * b);
+	}
+	return 1.f;
+}
+__device__ __forceinline__ bool mf_refract(float eta, const float wo[3], float wi[3], const float h[3], float wo_h, float &kr, float &kt)
+{
+	wi[0] = wi[1] = wi[2] = 0.f;
+	const float c = -dot3(wo, h);
+	const float sign = c > 0.f ? 1.f : -1.f;
+	const float t1 = 1.f - (eta * eta * (1.f - c * c));
+	if(t1 < 0.f) return false;
+	const float a = eta * c - sign * sqrtf(t1);
+	for(int k = 0; k < 3; ++k) wi[k] = -(eta * wo[k] + a * h[k]);
+	kt = 0.f;
+	kr = mf_fresnel(wo_h, 1.f / eta);
+	if(kr == 1.f) return false;
+	kt = 1.f - kr;
+	return true;
+}
+
+// Shared set-up of RoughGlassMaterial::sample (material_rough_glass.cc:165-190):
+// GGX half vector in the shading frame, D term.
+struct RoughFrame {
+	float n[3], h[3];
+	bool outside;
+	float cos_theta, d, wo_h, wo_n;
+};
+__device__ __forceinline__ void rough_frame(const Surface &s, const float wo[3], float s1, float s2, RoughFrame &f)
+{
+	face_forward(s, wo, f.n);
+	f.outside = dot3(s.ng, wo) > 0.f;
+	float hs[3];
+	ggx_sample(s.m->a2, s1, s2, hs);
+	for(int k = 0; k < 3; ++k) f.h[k] = hs[0] * s.u[k] + hs[1] * s.v[k] + hs[2] * f.n[k];
+	normalize3(f.h);
+	f.cos_theta = dot3(f.h, f.n);
+	const float ct2 = f.cos_theta * f.cos_theta;
+	const float tt2 = (1.f - ct2) / fmaxf(1.0e-8f, ct2);
+	f.d = f.cos_theta > 0.f ? ggx_d(s.m->a2, ct2, tt2) : 0.f;
+	f.wo_h = dot3(wo, f.h);
+	f.wo_n = dot3(wo, f.n);
+}
+__device__ __forceinline__ void rough_transmit(const Surface &s, const RoughFrame &f, const float wi[3], float kt, float col[3], float &w, float &pdf)
+{
+	const DevMaterial &m = *s.m;
+	const float wi_n = dot3(wi, f.n), wi_h = dot3(wi, f.h);
+	const float g = (wi_h * wi_n > 0.f && f.wo_h * f.wo_n > 0.f) ? ggx_g(m.a2, wi_n, f.wo_n) : 0.f;
+	const float ior_wi = f.outside ? m.ior : 1.f, ior_wo = f.outside ? 1.f : m.ior;
+	const float ht = ior_wo * f.wo_h + ior_wi * wi_h;
+	const float jac = (ior_wi * ior_wi) / fmaxf(1.0e-8f, ht * ht);
+	const float glossy = fabsf((f.wo_h * wi_h) / (wi_n * f.wo_n)) * kt * g * f.d * jac;
+	pdf = f.d * f.cos_theta * (jac * fabsf(wi_h));
+	for(int k = 0; k < 3; ++k) col[k] = glossy * m.col[k];
+	w = fabsf(wi_n) / fmaxf(0.1f, pdf);
+}
+__device__ __forceinline__ void rough_reflect(const Surface &s, const RoughFrame &f, const float wo[3], float kr, float wi[3], float col[3],
+                                              float &w, float &pdf)
+{
+	const DevMaterial &m = *s.m;
+	const float hw = 2.f * dot3(f.h, wo);       // microfacet::reflect (material_utils_microfacet.h:175-179)
+	for(int k = 0; k < 3; ++k) wi[k] = hw * f.h[k] - wo[k];
+	const float wi_n = dot3(wi, f.n), wi_h = dot3(wi, f.h);
+	const float g = ggx_g(m.a2, wi_n, f.wo_n);
+	const float jac = 1.f / fmaxf(1.0e-8f, 4.f * fabsf(wi_h));
+	const float glossy = (kr * g * f.d) / fmaxf(1.0e-8f, 4.f * fabsf(f.wo_n * wi_n));
+	pdf = f.d * f.cos_theta * jac;
+	for(int k = 0; k < 3; ++k) col[k] = glossy * m.col2[k];
+	w = fabsf(wi_n) / fmaxf(0.1f, pdf);
+}
+
+// RoughGlassMaterial::sample, one direction (material_rough_glass.cc:165-245):
+// transmission when s1 < kt, else reflection; TIR reflects with weight 1.
+__device__ __forceinline__ bool rough_sample(const Surface &s, const float wo[3], float s1, float s2, uint32_t req, float wi[3], float col[3],
+                                             float &w, float &pdf, uint32_t &sampled)
+{
+	col[0] = col[1] = col[2] = 0.f; w = 0.f; pdf = 1.f; sampled = 0u;
+	RoughFrame f;
+	rough_frame(s, wo, s1, s2, f);
+	float kr, kt;
+	if(mf_refract(f.outside ? 1.f / s.m->ior : s.m->ior, wo, wi, f.h, f.wo_h, kr, kt))
+	{
+		if(s1 < kt && (req & BF_TRANSMIT))
+		{
+			rough_transmit(s, f, wi, kt, col, w, pdf);
+			sampled = BF_GLOSSY | BF_TRANSMIT;
+			return true;
+		}
+		if(req & BF_REFLECT)
+		{
+			rough_reflect(s, f, wo, kr, wi, col, w, pdf);
+			sampled = BF_GLOSSY | BF_REFLECT;
+			return true;
+		}
+		return false;
+	}
+	const float hw = 2.f * dot3(wo, f.h);     // TIR: wo reflected about h
+	for(int k = 0; k < 3; ++k) wi[k] = hw * f.h[k] - wo[k];
+	col[0] = col[1] = col[2] = 1.f;
+	w = 1.f;
+	sampled = BF_GLOSSY | BF_REFLECT;
+	return true;
+}
+
+// RoughGlassMaterial::sample, both directions (material_rough_glass.cc:247-347),
+// as MonteCarloIntegrator::glossy calls it for transmissive materials with
+// flags Glossy | AllGlossy: slot 0 = transmission (TIR: the reflection,
+// colour 1, weight 1), slot 1 = reflection; n = slots filled.
+__device__ __forceinline__ int rough_sample2(const Surface &s, const float wo[3], float s1, float s2, float dir[2][3], float col[2][3], float w[2])
+{
+	RoughFrame f;
+	rough_frame(s, wo, s1, s2, f);
+	float kr, kt, wi[3], pdf;
+	if(mf_refract(f.outside ? 1.f / s.m->ior : s.m->ior, wo, wi, f.h, f.wo_h, kr, kt))
+	{
+		rough_transmit(s, f, wi, kt, col[0], w[0], pdf);
+		for(int k = 0; k < 3; ++k) dir[0][k] = wi[k];
+		rough_reflect(s, f, wo, kr, dir[1], col[1], w[1], pdf);
+		return 2;
+	}
+	const float hw = 2.f * dot3(wo, f.h);
+	for(int k = 0; k < 3; ++k) { dir[0][k] = hw * f.h[k] - wo[k]; col[0][k] = 1.f; }
+	w[0] = 1.f;
+	return 1;
+}
+
+
 // Material::eval dispatch; ShinyDiffuseMaterial::eval diffuse component
 // (material_shiny_diffuse.cc:297-337).
 __device__ __forceinline__ void mat_eval(const Surface &s, const float wo[3], const float wl[3], float out[3])
@@ -369,6 +659,8 @@ __device__ __forceinline__ bool mat_sample(const Surface &s, const float wo[3], 
 		glossy_sample(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
 		return sampled != 0u;
 	}
+	if(s.m->type == GBRT_MAT_GLASS) return glass_sample(s, wo, s1, req_flags, wi, col, w, pdf, sampled);
+	if(s.m->type == GBRT_MAT_ROUGH_GLASS) return rough_sample(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
 	if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return false;
 	const uint32_t cflags = BF_DIFFUSE | BF_REFLECT;
 	if((req_flags & cflags) != cflags) return false;
@@ -459,6 +751,7 @@ __device__ __forceinline__ bool mat_emit(const Surface &s, const float wo[3], fl
 	return true;
 }
 
+
 __device__ __forceinline__ void path_sum_add(const Work &W, uint32_t path, float r, float g, float b)
 {
 	float *p = reinterpret_cast<float *>(W.p_sum + path);
@@ -511,11 +804,44 @@ struct ShadowWriter {
 // (areaLightSampleLight, :192-330) and num_samples BSDF samples that hit the
 // light (areaLightSampleMaterial, :332-415), power-heuristic MIS, Halton
 // bases 2/3 from offs = num_samples * sample + pixel offset + loffs * 4567.
+__device__ __forceinline__ int light_samples(const DevLight &L, uint32_t division)
+{
+	if(L.type == GBRT_LIGHT_POINT) return 1;
+	return division > 1 ? max(1, L.samples / static_cast<int>(division)) : L.samples;   // integrator_montecarlo.cc:428-429
+}
+
+// Shadow rays one light estimation writes: 2 per area-light sample, 1 for a point light.
+__device__ __forceinline__ uint32_t light_shadow_rays(const DevLight &L, uint32_t division)
+{
+	return L.type == GBRT_LIGHT_POINT ? 1u : 2u * static_cast<uint32_t>(light_samples(L, division));
+}
+
 __device__ void light_estimation(const SceneDev &sc, const Surface &s, const float wo[3], uint32_t li, uint32_t loffs,
-                                 uint32_t sample_, uint32_t offset_, const float weight[3], uint32_t pixel, ShadowWriter &sw)
+                                 uint32_t sample_, uint32_t offset_, const float weight[3], uint32_t pixel, ShadowWriter &sw,
+                                 uint32_t division)
 {
 	const DevLight &L = sc.lights[li];
-	const int ns = L.samples;
+	if(L.type == GBRT_LIGHT_POINT)
+	{
+		// MonteCarloIntegrator::diracLight (integrator_montecarlo.cc:117-190) with
+		// PointLight::illuminate (light_point.cc:71-82)
+		float ldir[3];
+		for(int k = 0; k < 3; ++k) ldir[k] = L.c[k] - s.p[k];
+		const float dist_sqr = ldir[0] * ldir[0] + ldir[1] * ldir[1] + ldir[2] * ldir[2];
+		const float dist = sqrtf(dist_sqr);
+		if(dist == 0.f) return;
+		const float idist_sqr = 1.f / dist_sqr, inv = 1.f / dist;
+		for(int k = 0; k < 3; ++k) ldir[k] *= inv;
+		const float sbias = kShadowBias * fmaxf(1.f, sqrtf(dot3(s.p, s.p)));
+		float surf[3];
+		mat_eval(s, wo, ldir, surf);
+		const float angle = fabsf(dot3(s.n, ldir));
+		float c[3];
+		for(int k = 0; k < 3; ++k) c[k] = surf[k] * (L.col[k] * idist_sqr) * angle * weight[k];
+		if(c[0] != 0.f || c[1] != 0.f || c[2] != 0.f) sw.put(s.p, sbias, ldir, dist, pixel, c);
+		return;
+	}
+	const int ns = light_samples(L, division);
 	const float inv_ns = __fdiv_rn(1.f, static_cast<float>(ns));
 	const uint32_t offs = static_cast<uint32_t>(ns) * sample_ + offset_ + loffs * 4567u;
 	const float plen = sqrtf(dot3(s.p, s.p));
@@ -591,6 +917,108 @@ __device__ void light_estimation(const SceneDev &sc, const Surface &s, const flo
 	}
 }
 
+
+// Writes a lane's reserved run of spawn slots (recursive split of
+// MonteCarloIntegrator::recursiveRaytrace); unused slots are marked dead.
+struct SpawnWriter {
+	float4 *out;
+	uint32_t slot, end, cap;
+	__device__ void put(const float o[3], const float d[3], const float wt[3], uint32_t pixel, uint32_t si, uint32_t tx, uint32_t branch,
+	                    float d1, float d2)
+	{
+		if(slot >= end) return;
+		if(slot < cap)
+		{
+			float4 *r = out + 5ull * slot;
+			r[0] = make_float4(o[0], o[1], o[2], kRayMinDist);
+			r[1] = make_float4(d[0], d[1], d[2], -1.f);
+			r[2] = make_float4(wt[0], wt[1], wt[2], 0.f);
+			r[3] = make_float4(__uint_as_float(pixel), __uint_as_float(si), __uint_as_float(tx), __uint_as_float(branch));
+			r[4] = make_float4(d1, d2, 0.f, 0.f);
+		}
+		++slot;
+	}
+	__device__ void close()
+	{
+		for(; slot < end; ++slot)
+			if(slot < cap) reinterpret_cast<uint32_t *>(out + 5ull * slot + 3)[0] = kDead;
+	}
+};
+
+// Upper bound of the integrate() calls recursiveRaytrace starts at a hit
+// (each call as max(1, path_samples / division) paths).
+__device__ __forceinline__ uint32_t spawn_bound(uint32_t flags, bool glossy, bool spec, uint32_t division, uint32_t ps)
+{
+	uint32_t n = 0;
+	if(glossy)
+	{
+		const uint32_t rs = division > 1 ? max(1u, 8u / division) : 8u;
+		n += rs * ((flags & BF_TRANSMIT) ? 2u : 1u) * max(1u, ps / (division * rs));
+	}
+	if(spec) n += 2u * max(1u, ps / division);
+	return n;
+}
+
+// MonteCarloIntegrator::recursiveRaytrace at ray level nl
+// (integrator_montecarlo.cc:698-748): glossy() (:506-589) splits into
+// ray_samples_glossy = 8 / division directions (Halton 2/3 from
+// ray_samples * sample + pixel offset, decorrelation from Faure dims
+// 2 nl + 1, 2 nl + 2 at branch + pixel offset), each integrate() weighted by
+// colour x w / ray_samples; getSpecular's reflection and refraction keep the
+// parent's division.
+__device__ void spawn_children(const SceneDev &sc, const Params &P, const Surface &s, const float wo[3], const float thr[3],
+                               uint32_t pixel, uint32_t si, uint32_t sample_, uint32_t offset_, uint32_t nl, uint32_t addl,
+                               uint32_t division, uint32_t branch, float deco1, float deco2, bool do_glossy, bool do_spec, SpawnWriter &sw)
+{
+	const uint32_t ps = static_cast<uint32_t>(P.path_samples);
+	const uint32_t si0 = si - si % ps;
+	auto emit = [&](const float d[3], const float wt[3], uint32_t div, uint32_t br, float d1, float d2) {
+		if(wt[0] == 0.f && wt[1] == 0.f && wt[2] == 0.f) return;     // contributes nothing
+		const uint32_t nsub = max(1u, ps / div);
+		const uint32_t tx = nl | (addl << 8) | (div << 16);
+		for(uint32_t j = 0; j < nsub; ++j) sw.put(s.p, d, wt, pixel, si0 + j, tx, br, d1, d2);
+	};
+	if(do_glossy)
+	{
+		const uint32_t rs = division > 1 ? max(1u, 8u / division) : 8u;
+		const uint32_t ndiv = division * rs, branch0 = ndiv * branch, offs = rs * sample_ + offset_;
+		const float inv_rs = 1.f / static_cast<float>(rs);
+		for(uint32_t j = 0; j < rs; ++j)
+		{
+			const float d1 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 2 * static_cast<int>(nl) + 1, branch0 + j + offset_));
+			const float d2 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 2 * static_cast<int>(nl) + 2, branch0 + j + offset_));
+			const float s1 = gbrt::radical_inverse(offs + 1u + j, 2), s2 = gbrt::radical_inverse(offs + 1u + j, 3);
+			if(s.m->flags & BF_TRANSMIT)
+			{
+				float dir[2][3], col[2][3], w[2];
+				const int nd = rough_sample2(s, wo, s1, s2, dir, col, w);
+				for(int c = 0; c < nd; ++c)
+				{
+					float wt[3];
+					for(int k = 0; k < 3; ++k) wt[k] = thr[k] * col[c][k] * w[c] * inv_rs;
+					emit(dir[c], wt, ndiv, branch0 + j, d1, d2);
+				}
+			}
+			else
+			{
+				float wi[3], col[3], w, pdf, wt[3];
+				uint32_t sf;
+				mat_sample(s, wo, s1, s2, BF_GLOSSY | BF_REFLECT, wi, col, w, pdf, sf);
+				for(int k = 0; k < 3; ++k) wt[k] = thr[k] * col[k] * w * inv_rs;
+				emit(wi, wt, ndiv, branch0 + j, d1, d2);
+			}
+		}
+	}
+	if(do_spec && s.m->type == GBRT_MAT_GLASS)
+	{
+		bool hr, hl;
+		float rdir[3], rcol[3], ldir[3], lcol[3], wt[3];
+		glass_specular(s, wo, static_cast<int>(nl), hr, rdir, rcol, hl, ldir, lcol);
+		if(hl) { for(int k = 0; k < 3; ++k) wt[k] = thr[k] * lcol[k]; emit(ldir, wt, division, branch, deco1, deco2); }
+		if(hr) { for(int k = 0; k < 3; ++k) wt[k] = thr[k] * rcol[k]; emit(rdir, wt, division, branch, deco1, deco2); }
+	}
+}
+
 __device__ __forceinline__ uint32_t pixel_offset(uint32_t pixel, int resx)
 {
 	const uint32_t x = pixel % static_cast<uint32_t>(resx), y = pixel / static_cast<uint32_t>(resx);
@@ -629,6 +1057,7 @@ __global__ void __launch_bounds__(kThreads) k_camera(Camera cam, Params P, Work 
 		W.p_si[s] = si;
 		W.p_thr[s] = make_float4(1.f, 1.f, 1.f, 0.f);
 		W.p_state[s] = 0u;
+		W.p_task[s] = make_uint4(1u << 16, 0u, 0u, 0u);       // ray level 0, division 1
 		if(W.p_sum)
 		{
 			W.p_sum[s] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -680,6 +1109,8 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 		Surface s;
 		float wo[3] = {0.f, 0.f, 0.f}, thr[3] = {0.f, 0.f, 0.f};
 		uint32_t pixel = 0, sample_ = 0, offset_ = 0, sub = 0, k = 0, mat1 = 0, caustic = 0;
+		uint32_t level = 0, addl = 0, division = 1, branch = 0, si = 0, tseed = P.seed;
+		float deco1 = 0.f, deco2 = 0.f;
 		bool hit = false;
 		if(live)
 		{
@@ -699,7 +1130,12 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				coords_system(s.n, s.u, s.v);
 				wo[0] = -dir[0]; wo[1] = -dir[1]; wo[2] = -dir[2];
 				pixel = W.p_pixel[path];
-				const uint32_t si = W.p_si[path];
+				si = W.p_si[path];
+				const uint4 tk = W.p_task[path];
+				level = tk.x & 0xffu; addl = (tk.x >> 8) & 0xffu; division = max(1u, tk.x >> 16); branch = tk.y;
+				deco1 = __uint_as_float(tk.z); deco2 = __uint_as_float(tk.w);
+				// random streams of a spawned integrate() call differ from its siblings'
+				if(level) tseed = P.seed ^ hash32(tk.x * 0x9e3779b9u + branch * 0x85ebca6bu + 1u);
 				sub = si % static_cast<uint32_t>(P.path_samples);
 				sample_ = P.base_offset + si / static_cast<uint32_t>(P.path_samples);
 				offset_ = pixel_offset(pixel, resx);
@@ -718,30 +1154,43 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 			W.r_valid[slot] = 1u;     // complete
 		}
 		// --- decide this vertex's work, count its shadow rays -----------------
-		bool do_nee_all = false, do_nee_one = false, rr_dead = false;
+		bool do_nee_all = false, do_nee_one = false, rr_dead = false, do_glossy = false, do_spec = false;
 		float nee_weight[3] = {0.f, 0.f, 0.f};
-		uint32_t nee_light = 0;
+		uint32_t nee_light = 0, n_spawn = 0;
 		if(hit)
 		{
 			if(k == 0)
 			{
+				// root of an integrate() call: emission and all-light estimation
+				// weighted by the call's weight (1 for camera rays)
 				float e[3];
 				if((s.m->flags & BF_EMIT) && sub == 0 && mat_emit(s, wo, e))
 				{
-					film_add(film, film64, pixel, e[0], e[1], e[2]);
-					if(W.p_sum) path_sum_add(W, path, e[0], e[1], e[2]);
+					film_add(film, film64, pixel, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
+					if(W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
 				}
 				do_nee_all = (s.m->flags & BF_DIFFUSE) && sub == 0;
-				nee_weight[0] = nee_weight[1] = nee_weight[2] = 1.f;
+				for(int c = 0; c < 3; ++c) nee_weight[c] = thr[c];
 				if(do_nee_all)
-					for(uint32_t l = 0; l < P.n_lights; ++l) n_shadow += 2u * static_cast<uint32_t>(sc.lights[l].samples);
+					for(uint32_t l = 0; l < P.n_lights; ++l) n_shadow += light_shadow_rays(sc.lights[l], division);
+				// recursiveRaytrace at ray level + 1 (integrator_path_tracer.cc:287,
+				// integrator_montecarlo.cc:698-710)
+				addl = max(addl, s.m->addl_depth);
+				const uint32_t nl = level + 1u;
+				if(sub == 0 && W.sp_out && nl <= static_cast<uint32_t>(P.raydepth) + addl && nl < 20u)
+				{
+					const uint32_t f = s.m->flags;
+					do_glossy = (f & BF_GLOSSY) && (f & BF_REFLECT);
+					do_spec = (f & (BF_SPECULAR | BF_FILTER)) != 0u;
+					n_spawn = spawn_bound(f, do_glossy, do_spec, division, static_cast<uint32_t>(P.path_samples));
+				}
 			}
 			else
 			{
 				if(k == 1) mat1 = s.m->flags;
 				if(k >= 2 && static_cast<int>(k) - 1 > P.rr_min)   // integrator_path_tracer.cc:267-273
 				{
-					const float r = rng01(pixel, sample_ * 64u + sub, k, P.seed);
+					const float r = rng01(pixel, sample_ * 64u + sub, k, tseed);
 					const float prob = fmaxf(thr[0], fmaxf(thr[1], thr[2]));
 					if(prob <= 0.f || prob < r) rr_dead = true;
 					else { const float ip = __fdiv_rn(1.f, prob); for(int c = 0; c < 3; ++c) thr[c] = xm(thr[c], ip); }
@@ -751,10 +1200,10 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 					do_nee_one = P.n_lights > 0 && (k == 1 || (mat1 & BF_DIFFUSE));
 					if(do_nee_one)
 					{
-						const float r = rng01(pixel, sample_ * 64u + sub, k, P.seed ^ 0x9e3779b9u);
+						const float r = rng01(pixel, sample_ * 64u + sub, k, tseed ^ 0x9e3779b9u);
 						nee_light = min(static_cast<uint32_t>(r * static_cast<float>(P.n_lights)), P.n_lights - 1u);
 						for(int c = 0; c < 3; ++c) nee_weight[c] = xm(thr[c], static_cast<float>(P.n_lights));
-						n_shadow = 2u * static_cast<uint32_t>(sc.lights[nee_light].samples);
+						n_shadow = light_shadow_rays(sc.lights[nee_light], division);
 					}
 					float e[3];
 					if((k == 1 && (s.m->flags & BF_EMIT)) || (k >= 2 && (mat1 & BF_EMIT) && caustic))
@@ -780,9 +1229,28 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 		ShadowWriter sw{W.s_ray, W.s_col, W.s_pix, W.s_path, path, wbase + incl - n_shadow, wbase + incl};
 		if(sw.end > shadow_cap) sw.end = sw.slot > shadow_cap ? sw.slot : shadow_cap;
 		if(do_nee_all)
-			for(uint32_t l = 0; l < P.n_lights; ++l) light_estimation(sc, s, wo, l, l, sample_, offset_, nee_weight, pixel, sw);
-		if(do_nee_one) light_estimation(sc, s, wo, nee_light, nee_light, sample_, offset_, nee_weight, pixel, sw);
+			for(uint32_t l = 0; l < P.n_lights; ++l) light_estimation(sc, s, wo, l, l, sample_, offset_, nee_weight, pixel, sw, division);
+		if(do_nee_one) light_estimation(sc, s, wo, nee_light, nee_light, sample_, offset_, nee_weight, pixel, sw, division);
 		sw.close();
+		// --- spawned integrate() calls of the recursive split ----------------
+		if(W.sp_out && __any_sync(0xffffffffu, n_spawn != 0u))
+		{
+			uint32_t sincl = n_spawn;
+			for(int off = 1; off < 32; off <<= 1)
+			{
+				const uint32_t v = __shfl_up_sync(0xffffffffu, sincl, off);
+				if(lane >= static_cast<uint32_t>(off)) sincl += v;
+			}
+			const uint32_t stotal = __shfl_sync(0xffffffffu, sincl, 31);
+			uint32_t sbase = 0;
+			if(lane == 31) sbase = atomicAdd(W.sp_count, stotal);
+			sbase = __shfl_sync(0xffffffffu, sbase, 31);
+			SpawnWriter spw{W.sp_out, sbase + sincl - n_spawn, sbase + sincl, W.sp_cap};
+			if(n_spawn)
+				spawn_children(sc, P, s, wo, thr, pixel, si, sample_, offset_, level + 1u, addl, division, branch, deco1, deco2,
+				               do_glossy, do_spec, spw);
+			spw.close();
+		}
 		// --- continuation ray ----------------------------------------------
 		if(hit && !rr_dead)
 		{
@@ -790,11 +1258,16 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 			uint32_t req = BF_ALL;
 			if(k == 0)
 			{
-				if(s.m->flags & BF_DIFFUSE)    // path_flags = Diffuse (integrator_path_tracer.cc:178-190)
+				if(s.m->flags & BF_DIFFUSE)    // path_flags = Diffuse (integrator_path_tracer.cc:178-200)
 				{
 					const uint32_t offs = static_cast<uint32_t>(P.path_samples) * sample_ + offset_ + sub;
 					s1 = gbrt::ri_vdc(offs);
 					s2 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 2, offs));
+					if(division > 1)   // math::addMod1 with the split's decorrelation
+					{
+						s1 += deco1; if(s1 > 1.f) s1 -= 1.f;
+						s2 += deco2; if(s2 > 1.f) s2 -= 1.f;
+					}
 					req = BF_DIFFUSE | BF_REFLECT | BF_TRANSMIT;
 				}
 			}
@@ -809,8 +1282,8 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				}
 				else
 				{
-					s1 = rng01(pixel, sample_ * 64u + sub, 1000u + k, P.seed);
-					s2 = rng01(pixel, sample_ * 64u + sub, 2000u + k, P.seed);
+					s1 = rng01(pixel, sample_ * 64u + sub, 1000u + k, tseed);
+					s2 = rng01(pixel, sample_ * 64u + sub, 2000u + k, tseed);
 				}
 			}
 			if(s1 >= 0.f)
@@ -827,12 +1300,12 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 					// plain estimator targets, so guided and plain converge alike.
 					const float *lob = W.lobes + static_cast<size_t>(gbrt::kGuideOut) * q;
 					const uint32_t key = sample_ * 64u + sub;
-					const float u = rng01(pixel, key, k, P.seed ^ 0x51ed270bu);
+					const float u = rng01(pixel, key, k, tseed ^ 0x51ed270bu);
 					float fw[3], ptrue;
 					if(u < P.alpha)
 					{
-						gbrt::mixture_sample(lob, rng01(pixel, key, k, P.seed ^ 0x2545f491u), rng01(pixel, key, k, P.seed ^ 0x6c8e9cf5u),
-						                     rng01(pixel, key, k, P.seed ^ 0x1b873593u), wi);
+						gbrt::mixture_sample(lob, rng01(pixel, key, k, tseed ^ 0x2545f491u), rng01(pixel, key, k, tseed ^ 0x6c8e9cf5u),
+						                     rng01(pixel, key, k, tseed ^ 0x1b873593u), wi);
 						bsdf_eval_at(s, wo, wi, req, fw);
 						ptrue = bsdf_true_pdf(s, wo, wi, req);
 						sflags = BF_DIFFUSE | BF_REFLECT;
@@ -863,7 +1336,9 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				for(int c = 0; c < 3; ++c) nt[c] = xm(thr[c], mult[c]);
 				if(k == 0)
 				{
-					const float inv_ps = __fdiv_rn(1.f, static_cast<float>(P.path_samples));
+					// path_col / n_samples, n_samples = max(1, path_samples / division)
+					const int n_samples = max(1, P.path_samples / static_cast<int>(division));
+					const float inv_ps = __fdiv_rn(1.f, static_cast<float>(n_samples));
 					for(int c = 0; c < 3; ++c) nt[c] = xm(nt[c], inv_ps);
 				}
 				if(nt[0] != 0.f || nt[1] != 0.f || nt[2] != 0.f)
@@ -988,6 +1463,47 @@ __global__ void k_gather_batch(const float4 *__restrict__ rec, uint32_t n, uint3
 
 __global__ void k_reset(uint32_t *count, int which) { count[which] = 0u; count[2] = 0u; }
 
+// Spawned integrate() calls -> paths of a new wave (dead records skipped,
+// live ones compacted into path slots and the first ray queue).
+__global__ void __launch_bounds__(kThreads) k_spawn_init(Work W, const float4 *__restrict__ rec, uint32_t n)
+{
+	const uint32_t lane = threadIdx.x & 31u;
+	for(uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x)
+	{
+		const uint32_t i = base + threadIdx.x;
+		float4 r3 = make_float4(0.f, 0.f, 0.f, 0.f);
+		bool live = false;
+		if(i < n)
+		{
+			r3 = rec[5ull * i + 3];
+			live = __float_as_uint(r3.x) != kDead;
+		}
+		const uint32_t ballot = __ballot_sync(0xffffffffu, live);
+		if(!ballot) continue;
+		const uint32_t leader = __ffs(ballot) - 1u;
+		uint32_t qbase = 0;
+		if(lane == leader)
+		{
+			qbase = atomicAdd(W.count, static_cast<uint32_t>(__popc(ballot)));
+			atomicAdd(W.stats, static_cast<unsigned long long>(__popc(ballot)));
+		}
+		qbase = __shfl_sync(0xffffffffu, qbase, leader);
+		if(live)
+		{
+			const uint32_t slot = qbase + __popc(ballot & ((1u << lane) - 1u));
+			const float4 r0 = rec[5ull * i], r1 = rec[5ull * i + 1], r2 = rec[5ull * i + 2], r4 = rec[5ull * i + 4];
+			W.p_pixel[slot] = __float_as_uint(r3.x);
+			W.p_si[slot] = __float_as_uint(r3.y);
+			W.p_thr[slot] = make_float4(r2.x, r2.y, r2.z, 0.f);
+			W.p_state[slot] = 0u;
+			W.p_task[slot] = make_uint4(__float_as_uint(r3.z), __float_as_uint(r3.w), __float_as_uint(r4.x), __float_as_uint(r4.y));
+			W.q_ray[0][2ull * slot] = r0;
+			W.q_ray[0][2ull * slot + 1] = r1;
+			W.q_path[0][slot] = slot;
+		}
+	}
+}
+
 __global__ void k_mean(const float *sum, const double *sum64, float *out, size_t n, float inv)
 {
 	for(size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
@@ -1044,10 +1560,18 @@ struct gbrt_scene {
 	uint16_t *lds_perm = nullptr;
 	uint32_t *lds_off = nullptr, *lds_base = nullptr;
 	double *lds_inv = nullptr;
+	// materials that start the recursive split, for its buffer sizing
+	bool split_glossy = false, split_glossy_transmit = false, split_specular = false;
+	uint32_t max_addl = 0;
 	// work buffers (grown on demand)
 	size_t cap_paths = 0, cap_shadow = 0, cap_stride = 0;
 	void *work = nullptr;
 	Work w{};
+	// spawn buffers: one per ray level of the recursive split
+	float4 *spawn = nullptr;
+	uint32_t *spawn_count = nullptr;
+	size_t spawn_cap = 0;
+	int spawn_levels = 0;
 	std::mutex mu;
 };
 
@@ -1063,6 +1587,7 @@ int alloc_work(gbrt_scene *S, size_t paths, size_t shadow, size_t stride)
 	size_t off = 0;
 	auto carve = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
 	const size_t o_pix = carve(4 * paths), o_si = carve(4 * paths), o_st = carve(4 * paths), o_thr = carve(16 * paths);
+	const size_t o_task = carve(16 * paths);
 	const size_t o_qr0 = carve(32 * paths), o_qr1 = carve(32 * paths), o_qp0 = carve(4 * paths), o_qp1 = carve(4 * paths);
 	const size_t o_hit = carve(16 * paths);
 	const size_t o_sr = carve(32 * shadow), o_sc = carve(16 * shadow), o_sp = carve(4 * shadow), o_spath = carve(4 * shadow);
@@ -1084,6 +1609,7 @@ int alloc_work(gbrt_scene *S, size_t paths, size_t shadow, size_t stride)
 	w.p_si = reinterpret_cast<uint32_t *>(b + o_si);
 	w.p_state = reinterpret_cast<uint32_t *>(b + o_st);
 	w.p_thr = reinterpret_cast<float4 *>(b + o_thr);
+	w.p_task = reinterpret_cast<uint4 *>(b + o_task);
 	w.q_ray[0] = reinterpret_cast<float4 *>(b + o_qr0);
 	w.q_ray[1] = reinterpret_cast<float4 *>(b + o_qr1);
 	w.q_path[0] = reinterpret_cast<uint32_t *>(b + o_qp0);
@@ -1112,6 +1638,33 @@ int alloc_work(gbrt_scene *S, size_t paths, size_t shadow, size_t stride)
 	S->cap_shadow = shadow;
 	S->cap_stride = stride;
 	return GBRT_OK;
+}
+
+int alloc_spawn(gbrt_scene *S, size_t cap, int levels)
+{
+	if(cap <= S->spawn_cap && levels <= S->spawn_levels) return GBRT_OK;
+	cap = std::max(cap, S->spawn_cap);
+	levels = std::max(levels, S->spawn_levels);
+	if(S->spawn) { cudaFree(S->spawn); S->spawn = nullptr; }
+	if(S->spawn_count) { cudaFree(S->spawn_count); S->spawn_count = nullptr; }
+	S->spawn_cap = 0; S->spawn_levels = 0;
+	cudaError_t e = cudaMalloc(&S->spawn, cap * levels * 5 * sizeof(float4));
+	if(e == cudaSuccess) e = cudaMalloc(&S->spawn_count, levels * sizeof(uint32_t));
+	if(e != cudaSuccess)
+		return gbrt_set_error(GBRT_ERR_OOM, "recursive split buffers (%zu records x %d levels): %s", cap, levels, cudaGetErrorString(e));
+	S->spawn_cap = cap;
+	S->spawn_levels = levels;
+	return GBRT_OK;
+}
+
+// Upper bound of the spawn records one hit can write (largest at division 1).
+uint32_t split_fanout(const gbrt_scene *S, int path_samples)
+{
+	const uint32_t ps = static_cast<uint32_t>(std::max(1, path_samples));
+	uint32_t f = 0;
+	if(S->split_glossy) f += 8u * (S->split_glossy_transmit ? 2u : 1u) * std::max(1u, ps / 8u);
+	if(S->split_specular) f += 2u * ps;
+	return f;
 }
 
 // Camera::Camera axes (camera.cc:96-103) and PerspectiveCamera::setAxis
@@ -1201,19 +1754,45 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 			d.flags = (d.with_diffuse ? (BF_DIFFUSE | BF_REFLECT) : 0u) | (d.as_diffuse ? (BF_DIFFUSE | BF_REFLECT) : (BF_GLOSSY | BF_REFLECT));
 			d.p_diffuse = std::min(0.6f, 1.f - (d.m_glossy / (d.m_glossy + (1.f - d.m_glossy) * d.m_diffuse)));
 			for(int k = 0; k < 3; ++k) { d.col[k] = m.color[k]; d.col2[k] = m.color2[k]; }
-			if(!d.as_diffuse) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: glossy material %u with as_diffuse = false needs the recursive glossy tracer (not built)", i);
+		}
+		else if(m.type == GBRT_MAT_GLASS || m.type == GBRT_MAT_ROUGH_GLASS)
+		{
+			// GlassMaterial / RoughGlassMaterial ctors (material_glass.cc:140-151,
+			// material_rough_glass.cc:143-154; material_rough_glass.h:91-94):
+			// filter_color_ = transmit_filter x filter_color + (1 - transmit_filter)
+			const float tf = m.params[1];
+			for(int k = 0; k < 3; ++k) { d.col[k] = tf * m.color[k] + (1.f - tf); d.col2[k] = m.color2[k]; }
+			d.ior = m.params[0] > 0.f ? m.params[0] : 1.4f;
+			if(m.type == GBRT_MAT_GLASS) d.flags = BF_SPECULAR | BF_REFLECT | BF_TRANSMIT;
+			else
+			{
+				const float alpha = m.params[2] > 0.f ? m.params[2] : 0.5f;
+				const float a = std::max(1e-4f, std::min(alpha * 0.5f, 1.f));
+				d.a2 = a * a;
+				d.flags = BF_GLOSSY | BF_REFLECT | BF_TRANSMIT;
+			}
 		}
 		else return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: material %u has unsupported type %u", i, m.type);
+		d.addl_depth = static_cast<uint32_t>(std::max(0.f, std::min(m.params[5], 32.f)));    // additionaldepth (material.h:177)
 	}
 	// lights
 	std::vector<DevLight> ls(n_lights);
 	for(uint32_t i = 0; i < n_lights; ++i)
 	{
 		const gbrt_light_desc &L = lights[i];
-		if(L.type != GBRT_LIGHT_AREA) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: light %u has unsupported type %u", i, L.type);
-		if(L.samples < 1) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: light %u has %d samples", i, L.samples);
+		if(L.type != GBRT_LIGHT_AREA && L.type != GBRT_LIGHT_POINT)
+			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: light %u has unsupported type %u", i, L.type);
 		DevLight &d = ls[i];
 		std::memset(&d, 0, sizeof(d));
+		d.type = L.type;
+		if(L.type == GBRT_LIGHT_POINT)
+		{
+			// PointLight: color_ = color x power (light_point.h:64)
+			for(int k = 0; k < 3; ++k) { d.c[k] = L.corner[k]; d.col[k] = L.color[k] * L.power; }
+			d.samples = 1;
+			continue;
+		}
+		if(L.samples < 1) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: light %u has %d samples", i, L.samples);
 		float tx[3], ty[3];
 		for(int k = 0; k < 3; ++k) { d.c[k] = L.corner[k]; tx[k] = L.point1[k] - L.corner[k]; ty[k] = L.point2[k] - L.corner[k]; }
 		for(int k = 0; k < 3; ++k) { d.tx[k] = tx[k]; d.ty[k] = ty[k]; }
@@ -1254,6 +1833,12 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 	}
 	gbrt_scene *S = new gbrt_scene();
 	S->bvh = bvh;
+	for(const DevMaterial &d : mats)
+	{
+		if((d.flags & BF_GLOSSY) && (d.flags & BF_REFLECT)) { S->split_glossy = true; if(d.flags & BF_TRANSMIT) S->split_glossy_transmit = true; }
+		if(d.flags & (BF_SPECULAR | BF_FILTER)) S->split_specular = true;
+		S->max_addl = std::max(S->max_addl, d.addl_depth);
+	}
 	S->n_prims = n_faces; S->n_mats = n_materials; S->n_lights = n_lights;
 	auto fail = [&](int rc) { gbrt_scene_destroy(S); return rc; };
 	cudaError_t e;
@@ -1284,7 +1869,7 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 int gbrt_scene_destroy(gbrt_scene *S)
 {
 	if(!S) return GBRT_OK;
-	void *ptrs[] = {S->prim_ng, S->mats, S->lights, S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->work};
+	void *ptrs[] = {S->prim_ng, S->mats, S->lights, S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->work, S->spawn, S->spawn_count};
 	for(void *p : ptrs) if(p) cudaFree(p);
 	delete S;
 	return GBRT_OK;
@@ -1306,7 +1891,19 @@ int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 	if(pp.guide_batch > kMaxBatch) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_pt_render: guide_batch %u > %u", pp.guide_batch, kMaxBatch);
 	const bool guiding = guide && pp.guide_alpha > 0.f;
 	const bool record = guide && pp.guide_train_steps > 0;
-	const uint64_t wave = std::min<uint64_t>(total, pp.wave_paths ? pp.wave_paths : (record ? (1ull << 20) : (1ull << 22)));
+	uint64_t wave = std::min<uint64_t>(total, pp.wave_paths ? pp.wave_paths : (record ? (1ull << 20) : (1ull << 22)));
+	// recursive split: spawned integrate() calls go to one buffer per ray
+	// level; waves are cut so one wave's children always fit a buffer
+	const int raydepth = pp.raydepth > 0 ? pp.raydepth : 5;
+	const uint32_t fanout = split_fanout(S, pp.path_samples);
+	const int split_levels = fanout ? std::min(19, raydepth + static_cast<int>(S->max_addl)) : 0;
+	constexpr uint64_t kSpawnCap = 1ull << 22;
+	if(split_levels > 0)
+	{
+		wave = std::max<uint64_t>(1, std::min<uint64_t>(wave, kSpawnCap / fanout));
+		if(int rc = alloc_spawn(S, static_cast<size_t>(wave) * fanout, split_levels)) return rc;
+	}
+	const size_t spawn_cap = static_cast<size_t>(wave) * fanout;
 	uint32_t max_shadow = 0;
 	{
 		std::vector<DevLight> ls(S->n_lights);
@@ -1322,6 +1919,7 @@ int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 	SceneDev sc{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv}};
 	Params P{};
 	P.spp = pp.spp; P.path_samples = pp.path_samples; P.bounces = pp.bounces; P.rr_min = pp.russian_roulette_min_bounces;
+	P.raydepth = raydepth;
 	P.base_offset = pp.base_sampling_offset; P.seed = pp.seed;
 	P.d1 = 1.f / static_cast<float>(pp.spp);
 	P.n_lights = S->n_lights;
@@ -1339,27 +1937,74 @@ int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 		GBRT_CK(cudaEventRecord(e0, s));
 	}
 	GBRT_CK(cudaMemsetAsync(S->w.stats, 0, 2 * sizeof(unsigned long long), s));
-	for(uint64_t start = 0; start < total; start += wave)
-	{
-		P.wave_start = static_cast<uint32_t>(start);
-		P.wave_n = static_cast<uint32_t>(std::min<uint64_t>(wave, total - start));
-		k_camera<<<grid_for(P.wave_n, S->n_sm), kThreads, 0, s>>>(cam, P, W);
+	// one wave: the paths in the path slots (count[0] of them, at most n)
+	// advance vertex by vertex
+	auto vertex_loop = [&](Params &Pw, const Work &Ww, uint32_t n, bool camera_wave) -> int {
+		Pw.wave_n = n;
 		int cur = 0;
 		for(int vtx = 0; vtx <= pp.bounces; ++vtx)
 		{
 			// guide only the first guide_max_vertex vertex levels (a wavefront
 			// level holds the paths' vertex vtx, so the network runs only there)
 			const bool level_guided = guiding && (pp.guide_max_vertex == 0 || vtx < static_cast<int>(pp.guide_max_vertex));
-			P.guiding = level_guided ? 1 : 0;
-			P.record = (record && (pp.guide_max_vertex == 0 || vtx < static_cast<int>(pp.guide_max_vertex))) ? 1 : 0;
-			k_reset<<<1, 1, 0, s>>>(W.count, cur ^ 1);
-			k_extend<<<grid_for(P.wave_n, S->n_sm), kThreads, 0, s>>>(sc.bv, W.q_ray[cur], W.count + cur, W.hits, level_guided ? W.hitpos : nullptr);
+			Pw.guiding = level_guided ? 1 : 0;
+			Pw.record = (camera_wave && record && (pp.guide_max_vertex == 0 || vtx < static_cast<int>(pp.guide_max_vertex))) ? 1 : 0;
+			k_reset<<<1, 1, 0, s>>>(Ww.count, cur ^ 1);
+			k_extend<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc.bv, Ww.q_ray[cur], Ww.count + cur, Ww.hits, level_guided ? Ww.hitpos : nullptr);
 			if(level_guided)
-				if(int rc = gbrt_guide_eval_queue(guide, W.hitpos, P.wave_n, W.count + cur, W.lobes, s)) return rc;
-			k_shade<<<grid_for(P.wave_n, S->n_sm), kThreads, 0, s>>>(sc, P, W, cur, camera->resx, static_cast<uint32_t>(shadow_cap), film, film64_dev);
-			k_shadow<<<grid_for(shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, W, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+				if(int rc = gbrt_guide_eval_queue(guide, Ww.hitpos, n, Ww.count + cur, Ww.lobes, s)) return rc;
+			k_shade<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, camera->resx, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+			k_shadow<<<grid_for(shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Ww, static_cast<uint32_t>(shadow_cap), film, film64_dev);
 			cur ^= 1;
 		}
+		return GBRT_OK;
+	};
+	// spawn buffer of ray level L (1 .. split_levels)
+	auto spawn_buf = [&](int L) { return S->spawn + static_cast<size_t>(L - 1) * spawn_cap * 5; };
+	auto spawn_target = [&](Work &Ww, int child_level) -> int {
+		if(child_level > split_levels) { Ww.sp_out = nullptr; Ww.sp_count = nullptr; Ww.sp_cap = 0; return GBRT_OK; }
+		Ww.sp_out = spawn_buf(child_level);
+		Ww.sp_count = S->spawn_count + (child_level - 1);
+		Ww.sp_cap = static_cast<uint32_t>(spawn_cap);
+		GBRT_CK(cudaMemsetAsync(Ww.sp_count, 0, sizeof(uint32_t), s));
+		return GBRT_OK;
+	};
+	auto spawned = [&](int child_level, uint32_t &n) -> int {
+		n = 0;
+		if(child_level > split_levels) return GBRT_OK;
+		GBRT_CK(cudaMemcpyAsync(&n, S->spawn_count + (child_level - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+		GBRT_CK(cudaStreamSynchronize(s));
+		if(n > spawn_cap) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_pt_render: %u spawned rays at level %d exceed %zu", n, child_level, spawn_cap);
+		return GBRT_OK;
+	};
+	// integrate() calls of ray level L, depth first: a chunk of them, then
+	// everything they spawned, then the next chunk
+	std::function<int(int, uint32_t)> process_level = [&](int L, uint32_t n) -> int {
+		for(uint32_t c0 = 0; c0 < n; c0 += static_cast<uint32_t>(wave))
+		{
+			const uint32_t cn = static_cast<uint32_t>(std::min<uint64_t>(wave, n - c0));
+			Params Pc = P;
+			Work Wc = W;
+			Wc.p_sum = nullptr;
+			if(int rc = spawn_target(Wc, L + 1)) return rc;
+			GBRT_CK(cudaMemsetAsync(Wc.count, 0, sizeof(uint32_t), s));
+			k_spawn_init<<<grid_for(cn, S->n_sm), kThreads, 0, s>>>(Wc, spawn_buf(L) + 5ull * c0, cn);
+			if(int rc = vertex_loop(Pc, Wc, cn, false)) return rc;
+			uint32_t nc = 0;
+			if(int rc = spawned(L + 1, nc)) return rc;
+			if(nc)
+				if(int rc = process_level(L + 1, nc)) return rc;
+		}
+		return GBRT_OK;
+	};
+	for(uint64_t start = 0; start < total; start += wave)
+	{
+		P.wave_start = static_cast<uint32_t>(start);
+		P.wave_n = static_cast<uint32_t>(std::min<uint64_t>(wave, total - start));
+		Work Wv = W;
+		if(int rc = spawn_target(Wv, 1)) return rc;
+		k_camera<<<grid_for(P.wave_n, S->n_sm), kThreads, 0, s>>>(cam, P, Wv);
+		if(int rc = vertex_loop(P, Wv, P.wave_n, true)) return rc;
 		if(record)
 		{
 			GBRT_CK(cudaMemsetAsync(W.count + 3, 0, sizeof(uint32_t), s));
@@ -1385,6 +2030,10 @@ int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 					if(int rc = gbrt_guide_step(guide, bbuf, batch, nullptr, s)) return rc;
 				}
 		}
+		uint32_t nc = 0;
+		if(int rc = spawned(1, nc)) return rc;
+		if(nc)
+			if(int rc = process_level(1, nc)) return rc;
 	}
 	GBRT_CK(cudaGetLastError());
 	if(stats)

@@ -57,7 +57,7 @@ class PtParams(ctypes.Structure):
                 ("russian_roulette_min_bounces", ctypes.c_int32), ("base_sampling_offset", ctypes.c_uint32),
                 ("seed", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("wave_paths", ctypes.c_uint32),
                 ("guide", ctypes.c_void_p), ("guide_alpha", ctypes.c_float), ("guide_train_steps", ctypes.c_uint32),
-                ("guide_batch", ctypes.c_uint32), ("guide_max_vertex", ctypes.c_uint32)]
+                ("guide_batch", ctypes.c_uint32), ("guide_max_vertex", ctypes.c_uint32), ("raydepth", ctypes.c_int32)]
 
 
 class PtStats(ctypes.Structure):
@@ -238,10 +238,21 @@ def _material_desc(m):
         d.color[:] = [float(x) for x in m[1]]
         d.power = float(m[2])
     elif kind == "glossy":
-        _, dc, gc, e, gr, dr = m
+        _, dc, gc, e, gr, dr = m[:6]
         d.color[:] = [float(x) for x in gc]
         d.color2[:] = [float(x) for x in dc]
-        d.params[:4] = [float(e), float(gr), float(dr), 1.0]
+        d.params[:4] = [float(e), float(gr), float(dr), float(m[6]) if len(m) > 6 else 1.0]
+    elif kind in ("glass", "rough_glass"):
+        # ("glass", IOR, filter_color, transmit_filter, mirror_color)
+        # ("rough_glass", IOR, alpha, filter_color, transmit_filter, mirror_color)
+        ior, rest = float(m[1]), m[2:]
+        alpha = 0.0
+        if kind == "rough_glass":
+            alpha, rest = float(rest[0]), rest[1:]
+        fc, tf, mc = rest
+        d.color[:] = [float(x) for x in fc]
+        d.color2[:] = [float(x) for x in mc]
+        d.params[:3] = [ior, float(tf), alpha]
     else:
         vals = [float(x) for x in m[1]]
         d.color[:] = vals[0:3]
@@ -263,8 +274,15 @@ class Renderer:
             mats[i] = _material_desc(scene["materials"][name])
         lights = (LightDesc * max(1, len(scene["lights"])))()
         for i, L in enumerate(scene["lights"]):
+            if L["type"] == "pointlight":
+                lights[i].type = 1
+                lights[i].corner[:] = [float(x) for x in L["from"]]
+                lights[i].color[:] = [float(x) for x in L["color"]]
+                lights[i].power = float(L["power"])
+                lights[i].samples = 1
+                continue
             if L["type"] != "arealight":
-                raise ValueError("only arealight is supported by this renderer")
+                raise ValueError(f"unsupported light type {L['type']}")
             lights[i].type = 0
             lights[i].corner[:] = [float(x) for x in L["corner"]]
             lights[i].point1[:] = [float(x) for x in L["point1"]]
@@ -309,7 +327,7 @@ class Renderer:
         return PtParams(int(spp), int(it.get("path_samples", 1)), int(it.get("bounces", 5)),
                         int(it.get("russian_roulette_min_bounces", 0)), int(base_offset), int(seed),
                         PT_FP64_FILM if fp64 else 0, int(wave_paths), guide.handle if guide is not None else None,
-                        float(alpha), int(train_steps), int(batch), int(max_vertex))
+                        float(alpha), int(train_steps), int(batch), int(max_vertex), int(it.get("raydepth", 5)))
 
     def render(self, spp, base_offset=0, seed=1, fp64=False, guide=None, alpha=0.0, train_steps=0, batch=0,
                max_vertex=0):

@@ -141,12 +141,63 @@ def glossy_material(diffuse_color, glossy_color=(0.9, 0.9, 0.9), exponent=100.0,
             float(diffuse_reflect))
 
 
-def cornell_scene(res=512, light_samples=4, bounces=5, rr_min=3, path_samples=1, glossy=False):
+def glass_material(ior=1.5, filter_color=(1.0, 1.0, 1.0), transmit_filter=0.0, mirror_color=(1.0, 1.0, 1.0)):
+    """A "glass" material tuple: (type, IOR, filter_color, transmit_filter,
+    mirror_color); the filter colour acts in proportion to transmit_filter."""
+    return ("glass", float(ior), tuple(filter_color), float(transmit_filter), tuple(mirror_color))
+
+
+def rough_glass_material(ior=1.5, alpha=0.1, filter_color=(1.0, 1.0, 1.0), transmit_filter=0.0, mirror_color=(1.0, 1.0, 1.0)):
+    """A "rough_glass" material tuple: (type, IOR, alpha, filter_color,
+    transmit_filter, mirror_color)."""
+    return ("rough_glass", float(ior), float(alpha), tuple(filter_color), float(transmit_filter), tuple(mirror_color))
+
+
+def icosphere(center, radius, subdiv):
+    """Sphere mesh from a subdivided icosahedron: 20 * 4**subdiv outward-facing
+    triangles.  Returns (vertices float32 [n,3], faces uint32 [m,4] TRI-marked)."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    V = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    V = [np.asarray(v, np.float64) / np.linalg.norm(v) for v in V]
+    F = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6), (7, 1, 8),
+         (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdiv):
+        mid = {}
+
+        def midpoint(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in mid:
+                m = V[a] + V[b]
+                V.append(m / np.linalg.norm(m))
+                mid[key] = len(V) - 1
+            return mid[key]
+        nf = []
+        for a, b, c in F:
+            ab, bc, ca = midpoint(a, b), midpoint(b, c), midpoint(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        F = nf
+    P = np.asarray(V) * float(radius) + np.asarray(center, np.float64)
+    out = []
+    for a, b, c in F:
+        n = np.cross(P[b] - P[a], P[c] - P[a])
+        if np.dot(n, (P[a] + P[b] + P[c]) / 3.0 - np.asarray(center)) < 0:
+            b, c = c, b
+        out.append([a, b, c, TRI])
+    return P.astype(np.float32), np.asarray(out, np.uint32)
+
+
+def cornell_scene(res=512, light_samples=4, bounces=5, rr_min=3, path_samples=1, glossy=False, glass=False, point_light=False):
     """The Cornell-box configuration: 34 triangles of walls and boxes
     (shinydiffuse, grey 0.75 / red / green), a 0.5 x 0.5 m ceiling area light
     of colour (17,12,4) at y = 1.999 with a 2-triangle light_mat emitter,
     40-degree pinhole camera (focal 1.3737) from (0,1,3.7).  glossy=True
-    makes the tall box glossy (exponent 100) and the floor glossy (exponent 20)."""
+    makes the tall box glossy (exponent 100) and the floor glossy (exponent 20).
+    glass=True adds a glass sphere (IOR 1.5, r 0.25, 320 triangles) on the
+    short box and a rough-glass sphere (IOR 1.5, alpha 0.2, r 0.3) at the
+    front left, both rendered through the recursive split.  point_light=True
+    replaces the area light (and its emitter) by a pointlight at (0, 1.8, 0.2)
+    of power 3."""
     verts, faces, groups = cornell_mesh(as_quads=False)
     mats = {"grey": ("shinydiffusemat", (0.75, 0.75, 0.75)),
             "red": ("shinydiffusemat", (0.63, 0.065, 0.05)),
@@ -169,14 +220,25 @@ def cornell_scene(res=512, light_samples=4, bounces=5, rr_min=3, path_samples=1,
         remap = {int(u): i for i, u in enumerate(used)}
         ff = np.array([[remap[int(x)] for x in row[:3]] + [TRI] for row in f], np.uint32)
         objects.append({"name": f"group{g}", "material": gmat[g], "vertices": verts[used], "faces": ff})
+    if glass:
+        mats["glass"] = glass_material(1.5)
+        mats["rough_glass"] = rough_glass_material(1.5, 0.2)
+        v, f = icosphere((0.35, 0.85, 0.25), 0.25, 2)
+        objects.append({"name": "glass_ball", "material": "glass", "vertices": v, "faces": f})
+        v, f = icosphere((-0.5, 0.3, 0.55), 0.3, 2)
+        objects.append({"name": "rough_ball", "material": "rough_glass", "vertices": v, "faces": f})
     c = np.array([-0.25, 1.999, -0.25])
     x = np.array([0.5, 0.0, 0.0])
     z = np.array([0.0, 0.0, 0.5])
-    lv = np.array([c, c + x, c + x + z, c + z], np.float32)
-    objects.append({"name": "lamp", "material": "emitter", "vertices": lv,
-                    "faces": np.array([[0, 1, 2, TRI], [0, 2, 3, TRI]], np.uint32)})
-    lights = [{"type": "arealight", "corner": tuple(c), "point1": tuple(c + x), "point2": tuple(c + z),
-               "color": (17.0, 12.0, 4.0), "power": 1.0, "samples": light_samples}]
+    if point_light:
+        del mats["emitter"]
+        lights = [{"type": "pointlight", "from": (0.0, 1.8, 0.2), "color": (1.0, 0.9, 0.8), "power": 3.0}]
+    else:
+        lv = np.array([c, c + x, c + x + z, c + z], np.float32)
+        objects.append({"name": "lamp", "material": "emitter", "vertices": lv,
+                        "faces": np.array([[0, 1, 2, TRI], [0, 2, 3, TRI]], np.uint32)})
+        lights = [{"type": "arealight", "corner": tuple(c), "point1": tuple(c + x), "point2": tuple(c + z),
+                   "color": (17.0, 12.0, 4.0), "power": 1.0, "samples": light_samples}]
     camera = {"from": (0.0, 1.0, 3.7), "to": (0.0, 1.0, 0.0), "up": (0.0, 2.0, 3.7),
               "resx": res, "resy": res, "focal": 1.3737}
     integ = {"type": "pathtracing", "path_samples": path_samples, "bounces": bounces,

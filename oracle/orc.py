@@ -141,6 +141,14 @@ def reference_scene_text(scene, spp, batches, threads=-1):
             _, dc, gc, e, gr, dr = m
             vals = [*dc, *gc, e, gr, dr]
             out.append(f"material {name} glossy " + " ".join(repr(float(x)) for x in vals))
+        elif t == "glass":
+            _, ior, fc, tf, mc = m
+            vals = [ior, tf, *fc, *mc]
+            out.append(f"material {name} glass " + " ".join(repr(float(x)) for x in vals))
+        elif t == "rough_glass":
+            _, ior, alpha, fc, tf, mc = m
+            vals = [ior, alpha, tf, *fc, *mc]
+            out.append(f"material {name} rough_glass " + " ".join(repr(float(x)) for x in vals))
         else:
             out.append(f"material {name} {t} " + " ".join(repr(float(x)) for x in m[1]))
     for o in scene["objects"]:

@@ -10,8 +10,8 @@
 //   material NAME shinydiffusemat R G B
 //   material NAME light_mat R G B POWER
 //   material NAME glossy R G B  SR SG SB  EXPONENT  GLOSSY_REFLECT  DIFFUSE_REFLECT
-//   material NAME rough_glass IOR ALPHA  FR FG FB
-//   material NAME glass IOR  FR FG FB
+//   material NAME rough_glass IOR ALPHA TRANSMIT_FILTER  FR FG FB  MR MG MB
+//   material NAME glass IOR TRANSMIT_FILTER  FR FG FB  MR MG MB
 //   object NAME MATERIAL NV NF   then NV lines "x y z", NF lines "a b c" or "a b c d"
 //   arealight CX CY CZ  P1X P1Y P1Z  P2X P2Y P2Z  R G B  POWER SAMPLES
 //   pointlight X Y Z  R G B  POWER
@@ -87,17 +87,17 @@ int main(int argc, char **argv)
 				yafaray_setParamMapFloat(pm, "glossy_reflect", gr);
 				yafaray_setParamMapFloat(pm, "diffuse_reflect", dr);
 			}
-			else if(type == "rough_glass")
+			else if(type == "rough_glass" || type == "glass")
 			{
-				double ior, a, r, g, b; ss >> ior >> a >> r >> g >> b;
-				yafaray_setParamMapFloat(pm, "IOR", ior); yafaray_setParamMapFloat(pm, "alpha", a);
-				yafaray_setParamMapColor(pm, "filter_color", r, g, b, 1.0);
-			}
-			else if(type == "glass")
-			{
-				double ior, r, g, b; ss >> ior >> r >> g >> b;
+				double ior, a = 0.0, tf, r, g, b, mr, mg, mb;
+				ss >> ior;
+				if(type == "rough_glass") ss >> a;
+				ss >> tf >> r >> g >> b >> mr >> mg >> mb;
 				yafaray_setParamMapFloat(pm, "IOR", ior);
+				if(type == "rough_glass") yafaray_setParamMapFloat(pm, "alpha", a);
+				yafaray_setParamMapFloat(pm, "transmit_filter", tf);
 				yafaray_setParamMapColor(pm, "filter_color", r, g, b, 1.0);
+				yafaray_setParamMapColor(pm, "mirror_color", mr, mg, mb, 1.0);
 			}
 			size_t id;
 			yafaray_createMaterial(scene, &id, name.c_str(), pm, pml);

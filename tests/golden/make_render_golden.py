@@ -73,6 +73,18 @@ def render_golden(res=64, spp=16, batches=32, glossy=False):
     print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
 
 
+def variant_golden(name, res=64, spp=16, batches=32, **kw):
+    """Cornell variants: glass (glass + rough-glass spheres, the recursive
+    split) and point (a pointlight instead of the area light)."""
+    sc = scenes.cornell_scene(res=res, **kw)
+    rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
+    mean = rgb.mean(0)
+    se = rgb.std(0, ddof=1) / np.sqrt(batches)
+    np.savez_compressed(os.path.join(OUT, name), mean=mean.astype(np.float32), se=se.astype(np.float32),
+                        batches=np.int32(batches), spp=np.int32(spp), seconds=secs)
+    print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
+
+
 def indoor_golden(spp=16, batches=24):
     sc = scenes.indoor_scene(n_boxes=120, subdiv=1, res=(96, 54))
     rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
@@ -95,3 +107,7 @@ if __name__ == "__main__":
         render_golden(glossy=True)
     if "indoor" in what:
         indoor_golden()
+    if "cornell_glass" in what:
+        variant_golden("cornell_glass_64_render.npz", glass=True)
+    if "cornell_point" in what:
+        variant_golden("cornell_point_64_render.npz", point_light=True)
