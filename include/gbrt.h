@@ -272,6 +272,55 @@ int gbrt_pt_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const
                         float *image_out, gbrt_pt_stats *stats);
 
 
+/* ---- photon mapping (the `photonmapping` integrator) ---------------------
+ * Replaces PhotonIntegrator::preprocess / integrate / finalGathering and
+ * CausticPhotonIntegrator's caustic map and estimate
+ * (src/integrator/surface/integrator_photon_mapping.cc:157-828,
+ * integrator_photon_caustic.cc:102-304) with photon maps held as hashed
+ * grids on the device instead of PointKdTree (include/photon/pkdtree.h).
+ * Parameter names and defaults are the reference's; photon paths use Halton
+ * indices 0 .. n - 1, the set the reference shoots when n is a multiple of
+ * its photon threads (threads_photons). */
+typedef struct gbrt_pm_params {
+	int32_t diffuse_photons;    /* "diffuse_photons" (100000) */
+	int32_t caustic_photons;    /* "caustic_photons" (500000) */
+	float diffuse_radius;       /* "diffuse_radius" (0.1) */
+	int32_t diffuse_search;     /* "diffuse_search" (50), at most 64 */
+	float caustic_radius;       /* "caustic_radius" (0.25) */
+	int32_t caustic_mix;        /* "caustic_mix" (50), at most 64 */
+	int32_t caustic_depth;      /* "caustic_depth" (10) */
+	int32_t bounces;            /* "bounces" (3): diffuse photon bounces */
+	int32_t caustics;           /* "caustics" (0): build and use the caustic map */
+	int32_t diffuse;            /* "diffuse" (1): build and use the diffuse map */
+	int32_t final_gather;       /* "finalGather" (1) */
+	int32_t fg_samples;         /* "fg_samples" (32) */
+	int32_t fg_bounces;         /* "fg_bounces" (2) */
+	float fg_min_pathlen;       /* "fg_min_pathlen"; < 0 = diffuse_radius */
+} gbrt_pm_params;
+int gbrt_pm_default_params(gbrt_pm_params *params);
+/* Renders like gbrt_pt_render with the photonmapping integrator: builds the
+ * photon maps (and, with final gather, the radiance map) on the device, then
+ * traces the camera samples.  spp, base_sampling_offset, raydepth, seed,
+ * flags and wave_paths of `params` apply; path_samples, bounces and the
+ * guide fields are not used. */
+int gbrt_pm_render(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
+                   float *film_dev, double *film64_dev, gbrt_pt_stats *stats, void *stream);
+/* gbrt_pm_render into a temporary device film; per-pixel means copied to
+ * image_out [resy][resx][3] (host). */
+int gbrt_pm_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
+                        float *image_out, gbrt_pt_stats *stats);
+/* Diagnostic: shoots one photon map (which = 0 diffuse, 1 caustic) and copies
+ * its photons to host `out` [n][9] = (dir xyz, pos xyz, colour rgb) in
+ * deposit order; n_photons and n_paths as PhotonMap::nPhotons / nPaths. */
+int gbrt_pm_photons(gbrt_scene *scene, const gbrt_pm_params *pm, int which, float *out, uint32_t capacity, uint32_t *n_photons,
+                    uint32_t *n_paths);
+/* Diagnostic: k-nearest gather of PhotonMap::gather semantics over n host
+ * points (xyz) for m host queries through the device grid (cell edge >= the
+ * search radius): per query the count, the final squared radius and the
+ * indices of the found points ([m][k], unordered). */
+int gbrt_knn_gather(const float *points, uint32_t n, const float *queries, uint32_t m, float cell, int k, float r2,
+                    int32_t *count_out, float *r2_out, uint32_t *idx_out);
+
 /* ---- path-guiding network (no counterpart in the reference) -------------
  * q(w | x): 8-lobe von Mises-Fisher mixture over incident direction,
  * predicted from the hit position by a 16-level x 2-feature hash-grid

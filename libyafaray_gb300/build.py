@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbrt.so")
 
 SOURCES = ["capi.cu", "bvh_build.cu", "traverse.cu", "pathtrace.cu", "guiding.cu"]
-EXACT_FP = {"traverse.cu"}
+EXACT_FP = {"traverse.cu", "pathtrace.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

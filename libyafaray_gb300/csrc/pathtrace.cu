@@ -24,6 +24,7 @@
 #include "traverse_core.cuh"
 #include "sampling.cuh"
 #include "guide_device.cuh"
+#include "photon_map.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -90,12 +91,27 @@ struct Params {
 	int record;           // write training records
 	uint32_t rec_stride;  // record slots per path (= bounces)
 	int radiance_target;  // train on incident radiance instead of the product with the BSDF
+	// photonmapping integrator (PhotonIntegrator::integrate / finalGathering)
+	int pm;                    // 1: photonmapping
+	int pm_fg;                 // final gathering (path_samples then holds fg_samples)
+	int pm_fg_bounces;
+	float pm_gather_dist;      // fg_min_pathlen
+	int pm_diffuse;            // non-FG diffuse estimate from the diffuse map
+	int pm_caustics;
+	float pm_diffuse_r2;       // diffuse_radius, used as the squared radius (integrator_photon_mapping.cc:772)
+	int pm_diffuse_k;
+	float pm_caustic_r2;       // caustic_radius^2
+	int pm_caustic_k;
+	float pm_diffuse_paths, pm_caustic_paths;
+	float pm_lookup_r2;        // 4 diffuse_radius^2 (integrator_photon_mapping.h:90)
+	gbrt::PhotonGrid g_diffuse, g_caustic, g_radiance;
 };
 
 struct Work {
 	uint32_t *p_pixel, *p_si, *p_state;
 	float4 *p_thr;
 	uint4 *p_task;              // integrate() call of the path: {level | addl << 8 | division << 16, branch, deco1, deco2}
+	float4 *p_pm;               // final gathering: path length, colour of the last lookup
 	// spawned integrate() calls of the recursive split (5 float4 each:
 	// origin+tmin, dir+tmax, weight, {pixel, si, task.x, branch}, {deco1, deco2})
 	float4 *sp_out;
@@ -1154,7 +1170,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 			W.r_valid[slot] = 1u;     // complete
 		}
 		// --- decide this vertex's work, count its shadow rays -----------------
-		bool do_nee_all = false, do_nee_one = false, rr_dead = false, do_glossy = false, do_spec = false;
+		bool do_nee_all = false, do_nee_one = false, rr_dead = false, do_glossy = false, do_spec = false, pm_cont = false;
 		float nee_weight[3] = {0.f, 0.f, 0.f};
 		uint32_t nee_light = 0, n_spawn = 0;
 		if(hit)
@@ -1166,7 +1182,9 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				float e[3];
 				if((s.m->flags & BF_EMIT) && sub == 0 && mat_emit(s, wo, e))
 				{
-					film_add(film, film64, pixel, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
+					// photonmapping adds it twice (integrator_photon_mapping.cc:686-687, 713-721)
+					const float em = P.pm ? 2.f : 1.f;
+					film_add(film, film64, pixel, xm(thr[0], e[0]) * em, xm(thr[1], e[1]) * em, xm(thr[2], e[2]) * em);
 					if(W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
 				}
 				do_nee_all = (s.m->flags & BF_DIFFUSE) && sub == 0;
@@ -1183,6 +1201,97 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 					do_glossy = (f & BF_GLOSSY) && (f & BF_REFLECT);
 					do_spec = (f & (BF_SPECULAR | BF_FILTER)) != 0u;
 					n_spawn = spawn_bound(f, do_glossy, do_spec, division, static_cast<uint32_t>(P.path_samples));
+				}
+			}
+			else if(P.pm)
+			{
+				// PhotonIntegrator::finalGathering (integrator_photon_mapping.cc:547-668)
+				// after its zero'th bounce: vertex k is the loop's depth k - 1
+				const float4 pm4 = W.p_pm[path];
+				float length = pm4.x;
+				float lcol[3] = {pm4.y, pm4.z, pm4.w};
+				const float tk = W.hits[q].y;
+				bool fg_caustic = caustic != 0u;
+				bool do_bounce;
+				if(k == 1)
+				{
+					length = tk;
+					mat1 = s.m->flags;
+					fg_caustic = false;
+					do_bounce = length < P.pm_gather_dist || (mat1 & BF_SPECULAR);
+				}
+				else
+				{
+					length += tk;
+					fg_caustic = (fg_caustic || k == 2u) && ((W.p_state[path] >> 17) & 1u);
+					do_bounce = fg_caustic || length < P.pm_gather_dist;
+				}
+				const bool close = length < P.pm_gather_dist;
+				const int depth = static_cast<int>(k) - 1;
+				float nf[3];
+				face_forward(s, wo, nf);
+				if(do_bounce && depth < P.pm_fg_bounces)
+				{
+					bool add = false;
+					if(mat1 & BF_DIFFUSE)
+					{
+						if(close)
+						{
+							// estimateOneDirectLight: its value reaches the film through the
+							// shadow rays and is not kept in lcol
+							lcol[0] = lcol[1] = lcol[2] = 0.f;
+							do_nee_one = P.n_lights > 0;
+							if(do_nee_one)
+							{
+								const float r = rng01(pixel, sample_ * 64u + sub, k, tseed ^ 0x9e3779b9u);
+								nee_light = min(static_cast<uint32_t>(r * static_cast<float>(P.n_lights)), P.n_lights - 1u);
+								for(int c = 0; c < 3; ++c) nee_weight[c] = thr[c] * static_cast<float>(P.n_lights);
+								n_shadow = light_shadow_rays(sc.lights[nee_light], division);
+							}
+						}
+						else if(fg_caustic)
+						{
+							const int j = gbrt::find_nearest(P.g_radiance, s.p, nf, P.pm_lookup_r2);
+							if(j >= 0) { const float4 c4 = __ldg(P.g_radiance.col + j); lcol[0] = c4.x; lcol[1] = c4.y; lcol[2] = c4.z; }
+						}
+						add = close || fg_caustic;
+					}
+					if(add)
+					{
+						float e[3];
+						if((mat1 & BF_EMIT) && mat_emit(s, wo, e)) for(int c = 0; c < 3; ++c) lcol[c] += e[c];
+						film_add(film, film64, pixel, lcol[0] * thr[0], lcol[1] * thr[1], lcol[2] * thr[2]);
+					}
+					// next direction: All when close, else specular only (finalGathering :625-628)
+					const uint32_t offs = static_cast<uint32_t>(P.path_samples) * sample_ + offset_ + sub;
+					float s1 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 4 * depth + 3, offs));
+					float s2 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 4 * depth + 4, offs));
+					if(division > 1) { s1 += deco1; if(s1 > 1.f) s1 -= 1.f; s2 += deco2; if(s2 > 1.f) s2 -= 1.f; }
+					const uint32_t fl = close ? BF_ALL : (BF_SPECULAR | BF_REFLECT | BF_TRANSMIT | BF_FILTER);
+					float wi[3], scol[3], w, pdf;
+					uint32_t sf;
+					mat_sample(s, wo, s1, s2, fl, wi, scol, w, pdf, sf);
+					if(pdf > 1.0e-6f)
+					{
+						float nt[3];
+						for(int c = 0; c < 3; ++c) nt[c] = thr[c] * (scol[c] * w);
+						pm_cont = true;
+						W.p_thr[path] = make_float4(nt[0], nt[1], nt[2], 0.f);
+						W.p_state[path] = (k + 1u) | (mat1 << 8) | ((fg_caustic ? 1u : 0u) << 16) | (((sf & (BF_SPECULAR | BF_FILTER)) ? 1u : 0u) << 17);
+						W.p_pm[path] = make_float4(length, lcol[0], lcol[1], lcol[2]);
+						nray[0] = s.p[0]; nray[1] = s.p[1]; nray[2] = s.p[2]; nray[3] = kRayMinDist;
+						nray[4] = wi[0]; nray[5] = wi[1]; nray[6] = wi[2]; nray[7] = -1.f;
+					}
+				}
+				else if(mat1 & (BF_DIFFUSE | BF_GLOSSY))
+				{
+					// end of the gather path: radiance-map lookup (:650-664); without a
+					// radiance photon the last lcol stands
+					const int j = gbrt::find_nearest(P.g_radiance, s.p, nf, P.pm_lookup_r2);
+					if(j >= 0) { const float4 c4 = __ldg(P.g_radiance.col + j); lcol[0] = c4.x; lcol[1] = c4.y; lcol[2] = c4.z; }
+					float e[3];
+					if((mat1 & BF_EMIT) && mat_emit(s, wo, e)) for(int c = 0; c < 3; ++c) lcol[c] += e[c];
+					film_add(film, film64, pixel, lcol[0] * thr[0], lcol[1] * thr[1], lcol[2] * thr[2]);
 				}
 			}
 			else
@@ -1252,13 +1361,14 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 			spw.close();
 		}
 		// --- continuation ray ----------------------------------------------
-		if(hit && !rr_dead)
+		// (photonmapping: only the zero'th final-gather bounce comes here)
+		if(hit && !rr_dead && !(P.pm && k >= 1))
 		{
 			float s1 = -1.f, s2 = 0.f;
 			uint32_t req = BF_ALL;
 			if(k == 0)
 			{
-				if(s.m->flags & BF_DIFFUSE)    // path_flags = Diffuse (integrator_path_tracer.cc:178-200)
+				if((s.m->flags & BF_DIFFUSE) && (!P.pm || P.pm_fg))   // path_flags = Diffuse (integrator_path_tracer.cc:178-200)
 				{
 					const uint32_t offs = static_cast<uint32_t>(P.path_samples) * sample_ + offset_ + sub;
 					s1 = gbrt::ri_vdc(offs);
@@ -1353,6 +1463,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 						W.r_valid[slot] = 2u;     // waiting for the next vertex
 					}
 					caustic = (sflags & (BF_SPECULAR | BF_GLOSSY | BF_FILTER)) ? 1u : 0u;
+					if(P.pm) { caustic = 0u; W.p_pm[path] = make_float4(0.f, 0.f, 0.f, 0.f); }
 					W.p_thr[path] = make_float4(nt[0], nt[1], nt[2], 0.f);
 					W.p_state[path] = (k + 1u) | (mat1 << 8) | (caustic << 16);
 					nray[0] = s.p[0]; nray[1] = s.p[1]; nray[2] = s.p[2]; nray[3] = kRayMinDist;
@@ -1360,6 +1471,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				}
 			}
 		}
+		cont = cont || pm_cont;
 		const uint32_t ballot = __ballot_sync(0xffffffffu, cont);
 		if(ballot)
 		{
@@ -1547,6 +1659,445 @@ __global__ void k_sampler(gbrt::LdsTables t, int kind, int dim, const uint32_t *
 	if(i < n) out[i] = sampler_value(t, kind, dim, in[i]);
 }
 
+
+// ---- photon shooting (PhotonIntegrator::diffuseWorker, integrator_photon_mapping.cc:157-280;
+// CausticPhotonIntegrator::causticWorker, integrator_photon_caustic.cc:102-223) ----
+
+struct PhotonJob {
+	uint32_t n;               // photon paths: Halton indices 0 .. n - 1
+	float inv_n;              // 1 / n (the diffuse worker's light-pick sample is i * (1 / n))
+	int caustic;              // 1: caustic map, 0: diffuse map
+	int max_bounces;          // bounces / caustic_depth
+	int radiance_points;      // diffuse map with final gather: keep 1 in 8 diffuse hits as radiance points
+	uint32_t n_lights;
+	const float *light_cdf;   // Pdf1D over the lights' totalEnergy().energy() (sample_pdf1d.h:59-94)
+	const float *light_pdf;
+	uint32_t seed;
+	float4 *pos, *dir, *col;  // deposited photons
+	uint32_t *count;          // [0] photons, [1] radiance points
+	uint32_t cap, rp_cap;
+	float4 *rp_pos, *rp_nrm, *rp_refl, *rp_transm;
+};
+
+// sample::sphere (include/sampler/sample.h:56-74), FAST_TRIG
+__device__ __forceinline__ void sample_sphere(float s1, float s2, float d[3])
+{
+	d[2] = 1.f - 2.f * s1;
+	float r = 1.f - d[2] * d[2];
+	if(r > 0.f)
+	{
+		r = sqrtf(r);
+		const float a = 6.28318530717958647692f * s2;
+		d[0] = gbrt::fast_cos(a) * r;
+		d[1] = gbrt::fast_sin(a) * r;
+	}
+	else d[0] = d[1] = 0.f;
+}
+
+// Warp-aggregated append: one atomic per warp and call site.
+__device__ __forceinline__ uint32_t append_slot(uint32_t *counter, bool want)
+{
+	const uint32_t m = __activemask();
+	const uint32_t b = __ballot_sync(m, want);
+	if(!b) return 0xFFFFFFFFu;
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t leader = __ffs(b) - 1u;
+	uint32_t base = 0;
+	if(lane == leader) base = atomicAdd(counter, static_cast<uint32_t>(__popc(b)));
+	base = __shfl_sync(m, base, leader);
+	return want ? base + __popc(b & ((1u << lane) - 1u)) : 0xFFFFFFFFu;
+}
+
+// Material::getReflectivity (src/material/material.cc:198-216): mean of
+// 16 sample colour x weight over fixed incoming directions.
+__device__ void reflectivity(const SceneDev &sc, const Surface &s, uint32_t flags, float out[3])
+{
+	out[0] = out[1] = out[2] = 0.f;
+	if(!(flags & (BF_TRANSMIT | BF_REFLECT) & s.m->flags)) return;
+	for(int i = 0; i < 16; ++i)
+	{
+		const float s1 = 0.03125f + 0.0625f * static_cast<float>(i);
+		const float s2 = gbrt::ri_vdc(static_cast<uint32_t>(i));
+		const float s3 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 2, static_cast<uint32_t>(i)));
+		const float s4 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 3, static_cast<uint32_t>(i)));
+		float wo[3], wi[3], col[3], w, pdf;
+		uint32_t sf;
+		cos_hemisphere(s.n, s.u, s.v, s1, s2, wo);
+		mat_sample(s, wo, s3, s4, flags, wi, col, w, pdf, sf);
+		for(int k = 0; k < 3; ++k) out[k] += col[k] * w;
+	}
+	for(int k = 0; k < 3; ++k) out[k] *= 0.0625f;
+}
+
+__global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJob J)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < J.n; i += gridDim.x * blockDim.x)
+	{
+		const float s1 = gbrt::ri_vdc(i);
+		const float s2 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 2, i));
+		const float s3 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 3, i));
+		const float s4 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 4, i));
+		const float s_l = J.caustic ? static_cast<float>(i) / static_cast<float>(J.n) : static_cast<float>(i) * J.inv_n;
+		uint32_t ln = 0;
+		if(s_l >= 1.f) ln = J.n_lights - 1u;
+		else if(s_l > 0.f) { while(ln + 1u < J.n_lights && J.light_cdf[ln] < s_l) ++ln; }   // std::lower_bound
+		const DevLight &L = sc.lights[ln];
+		float o[3], d[3], pcol[3], ipdf;
+		if(L.type == GBRT_LIGHT_POINT)
+		{
+			// PointLight::emitPhoton (light_point.cc:99-104)
+			for(int k = 0; k < 3; ++k) { o[k] = L.c[k]; pcol[k] = L.col[k]; }
+			sample_sphere(s1, s2, d);
+			ipdf = 4.f * kPi;
+		}
+		else
+		{
+			// AreaLight::emitPhoton (light_area.cc:126-133): cosine hemisphere
+			// around normal_ = -normal_flipped_ (not normalised), frame duv_
+			float nrm[3], u[3], v[3];
+			for(int k = 0; k < 3; ++k) { o[k] = L.c[k] + s3 * L.tx[k] + s4 * L.ty[k]; nrm[k] = -L.nflip[k]; u[k] = L.tx[k]; pcol[k] = L.col[k]; }
+			normalize3(u);
+			v[0] = nrm[1] * u[2] - nrm[2] * u[1]; v[1] = nrm[2] * u[0] - nrm[0] * u[2]; v[2] = nrm[0] * u[1] - nrm[1] * u[0];
+			cos_hemisphere(nrm, u, v, s1, s2, d);
+			ipdf = 1.f;                                // area_ (light_area.h:79)
+		}
+		const float f = static_cast<float>(J.n_lights) * ipdf / J.light_pdf[ln];
+		for(int k = 0; k < 3; ++k) pcol[k] *= f;
+		if(pcol[0] == 0.f && pcol[1] == 0.f && pcol[2] == 0.f) continue;
+		bool caustic = false, direct = true;
+		float tmin = kRayMinDist;
+		for(int nb = 0;; ++nb)
+		{
+			const gbrt::Hit h = gbrt::trace_ray<false>(sc.bv, o[0], o[1], o[2], tmin, d[0], d[1], d[2], -1.f);
+			if(h.prim < 0) break;
+			Surface s;
+			for(int k = 0; k < 3; ++k) s.p[k] = xa(o[k], xm(h.t, d[k]));
+			const float4 ng = __ldg(sc.prim_ng + h.prim);
+			s.ng[0] = ng.x; s.ng[1] = ng.y; s.ng[2] = ng.z;
+			s.n[0] = ng.x; s.n[1] = ng.y; s.n[2] = ng.z;
+			s.m = sc.mats + __float_as_uint(ng.w);
+			coords_system(s.n, s.u, s.v);
+			const float wi[3] = {-d[0], -d[1], -d[2]};
+			const uint32_t mf = s.m->flags;
+			const bool dep = J.caustic ? ((mf & (BF_DIFFUSE | BF_GLOSSY)) && caustic) : ((mf & BF_DIFFUSE) && !caustic);
+			const uint32_t slot = append_slot(J.count, dep);
+			if(dep && slot < J.cap)
+			{
+				J.pos[slot] = make_float4(s.p[0], s.p[1], s.p[2], 0.f);
+				J.dir[slot] = make_float4(wi[0], wi[1], wi[2], 0.f);
+				J.col[slot] = make_float4(pcol[0], pcol[1], pcol[2], 0.f);
+			}
+			if(J.radiance_points)
+			{
+				// 1 in 8 diffuse hits (the reference draws FastRandom < 0.125)
+				const bool rp = (mf & BF_DIFFUSE) && !caustic && rng01(i, static_cast<uint32_t>(nb), 0x7adu, J.seed) < 0.125f;
+				const uint32_t rs = append_slot(J.count + 1, rp);
+				if(rp && rs < J.rp_cap)
+				{
+					float nf[3], refl[3], tr[3];
+					face_forward(s, wi, nf);
+					reflectivity(sc, s, BF_DIFFUSE | BF_GLOSSY | BF_REFLECT, refl);
+					reflectivity(sc, s, BF_DIFFUSE | BF_GLOSSY | BF_TRANSMIT, tr);
+					J.rp_pos[rs] = make_float4(s.p[0], s.p[1], s.p[2], 0.f);
+					J.rp_nrm[rs] = make_float4(nf[0], nf[1], nf[2], 0.f);
+					J.rp_refl[rs] = make_float4(refl[0], refl[1], refl[2], 0.f);
+					J.rp_transm[rs] = make_float4(tr[0], tr[1], tr[2], 0.f);
+				}
+			}
+			if(nb == J.max_bounces) break;
+			// Material::scatterPhoton (src/material/material.cc:179-196)
+			const int d5 = 3 * nb + 5;
+			const float s5 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d5, i));
+			const float s6 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d5 + 1, i));
+			const float s7 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d5 + 2, i));
+			const uint32_t flags = J.caustic ? (BF_SPECULAR | BF_REFLECT | BF_TRANSMIT | BF_GLOSSY | BF_FILTER | BF_DISPERSIVE) : BF_ALL;
+			float wo[3], scol[3], w, pdf;
+			uint32_t sf;
+			mat_sample(s, wi, s5, s6, flags, wo, scol, w, pdf, sf);
+			if(!(pdf > 1.0e-6f)) break;
+			float cnew[3];
+			for(int k = 0; k < 3; ++k) cnew[k] = pcol[k] * 1.f * scol[k] * w;
+			const float new_max = fmaxf(cnew[0], fmaxf(cnew[1], cnew[2]));
+			const float old_max = fmaxf(pcol[0], fmaxf(pcol[1], pcol[2]));
+			const float prob = fminf(1.f, new_max / old_max);
+			if(!(s7 <= prob && prob > 1e-4f)) break;
+			for(int k = 0; k < 3; ++k) pcol[k] = cnew[k] / prob;
+			caustic = ((sf & (BF_GLOSSY | BF_SPECULAR | BF_DISPERSIVE)) && direct) ||
+			          ((sf & (BF_GLOSSY | BF_SPECULAR | BF_FILTER | BF_DISPERSIVE)) && caustic);
+			direct = (sf & BF_FILTER) && direct;
+			if(J.caustic && !(caustic || direct)) break;
+			for(int k = 0; k < 3; ++k) { o[k] = s.p[k]; d[k] = wo[k]; }
+			tmin = kRayMinDist;
+		}
+	}
+}
+
+// Material::eval with explicit BSDF flags, for the photon estimates.
+__device__ __forceinline__ void eval_flags(const Surface &s, const float wo[3], const float wl[3], uint32_t flags, float out[3])
+{
+	out[0] = out[1] = out[2] = 0.f;
+	if(s.m->type == GBRT_MAT_GLOSSY) { glossy_eval(s, wo, wl, flags, out); return; }
+	if(s.m->type == GBRT_MAT_SHINYDIFFUSE && (flags & BF_DIFFUSE)) mat_eval(s, wo, wl, out);
+}
+
+// Photon estimates at the roots of integrate() calls (vertex level 0 of a
+// wave), PhotonIntegrator::integrate (integrator_photon_mapping.cc:762-793)
+// and CausticPhotonIntegrator::estimateCausticPhotons (integrator_photon_caustic.cc:284-304).
+__global__ void __launch_bounds__(kThreads) k_pm_root(SceneDev sc, Params P, Work W, int cur, float *film, double *film64)
+{
+	const uint32_t n = W.count[cur];
+	for(uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+	{
+		const uint32_t path = W.q_path[cur][q];
+		const float4 h = W.hits[q];
+		const int32_t prim = __float_as_int(h.x);
+		if(prim < 0) continue;
+		if(W.p_si[path] % static_cast<uint32_t>(P.path_samples) != 0u) continue;
+		const float4 ng = __ldg(sc.prim_ng + prim);
+		Surface s;
+		s.m = sc.mats + __float_as_uint(ng.w);
+		if(!(s.m->flags & BF_DIFFUSE)) continue;
+		const float4 ra = W.q_ray[cur][2ull * q], rb = W.q_ray[cur][2ull * q + 1];
+		const float dir[3] = {rb.x, rb.y, rb.z};
+		s.p[0] = xa(ra.x, xm(h.y, dir[0])); s.p[1] = xa(ra.y, xm(h.y, dir[1])); s.p[2] = xa(ra.z, xm(h.y, dir[2]));
+		s.ng[0] = ng.x; s.ng[1] = ng.y; s.ng[2] = ng.z;
+		s.n[0] = ng.x; s.n[1] = ng.y; s.n[2] = ng.z;
+		coords_system(s.n, s.u, s.v);
+		const float wo[3] = {-dir[0], -dir[1], -dir[2]};
+		float est[3] = {0.f, 0.f, 0.f};
+		uint32_t idx[gbrt::kMaxGather];
+		float d2[gbrt::kMaxGather];
+		if(P.pm_diffuse && !P.pm_fg && P.g_diffuse.n)
+		{
+			float r2 = P.pm_diffuse_r2;
+			const int f = gbrt::knn_gather(P.g_diffuse, s.p, P.pm_diffuse_k, r2, idx, d2);
+			if(f > 0)
+			{
+				const float scale = 1.f / (P.pm_diffuse_paths * r2 * kPi);
+				for(int j = 0; j < f; ++j)
+				{
+					const float4 pd = __ldg(P.g_diffuse.dir + idx[j]), pc = __ldg(P.g_diffuse.col + idx[j]);
+					const float pdir[3] = {pd.x, pd.y, pd.z};
+					float sc3[3];
+					eval_flags(s, wo, pdir, BF_DIFFUSE, sc3);
+					est[0] += sc3[0] * scale * pc.x; est[1] += sc3[1] * scale * pc.y; est[2] += sc3[2] * scale * pc.z;
+				}
+			}
+		}
+		if(P.pm_caustics && P.g_caustic.n)
+		{
+			float r2 = P.pm_caustic_r2;
+			const int f = gbrt::knn_gather(P.g_caustic, s.p, P.pm_caustic_k, r2, idx, d2);
+			if(f > 0)
+			{
+				const float ir2 = 1.f / r2;
+				float sum[3] = {0.f, 0.f, 0.f};
+				for(int j = 0; j < f; ++j)
+				{
+					const float4 pd = __ldg(P.g_caustic.dir + idx[j]), pc = __ldg(P.g_caustic.col + idx[j]);
+					const float pdir[3] = {pd.x, pd.y, pd.z};
+					float sc3[3];
+					eval_flags(s, wo, pdir, BF_ALL, sc3);
+					// sample::kernel (include/sampler/sample.h:29-33)
+					const float t = 1.f - d2[j] * ir2;
+					const float kk = 3.f * ir2 * 0.318309886183790671538f * t * t;
+					sum[0] += sc3[0] * kk * pc.x; sum[1] += sc3[1] * kk * pc.y; sum[2] += sc3[2] * kk * pc.z;
+				}
+				const float inv = 1.f / P.pm_caustic_paths;
+				for(int c = 0; c < 3; ++c) est[c] += sum[c] * inv;
+			}
+		}
+		if(est[0] != 0.f || est[1] != 0.f || est[2] != 0.f)
+		{
+			const float4 t4 = W.p_thr[path];
+			film_add(film, film64, W.p_pixel[path], est[0] * t4.x, est[1] * t4.y, est[2] * t4.z);
+		}
+	}
+}
+
+// Radiance points, "remove too close radiance points" (integrator_photon_mapping.cc:527-540):
+// the reference keeps each point whose lookup still finds it unused, in its
+// (thread-scheduled) order, and drops the points within r^2 = 0.01 x
+// diffuse_radius whose normals face the same side.  Here the order is a
+// random priority and the result is that greedy's, computed in rounds: a
+// point joins when no undecided neighbour precedes it, and leaves when a
+// neighbour joined.  States: 0 undecided, 1 kept, 2 dropped.
+__device__ __forceinline__ bool rp_before(uint32_t a, uint32_t b, uint32_t seed)
+{
+	const uint32_t ha = hash32(a ^ seed), hb = hash32(b ^ seed);
+	return ha < hb || (ha == hb && a < b);
+}
+
+__global__ void k_rp_round(gbrt::PhotonGrid g, float r2, uint32_t seed, const uint8_t *__restrict__ st_in, uint8_t *__restrict__ st_out,
+                           uint32_t *__restrict__ undecided)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x)
+	{
+		uint8_t st = st_in[i];
+		if(st == 0)
+		{
+			const float4 pi = __ldg(g.pos + i), ni = __ldg(g.dir + i);
+			const float p[3] = {pi.x, pi.y, pi.z};
+			const uint32_t oi = __float_as_uint(pi.w);
+			bool drop = false, wait = false;
+			gbrt::grid_visit(g, p, [&](uint32_t first, uint32_t end) {
+				for(uint32_t j = first; j < end && !drop; ++j)
+				{
+					if(j == i) continue;
+					const uint8_t sj = st_in[j];
+					if(sj == 2) continue;
+					const float4 pj = __ldg(g.pos + j);
+					const float vx = pj.x - p[0], vy = pj.y - p[1], vz = pj.z - p[2];
+					if(!(vx * vx + vy * vy + vz * vz < r2)) continue;
+					const float4 nj = __ldg(g.dir + j);
+					if(!(nj.x * ni.x + nj.y * ni.y + nj.z * ni.z > 0.f)) continue;
+					if(sj == 1) drop = true;
+					else if(rp_before(__float_as_uint(pj.w), oi, seed)) wait = true;
+				}
+			});
+			st = drop ? 2 : (wait ? 0 : 1);
+			if(st == 0) atomicAdd(undecided, 1u);
+		}
+		st_out[i] = st;
+	}
+}
+
+// Pre-gathered radiance of the kept points (preGatherWorker, :98-146):
+// sum over the k nearest diffuse photons of (reflectance or transmittance by
+// the side the photon came from) x col / (paths x pi x r^2).
+__global__ void k_pregather(gbrt::PhotonGrid rp, const uint8_t *__restrict__ st, const float4 *__restrict__ refl, const float4 *__restrict__ transm,
+                            gbrt::PhotonGrid dm, float r2_0, int k, float inv_scale_paths,
+                            float4 *__restrict__ opos, float4 *__restrict__ odir, float4 *__restrict__ ocol, uint32_t *__restrict__ count)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < rp.n; i += gridDim.x * blockDim.x)
+	{
+		if(st[i] != 1) continue;
+		const float4 pi = __ldg(rp.pos + i), ni = __ldg(rp.dir + i);
+		const uint32_t oi = __float_as_uint(pi.w);
+		const float p[3] = {pi.x, pi.y, pi.z};
+		uint32_t idx[gbrt::kMaxGather];
+		float d2[gbrt::kMaxGather];
+		float r2 = r2_0;
+		const int f = dm.n ? gbrt::knn_gather(dm, p, k, r2, idx, d2) : 0;
+		float sum[3] = {0.f, 0.f, 0.f};
+		if(f > 0)
+		{
+			const float scale = inv_scale_paths / r2;
+			const float4 rf = refl[oi], tr = transm[oi];
+			for(int j = 0; j < f; ++j)
+			{
+				const float4 pd = __ldg(dm.dir + idx[j]), pc = __ldg(dm.col + idx[j]);
+				const bool front = ni.x * pd.x + ni.y * pd.y + ni.z * pd.z > 0.f;
+				const float4 a = front ? rf : tr;
+				sum[0] += a.x * scale * pc.x; sum[1] += a.y * scale * pc.y; sum[2] += a.z * scale * pc.z;
+			}
+		}
+		const uint32_t o = atomicAdd(count, 1u);
+		opos[o] = make_float4(p[0], p[1], p[2], 0.f);
+		odir[o] = make_float4(ni.x, ni.y, ni.z, 0.f);
+		ocol[o] = make_float4(sum[0], sum[1], sum[2], 0.f);
+	}
+}
+
+// ---- photon grid build ------------------------------------------------------
+
+__global__ void k_index_w(float4 *__restrict__ pos, uint32_t n)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) pos[i].w = __uint_as_float(i);
+}
+
+__global__ void k_grid_count(const float4 *__restrict__ pos, uint32_t n, gbrt::PhotonGrid g, uint32_t *__restrict__ key, uint32_t *__restrict__ cnt)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	{
+		const float4 q = pos[i];
+		const float p[3] = {q.x, q.y, q.z};
+		int c[3];
+		gbrt::grid_cell(g, p, c);
+		const uint32_t b = gbrt::grid_bucket(c[0], c[1], c[2], g.mask);
+		key[i] = b;
+		atomicAdd(cnt + b, 1u);
+	}
+}
+
+__global__ void k_grid_scatter(const float4 *__restrict__ pos, const float4 *__restrict__ dir, const float4 *__restrict__ col, uint32_t n,
+                               const uint32_t *__restrict__ key, const uint32_t *__restrict__ start, uint32_t *__restrict__ cursor,
+                               float4 *__restrict__ opos, float4 *__restrict__ odir, float4 *__restrict__ ocol)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	{
+		const uint32_t b = key[i];
+		const uint32_t j = start[b] + atomicAdd(cursor + b, 1u);
+		opos[j] = pos[i];
+		if(dir) odir[j] = dir[i];
+		if(col) ocol[j] = col[i];
+	}
+}
+
+// Exclusive scan in three passes: per-block scan of 4096 words, scan of the
+// block totals by one block, add-back.
+__global__ void __launch_bounds__(1024) k_scan_local(uint32_t *__restrict__ data, uint32_t n, uint32_t *__restrict__ totals)
+{
+	__shared__ uint32_t s[1024];
+	const uint32_t base = blockIdx.x * 4096u + threadIdx.x * 4u;
+	uint32_t v[4], sum = 0;
+	for(int k = 0; k < 4; ++k) { v[k] = base + k < n ? data[base + k] : 0u; sum += v[k]; }
+	s[threadIdx.x] = sum;
+	__syncthreads();
+	for(int off = 1; off < 1024; off <<= 1)
+	{
+		const uint32_t t = threadIdx.x >= static_cast<unsigned>(off) ? s[threadIdx.x - off] : 0u;
+		__syncthreads();
+		s[threadIdx.x] += t;
+		__syncthreads();
+	}
+	uint32_t run = s[threadIdx.x] - sum;
+	for(int k = 0; k < 4; ++k) { if(base + k < n) data[base + k] = run; run += v[k]; }
+	if(threadIdx.x == 1023) totals[blockIdx.x] = s[1023];
+}
+
+__global__ void __launch_bounds__(1024) k_scan_totals(uint32_t *__restrict__ t, uint32_t m)
+{
+	__shared__ uint32_t s[1024];
+	const uint32_t per = (m + 1023u) / 1024u, lo = threadIdx.x * per, hi = min(lo + per, m);
+	uint32_t sum = 0;
+	for(uint32_t i = lo; i < hi; ++i) sum += t[i];
+	s[threadIdx.x] = sum;
+	__syncthreads();
+	for(int off = 1; off < 1024; off <<= 1)
+	{
+		const uint32_t v = threadIdx.x >= static_cast<unsigned>(off) ? s[threadIdx.x - off] : 0u;
+		__syncthreads();
+		s[threadIdx.x] += v;
+		__syncthreads();
+	}
+	uint32_t run = s[threadIdx.x] - sum;
+	for(uint32_t i = lo; i < hi; ++i) { const uint32_t x = t[i]; t[i] = run; run += x; }
+}
+
+__global__ void k_scan_add(uint32_t *__restrict__ data, uint32_t n, const uint32_t *__restrict__ totals)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) data[i] += totals[i / 4096u];
+}
+
+// kNN over a grid of bare points (test entry): counts, final r^2, indices
+// into the caller's point order (kept in pos.w).
+__global__ void k_knn_test(gbrt::PhotonGrid g, const float *__restrict__ q, uint32_t m, int k, float r2,
+                           int32_t *__restrict__ cnt, float *__restrict__ r2_out, uint32_t *__restrict__ idx_out)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+	{
+		const float p[3] = {q[3ull * i], q[3ull * i + 1], q[3ull * i + 2]};
+		uint32_t idx[gbrt::kMaxGather];
+		float d2[gbrt::kMaxGather];
+		float r = r2;
+		const int f = gbrt::knn_gather(g, p, k, r, idx, d2);
+		cnt[i] = f;
+		r2_out[i] = r;
+		for(int j = 0; j < f; ++j) idx_out[static_cast<size_t>(i) * k + j] = __float_as_uint(__ldg(g.pos + idx[j]).w);
+	}
+}
+
 } // namespace
 
 struct gbrt_scene {
@@ -1567,6 +2118,7 @@ struct gbrt_scene {
 	size_t cap_paths = 0, cap_shadow = 0, cap_stride = 0;
 	void *work = nullptr;
 	Work w{};
+	std::vector<DevLight> lights_host;
 	// spawn buffers: one per ray level of the recursive split
 	float4 *spawn = nullptr;
 	uint32_t *spawn_count = nullptr;
@@ -1587,7 +2139,7 @@ int alloc_work(gbrt_scene *S, size_t paths, size_t shadow, size_t stride)
 	size_t off = 0;
 	auto carve = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
 	const size_t o_pix = carve(4 * paths), o_si = carve(4 * paths), o_st = carve(4 * paths), o_thr = carve(16 * paths);
-	const size_t o_task = carve(16 * paths);
+	const size_t o_task = carve(16 * paths), o_pm = carve(16 * paths);
 	const size_t o_qr0 = carve(32 * paths), o_qr1 = carve(32 * paths), o_qp0 = carve(4 * paths), o_qp1 = carve(4 * paths);
 	const size_t o_hit = carve(16 * paths);
 	const size_t o_sr = carve(32 * shadow), o_sc = carve(16 * shadow), o_sp = carve(4 * shadow), o_spath = carve(4 * shadow);
@@ -1610,6 +2162,7 @@ int alloc_work(gbrt_scene *S, size_t paths, size_t shadow, size_t stride)
 	w.p_state = reinterpret_cast<uint32_t *>(b + o_st);
 	w.p_thr = reinterpret_cast<float4 *>(b + o_thr);
 	w.p_task = reinterpret_cast<uint4 *>(b + o_task);
+	w.p_pm = reinterpret_cast<float4 *>(b + o_pm);
 	w.q_ray[0] = reinterpret_cast<float4 *>(b + o_qr0);
 	w.q_ray[1] = reinterpret_cast<float4 *>(b + o_qr1);
 	w.q_path[0] = reinterpret_cast<uint32_t *>(b + o_qp0);
@@ -1705,6 +2258,160 @@ unsigned grid_for(size_t n, int n_sm)
 	const size_t want = (n + kThreads - 1) / kThreads;
 	const size_t cap = static_cast<size_t>(n_sm > 0 ? n_sm : 148) * 16;
 	return static_cast<unsigned>(std::max<size_t>(1, std::min(want, cap)));
+}
+
+
+// ---- photon maps (host side) ------------------------------------------------
+
+struct DevBuf {
+	void *p = nullptr;
+	DevBuf() = default;
+	DevBuf(const DevBuf &) = delete;
+	DevBuf &operator=(const DevBuf &) = delete;
+	~DevBuf() { if(p) cudaFree(p); }
+	template<typename T> T *as() const { return static_cast<T *>(p); }
+	int alloc(size_t bytes)
+	{
+		if(p) cudaFree(p);
+		p = nullptr;
+		const cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 16));
+		if(e != cudaSuccess) { p = nullptr; return gbrt_set_error(GBRT_ERR_OOM, "photon map buffers (%zu bytes): %s", bytes, cudaGetErrorString(e)); }
+		return GBRT_OK;
+	}
+};
+
+struct GridStore {
+	DevBuf pos, dir, col, start, key, cursor, totals;
+	gbrt::PhotonGrid g{};
+};
+
+// Sorts n points (and their dir / col when given) into a hashed grid of cell
+// edge `cell` (>= every query radius made of it).
+int build_grid(const float4 *pos, const float4 *dir, const float4 *col, uint32_t n, float cell, const float lo[3], int n_sm,
+               GridStore &G, cudaStream_t s)
+{
+	uint32_t T = 1024;
+	while(T < n && T < (1u << 27)) T <<= 1;
+	const uint32_t words = T + 1, nblk = (words + 4095u) / 4096u;
+	if(int rc = G.pos.alloc(16ull * n)) return rc;
+	if(dir) if(int rc = G.dir.alloc(16ull * n)) return rc;
+	if(col) if(int rc = G.col.alloc(16ull * n)) return rc;
+	if(int rc = G.start.alloc(4ull * words)) return rc;
+	if(int rc = G.key.alloc(4ull * n)) return rc;
+	if(int rc = G.cursor.alloc(4ull * T)) return rc;
+	if(int rc = G.totals.alloc(4ull * nblk)) return rc;
+	GBRT_CK(cudaMemsetAsync(G.start.p, 0, 4ull * words, s));
+	GBRT_CK(cudaMemsetAsync(G.cursor.p, 0, 4ull * T, s));
+	gbrt::PhotonGrid &g = G.g;
+	g = gbrt::PhotonGrid{};
+	g.pos = G.pos.as<float4>();
+	g.dir = dir ? G.dir.as<float4>() : nullptr;
+	g.col = col ? G.col.as<float4>() : nullptr;
+	g.start = G.start.as<uint32_t>();
+	g.mask = T - 1u;
+	g.n = n;
+	for(int a = 0; a < 3; ++a) g.lo[a] = lo[a];
+	g.inv_cell = 1.f / cell;
+	if(n)
+		k_grid_count<<<grid_for(n, n_sm), kThreads, 0, s>>>(pos, n, g, G.key.as<uint32_t>(), G.start.as<uint32_t>());
+	k_scan_local<<<nblk, 1024, 0, s>>>(G.start.as<uint32_t>(), words, G.totals.as<uint32_t>());
+	k_scan_totals<<<1, 1024, 0, s>>>(G.totals.as<uint32_t>(), nblk);
+	k_scan_add<<<grid_for(words, n_sm), kThreads, 0, s>>>(G.start.as<uint32_t>(), words, G.totals.as<uint32_t>());
+	if(n)
+		k_grid_scatter<<<grid_for(n, n_sm), kThreads, 0, s>>>(pos, dir, col, n, G.key.as<uint32_t>(), G.start.as<uint32_t>(),
+		                                                      G.cursor.as<uint32_t>(), G.pos.as<float4>(), G.dir.as<float4>(), G.col.as<float4>());
+	GBRT_CK(cudaGetLastError());
+	return GBRT_OK;
+}
+
+// Pdf1D over the lights' totalEnergy().energy() (sample_pdf1d.h:59-80):
+// cdf and pdf = function x inv_integral, in the reference's float/double mix.
+void light_pdf_tables(const std::vector<DevLight> &ls, std::vector<float> &cdf, std::vector<float> &pdf)
+{
+	const size_t n = ls.size();
+	std::vector<float> fn(n);
+	for(size_t i = 0; i < n; ++i)
+	{
+		const DevLight &L = ls[i];
+		float e[3];
+		for(int k = 0; k < 3; ++k) e[k] = L.type == GBRT_LIGHT_POINT ? L.col[k] * 4.0f * 3.14159265358979323846f : L.col[k] * 1.f;
+		fn[i] = (e[0] + e[1] + e[2]) * 0.333333f;      // Rgb::energy (color.h:55)
+	}
+	cdf.assign(n, 0.f);
+	pdf.assign(n, 0.f);
+	const double delta = 1.0 / static_cast<double>(n);
+	double c = 0.0;
+	for(size_t i = 0; i < n; ++i) { c += static_cast<double>(fn[i]) * delta; cdf[i] = static_cast<float>(c); }
+	const float integral = static_cast<float>(c);
+	for(auto &x : cdf) x /= integral;
+	const float inv = 1.f / integral;
+	for(size_t i = 0; i < n; ++i) pdf[i] = fn[i] * inv;
+}
+
+struct ShotMap {
+	DevBuf pos, dir, col, count, rp_pos, rp_nrm, rp_refl, rp_transm;
+	uint32_t n = 0, paths = 0, n_rp = 0;
+};
+
+// One photon map: shoots n photon paths, keeps the deposits (and, for the
+// diffuse map with final gather, the radiance points).
+int shoot_map(gbrt_scene *S, const SceneDev &sc, bool caustic, uint32_t n, int max_bounces, bool radiance_points, uint32_t seed,
+              ShotMap &M, cudaStream_t s)
+{
+	M.paths = n;
+	M.n = M.n_rp = 0;
+	if(n == 0 || S->n_lights == 0) return GBRT_OK;
+	std::vector<float> cdf, pdf;
+	light_pdf_tables(S->lights_host, cdf, pdf);
+	DevBuf dcdf, dpdf;
+	if(int rc = dcdf.alloc(4 * cdf.size())) return rc;
+	if(int rc = dpdf.alloc(4 * pdf.size())) return rc;
+	GBRT_CK(cudaMemcpyAsync(dcdf.p, cdf.data(), 4 * cdf.size(), cudaMemcpyHostToDevice, s));
+	GBRT_CK(cudaMemcpyAsync(dpdf.p, pdf.data(), 4 * pdf.size(), cudaMemcpyHostToDevice, s));
+	const uint64_t cap64 = static_cast<uint64_t>(n) * static_cast<uint64_t>(max_bounces + 1);
+	if(cap64 >= (1ull << 31)) return gbrt_set_error(GBRT_ERR_CAPACITY, "photon map: %u paths x %d bounces exceed 2^31 photons", n, max_bounces + 1);
+	const uint32_t cap = static_cast<uint32_t>(cap64);
+	const uint32_t rp_cap = radiance_points ? cap / 4u + 4096u : 0u;
+	if(int rc = M.pos.alloc(16ull * cap)) return rc;
+	if(int rc = M.dir.alloc(16ull * cap)) return rc;
+	if(int rc = M.col.alloc(16ull * cap)) return rc;
+	if(int rc = M.count.alloc(8)) return rc;
+	if(radiance_points)
+	{
+		if(int rc = M.rp_pos.alloc(16ull * rp_cap)) return rc;
+		if(int rc = M.rp_nrm.alloc(16ull * rp_cap)) return rc;
+		if(int rc = M.rp_refl.alloc(16ull * rp_cap)) return rc;
+		if(int rc = M.rp_transm.alloc(16ull * rp_cap)) return rc;
+	}
+	GBRT_CK(cudaMemsetAsync(M.count.p, 0, 8, s));
+	PhotonJob J{};
+	J.n = n;
+	J.inv_n = 1.f / static_cast<float>(n);
+	J.caustic = caustic ? 1 : 0;
+	J.max_bounces = max_bounces;
+	J.radiance_points = radiance_points ? 1 : 0;
+	J.n_lights = S->n_lights;
+	J.light_cdf = dcdf.as<float>();
+	J.light_pdf = dpdf.as<float>();
+	J.seed = seed;
+	J.pos = M.pos.as<float4>(); J.dir = M.dir.as<float4>(); J.col = M.col.as<float4>();
+	J.count = M.count.as<uint32_t>();
+	J.cap = cap; J.rp_cap = rp_cap;
+	J.rp_pos = M.rp_pos.as<float4>(); J.rp_nrm = M.rp_nrm.as<float4>(); J.rp_refl = M.rp_refl.as<float4>(); J.rp_transm = M.rp_transm.as<float4>();
+	k_photon_shoot<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, J);
+	GBRT_CK(cudaGetLastError());
+	uint32_t cnt[2];
+	GBRT_CK(cudaMemcpyAsync(cnt, M.count.p, 8, cudaMemcpyDeviceToHost, s));
+	GBRT_CK(cudaStreamSynchronize(s));
+	if(cnt[0] > cap || cnt[1] > rp_cap) return gbrt_set_error(GBRT_ERR_CAPACITY, "photon map: %u photons / %u radiance points overflow %u / %u", cnt[0], cnt[1], cap, rp_cap);
+	M.n = cnt[0];
+	M.n_rp = cnt[1];
+	return GBRT_OK;
+}
+
+SceneDev scene_dev(const gbrt_scene *S)
+{
+	return SceneDev{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv}};
 }
 
 } // namespace
@@ -1833,6 +2540,7 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 	}
 	gbrt_scene *S = new gbrt_scene();
 	S->bvh = bvh;
+	S->lights_host = ls;
 	for(const DevMaterial &d : mats)
 	{
 		if((d.flags & BF_GLOSSY) && (d.flags & BF_REFLECT)) { S->split_glossy = true; if(d.flags & BF_TRANSMIT) S->split_glossy_transmit = true; }
@@ -1875,16 +2583,25 @@ int gbrt_scene_destroy(gbrt_scene *S)
 	return GBRT_OK;
 }
 
-int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, float *film_dev, double *film64_dev,
-                   gbrt_pt_stats *stats, void *stream)
+// The wavefront render of gbrt_pt_render / gbrt_pm_render (scene lock held).
+// pm: photonmapping setup (the PM fields of Params and its photon grids), or
+// NULL for pathtracing.
+static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params &pp_in, const Params *pm, float *film_dev,
+                         double *film64_dev, gbrt_pt_stats *stats, cudaStream_t s)
 {
-	if(!S || !camera || !params) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: NULL argument");
-	if(!film_dev && !film64_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: no film buffer");
-	const gbrt_pt_params &pp = *params;
+	gbrt_pt_params pp = pp_in;
+	if(pm)
+	{
+		// camera sample = one integrate(); with final gathering, fg_samples gather
+		// paths of fg_bounces + 1 vertices each (path_samples / bounces slots)
+		pp.path_samples = pm->pm_fg ? pm->path_samples : 1;
+		pp.bounces = pm->pm_fg ? pm->pm_fg_bounces + 1 : 0;
+		pp.guide = nullptr;
+		pp.guide_alpha = 0.f;
+		pp.guide_train_steps = 0;
+	}
 	if(camera->resx <= 0 || camera->resy <= 0 || pp.spp <= 0 || pp.path_samples <= 0 || pp.bounces < 0 || pp.path_samples > 64)
-		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: bad resolution or sampling parameters");
-	cudaStream_t s = static_cast<cudaStream_t>(stream);
-	std::lock_guard<std::mutex> lock(S->mu);
+		return gbrt_set_error(GBRT_ERR_INVALID, "render: bad resolution or sampling parameters");
 	const uint64_t total = static_cast<uint64_t>(camera->resx) * camera->resy * pp.spp * pp.path_samples;
 	if(total >= (1ull << 32)) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_pt_render: %llu paths exceed 2^32", static_cast<unsigned long long>(total));
 	gbrt_guide *guide = pp.guide;
@@ -1920,6 +2637,14 @@ int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 	Params P{};
 	P.spp = pp.spp; P.path_samples = pp.path_samples; P.bounces = pp.bounces; P.rr_min = pp.russian_roulette_min_bounces;
 	P.raydepth = raydepth;
+	if(pm)
+	{
+		P.pm = 1; P.pm_fg = pm->pm_fg; P.pm_fg_bounces = pm->pm_fg_bounces; P.pm_gather_dist = pm->pm_gather_dist;
+		P.pm_diffuse = pm->pm_diffuse; P.pm_caustics = pm->pm_caustics; P.pm_diffuse_r2 = pm->pm_diffuse_r2; P.pm_diffuse_k = pm->pm_diffuse_k;
+		P.pm_caustic_r2 = pm->pm_caustic_r2; P.pm_caustic_k = pm->pm_caustic_k; P.pm_diffuse_paths = pm->pm_diffuse_paths;
+		P.pm_caustic_paths = pm->pm_caustic_paths; P.pm_lookup_r2 = pm->pm_lookup_r2;
+		P.g_diffuse = pm->g_diffuse; P.g_caustic = pm->g_caustic; P.g_radiance = pm->g_radiance;
+	}
 	P.base_offset = pp.base_sampling_offset; P.seed = pp.seed;
 	P.d1 = 1.f / static_cast<float>(pp.spp);
 	P.n_lights = S->n_lights;
@@ -1951,6 +2676,8 @@ int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 			Pw.record = (camera_wave && record && (pp.guide_max_vertex == 0 || vtx < static_cast<int>(pp.guide_max_vertex))) ? 1 : 0;
 			k_reset<<<1, 1, 0, s>>>(Ww.count, cur ^ 1);
 			k_extend<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc.bv, Ww.q_ray[cur], Ww.count + cur, Ww.hits, level_guided ? Ww.hitpos : nullptr);
+			if(vtx == 0 && Pw.pm && (Pw.pm_caustics || (Pw.pm_diffuse && !Pw.pm_fg)))
+				k_pm_root<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, film, film64_dev);
 			if(level_guided)
 				if(int rc = gbrt_guide_eval_queue(guide, Ww.hitpos, n, Ww.count + cur, Ww.lobes, s)) return rc;
 			k_shade<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, camera->resx, static_cast<uint32_t>(shadow_cap), film, film64_dev);
@@ -2053,9 +2780,19 @@ int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 	return GBRT_OK;
 }
 
-int gbrt_pt_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, float *image_out, gbrt_pt_stats *stats)
+int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, float *film_dev, double *film64_dev,
+                   gbrt_pt_stats *stats, void *stream)
 {
-	if(!S || !camera || !params || !image_out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_host: NULL argument");
+	if(!S || !camera || !params) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: NULL argument");
+	if(!film_dev && !film64_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: no film buffer");
+	std::lock_guard<std::mutex> lock(S->mu);
+	return render_locked(S, camera, *params, nullptr, film_dev, film64_dev, stats, static_cast<cudaStream_t>(stream));
+}
+
+// Device film around a render call, per-pixel means copied to the host.
+static int render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
+                       float *image_out, gbrt_pt_stats *stats)
+{
 	const size_t n = 3ull * camera->resx * camera->resy;
 	const bool fp64 = (params->flags & GBRT_PT_FP64_FILM) != 0;
 	void *sum = nullptr, *mean = nullptr;
@@ -2064,7 +2801,9 @@ int gbrt_pt_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbr
 	if(e != cudaSuccess) { cudaFree(sum); return gbrt_set_error(GBRT_ERR_OOM, "gbrt_pt_render_host: %s", cudaGetErrorString(e)); }
 	int rc = GBRT_OK;
 	if((e = cudaMemset(sum, 0, n * (fp64 ? 8 : 4))) != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
-	if(!rc) rc = gbrt_pt_render(S, camera, params, fp64 ? nullptr : static_cast<float *>(sum), fp64 ? static_cast<double *>(sum) : nullptr, stats, nullptr);
+	if(!rc)
+		rc = pm ? gbrt_pm_render(S, camera, params, pm, fp64 ? nullptr : static_cast<float *>(sum), fp64 ? static_cast<double *>(sum) : nullptr, stats, nullptr)
+		        : gbrt_pt_render(S, camera, params, fp64 ? nullptr : static_cast<float *>(sum), fp64 ? static_cast<double *>(sum) : nullptr, stats, nullptr);
 	if(!rc)
 	{
 		k_mean<<<grid_for(n, S->n_sm), kThreads>>>(fp64 ? nullptr : static_cast<float *>(sum), fp64 ? static_cast<double *>(sum) : nullptr,
@@ -2074,6 +2813,19 @@ int gbrt_pt_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbr
 	cudaFree(sum);
 	cudaFree(mean);
 	return rc;
+}
+
+int gbrt_pt_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, float *image_out, gbrt_pt_stats *stats)
+{
+	if(!S || !camera || !params || !image_out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_host: NULL argument");
+	return render_host(S, camera, params, nullptr, image_out, stats);
+}
+
+int gbrt_pm_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
+                        float *image_out, gbrt_pt_stats *stats)
+{
+	if(!S || !camera || !params || !pm || !image_out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pm_render_host: NULL argument");
+	return render_host(S, camera, params, pm, image_out, stats);
 }
 
 // Diagnostics: evaluates one sampling primitive on n inputs, on the device
@@ -2112,6 +2864,188 @@ int gbrt_sampler_eval(int kind, int dim, const uint32_t *input, uint32_t n, doub
 	}
 	if(e != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "gbrt_sampler_eval: %s", cudaGetErrorString(e));
 	for(void *p : {d_perm, d_off, d_base, d_inv, d_in, d_out}) if(p) cudaFree(p);
+	return rc;
+}
+
+int gbrt_pm_default_params(gbrt_pm_params *p)
+{
+	if(!p) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pm_default_params: NULL");
+	// PhotonIntegrator / CausticPhotonIntegrator parameter defaults
+	// (integrator_photon_mapping.h:65-74, integrator_photon_caustic.h:44-49)
+	p->diffuse_photons = 100000;
+	p->caustic_photons = 500000;
+	p->diffuse_radius = 0.1f;
+	p->diffuse_search = 50;
+	p->caustic_radius = 0.25f;
+	p->caustic_mix = 50;
+	p->caustic_depth = 10;
+	p->bounces = 3;
+	p->caustics = 0;
+	p->diffuse = 1;
+	p->final_gather = 1;
+	p->fg_samples = 32;
+	p->fg_bounces = 2;
+	p->fg_min_pathlen = -1.f;
+	return GBRT_OK;
+}
+
+int gbrt_pm_photons(gbrt_scene *S, const gbrt_pm_params *pm, int which, float *out, uint32_t cap, uint32_t *n_photons, uint32_t *n_paths)
+{
+	if(!S || !pm || (which != 0 && which != 1)) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pm_photons: bad argument");
+	std::lock_guard<std::mutex> lock(S->mu);
+	const SceneDev sc = scene_dev(S);
+	ShotMap M;
+	const bool caustic = which == 1;
+	if(int rc = shoot_map(S, sc, caustic, static_cast<uint32_t>(std::max(0, caustic ? pm->caustic_photons : pm->diffuse_photons)),
+	                      caustic ? pm->caustic_depth : pm->bounces, false, 1u, M, nullptr)) return rc;
+	if(n_photons) *n_photons = M.n;
+	if(n_paths) *n_paths = M.paths;
+	if(out && M.n)
+	{
+		if(cap < M.n) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_pm_photons: %u photons, room for %u", M.n, cap);
+		std::vector<float4> p(M.n), d(M.n), c(M.n);
+		GBRT_CK(cudaMemcpy(p.data(), M.pos.p, 16ull * M.n, cudaMemcpyDeviceToHost));
+		GBRT_CK(cudaMemcpy(d.data(), M.dir.p, 16ull * M.n, cudaMemcpyDeviceToHost));
+		GBRT_CK(cudaMemcpy(c.data(), M.col.p, 16ull * M.n, cudaMemcpyDeviceToHost));
+		for(uint32_t i = 0; i < M.n; ++i)
+		{
+			float *o = out + 9ull * i;
+			o[0] = d[i].x; o[1] = d[i].y; o[2] = d[i].z;
+			o[3] = p[i].x; o[4] = p[i].y; o[5] = p[i].z;
+			o[6] = c[i].x; o[7] = c[i].y; o[8] = c[i].z;
+		}
+	}
+	return GBRT_OK;
+}
+
+int gbrt_knn_gather(const float *points, uint32_t n, const float *queries, uint32_t m, float cell, int k, float r2,
+                    int32_t *count_out, float *r2_out, uint32_t *idx_out)
+{
+	if((n && !points) || (m && (!queries || !count_out || !r2_out || !idx_out)) || !(cell > 0.f) || k < 1 || k > gbrt::kMaxGather)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_knn_gather: bad argument (k in [1, %d], cell > 0)", gbrt::kMaxGather);
+	if(!(cell * cell >= r2)) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_knn_gather: cell edge %g below the search radius", cell);
+	int dev = 0, n_sm = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+	std::vector<float4> p4(n);
+	float lo[3] = {0.f, 0.f, 0.f};
+	for(uint32_t i = 0; i < n; ++i)
+	{
+		p4[i] = make_float4(points[3ull * i], points[3ull * i + 1], points[3ull * i + 2], 0.f);
+		for(int a = 0; a < 3; ++a) lo[a] = i ? std::min(lo[a], points[3ull * i + a]) : points[3ull * i + a];
+	}
+	DevBuf raw, q, cnt, rr, idx;
+	if(int rc = raw.alloc(16ull * n)) return rc;
+	if(int rc = q.alloc(12ull * m)) return rc;
+	if(int rc = cnt.alloc(4ull * m)) return rc;
+	if(int rc = rr.alloc(4ull * m)) return rc;
+	if(int rc = idx.alloc(4ull * m * k)) return rc;
+	GBRT_CK(cudaMemcpy(raw.p, p4.data(), 16ull * n, cudaMemcpyHostToDevice));
+	GBRT_CK(cudaMemcpy(q.p, queries, 12ull * m, cudaMemcpyHostToDevice));
+	GBRT_CK(cudaMemset(idx.p, 0xFF, 4ull * m * k));
+	if(n) k_index_w<<<grid_for(n, n_sm), kThreads>>>(raw.as<float4>(), n);
+	GridStore G;
+	if(int rc = build_grid(raw.as<float4>(), nullptr, nullptr, n, cell, lo, n_sm, G, nullptr)) return rc;
+	if(m) k_knn_test<<<grid_for(m, n_sm), kThreads>>>(G.g, q.as<float>(), m, k, r2, cnt.as<int32_t>(), rr.as<float>(), idx.as<uint32_t>());
+	GBRT_CK(cudaGetLastError());
+	GBRT_CK(cudaMemcpy(count_out, cnt.p, 4ull * m, cudaMemcpyDeviceToHost));
+	GBRT_CK(cudaMemcpy(r2_out, rr.p, 4ull * m, cudaMemcpyDeviceToHost));
+	GBRT_CK(cudaMemcpy(idx_out, idx.p, 4ull * m * k, cudaMemcpyDeviceToHost));
+	return GBRT_OK;
+}
+
+int gbrt_pm_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
+                   float *film_dev, double *film64_dev, gbrt_pt_stats *stats, void *stream)
+{
+	if(!S || !camera || !params || !pm) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pm_render: NULL argument");
+	if(!film_dev && !film64_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pm_render: no film buffer");
+	const gbrt_pm_params &q = *pm;
+	if(q.diffuse_search < 1 || q.diffuse_search > gbrt::kMaxGather || q.caustic_mix < 1 || q.caustic_mix > gbrt::kMaxGather ||
+	   !(q.diffuse_radius > 0.f) || !(q.caustic_radius > 0.f) || q.fg_samples < 1 || q.fg_samples > 64 || q.fg_bounces < 0 ||
+	   q.bounces < 0 || q.caustic_depth < 0 || q.diffuse_photons < 0 || q.caustic_photons < 0)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pm_render: bad photon-mapping parameters (searches in [1, %d], fg_samples in [1, 64])", gbrt::kMaxGather);
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	std::lock_guard<std::mutex> lock(S->mu);
+	const SceneDev sc = scene_dev(S);
+	float bound[6];
+	if(int rc = gbrt_bvh_get_bound(S->bvh, bound)) return rc;
+	const float lo[3] = {bound[0], bound[1], bound[2]};
+	const bool fg = q.final_gather && q.diffuse;
+	const float dr = q.diffuse_radius;
+	Params M{};
+	M.pm = 1;
+	M.pm_fg = fg ? 1 : 0;
+	M.path_samples = q.fg_samples;
+	M.pm_fg_bounces = q.fg_bounces;
+	M.pm_gather_dist = q.fg_min_pathlen < 0.f ? dr : q.fg_min_pathlen;
+	M.pm_diffuse = q.diffuse ? 1 : 0;
+	M.pm_caustics = q.caustics ? 1 : 0;
+	M.pm_diffuse_r2 = dr;
+	M.pm_diffuse_k = q.diffuse_search;
+	M.pm_caustic_r2 = q.caustic_radius * q.caustic_radius;
+	M.pm_caustic_k = q.caustic_mix;
+	M.pm_lookup_r2 = 4.f * dr * dr;
+	const uint32_t seed = params->seed * 0x9e3779b9u + params->base_sampling_offset;
+	ShotMap D, C;
+	GridStore GD, GC, GP, GR;
+	DevBuf st0, st1, und, rpos, rdir, rcol, rcnt;
+	if(q.diffuse)
+	{
+		if(int rc = shoot_map(S, sc, false, static_cast<uint32_t>(q.diffuse_photons), q.bounces, fg, seed, D, s)) return rc;
+		if(D.n < 50) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pm_render: too few diffuse photons (%u)", D.n);
+		M.pm_diffuse_paths = static_cast<float>(D.paths);
+		if(int rc = build_grid(D.pos.as<float4>(), D.dir.as<float4>(), D.col.as<float4>(), D.n, fg ? dr : std::sqrt(dr), lo, S->n_sm, GD, s)) return rc;
+		M.g_diffuse = GD.g;
+	}
+	if(q.caustics)
+	{
+		if(int rc = shoot_map(S, sc, true, static_cast<uint32_t>(q.caustic_photons), q.caustic_depth, false, seed, C, s)) return rc;
+		M.pm_caustic_paths = static_cast<float>(C.paths);
+		if(int rc = build_grid(C.pos.as<float4>(), C.dir.as<float4>(), C.col.as<float4>(), C.n, q.caustic_radius, lo, S->n_sm, GC, s)) return rc;
+		M.g_caustic = GC.g;
+	}
+	if(fg)
+	{
+		// radiance map: thin the radiance points, pre-gather their radiance,
+		// grid them for findNearest within 2 x diffuse_radius
+		const uint32_t n = D.n_rp;
+		const float r2c = 0.01f * dr;
+		if(n) k_index_w<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(D.rp_pos.as<float4>(), n);
+		if(int rc = build_grid(D.rp_pos.as<float4>(), D.rp_nrm.as<float4>(), nullptr, n, std::sqrt(r2c), lo, S->n_sm, GP, s)) return rc;
+		if(int rc = st0.alloc(n)) return rc;
+		if(int rc = st1.alloc(n)) return rc;
+		if(int rc = und.alloc(4)) return rc;
+		GBRT_CK(cudaMemsetAsync(st0.p, 0, n, s));
+		uint8_t *sa = st0.as<uint8_t>(), *sb = st1.as<uint8_t>();
+		for(int round = 0; n; ++round)
+		{
+			if(round == 4096) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pm_render: radiance point thinning did not settle");
+			GBRT_CK(cudaMemsetAsync(und.p, 0, 4, s));
+			k_rp_round<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(GP.g, r2c, seed, sa, sb, und.as<uint32_t>());
+			std::swap(sa, sb);
+			uint32_t left = 0;
+			GBRT_CK(cudaMemcpyAsync(&left, und.p, 4, cudaMemcpyDeviceToHost, s));
+			GBRT_CK(cudaStreamSynchronize(s));
+			if(!left) break;
+		}
+		if(int rc = rpos.alloc(16ull * n)) return rc;
+		if(int rc = rdir.alloc(16ull * n)) return rc;
+		if(int rc = rcol.alloc(16ull * n)) return rc;
+		if(int rc = rcnt.alloc(4)) return rc;
+		GBRT_CK(cudaMemsetAsync(rcnt.p, 0, 4, s));
+		const float inv_scale = 1.f / (static_cast<float>(D.paths) * 3.14159265358979323846f);
+		if(n)
+			k_pregather<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(GP.g, sa, D.rp_refl.as<float4>(), D.rp_transm.as<float4>(), GD.g, dr * dr,
+			                                                   q.diffuse_search, inv_scale, rpos.as<float4>(), rdir.as<float4>(), rcol.as<float4>(),
+			                                                   rcnt.as<uint32_t>());
+		uint32_t nr = 0;
+		GBRT_CK(cudaMemcpyAsync(&nr, rcnt.p, 4, cudaMemcpyDeviceToHost, s));
+		GBRT_CK(cudaStreamSynchronize(s));
+		if(int rc = build_grid(rpos.as<float4>(), rdir.as<float4>(), rcol.as<float4>(), nr, 2.f * dr, lo, S->n_sm, GR, s)) return rc;
+		M.g_radiance = GR.g;
+	}
+	const int rc = render_locked(S, camera, *params, &M, film_dev, film64_dev, stats, s);
+	cudaStreamSynchronize(s);      // the photon buffers are freed on return
 	return rc;
 }
 

@@ -60,6 +60,32 @@ class PtParams(ctypes.Structure):
                 ("guide_batch", ctypes.c_uint32), ("guide_max_vertex", ctypes.c_uint32), ("raydepth", ctypes.c_int32)]
 
 
+class PmParams(ctypes.Structure):
+    _fields_ = [("diffuse_photons", ctypes.c_int32), ("caustic_photons", ctypes.c_int32), ("diffuse_radius", ctypes.c_float),
+                ("diffuse_search", ctypes.c_int32), ("caustic_radius", ctypes.c_float), ("caustic_mix", ctypes.c_int32),
+                ("caustic_depth", ctypes.c_int32), ("bounces", ctypes.c_int32), ("caustics", ctypes.c_int32),
+                ("diffuse", ctypes.c_int32), ("final_gather", ctypes.c_int32), ("fg_samples", ctypes.c_int32),
+                ("fg_bounces", ctypes.c_int32), ("fg_min_pathlen", ctypes.c_float)]
+
+
+# photonmapping parameter names of the reference -> PmParams fields
+PM_KEYS = {"diffuse_photons": "diffuse_photons", "caustic_photons": "caustic_photons", "diffuse_radius": "diffuse_radius",
+           "diffuse_search": "diffuse_search", "caustic_radius": "caustic_radius", "caustic_mix": "caustic_mix",
+           "caustic_depth": "caustic_depth", "bounces": "bounces", "caustics": "caustics", "diffuse": "diffuse",
+           "finalGather": "final_gather", "fg_samples": "fg_samples", "fg_bounces": "fg_bounces",
+           "fg_min_pathlen": "fg_min_pathlen"}
+
+
+def pm_params(integrator):
+    """PmParams from a photonmapping integrator dict (reference names)."""
+    p = PmParams()
+    check(load().gbrt_pm_default_params(ctypes.byref(p)))
+    for k, v in integrator.items():
+        if k in PM_KEYS:
+            setattr(p, PM_KEYS[k], type(getattr(p, PM_KEYS[k]))(v))
+    return p
+
+
 class PtStats(ctypes.Structure):
     _fields_ = [("camera_samples", ctypes.c_uint64), ("extension_rays", ctypes.c_uint64),
                 ("shadow_rays", ctypes.c_uint64), ("ms", ctypes.c_float)]
@@ -109,6 +135,11 @@ SIGNATURES = {
     "gbrt_guide_set_eval_mode": (_I, [_VP, ctypes.c_int]),
     "gbrt_guide_status": (_I, [_VP, ctypes.POINTER(ctypes.c_uint32)]),
     "gbrt_tc_selftest": (_I, [_VP, _VP, _U32, _U32, _VP]),
+    "gbrt_pm_default_params": (_I, [_VP]),
+    "gbrt_pm_render": (_I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "gbrt_pm_render_host": (_I, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    "gbrt_pm_photons": (_I, [_VP, _VP, ctypes.c_int, _VP, _U32, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]),
+    "gbrt_knn_gather": (_I, [_VP, _U32, _VP, _U32, ctypes.c_float, ctypes.c_int, ctypes.c_float, _VP, _VP, _VP]),
     "gbrt_pt_render": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP, _VP,
                             ctypes.POINTER(PtStats), _VP]),
     "gbrt_pt_render_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP,
@@ -308,6 +339,21 @@ class Renderer:
         except Exception:
             pass
 
+    @property
+    def is_pm(self):
+        return self.scene["integrator"].get("type") == "photonmapping"
+
+    def photons(self, which):
+        """One photon map of this scene's photonmapping parameters (which =
+        "diffuse" or "caustic"): (photons [n, 9] = dir, pos, col; n_paths)."""
+        pm = pm_params(self.scene["integrator"])
+        w = {"diffuse": 0, "caustic": 1}[which]
+        n, paths = ctypes.c_uint32(), ctypes.c_uint32()
+        check(load().gbrt_pm_photons(self._h, ctypes.byref(pm), w, None, 0, ctypes.byref(n), ctypes.byref(paths)))
+        out = np.empty((max(1, n.value), 9), np.float32)
+        check(load().gbrt_pm_photons(self._h, ctypes.byref(pm), w, _ptr(out), len(out), ctypes.byref(n), ctypes.byref(paths)))
+        return out[:n.value], paths.value
+
     def make_guide(self, **kw):
         """A guiding network over this scene's tree bound."""
         return Guide(self.bvh.bound(), **kw)
@@ -336,7 +382,12 @@ class Renderer:
         p = self.params(spp, base_offset, seed, fp64, 0, guide, alpha, train_steps, batch, max_vertex)
         img = np.empty((cam.resy, cam.resx, 3), np.float32)
         st = PtStats()
-        check(load().gbrt_pt_render_host(self._h, ctypes.byref(cam), ctypes.byref(p), _ptr(img), ctypes.byref(st)))
+        if self.is_pm:
+            pm = pm_params(self.scene["integrator"])
+            check(load().gbrt_pm_render_host(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.byref(pm), _ptr(img),
+                                             ctypes.byref(st)))
+        else:
+            check(load().gbrt_pt_render_host(self._h, ctypes.byref(cam), ctypes.byref(p), _ptr(img), ctypes.byref(st)))
         return img, {"camera_samples": st.camera_samples, "extension_rays": st.extension_rays,
                      "shadow_rays": st.shadow_rays, "ms": st.ms}
 
@@ -349,9 +400,15 @@ class Renderer:
         if radiance_target:
             p.flags |= PT_GUIDE_RADIANCE
         st = PtStats()
-        check(load().gbrt_pt_render(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.c_void_p(film_ptr or None),
-                                    ctypes.c_void_p(film64_ptr or None), ctypes.byref(st) if stats else None,
-                                    ctypes.c_void_p(stream)))
+        if self.is_pm:
+            pm = pm_params(self.scene["integrator"])
+            check(load().gbrt_pm_render(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.byref(pm),
+                                        ctypes.c_void_p(film_ptr or None), ctypes.c_void_p(film64_ptr or None),
+                                        ctypes.byref(st) if stats else None, ctypes.c_void_p(stream)))
+        else:
+            check(load().gbrt_pt_render(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.c_void_p(film_ptr or None),
+                                        ctypes.c_void_p(film64_ptr or None), ctypes.byref(st) if stats else None,
+                                        ctypes.c_void_p(stream)))
         if stats:
             return {"camera_samples": st.camera_samples, "extension_rays": st.extension_rays,
                     "shadow_rays": st.shadow_rays, "ms": st.ms}
@@ -459,3 +516,16 @@ def guide_forward_host(bound, mlp, table, pos, log2_table=19, base_resolution=16
     out = np.empty((len(x), 40), np.float32)
     check(load().gbrt_guide_forward_host(b, ctypes.byref(p), _ptr(m), _ptr(t), _ptr(x), len(x), _ptr(out)))
     return out
+
+
+def knn_gather(points, queries, cell, k, r2):
+    """PhotonMap::gather semantics on the device grid: (count [m], final r2
+    [m], indices [m, k] of the found points, unordered; -1 past count)."""
+    P = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    Q = np.ascontiguousarray(queries, np.float32).reshape(-1, 3)
+    m = len(Q)
+    cnt = np.empty(m, np.int32)
+    rr = np.empty(m, np.float32)
+    idx = np.full((m, k), 0xFFFFFFFF, np.uint32)
+    check(load().gbrt_knn_gather(_ptr(P), len(P), _ptr(Q), m, float(cell), int(k), float(r2), _ptr(cnt), _ptr(rr), _ptr(idx)))
+    return cnt, rr, idx.astype(np.int64) - np.where(idx == 0xFFFFFFFF, 1 << 32, 0)

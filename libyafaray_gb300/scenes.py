@@ -362,3 +362,52 @@ def indoor_scene(n_boxes=463, subdiv=6, res=(960, 540), seed=5, bounces=12, rr_m
               "resx": res[0], "resy": res[1], "focal": 1.0}
     integ = {"type": "pathtracing", "path_samples": 1, "bounces": bounces, "russian_roulette_min_bounces": rr_min}
     return {"materials": mats, "objects": objects, "lights": lights, "camera": camera, "integrator": integ}
+
+
+def caustic_scene(res=(1024, 1024), subdiv=7, diffuse_photons=10_000_000, caustic_photons=10_000_000, final_gather=True,
+                  fg_samples=32, radius=0.02, search=50, fg_bounces=2, bounces=3):
+    """Photon-mapping configuration: a glass icosphere (r 0.5, IOR 1.5,
+    20 * 4**subdiv triangles: 327,680 at subdiv 7) resting on a 4 x 4 m
+    shinydiffuse plane (albedo 0.8), lit by a pointlight at (1, 3, 1) of power
+    1000; `photonmapping` with caustics, diffuse_search = caustic_mix =
+    search, diffuse_radius = caustic_radius = radius, finalGather."""
+    mats = {"floor": ("shinydiffusemat", (0.8, 0.8, 0.8)), "glass": glass_material(1.5)}
+    plane = np.array([[-2, 0, -2], [2, 0, -2], [2, 0, 2], [-2, 0, 2]], np.float32)
+    objects = [{"name": "floor", "material": "floor", "vertices": plane,
+                "faces": np.array([[0, 2, 1, TRI], [0, 3, 2, TRI]], np.uint32)}]
+    v, f = icosphere((0.0, 0.5, 0.0), 0.5, subdiv)
+    objects.append({"name": "ball", "material": "glass", "vertices": v, "faces": f})
+    lights = [{"type": "pointlight", "from": (1.0, 3.0, 1.0), "color": (1.0, 1.0, 1.0), "power": 1000.0}]
+    rx, ry = (res, res) if isinstance(res, int) else res
+    camera = {"from": (0.0, 2.2, 3.6), "to": (0.0, 0.3, 0.0), "up": (0.0, 3.2, 3.6), "resx": rx, "resy": ry, "focal": 1.3737}
+    integ = {"type": "photonmapping", "diffuse_photons": int(diffuse_photons), "caustic_photons": int(caustic_photons),
+             "caustics": True, "diffuse_search": int(search), "caustic_mix": int(search), "diffuse_radius": float(radius),
+             "caustic_radius": float(radius), "finalGather": bool(final_gather), "fg_samples": int(fg_samples),
+             "fg_bounces": int(fg_bounces), "bounces": int(bounces), "threads_photons": 1}
+    return {"materials": mats, "objects": objects, "lights": lights, "camera": camera, "integrator": integ}
+
+
+def caustic_scene_small(final_gather):
+    """The photon-mapping configuration at test size: 1280-triangle glass
+    ball, 200k diffuse and 200k caustic photon paths, 48x48.  Without final
+    gather diffuse_radius = 0.01 (the reference takes it as the squared
+    radius); with it diffuse_radius = 0.05 and fg_samples 8."""
+    kw = dict(res=48, subdiv=3, diffuse_photons=200000, caustic_photons=200000, radius=0.05, search=50, bounces=3)
+    if final_gather:
+        return caustic_scene(final_gather=True, fg_samples=8, **kw)
+    sc = caustic_scene(final_gather=False, **kw)
+    sc["integrator"]["diffuse_radius"] = 0.01
+    return sc
+
+
+def cornell_pm_scene(res, final_gather, diffuse_photons=100000):
+    """The Cornell box rendered by `photonmapping` (no caustic map): direct
+    photon estimate with diffuse_radius 0.005 (the reference takes it as the
+    squared radius), or final gather with diffuse_radius 0.1, fg_samples 8,
+    fg_bounces 2; diffuse_search 50, photon bounces 3."""
+    sc = cornell_scene(res=res)
+    sc["integrator"] = {"type": "photonmapping", "diffuse_photons": int(diffuse_photons), "caustic_photons": 0,
+                        "caustics": False, "diffuse_search": 50, "diffuse_radius": 0.1 if final_gather else 0.005,
+                        "finalGather": bool(final_gather), "fg_samples": 8, "fg_bounces": 2, "bounces": 3,
+                        "threads_photons": 1}
+    return sc

@@ -187,3 +187,20 @@ def run_reference_render(scene, spp, batches, threads=-1):
     secs = np.frombuffer(raw[12:12 + 8 * K], np.float64).copy()
     rgb = np.frombuffer(raw[12 + 8 * K:], np.float32).reshape(K, H, W, 3).copy()
     return rgb, secs
+
+
+def run_reference_photons(scene):
+    """Diffuse and caustic photon maps of the reference's photonmapping
+    preprocess: [(photons [n, 9] = dir, pos, col; n_paths), (caustic ...)]."""
+    text = reference_scene_text(scene, 1, 1, 1)
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout, fph = os.path.join(d, "scene.txt"), os.path.join(d, "out.bin"), os.path.join(d, "ph.bin")
+        open(fin, "w").write(text)
+        subprocess.run([REF_RENDER, fin, fout, fph], check=True, stdout=subprocess.DEVNULL)
+        raw = open(fph, "rb").read()
+    out, o = [], 0
+    for _ in range(2):
+        n, paths = struct.unpack("<ii", raw[o:o + 8]); o += 8
+        ph = np.frombuffer(raw, np.float32, 9 * n, o).reshape(n, 9).copy(); o += 36 * n
+        out.append((ph, paths))
+    return out

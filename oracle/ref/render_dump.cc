@@ -19,14 +19,32 @@
 //   integrator TYPE key=value ...      (ints/floats/bools/strings by key)
 //   render SPP BATCHES THREADS
 // Output (binary): i32 K, H, W; f64 seconds[K]; f32 rgb[K][H][W][3]
+// Optional third argument (photonmapping only): after the first batch's
+// preprocess, the diffuse and caustic photon maps are written there:
+//   per map: i32 n_photons, i32 n_paths, f32 [n][9] (dir xyz, pos xyz, col rgb)
+// (the maps are private members of PhotonIntegrator, read by opening their
+// access for this file only).
 #include "yafaray_c_api.h"
+#include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <set>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
+#define private public
+#define protected public
+#include "integrator/surface/integrator_photon_mapping.h"
+#undef private
+#undef protected
 
 namespace {
 struct Film { int w = 0, h = 0; std::vector<float> rgb; };
@@ -54,7 +72,7 @@ void setTyped(yafaray_ParamMap *pm, const std::string &key, const std::string &v
 
 int main(int argc, char **argv)
 {
-	if(argc != 3) { fprintf(stderr, "usage: %s scene.txt out.bin\n", argv[0]); return 2; }
+	if(argc != 3 && argc != 4) { fprintf(stderr, "usage: %s scene.txt out.bin [photons.bin]\n", argv[0]); return 2; }
 	std::ifstream in(argv[1]);
 	if(!in) { perror("scene"); return 2; }
 	yafaray_Logger *logger = yafaray_createLogger("oracle", nullptr, nullptr, YAFARAY_DISPLAY_CONSOLE_HIDDEN);
@@ -210,6 +228,26 @@ int main(int argc, char **argv)
 		const auto t0 = std::chrono::steady_clock::now();
 		yafaray_preprocessScene(scene, rc, flags);
 		yafaray_preprocessSurfaceIntegrator(rm, integrator, rc, scene);
+		if(k == 0 && argc > 3)
+		{
+			auto *pmi = dynamic_cast<yafaray::PhotonIntegrator *>(reinterpret_cast<yafaray::SurfaceIntegrator *>(integrator));
+			if(!pmi) { fprintf(stderr, "photon dump needs the photonmapping integrator\n"); return 2; }
+			FILE *fp = fopen(argv[3], "wb");
+			if(!fp) { perror("photons"); return 2; }
+			for(const yafaray::PhotonMap *map : {pmi->diffuse_map_.get(), pmi->caustic_map_.get()})
+			{
+				const int hdr2[2] = {map->nPhotons(), map->nPaths()};
+				fwrite(hdr2, 4, 2, fp);
+				for(const auto &ph : map->photons_)
+				{
+					const float v[9] = {ph.dir_[yafaray::Axis::X], ph.dir_[yafaray::Axis::Y], ph.dir_[yafaray::Axis::Z],
+					                    ph.pos_[yafaray::Axis::X], ph.pos_[yafaray::Axis::Y], ph.pos_[yafaray::Axis::Z],
+					                    ph.col_.r_, ph.col_.g_, ph.col_.b_};
+					fwrite(v, 4, 9, fp);
+				}
+			}
+			fclose(fp);
+		}
 		yafaray_render(rc, rm, integrator, film);
 		secs.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
 		all.insert(all.end(), f.rgb.begin(), f.rgb.end());

@@ -85,6 +85,46 @@ def variant_golden(name, res=64, spp=16, batches=32, **kw):
     print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
 
 
+def pm_golden(spp=8, batches=16):
+    """photons_small.npz: diffuse and caustic photon maps of the reference
+    (threads_photons 1, so photon path i uses Halton index i) for a 20k-path
+    version of the scene; pm_*_render.npz: photonmapping renders."""
+    sc = scenes.caustic_scene(res=32, subdiv=3, diffuse_photons=20000, caustic_photons=20000, final_gather=False)
+    (d, dp), (c, cp) = orc.run_reference_photons(sc)
+    np.savez_compressed(os.path.join(OUT, "photons_small.npz"), diffuse=d, diffuse_paths=np.int32(dp), caustic=c,
+                        caustic_paths=np.int32(cp))
+    print(f"photons_small.npz: {len(d)} diffuse / {len(c)} caustic photons of {dp} / {cp} paths")
+    # area light (Cornell box): 5k diffuse photon paths
+    (d, dp), _ = orc.run_reference_photons(scenes.cornell_pm_scene(16, False, diffuse_photons=5000))
+    np.savez_compressed(os.path.join(OUT, "photons_cornell.npz"), diffuse=d, diffuse_paths=np.int32(dp))
+    print(f"photons_cornell.npz: {len(d)} diffuse photons of {dp} paths")
+    for fg in (False, True):
+        sc = scenes.caustic_scene_small(fg)
+        rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
+        mean = rgb.mean(0)
+        se = rgb.std(0, ddof=1) / np.sqrt(batches)
+        name = f"pm_{'fg' if fg else 'direct'}_48_render.npz"
+        np.savez_compressed(os.path.join(OUT, name), mean=mean.astype(np.float32), se=se.astype(np.float32),
+                            batches=np.int32(batches), spp=np.int32(spp), seconds=secs)
+        print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
+
+
+def cornell_pm_golden(spp=8, batches=24):
+    """cornell_pm_{direct,fg}_48_render.npz: the Cornell box (area light) with
+    photonmapping: 100k diffuse photon paths, diffuse_search 50; direct
+    estimate with diffuse_radius 0.005 (taken as r^2), or final gather with
+    diffuse_radius 0.1, fg_samples 8, fg_bounces 2."""
+    for fg in (False, True):
+        sc = scenes.cornell_pm_scene(48, fg)
+        rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
+        mean = rgb.mean(0)
+        se = rgb.std(0, ddof=1) / np.sqrt(batches)
+        name = f"cornell_pm_{'fg' if fg else 'direct'}_48_render.npz"
+        np.savez_compressed(os.path.join(OUT, name), mean=mean.astype(np.float32), se=se.astype(np.float32),
+                            batches=np.int32(batches), spp=np.int32(spp), seconds=secs)
+        print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
+
+
 def indoor_golden(spp=16, batches=24):
     sc = scenes.indoor_scene(n_boxes=120, subdiv=1, res=(96, 54))
     rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
@@ -109,5 +149,9 @@ if __name__ == "__main__":
         indoor_golden()
     if "cornell_glass" in what:
         variant_golden("cornell_glass_64_render.npz", glass=True)
+    if "pm" in what:
+        pm_golden()
+    if "cornell_pm" in what:
+        cornell_pm_golden()
     if "cornell_point" in what:
         variant_golden("cornell_point_64_render.npz", point_light=True)

@@ -55,3 +55,19 @@ def test_guide_and_tensor_core_argument_checks(gbrt_lib):
         gbrt.tc_selftest(np.zeros((128, 8), np.float32), np.zeros((8, 8), np.float32))
     with pytest.raises(gbrt.GbrtError, match="multiple of 16"):
         gbrt.tc_selftest(a, np.zeros((80, 16), np.float32))
+
+
+def test_photon_mapping_argument_checks(gbrt_lib):
+    """Photon-mapping defaults are the reference's; argument errors are
+    reported before any CUDA call."""
+    from libyafaray_gb300 import gbrt
+    p = gbrt.PmParams()
+    assert gbrt_lib.gbrt_pm_default_params(ctypes.byref(p)) == 0
+    assert (p.diffuse_photons, p.caustic_photons, p.diffuse_search, p.caustic_mix, p.caustic_depth, p.bounces) == (100000, 500000, 50, 50, 10, 3)
+    assert abs(p.diffuse_radius - 0.1) < 1e-7 and abs(p.caustic_radius - 0.25) < 1e-7
+    assert (p.caustics, p.diffuse, p.final_gather, p.fg_samples, p.fg_bounces) == (0, 1, 1, 32, 2)
+    assert gbrt_lib.gbrt_pm_render(None, None, None, None, None, None, None, None) == -1
+    with pytest.raises(gbrt.GbrtError, match="k in"):
+        gbrt.knn_gather([[0, 0, 0]], [[0, 0, 0]], cell=0.1, k=65, r2=0.01)
+    with pytest.raises(gbrt.GbrtError, match="below the search radius"):
+        gbrt.knn_gather([[0, 0, 0]], [[0, 0, 0]], cell=0.05, k=8, r2=0.01)
