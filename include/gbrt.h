@@ -247,6 +247,11 @@ typedef struct gbrt_pt_stats {
 	uint64_t extension_rays;    /* camera + path continuation rays traced */
 	uint64_t shadow_rays;       /* shadow rays traced */
 	float ms;                   /* device time of the render (CUDA events) */
+	/* photonmapping only (gbrt_pm_render) */
+	uint64_t photon_paths;      /* diffuse + caustic photon paths shot */
+	uint64_t photons_stored;    /* diffuse + caustic photons deposited */
+	uint64_t radiance_photons;  /* radiance-map photons after thinning */
+	float photon_ms;            /* device time of the photon-map preprocess */
 } gbrt_pt_stats;
 
 typedef struct gbrt_scene gbrt_scene;

@@ -2772,6 +2772,7 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 		float ms = 0.f;
 		cudaEventElapsedTime(&ms, e0, e1);
 		cudaEventDestroy(e0); cudaEventDestroy(e1);
+		*stats = gbrt_pt_stats{};
 		stats->camera_samples = total / pp.path_samples;
 		stats->extension_rays = st[0];
 		stats->shadow_rays = st[1];
@@ -2986,6 +2987,13 @@ int gbrt_pm_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 	M.pm_caustic_k = q.caustic_mix;
 	M.pm_lookup_r2 = 4.f * dr * dr;
 	const uint32_t seed = params->seed * 0x9e3779b9u + params->base_sampling_offset;
+	cudaEvent_t p0 = nullptr, p1 = nullptr;
+	if(stats)
+	{
+		GBRT_CK(cudaEventCreate(&p0)); GBRT_CK(cudaEventCreate(&p1));
+		GBRT_CK(cudaEventRecord(p0, s));
+	}
+	uint32_t n_radiance = 0;
 	ShotMap D, C;
 	GridStore GD, GC, GP, GR;
 	DevBuf st0, st1, und, rpos, rdir, rcol, rcnt;
@@ -3043,9 +3051,25 @@ int gbrt_pm_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 		GBRT_CK(cudaStreamSynchronize(s));
 		if(int rc = build_grid(rpos.as<float4>(), rdir.as<float4>(), rcol.as<float4>(), nr, 2.f * dr, lo, S->n_sm, GR, s)) return rc;
 		M.g_radiance = GR.g;
+		n_radiance = nr;
+	}
+	float photon_ms = 0.f;
+	if(stats)
+	{
+		GBRT_CK(cudaEventRecord(p1, s));
+		GBRT_CK(cudaEventSynchronize(p1));
+		cudaEventElapsedTime(&photon_ms, p0, p1);
+		cudaEventDestroy(p0); cudaEventDestroy(p1);
 	}
 	const int rc = render_locked(S, camera, *params, &M, film_dev, film64_dev, stats, s);
 	cudaStreamSynchronize(s);      // the photon buffers are freed on return
+	if(stats && !rc)
+	{
+		stats->photon_paths = static_cast<uint64_t>(D.paths) + C.paths;
+		stats->photons_stored = static_cast<uint64_t>(D.n) + C.n;
+		stats->radiance_photons = n_radiance;
+		stats->photon_ms = photon_ms;
+	}
 	return rc;
 }
 

@@ -88,7 +88,8 @@ def pm_params(integrator):
 
 class PtStats(ctypes.Structure):
     _fields_ = [("camera_samples", ctypes.c_uint64), ("extension_rays", ctypes.c_uint64),
-                ("shadow_rays", ctypes.c_uint64), ("ms", ctypes.c_float)]
+                ("shadow_rays", ctypes.c_uint64), ("ms", ctypes.c_float), ("photon_paths", ctypes.c_uint64),
+                ("photons_stored", ctypes.c_uint64), ("radiance_photons", ctypes.c_uint64), ("photon_ms", ctypes.c_float)]
 
 
 class GuideParams(ctypes.Structure):
@@ -410,8 +411,12 @@ class Renderer:
                                         ctypes.c_void_p(film64_ptr or None), ctypes.byref(st) if stats else None,
                                         ctypes.c_void_p(stream)))
         if stats:
-            return {"camera_samples": st.camera_samples, "extension_rays": st.extension_rays,
-                    "shadow_rays": st.shadow_rays, "ms": st.ms}
+            out = {"camera_samples": st.camera_samples, "extension_rays": st.extension_rays,
+                   "shadow_rays": st.shadow_rays, "ms": st.ms}
+            if self.is_pm:
+                out.update(photon_paths=st.photon_paths, photons_stored=st.photons_stored,
+                           radiance_photons=st.radiance_photons, photon_ms=st.photon_ms)
+            return out
         return None
 
 
