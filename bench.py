@@ -220,6 +220,31 @@ def render_sections(args):
         "reference_cpu_note": "reference: 4.32 s per frame (photon maps + render, scene tree already built), "
                               "8 x86 threads, oracle/_ref render_dump, threads_photons auto"}
     del r, film
+    # 64 random scenes (spheres / tori, shinydiffuse / glossy / rough glass,
+    # 1-4 area lights), 64 spp, bounces 8, rendered as one batch
+    t0 = time.perf_counter()
+    rs = [gbrt.Renderer(scenes.batch_scene(i)) for i in range(64)]
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    films = [torch.zeros(r.scene["camera"]["resx"] * r.scene["camera"]["resy"] * 3, dtype=torch.float32, device="cuda")
+             for r in rs]
+    gbrt.render_batch(rs[:4], 1, [f.data_ptr() for f in films[:4]])        # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st = gbrt.render_batch(rs, 64, [f.data_ptr() for f in films], concurrency=8)
+    torch.cuda.synchronize()
+    batch_s = time.perf_counter() - t0
+    rays = sum(x["extension_rays"] + x["shadow_rays"] for x in st)
+    samples = sum(x["camera_samples"] for x in st)
+    out["batch_64_scenes"] = {
+        "workload": "64 seeded scenes (seed 1000+i): round(10^U[3, log10 2e6]) triangles of spheres / tori on a plane, "
+                    "50 % shinydiffuse, 30 % glossy, 20 % rough_glass, 1-4 area lights, 256/512/1024 square, 64 spp, bounces 8",
+        "triangles": int(sum(len(r.faces) for r in rs)), "camera_samples": samples, "rays": rays,
+        "scene_setup_s": setup_s, "batch_wall_s": batch_s, "mrays_s": rays / batch_s / 1e6,
+        "msamples_s": samples / batch_s / 1e6, "concurrency": 8,
+        "reference_cpu_note": "reference, extrapolated: 8 of the 64 scenes (every 8th) at 1 spp took 4.49 s on 8 x86 threads "
+                              "(oracle/_ref render_dump, scene trees already built) -> about 2,300 s for 64 scenes x 64 spp"}
+    del rs, films
     # indoor scene lit through a door gap: guided vs plain time to relMSE 0.01
     r = gbrt.Renderer(scenes.indoor_scene())
     t0 = time.perf_counter()

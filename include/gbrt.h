@@ -277,6 +277,14 @@ int gbrt_pt_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const
                         float *image_out, gbrt_pt_stats *stats);
 
 
+/* Renders n scenes (each with its camera, parameters and device float film),
+ * up to `concurrency` at a time (0 = 8), each on its own stream from its own
+ * host thread, freeing each scene's work buffers after its render; wave_paths
+ * 0 means 1 Mi per scene here.  stats: NULL or n entries.  Returns the first
+ * error (its message names the scene). */
+int gbrt_pt_render_batch(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params, float *const *films,
+                         uint32_t n, uint32_t concurrency, gbrt_pt_stats *stats);
+
 /* ---- photon mapping (the `photonmapping` integrator) ---------------------
  * Replaces PhotonIntegrator::preprocess / integrate / finalGathering and
  * CausticPhotonIntegrator's caustic map and estimate
@@ -313,6 +321,16 @@ int gbrt_pm_render(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt
 /* gbrt_pm_render into a temporary device film; per-pixel means copied to
  * image_out [resy][resx][3] (host). */
 int gbrt_pm_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
+                        float *image_out, gbrt_pt_stats *stats);
+/* The `directlighting` integrator (DirectLightIntegrator::integrate,
+ * src/integrator/surface/integrator_direct_light.cc:97-152): emission,
+ * all-light estimation at diffuse hits, the recursive glossy / specular
+ * split, and, when caustic != NULL and caustic->caustics, the caustic photon
+ * map of CausticPhotonIntegrator (caustic_photons, caustic_radius,
+ * caustic_mix, caustic_depth of `caustic`).  Ambient occlusion is not built. */
+int gbrt_dl_render(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *caustic,
+                   float *film_dev, double *film64_dev, gbrt_pt_stats *stats, void *stream);
+int gbrt_dl_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *caustic,
                         float *image_out, gbrt_pt_stats *stats);
 /* Diagnostic: shoots one photon map (which = 0 diffuse, 1 caustic) and copies
  * its photons to host `out` [n][9] = (dir xyz, pos xyz, colour rgb) in

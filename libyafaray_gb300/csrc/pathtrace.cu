@@ -29,6 +29,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <atomic>
+#include <string>
+#include <thread>
 #include <functional>
 #include <mutex>
 #include <vector>
@@ -92,7 +95,7 @@ struct Params {
 	uint32_t rec_stride;  // record slots per path (= bounces)
 	int radiance_target;  // train on incident radiance instead of the product with the BSDF
 	// photonmapping integrator (PhotonIntegrator::integrate / finalGathering)
-	int pm;                    // 1: photonmapping
+	int pm;                    // 1: photonmapping, 2: directlighting (DirectLightIntegrator::integrate)
 	int pm_fg;                 // final gathering (path_samples then holds fg_samples)
 	int pm_fg_bounces;
 	float pm_gather_dist;      // fg_min_pathlen
@@ -1183,7 +1186,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				if((s.m->flags & BF_EMIT) && sub == 0 && mat_emit(s, wo, e))
 				{
 					// photonmapping adds it twice (integrator_photon_mapping.cc:686-687, 713-721)
-					const float em = P.pm ? 2.f : 1.f;
+					const float em = P.pm == 1 ? 2.f : 1.f;
 					film_add(film, film64, pixel, xm(thr[0], e[0]) * em, xm(thr[1], e[1]) * em, xm(thr[2], e[2]) * em);
 					if(W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
 				}
@@ -2210,6 +2213,18 @@ int alloc_spawn(gbrt_scene *S, size_t cap, int levels)
 	return GBRT_OK;
 }
 
+// Frees a scene's work and spawn buffers (they are re-made by the next render).
+void release_work(gbrt_scene *S)
+{
+	if(S->work) cudaFree(S->work);
+	if(S->spawn) cudaFree(S->spawn);
+	if(S->spawn_count) cudaFree(S->spawn_count);
+	S->work = nullptr; S->spawn = nullptr; S->spawn_count = nullptr;
+	S->w = Work{};
+	S->cap_paths = S->cap_shadow = S->cap_stride = 0;
+	S->spawn_cap = 0; S->spawn_levels = 0;
+}
+
 // Upper bound of the spawn records one hit can write (largest at division 1).
 uint32_t split_fanout(const gbrt_scene *S, int path_samples)
 {
@@ -2639,7 +2654,7 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	P.raydepth = raydepth;
 	if(pm)
 	{
-		P.pm = 1; P.pm_fg = pm->pm_fg; P.pm_fg_bounces = pm->pm_fg_bounces; P.pm_gather_dist = pm->pm_gather_dist;
+		P.pm = pm->pm; P.pm_fg = pm->pm_fg; P.pm_fg_bounces = pm->pm_fg_bounces; P.pm_gather_dist = pm->pm_gather_dist;
 		P.pm_diffuse = pm->pm_diffuse; P.pm_caustics = pm->pm_caustics; P.pm_diffuse_r2 = pm->pm_diffuse_r2; P.pm_diffuse_k = pm->pm_diffuse_k;
 		P.pm_caustic_r2 = pm->pm_caustic_r2; P.pm_caustic_k = pm->pm_caustic_k; P.pm_diffuse_paths = pm->pm_diffuse_paths;
 		P.pm_caustic_paths = pm->pm_caustic_paths; P.pm_lookup_r2 = pm->pm_lookup_r2;
@@ -2792,7 +2807,7 @@ int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 
 // Device film around a render call, per-pixel means copied to the host.
 static int render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
-                       float *image_out, gbrt_pt_stats *stats)
+                       float *image_out, gbrt_pt_stats *stats, int kind)
 {
 	const size_t n = 3ull * camera->resx * camera->resy;
 	const bool fp64 = (params->flags & GBRT_PT_FP64_FILM) != 0;
@@ -2803,8 +2818,13 @@ static int render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt
 	int rc = GBRT_OK;
 	if((e = cudaMemset(sum, 0, n * (fp64 ? 8 : 4))) != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
 	if(!rc)
-		rc = pm ? gbrt_pm_render(S, camera, params, pm, fp64 ? nullptr : static_cast<float *>(sum), fp64 ? static_cast<double *>(sum) : nullptr, stats, nullptr)
-		        : gbrt_pt_render(S, camera, params, fp64 ? nullptr : static_cast<float *>(sum), fp64 ? static_cast<double *>(sum) : nullptr, stats, nullptr);
+	{
+		float *f32 = fp64 ? nullptr : static_cast<float *>(sum);
+		double *f64 = fp64 ? static_cast<double *>(sum) : nullptr;
+		rc = kind == 1 ? gbrt_pm_render(S, camera, params, pm, f32, f64, stats, nullptr)
+		   : kind == 2 ? gbrt_dl_render(S, camera, params, pm, f32, f64, stats, nullptr)
+		               : gbrt_pt_render(S, camera, params, f32, f64, stats, nullptr);
+	}
 	if(!rc)
 	{
 		k_mean<<<grid_for(n, S->n_sm), kThreads>>>(fp64 ? nullptr : static_cast<float *>(sum), fp64 ? static_cast<double *>(sum) : nullptr,
@@ -2819,14 +2839,21 @@ static int render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt
 int gbrt_pt_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, float *image_out, gbrt_pt_stats *stats)
 {
 	if(!S || !camera || !params || !image_out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_host: NULL argument");
-	return render_host(S, camera, params, nullptr, image_out, stats);
+	return render_host(S, camera, params, nullptr, image_out, stats, 0);
 }
 
 int gbrt_pm_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
                         float *image_out, gbrt_pt_stats *stats)
 {
 	if(!S || !camera || !params || !pm || !image_out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pm_render_host: NULL argument");
-	return render_host(S, camera, params, pm, image_out, stats);
+	return render_host(S, camera, params, pm, image_out, stats, 1);
+}
+
+int gbrt_dl_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *caustic,
+                        float *image_out, gbrt_pt_stats *stats)
+{
+	if(!S || !camera || !params || !image_out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_dl_render_host: NULL argument");
+	return render_host(S, camera, params, caustic, image_out, stats, 2);
 }
 
 // Diagnostics: evaluates one sampling primitive on n inputs, on the device
@@ -3070,6 +3097,89 @@ int gbrt_pm_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 		stats->radiance_photons = n_radiance;
 		stats->photon_ms = photon_ms;
 	}
+	return rc;
+}
+
+int gbrt_pt_render_batch(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params, float *const *films,
+                         uint32_t n, uint32_t concurrency, gbrt_pt_stats *stats)
+{
+	if(n && (!scenes || !cameras || !params || !films)) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_batch: NULL argument");
+	for(uint32_t i = 0; i < n; ++i)
+		if(!scenes[i] || !films[i]) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_batch: scene or film %u is NULL", i);
+	int dev = 0;
+	GBRT_CK(cudaGetDevice(&dev));
+	const uint32_t workers = std::max(1u, std::min(n, concurrency ? concurrency : 8u));
+	std::atomic<uint32_t> next{0};
+	std::atomic<int> first_rc{GBRT_OK};
+	std::mutex err_mu;
+	std::string err_msg;
+	auto work = [&]() {
+		if(cudaSetDevice(dev) != cudaSuccess) { first_rc = GBRT_ERR_CUDA; return; }
+		cudaStream_t st = nullptr;
+		if(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) { first_rc = GBRT_ERR_CUDA; return; }
+		for(uint32_t i = next++; i < n && first_rc.load() == GBRT_OK; i = next++)
+		{
+			gbrt_scene *S = scenes[i];
+			gbrt_pt_params p = params[i];
+			if(!p.wave_paths) p.wave_paths = 1u << 20;      // bound each scene's work buffers
+			int rc = gbrt_pt_render(S, cameras + i, &p, films[i], nullptr, stats ? stats + i : nullptr, st);
+			if(!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "scene %u: stream error", i);
+			{
+				std::lock_guard<std::mutex> lock(S->mu);
+				release_work(S);                                  // the next scenes need the memory
+			}
+			if(rc)
+			{
+				int expect = GBRT_OK;
+				if(first_rc.compare_exchange_strong(expect, rc))
+				{
+					std::lock_guard<std::mutex> lock(err_mu);
+					err_msg = std::string("scene ") + std::to_string(i) + ": " + gbrt_last_error();
+				}
+			}
+		}
+		cudaStreamDestroy(st);
+	};
+	std::vector<std::thread> pool;
+	for(uint32_t w = 1; w < workers; ++w) pool.emplace_back(work);
+	work();
+	for(auto &t : pool) t.join();
+	if(first_rc.load() != GBRT_OK) return gbrt_set_error(first_rc.load(), "gbrt_pt_render_batch: %s", err_msg.c_str());
+	return GBRT_OK;
+}
+
+int gbrt_dl_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *caustic,
+                   float *film_dev, double *film64_dev, gbrt_pt_stats *stats, void *stream)
+{
+	if(!S || !camera || !params) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_dl_render: NULL argument");
+	if(!film_dev && !film64_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_dl_render: no film buffer");
+	const bool caustics = caustic && caustic->caustics;
+	if(caustics && (caustic->caustic_mix < 1 || caustic->caustic_mix > gbrt::kMaxGather || !(caustic->caustic_radius > 0.f) ||
+	                caustic->caustic_depth < 0 || caustic->caustic_photons < 0))
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_dl_render: bad caustic parameters (caustic_mix in [1, %d])", gbrt::kMaxGather);
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	std::lock_guard<std::mutex> lock(S->mu);
+	Params M{};
+	M.pm = 2;
+	M.path_samples = 1;
+	ShotMap C;
+	GridStore GC;
+	if(caustics)
+	{
+		float bound[6];
+		if(int rc = gbrt_bvh_get_bound(S->bvh, bound)) return rc;
+		const float lo[3] = {bound[0], bound[1], bound[2]};
+		const uint32_t seed = params->seed * 0x9e3779b9u + params->base_sampling_offset;
+		if(int rc = shoot_map(S, scene_dev(S), true, static_cast<uint32_t>(caustic->caustic_photons), caustic->caustic_depth, false, seed, C, s)) return rc;
+		if(int rc = build_grid(C.pos.as<float4>(), C.dir.as<float4>(), C.col.as<float4>(), C.n, caustic->caustic_radius, lo, S->n_sm, GC, s)) return rc;
+		M.pm_caustics = 1;
+		M.pm_caustic_r2 = caustic->caustic_radius * caustic->caustic_radius;
+		M.pm_caustic_k = caustic->caustic_mix;
+		M.pm_caustic_paths = static_cast<float>(C.paths);
+		M.g_caustic = GC.g;
+	}
+	const int rc = render_locked(S, camera, *params, &M, film_dev, film64_dev, stats, s);
+	cudaStreamSynchronize(s);
 	return rc;
 }
 

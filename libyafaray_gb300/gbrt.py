@@ -137,8 +137,11 @@ SIGNATURES = {
     "gbrt_guide_status": (_I, [_VP, ctypes.POINTER(ctypes.c_uint32)]),
     "gbrt_tc_selftest": (_I, [_VP, _VP, _U32, _U32, _VP]),
     "gbrt_pm_default_params": (_I, [_VP]),
+    "gbrt_pt_render_batch": (_I, [_VP, _VP, _VP, _VP, _U32, _U32, _VP]),
     "gbrt_pm_render": (_I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "gbrt_pm_render_host": (_I, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    "gbrt_dl_render": (_I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "gbrt_dl_render_host": (_I, [_VP, _VP, _VP, _VP, _VP, _VP]),
     "gbrt_pm_photons": (_I, [_VP, _VP, ctypes.c_int, _VP, _U32, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]),
     "gbrt_knn_gather": (_I, [_VP, _U32, _VP, _U32, ctypes.c_float, ctypes.c_int, ctypes.c_float, _VP, _VP, _VP]),
     "gbrt_pt_render": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP, _VP,
@@ -341,8 +344,12 @@ class Renderer:
             pass
 
     @property
+    def kind(self):
+        return self.scene["integrator"].get("type", "pathtracing")
+
+    @property
     def is_pm(self):
-        return self.scene["integrator"].get("type") == "photonmapping"
+        return self.kind == "photonmapping"
 
     def photons(self, which):
         """One photon map of this scene's photonmapping parameters (which =
@@ -383,10 +390,10 @@ class Renderer:
         p = self.params(spp, base_offset, seed, fp64, 0, guide, alpha, train_steps, batch, max_vertex)
         img = np.empty((cam.resy, cam.resx, 3), np.float32)
         st = PtStats()
-        if self.is_pm:
+        if self.kind in ("photonmapping", "directlighting"):
             pm = pm_params(self.scene["integrator"])
-            check(load().gbrt_pm_render_host(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.byref(pm), _ptr(img),
-                                             ctypes.byref(st)))
+            fn = load().gbrt_pm_render_host if self.kind == "photonmapping" else load().gbrt_dl_render_host
+            check(fn(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.byref(pm), _ptr(img), ctypes.byref(st)))
         else:
             check(load().gbrt_pt_render_host(self._h, ctypes.byref(cam), ctypes.byref(p), _ptr(img), ctypes.byref(st)))
         return img, {"camera_samples": st.camera_samples, "extension_rays": st.extension_rays,
@@ -401,11 +408,11 @@ class Renderer:
         if radiance_target:
             p.flags |= PT_GUIDE_RADIANCE
         st = PtStats()
-        if self.is_pm:
+        if self.kind in ("photonmapping", "directlighting"):
             pm = pm_params(self.scene["integrator"])
-            check(load().gbrt_pm_render(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.byref(pm),
-                                        ctypes.c_void_p(film_ptr or None), ctypes.c_void_p(film64_ptr or None),
-                                        ctypes.byref(st) if stats else None, ctypes.c_void_p(stream)))
+            fn = load().gbrt_pm_render if self.kind == "photonmapping" else load().gbrt_dl_render
+            check(fn(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.byref(pm), ctypes.c_void_p(film_ptr or None),
+                     ctypes.c_void_p(film64_ptr or None), ctypes.byref(st) if stats else None, ctypes.c_void_p(stream)))
         else:
             check(load().gbrt_pt_render(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.c_void_p(film_ptr or None),
                                         ctypes.c_void_p(film64_ptr or None), ctypes.byref(st) if stats else None,
@@ -534,3 +541,18 @@ def knn_gather(points, queries, cell, k, r2):
     idx = np.full((m, k), 0xFFFFFFFF, np.uint32)
     check(load().gbrt_knn_gather(_ptr(P), len(P), _ptr(Q), m, float(cell), int(k), float(r2), _ptr(cnt), _ptr(rr), _ptr(idx)))
     return cnt, rr, idx.astype(np.int64) - np.where(idx == 0xFFFFFFFF, 1 << 32, 0)
+
+
+def render_batch(renderers, spp, film_ptrs, concurrency=8, base_offset=0, seed=1):
+    """gbrt_pt_render_batch: renders every Renderer's scene into its device
+    float film (pointer), several scenes at a time on their own streams.
+    Returns the per-scene stats."""
+    n = len(renderers)
+    S = (ctypes.c_void_p * n)(*[r._h.value for r in renderers])
+    cams = (CameraDesc * n)(*[r.camera_desc() for r in renderers])
+    ps = (PtParams * n)(*[r.params(spp, base_offset, seed) for r in renderers])
+    F = (ctypes.c_void_p * n)(*[int(f) for f in film_ptrs])
+    st = (PtStats * n)()
+    check(load().gbrt_pt_render_batch(S, cams, ps, F, n, int(concurrency), st))
+    return [{"camera_samples": x.camera_samples, "extension_rays": x.extension_rays, "shadow_rays": x.shadow_rays,
+             "ms": x.ms} for x in st]

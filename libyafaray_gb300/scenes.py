@@ -411,3 +411,101 @@ def cornell_pm_scene(res, final_gather, diffuse_photons=100000):
                         "finalGather": bool(final_gather), "fg_samples": 8, "fg_bounces": 2, "bounces": 3,
                         "threads_photons": 1}
     return sc
+
+
+def uv_sphere(center, radius, nu, nv):
+    """Latitude-longitude sphere: nu x nv quads as 2 nu nv outward triangles."""
+    th = np.linspace(0.0, math.pi, nv + 1)
+    ph = np.linspace(0.0, 2.0 * math.pi, nu + 1)[:-1]
+    P = np.stack([np.outer(np.sin(th), np.cos(ph)), np.repeat(np.cos(th)[:, None], nu, 1), np.outer(np.sin(th), np.sin(ph))], -1)
+    P = P.reshape(-1, 3) * radius + np.asarray(center, np.float64)
+    i, j = np.meshgrid(np.arange(nv), np.arange(nu), indexing="ij")
+    a, b = i * nu + j, i * nu + (j + 1) % nu
+    c, d = a + nu, b + nu
+    F = np.stack([np.stack([a, d, c], -1), np.stack([a, b, d], -1)], 2).reshape(-1, 3)
+    return P, F
+
+
+def torus(center, R, r, nu, nv):
+    """Torus around +y: nu x nv quads as 2 nu nv outward triangles."""
+    u = np.linspace(0.0, 2.0 * math.pi, nu + 1)[:-1]
+    v = np.linspace(0.0, 2.0 * math.pi, nv + 1)[:-1]
+    U, V = np.meshgrid(u, v, indexing="ij")
+    P = np.stack([(R + r * np.cos(V)) * np.cos(U), r * np.sin(V), (R + r * np.cos(V)) * np.sin(U)], -1).reshape(-1, 3)
+    P = P + np.asarray(center, np.float64)
+    i, j = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
+    a, b = i * nv + j, i * nv + (j + 1) % nv
+    c, d = ((i + 1) % nu) * nv + j, ((i + 1) % nu) * nv + (j + 1) % nv
+    F = np.stack([np.stack([a, b, d], -1), np.stack([a, d, c], -1)], 2).reshape(-1, 3)
+    return P, F
+
+
+def batch_scene(i, res=None, spp_scale=1.0):
+    """Scene i of the 64-scene batch (seed 1000 + i): about
+    round(10^U[3, log10 2e6]) triangles of tessellated spheres and tori under
+    random rotations, scales and translations on a ground plane; each object
+    50 % shinydiffuse, 30 % glossy (exponent U[50, 500]), 20 % rough_glass
+    (IOR 1.5, alpha 0.1); 1-4 quad area lights (power U[5, 50]) with their
+    light_mat emitters; resolution from {256, 512, 1024}; pathtracing,
+    bounces 8.  res overrides the resolution (tests)."""
+    rng = np.random.default_rng(1000 + i)
+    n_tris = int(round(10 ** rng.uniform(3.0, math.log10(2e6))))
+    n_obj = int(rng.integers(1, 6))
+    mats = {"ground": ("shinydiffusemat", (0.6, 0.6, 0.6))}
+    objects = [{"name": "ground", "material": "ground",
+                "vertices": np.array([[-8, 0, -8], [8, 0, -8], [8, 0, 8], [-8, 0, 8]], np.float32),
+                "faces": np.array([[0, 2, 1, TRI], [0, 3, 2, TRI]], np.uint32)}]
+    per = max(200, n_tris // n_obj)
+    for k in range(n_obj):
+        u = rng.uniform()
+        if u < 0.5:
+            mats[f"m{k}"] = ("shinydiffusemat", tuple(float(x) for x in rng.uniform(0.2, 0.8, 3)))
+        elif u < 0.8:
+            mats[f"m{k}"] = glossy_material(tuple(float(x) for x in rng.uniform(0.2, 0.8, 3)), exponent=float(rng.uniform(50, 500)))
+        else:
+            mats[f"m{k}"] = rough_glass_material(1.5, 0.1)
+        size = float(rng.uniform(0.4, 1.2))
+        q = max(4, int(math.sqrt(per / 2.0)))
+        if rng.uniform() < 0.5:
+            P, F = uv_sphere((0, 0, 0), size, q, q)
+        else:
+            P, F = torus((0, 0, 0), size, size * float(rng.uniform(0.2, 0.45)), q, q)
+        a, b = rng.uniform(0, 2 * math.pi, 2)
+        Ry = np.array([[math.cos(a), 0, math.sin(a)], [0, 1, 0], [-math.sin(a), 0, math.cos(a)]])
+        Rx = np.array([[1, 0, 0], [0, math.cos(b), -math.sin(b)], [0, math.sin(b), math.cos(b)]])
+        S = np.diag(rng.uniform(0.7, 1.3, 3))
+        M = Ry @ Rx @ S
+        t = np.array([rng.uniform(-3, 3), 0.0, rng.uniform(-3, 3)])
+        P = P @ M.T + t
+        P[:, 1] += -P[:, 1].min() + 0.001                # rest on the ground
+        objects.append({"name": f"o{k}", "material": f"m{k}", "vertices": P.astype(np.float32),
+                        "faces": np.concatenate([F, np.full((len(F), 1), TRI)], 1).astype(np.uint32)})
+    lights = []
+    for k in range(int(rng.integers(1, 5))):
+        c = np.array([rng.uniform(-3, 3), rng.uniform(4, 6), rng.uniform(-3, 3)])
+        w = float(rng.uniform(0.5, 1.5))
+        x, z = np.array([w, 0, 0]), np.array([0, 0, w])
+        power = float(rng.uniform(5, 50))
+        mats[f"lamp{k}"] = ("light_mat", (1.0, 1.0, 1.0), power)
+        lv = np.array([c, c + x, c + x + z, c + z], np.float32)
+        objects.append({"name": f"lamp{k}", "material": f"lamp{k}", "vertices": lv,
+                        "faces": np.array([[0, 1, 2, TRI], [0, 2, 3, TRI]], np.uint32)})
+        lights.append({"type": "arealight", "corner": tuple(c), "point1": tuple(c + x), "point2": tuple(c + z),
+                       "color": (1.0, 1.0, 1.0), "power": power, "samples": 1})
+    if res is None:
+        res = int(rng.choice([256, 512, 1024]))
+    cam_a = rng.uniform(0, 2 * math.pi)
+    camera = {"from": (9.0 * math.cos(cam_a), 4.0, 9.0 * math.sin(cam_a)), "to": (0.0, 0.5, 0.0),
+              "up": (9.0 * math.cos(cam_a), 5.0, 9.0 * math.sin(cam_a)), "resx": res, "resy": res, "focal": 1.3737}
+    integ = {"type": "pathtracing", "path_samples": 1, "bounces": 8, "russian_roulette_min_bounces": 3}
+    return {"materials": mats, "objects": objects, "lights": lights, "camera": camera, "integrator": integ}
+
+
+def cornell_dl_scene(res, caustics=True, caustic_photons=200000):
+    """The glass Cornell box (glass + rough-glass balls) rendered by
+    `directlighting` with a caustic photon map (caustic_radius 0.05,
+    caustic_mix 50)."""
+    sc = cornell_scene(res=res, glass=True)
+    sc["integrator"] = {"type": "directlighting", "caustics": bool(caustics), "caustic_photons": int(caustic_photons),
+                        "caustic_radius": 0.05, "caustic_mix": 50, "caustic_depth": 10, "threads_photons": 1}
+    return sc

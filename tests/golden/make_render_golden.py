@@ -125,6 +125,36 @@ def cornell_pm_golden(spp=8, batches=24):
         print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
 
 
+BATCH_CASES = (5, 26)
+
+
+def batch_golden(spp=8, batches=24):
+    """batch_scene_{i}_48_render.npz: scenes of the 64-scene batch (seed
+    1000 + i; spheres / tori, shinydiffuse + glossy + rough glass, 2-4 area
+    lights, bounces 8) at 48x48."""
+    for i in BATCH_CASES:
+        sc = scenes.batch_scene(i, res=48)
+        rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
+        mean = rgb.mean(0)
+        se = rgb.std(0, ddof=1) / np.sqrt(batches)
+        name = f"batch_scene_{i}_48_render.npz"
+        np.savez_compressed(os.path.join(OUT, name), mean=mean.astype(np.float32), se=se.astype(np.float32),
+                            batches=np.int32(batches), spp=np.int32(spp), seconds=secs)
+        print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
+
+
+def dl_golden(spp=8, batches=24):
+    """cornell_dl_48_render.npz: the glass Cornell box with directlighting
+    and a 200k-path caustic photon map."""
+    sc = scenes.cornell_dl_scene(48)
+    rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
+    mean = rgb.mean(0)
+    se = rgb.std(0, ddof=1) / np.sqrt(batches)
+    np.savez_compressed(os.path.join(OUT, "cornell_dl_48_render.npz"), mean=mean.astype(np.float32), se=se.astype(np.float32),
+                        batches=np.int32(batches), spp=np.int32(spp), seconds=secs)
+    print(f"cornell_dl_48_render.npz: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
+
+
 def indoor_golden(spp=16, batches=24):
     sc = scenes.indoor_scene(n_boxes=120, subdiv=1, res=(96, 54))
     rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
@@ -151,6 +181,10 @@ if __name__ == "__main__":
         variant_golden("cornell_glass_64_render.npz", glass=True)
     if "pm" in what:
         pm_golden()
+    if "dl" in what:
+        dl_golden()
+    if "batch" in what:
+        batch_golden()
     if "cornell_pm" in what:
         cornell_pm_golden()
     if "cornell_point" in what:

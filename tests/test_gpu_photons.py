@@ -149,3 +149,16 @@ def test_photonmapping_cornell_matches_reference(cuda_device, fg):
     print(f"photonmapping cornell, {'final gather' if fg else 'direct'} 48x48: {100 * frac:.2f}% agree, relMSE {relmse:.3g}, "
           f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
     assert frac >= 0.99 and relmse < 1e-3
+
+
+def test_directlighting_caustics_matches_reference(cuda_device):
+    """directlighting on the glass Cornell box: emission, all-light
+    estimation, the recursive split through the glass and rough-glass balls,
+    and the caustic photon map (glossy and specular photon paths)."""
+    g = np.load(os.path.join(GOLD, "cornell_dl_48_render.npz"))
+    r = gbrt.Renderer(scenes.cornell_dl_scene(48))
+    gb = render_batches(r, int(g["spp"]), int(g["batches"]))
+    frac, relmse, m = pm_parity(gb, g["mean"], g["se"])
+    print(f"directlighting glass cornell 48x48: {100 * frac:.2f}% agree, relMSE {relmse:.3g}, "
+          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
+    assert frac >= 0.99

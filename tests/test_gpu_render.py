@@ -134,3 +134,32 @@ def test_gpu_recursive_split_small_waves_agree(cuda_device):
     torch.cuda.synchronize()
     assert st_a["extension_rays"] == st_b["extension_rays"] and st_a["shadow_rays"] == st_b["shadow_rays"]
     assert torch.allclose(a, b, rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("i", [5, 26])
+def test_gpu_batch_scene_matches_reference(cuda_device, i):
+    """Scenes of the 64-scene batch (tessellated spheres / tori, shinydiffuse +
+    glossy + rough glass, several area lights, bounces 8) at 48x48."""
+    g = np.load(os.path.join(GOLD, f"batch_scene_{i}_48_render.npz"))
+    r = gbrt.Renderer(scenes.batch_scene(i, res=48))
+    gb = batches(r, int(g["spp"]), int(g["batches"]))
+    frac, relmse, m = parity(gb, g["mean"], g["se"])
+    print(f"batch scene {i} 48x48: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
+          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
+    assert frac >= 0.995
+
+
+def test_gpu_render_batch_equals_single_renders(cuda_device):
+    """gbrt_pt_render_batch (several scenes at once on their own streams)
+    gives each scene the image its own render gives."""
+    torch = pytest.importorskip("torch")
+    rs = [gbrt.Renderer(scenes.batch_scene(i, res=32)) for i in (5, 26, 30)]
+    films = [torch.zeros(32 * 32 * 3, dtype=torch.float32, device="cuda") for _ in rs]
+    st = gbrt.render_batch(rs, 4, [f.data_ptr() for f in films], concurrency=3)
+    torch.cuda.synchronize()
+    for r, f, s in zip(rs, films, st):
+        single = torch.zeros_like(f)
+        s1 = r.render_device(4, single.data_ptr(), stats=True)
+        torch.cuda.synchronize()
+        assert s["extension_rays"] == s1["extension_rays"] and s["shadow_rays"] == s1["shadow_rays"]
+        assert torch.allclose(f, single, rtol=1e-4, atol=1e-6)
