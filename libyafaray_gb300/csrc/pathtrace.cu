@@ -1048,12 +1048,16 @@ __global__ void __launch_bounds__(kThreads) k_camera(Camera cam, Params P, Work 
 {
 	// sample-major order: a wave holds whole sample indices of every pixel,
 	// so each wave (and each guide training batch drawn from it) covers the
-	// full image, and neighbouring threads shoot neighbouring pixels
+	// full image, and neighbouring threads shoot neighbouring pixels; the
+	// path samples of one camera sample are adjacent (so a wave of W paths
+	// holds at most W / path_samples + 2 integrate() roots)
 	const uint32_t n_pix = static_cast<uint32_t>(cam.resx) * static_cast<uint32_t>(cam.resy);
+	const uint32_t ps = static_cast<uint32_t>(P.path_samples);
 	for(uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < P.wave_n; s += gridDim.x * blockDim.x)
 	{
 		const uint32_t g = P.wave_start + s;
-		const uint32_t pixel = g % n_pix, si = g / n_pix;
+		const uint32_t rest = g / ps, sub = g % ps;
+		const uint32_t pixel = rest % n_pix, si = (rest / n_pix) * ps + sub;
 		const uint32_t sample = si / static_cast<uint32_t>(P.path_samples);
 		const uint32_t offset_ = pixel_offset(pixel, cam.resx);
 		float dx = 0.5f, dy = 0.5f;
@@ -2114,6 +2118,8 @@ struct gbrt_scene {
 	uint16_t *lds_perm = nullptr;
 	uint32_t *lds_off = nullptr, *lds_base = nullptr;
 	double *lds_inv = nullptr;
+	double *lds_sfac = nullptr;
+	uint32_t *lds_sfac_off = nullptr, *lds_sfac_nd = nullptr;
 	// materials that start the recursive split, for its buffer sizing
 	bool split_glossy = false, split_glossy_transmit = false, split_specular = false;
 	uint32_t max_addl = 0;
@@ -2426,7 +2432,7 @@ int shoot_map(gbrt_scene *S, const SceneDev &sc, bool caustic, uint32_t n, int m
 
 SceneDev scene_dev(const gbrt_scene *S)
 {
-	return SceneDev{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv}};
+	return SceneDev{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off, S->lds_sfac_nd}};
 }
 
 } // namespace
@@ -2577,6 +2583,9 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 		{reinterpret_cast<void **>(&S->lds_off), T.offset.data(), T.offset.size() * sizeof(uint32_t)},
 		{reinterpret_cast<void **>(&S->lds_base), T.base.data(), T.base.size() * sizeof(uint32_t)},
 		{reinterpret_cast<void **>(&S->lds_inv), T.inv.data(), T.inv.size() * sizeof(double)},
+		{reinterpret_cast<void **>(&S->lds_sfac), T.sfac.data(), T.sfac.size() * sizeof(double)},
+		{reinterpret_cast<void **>(&S->lds_sfac_off), T.sfac_offset.data(), T.sfac_offset.size() * sizeof(uint32_t)},
+		{reinterpret_cast<void **>(&S->lds_sfac_nd), T.sfac_digits.data(), T.sfac_digits.size() * sizeof(uint32_t)},
 	};
 	for(const Up &u : ups)
 	{
@@ -2592,7 +2601,8 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 int gbrt_scene_destroy(gbrt_scene *S)
 {
 	if(!S) return GBRT_OK;
-	void *ptrs[] = {S->prim_ng, S->mats, S->lights, S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->work, S->spawn, S->spawn_count};
+	void *ptrs[] = {S->prim_ng, S->mats, S->lights, S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off,
+	                S->lds_sfac_nd, S->work, S->spawn, S->spawn_count};
 	for(void *p : ptrs) if(p) cudaFree(p);
 	delete S;
 	return GBRT_OK;
@@ -2629,13 +2639,24 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	const int raydepth = pp.raydepth > 0 ? pp.raydepth : 5;
 	const uint32_t fanout = split_fanout(S, pp.path_samples);
 	const int split_levels = fanout ? std::min(19, raydepth + static_cast<int>(S->max_addl)) : 0;
-	constexpr uint64_t kSpawnCap = 1ull << 22;
+	// spawn records per wave: only the first path sample of an integrate()
+	// call spawns (at most `fanout` records); a camera wave of W paths holds
+	// at most W / path_samples + 2 such roots, a chunk of c spawned records at
+	// most c / n_min + 1, n_min = the fewest path samples a spawned call gets
+	// (the glossy split divides by up to 8)
+	constexpr uint64_t kSpawnCap = 1ull << 23;
+	const uint64_t ps = static_cast<uint64_t>(pp.path_samples);
+	const uint64_t n_min = std::max<uint64_t>(1, ps / (S->split_glossy ? 8u : 1u));
+	size_t spawn_cap = 0;
+	uint64_t chunk = wave;
 	if(split_levels > 0)
 	{
-		wave = std::max<uint64_t>(1, std::min<uint64_t>(wave, kSpawnCap / fanout));
-		if(int rc = alloc_spawn(S, static_cast<size_t>(wave) * fanout, split_levels)) return rc;
+		const uint64_t roots = std::max<uint64_t>(1, kSpawnCap / fanout - 2);
+		wave = std::max<uint64_t>(1, std::min<uint64_t>(wave, roots * ps));
+		spawn_cap = static_cast<size_t>((wave / ps + 2) * fanout);
+		chunk = std::max<uint64_t>(1, std::min<uint64_t>(wave, (spawn_cap / fanout - 1) * n_min));
+		if(int rc = alloc_spawn(S, spawn_cap, split_levels)) return rc;
 	}
-	const size_t spawn_cap = static_cast<size_t>(wave) * fanout;
 	uint32_t max_shadow = 0;
 	{
 		std::vector<DevLight> ls(S->n_lights);
@@ -2648,7 +2669,7 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	const uint32_t stride = static_cast<uint32_t>(std::max(1, pp.bounces));
 	if(int rc = alloc_work(S, wave, shadow_cap, guide ? stride : 0)) return rc;
 	Camera cam = make_camera(*camera);
-	SceneDev sc{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv}};
+	SceneDev sc{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off, S->lds_sfac_nd}};
 	Params P{};
 	P.spp = pp.spp; P.path_samples = pp.path_samples; P.bounces = pp.bounces; P.rr_min = pp.russian_roulette_min_bounces;
 	P.raydepth = raydepth;
@@ -2722,9 +2743,9 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	// integrate() calls of ray level L, depth first: a chunk of them, then
 	// everything they spawned, then the next chunk
 	std::function<int(int, uint32_t)> process_level = [&](int L, uint32_t n) -> int {
-		for(uint32_t c0 = 0; c0 < n; c0 += static_cast<uint32_t>(wave))
+		for(uint32_t c0 = 0; c0 < n; c0 += static_cast<uint32_t>(chunk))
 		{
-			const uint32_t cn = static_cast<uint32_t>(std::min<uint64_t>(wave, n - c0));
+			const uint32_t cn = static_cast<uint32_t>(std::min<uint64_t>(chunk, n - c0));
 			Params Pc = P;
 			Work Wc = W;
 			Wc.p_sum = nullptr;
@@ -2866,17 +2887,20 @@ int gbrt_sampler_eval(int kind, int dim, const uint32_t *input, uint32_t n, doub
 	const auto T = gbrt::make_lds_tables();
 	if(!on_device)
 	{
-		const gbrt::LdsTables t{T.perm.data(), T.offset.data(), T.base.data(), T.inv.data()};
+		const gbrt::LdsTables t = T.view();
 		for(uint32_t i = 0; i < n; ++i) out[i] = sampler_value(t, kind, dim, input[i]);
 		return GBRT_OK;
 	}
 	if(n == 0) return GBRT_OK;
 	void *d_perm = nullptr, *d_off = nullptr, *d_base = nullptr, *d_inv = nullptr, *d_in = nullptr, *d_out = nullptr;
+	void *d_sf = nullptr, *d_sfo = nullptr, *d_sfd = nullptr;
 	int rc = GBRT_OK;
 	cudaError_t e = cudaSuccess;
 	struct Up { void **dst; const void *src; size_t bytes; };
 	const Up ups[] = {{&d_perm, T.perm.data(), T.perm.size() * 2}, {&d_off, T.offset.data(), T.offset.size() * 4},
 	                  {&d_base, T.base.data(), T.base.size() * 4}, {&d_inv, T.inv.data(), T.inv.size() * 8},
+	                  {&d_sf, T.sfac.data(), T.sfac.size() * 8}, {&d_sfo, T.sfac_offset.data(), T.sfac_offset.size() * 4},
+	                  {&d_sfd, T.sfac_digits.data(), T.sfac_digits.size() * 4},
 	                  {&d_in, input, 4ull * n}, {&d_out, nullptr, 8ull * n}};
 	for(const Up &u : ups)
 	{
@@ -2885,13 +2909,14 @@ int gbrt_sampler_eval(int kind, int dim, const uint32_t *input, uint32_t n, doub
 	}
 	if(e == cudaSuccess)
 	{
-		const gbrt::LdsTables t{static_cast<uint16_t *>(d_perm), static_cast<uint32_t *>(d_off), static_cast<uint32_t *>(d_base), static_cast<double *>(d_inv)};
+		const gbrt::LdsTables t{static_cast<uint16_t *>(d_perm), static_cast<uint32_t *>(d_off), static_cast<uint32_t *>(d_base),
+		                        static_cast<double *>(d_inv), static_cast<double *>(d_sf), static_cast<uint32_t *>(d_sfo), static_cast<uint32_t *>(d_sfd)};
 		k_sampler<<<(n + 127) / 128, 128>>>(t, kind, dim, static_cast<const uint32_t *>(d_in), n, static_cast<double *>(d_out));
 		e = cudaGetLastError();
 		if(e == cudaSuccess) e = cudaMemcpy(out, d_out, 8ull * n, cudaMemcpyDeviceToHost);
 	}
 	if(e != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "gbrt_sampler_eval: %s", cudaGetErrorString(e));
-	for(void *p : {d_perm, d_off, d_base, d_inv, d_in, d_out}) if(p) cudaFree(p);
+	for(void *p : {d_perm, d_off, d_base, d_inv, d_sf, d_sfo, d_sfd, d_in, d_out}) if(p) cudaFree(p);
 	return rc;
 }
 

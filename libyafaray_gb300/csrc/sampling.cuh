@@ -33,6 +33,11 @@ struct LdsTables {
 	const uint32_t *perm_offset;       // [kLdsDims]
 	const uint32_t *base;              // [kLdsDims]
 	const double *inv;                 // [kLdsDims] 1/base rounded to 9 decimals
+	// sigma[d] x factor_k as the reference's loop forms them (factor_0 = inv,
+	// factor_{k+1} = factor_k x inv, both rounded in double): [digit k][d]
+	const double *sfac;
+	const uint32_t *sfac_offset;       // [kLdsDims]
+	const uint32_t *sfac_digits;       // [kLdsDims] digits tabulated
 };
 
 GBRT_HD float fmul(float a, float b)
@@ -94,10 +99,15 @@ GBRT_HD uint32_t bit_reverse(uint32_t b)
 #endif
 }
 
+// x * 2^-32 rounded to float: the reference forms it in double (exact, x <
+// 2^32) and rounds once, which equals rounding x to float and scaling by
+// the power of two.
+GBRT_HD float u32_fraction(uint32_t x) { return clamp01(static_cast<float>(x) * 2.3283064365386962890625e-10f); }
+
 // van der Corput: bit-reversed index as a fraction
 GBRT_HD float ri_vdc(uint32_t bits, uint32_t r = 0)
 {
-	return clamp01(static_cast<float>(dmul(static_cast<double>(bit_reverse(bits) ^ r), kTwoPowMinus32)));
+	return u32_fraction(bit_reverse(bits) ^ r);
 }
 
 // Larcher & Pillichshammer
@@ -105,7 +115,7 @@ GBRT_HD float ri_lp(uint32_t i, uint32_t r = 0)
 {
 	for(uint32_t v = 1u << 31; i; i >>= 1, v |= v >> 1)
 		if(i & 1u) r ^= v;
-	return clamp01(static_cast<float>(dmul(static_cast<double>(r), kTwoPowMinus32)));
+	return u32_fraction(r);
 }
 
 // Sobol' second dimension
@@ -113,7 +123,7 @@ GBRT_HD float ri_s(uint32_t i, uint32_t r = 0)
 {
 	for(uint32_t v = 1u << 31; i; i >>= 1, v ^= v >> 1)
 		if(i & 1u) r ^= v;
-	return clamp01(static_cast<float>(dmul(static_cast<double>(r), kTwoPowMinus32)));
+	return u32_fraction(r);
 }
 
 // FNV-1a over the four bytes of a 32-bit value, lowest byte first
@@ -128,9 +138,45 @@ GBRT_HD uint32_t fnv32(uint32_t value)
 	return h;
 }
 
+// 3^-(k+1) as the loop below forms it in double (f_0 = 1/3, f_{k+1} = f_k / 3
+// rounded), k = 0 .. 20.
+#define GBRT_INV3_POW {0x1.5555555555555p-2, 0x1.c71c71c71c71cp-4, 0x1.2f684bda12f68p-5, 0x1.948b0fcd6e9e0p-7, \
+	0x1.0db20a88f4695p-8, 0x1.67980e0bf08c6p-10, 0x1.df75680feb65dp-12, 0x1.3fa39ab547993p-13, 0x1.aa2f78f1b4cc4p-15, \
+	0x1.1c1fa5f678882p-16, 0x1.7ad4dd48a0b58p-18, 0x1.f91bd1b62b9cap-20, 0x1.50bd367972686p-21, 0x1.c0fc48a1ede08p-23, \
+	0x1.2b52db169e95ap-24, 0x1.8f19241e28c78p-26, 0x1.0a10c2bec5da5p-27, 0x1.62c103a907cdcp-29, 0x1.d9015a36b5125p-31, \
+	0x1.3b563c2478b6ep-32, 0x1.a472fadb4b9e8p-34}
+#if defined(__CUDACC__)
+static __constant__ double c_inv3_pow[21] = GBRT_INV3_POW;
+#endif
+static constexpr double h_inv3_pow[21] = GBRT_INV3_POW;
+GBRT_HD double inv3_pow(int k)
+{
+#if defined(__CUDA_ARCH__)
+	return c_inv3_pow[k];
+#else
+	return h_inv3_pow[k];
+#endif
+}
+
 // Radical inverse of n in base b (the value Halton(b, n - 1).getNext() returns).
+// In base 2 every term and partial sum is exact in double, so the value is
+// bitrev(n) x 2^-32 rounded once to float; in base 3 the digit products
+// (0, 1 or 2 x 3^-(k+1)) are exact and only the additions round.  Both give
+// the general loop's result bit for bit with far less FP64 work.
 GBRT_HD float radical_inverse(uint32_t n, uint32_t b)
 {
+	if(b == 2) return clamp01(static_cast<float>(bit_reverse(n)) * 2.3283064365386962890625e-10f);
+	if(b == 3)
+	{
+		double v = 0.0;
+		for(int k = 0; n > 0; ++k)
+		{
+			const uint32_t d = n % 3u;
+			n /= 3u;
+			if(d) v = dadd(v, d == 1u ? inv3_pow(k) : 2.0 * inv3_pow(k));
+		}
+		return clamp01(static_cast<float>(v));
+	}
 	const double inv = 1.0 / static_cast<double>(b);
 	double f = inv, v = 0.0;
 	while(n > 0)
@@ -146,17 +192,26 @@ GBRT_HD float radical_inverse(uint32_t n, uint32_t b)
 // reference does it (so multiples of the base round like the reference).
 GBRT_HD double low_discrepancy(const LdsTables &t, int dim, uint32_t n)
 {
-	const uint16_t *sigma = t.perm + t.perm_offset[dim];
 	const uint32_t base = t.base[dim];
-	const double f = t.inv[dim];
 	if(base < 2) return 0.0;
-	double value = 0.0, dn = static_cast<double>(n), factor = f;
-	while(n > 0)
+	const double f = t.inv[dim];
+	const double *sf = t.sfac + t.sfac_offset[dim];
+	const uint32_t nd = t.sfac_digits[dim];
+	double value = 0.0, dn = static_cast<double>(n);
+	for(uint32_t k = 0; n > 0; ++k)
 	{
-		value = dadd(value, dmul(static_cast<double>(sigma[n % base]), factor));
+		double term;
+		if(k < nd) term = sf[k * base + n % base];
+		else
+		{
+			// past the tabulated digits (not reached for 32-bit n): form the factor
+			double factor = f;
+			for(uint32_t j = 0; j < k; ++j) factor = dmul(factor, f);
+			term = dmul(static_cast<double>(t.perm[t.perm_offset[dim] + n % base]), factor);
+		}
+		value = dadd(value, term);
 		dn = dmul(dn, f);
 		n = static_cast<uint32_t>(dn);
-		factor = dmul(factor, f);
 	}
 	return value;
 }
@@ -265,6 +320,12 @@ struct LdsHostTables {
 	std::vector<uint16_t> perm;
 	std::vector<uint32_t> offset, base;
 	std::vector<double> inv;
+	std::vector<double> sfac;
+	std::vector<uint32_t> sfac_offset, sfac_digits;
+	LdsTables view() const
+	{
+		return LdsTables{perm.data(), offset.data(), base.data(), inv.data(), sfac.data(), sfac_offset.data(), sfac_digits.data()};
+	}
 };
 
 inline LdsHostTables make_lds_tables()
@@ -279,6 +340,21 @@ inline LdsHostTables make_lds_tables()
 		t.inv.push_back(std::round(1e9 / static_cast<double>(b)) / 1e9);
 		const auto p = faure_permutation(b < 2 ? 2 : b);
 		t.perm.insert(t.perm.end(), p.begin(), p.end());
+		// digits a 32-bit index can have in base b, plus margin
+		uint32_t nd = 2;
+		for(double x = 4294967296.0; x >= 1.0; x /= static_cast<double>(b < 2 ? 2 : b)) ++nd;
+		t.sfac_offset.push_back(static_cast<uint32_t>(t.sfac.size()));
+		t.sfac_digits.push_back(b < 2 ? 0u : nd);
+		if(b >= 2)
+		{
+			const double f = t.inv.back();
+			double factor = f;
+			for(uint32_t k = 0; k < nd; ++k)
+			{
+				for(uint32_t d = 0; d < b; ++d) t.sfac.push_back(static_cast<double>(p[d]) * factor);
+				factor = factor * f;
+			}
+		}
 	}
 	return t;
 }
