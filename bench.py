@@ -252,9 +252,9 @@ def render_sections(args):
     ref_s = time.perf_counter() - t0
     plain = convergence.time_to_relmse(r, ref, target=0.01, spp_pass=16, max_time=90)
     guide = r.make_guide()
-    guided = convergence.time_to_relmse(r, ref, target=0.01, spp_pass=4, max_time=90, guide=guide, alpha=0.5,
-                                        train_fraction=0.25, train_steps=16, batch=65536, max_vertex=0,
-                                        expected_time=plain["time_s"])
+    guided = convergence.time_to_relmse(r, ref, target=0.01, spp_pass=4, max_time=90, guide=guide, alpha=0.6,
+                                        train_fraction=0.1, train_steps=16, batch=65536, max_vertex=0,
+                                        expected_time=plain["time_s"], spp_pass_after=16)
     out["guided_vs_plain"] = {
         "workload": "indoor room 10x4x6 m, door ajar 0.1 m, outdoor 2x2 m light radiance 200, 200,036 triangles, "
                     "960x540, bounces 12",
@@ -262,8 +262,9 @@ def render_sections(args):
         "target_relmse": 0.01, "relmse": "mean (x - r)^2 / (r^2 + 1e-2) over pixels and RGB",
         "plain": {k: plain[k] for k in ("time_s", "spp", "relmse", "reached")},
         "guided": {k: guided[k] for k in ("time_s", "spp", "relmse", "reached")},
-        "guided_settings": {"alpha": 0.5, "train_fraction_of_plain_time": 0.25, "adam_steps_per_pass": 16,
-                            "batch": 65536, "target": "incident radiance x BSDF cosine", "guided_vertices": "all"},
+        "guided_settings": {"alpha": 0.6, "train_fraction_of_plain_time": 0.1, "adam_steps_per_wave": 16,
+                            "batch": 65536, "spp_per_pass": "4 while training, then 16",
+                            "target": "incident radiance x BSDF cosine", "guided_vertices": "all"},
         "speedup_wall_time": plain["time_s"] / guided["time_s"] if guided["reached"] and plain["reached"] else None,
         "speedup_samples": plain["spp"] / guided["spp"] if guided["reached"] and plain["reached"] else None,
     }

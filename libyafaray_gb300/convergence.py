@@ -36,10 +36,12 @@ def relmse_device(film_sum, spp, ref):
 
 
 def time_to_relmse(renderer, ref, target=0.01, spp_pass=4, max_time=60.0, guide=None, alpha=0.6,
-                   train_fraction=0.25, train_steps=16, batch=65536, max_vertex=2, expected_time=None, seed=1000):
+                   train_fraction=0.25, train_steps=16, batch=65536, max_vertex=2, expected_time=None, seed=1000,
+                   spp_pass_after=None):
     """Returns dict(time_s, spp, relmse, reached, curve).  expected_time sets
     the training window for guided runs (train while elapsed < train_fraction
-    x expected_time); defaults to max_time."""
+    x expected_time); defaults to max_time.  spp_pass_after: samples per pass
+    once training has stopped (default spp_pass)."""
     import torch
     c = renderer.scene["camera"]
     n = int(c["resx"]) * int(c["resy"]) * 3
@@ -55,12 +57,13 @@ def time_to_relmse(renderer, ref, target=0.01, spp_pass=4, max_time=60.0, guide=
             renderer.render_device(spp_pass, film.data_ptr(), base_offset=spp, seed=seed + step)
         else:
             training = t_acc < window
-            renderer.render_device(spp_pass, film.data_ptr(), base_offset=spp, seed=seed + step, guide=guide,
+            n = spp_pass if training or not spp_pass_after else spp_pass_after
+            renderer.render_device(n, film.data_ptr(), base_offset=spp, seed=seed + step, guide=guide,
                                    alpha=0.0 if step == 0 else alpha, train_steps=train_steps if training else 0,
                                    batch=batch, max_vertex=max_vertex)
         torch.cuda.synchronize()
         t_acc += time.perf_counter() - t0
-        spp += spp_pass
+        spp += spp_pass if guide is None or training or not spp_pass_after else spp_pass_after
         step += 1
         err = relmse_device(film, spp, ref)
         curve.append((round(t_acc, 4), spp, err))
