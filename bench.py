@@ -163,6 +163,52 @@ def run_reference(args, rank, world):
     print(json.dumps(out))
 
 
+def coherent_traversal_section():
+    """The micro-benchmark's second mesh: a 2,097,152-triangle unit sphere with
+    seeded Perlin displacement (amplitude 0.05) and camera-coherent primary
+    rays at 1920x1080 (one per pixel centre), closest hit; a 20,000-ray
+    sample is checked against the oracle."""
+    import torch
+    from libyafaray_gb300 import gbrt, scenes
+    from oracle import orc
+    v, f = scenes.perlin_sphere()
+    rays = scenes.camera_rays(1920, 1080, (0.0, 0.6, 3.2), (0.0, 0.0, 0.0))
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    v_d = torch.from_numpy(v).cuda()
+    f_d = torch.from_numpy(f.view(np.int32)).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bvh = gbrt.Bvh.build_device(v_d.data_ptr(), len(v), f_d.data_ptr(), len(f), stream=sp)
+    torch.cuda.synchronize()
+    build_ms = (time.perf_counter() - t0) * 1e3
+    n = len(rays)
+    r_d = torch.from_numpy(rays).cuda()
+    h_d = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        bvh.trace_closest_device(r_d.data_ptr(), n, h_d.data_ptr(), stream=sp)
+    steps = 50
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for _ in range(steps):
+        bvh.trace_closest_device(r_d.data_ptr(), n, h_d.data_ptr(), stream=sp)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1]) / steps
+    hits = h_d.cpu().numpy()
+    prim = hits[:, 0].view(np.int32)
+    sel = np.random.default_rng(4).choice(n, 20000, replace=False)
+    o = orc.OracleScene(v, f)
+    ep, et, _, _ = o.trace(rays[sel], 0)
+    agree = float(np.mean((ep == prim[sel]) & (np.where(ep >= 0, et == hits[sel, 1], True))))
+    return {"workload": "2,097,152-triangle unit sphere, Perlin displacement amplitude 0.05 (seed 3), 1920x1080 pinhole "
+                        "primary rays (pixel centres), closest hit",
+            "bvh_build_ms": build_ms, "rays": n, "ms_per_launch": ms, "mrays_s": n / ms / 1e3,
+            "hit_fraction": float((prim >= 0).mean()),
+            "oracle_sample_agreement": agree, "oracle_sample": 20000}
+
+
 def render_sections(args):
     """Cornell path tracing throughput and the guided-vs-plain time to
     relMSE 0.01 on the indoor scene (against an FP64-accumulated plain
@@ -251,10 +297,15 @@ def render_sections(args):
     ref = convergence.reference_image(r, spp=args.ref_spp)
     ref_s = time.perf_counter() - t0
     plain = convergence.time_to_relmse(r, ref, target=0.01, spp_pass=16, max_time=90)
-    guide = r.make_guide()
-    guided = convergence.time_to_relmse(r, ref, target=0.01, spp_pass=4, max_time=90, guide=guide, alpha=0.6,
-                                        train_fraction=0.1, train_steps=16, batch=65536, max_vertex=0,
-                                        expected_time=plain["time_s"], spp_pass_after=16)
+    runs = {}
+    for frac in (0.25, 0.1):
+        guide = r.make_guide()
+        runs[frac] = convergence.time_to_relmse(r, ref, target=0.01, spp_pass=4, max_time=90, guide=guide,
+                                                alpha=0.6, train_fraction=frac, train_steps=16, batch=65536,
+                                                max_vertex=0, expected_time=plain["time_s"], spp_pass_after=16)
+        del guide
+    guided, short = runs[0.25], runs[0.1]
+    ok = plain["reached"]
     out["guided_vs_plain"] = {
         "workload": "indoor room 10x4x6 m, door ajar 0.1 m, outdoor 2x2 m light radiance 200, 200,036 triangles, "
                     "960x540, bounces 12",
@@ -262,11 +313,15 @@ def render_sections(args):
         "target_relmse": 0.01, "relmse": "mean (x - r)^2 / (r^2 + 1e-2) over pixels and RGB",
         "plain": {k: plain[k] for k in ("time_s", "spp", "relmse", "reached")},
         "guided": {k: guided[k] for k in ("time_s", "spp", "relmse", "reached")},
-        "guided_settings": {"alpha": 0.6, "train_fraction_of_plain_time": 0.1, "adam_steps_per_wave": 16,
+        "guided_settings": {"alpha": 0.6, "train_fraction_of_plain_time": 0.25, "adam_steps_per_wave": 16,
                             "batch": 65536, "spp_per_pass": "4 while training, then 16",
                             "target": "incident radiance x BSDF cosine", "guided_vertices": "all"},
-        "speedup_wall_time": plain["time_s"] / guided["time_s"] if guided["reached"] and plain["reached"] else None,
-        "speedup_samples": plain["spp"] / guided["spp"] if guided["reached"] and plain["reached"] else None,
+        "speedup_wall_time": plain["time_s"] / guided["time_s"] if guided["reached"] and ok else None,
+        "speedup_samples": plain["spp"] / guided["spp"] if guided["reached"] and ok else None,
+        "guided_training_10pct": {**{k: short[k] for k in ("time_s", "spp", "relmse", "reached")},
+                                  "train_fraction_of_plain_time": 0.1,
+                                  "speedup_wall_time": plain["time_s"] / short["time_s"] if short["reached"] and ok
+                                  else None},
     }
     return out
 
@@ -382,6 +437,8 @@ def main():
                "ms_per_step": e2e_s * 1e3, "gpu_launches_per_step": (args.rays + (1 << 21) - 1) >> 21}
 
     render = None if args.no_render else render_sections(args)
+    if render is not None:
+        render["traversal_coherent_2M"] = coherent_traversal_section()
 
     if rank != 0:
         if dist:

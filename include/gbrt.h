@@ -337,6 +337,13 @@ int gbrt_dl_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const
  * deposit order; n_photons and n_paths as PhotonMap::nPhotons / nPaths. */
 int gbrt_pm_photons(gbrt_scene *scene, const gbrt_pm_params *pm, int which, float *out, uint32_t capacity, uint32_t *n_photons,
                     uint32_t *n_paths);
+/* Diagnostic: the photon grid's bucket of each of n host points (xyz) with
+ * the reference HashGrid's cell assignment (src/photon/hashgrid.cc:59-75):
+ * cell coordinates |int((p - box_lo) x float(1 / cell_size))|, bucket
+ * (ix 73856093 ^ iy 19349663 ^ iz 83492791) mod grid_size.  The photon
+ * maps are bucketed this way with grid_size = the photon count (at least
+ * 1024) and cell_size a hair above the search radius. */
+int gbrt_grid_buckets(const float *points, uint32_t n, double cell_size, uint32_t grid_size, const float box_lo[3], uint32_t *bucket_out);
 /* Diagnostic: k-nearest gather of PhotonMap::gather semantics over n host
  * points (xyz) for m host queries through the device grid (cell edge >= the
  * search radius): per query the count, the final squared radius and the

@@ -2021,7 +2021,7 @@ __global__ void k_grid_count(const float4 *__restrict__ pos, uint32_t n, gbrt::P
 		const float p[3] = {q.x, q.y, q.z};
 		int c[3];
 		gbrt::grid_cell(g, p, c);
-		const uint32_t b = gbrt::grid_bucket(c[0], c[1], c[2], g.mask);
+		const uint32_t b = gbrt::grid_bucket(c[0], c[1], c[2], g.buckets);
 		key[i] = b;
 		atomicAdd(cnt + b, 1u);
 	}
@@ -2085,6 +2085,18 @@ __global__ void __launch_bounds__(1024) k_scan_totals(uint32_t *__restrict__ t, 
 __global__ void k_scan_add(uint32_t *__restrict__ data, uint32_t n, const uint32_t *__restrict__ totals)
 {
 	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) data[i] += totals[i / 4096u];
+}
+
+// HashGrid bucket of each point (test entry for the cell assignment).
+__global__ void k_grid_buckets(gbrt::PhotonGrid g, const float *__restrict__ p, uint32_t n, uint32_t *__restrict__ out)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	{
+		const float q[3] = {p[3ull * i], p[3ull * i + 1], p[3ull * i + 2]};
+		int c[3];
+		gbrt::grid_cell(g, q, c);
+		out[i] = gbrt::grid_bucket(c[0], c[1], c[2], g.buckets);
+	}
 }
 
 // kNN over a grid of bare points (test entry): counts, final r^2, indices
@@ -2311,8 +2323,8 @@ struct GridStore {
 int build_grid(const float4 *pos, const float4 *dir, const float4 *col, uint32_t n, float cell, const float lo[3], int n_sm,
                GridStore &G, cudaStream_t s)
 {
-	uint32_t T = 1024;
-	while(T < n && T < (1u << 27)) T <<= 1;
+	// buckets: the photon count (HashGrid's grid_size is a free parameter), at least 1024
+	const uint32_t T = std::max<uint32_t>(1024u, std::min<uint32_t>(n, 1u << 27));
 	const uint32_t words = T + 1, nblk = (words + 4095u) / 4096u;
 	if(int rc = G.pos.alloc(16ull * n)) return rc;
 	if(dir) if(int rc = G.dir.alloc(16ull * n)) return rc;
@@ -2329,10 +2341,12 @@ int build_grid(const float4 *pos, const float4 *dir, const float4 *col, uint32_t
 	g.dir = dir ? G.dir.as<float4>() : nullptr;
 	g.col = col ? G.col.as<float4>() : nullptr;
 	g.start = G.start.as<uint32_t>();
-	g.mask = T - 1u;
+	g.buckets = T;
 	g.n = n;
 	for(int a = 0; a < 3; ++a) g.lo[a] = lo[a];
-	g.inv_cell = 1.f / cell;
+	// a hair wider than the largest query radius, so float rounding of the cell
+	// coordinates never puts a photon within the radius two cells away
+	g.inv_cell = static_cast<float>(1.0 / (static_cast<double>(cell) * (1.0 + 1.0 / 1024.0)));
 	if(n)
 		k_grid_count<<<grid_for(n, n_sm), kThreads, 0, s>>>(pos, n, g, G.key.as<uint32_t>(), G.start.as<uint32_t>());
 	k_scan_local<<<nblk, 1024, 0, s>>>(G.start.as<uint32_t>(), words, G.totals.as<uint32_t>());
@@ -3206,6 +3220,25 @@ int gbrt_dl_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 	const int rc = render_locked(S, camera, *params, &M, film_dev, film64_dev, stats, s);
 	cudaStreamSynchronize(s);
 	return rc;
+}
+
+int gbrt_grid_buckets(const float *points, uint32_t n, double cell_size, uint32_t grid_size, const float box_lo[3], uint32_t *bucket_out)
+{
+	if((n && (!points || !bucket_out)) || !box_lo || !(cell_size > 0.0) || grid_size == 0)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_grid_buckets: bad argument");
+	if(n == 0) return GBRT_OK;
+	gbrt::PhotonGrid g{};
+	g.buckets = grid_size;
+	for(int a = 0; a < 3; ++a) g.lo[a] = box_lo[a];
+	g.inv_cell = static_cast<float>(1.0 / cell_size);
+	DevBuf dp, db;
+	if(int rc = dp.alloc(12ull * n)) return rc;
+	if(int rc = db.alloc(4ull * n)) return rc;
+	GBRT_CK(cudaMemcpy(dp.p, points, 12ull * n, cudaMemcpyHostToDevice));
+	k_grid_buckets<<<(n + 127) / 128, 128>>>(g, dp.as<float>(), n, db.as<uint32_t>());
+	GBRT_CK(cudaGetLastError());
+	GBRT_CK(cudaMemcpy(bucket_out, db.p, 4ull * n, cudaMemcpyDeviceToHost));
+	return GBRT_OK;
 }
 
 } // extern "C"

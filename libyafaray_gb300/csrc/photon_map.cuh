@@ -12,9 +12,12 @@
 // Both return the same photon sets as the kd-tree walk (ties at exactly equal
 // distances aside); only the order of the found photons differs, which the
 // estimators sum over.  Grid: cells of edge >= the query radius, so a query
-// visits the 27 cells around its own; cells hash into a power-of-two bucket
-// table, photons are sorted by bucket (counting sort), and a bucket shared by
-// two of the 27 cells is visited once.
+// visits the 27 cells around its own.  Cell coordinates and the bucket of a
+// cell are the reference's HashGrid (src/photon/hashgrid.cc:59-75,
+// include/photon/hashgrid.h:48-51): |int((p - box.a) x float(1 / cell))| per
+// axis and (ix 73856093 ^ iy 19349663 ^ iz 83492791) mod the bucket count.
+// Photons are sorted by bucket (counting sort); a bucket shared by two of
+// the 27 cells is visited once.
 #pragma once
 
 #include <cstdint>
@@ -26,25 +29,27 @@ struct PhotonGrid {
 	const float4 *pos;          // xyz; w unused
 	const float4 *dir;          // stored direction (photon: towards where it came from; radiance point: normal)
 	const float4 *col;          // rgb
-	const uint32_t *start;      // [mask + 2] bucket offsets into the sorted photons
-	uint32_t mask;              // bucket table size - 1
+	const uint32_t *start;      // [buckets + 1] bucket offsets into the sorted photons
+	uint32_t buckets;           // HashGrid grid_size
 	uint32_t n;
-	float lo[3];                // grid origin
-	float inv_cell;             // 1 / cell edge
+	float lo[3];                // HashGrid bounding_box.a
+	float inv_cell;             // float(1 / cell_size), cell_size in double
 };
 
-__host__ __device__ __forceinline__ uint32_t grid_bucket(int ix, int iy, int iz, uint32_t mask)
+// HashGrid::hash: int products wrap like the reference's, then mod grid_size.
+__host__ __device__ __forceinline__ uint32_t grid_bucket(int ix, int iy, int iz, uint32_t buckets)
 {
-	uint32_t h = static_cast<uint32_t>(ix) * 73856093u ^ static_cast<uint32_t>(iy) * 19349663u ^ static_cast<uint32_t>(iz) * 83492791u;
-	h ^= h >> 15;
-	h *= 0x2c1b3c6du;
-	h ^= h >> 12;
-	return h & mask;
+	const uint32_t h = (static_cast<uint32_t>(ix) * 73856093u) ^ (static_cast<uint32_t>(iy) * 19349663u) ^ (static_cast<uint32_t>(iz) * 83492791u);
+	return h % buckets;
 }
 
-__device__ __forceinline__ void grid_cell(const PhotonGrid &g, const float p[3], int c[3])
+__host__ __device__ __forceinline__ void grid_cell(const PhotonGrid &g, const float p[3], int c[3])
 {
-	for(int a = 0; a < 3; ++a) c[a] = static_cast<int>(floorf((p[a] - g.lo[a]) * g.inv_cell));
+	for(int a = 0; a < 3; ++a)
+	{
+		const int i = static_cast<int>((p[a] - g.lo[a]) * g.inv_cell);
+		c[a] = i < 0 ? -i : i;
+	}
 }
 
 // Visits every distinct bucket of the 27 cells around p: f(first, end).
@@ -59,7 +64,9 @@ __device__ __forceinline__ void grid_visit(const PhotonGrid &g, const float p[3]
 		for(int dy = -1; dy <= 1; ++dy)
 			for(int dx = -1; dx <= 1; ++dx)
 			{
-				const uint32_t b = grid_bucket(c[0] + dx, c[1] + dy, c[2] + dz, g.mask);
+				// photons lie inside the box, so their cells are >= 0 on every axis
+				if(c[0] + dx < 0 || c[1] + dy < 0 || c[2] + dz < 0) continue;
+				const uint32_t b = grid_bucket(c[0] + dx, c[1] + dy, c[2] + dz, g.buckets);
 				bool dup = false;
 				for(int i = 0; i < ns; ++i) dup |= seen[i] == b;
 				if(dup) continue;

@@ -144,6 +144,7 @@ SIGNATURES = {
     "gbrt_dl_render_host": (_I, [_VP, _VP, _VP, _VP, _VP, _VP]),
     "gbrt_pm_photons": (_I, [_VP, _VP, ctypes.c_int, _VP, _U32, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]),
     "gbrt_knn_gather": (_I, [_VP, _U32, _VP, _U32, ctypes.c_float, ctypes.c_int, ctypes.c_float, _VP, _VP, _VP]),
+    "gbrt_grid_buckets": (_I, [_VP, _U32, ctypes.c_double, _U32, _VP, _VP]),
     "gbrt_pt_render": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP, _VP,
                             ctypes.POINTER(PtStats), _VP]),
     "gbrt_pt_render_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP,
@@ -556,3 +557,12 @@ def render_batch(renderers, spp, film_ptrs, concurrency=8, base_offset=0, seed=1
     check(load().gbrt_pt_render_batch(S, cams, ps, F, n, int(concurrency), st))
     return [{"camera_samples": x.camera_samples, "extension_rays": x.extension_rays, "shadow_rays": x.shadow_rays,
              "ms": x.ms} for x in st]
+
+
+def grid_buckets(points, cell_size, grid_size, box_lo):
+    """Bucket of each point under the reference HashGrid's cell assignment."""
+    P = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    lo = (ctypes.c_float * 3)(*[float(x) for x in box_lo])
+    out = np.empty(len(P), np.uint32)
+    check(load().gbrt_grid_buckets(_ptr(P), len(P), float(cell_size), int(grid_size), lo, _ptr(out)))
+    return out

@@ -97,6 +97,46 @@ def cornell_mesh(as_quads=True):
     return verts, faces, np.array(G, np.int32)
 
 
+def perlin_noise(p, seed=3):
+    """Improved Perlin gradient noise (Perlin 2002: quintic fade, 12 edge
+    gradients, seeded permutation) at points p [n, 3]; values in about [-1, 1]."""
+    perm = np.random.default_rng(seed).permutation(256)
+    perm = np.concatenate([perm, perm])
+    grads = np.array([[1, 1, 0], [-1, 1, 0], [1, -1, 0], [-1, -1, 0], [1, 0, 1], [-1, 0, 1], [1, 0, -1], [-1, 0, -1],
+                      [0, 1, 1], [0, -1, 1], [0, 1, -1], [0, -1, -1]], np.float64)
+    p = np.asarray(p, np.float64)
+    pi = np.floor(p).astype(np.int64)
+    f = p - pi
+    pi &= 255
+    fade = f * f * f * (f * (f * 6.0 - 15.0) + 10.0)
+
+    def grad(ix, iy, iz, dx, dy, dz):
+        h = perm[perm[perm[ix] + iy] + iz] % 12
+        g = grads[h]
+        return g[:, 0] * dx + g[:, 1] * dy + g[:, 2] * dz
+    x, y, z = pi[:, 0], pi[:, 1], pi[:, 2]
+    fx, fy, fz = f[:, 0], f[:, 1], f[:, 2]
+    c = {}
+    for a in (0, 1):
+        for b in (0, 1):
+            for d in (0, 1):
+                c[a, b, d] = grad(x + a, y + b, z + d, fx - a, fy - b, fz - d)
+    lerp = lambda t, u, v: u + t * (v - u)
+    x00 = lerp(fade[:, 0], c[0, 0, 0], c[1, 0, 0]); x10 = lerp(fade[:, 0], c[0, 1, 0], c[1, 1, 0])
+    x01 = lerp(fade[:, 0], c[0, 0, 1], c[1, 0, 1]); x11 = lerp(fade[:, 0], c[0, 1, 1], c[1, 1, 1])
+    return lerp(fade[:, 2], lerp(fade[:, 1], x00, x10), lerp(fade[:, 1], x01, x11))
+
+
+def perlin_sphere(nu=2048, nv=512, amplitude=0.05, frequency=4.0, seed=3):
+    """Unit sphere tessellated into nu x nv quads (2 nu nv triangles: 2,097,152
+    at the defaults) displaced along the normal by amplitude x Perlin noise.
+    Returns (vertices float32 [n, 3], faces uint32 [m, 4] TRI-marked)."""
+    P, F = uv_sphere((0.0, 0.0, 0.0), 1.0, nu, nv)
+    n = P / np.maximum(np.linalg.norm(P, axis=1, keepdims=True), 1e-12)
+    P = n * (1.0 + amplitude * perlin_noise(n * frequency + 17.0, seed))[:, None]
+    return P.astype(np.float32), np.concatenate([F, np.full((len(F), 1), TRI)], 1).astype(np.uint32)
+
+
 def camera_rays(width, height, eye, target, up=(0.0, 1.0, 0.0), fov_deg=40.0, seed=None):
     """Pinhole primary rays through pixel centres (or jittered when seed is
     given), one per pixel, row-major from the top-left."""

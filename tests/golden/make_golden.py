@@ -65,6 +65,7 @@ def run_case(name, verts, faces, rays):
 
 
 def main():
+    only = sys.argv[1:]
     if not orc.reference_available():
         sys.exit("oracle/_ref/kdtree_dump missing: run make -C oracle/ref first")
     # 1. triangle soup, the traversal micro-benchmark's distribution, small
@@ -99,6 +100,12 @@ def main():
     r[::3, 6] = 1.0   # pointing away
     r[::5, 2] = 0.0; r[::5, 4] = 1.0; r[::5, 6] = 0.0  # in-plane rays
     run_case("single_tri", v, f, r)
+    # 5. displaced sphere (Perlin amplitude 0.05), the micro-benchmark's second
+    # mesh at 16k triangles: camera-coherent primary rays + random rays
+    v, f = scenes.perlin_sphere(128, 64)
+    cam = scenes.camera_rays(96, 54, (0.0, 0.6, 3.2), (0.0, 0.0, 0.0), seed=16)
+    r = np.concatenate([cam, scenes.random_rays(2048, seed=17, lo=-1.5, hi=1.5), edge_rays(v, f, 512, seed=18)])
+    run_case("perlin_sphere_16k", v, f, r)
 
 
 if __name__ == "__main__":

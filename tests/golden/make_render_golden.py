@@ -73,6 +73,33 @@ def render_golden(res=64, spp=16, batches=32, glossy=False):
     print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
 
 
+HASHGRID = os.path.join(ROOT, "oracle", "_ref", "hashgrid_dump")
+
+
+def hashgrid_golden():
+    """hashgrid.npz: the reference HashGrid's bucket (updateGrid) of every
+    photon of photons_small.npz, for two cell sizes and grid sizes, box a =
+    the photons' own minimum corner."""
+    g = np.load(os.path.join(OUT, "photons_small.npz"))
+    pos = np.concatenate([g["diffuse"][:, 3:6], g["caustic"][:, 3:6]]).astype(np.float32)
+    lo = pos.min(0) - np.float32(0.001)
+    hi = pos.max(0) + np.float32(0.001)
+    cases = [(0.02 * (1.0 + 1.0 / 1024.0), 1700), (0.05, 1024), (0.3, 97)]
+    out = {"pos": pos, "lo": lo}
+    for i, (cell, size) in enumerate(cases):
+        with tempfile.TemporaryDirectory() as d:
+            fi, fo = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
+            with open(fi, "wb") as f:
+                f.write(struct.pack("<dI", cell, size) + np.concatenate([lo, hi]).astype(np.float32).tobytes()
+                        + struct.pack("<I", len(pos)) + pos.tobytes())
+            subprocess.run([HASHGRID, fi, fo], check=True)
+            out[f"bucket{i}"] = np.frombuffer(open(fo, "rb").read(), np.uint32).copy()
+        out[f"cell{i}"] = np.float64(cell)
+        out[f"size{i}"] = np.uint32(size)
+    np.savez_compressed(os.path.join(OUT, "hashgrid.npz"), **out)
+    print(f"hashgrid.npz: {len(pos)} points, {len(cases)} cases")
+
+
 def variant_golden(name, res=64, spp=16, batches=32, **kw):
     """Cornell variants: glass (glass + rough-glass spheres, the recursive
     split) and point (a pointlight instead of the area light)."""
@@ -181,6 +208,8 @@ if __name__ == "__main__":
         variant_golden("cornell_glass_64_render.npz", glass=True)
     if "pm" in what:
         pm_golden()
+    if "hashgrid" in what:
+        hashgrid_golden()
     if "dl" in what:
         dl_golden()
     if "batch" in what:

@@ -162,3 +162,12 @@ def test_directlighting_caustics_matches_reference(cuda_device):
     print(f"directlighting glass cornell 48x48: {100 * frac:.2f}% agree, relMSE {relmse:.3g}, "
           f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
     assert frac >= 0.99
+
+
+def test_grid_cell_assignment_matches_reference_hashgrid(cuda_device):
+    """The photon grid puts every photon in the bucket the reference's
+    HashGrid::updateGrid puts it (cell coordinates and hash, bit for bit)."""
+    g = np.load(os.path.join(GOLD, "hashgrid.npz"))
+    for i in range(3):
+        got = gbrt.grid_buckets(g["pos"], float(g[f"cell{i}"]), int(g[f"size{i}"]), g["lo"])
+        assert np.array_equal(got, g[f"bucket{i}"]), f"case {i}: {np.count_nonzero(got != g[f'bucket{i}'])} photons differ"

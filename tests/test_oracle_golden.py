@@ -9,7 +9,7 @@ import pytest
 from oracle import orc
 from tests import parity
 
-TRAVERSAL_CASES = ["cornell_quads", "cornell_tris", "single_tri", "tri_soup_4k", "tri_soup_dense"]
+TRAVERSAL_CASES = ["cornell_quads", "cornell_tris", "single_tri", "tri_soup_4k", "tri_soup_dense", "perlin_sphere_16k"]
 GOLDEN = [os.path.join(os.path.dirname(__file__), "golden", n + ".npz") for n in TRAVERSAL_CASES]
 
 
