@@ -68,8 +68,12 @@ typedef struct gbrt_build_params {
 	uint32_t max_leaf_size;   /* 1..16; 0 = default (4) */
 	float traversal_cost;     /* SAH cost of a node visit; 0 = default (1.0) */
 	float intersect_cost;     /* SAH cost of a primitive test; 0 = default (1.0) */
-	uint32_t flags;           /* reserved, 0 */
+	uint32_t flags;           /* GBRT_BUILD_* bits; 0 = default */
 } gbrt_build_params;
+
+/* gbrt_build_params.flags: skip the treelet restructuring passes (plain
+ * LBVH topology; for comparisons). */
+#define GBRT_BUILD_NO_TREELETS 1u
 
 typedef struct gbrt_bvh_info {
 	uint32_t n_prims;
@@ -91,8 +95,10 @@ int gbrt_device_count(int *count);
 /* BVH build.  Replaces the kd-tree construction that Accelerator::factory
  * runs from Scene::preprocess (src/scene/scene.cc:347,
  * src/accelerator/accelerator.cc:44-55, accelerator_kdtree_original.cc:65-141).
- * LBVH: Morton codes, radix sort, Karras hierarchy, bottom-up refit with an
- * SAH leaf-collapse.  Device-resident inputs. */
+ * LBVH: Morton codes, radix sort, Karras hierarchy, SAH treelet
+ * restructuring (optimal 7-leaf treelets, bottom-up, three passes), bottom-up
+ * refit with an SAH leaf-collapse, then the 8-wide compressed copy the
+ * traversal walks.  Device-resident inputs. */
 int gbrt_bvh_build(const float *vertices_dev, uint32_t n_vertices,
                    const uint32_t *faces_dev, uint32_t n_faces,
                    const gbrt_build_params *params, void *stream, gbrt_bvh **out);
@@ -148,6 +154,15 @@ int gbrt_bvh_get_info(const gbrt_bvh *bvh, gbrt_bvh_info *info);
  * Layout: see libyafaray_gb300/csrc/gbrt_internal.cuh.  Synchronises. */
 int gbrt_bvh_export(const gbrt_bvh *bvh, void *nodes, size_t nodes_bytes, void *prims, size_t prims_bytes,
                     uint32_t *ids, size_t ids_bytes);
+
+/* Copies the 8-wide compressed hierarchy the traversal walks (for
+ * validation tools): *n_nodes and *depth receive its node count and depth;
+ * nodes: 80 bytes per node (room for max(n_prims - 1, 1) nodes is always
+ * enough), prims: 48 bytes and ids: 4 bytes per primitive, in wide-leaf
+ * order.  Any buffer may be NULL to skip it.  Layout: see
+ * libyafaray_gb300/csrc/gbrt_internal.cuh.  Synchronises. */
+int gbrt_bvh_export_wide(const gbrt_bvh *bvh, uint32_t *n_nodes, uint32_t *depth, void *nodes, size_t nodes_bytes,
+                         void *prims, size_t prims_bytes, uint32_t *ids, size_t ids_bytes);
 
 /* Closest hit for n rays: Accelerator::intersect(ray, camera)
  * (accelerator.h:89-101 -> kdtree::intersect<Nearest>,

@@ -13,8 +13,23 @@
 //   6. k_refit       bottom-up boxes, primitive counts and SAH costs; a node
 //                    becomes a leaf when that is cheaper and it holds <= max
 //                    leaf size primitives
-//   7. k_emit_nodes  64-byte nodes holding both children's boxes
-//   8. k_emit_prims  48-byte primitive records in leaf order
+//   7. k_treelet     SAH treelet restructuring (Karras & Aila, "Fast
+//                    parallel construction of high-quality bounding volume
+//                    hierarchies", HPG 2013): bottom-up, every node over
+//                    gamma primitives rebuilds the optimal binary tree over
+//                    its 7-leaf treelet by dynamic programming over leaf
+//                    subsets; three passes, then k_refit again
+//   8. k_order_*     leaf slots in depth-first order (every subtree's
+//                    primitives contiguous after restructuring)
+//   9. k_emit_nodes  64-byte binary nodes holding both children's boxes
+//  10. k_emit_prims  48-byte primitive records in leaf order
+//  11. k_wide_level  8-wide compressed hierarchy for the traversal, one
+//                    launch per level (layout in gbrt_internal.cuh), after
+//                    Ylitie, Karras & Laine, "Efficient incoherent ray
+//                    traversal on GPUs through compressed wide BVHs", HPG
+//                    2017: greedy collapse of the binary tree (open the
+//                    largest-area child until 8), 8-bit child planes on a
+//                    per-node power-of-two grid, slots by ray octant
 #include "gbrt_internal.cuh"
 
 #include <cfloat>
@@ -29,6 +44,15 @@ constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr uint32_t kNoParent = 0xFFFFFFFFu;
+// Upper bound on any leaf-to-root walk; a longer walk means a broken
+// hierarchy: the walk stops and raises GBRT_META_ERR bit 4.
+constexpr int kMaxWalk = 1 << 14;
+constexpr uint32_t kErrWalk = 4u, kErrWide = 8u;
+
+__device__ __forceinline__ void raise_err(float *meta, uint32_t bit)
+{
+	atomicOr(reinterpret_cast<uint32_t *>(meta) + GBRT_META_ERR, bit);
+}
 
 __device__ __forceinline__ uint32_t f2ord(float f)
 {
@@ -297,17 +321,18 @@ __device__ __forceinline__ float half_area(float4 lo, float4 hi)
 __global__ void k_refit(const uint32_t *__restrict__ vals, int n, const float4 *__restrict__ box_lo, const float4 *__restrict__ box_hi,
                         const uint2 *__restrict__ child, const uint32_t *__restrict__ parent_int, const uint32_t *__restrict__ parent_leaf,
                         float4 *node_lo, float4 *node_hi, uint32_t *flags, uint8_t *collapse,
-                        uint32_t max_leaf, float ct, float ci)
+                        uint32_t max_leaf, float ct, float ci, float *meta)
 {
 	const int j = blockIdx.x * blockDim.x + threadIdx.x;
 	if(j >= n) return;
-	uint32_t p = parent_leaf[j];
-	while(p != kNoParent)
+	uint32_t p = __ldcg(parent_leaf + j);
+	for(int walk = 0; p != kNoParent; ++walk)
 	{
+		if(walk == kMaxWalk) { raise_err(meta, kErrWalk); return; }
 		__threadfence();
 		if(atomicAdd(&flags[p], 1u) == 0u) return;
 		__threadfence();
-		const uint2 c = child[p];
+		const uint2 c = __ldcg(child + p);
 		float4 lo[2], hi[2];
 		float cost[2];
 		uint32_t cnt[2];
@@ -341,8 +366,209 @@ __global__ void k_refit(const uint32_t *__restrict__ vals, int n, const float4 *
 		__stcg(&node_lo[p], L);
 		__stcg(&node_hi[p], H);
 		collapse[p] = leaf ? 1 : 0;
+		p = __ldcg(parent_int + p);
+	}
+}
+
+// ---- treelet restructuring -------------------------------------------------
+constexpr int kTreeletLeaves = 7;
+constexpr uint32_t kTreeletSubsets = 1u << kTreeletLeaves;
+
+// Box, SAH cost and primitive count of a child reference.  Internal nodes are
+// rewritten by other threads of the same launch: read them through L2.
+__device__ __forceinline__ void ref_info(uint32_t ref, const uint32_t *__restrict__ vals, const float4 *__restrict__ box_lo,
+                                         const float4 *__restrict__ box_hi, const float4 *node_lo, const float4 *node_hi, float ci,
+                                         float4 &lo, float4 &hi, float &cost, uint32_t &cnt)
+{
+	if(ref & GBRT_LEAF_BIT)
+	{
+		const uint32_t prim = __ldg(vals + (ref & ~GBRT_LEAF_BIT));
+		lo = __ldg(box_lo + prim); hi = __ldg(box_hi + prim);
+		cost = ci * half_area(lo, hi);
+		cnt = 1u;
+	}
+	else
+	{
+		lo = __ldcg(node_lo + ref); hi = __ldcg(node_hi + ref);
+		cost = lo.w;
+		cnt = __float_as_uint(hi.w);
+	}
+}
+
+// Rebuilds the treelet under `root` as the SAH-optimal binary tree over the
+// same leaves, reusing its internal node indices.
+__device__ __noinline__ void restructure(uint32_t root, const uint32_t *__restrict__ vals, const float4 *__restrict__ box_lo,
+                                         const float4 *__restrict__ box_hi, uint2 *child, uint32_t *parent_int, uint32_t *parent_leaf,
+                                         float4 *node_lo, float4 *node_hi, uint32_t max_leaf, float ct, float ci)
+{
+	uint32_t T[kTreeletLeaves], I[kTreeletLeaves - 1], cnt[kTreeletLeaves];
+	float4 lo[kTreeletLeaves], hi[kTreeletLeaves];
+	float cost[kTreeletLeaves];
+	int m = 2, ni = 1;
+	I[0] = root;
+	{
+		const uint2 c = __ldcg(child + root);
+		T[0] = c.x; T[1] = c.y;
+		ref_info(c.x, vals, box_lo, box_hi, node_lo, node_hi, ci, lo[0], hi[0], cost[0], cnt[0]);
+		ref_info(c.y, vals, box_lo, box_hi, node_lo, node_hi, ci, lo[1], hi[1], cost[1], cnt[1]);
+	}
+	// grow the treelet: open the internal leaf of largest area
+	while(m < kTreeletLeaves)
+	{
+		int best = -1;
+		float ba = -1.f;
+		for(int k = 0; k < m; ++k)
+			if(!(T[k] & GBRT_LEAF_BIT))
+			{
+				const float a = half_area(lo[k], hi[k]);
+				if(a > ba) { ba = a; best = k; }
+			}
+		if(best < 0) break;
+		const uint32_t r = T[best];
+		I[ni++] = r;
+		const uint2 c = __ldcg(child + r);
+		T[best] = c.x;
+		ref_info(c.x, vals, box_lo, box_hi, node_lo, node_hi, ci, lo[best], hi[best], cost[best], cnt[best]);
+		T[m] = c.y;
+		ref_info(c.y, vals, box_lo, box_hi, node_lo, node_hi, ci, lo[m], hi[m], cost[m], cnt[m]);
+		++m;
+	}
+	if(m < 3) return;
+	// optimal cost of every leaf subset: c(S) = min(Ci A(S) N(S) [N <= max leaf],
+	// Ct A(S) + min over splits P of c(P) + c(S \ P))
+	const uint32_t full = (1u << m) - 1u;
+	float C[kTreeletSubsets];
+	uint8_t split[kTreeletSubsets];
+	for(uint32_t S = 1; S <= full; ++S)
+	{
+		if(!(S & (S - 1u))) { C[S] = cost[__ffs(S) - 1]; split[S] = 0; continue; }
+		float4 L = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f), H = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
+		uint32_t N = 0;
+		for(int k = 0; k < m; ++k)
+			if((S >> k) & 1u)
+			{
+				L.x = fminf(L.x, lo[k].x); L.y = fminf(L.y, lo[k].y); L.z = fminf(L.z, lo[k].z);
+				H.x = fmaxf(H.x, hi[k].x); H.y = fmaxf(H.y, hi[k].y); H.z = fmaxf(H.z, hi[k].z);
+				N += cnt[k];
+			}
+		const float A = half_area(L, H);
+		const uint32_t low = S & (0u - S);
+		float best = FLT_MAX;
+		uint32_t bp = low;
+		for(uint32_t P = (S - 1u) & S; P; P = (P - 1u) & S)
+			if(P & low)
+			{
+				const float c = C[P] + C[S ^ P];
+				if(c < best) { best = c; bp = P; }
+			}
+		const float c_int = ct * A + best;
+		const float c_leaf = N <= max_leaf ? ci * A * static_cast<float>(N) : FLT_MAX;
+		C[S] = c_leaf <= c_int ? c_leaf : c_int;
+		split[S] = static_cast<uint8_t>(bp);
+	}
+	// rewrite: the root keeps its index, the other internal nodes are reused
+	uint32_t stS[kTreeletLeaves], stN[kTreeletLeaves];
+	uint32_t ordS[kTreeletLeaves], ordN[kTreeletLeaves];
+	int sp = 1, no = 0, next = 1;
+	stS[0] = full; stN[0] = root;
+	while(sp > 0)
+	{
+		--sp;
+		const uint32_t S = stS[sp], nd = stN[sp];
+		ordS[no] = S; ordN[no] = nd; ++no;
+		const uint32_t sub[2] = {split[S], S ^ split[S]};
+		uint32_t ref[2];
+		for(int k = 0; k < 2; ++k)
+		{
+			if(!(sub[k] & (sub[k] - 1u))) ref[k] = T[__ffs(sub[k]) - 1];
+			else { ref[k] = I[next++]; stS[sp] = sub[k]; stN[sp] = ref[k]; ++sp; }
+			if(ref[k] & GBRT_LEAF_BIT) parent_leaf[ref[k] & ~GBRT_LEAF_BIT] = nd;
+			else parent_int[ref[k]] = nd;
+		}
+		child[nd] = make_uint2(ref[0], ref[1]);
+	}
+	for(int q = 0; q < no; ++q)
+	{
+		const uint32_t S = ordS[q];
+		float4 L = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f), H = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
+		uint32_t N = 0;
+		for(int k = 0; k < m; ++k)
+			if((S >> k) & 1u)
+			{
+				L.x = fminf(L.x, lo[k].x); L.y = fminf(L.y, lo[k].y); L.z = fminf(L.z, lo[k].z);
+				H.x = fmaxf(H.x, hi[k].x); H.y = fmaxf(H.y, hi[k].y); H.z = fmaxf(H.z, hi[k].z);
+				N += cnt[k];
+			}
+		L.w = C[S];
+		H.w = __uint_as_float(N);
+		node_lo[ordN[q]] = L;
+		node_hi[ordN[q]] = H;
+	}
+}
+
+// Bottom-up like k_refit: the second thread to reach a node owns it, and its
+// whole subtree is final.  Nodes holding at least gamma primitives are
+// restructured.
+__global__ void k_treelet(int n, const uint32_t *__restrict__ vals, const float4 *__restrict__ box_lo, const float4 *__restrict__ box_hi,
+                          uint2 *child, uint32_t *parent_int, uint32_t *parent_leaf, float4 *node_lo, float4 *node_hi,
+                          uint32_t *flags, uint32_t gamma, uint32_t max_leaf, float ct, float ci, float *meta)
+{
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if(j >= n) return;
+	uint32_t p = __ldcg(parent_leaf + j);
+	for(int walk = 0; p != kNoParent; ++walk)
+	{
+		if(walk == kMaxWalk) { raise_err(meta, kErrWalk); return; }
+		__threadfence();
+		if(atomicAdd(&flags[p], 1u) == 0u) return;
+		__threadfence();
+		if(__float_as_uint(__ldcg(node_hi + p).w) >= gamma)
+			restructure(p, vals, box_lo, box_hi, child, parent_int, parent_leaf, node_lo, node_hi, max_leaf, ct, ci);
+		p = __ldcg(parent_int + p);
+	}
+}
+
+// ---- depth-first leaf order -------------------------------------------------
+__device__ __forceinline__ uint32_t ref_count(uint32_t ref, const float4 *__restrict__ node_hi)
+{
+	return (ref & GBRT_LEAF_BIT) ? 1u : __float_as_uint(node_hi[ref].w);
+}
+
+// Primitives before `ref` in depth-first order: the left siblings' counts
+// along the path to the root.
+__device__ __forceinline__ uint32_t dfs_offset(uint32_t ref, uint32_t p, const uint2 *__restrict__ child, const uint32_t *__restrict__ parent_int,
+                                               const float4 *__restrict__ node_hi, float *meta)
+{
+	uint32_t off = 0;
+	for(int walk = 0; p != kNoParent; ++walk)
+	{
+		if(walk == kMaxWalk) { raise_err(meta, kErrWalk); return 0u; }
+		const uint2 c = child[p];
+		if(c.y == ref) off += ref_count(c.x, node_hi);
+		ref = p;
 		p = parent_int[p];
 	}
+	return off;
+}
+
+__global__ void k_order_leaves(int n, const uint32_t *__restrict__ vals, const uint2 *__restrict__ child, const uint32_t *__restrict__ parent_int,
+                               const uint32_t *__restrict__ parent_leaf, const float4 *__restrict__ node_hi,
+                               uint32_t *__restrict__ pos_leaf, uint32_t *__restrict__ vals_out, float *meta)
+{
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if(j >= n) return;
+	const uint32_t off = dfs_offset(GBRT_LEAF_BIT | static_cast<uint32_t>(j), parent_leaf[j], child, parent_int, node_hi, meta);
+	if(off >= static_cast<uint32_t>(n)) { raise_err(meta, kErrWalk); return; }
+	pos_leaf[j] = off;
+	vals_out[off] = vals[j];
+}
+
+__global__ void k_order_nodes(int n_int, const uint2 *__restrict__ child, const uint32_t *__restrict__ parent_int,
+                              const float4 *__restrict__ node_hi, uint32_t *__restrict__ first_int, float *meta)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n_int) return;
+	first_int[i] = dfs_offset(static_cast<uint32_t>(i), parent_int[i], child, parent_int, node_hi, meta);
 }
 
 // Node boxes are grown by 2^-18 of the coordinate plus 2^-18 of the scene
@@ -359,9 +585,9 @@ __device__ __forceinline__ float grow_down(float x, float pad) { return x - (fab
 __device__ __forceinline__ float grow_up(float x, float pad) { return x + (fabsf(x) * kGrowRel + pad); }
 
 __global__ void k_emit_nodes(int n_int, const uint32_t *__restrict__ vals, const float4 *__restrict__ box_lo, const float4 *__restrict__ box_hi,
-                             const uint2 *__restrict__ child, const uint2 *__restrict__ range, const float4 *__restrict__ node_lo,
-                             const float4 *__restrict__ node_hi, const uint8_t *__restrict__ collapse, const float *__restrict__ meta,
-                             float4 *__restrict__ nodes)
+                             const uint2 *__restrict__ child, const uint32_t *__restrict__ pos_leaf, const uint32_t *__restrict__ first_int,
+                             const float4 *__restrict__ node_lo, const float4 *__restrict__ node_hi, const uint8_t *__restrict__ collapse,
+                             const float *__restrict__ meta, float4 *__restrict__ nodes)
 {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= n_int) return;
@@ -377,12 +603,12 @@ __global__ void k_emit_nodes(int n_int, const uint32_t *__restrict__ vals, const
 			const uint32_t leaf = cc[k] & ~GBRT_LEAF_BIT;
 			const uint32_t prim = vals[leaf];
 			lo[k] = box_lo[prim]; hi[k] = box_hi[prim];
-			ref[k] = gbrt_leaf_ref(leaf, 1u);
+			ref[k] = gbrt_leaf_ref(pos_leaf[leaf], 1u);
 		}
 		else
 		{
 			lo[k] = node_lo[cc[k]]; hi[k] = node_hi[cc[k]];
-			if(collapse[cc[k]]) ref[k] = gbrt_leaf_ref(range[cc[k]].x, __float_as_uint(hi[k].w));
+			if(collapse[cc[k]]) ref[k] = gbrt_leaf_ref(first_int[cc[k]], __float_as_uint(hi[k].w));
 			else ref[k] = cc[k];
 		}
 	}
@@ -434,6 +660,253 @@ __global__ void k_emit_prims(const float *__restrict__ verts, const uint32_t *__
 	ids[j] = prim | (quad ? GBRT_QUAD_BIT : 0u);
 }
 
+// ---- 8-wide compressed hierarchy -------------------------------------------
+constexpr uint32_t kWideLeafMax = 3;      // primitives per wide leaf child (unary count in 3 bits)
+constexpr int kWideLevels = GBRT_WIDE_MAX_LEVELS;
+
+struct WideSrc {
+	const uint2 *child;
+	const uint32_t *vals;          // primitive of each binary leaf (sorted order)
+	const float4 *box_lo, *box_hi;
+	const float4 *node_lo, *node_hi;
+	const uint8_t *collapse;
+	const uint32_t *pos_leaf, *first_int;
+	const float4 *tris;
+	const uint32_t *ids;
+	uint32_t n_node_cap;           // wide node slots (= task buffer entries)
+	uint32_t n_prims;
+};
+
+__device__ __forceinline__ bool wide_leaf(uint32_t ref, const WideSrc &W)
+{
+	if(ref & GBRT_LEAF_BIT) return true;
+	return W.collapse[ref] && __float_as_uint(W.node_hi[ref].w) <= kWideLeafMax;
+}
+
+__device__ __forceinline__ void ref_box(uint32_t ref, const WideSrc &W, float4 &lo, float4 &hi)
+{
+	if(ref & GBRT_LEAF_BIT)
+	{
+		const uint32_t prim = W.vals[ref & ~GBRT_LEAF_BIT];
+		lo = W.box_lo[prim]; hi = W.box_hi[prim];
+	}
+	else { lo = W.node_lo[ref]; hi = W.node_hi[ref]; }
+}
+
+__device__ __forceinline__ float axis_of(const float4 &v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
+
+__global__ void k_wide_init(float *meta, uint2 *tasks, uint32_t *counts)
+{
+	uint32_t *m = reinterpret_cast<uint32_t *>(meta);
+	m[GBRT_META_WNODES] = 1u;
+	m[GBRT_META_WPRIMS] = 0u;
+	m[GBRT_META_WDEPTH] = 0u;
+	tasks[0] = make_uint2(0u, 0u);    // binary root -> wide node 0
+	counts[0] = 1u;
+}
+
+// One thread per wide node of this level: task = (binary node, wide index).
+__global__ void __launch_bounds__(128) k_wide_level(int level, const uint2 *__restrict__ tin, uint32_t *counts, uint2 *__restrict__ tout,
+                                                    WideSrc W, float *meta, uint4 *__restrict__ wnodes, float4 *__restrict__ wtris,
+                                                    uint32_t *__restrict__ wids)
+{
+	const uint32_t n_in = counts[level];
+	if(n_in == 0) return;
+	uint32_t *m = reinterpret_cast<uint32_t *>(meta);
+	if(blockIdx.x == 0 && threadIdx.x == 0) atomicMax(m + GBRT_META_WDEPTH, static_cast<uint32_t>(level + 1));
+	const float pad = scene_pad(meta);
+	for(uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_in; t += gridDim.x * blockDim.x)
+	{
+		const uint2 task = tin[t];
+		uint32_t c[8];
+		float4 lo[8], hi[8];
+		int n = 2;
+		{
+			const uint2 cc = W.child[task.x];
+			c[0] = cc.x; c[1] = cc.y;
+			ref_box(c[0], W, lo[0], hi[0]);
+			ref_box(c[1], W, lo[1], hi[1]);
+		}
+		while(n < 8)
+		{
+			int best = -1;
+			float ba = -1.f;
+			for(int k = 0; k < n; ++k)
+				if(!wide_leaf(c[k], W))
+				{
+					const float a = half_area(lo[k], hi[k]);
+					if(a > ba) { ba = a; best = k; }
+				}
+			if(best < 0) break;
+			const uint2 rc = W.child[c[best]];
+			c[best] = rc.x; ref_box(rc.x, W, lo[best], hi[best]);
+			c[n] = rc.y; ref_box(rc.y, W, lo[n], hi[n]);
+			++n;
+		}
+		// grown child boxes (as the binary nodes) and the node's grid
+		float org[3], top[3];
+		for(int a = 0; a < 3; ++a) { org[a] = FLT_MAX; top[a] = -FLT_MAX; }
+		for(int k = 0; k < n; ++k)
+		{
+			lo[k] = make_float4(grow_down(lo[k].x, pad), grow_down(lo[k].y, pad), grow_down(lo[k].z, pad), 0.f);
+			hi[k] = make_float4(grow_up(hi[k].x, pad), grow_up(hi[k].y, pad), grow_up(hi[k].z, pad), 0.f);
+			for(int a = 0; a < 3; ++a) { org[a] = fminf(org[a], axis_of(lo[k], a)); top[a] = fmaxf(top[a], axis_of(hi[k], a)); }
+		}
+		int eb[3];
+		double scale[3];
+		for(int a = 0; a < 3; ++a)
+		{
+			const double ext = static_cast<double>(top[a]) - static_cast<double>(org[a]);
+			int e = -126;
+			if(ext > 0.0) { int x; frexp(ext / 255.0, &x); e = x; }
+			e = max(-126, min(127, e));
+			while(e < 127 && 255.0 * ldexp(1.0, e) < ext) ++e;
+			eb[a] = e + 127;
+			scale[a] = ldexp(1.0, e);
+		}
+		// slots by octant: child nearest along octant s's diagonal goes to slot s
+		float cost[8][8];
+		for(int k = 0; k < n; ++k)
+		{
+			float d[3];
+			for(int a = 0; a < 3; ++a)
+				d[a] = 0.5f * (axis_of(lo[k], a) + axis_of(hi[k], a)) - 0.5f * (org[a] + top[a]);
+			for(int sl = 0; sl < 8; ++sl)
+				cost[k][sl] = ((sl & 1) ? -d[0] : d[0]) + ((sl & 2) ? -d[1] : d[1]) + ((sl & 4) ? -d[2] : d[2]);
+		}
+		int in_slot[8];
+		for(int sl = 0; sl < 8; ++sl) in_slot[sl] = -1;
+		uint32_t placed = 0;
+		for(int it = 0; it < n; ++it)
+		{
+			float bc = FLT_MAX;
+			int bk = -1, bs = -1;
+			for(int k = 0; k < n; ++k)
+			{
+				if((placed >> k) & 1u) continue;
+				for(int sl = 0; sl < 8; ++sl)
+					if(in_slot[sl] < 0 && (bk < 0 || cost[k][sl] < bc)) { bc = cost[k][sl]; bk = k; bs = sl; }
+			}
+			in_slot[bs] = bk;
+			placed |= 1u << bk;
+		}
+		uint32_t imask = 0, n_internal = 0, n_leaf_prims = 0;
+		for(int sl = 0; sl < 8; ++sl)
+		{
+			const int k = in_slot[sl];
+			if(k < 0) continue;
+			if(wide_leaf(c[k], W)) n_leaf_prims += ref_count(c[k], W.node_hi);
+			else { imask |= 1u << sl; ++n_internal; }
+		}
+		const uint32_t child_base = n_internal ? atomicAdd(m + GBRT_META_WNODES, n_internal) : 0u;
+		const uint32_t prim_base = n_leaf_prims ? atomicAdd(m + GBRT_META_WPRIMS, n_leaf_prims) : 0u;
+		if(child_base + n_internal > W.n_node_cap || prim_base + n_leaf_prims > W.n_prims || task.y >= W.n_node_cap)
+		{
+			raise_err(meta, kErrWide);
+			continue;
+		}
+		// empty slots: inverted boxes (lo 255, hi 0), which no ray enters
+		uint32_t meta_w[2] = {0u, 0u}, q[6][2] = {};
+		uint32_t off = 0;
+		for(int sl = 0; sl < 8; ++sl)
+		{
+			const int k = in_slot[sl];
+			if(k < 0)
+			{
+				for(int a = 0; a < 3; ++a) q[a][sl >> 2] |= 0xFFu << (8 * (sl & 3));
+				continue;
+			}
+			uint32_t mb;
+			if((imask >> sl) & 1u)
+			{
+				mb = 0x20u | (24u + static_cast<uint32_t>(sl));
+				const uint32_t idx = child_base + __popc(imask & ((1u << sl) - 1u));
+				const uint32_t at = atomicAdd(counts + level + 1, 1u);
+				if(at < W.n_node_cap) tout[at] = make_uint2(c[k], idx);
+				else raise_err(meta, kErrWide);
+			}
+			else
+			{
+				uint32_t cnt = ref_count(c[k], W.node_hi);
+				if(cnt > kWideLeafMax) { raise_err(meta, kErrWide); cnt = 0; }
+				uint32_t first = (c[k] & GBRT_LEAF_BIT) ? W.pos_leaf[c[k] & ~GBRT_LEAF_BIT] : W.first_int[c[k]];
+				if(first + cnt > W.n_prims) { raise_err(meta, kErrWide); first = 0; cnt = 0; }
+				mb = (((1u << cnt) - 1u) << 5) | off;
+				for(uint32_t i = 0; i < cnt; ++i)
+				{
+					const uint64_t dst = prim_base + off + i, src = first + i;
+					wtris[3 * dst] = W.tris[3 * src];
+					wtris[3 * dst + 1] = W.tris[3 * src + 1];
+					wtris[3 * dst + 2] = W.tris[3 * src + 2];
+					wids[dst] = W.ids[src];
+				}
+				off += cnt;
+			}
+			meta_w[sl >> 2] |= mb << (8 * (sl & 3));
+			// outward-rounded 8-bit planes: org + q 2^e <= lo and >= hi, exactly (double)
+			for(int a = 0; a < 3; ++a)
+			{
+				const double o = org[a], sc = scale[a];
+				const double l = axis_of(lo[k], a), h = axis_of(hi[k], a);
+				double ql = floor((l - o) / sc);
+				while(ql > 0.0 && o + ql * sc > l) ql -= 1.0;
+				ql = fmax(ql, 0.0);
+				double qh = ceil((h - o) / sc);
+				while(qh < 255.0 && o + qh * sc < h) qh += 1.0;
+				qh = fmin(qh, 255.0);
+				q[a][sl >> 2] |= static_cast<uint32_t>(ql) << (8 * (sl & 3));
+				q[3 + a][sl >> 2] |= static_cast<uint32_t>(qh) << (8 * (sl & 3));
+			}
+		}
+		uint4 *o = wnodes + 5ull * task.y;
+		o[0] = make_uint4(__float_as_uint(org[0]), __float_as_uint(org[1]), __float_as_uint(org[2]),
+		                  static_cast<uint32_t>(eb[0]) | (static_cast<uint32_t>(eb[1]) << 8) | (static_cast<uint32_t>(eb[2]) << 16) | (imask << 24));
+		o[1] = make_uint4(child_base, prim_base, meta_w[0], meta_w[1]);
+		o[2] = make_uint4(q[0][0], q[0][1], q[1][0], q[1][1]);
+		o[3] = make_uint4(q[2][0], q[2][1], q[3][0], q[3][1]);
+		o[4] = make_uint4(q[4][0], q[4][1], q[5][0], q[5][1]);
+	}
+}
+
+// One primitive: a root whose slot 0 is a one-primitive leaf.
+__global__ void k_wide_single(const float4 *__restrict__ box_lo, const float4 *__restrict__ box_hi, float *meta, const float4 *__restrict__ tris,
+                              const uint32_t *__restrict__ ids, uint4 *wnodes, float4 *wtris, uint32_t *wids)
+{
+	const float pad = scene_pad(meta);
+	const float4 l = box_lo[0], h = box_hi[0];
+	const float lo[3] = {grow_down(l.x, pad), grow_down(l.y, pad), grow_down(l.z, pad)};
+	const float hi[3] = {grow_up(h.x, pad), grow_up(h.y, pad), grow_up(h.z, pad)};
+	uint32_t ebits = 0, qh[3];
+	for(int a = 0; a < 3; ++a)
+	{
+		const double ext = static_cast<double>(hi[a]) - static_cast<double>(lo[a]);
+		int e = -126;
+		if(ext > 0.0) { int x; frexp(ext / 255.0, &x); e = x; }
+		e = max(-126, min(127, e));
+		while(e < 127 && 255.0 * ldexp(1.0, e) < ext) ++e;
+		const double sc = ldexp(1.0, e);
+		double q = ceil(ext / sc);
+		while(q < 255.0 && lo[a] + q * sc < hi[a]) q += 1.0;
+		qh[a] = static_cast<uint32_t>(fmin(q, 255.0));
+		ebits |= static_cast<uint32_t>(e + 127) << (8 * a);
+	}
+	wnodes[0] = make_uint4(__float_as_uint(lo[0]), __float_as_uint(lo[1]), __float_as_uint(lo[2]), ebits);
+	wnodes[1] = make_uint4(0u, 0u, (1u << 5) | 0u, 0u);
+	wnodes[2] = make_uint4(0xFFFFFF00u, 0xFFFFFFFFu, 0xFFFFFF00u, 0xFFFFFFFFu);
+	wnodes[3] = make_uint4(0xFFFFFF00u, 0xFFFFFFFFu, qh[0], 0u);
+	wnodes[4] = make_uint4(qh[1], 0u, qh[2], 0u);
+	wtris[0] = tris[0]; wtris[1] = tris[1]; wtris[2] = tris[2];
+	wids[0] = ids[0];
+	uint32_t *m = reinterpret_cast<uint32_t *>(meta);
+	m[GBRT_META_WNODES] = 1u; m[GBRT_META_WPRIMS] = 1u; m[GBRT_META_WDEPTH] = 1u;
+}
+
+// Wide levels left unprocessed (deeper than GBRT_WIDE_MAX_LEVELS): flag.
+__global__ void k_wide_check(const uint32_t *counts, float *meta)
+{
+	if(counts[kWideLevels] != 0u) atomicOr(reinterpret_cast<uint32_t *>(meta) + GBRT_META_ERR, 2u);
+}
+
 inline unsigned blocks_for(uint64_t n, unsigned t) { return static_cast<unsigned>((n + t - 1) / t); }
 
 struct Scratch {
@@ -442,6 +915,73 @@ struct Scratch {
 	explicit Scratch(cudaStream_t st) : s(st) { }
 	~Scratch() { if(p) cudaFreeAsync(p, s); }
 };
+
+// Temporaries of the binary build.  After the sort the key buffers and the
+// unused value buffer are free again: the leaf order reuses them.
+struct BinaryBufs {
+	float4 *blo, *bhi;
+	uint32_t *k0, *k1, *v0, *v1, *hist;
+	uint2 *child, *range;
+	uint32_t *pint, *pleaf;
+	float4 *nlo, *nhi;
+	uint32_t *flags;
+	uint8_t *coll;
+	// set by build_binary
+	uint32_t *vals = nullptr;        // primitive of each binary leaf (Morton order)
+	uint32_t *pos_leaf = nullptr;    // slot of each binary leaf
+	uint32_t *first_int = nullptr;   // first slot under each internal node
+	uint32_t *vals_dfs = nullptr;    // primitive of each slot
+};
+
+constexpr uint32_t kTreeletGamma[] = {7u, 14u, 28u};
+
+// Morton codes through the emitted binary nodes and primitive records
+// (nf >= 2; k_setup and k_finalize have run).
+cudaError_t build_binary(BinaryBufs &B, const float *verts, const uint32_t *faces, uint32_t nf, const gbrt_build_params &p,
+                         float *meta, float4 *nodes, float4 *tris, uint32_t *ids, cudaStream_t s)
+{
+	cudaError_t e;
+	const uint32_t n_int = nf - 1;
+	const uint32_t nblk = blocks_for(nf, kSortTile);
+	k_morton<<<blocks_for(nf, 256), 256, 0, s>>>(B.blo, B.bhi, nf, meta, B.k0, B.v0);
+	uint32_t *kin = B.k0, *kout = B.k1, *vin = B.v0, *vout = B.v1;
+	for(int shift = 0; shift < 30; shift += 8)
+	{
+		k_hist<<<nblk, kSortThreads, 0, s>>>(kin, nf, shift, B.hist, nblk);
+		k_scan<<<1, 1024, 0, s>>>(B.hist, 256u * nblk);
+		k_scatter<<<nblk, kSortThreads, 0, s>>>(kin, vin, nf, shift, B.hist, nblk, kout, vout);
+		std::swap(kin, kout); std::swap(vin, vout);
+	}
+	if((e = cudaMemsetAsync(B.pint, 0xFF, 4ull * n_int, s)) != cudaSuccess) return e;
+	if((e = cudaMemsetAsync(B.flags, 0, 4ull * n_int, s)) != cudaSuccess) return e;
+	k_karras<<<blocks_for(n_int, 256), 256, 0, s>>>(kin, static_cast<int>(nf), B.child, B.range, B.pint, B.pleaf);
+	k_refit<<<blocks_for(nf, 256), 256, 0, s>>>(vin, static_cast<int>(nf), B.blo, B.bhi, B.child, B.pint, B.pleaf, B.nlo, B.nhi, B.flags,
+	                                            B.coll, p.max_leaf_size, p.traversal_cost, p.intersect_cost, meta);
+	if(!(p.flags & GBRT_BUILD_NO_TREELETS))
+	{
+		for(uint32_t gamma : kTreeletGamma)
+		{
+			if((e = cudaMemsetAsync(B.flags, 0, 4ull * n_int, s)) != cudaSuccess) return e;
+			k_treelet<<<blocks_for(nf, 128), 128, 0, s>>>(static_cast<int>(nf), vin, B.blo, B.bhi, B.child, B.pint, B.pleaf, B.nlo, B.nhi,
+			                                              B.flags, gamma, p.max_leaf_size, p.traversal_cost, p.intersect_cost, meta);
+		}
+		if((e = cudaMemsetAsync(B.flags, 0, 4ull * n_int, s)) != cudaSuccess) return e;
+		k_refit<<<blocks_for(nf, 256), 256, 0, s>>>(vin, static_cast<int>(nf), B.blo, B.bhi, B.child, B.pint, B.pleaf, B.nlo, B.nhi, B.flags,
+		                                            B.coll, p.max_leaf_size, p.traversal_cost, p.intersect_cost, meta);
+	}
+	B.vals = vin;
+	B.pos_leaf = kin;
+	B.first_int = kout;
+	B.vals_dfs = vout;
+	k_order_leaves<<<blocks_for(nf, 256), 256, 0, s>>>(static_cast<int>(nf), vin, B.child, B.pint, B.pleaf, B.nhi, B.pos_leaf, B.vals_dfs, meta);
+	k_order_nodes<<<blocks_for(n_int, 256), 256, 0, s>>>(static_cast<int>(n_int), B.child, B.pint, B.nhi, B.first_int, meta);
+	k_emit_nodes<<<blocks_for(n_int, 256), 256, 0, s>>>(static_cast<int>(n_int), vin, B.blo, B.bhi, B.child, B.pos_leaf, B.first_int,
+	                                                     B.nlo, B.nhi, B.coll, meta, nodes);
+	k_emit_prims<<<blocks_for(nf, 256), 256, 0, s>>>(verts, faces, B.vals_dfs, nf, meta, tris, ids);
+	return cudaGetLastError();
+}
+
+constexpr int kWideLevelsPerCheck = 12;
 
 } // namespace
 
@@ -468,18 +1008,22 @@ int gbrt_build_impl(const float *verts, uint32_t nv, const uint32_t *faces, uint
 	auto fail = [&](int code) { gbrt_bvh_destroy(b); return code; };
 	cudaError_t e;
 	const size_t node_bytes = 64ull * n_int, tri_bytes = 48ull * (nf ? nf : 1), id_bytes = 4ull * (nf ? nf : 1);
+	const size_t wnode_bytes = 80ull * n_int;
 	if((e = cudaMalloc(&b->nodes, node_bytes)) != cudaSuccess ||
 	   (e = cudaMalloc(&b->tris, tri_bytes)) != cudaSuccess ||
 	   (e = cudaMalloc(&b->ids, id_bytes)) != cudaSuccess ||
-	   (e = cudaMalloc(&b->meta, GBRT_META_WORDS * sizeof(float))) != cudaSuccess)
+	   (e = cudaMalloc(&b->meta, GBRT_META_WORDS * sizeof(float))) != cudaSuccess ||
+	   (e = cudaMalloc(&b->wnodes, wnode_bytes)) != cudaSuccess ||
+	   (e = cudaMalloc(&b->wtris, tri_bytes)) != cudaSuccess ||
+	   (e = cudaMalloc(&b->wids, id_bytes)) != cudaSuccess)
 		return fail(gbrt_set_error(GBRT_ERR_OOM, "gbrt_bvh_build: device allocation failed: %s", cudaGetErrorString(e)));
-	b->bytes = node_bytes + tri_bytes + id_bytes + GBRT_META_WORDS * sizeof(float);
+	b->bytes = node_bytes + 2 * (tri_bytes + id_bytes) + wnode_bytes + GBRT_META_WORDS * sizeof(float);
 
 	k_init_meta<<<1, 32, 0, s>>>(b->meta);
 	if(nf == 0)
 	{
 		k_finalize<<<1, 32, 0, s>>>(b->meta, 0);
-		if((e = cudaMemsetAsync(b->nodes, 0, node_bytes, s)) != cudaSuccess)
+		if((e = cudaMemsetAsync(b->nodes, 0, node_bytes, s)) != cudaSuccess || (e = cudaMemsetAsync(b->wnodes, 0, wnode_bytes, s)) != cudaSuccess)
 			return fail(gbrt_set_error(GBRT_ERR_CUDA, "memset: %s", cudaGetErrorString(e)));
 		if((e = cudaGetLastError()) != cudaSuccess) return fail(gbrt_set_error(GBRT_ERR_CUDA, "build launch: %s", cudaGetErrorString(e)));
 		*out = b;
@@ -498,46 +1042,57 @@ int gbrt_build_impl(const float *verts, uint32_t nv, const uint32_t *faces, uint
 	const size_t o_pint = carve(4ull * n_int), o_pleaf = carve(4ull * nf);
 	const size_t o_nlo = carve(16ull * n_int), o_nhi = carve(16ull * n_int);
 	const size_t o_flags = carve(4ull * n_int), o_coll = carve(n_int);
+	const size_t o_task0 = carve(8ull * n_int), o_task1 = carve(8ull * n_int), o_counts = carve(4ull * (GBRT_WIDE_MAX_LEVELS + 1));
 	Scratch sc(s);
 	if((e = cudaMallocAsync(&sc.p, off, s)) != cudaSuccess)
 		return fail(gbrt_set_error(GBRT_ERR_OOM, "gbrt_bvh_build: scratch allocation of %zu bytes failed: %s", off, cudaGetErrorString(e)));
 	char *base = static_cast<char *>(sc.p);
-	float4 *blo = reinterpret_cast<float4 *>(base + o_blo), *bhi = reinterpret_cast<float4 *>(base + o_bhi);
-	uint32_t *k0 = reinterpret_cast<uint32_t *>(base + o_k0), *k1 = reinterpret_cast<uint32_t *>(base + o_k1);
-	uint32_t *v0 = reinterpret_cast<uint32_t *>(base + o_v0), *v1 = reinterpret_cast<uint32_t *>(base + o_v1);
-	uint32_t *hist = reinterpret_cast<uint32_t *>(base + o_hist);
-	uint2 *child = reinterpret_cast<uint2 *>(base + o_child), *range = reinterpret_cast<uint2 *>(base + o_range);
-	uint32_t *pint = reinterpret_cast<uint32_t *>(base + o_pint), *pleaf = reinterpret_cast<uint32_t *>(base + o_pleaf);
-	float4 *nlo = reinterpret_cast<float4 *>(base + o_nlo), *nhi = reinterpret_cast<float4 *>(base + o_nhi);
-	uint32_t *flags = reinterpret_cast<uint32_t *>(base + o_flags);
-	uint8_t *coll = reinterpret_cast<uint8_t *>(base + o_coll);
+	BinaryBufs B;
+	B.blo = reinterpret_cast<float4 *>(base + o_blo); B.bhi = reinterpret_cast<float4 *>(base + o_bhi);
+	B.k0 = reinterpret_cast<uint32_t *>(base + o_k0); B.k1 = reinterpret_cast<uint32_t *>(base + o_k1);
+	B.v0 = reinterpret_cast<uint32_t *>(base + o_v0); B.v1 = reinterpret_cast<uint32_t *>(base + o_v1);
+	B.hist = reinterpret_cast<uint32_t *>(base + o_hist);
+	B.child = reinterpret_cast<uint2 *>(base + o_child); B.range = reinterpret_cast<uint2 *>(base + o_range);
+	B.pint = reinterpret_cast<uint32_t *>(base + o_pint); B.pleaf = reinterpret_cast<uint32_t *>(base + o_pleaf);
+	B.nlo = reinterpret_cast<float4 *>(base + o_nlo); B.nhi = reinterpret_cast<float4 *>(base + o_nhi);
+	B.flags = reinterpret_cast<uint32_t *>(base + o_flags);
+	B.coll = reinterpret_cast<uint8_t *>(base + o_coll);
+	uint2 *task[2] = {reinterpret_cast<uint2 *>(base + o_task0), reinterpret_cast<uint2 *>(base + o_task1)};
+	uint32_t *counts = reinterpret_cast<uint32_t *>(base + o_counts);
 
-	k_setup<<<blocks_for(nf, 256), 256, 0, s>>>(verts, nv, faces, nf, blo, bhi, b->meta);
+	k_setup<<<blocks_for(nf, 256), 256, 0, s>>>(verts, nv, faces, nf, B.blo, B.bhi, b->meta);
 	k_finalize<<<1, 32, 0, s>>>(b->meta, nf);
 	if(nf == 1)
 	{
-		k_emit_single<<<1, 1, 0, s>>>(blo, bhi, b->meta, b->nodes);
+		k_emit_single<<<1, 1, 0, s>>>(B.blo, B.bhi, b->meta, b->nodes);
 		k_emit_prims<<<1, 32, 0, s>>>(verts, faces, nullptr, 1, b->meta, b->tris, b->ids);
+		k_wide_single<<<1, 1, 0, s>>>(B.blo, B.bhi, b->meta, b->tris, b->ids, b->wnodes, b->wtris, b->wids);
 	}
 	else
 	{
-		k_morton<<<blocks_for(nf, 256), 256, 0, s>>>(blo, bhi, nf, b->meta, k0, v0);
-		uint32_t *kin = k0, *kout = k1, *vin = v0, *vout = v1;
-		for(int shift = 0; shift < 30; shift += 8)
-		{
-			k_hist<<<nblk, kSortThreads, 0, s>>>(kin, nf, shift, hist, nblk);
-			k_scan<<<1, 1024, 0, s>>>(hist, static_cast<uint32_t>(hist_words));
-			k_scatter<<<nblk, kSortThreads, 0, s>>>(kin, vin, nf, shift, hist, nblk, kout, vout);
-			std::swap(kin, kout); std::swap(vin, vout);
-		}
-		if((e = cudaMemsetAsync(pint, 0xFF, 4ull * n_int, s)) != cudaSuccess ||
-		   (e = cudaMemsetAsync(flags, 0, 4ull * n_int, s)) != cudaSuccess)
+		if((e = build_binary(B, verts, faces, nf, p, b->meta, b->nodes, b->tris, b->ids, s)) != cudaSuccess)
+			return fail(gbrt_set_error(GBRT_ERR_CUDA, "build launch: %s", cudaGetErrorString(e)));
+		// wide levels, checked every few levels for remaining work
+		if((e = cudaMemsetAsync(counts, 0, 4ull * (GBRT_WIDE_MAX_LEVELS + 1), s)) != cudaSuccess)
 			return fail(gbrt_set_error(GBRT_ERR_CUDA, "memset: %s", cudaGetErrorString(e)));
-		k_karras<<<blocks_for(n_int, 256), 256, 0, s>>>(kin, static_cast<int>(nf), child, range, pint, pleaf);
-		k_refit<<<blocks_for(nf, 256), 256, 0, s>>>(vin, static_cast<int>(nf), blo, bhi, child, pint, pleaf, nlo, nhi, flags, coll,
-		                                            p.max_leaf_size, p.traversal_cost, p.intersect_cost);
-		k_emit_nodes<<<blocks_for(n_int, 256), 256, 0, s>>>(static_cast<int>(n_int), vin, blo, bhi, child, range, nlo, nhi, coll, b->meta, b->nodes);
-		k_emit_prims<<<blocks_for(nf, 256), 256, 0, s>>>(verts, faces, vin, nf, b->meta, b->tris, b->ids);
+		k_wide_init<<<1, 1, 0, s>>>(b->meta, task[0], counts);
+		WideSrc W{B.child, B.vals, B.blo, B.bhi, B.nlo, B.nhi, B.coll, B.pos_leaf, B.first_int, b->tris, b->ids, n_int, nf};
+		int n_sm = 0;
+		GBRT_CK(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, b->device));
+		const unsigned wgrid = std::max(1u, std::min(blocks_for(n_int, 128), static_cast<unsigned>(n_sm) * 8u));
+		for(int L = 0; L < GBRT_WIDE_MAX_LEVELS; ++L)
+		{
+			k_wide_level<<<wgrid, 128, 0, s>>>(L, task[L & 1], counts, task[(L + 1) & 1], W, b->meta, b->wnodes, b->wtris, b->wids);
+			if((L + 1) % kWideLevelsPerCheck == 0 && L + 1 < GBRT_WIDE_MAX_LEVELS)
+			{
+				uint32_t left = 0;
+				if((e = cudaMemcpyAsync(&left, counts + L + 1, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+				   (e = cudaStreamSynchronize(s)) != cudaSuccess)
+					return fail(gbrt_set_error(GBRT_ERR_CUDA, "gbrt_bvh_build: %s", cudaGetErrorString(e)));
+				if(left == 0) break;
+			}
+		}
+		k_wide_check<<<1, 1, 0, s>>>(counts, b->meta);
 	}
 	if((e = cudaGetLastError()) != cudaSuccess) return fail(gbrt_set_error(GBRT_ERR_CUDA, "build launch: %s", cudaGetErrorString(e)));
 	*out = b;
@@ -648,43 +1203,29 @@ extern "C" int gbrt_bvh_build_static(const float *verts, uint32_t nv, const uint
 	}
 	else
 	{
-		float4 *blo = reinterpret_cast<float4 *>(base + L.blo), *bhi = reinterpret_cast<float4 *>(base + L.bhi);
-		uint32_t *k0 = reinterpret_cast<uint32_t *>(base + L.k0), *k1 = reinterpret_cast<uint32_t *>(base + L.k1);
-		uint32_t *v0 = reinterpret_cast<uint32_t *>(base + L.v0), *v1 = reinterpret_cast<uint32_t *>(base + L.v1);
-		uint32_t *hist = reinterpret_cast<uint32_t *>(base + L.hist);
-		uint2 *child = reinterpret_cast<uint2 *>(base + L.child), *range = reinterpret_cast<uint2 *>(base + L.range);
-		uint32_t *pint = reinterpret_cast<uint32_t *>(base + L.pint), *pleaf = reinterpret_cast<uint32_t *>(base + L.pleaf);
-		float4 *nlo = reinterpret_cast<float4 *>(base + L.nlo), *nhi = reinterpret_cast<float4 *>(base + L.nhi);
-		uint32_t *flags = reinterpret_cast<uint32_t *>(base + L.flags);
-		uint8_t *coll = reinterpret_cast<uint8_t *>(base + L.coll);
+		BinaryBufs B;
+		B.blo = reinterpret_cast<float4 *>(base + L.blo); B.bhi = reinterpret_cast<float4 *>(base + L.bhi);
+		B.k0 = reinterpret_cast<uint32_t *>(base + L.k0); B.k1 = reinterpret_cast<uint32_t *>(base + L.k1);
+		B.v0 = reinterpret_cast<uint32_t *>(base + L.v0); B.v1 = reinterpret_cast<uint32_t *>(base + L.v1);
+		B.hist = reinterpret_cast<uint32_t *>(base + L.hist);
+		B.child = reinterpret_cast<uint2 *>(base + L.child); B.range = reinterpret_cast<uint2 *>(base + L.range);
+		B.pint = reinterpret_cast<uint32_t *>(base + L.pint); B.pleaf = reinterpret_cast<uint32_t *>(base + L.pleaf);
+		B.nlo = reinterpret_cast<float4 *>(base + L.nlo); B.nhi = reinterpret_cast<float4 *>(base + L.nhi);
+		B.flags = reinterpret_cast<uint32_t *>(base + L.flags);
+		B.coll = reinterpret_cast<uint8_t *>(base + L.coll);
 		float4 *tris = static_cast<float4 *>(prims_dev);
-		k_setup<<<blocks_for(nf, 256), 256, 0, s>>>(verts, nv, faces, nf, blo, bhi, meta);
+		k_setup<<<blocks_for(nf, 256), 256, 0, s>>>(verts, nv, faces, nf, B.blo, B.bhi, meta);
 		k_finalize<<<1, 32, 0, s>>>(meta, nf);
 		if(nf == 1)
 		{
-			k_emit_single<<<1, 1, 0, s>>>(blo, bhi, meta, nodes);
+			k_emit_single<<<1, 1, 0, s>>>(B.blo, B.bhi, meta, nodes);
 			k_emit_prims<<<1, 32, 0, s>>>(verts, faces, nullptr, 1, meta, tris, ids_dev);
 		}
 		else
 		{
-			const uint32_t nblk = blocks_for(nf, kSortTile);
-			k_morton<<<blocks_for(nf, 256), 256, 0, s>>>(blo, bhi, nf, meta, k0, v0);
-			uint32_t *kin = k0, *kout = k1, *vin = v0, *vout = v1;
-			for(int shift = 0; shift < 30; shift += 8)
-			{
-				k_hist<<<nblk, kSortThreads, 0, s>>>(kin, nf, shift, hist, nblk);
-				k_scan<<<1, 1024, 0, s>>>(hist, 256u * nblk);
-				k_scatter<<<nblk, kSortThreads, 0, s>>>(kin, vin, nf, shift, hist, nblk, kout, vout);
-				std::swap(kin, kout); std::swap(vin, vout);
-			}
-			// the array keeps the previous call's contents: reset parents and arrival counters
-			GBRT_CK(cudaMemsetAsync(pint, 0xFF, 4ull * n_int, s));
-			GBRT_CK(cudaMemsetAsync(flags, 0, 4ull * n_int, s));
-			k_karras<<<blocks_for(n_int, 256), 256, 0, s>>>(kin, static_cast<int>(nf), child, range, pint, pleaf);
-			k_refit<<<blocks_for(nf, 256), 256, 0, s>>>(vin, static_cast<int>(nf), blo, bhi, child, pint, pleaf, nlo, nhi, flags, coll,
-			                                            p.max_leaf_size, p.traversal_cost, p.intersect_cost);
-			k_emit_nodes<<<blocks_for(n_int, 256), 256, 0, s>>>(static_cast<int>(n_int), vin, blo, bhi, child, range, nlo, nhi, coll, meta, nodes);
-			k_emit_prims<<<blocks_for(nf, 256), 256, 0, s>>>(verts, faces, vin, nf, meta, tris, ids_dev);
+			// the array keeps the previous call's contents: build_binary resets
+			// parents and arrival counters before use
+			GBRT_CK(build_binary(B, verts, faces, nf, p, meta, nodes, tris, ids_dev, s));
 		}
 	}
 	GBRT_CK(cudaGetLastError());
@@ -693,7 +1234,8 @@ extern "C" int gbrt_bvh_build_static(const float *verts, uint32_t nv, const uint
 	GBRT_CK(cudaStreamSynchronize(s));
 	uint32_t err;
 	std::memcpy(&err, &m[GBRT_META_ERR], 4);
-	if(err) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_bvh_build_static: a face references a vertex index >= %u", nv);
+	if(err & 1u) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_bvh_build_static: a face references a vertex index >= %u", nv);
+	if(err) return gbrt_set_error(GBRT_ERR_CUDA, "gbrt_bvh_build_static: internal error: inconsistent hierarchy (flags 0x%x)", err);
 	std::memcpy(bound_out, &m[GBRT_META_BOUND], 6 * sizeof(float));
 	return GBRT_OK;
 }

@@ -101,6 +101,9 @@ int gbrt_bvh_destroy(gbrt_bvh *b)
 	if(b->tris) cudaFree(b->tris);
 	if(b->ids) cudaFree(b->ids);
 	if(b->meta) cudaFree(b->meta);
+	if(b->wnodes) cudaFree(b->wnodes);
+	if(b->wtris) cudaFree(b->wtris);
+	if(b->wids) cudaFree(b->wids);
 	if(dev >= 0 && dev != b->device) cudaSetDevice(dev);
 	delete b;
 	return GBRT_OK;
@@ -123,11 +126,26 @@ int gbrt_bvh_build(const float *vertices_dev, uint32_t n_vertices, const uint32_
 	}
 	uint32_t err;
 	std::memcpy(&err, &meta[GBRT_META_ERR], 4);
-	if(err)
+	if(err & 1u)
 	{
 		gbrt_bvh_destroy(*out); *out = nullptr;
 		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_bvh_build: a face references a vertex index >= %u", n_vertices);
 	}
+	if(err & 12u)
+	{
+		gbrt_bvh_destroy(*out); *out = nullptr;
+		return gbrt_set_error(GBRT_ERR_CUDA, "gbrt_bvh_build: internal error: inconsistent hierarchy (flags 0x%x)", err);
+	}
+	if(err & 2u)
+	{
+		gbrt_bvh_destroy(*out); *out = nullptr;
+		return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_bvh_build: the wide hierarchy is deeper than %d levels", GBRT_WIDE_MAX_LEVELS);
+	}
+	uint32_t wn, wd;
+	std::memcpy(&wn, &meta[GBRT_META_WNODES], 4);
+	std::memcpy(&wd, &meta[GBRT_META_WDEPTH], 4);
+	(*out)->n_wide_nodes = n_faces ? wn : 0u;
+	(*out)->wide_depth = n_faces ? wd : 0u;
 	std::memcpy((*out)->host_bound, &meta[GBRT_META_BOUND], 6 * sizeof(float));
 	(*out)->host_bound_valid = true;
 	return GBRT_OK;
@@ -209,6 +227,21 @@ int gbrt_bvh_export(const gbrt_bvh *b, void *nodes, size_t nodes_bytes, void *pr
 	if(nodes) GBRT_CK(cudaMemcpy(nodes, b->nodes, nb, cudaMemcpyDeviceToHost));
 	if(prims && pb) GBRT_CK(cudaMemcpy(prims, b->tris, pb, cudaMemcpyDeviceToHost));
 	if(ids && ib) GBRT_CK(cudaMemcpy(ids, b->ids, ib, cudaMemcpyDeviceToHost));
+	return GBRT_OK;
+}
+
+int gbrt_bvh_export_wide(const gbrt_bvh *b, uint32_t *n_nodes, uint32_t *depth, void *nodes, size_t nodes_bytes,
+                         void *prims, size_t prims_bytes, uint32_t *ids, size_t ids_bytes)
+{
+	if(!b) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_bvh_export_wide: NULL handle");
+	const size_t nb = 80ull * b->n_wide_nodes, pb = 48ull * b->n_prims, ib = 4ull * b->n_prims;
+	if((nodes && nodes_bytes < nb) || (prims && prims_bytes < pb) || (ids && ids_bytes < ib))
+		return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_bvh_export_wide: buffers too small (need %zu/%zu/%zu bytes)", nb, pb, ib);
+	if(n_nodes) *n_nodes = b->n_wide_nodes;
+	if(depth) *depth = b->wide_depth;
+	if(nodes && nb) GBRT_CK(cudaMemcpy(nodes, b->wnodes, nb, cudaMemcpyDeviceToHost));
+	if(prims && pb) GBRT_CK(cudaMemcpy(prims, b->wtris, pb, cudaMemcpyDeviceToHost));
+	if(ids && ib) GBRT_CK(cudaMemcpy(ids, b->wids, ib, cudaMemcpyDeviceToHost));
 	return GBRT_OK;
 }
 

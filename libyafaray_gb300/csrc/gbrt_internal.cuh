@@ -15,6 +15,9 @@
 #define GBRT_LEAF_MAX_SLOTS (1u << 27)
 #define GBRT_LEAF_MAX_COUNT 16u
 #define GBRT_QUAD_BIT 0x80000000u
+// Levels of the 8-wide hierarchy the build accepts; also the traversal
+// stack depth (a traversal pushes at most one entry per level).
+#define GBRT_WIDE_MAX_LEVELS 96
 
 __host__ __device__ inline uint32_t gbrt_leaf_ref(uint32_t first, uint32_t count)
 {
@@ -32,6 +35,22 @@ __host__ __device__ inline uint32_t gbrt_leaf_ref(uint32_t first, uint32_t count
 //           (e_k = v_k - v0 in float, exactly as shape_polygon.h:130-131,155)
 //   ids   : primitive ID per slot, GBRT_QUAD_BIT set for quads
 //   meta  : float bound[6] (reference tree bound) + build scratch words
+//
+// The traversal kernels walk a second, 8-wide copy of the hierarchy built
+// from the binary one (the binary layout stays as the export / no-allocation
+// build format):
+//   wnodes: 5 uint4 (80 bytes) per wide node
+//           [0] origin xyz (float bits), exponent bytes ex | ey<<8 | ez<<16 | imask<<24
+//           [1] child_base, prim_base, meta bytes of slots 0-3, slots 4-7
+//           [2] qlo.x slots 0-7 (2 words), qlo.y slots 0-7
+//           [3] qlo.z, qhi.x   [4] qhi.y, qhi.z   (8-bit quantised child boxes)
+//       Child box plane = origin + q * 2^(e - 127); planes round outward.
+//       meta byte: 0 empty; internal child 0x20 | (24 + slot), its node index
+//       child_base + popc(imask below slot); leaf child (unary count << 5) |
+//       offset, primitives prim_base + offset .. + count - 1 (count 1..3).
+//       Children sit in slots by octant: the child nearest for rays whose
+//       direction signs are octant o is in slot o.
+//   wtris, wids: primitive records and IDs in wide-leaf order.
 struct gbrt_bvh {
 	int device = 0;
 	uint32_t n_prims = 0;
@@ -40,6 +59,11 @@ struct gbrt_bvh {
 	float4 *tris = nullptr;
 	uint32_t *ids = nullptr;
 	float *meta = nullptr;
+	uint4 *wnodes = nullptr;
+	float4 *wtris = nullptr;
+	uint32_t *wids = nullptr;
+	uint32_t n_wide_nodes = 0;
+	uint32_t wide_depth = 0;
 	uint64_t bytes = 0;
 	gbrt_build_params params{};
 	float host_bound[6]{};
@@ -59,6 +83,9 @@ enum : int {
 	GBRT_META_CINV = 9,         // 3 floats: 1 / centroid extent (0 if flat)
 	GBRT_META_ORD = 12,         // 12 uints: ordered-int reduction scratch
 	GBRT_META_ERR = 24,         // 1 uint: build error flag (bad vertex index)
+	GBRT_META_WNODES = 25,      // 1 uint: wide nodes written
+	GBRT_META_WDEPTH = 26,      // 1 uint: wide tree depth (levels)
+	GBRT_META_WPRIMS = 27,      // 1 uint: primitives placed in wide leaves
 	GBRT_META_WORDS = 32
 };
 

@@ -1100,11 +1100,12 @@ __global__ void __launch_bounds__(kThreads) k_camera(Camera cam, Params P, Work 
 __global__ void __launch_bounds__(kThreads) k_extend(gbrt::BvhView bv, const float4 *__restrict__ rays, const uint32_t *__restrict__ count,
                                                      float4 *__restrict__ hits, float *__restrict__ hitpos)
 {
+	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
 	const uint32_t n = *count;
 	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
 	{
 		const float4 a = rays[2ull * i], b = rays[2ull * i + 1];
-		const gbrt::Hit h = gbrt::trace_ray<false>(bv, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w);
+		const gbrt::Hit h = gbrt::trace_ray<false>(bv, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, stack + threadIdx.x, kThreads);
 		hits[i] = make_float4(__int_as_float(h.prim), h.t, h.u, h.v);
 		if(hitpos)
 		{
@@ -1500,6 +1501,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 
 __global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Work W, uint32_t shadow_cap, float *film, double *film64)
 {
+	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
 	const uint32_t n = min(W.count[2], shadow_cap);
 	uint32_t traced = 0;
 	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -1507,7 +1509,7 @@ __global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Work W, u
 		const uint32_t pixel = W.s_pix[i];
 		if(pixel == kDead) continue;
 		const float4 a = W.s_ray[2ull * i], b = W.s_ray[2ull * i + 1];
-		const gbrt::Hit h = gbrt::trace_ray<true>(bv, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w);
+		const gbrt::Hit h = gbrt::trace_ray<true>(bv, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, stack + threadIdx.x, kThreads);
 		++traced;
 		if(h.prim < 0)
 		{
@@ -1738,6 +1740,7 @@ __device__ void reflectivity(const SceneDev &sc, const Surface &s, uint32_t flag
 
 __global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJob J)
 {
+	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
 	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < J.n; i += gridDim.x * blockDim.x)
 	{
 		const float s1 = gbrt::ri_vdc(i);
@@ -1775,7 +1778,7 @@ __global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJo
 		float tmin = kRayMinDist;
 		for(int nb = 0;; ++nb)
 		{
-			const gbrt::Hit h = gbrt::trace_ray<false>(sc.bv, o[0], o[1], o[2], tmin, d[0], d[1], d[2], -1.f);
+			const gbrt::Hit h = gbrt::trace_ray<false>(sc.bv, o[0], o[1], o[2], tmin, d[0], d[1], d[2], -1.f, stack + threadIdx.x, kThreads);
 			if(h.prim < 0) break;
 			Surface s;
 			for(int k = 0; k < 3; ++k) s.p[k] = xa(o[k], xm(h.t, d[k]));

@@ -16,17 +16,21 @@
 
 namespace gbrt {
 
-constexpr int kTraceStack = 64;   // > maximum LBVH depth (30 Morton + 32 index bits)
+// Traversal stack: kStackShared entries per thread in the calling block's
+// shared memory, the rest in local memory.  A traversal pushes at most one
+// entry per level of the wide hierarchy.
+constexpr int kStackShared = 8;
+constexpr int kTraceStack = GBRT_WIDE_MAX_LEVELS;
 
 struct BvhView {
-	const float4 *nodes;
-	const float4 *tris;
+	const uint4 *wnodes;        // 8-wide compressed nodes (gbrt_internal.cuh)
+	const float4 *tris;         // primitive records in wide-leaf order
 	const uint32_t *ids;
 	const float *meta;
 	uint32_t n_prims;
 };
 
-inline BvhView view_of(const gbrt_bvh *b) { return {b->nodes, b->tris, b->ids, b->meta, b->n_prims}; }
+inline BvhView view_of(const gbrt_bvh *b) { return {b->wnodes, b->wtris, b->wids, b->meta, b->n_prims}; }
 
 __device__ __forceinline__ float xm(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float xa(float a, float b) { return __fadd_rn(a, b); }
@@ -118,24 +122,76 @@ __device__ __forceinline__ float mt_intersect(const float4 A, const float4 B, co
 	return 0.f;
 }
 
-// Conservative slab test of a node's two children against [0, t_hi].
-__device__ __forceinline__ void child_tests(const float4 n0, const float4 n1, const float4 n2, const float o[3], const float inv[3],
-                                            float t_hi, bool &hit0, bool &hit1, float &tn0, float &tn1)
+// Byte k of w as a float (exact): 2^23 + b - 2^23.
+template <int k>
+__device__ __forceinline__ float byte_f(uint32_t w)
 {
-	const float ax0 = (n0.x - o[0]) * inv[0], ax1 = (n0.y - o[0]) * inv[0];
-	const float ay0 = (n0.z - o[1]) * inv[1], ay1 = (n0.w - o[1]) * inv[1];
-	const float az0 = (n2.x - o[2]) * inv[2], az1 = (n2.y - o[2]) * inv[2];
-	const float bx0 = (n1.x - o[0]) * inv[0], bx1 = (n1.y - o[0]) * inv[0];
-	const float by0 = (n1.z - o[1]) * inv[1], by1 = (n1.w - o[1]) * inv[1];
-	const float bz0 = (n2.z - o[2]) * inv[2], bz1 = (n2.w - o[2]) * inv[2];
-	const float an = fmaxf(fmaxf(fminf(ax0, ax1), fminf(ay0, ay1)), fmaxf(fminf(az0, az1), 0.f));
-	const float af = fminf(fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1)), fminf(fmaxf(az0, az1), t_hi)) * 1.0000004f;
-	const float bn = fmaxf(fmaxf(fminf(bx0, bx1), fminf(by0, by1)), fmaxf(fminf(bz0, bz1), 0.f));
-	const float bf = fminf(fminf(fmaxf(bx0, bx1), fmaxf(by0, by1)), fminf(fmaxf(bz0, bz1), t_hi)) * 1.0000004f;
-	hit0 = an <= af;
-	hit1 = bn <= bf;
-	tn0 = an;
-	tn1 = bn;
+	return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440 + k)) - 8388608.f;
+}
+
+// Conservative test of a wide node's 8 child boxes against [0, t_hi]:
+// node-hit bits ((slot ^ oct) for internal children) and primitive-hit bits
+// (prim_base-relative) of the children that pass.  Planes are
+// origin + q 2^e, rounded outward at build time; t = q (2^e / d) +
+// (origin - o) / d with one FMA, the far distance widened by 3 ulp (Ize,
+// "Robust BVH ray traversal", JCGT 2013) and the boxes grown at build time
+// by more than the rounding of these expressions.  Per axis the near plane
+// is the low one when the direction's sign bit is clear (octant bit 0),
+// else the high one; a zero direction component gives infinities or NaNs
+// that the min/max chains treat conservatively.
+__device__ __forceinline__ void wide_node_test(const uint4 w0, const uint4 w1, const uint4 w2, const uint4 w3, const uint4 w4,
+                                               const float o[3], const float inv[3], uint32_t oct, float t_hi,
+                                               uint32_t &node_hits, uint32_t &prim_hits)
+{
+	const float ax = __uint_as_float((w0.w & 0xFFu) << 23) * inv[0];
+	const float ay = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23) * inv[1];
+	const float az = __uint_as_float(((w0.w >> 16) & 0xFFu) << 23) * inv[2];
+	const float bx = (__uint_as_float(w0.x) - o[0]) * inv[0];
+	const float by = (__uint_as_float(w0.y) - o[1]) * inv[1];
+	const float bz = (__uint_as_float(w0.z) - o[2]) * inv[2];
+	// near / far plane words of slots 0-3 (index 0) and 4-7 (index 1)
+	const bool sx = oct & 1u, sy = oct & 2u, sz = oct & 4u;
+	const uint32_t nx0 = sx ? w3.z : w2.x, nx1 = sx ? w3.w : w2.y, fx0 = sx ? w2.x : w3.z, fx1 = sx ? w2.y : w3.w;
+	const uint32_t ny0 = sy ? w4.x : w2.z, ny1 = sy ? w4.y : w2.w, fy0 = sy ? w2.z : w4.x, fy1 = sy ? w2.w : w4.y;
+	const uint32_t nz0 = sz ? w4.z : w3.x, nz1 = sz ? w4.w : w3.y, fz0 = sz ? w3.x : w4.z, fz1 = sz ? w3.y : w4.w;
+	uint32_t hit = 0;
+#define GBRT_WIDE_CHILD(K, NX, NY, NZ, FX, FY, FZ, SLOT)                                                   \
+	{                                                                                                      \
+		const float tn = fmaxf(fmaxf(fmaf(byte_f<(K)>(NX), ax, bx), fmaf(byte_f<(K)>(NY), ay, by)),         \
+		                       fmaxf(fmaf(byte_f<(K)>(NZ), az, bz), 0.f));                                 \
+		const float tf = fminf(fminf(fmaf(byte_f<(K)>(FX), ax, bx), fmaf(byte_f<(K)>(FY), ay, by)),         \
+		                       fminf(fmaf(byte_f<(K)>(FZ), az, bz), t_hi)) * 1.0000004f;                   \
+		if(tn <= tf) hit |= 1u << (SLOT);                                                                  \
+	}
+	GBRT_WIDE_CHILD(0, nx0, ny0, nz0, fx0, fy0, fz0, 0)
+	GBRT_WIDE_CHILD(1, nx0, ny0, nz0, fx0, fy0, fz0, 1)
+	GBRT_WIDE_CHILD(2, nx0, ny0, nz0, fx0, fy0, fz0, 2)
+	GBRT_WIDE_CHILD(3, nx0, ny0, nz0, fx0, fy0, fz0, 3)
+	GBRT_WIDE_CHILD(0, nx1, ny1, nz1, fx1, fy1, fz1, 4)
+	GBRT_WIDE_CHILD(1, nx1, ny1, nz1, fx1, fy1, fz1, 5)
+	GBRT_WIDE_CHILD(2, nx1, ny1, nz1, fx1, fy1, fz1, 6)
+	GBRT_WIDE_CHILD(3, nx1, ny1, nz1, fx1, fy1, fz1, 7)
+#undef GBRT_WIDE_CHILD
+	// Empty slots hold inverted boxes (missed except on a degenerate axis)
+	// and meta 0, so a stray hit on one adds no bits below.
+	const uint32_t m0 = w1.z, m1 = w1.w;
+	const uint32_t imask = w0.w >> 24;
+	// internal children: bit slot -> bit slot ^ oct (a permutation of 8 bits)
+	uint32_t nh = hit & imask;
+	if(oct & 1u) nh = ((nh & 0x55u) << 1) | ((nh >> 1) & 0x55u);
+	if(oct & 2u) nh = ((nh & 0x33u) << 2) | ((nh >> 2) & 0x33u);
+	if(oct & 4u) nh = ((nh & 0x0Fu) << 4) | ((nh >> 4) & 0x0Fu);
+	// leaf children: unary count << offset from the meta byte
+	uint32_t lh = hit & ~imask, ph = 0;
+	while(lh)
+	{
+		const uint32_t sl = __ffs(lh) - 1u;
+		lh &= lh - 1u;
+		const uint32_t mb = ((sl < 4u ? m0 : m1) >> (8u * (sl & 3u))) & 0xFFu;
+		ph |= (mb >> 5) << (mb & 0x1Fu);
+	}
+	node_hits = nh;
+	prim_hits = ph;
 }
 
 struct Hit {
@@ -143,82 +199,129 @@ struct Hit {
 	float t, u, v;
 };
 
-// One query.  Closest hit follows Accelerator::intersect(ray, camera)
+// Per-ray traversal state: the ray in the reference's set-up, the best hit
+// so far, the current node group (child_base; hit bits 0-7, imask 8-15),
+// the current primitive group and the stack depth.
+struct TraceState {
+	float from[3], dir[3], inv[3];
+	float t_min, t_max;
+	uint32_t oct;
+	Hit h;
+	uint32_t nbase, nhits, pbase, phits;
+	int sp;
+};
+
+// Ray set-up.  Closest hit follows Accelerator::intersect(ray, camera)
 // (accelerator.h:89-101); shadow follows Accelerator::isShadowed
 // (accelerator.h:103-111): origin advanced by tmin, t_max = tmax - 2 tmin,
-// bias-only t_min, first accepted primitive returns.
+// bias-only t_min.  Returns false when the ray misses the tree bound (no
+// traversal).
 template <bool kShadow>
-__device__ __forceinline__ Hit trace_ray(const BvhView &bv, float ox, float oy, float oz, float tmin, float dx, float dy, float dz, float tmax)
+__device__ __forceinline__ bool trace_init(TraceState &S, const BvhView &bv, float ox, float oy, float oz, float tmin, float dx, float dy,
+                                           float dz, float tmax)
 {
-	float from[3] = {ox, oy, oz};
-	const float dir[3] = {dx, dy, dz};
-	float t_max;
-	if(!kShadow) t_max = (tmax >= 0.f) ? tmax : FLT_MAX;
+	S.from[0] = ox; S.from[1] = oy; S.from[2] = oz;
+	S.dir[0] = dx; S.dir[1] = dy; S.dir[2] = dz;
+	if(!kShadow) S.t_max = (tmax >= 0.f) ? tmax : FLT_MAX;
 	else
 	{
-		from[0] = xa(from[0], xm(dir[0], tmin));
-		from[1] = xa(from[1], xm(dir[1], tmin));
-		from[2] = xa(from[2], xm(dir[2], tmin));
-		t_max = (tmax >= 0.f) ? xs(tmax, xm(2.f, tmin)) : FLT_MAX;
+		S.from[0] = xa(S.from[0], xm(dx, tmin));
+		S.from[1] = xa(S.from[1], xm(dy, tmin));
+		S.from[2] = xa(S.from[2], xm(dz, tmin));
+		S.t_max = (tmax >= 0.f) ? xs(tmax, xm(2.f, tmin)) : FLT_MAX;
 	}
 	float bnd[6];
 #pragma unroll
 	for(int k = 0; k < 6; ++k) bnd[k] = __ldg(bv.meta + GBRT_META_BOUND + k);
 	float enter, leave;
-	Hit h{-1, t_max, 0.f, 0.f};
-	if(bv.n_prims == 0 || !bound_cross(bnd, from, dir, t_max, enter, leave)) { h.t = 0.f; return h; }
+	S.h = Hit{-1, S.t_max, 0.f, 0.f};
+	if(bv.n_prims == 0 || !bound_cross(bnd, S.from, S.dir, S.t_max, enter, leave)) return false;
 	// accelerator_kdtree_common.h:139, accelerator.h:64
 	const float bias = xm(0.1f * 0.00005f, fabsf(xs(leave, enter)));
-	const float t_min = kShadow ? bias : fmaxf(tmin, bias);
-	const float inv[3] = {1.f / dir[0], 1.f / dir[1], 1.f / dir[2]};
-	uint32_t stack[kTraceStack];
-	int sp = 0;
-	uint32_t ref = 0;
-	bool done = false;
-	while(!done)
+	S.t_min = kShadow ? bias : fmaxf(tmin, bias);
+	S.inv[0] = 1.f / dx; S.inv[1] = 1.f / dy; S.inv[2] = 1.f / dz;
+	S.oct = (dx < 0.f ? 1u : 0u) | (dy < 0.f ? 2u : 0u) | (dz < 0.f ? 4u : 0u);
+	// a virtual group whose only (internal) child, in slot 0, is the root
+	S.nbase = 0;
+	S.nhits = (1u << S.oct) | (1u << 8);
+	S.pbase = 0;
+	S.phits = 0;
+	S.sp = 0;
+	return true;
+}
+
+// One step of the walk of the 8-wide hierarchy: open the nearest remaining
+// child of the current group by octant order (pushing the rest of the
+// group), test the opened node's primitive hits, pop when the group is
+// spent.  `sh` is this thread's column of a shared [kStackShared][stride]
+// uint2 array, `spill` a local array of kTraceStack - kStackShared entries.
+// Returns true when the query is answered.
+template <bool kShadow>
+__device__ __forceinline__ bool trace_step(TraceState &S, const BvhView &bv, uint2 *sh, int stride, uint2 *spill)
+{
+	if(S.nhits & 0xFFu)
 	{
-		while(!(ref & GBRT_LEAF_BIT))
+		const uint32_t b = __ffs(S.nhits & 0xFFu) - 1u;
+		S.nhits &= ~(1u << b);
+		const uint32_t slot = b ^ S.oct;
+		const uint32_t idx = S.nbase + __popc((S.nhits >> 8) & ((1u << slot) - 1u));
+		if(S.nhits & 0xFFu)
 		{
-			const float4 *nd = bv.nodes + 4ull * ref;
-			const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
-			bool h0, h1; float tn0, tn1;
-			child_tests(n0, n1, n2, from, inv, h.t, h0, h1, tn0, tn1);
-			const uint32_t r0 = __float_as_uint(n3.x), r1 = __float_as_uint(n3.y);
-			if(h0 && h1)
-			{
-				const bool first0 = tn0 <= tn1;
-				ref = first0 ? r0 : r1;
-				if(sp < kTraceStack) stack[sp++] = first0 ? r1 : r0;
-			}
-			else if(h0) ref = r0;
-			else if(h1) ref = r1;
-			else
-			{
-				if(sp == 0) { done = true; break; }
-				ref = stack[--sp];
-			}
+			const uint2 e = make_uint2(S.nbase, S.nhits);
+			if(S.sp < kStackShared) sh[S.sp * stride] = e;
+			else if(S.sp < kTraceStack) spill[S.sp - kStackShared] = e;
+			++S.sp;
 		}
-		if(done) break;
-		const uint32_t first = ref & (GBRT_LEAF_MAX_SLOTS - 1u);
-		const uint32_t cnt = ((ref >> 27) & 15u) + 1u;
-		for(uint32_t k = 0; k < cnt; ++k)
-		{
-			const uint32_t slot = first + k;
-			const float4 A = __ldg(bv.tris + 3ull * slot), B = __ldg(bv.tris + 3ull * slot + 1), C = __ldg(bv.tris + 3ull * slot + 2);
-			const uint32_t id = __ldg(bv.ids + slot);
-			float u, v;
-			const float t = mt_intersect(A, B, C, (id & GBRT_QUAD_BIT) != 0u, from, dir, u, v);
-			if(t <= 0.f || t < t_min || t >= t_max) continue;   // accelerator.h:125 / 137
-			const int32_t pid = static_cast<int32_t>(id & ~GBRT_QUAD_BIT);
-			if(kShadow) { h.prim = pid; h.t = t; h.u = u; h.v = v; done = true; break; }
-			if(t < h.t || (t == h.t && h.prim >= 0 && pid < h.prim)) { h.t = t; h.prim = pid; h.u = u; h.v = v; }
-		}
-		if(done) break;
-		if(sp == 0) break;
-		ref = stack[--sp];
+		const uint4 *nd = bv.wnodes + 5ull * idx;
+		const uint4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3), w4 = __ldg(nd + 4);
+		uint32_t nh, ph;
+		wide_node_test(w0, w1, w2, w3, w4, S.from, S.inv, S.oct, S.h.t, nh, ph);
+		S.nbase = w1.x;
+		S.nhits = nh | ((w0.w >> 24) << 8);
+		S.pbase = w1.y;
+		S.phits = ph;
 	}
-	if(h.prim < 0) { h.t = 0.f; h.u = 0.f; h.v = 0.f; }
-	return h;
+	while(S.phits)
+	{
+		const uint32_t slot = S.pbase + __ffs(S.phits) - 1u;
+		S.phits &= S.phits - 1u;
+		const float4 A = __ldg(bv.tris + 3ull * slot), B = __ldg(bv.tris + 3ull * slot + 1), C = __ldg(bv.tris + 3ull * slot + 2);
+		const uint32_t id = __ldg(bv.ids + slot);
+		float u, v;
+		const float t = mt_intersect(A, B, C, (id & GBRT_QUAD_BIT) != 0u, S.from, S.dir, u, v);
+		if(t <= 0.f || t < S.t_min || t >= S.t_max) continue;   // accelerator.h:125 / 137
+		const int32_t pid = static_cast<int32_t>(id & ~GBRT_QUAD_BIT);
+		if(kShadow) { S.h = Hit{pid, t, u, v}; return true; }
+		if(t < S.h.t || (t == S.h.t && S.h.prim >= 0 && pid < S.h.prim)) S.h = Hit{pid, t, u, v};
+	}
+	if(!(S.nhits & 0xFFu))
+	{
+		if(S.sp == 0) return true;
+		--S.sp;
+		const uint2 e = S.sp < kStackShared ? sh[S.sp * stride] : (S.sp < kTraceStack ? spill[S.sp - kStackShared] : make_uint2(0u, 0u));
+		S.nbase = e.x;
+		S.nhits = e.y;
+	}
+	return false;
+}
+
+// The answer in the reference's form: a miss has t = u = v = 0.
+__device__ __forceinline__ Hit trace_result(const TraceState &S)
+{
+	if(S.h.prim < 0) return Hit{-1, 0.f, 0.f, 0.f};
+	return S.h;
+}
+
+// One complete query (see trace_init / trace_step).
+template <bool kShadow>
+__device__ __forceinline__ Hit trace_ray(const BvhView &bv, float ox, float oy, float oz, float tmin, float dx, float dy, float dz, float tmax,
+                                         uint2 *sh, int stride)
+{
+	TraceState S;
+	if(!trace_init<kShadow>(S, bv, ox, oy, oz, tmin, dx, dy, dz, tmax)) return Hit{-1, 0.f, 0.f, 0.f};
+	uint2 spill[kTraceStack - kStackShared];
+	while(!trace_step<kShadow>(S, bv, sh, stride, spill)) { }
+	return trace_result(S);
 }
 
 } // namespace gbrt

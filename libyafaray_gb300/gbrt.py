@@ -25,6 +25,9 @@ class GbrtError(RuntimeError):
         self.code = code
 
 
+BUILD_NO_TREELETS = 1
+
+
 class BuildParams(ctypes.Structure):
     _fields_ = [("max_leaf_size", ctypes.c_uint32), ("traversal_cost", ctypes.c_float),
                 ("intersect_cost", ctypes.c_float), ("flags", ctypes.c_uint32)]
@@ -113,6 +116,8 @@ SIGNATURES = {
     "gbrt_bvh_get_bound": (_I, [_VP, ctypes.POINTER(ctypes.c_float)]),
     "gbrt_bvh_get_info": (_I, [_VP, ctypes.POINTER(BvhInfo)]),
     "gbrt_bvh_export": (_I, [_VP, _VP, ctypes.c_size_t, _VP, ctypes.c_size_t, _VP, ctypes.c_size_t]),
+    "gbrt_bvh_export_wide": (_I, [_VP, ctypes.POINTER(_U32), ctypes.POINTER(_U32), _VP, ctypes.c_size_t, _VP, ctypes.c_size_t,
+                                  _VP, ctypes.c_size_t]),
     "gbrt_bvh_build_static": (_I, [_VP, _U32, _VP, _U32, ctypes.POINTER(BuildParams), _VP, ctypes.c_size_t, _VP,
                                    ctypes.c_size_t, _VP, ctypes.c_size_t, ctypes.POINTER(ctypes.c_float), _VP]),
     "gbrt_trace_closest": (_I, [_VP, _VP, _U32, _VP, _VP]),
@@ -187,18 +192,18 @@ class Bvh:
         self._h = handle
 
     @classmethod
-    def build_host(cls, vertices, faces, max_leaf_size=0, traversal_cost=0.0, intersect_cost=0.0):
+    def build_host(cls, vertices, faces, max_leaf_size=0, traversal_cost=0.0, intersect_cost=0.0, treelets=True):
         v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
         f = np.ascontiguousarray(faces, np.uint32).reshape(-1, 4)
-        p = BuildParams(max_leaf_size, traversal_cost, intersect_cost, 0)
+        p = BuildParams(max_leaf_size, traversal_cost, intersect_cost, 0 if treelets else BUILD_NO_TREELETS)
         h = ctypes.c_void_p()
         check(load().gbrt_bvh_build_host(_ptr(v), len(v), _ptr(f), len(f), ctypes.byref(p), ctypes.byref(h)))
         return cls(h)
 
     @classmethod
     def build_device(cls, vertices_ptr, n_vertices, faces_ptr, n_faces, stream=0, max_leaf_size=0,
-                     traversal_cost=0.0, intersect_cost=0.0):
-        p = BuildParams(max_leaf_size, traversal_cost, intersect_cost, 0)
+                     traversal_cost=0.0, intersect_cost=0.0, treelets=True):
+        p = BuildParams(max_leaf_size, traversal_cost, intersect_cost, 0 if treelets else BUILD_NO_TREELETS)
         h = ctypes.c_void_p()
         check(load().gbrt_bvh_build(ctypes.c_void_p(vertices_ptr), n_vertices, ctypes.c_void_p(faces_ptr), n_faces,
                                     ctypes.byref(p), ctypes.c_void_p(stream), ctypes.byref(h)))
@@ -241,6 +246,19 @@ class Bvh:
         ids = np.empty(max(n, 1), np.uint32)
         check(load().gbrt_bvh_export(self._h, _ptr(nodes), nodes.nbytes, _ptr(prims), prims.nbytes, _ptr(ids), ids.nbytes))
         return nodes, prims[:n], ids[:n]
+
+    def export_wide(self):
+        """(nodes uint32 [n_nodes, 20], prims float32 [n,12], ids uint32 [n], depth): the 8-wide
+        compressed hierarchy the traversal walks."""
+        n = self.info()["n_prims"]
+        nn, depth = _U32(), _U32()
+        check(load().gbrt_bvh_export_wide(self._h, ctypes.byref(nn), ctypes.byref(depth), None, 0, None, 0, None, 0))
+        nodes = np.empty((max(nn.value, 1), 20), np.uint32)
+        prims = np.empty((max(n, 1), 12), np.float32)
+        ids = np.empty(max(n, 1), np.uint32)
+        check(load().gbrt_bvh_export_wide(self._h, None, None, _ptr(nodes), nodes.nbytes, _ptr(prims), prims.nbytes,
+                                          _ptr(ids), ids.nbytes))
+        return nodes[:nn.value], prims[:n], ids[:n], depth.value
 
     def trace_closest_host(self, rays):
         r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)

@@ -247,15 +247,17 @@ def test_trained_guide_lowers_error_at_equal_samples(cuda_device):
     """What the trained network gains: relMSE at 64 spp against an 8192-spp
     plain reference, guided (after online training) vs plain.  relMSE of a
     64-spp image of this scene is heavy-tailed (rare long paths through the
-    door gap), so the comparison is of medians over 12 independent images."""
+    door gap), so the comparison is of medians over 24 independent images.
+    Training is not deterministic (gradient atomics); after 48 passes the
+    gain measured 1.2-1.4x over three guide seeds, after 24 passes 1.0-1.2x."""
     r = gbrt.Renderer(_indoor_small())
     ref = np.mean([r.render(1024, base_offset=10_000_000 + b * 1024, seed=900 + b)[0] for b in range(8)], axis=0)
     guide = r.make_guide(log2_table=16, seed=4)
-    _train(r, guide, passes=24)
+    _train(r, guide, passes=48)
 
     def relmse(x):
         return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
-    ep = np.median([relmse(r.render(64, base_offset=b * 64, seed=70 + b)[0]) for b in range(12)])
-    eg = np.median([relmse(r.render(64, base_offset=b * 64, seed=70 + b, guide=guide, alpha=0.5)[0]) for b in range(12)])
+    ep = np.median([relmse(r.render(64, base_offset=b * 64, seed=70 + b)[0]) for b in range(24)])
+    eg = np.median([relmse(r.render(64, base_offset=b * 64, seed=70 + b, guide=guide, alpha=0.5)[0]) for b in range(24)])
     print(f"median relMSE at 64 spp: plain {ep:.4g}, guided {eg:.4g} (x{ep / eg:.2f})")
     assert eg < ep

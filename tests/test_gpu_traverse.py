@@ -159,3 +159,42 @@ def test_gpu_bvh_structure_random(dev):
         bvh = gbrt.Bvh.build_host(v, f, max_leaf_size=leaf)
         nodes, prims, ids = bvh.export()
         assert check_bvh(nodes, prims, ids, v, f) == []
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_gpu_wide_structure(dev, path):
+    from tests.bvh_check import check_wide
+    g = np.load(path)
+    bvh = gbrt.Bvh.build_host(g["vertices"], g["faces"])
+    nodes, prims, ids, depth = bvh.export_wide()
+    assert check_wide(nodes, prims, ids, g["vertices"], g["faces"], depth) == []
+
+
+def test_gpu_wide_structure_random(dev):
+    from tests.bvh_check import check_wide
+    v, f = scenes.random_triangles(30_000, seed=62)
+    for leaf in (1, 4, 16):
+        for treelets in (True, False):
+            bvh = gbrt.Bvh.build_host(v, f, max_leaf_size=leaf, treelets=treelets)
+            nodes, prims, ids, depth = bvh.export_wide()
+            assert check_wide(nodes, prims, ids, v, f, depth) == [], (leaf, treelets)
+            assert len(nodes) < len(f) // 2 and depth < 30
+
+
+def test_gpu_treelets_lower_sah_and_keep_results(dev):
+    """Treelet restructuring lowers the hierarchy's SAH cost; the binary
+    export stays a valid hierarchy and every query answer is unchanged."""
+    from tests.bvh_check import check_bvh
+    v, f = scenes.random_triangles(200_000, seed=63, spread=0.02)
+    plain = gbrt.Bvh.build_host(v, f, treelets=False)
+    opt = gbrt.Bvh.build_host(v, f)
+    s0, s1 = plain.info()["sah_cost"], opt.info()["sah_cost"]
+    print("SAH", s0, "->", s1)
+    assert s1 < 0.995 * s0
+    nodes, prims, ids = opt.export()
+    assert check_bvh(nodes, prims, ids, v, f) == []
+    r = scenes.random_rays(300_000, seed=64)
+    a = plain.trace_closest_host(r)
+    b = opt.trace_closest_host(r)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1].view(np.uint32), b[1].view(np.uint32))
+    assert np.array_equal(plain.trace_shadow_host(r) >= 0, opt.trace_shadow_host(r) >= 0)
