@@ -210,26 +210,78 @@ __global__ void k_hist(const uint32_t *__restrict__ keys, uint32_t n, int shift,
 	hist[threadIdx.x * nblk + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of m words by one block of 1024 threads (m <= a few million).
-__global__ void k_scan(uint32_t *__restrict__ data, uint32_t m)
+// Exclusive scan of m words in three launches: tiles of kScanTile words
+// scanned in place (tile sums to `totals`), the tile sums scanned by one
+// block, then added back.
+constexpr uint32_t kScanThreads = 1024, kScanItems = 4, kScanTile = kScanThreads * kScanItems;
+
+__host__ __device__ constexpr uint32_t scan_tiles(uint32_t m) { return (m + kScanTile - 1) / kScanTile; }
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &total)
 {
-	__shared__ uint32_t s[1024];
-	const uint32_t per = (m + 1023u) / 1024u;
-	const uint32_t lo = threadIdx.x * per;
-	const uint32_t hi = min(lo + per, m);
-	uint32_t sum = 0;
-	for(uint32_t i = lo; i < hi; ++i) sum += data[i];
-	s[threadIdx.x] = sum;
-	__syncthreads();
-	for(int off = 1; off < 1024; off <<= 1)
+	__shared__ uint32_t warp_sums[kScanThreads / 32];
+	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+	uint32_t x = v;
+	for(int off = 1; off < 32; off <<= 1)
 	{
-		const uint32_t v = threadIdx.x >= static_cast<unsigned>(off) ? s[threadIdx.x - off] : 0u;
-		__syncthreads();
-		s[threadIdx.x] += v;
-		__syncthreads();
+		const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+		if(lane >= static_cast<uint32_t>(off)) x += y;
 	}
-	uint32_t run = s[threadIdx.x] - sum;
-	for(uint32_t i = lo; i < hi; ++i) { const uint32_t x = data[i]; data[i] = run; run += x; }
+	if(lane == 31) warp_sums[warp] = x;
+	__syncthreads();
+	if(warp == 0)
+	{
+		uint32_t w = warp_sums[lane];
+		for(int off = 1; off < 32; off <<= 1)
+		{
+			const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, off);
+			if(lane >= static_cast<uint32_t>(off)) w += y;
+		}
+		warp_sums[lane] = w;
+	}
+	__syncthreads();
+	total = warp_sums[31];
+	const uint32_t before = warp ? warp_sums[warp - 1] : 0u;
+	__syncthreads();
+	return before + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(uint32_t *__restrict__ data, uint32_t m, uint32_t *__restrict__ totals)
+{
+	const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+	uint32_t v[kScanItems], sum = 0;
+	for(uint32_t k = 0; k < kScanItems; ++k) { v[k] = base + k < m ? data[base + k] : 0u; sum += v[k]; }
+	uint32_t total;
+	uint32_t run = block_exclusive_scan(sum, total);
+	for(uint32_t k = 0; k < kScanItems; ++k)
+	{
+		if(base + k < m) data[base + k] = run;
+		run += v[k];
+	}
+	if(threadIdx.x == 0) totals[blockIdx.x] = total;
+}
+
+// one block: exclusive scan of the tile sums (any count, in rounds of kScanThreads)
+__global__ void __launch_bounds__(kScanThreads) k_scan_totals(uint32_t *__restrict__ totals, uint32_t tiles)
+{
+	uint32_t carry = 0;
+	for(uint32_t b = 0; b < tiles; b += kScanThreads)
+	{
+		const uint32_t i = b + threadIdx.x;
+		const uint32_t v = i < tiles ? totals[i] : 0u;
+		uint32_t total;
+		const uint32_t ex = block_exclusive_scan(v, total);
+		if(i < tiles) totals[i] = carry + ex;
+		carry += total;
+	}
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_add(uint32_t *__restrict__ data, uint32_t m, const uint32_t *__restrict__ totals)
+{
+	const uint32_t add = totals[blockIdx.x];
+	const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+	for(uint32_t k = 0; k < kScanItems; ++k)
+		if(base + k < m) data[base + k] += add;
 }
 
 __global__ void k_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, uint32_t n, int shift,
@@ -395,12 +447,26 @@ __device__ __forceinline__ void ref_info(uint32_t ref, const uint32_t *__restric
 	}
 }
 
+// Per-warp shared arrays of the treelet dynamic programme.
+struct TreeletSmem {
+	float C[kTreeletSubsets];          // optimal cost of each leaf subset
+	float A[kTreeletSubsets];          // half area of its union box
+	uint32_t N[kTreeletSubsets];       // primitives under it
+	uint8_t split[kTreeletSubsets];    // best first part (contains the lowest leaf)
+};
+
 // Rebuilds the treelet under `root` as the SAH-optimal binary tree over the
-// same leaves, reusing its internal node indices.
-__device__ __noinline__ void restructure(uint32_t root, const uint32_t *__restrict__ vals, const float4 *__restrict__ box_lo,
-                                         const float4 *__restrict__ box_hi, uint2 *child, uint32_t *parent_int, uint32_t *parent_leaf,
-                                         float4 *node_lo, float4 *node_hi, uint32_t max_leaf, float ct, float ci)
+// same leaves, reusing its internal node indices; called by all 32 lanes of
+// a warp with the same root.  The treelet (at most 7 leaves, grown by
+// opening the leaf of largest area) is formed redundantly by every lane;
+// subset areas and the costs of the subsets of each size are computed
+// across the lanes; lane 0 writes the result.
+__device__ __noinline__ void restructure_warp(uint32_t root, TreeletSmem &sm, const uint32_t *__restrict__ vals,
+                                              const float4 *__restrict__ box_lo, const float4 *__restrict__ box_hi, uint2 *child,
+                                              uint32_t *parent_int, uint32_t *parent_leaf, float4 *node_lo, float4 *node_hi,
+                                              uint32_t max_leaf, float ct, float ci)
 {
+	const uint32_t lane = threadIdx.x & 31u;
 	uint32_t T[kTreeletLeaves], I[kTreeletLeaves - 1], cnt[kTreeletLeaves];
 	float4 lo[kTreeletLeaves], hi[kTreeletLeaves];
 	float cost[kTreeletLeaves];
@@ -412,7 +478,6 @@ __device__ __noinline__ void restructure(uint32_t root, const uint32_t *__restri
 		ref_info(c.x, vals, box_lo, box_hi, node_lo, node_hi, ci, lo[0], hi[0], cost[0], cnt[0]);
 		ref_info(c.y, vals, box_lo, box_hi, node_lo, node_hi, ci, lo[1], hi[1], cost[1], cnt[1]);
 	}
-	// grow the treelet: open the internal leaf of largest area
 	while(m < kTreeletLeaves)
 	{
 		int best = -1;
@@ -433,15 +498,11 @@ __device__ __noinline__ void restructure(uint32_t root, const uint32_t *__restri
 		ref_info(c.y, vals, box_lo, box_hi, node_lo, node_hi, ci, lo[m], hi[m], cost[m], cnt[m]);
 		++m;
 	}
-	if(m < 3) return;
-	// optimal cost of every leaf subset: c(S) = min(Ci A(S) N(S) [N <= max leaf],
-	// Ct A(S) + min over splits P of c(P) + c(S \ P))
+	if(m < 3) return;   // warp-uniform: every lane formed the same treelet
 	const uint32_t full = (1u << m) - 1u;
-	float C[kTreeletSubsets];
-	uint8_t split[kTreeletSubsets];
-	for(uint32_t S = 1; S <= full; ++S)
+	// union areas and counts of every subset, 32 subsets at a time
+	for(uint32_t S = lane + 1u; S <= full; S += 32u)
 	{
-		if(!(S & (S - 1u))) { C[S] = cost[__ffs(S) - 1]; split[S] = 0; continue; }
 		float4 L = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f), H = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
 		uint32_t N = 0;
 		for(int k = 0; k < m; ++k)
@@ -451,80 +512,115 @@ __device__ __noinline__ void restructure(uint32_t root, const uint32_t *__restri
 				H.x = fmaxf(H.x, hi[k].x); H.y = fmaxf(H.y, hi[k].y); H.z = fmaxf(H.z, hi[k].z);
 				N += cnt[k];
 			}
-		const float A = half_area(L, H);
-		const uint32_t low = S & (0u - S);
-		float best = FLT_MAX;
-		uint32_t bp = low;
-		for(uint32_t P = (S - 1u) & S; P; P = (P - 1u) & S)
-			if(P & low)
-			{
-				const float c = C[P] + C[S ^ P];
-				if(c < best) { best = c; bp = P; }
-			}
-		const float c_int = ct * A + best;
-		const float c_leaf = N <= max_leaf ? ci * A * static_cast<float>(N) : FLT_MAX;
-		C[S] = c_leaf <= c_int ? c_leaf : c_int;
-		split[S] = static_cast<uint8_t>(bp);
+		sm.A[S] = half_area(L, H);
+		sm.N[S] = N;
+		if(!(S & (S - 1u))) { sm.C[S] = cost[__ffs(S) - 1]; sm.split[S] = 0; }
 	}
-	// rewrite: the root keeps its index, the other internal nodes are reused
-	uint32_t stS[kTreeletLeaves], stN[kTreeletLeaves];
-	uint32_t ordS[kTreeletLeaves], ordN[kTreeletLeaves];
-	int sp = 1, no = 0, next = 1;
-	stS[0] = full; stN[0] = root;
-	while(sp > 0)
+	__syncwarp();
+	// c(S) = min(Ci A(S) N(S) [N <= max leaf], Ct A(S) + min over splits P of c(P) + c(S \ P)),
+	// the subsets of one size at a time
+	for(int size = 2; size <= m; ++size)
 	{
-		--sp;
-		const uint32_t S = stS[sp], nd = stN[sp];
-		ordS[no] = S; ordN[no] = nd; ++no;
-		const uint32_t sub[2] = {split[S], S ^ split[S]};
-		uint32_t ref[2];
-		for(int k = 0; k < 2; ++k)
+		for(uint32_t S = lane + 1u; S <= full; S += 32u)
 		{
-			if(!(sub[k] & (sub[k] - 1u))) ref[k] = T[__ffs(sub[k]) - 1];
-			else { ref[k] = I[next++]; stS[sp] = sub[k]; stN[sp] = ref[k]; ++sp; }
-			if(ref[k] & GBRT_LEAF_BIT) parent_leaf[ref[k] & ~GBRT_LEAF_BIT] = nd;
-			else parent_int[ref[k]] = nd;
+			if(__popc(S) != size) continue;
+			const uint32_t low = S & (0u - S);
+			float best = FLT_MAX;
+			uint32_t bp = low;
+			for(uint32_t P = (S - 1u) & S; P; P = (P - 1u) & S)
+				if(P & low)
+				{
+					const float c = sm.C[P] + sm.C[S ^ P];
+					if(c < best) { best = c; bp = P; }
+				}
+			const float A = sm.A[S];
+			const float c_int = ct * A + best;
+			const float c_leaf = sm.N[S] <= max_leaf ? ci * A * static_cast<float>(sm.N[S]) : FLT_MAX;
+			sm.C[S] = c_leaf <= c_int ? c_leaf : c_int;
+			sm.split[S] = static_cast<uint8_t>(bp);
 		}
-		child[nd] = make_uint2(ref[0], ref[1]);
+		__syncwarp();
 	}
-	for(int q = 0; q < no; ++q)
+	if(lane == 0)
 	{
-		const uint32_t S = ordS[q];
-		float4 L = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f), H = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
-		uint32_t N = 0;
-		for(int k = 0; k < m; ++k)
-			if((S >> k) & 1u)
+		// rewrite: the root keeps its index, the other internal nodes are reused
+		uint32_t stS[kTreeletLeaves], stN[kTreeletLeaves];
+		int sp = 1, next = 1;
+		stS[0] = full; stN[0] = root;
+		while(sp > 0)
+		{
+			--sp;
+			const uint32_t S = stS[sp], nd = stN[sp];
+			const uint32_t sub[2] = {sm.split[S], S ^ sm.split[S]};
+			uint32_t ref[2];
+			for(int k = 0; k < 2; ++k)
 			{
-				L.x = fminf(L.x, lo[k].x); L.y = fminf(L.y, lo[k].y); L.z = fminf(L.z, lo[k].z);
-				H.x = fmaxf(H.x, hi[k].x); H.y = fmaxf(H.y, hi[k].y); H.z = fmaxf(H.z, hi[k].z);
-				N += cnt[k];
+				if(!(sub[k] & (sub[k] - 1u))) ref[k] = T[__ffs(sub[k]) - 1];
+				else { ref[k] = I[next++]; stS[sp] = sub[k]; stN[sp] = ref[k]; ++sp; }
+				if(ref[k] & GBRT_LEAF_BIT) parent_leaf[ref[k] & ~GBRT_LEAF_BIT] = nd;
+				else parent_int[ref[k]] = nd;
 			}
-		L.w = C[S];
-		H.w = __uint_as_float(N);
-		node_lo[ordN[q]] = L;
-		node_hi[ordN[q]] = H;
+			child[nd] = make_uint2(ref[0], ref[1]);
+			float4 L = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f), H = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
+			for(int k = 0; k < m; ++k)
+				if((S >> k) & 1u)
+				{
+					L.x = fminf(L.x, lo[k].x); L.y = fminf(L.y, lo[k].y); L.z = fminf(L.z, lo[k].z);
+					H.x = fmaxf(H.x, hi[k].x); H.y = fmaxf(H.y, hi[k].y); H.z = fmaxf(H.z, hi[k].z);
+				}
+			L.w = sm.C[S];
+			H.w = __uint_as_float(sm.N[S]);
+			node_lo[nd] = L;
+			node_hi[nd] = H;
+		}
+		__threadfence();
 	}
+	__syncwarp();
 }
 
+constexpr int kTreeletThreads = 128;
+
 // Bottom-up like k_refit: the second thread to reach a node owns it, and its
-// whole subtree is final.  Nodes holding at least gamma primitives are
-// restructured.
-__global__ void k_treelet(int n, const uint32_t *__restrict__ vals, const float4 *__restrict__ box_lo, const float4 *__restrict__ box_hi,
-                          uint2 *child, uint32_t *parent_int, uint32_t *parent_leaf, float4 *node_lo, float4 *node_hi,
-                          uint32_t *flags, uint32_t gamma, uint32_t max_leaf, float ct, float ci, float *meta)
+// whole subtree is final.  Owned nodes holding at least gamma primitives are
+// restructured, one at a time per warp with the whole warp; every lane stays
+// in the loop (full-warp ballots) until all lanes of the warp are done.
+__global__ void __launch_bounds__(kTreeletThreads)
+k_treelet(int n, const uint32_t *__restrict__ vals, const float4 *__restrict__ box_lo, const float4 *__restrict__ box_hi,
+          uint2 *child, uint32_t *parent_int, uint32_t *parent_leaf, float4 *node_lo, float4 *node_hi,
+          uint32_t *flags, uint32_t gamma, uint32_t max_leaf, float ct, float ci, float *meta)
 {
+	__shared__ TreeletSmem smem[kTreeletThreads / 32];
+	TreeletSmem &sm = smem[threadIdx.x >> 5];
 	const int j = blockIdx.x * blockDim.x + threadIdx.x;
-	if(j >= n) return;
-	uint32_t p = __ldcg(parent_leaf + j);
-	for(int walk = 0; p != kNoParent; ++walk)
+	bool active = j < n;
+	uint32_t p = active ? __ldcg(parent_leaf + j) : kNoParent;
+	active = active && p != kNoParent;
+	for(int walk = 0; __any_sync(0xFFFFFFFFu, active); ++walk)
 	{
-		if(walk == kMaxWalk) { raise_err(meta, kErrWalk); return; }
-		__threadfence();
-		if(atomicAdd(&flags[p], 1u) == 0u) return;
-		__threadfence();
-		if(__float_as_uint(__ldcg(node_hi + p).w) >= gamma)
-			restructure(p, vals, box_lo, box_hi, child, parent_int, parent_leaf, node_lo, node_hi, max_leaf, ct, ci);
-		p = __ldcg(parent_int + p);
+		bool own = false;
+		if(active)
+		{
+			if(walk == kMaxWalk) { raise_err(meta, kErrWalk); active = false; }
+			else
+			{
+				__threadfence();
+				if(atomicAdd(&flags[p], 1u) == 0u) active = false;
+				else { __threadfence(); own = __float_as_uint(__ldcg(node_hi + p).w) >= gamma; }
+			}
+		}
+		uint32_t todo = __ballot_sync(0xFFFFFFFFu, own);
+		while(todo)
+		{
+			const int l = __ffs(todo) - 1;
+			todo &= todo - 1u;
+			const uint32_t root = __shfl_sync(0xFFFFFFFFu, p, l);
+			restructure_warp(root, sm, vals, box_lo, box_hi, child, parent_int, parent_leaf, node_lo, node_hi, max_leaf, ct, ci);
+		}
+		if(active)
+		{
+			p = __ldcg(parent_int + p);
+			active = p != kNoParent;
+		}
 	}
 }
 
@@ -948,7 +1044,10 @@ cudaError_t build_binary(BinaryBufs &B, const float *verts, const uint32_t *face
 	for(int shift = 0; shift < 30; shift += 8)
 	{
 		k_hist<<<nblk, kSortThreads, 0, s>>>(kin, nf, shift, B.hist, nblk);
-		k_scan<<<1, 1024, 0, s>>>(B.hist, 256u * nblk);
+		const uint32_t hw = 256u * nblk, tiles = scan_tiles(hw);
+		k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(B.hist, hw, B.hist + hw);
+		k_scan_totals<<<1, kScanThreads, 0, s>>>(B.hist + hw, tiles);
+		k_scan_add<<<tiles, kScanThreads, 0, s>>>(B.hist, hw, B.hist + hw);
 		k_scatter<<<nblk, kSortThreads, 0, s>>>(kin, vin, nf, shift, B.hist, nblk, kout, vout);
 		std::swap(kin, kout); std::swap(vin, vout);
 	}
@@ -962,7 +1061,7 @@ cudaError_t build_binary(BinaryBufs &B, const float *verts, const uint32_t *face
 		for(uint32_t gamma : kTreeletGamma)
 		{
 			if((e = cudaMemsetAsync(B.flags, 0, 4ull * n_int, s)) != cudaSuccess) return e;
-			k_treelet<<<blocks_for(nf, 128), 128, 0, s>>>(static_cast<int>(nf), vin, B.blo, B.bhi, B.child, B.pint, B.pleaf, B.nlo, B.nhi,
+			k_treelet<<<blocks_for(nf, kTreeletThreads), kTreeletThreads, 0, s>>>(static_cast<int>(nf), vin, B.blo, B.bhi, B.child, B.pint, B.pleaf, B.nlo, B.nhi,
 			                                              B.flags, gamma, p.max_leaf_size, p.traversal_cost, p.intersect_cost, meta);
 		}
 		if((e = cudaMemsetAsync(B.flags, 0, 4ull * n_int, s)) != cudaSuccess) return e;
@@ -1032,7 +1131,7 @@ int gbrt_build_impl(const float *verts, uint32_t nv, const uint32_t *faces, uint
 
 	// scratch carve-up (one stream-ordered allocation)
 	const uint32_t nblk = blocks_for(nf, kSortTile);
-	const size_t hist_words = 256ull * nblk;
+	const size_t hist_words = 256ull * nblk + scan_tiles(256u * nblk);   // digit counts + scan tile sums
 	size_t off = 0;
 	auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
 	const size_t o_blo = carve(16ull * nf), o_bhi = carve(16ull * nf);
@@ -1123,7 +1222,7 @@ constexpr StaticLayout static_layout(uint64_t nf)
 	L.k1 = o; o += round256(4 * nf);
 	L.v0 = o; o += round256(4 * nf);
 	L.v1 = o; o += round256(4 * nf);
-	L.hist = o; o += round256(4 * 256 * nblk);
+	L.hist = o; o += round256(4 * (256 * nblk + scan_tiles(static_cast<uint32_t>(256 * nblk))));
 	L.child = o; o += round256(8 * n_int);
 	L.range = o; o += round256(8 * n_int);
 	L.pint = o; o += round256(4 * n_int);

@@ -1098,22 +1098,26 @@ __global__ void __launch_bounds__(kThreads) k_camera(Camera cam, Params P, Work 
 }
 
 __global__ void __launch_bounds__(kThreads) k_extend(gbrt::BvhView bv, const float4 *__restrict__ rays, const uint32_t *__restrict__ count,
-                                                     float4 *__restrict__ hits, float *__restrict__ hitpos)
+                                                     uint32_t *counter, float4 *__restrict__ hits, float *__restrict__ hitpos)
 {
 	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
-	const uint32_t n = *count;
-	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-	{
-		const float4 a = rays[2ull * i], b = rays[2ull * i + 1];
-		const gbrt::Hit h = gbrt::trace_ray<false>(bv, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, stack + threadIdx.x, kThreads);
-		hits[i] = make_float4(__int_as_float(h.prim), h.t, h.u, h.v);
-		if(hitpos)
-		{
-			hitpos[3ull * i] = xa(a.x, xm(h.t, b.x));
-			hitpos[3ull * i + 1] = xa(a.y, xm(h.t, b.y));
-			hitpos[3ull * i + 2] = xa(a.z, xm(h.t, b.z));
-		}
-	}
+	gbrt::trace_persistent<false>(
+		bv, *count, counter, stack + threadIdx.x, kThreads,
+		[&](uint32_t i, float r[8]) {
+			const float4 a = rays[2ull * i], b = rays[2ull * i + 1];
+			r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w; r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+			return true;
+		},
+		[&](uint32_t i, const gbrt::Hit &h) {
+			hits[i] = make_float4(__int_as_float(h.prim), h.t, h.u, h.v);
+			if(hitpos)
+			{
+				const float4 a = rays[2ull * i], b = rays[2ull * i + 1];
+				hitpos[3ull * i] = xa(a.x, xm(h.t, b.x));
+				hitpos[3ull * i + 1] = xa(a.y, xm(h.t, b.y));
+				hitpos[3ull * i + 2] = xa(a.z, xm(h.t, b.z));
+			}
+		});
 }
 
 __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work W, int cur, int resx, uint32_t shadow_cap,
@@ -1504,20 +1508,23 @@ __global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Work W, u
 	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
 	const uint32_t n = min(W.count[2], shadow_cap);
 	uint32_t traced = 0;
-	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-	{
-		const uint32_t pixel = W.s_pix[i];
-		if(pixel == kDead) continue;
-		const float4 a = W.s_ray[2ull * i], b = W.s_ray[2ull * i + 1];
-		const gbrt::Hit h = gbrt::trace_ray<true>(bv, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, stack + threadIdx.x, kThreads);
-		++traced;
-		if(h.prim < 0)
-		{
-			const float4 c = W.s_col[i];
-			film_add(film, film64, pixel, c.x, c.y, c.z);
-			if(W.p_sum) path_sum_add(W, W.s_path[i], c.x, c.y, c.z);
-		}
-	}
+	gbrt::trace_persistent<true>(
+		bv, n, W.count + 5, stack + threadIdx.x, kThreads,
+		[&](uint32_t i, float r[8]) {
+			if(W.s_pix[i] == kDead) return false;
+			const float4 a = W.s_ray[2ull * i], b = W.s_ray[2ull * i + 1];
+			r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w; r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+			++traced;
+			return true;
+		},
+		[&](uint32_t i, const gbrt::Hit &h) {
+			if(h.prim < 0)
+			{
+				const float4 c = W.s_col[i];
+				film_add(film, film64, W.s_pix[i], c.x, c.y, c.z);
+				if(W.p_sum) path_sum_add(W, W.s_path[i], c.x, c.y, c.z);
+			}
+		});
 	for(int off = 16; off > 0; off >>= 1) traced += __shfl_xor_sync(0xffffffffu, traced, off);
 	if((threadIdx.x & 31u) == 0 && traced) atomicAdd(W.stats + 1, static_cast<unsigned long long>(traced));
 }
@@ -1582,7 +1589,9 @@ __global__ void k_gather_batch(const float4 *__restrict__ rec, uint32_t n, uint3
 	}
 }
 
-__global__ void k_reset(uint32_t *count, int which) { count[which] = 0u; count[2] = 0u; }
+// Queue counts of the next vertex level; count[4] / count[5] are the chunk
+// counters of k_extend / k_shadow (gbrt::trace_persistent).
+__global__ void k_reset(uint32_t *count, int which) { count[which] = 0u; count[2] = 0u; count[4] = 0u; count[5] = 0u; }
 
 // Spawned integrate() calls -> paths of a new wave (dead records skipped,
 // live ones compacted into path slots and the first ray queue).
@@ -2296,6 +2305,18 @@ unsigned grid_for(size_t n, int n_sm)
 	return static_cast<unsigned>(std::max<size_t>(1, std::min(want, cap)));
 }
 
+// Grid of a gbrt::trace_persistent kernel: the blocks that fit on the GPU at
+// once, no more than n queries need.
+template <typename K>
+unsigned persistent_grid(K kernel, size_t n, int n_sm)
+{
+	int bps = 0;
+	if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, kThreads, 0) != cudaSuccess || bps < 1) bps = 1;
+	const size_t want = (n + kThreads - 1) / kThreads;
+	const size_t cap = static_cast<size_t>(n_sm > 0 ? n_sm : 148) * static_cast<size_t>(bps);
+	return static_cast<unsigned>(std::max<size_t>(1, std::min(want, cap)));
+}
+
 
 // ---- photon maps (host side) ------------------------------------------------
 
@@ -2728,13 +2749,15 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 			Pw.guiding = level_guided ? 1 : 0;
 			Pw.record = (camera_wave && record && (pp.guide_max_vertex == 0 || vtx < static_cast<int>(pp.guide_max_vertex))) ? 1 : 0;
 			k_reset<<<1, 1, 0, s>>>(Ww.count, cur ^ 1);
-			k_extend<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc.bv, Ww.q_ray[cur], Ww.count + cur, Ww.hits, level_guided ? Ww.hitpos : nullptr);
+			k_extend<<<persistent_grid(k_extend, n, S->n_sm), kThreads, 0, s>>>(sc.bv, Ww.q_ray[cur], Ww.count + cur, Ww.count + 4, Ww.hits,
+			                                                                     level_guided ? Ww.hitpos : nullptr);
 			if(vtx == 0 && Pw.pm && (Pw.pm_caustics || (Pw.pm_diffuse && !Pw.pm_fg)))
 				k_pm_root<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, film, film64_dev);
 			if(level_guided)
 				if(int rc = gbrt_guide_eval_queue(guide, Ww.hitpos, n, Ww.count + cur, Ww.lobes, s)) return rc;
 			k_shade<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, camera->resx, static_cast<uint32_t>(shadow_cap), film, film64_dev);
-			k_shadow<<<grid_for(shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Ww, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+			k_shadow<<<persistent_grid(k_shadow, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Ww, static_cast<uint32_t>(shadow_cap), film,
+			                                                                             film64_dev);
 			cur ^= 1;
 		}
 		return GBRT_OK;

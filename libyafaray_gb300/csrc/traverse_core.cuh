@@ -324,4 +324,60 @@ __device__ __forceinline__ Hit trace_ray(const BvhView &bv, float ox, float oy, 
 	return trace_result(S);
 }
 
+// Persistent-warp driver for a batch of n queries (Aila & Laine,
+// "Understanding the efficiency of ray traversal on GPUs", HPG 2009, with
+// dynamic fetch): each warp takes chunks of kTraceChunk query indices from
+// *counter (zero before the launch); a lane whose query is answered takes
+// the warp's next index at the top of the following step, so lanes do not
+// idle while the slowest ray of their warp finishes, and warps that draw
+// expensive rays do not hold up the launch.  Launch with every thread of
+// every warp (the loop uses full-warp ballots) and a grid that fits on the
+// GPU at once.
+//   load(i, ray[8]) -> bool   false: entry i holds no query (skipped)
+//   store(i, const Hit &)     the answer of query i
+constexpr uint32_t kTraceChunk = 32;
+
+template <bool kShadow, typename Load, typename Store>
+__device__ __forceinline__ void trace_persistent(const BvhView &bv, uint32_t n, uint32_t *counter, uint2 *sh, int stride, Load &&load,
+                                                 Store &&store)
+{
+	uint2 spill[kTraceStack - kStackShared];
+	const uint32_t lane = threadIdx.x & 31u;
+	uint32_t next = 0, end = 0;      // the warp's current chunk (warp-uniform)
+	bool exhausted = false;
+	TraceState S;
+	bool active = false;
+	uint32_t idx = 0;
+	while(true)
+	{
+		const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !active);
+		if(idle && next >= end && !exhausted)
+		{
+			uint32_t b = 0;
+			if(lane == 0) b = atomicAdd(counter, kTraceChunk);
+			b = __shfl_sync(0xFFFFFFFFu, b, 0);
+			if(b >= n) exhausted = true;
+			else { next = b; end = min(b + kTraceChunk, n); }
+		}
+		if(idle == 0xFFFFFFFFu && exhausted) break;
+		if(idle && next < end)
+		{
+			const uint32_t mine = next + __popc(idle & ((1u << lane) - 1u));
+			next = min(next + static_cast<uint32_t>(__popc(idle)), end);
+			float r[8];
+			if(!active && mine < end && load(mine, r))
+			{
+				idx = mine;
+				active = trace_init<kShadow>(S, bv, r[0], r[1], r[2], r[3], r[4], r[5], r[6], r[7]);
+				if(!active) store(idx, Hit{-1, 0.f, 0.f, 0.f});
+			}
+		}
+		if(active && trace_step<kShadow>(S, bv, sh, stride, spill))
+		{
+			store(idx, trace_result(S));
+			active = false;
+		}
+	}
+}
+
 } // namespace gbrt
