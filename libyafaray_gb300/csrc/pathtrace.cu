@@ -2157,18 +2157,38 @@ struct gbrt_scene {
 	uint32_t *spawn_count = nullptr;
 	size_t spawn_cap = 0;
 	int spawn_levels = 0;
+	cudaEvent_t ev_last = nullptr;      // recorded after each render: the buffers' last use
 	std::mutex mu;
 };
 
 namespace {
 
-int alloc_work(gbrt_scene *S, size_t paths, size_t shadow, size_t stride)
+// The render buffers below are stream-ordered allocations from the device's
+// default pool, which keeps freed memory for reuse: growing or releasing
+// them does not synchronise the device, so scenes rendered concurrently on
+// their own streams (gbrt_pt_render_batch) do not stall each other.
+void pool_retain(int dev)
+{
+	static std::atomic<uint64_t> done{0};
+	if(dev < 0 || dev >= 64 || ((done.load() >> dev) & 1u)) return;
+	cudaMemPool_t pool;
+	if(cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+	{
+		uint64_t keep = ~0ull;
+		cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+	}
+	done.fetch_or(1ull << dev);
+}
+
+int alloc_work(gbrt_scene *S, size_t paths, size_t shadow, size_t stride, cudaStream_t s)
 {
 	if(paths <= S->cap_paths && shadow <= S->cap_shadow && stride <= S->cap_stride) return GBRT_OK;
 	paths = std::max(paths, S->cap_paths);
 	shadow = std::max(shadow, S->cap_shadow);
 	stride = std::max(stride, S->cap_stride);
-	if(S->work) { cudaFree(S->work); S->work = nullptr; }
+	pool_retain(S->device);
+	if(S->ev_last) cudaStreamWaitEvent(s, S->ev_last, 0);
+	if(S->work) { cudaFreeAsync(S->work, s); S->work = nullptr; }
 	size_t off = 0;
 	auto carve = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
 	const size_t o_pix = carve(4 * paths), o_si = carve(4 * paths), o_st = carve(4 * paths), o_thr = carve(16 * paths);
@@ -2185,7 +2205,7 @@ int alloc_work(gbrt_scene *S, size_t paths, size_t shadow, size_t stride)
 		o_rpos = carve(16 * recs); o_rdir = carve(16 * recs); o_rthr = carve(16 * recs); o_rpre = carve(16 * recs);
 		o_rval = carve(4 * recs); o_train = carve(32 * (recs + kMaxBatch));
 	}
-	cudaError_t e = cudaMalloc(&S->work, off);
+	cudaError_t e = cudaMallocAsync(&S->work, off, s);
 	if(e != cudaSuccess) { S->work = nullptr; S->cap_paths = S->cap_shadow = S->cap_stride = 0; return gbrt_set_error(GBRT_ERR_OOM, "path tracer work buffers (%zu bytes): %s", off, cudaGetErrorString(e)); }
 	char *b = static_cast<char *>(S->work);
 	Work &w = S->w;
@@ -2226,16 +2246,18 @@ int alloc_work(gbrt_scene *S, size_t paths, size_t shadow, size_t stride)
 	return GBRT_OK;
 }
 
-int alloc_spawn(gbrt_scene *S, size_t cap, int levels)
+int alloc_spawn(gbrt_scene *S, size_t cap, int levels, cudaStream_t s)
 {
 	if(cap <= S->spawn_cap && levels <= S->spawn_levels) return GBRT_OK;
 	cap = std::max(cap, S->spawn_cap);
 	levels = std::max(levels, S->spawn_levels);
-	if(S->spawn) { cudaFree(S->spawn); S->spawn = nullptr; }
-	if(S->spawn_count) { cudaFree(S->spawn_count); S->spawn_count = nullptr; }
+	pool_retain(S->device);
+	if(S->ev_last) cudaStreamWaitEvent(s, S->ev_last, 0);
+	if(S->spawn) { cudaFreeAsync(S->spawn, s); S->spawn = nullptr; }
+	if(S->spawn_count) { cudaFreeAsync(S->spawn_count, s); S->spawn_count = nullptr; }
 	S->spawn_cap = 0; S->spawn_levels = 0;
-	cudaError_t e = cudaMalloc(&S->spawn, cap * levels * 5 * sizeof(float4));
-	if(e == cudaSuccess) e = cudaMalloc(&S->spawn_count, levels * sizeof(uint32_t));
+	cudaError_t e = cudaMallocAsync(&S->spawn, cap * levels * 5 * sizeof(float4), s);
+	if(e == cudaSuccess) e = cudaMallocAsync(&S->spawn_count, levels * sizeof(uint32_t), s);
 	if(e != cudaSuccess)
 		return gbrt_set_error(GBRT_ERR_OOM, "recursive split buffers (%zu records x %d levels): %s", cap, levels, cudaGetErrorString(e));
 	S->spawn_cap = cap;
@@ -2244,11 +2266,12 @@ int alloc_spawn(gbrt_scene *S, size_t cap, int levels)
 }
 
 // Frees a scene's work and spawn buffers (they are re-made by the next render).
-void release_work(gbrt_scene *S)
+void release_work(gbrt_scene *S, cudaStream_t s)
 {
-	if(S->work) cudaFree(S->work);
-	if(S->spawn) cudaFree(S->spawn);
-	if(S->spawn_count) cudaFree(S->spawn_count);
+	if(S->ev_last) cudaStreamWaitEvent(s, S->ev_last, 0);
+	if(S->work) cudaFreeAsync(S->work, s);
+	if(S->spawn) cudaFreeAsync(S->spawn, s);
+	if(S->spawn_count) cudaFreeAsync(S->spawn_count, s);
 	S->work = nullptr; S->spawn = nullptr; S->spawn_count = nullptr;
 	S->w = Work{};
 	S->cap_paths = S->cap_shadow = S->cap_stride = 0;
@@ -2310,8 +2333,14 @@ unsigned grid_for(size_t n, int n_sm)
 template <typename K>
 unsigned persistent_grid(K kernel, size_t n, int n_sm)
 {
-	int bps = 0;
-	if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, kThreads, 0) != cudaSuccess || bps < 1) bps = 1;
+	// resident blocks per SM, queried once per kernel (all devices are GB300s)
+	static std::atomic<int> cached{0};
+	int bps = cached.load(std::memory_order_relaxed);
+	if(bps == 0)
+	{
+		if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, kThreads, 0) != cudaSuccess || bps < 1) bps = 1;
+		cached.store(bps, std::memory_order_relaxed);
+	}
 	const size_t want = (n + kThreads - 1) / kThreads;
 	const size_t cap = static_cast<size_t>(n_sm > 0 ? n_sm : 148) * static_cast<size_t>(bps);
 	return static_cast<unsigned>(std::max<size_t>(1, std::min(want, cap)));
@@ -2642,6 +2671,7 @@ int gbrt_scene_destroy(gbrt_scene *S)
 	void *ptrs[] = {S->prim_ng, S->mats, S->lights, S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off,
 	                S->lds_sfac_nd, S->work, S->spawn, S->spawn_count};
 	for(void *p : ptrs) if(p) cudaFree(p);
+	if(S->ev_last) cudaEventDestroy(S->ev_last);
 	delete S;
 	return GBRT_OK;
 }
@@ -2693,19 +2723,17 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 		wave = std::max<uint64_t>(1, std::min<uint64_t>(wave, roots * ps));
 		spawn_cap = static_cast<size_t>((wave / ps + 2) * fanout);
 		chunk = std::max<uint64_t>(1, std::min<uint64_t>(wave, (spawn_cap / fanout - 1) * n_min));
-		if(int rc = alloc_spawn(S, spawn_cap, split_levels)) return rc;
+		if(int rc = alloc_spawn(S, spawn_cap, split_levels, s)) return rc;
 	}
 	uint32_t max_shadow = 0;
 	{
-		std::vector<DevLight> ls(S->n_lights);
-		if(S->n_lights) GBRT_CK(cudaMemcpy(ls.data(), S->lights, ls.size() * sizeof(DevLight), cudaMemcpyDeviceToHost));
 		uint32_t all = 0, one = 0;
-		for(const auto &l : ls) { all += 2u * l.samples; one = std::max(one, 2u * static_cast<uint32_t>(l.samples)); }
+		for(const auto &l : S->lights_host) { all += 2u * l.samples; one = std::max(one, 2u * static_cast<uint32_t>(l.samples)); }
 		max_shadow = std::max(all, one);
 	}
 	const size_t shadow_cap = std::max<size_t>(1, wave * max_shadow);
 	const uint32_t stride = static_cast<uint32_t>(std::max(1, pp.bounces));
-	if(int rc = alloc_work(S, wave, shadow_cap, guide ? stride : 0)) return rc;
+	if(int rc = alloc_work(S, wave, shadow_cap, guide ? stride : 0, s)) return rc;
 	Camera cam = make_camera(*camera);
 	SceneDev sc{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off, S->lds_sfac_nd}};
 	Params P{};
@@ -2839,6 +2867,8 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 			if(int rc = process_level(1, nc)) return rc;
 	}
 	GBRT_CK(cudaGetLastError());
+	if(!S->ev_last) GBRT_CK(cudaEventCreateWithFlags(&S->ev_last, cudaEventDisableTiming));
+	GBRT_CK(cudaEventRecord(S->ev_last, s));
 	if(stats)
 	{
 		GBRT_CK(cudaEventRecord(e1, s));
@@ -3191,7 +3221,7 @@ int gbrt_pt_render_batch(gbrt_scene *const *scenes, const gbrt_camera_desc *came
 			if(!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "scene %u: stream error", i);
 			{
 				std::lock_guard<std::mutex> lock(S->mu);
-				release_work(S);                                  // the next scenes need the memory
+				release_work(S, st);                              // back to the pool for the next scenes
 			}
 			if(rc)
 			{

@@ -5,6 +5,8 @@
 // chunks from a per-launch counter.
 #include "traverse_core.cuh"
 
+#include <atomic>
+
 namespace {
 
 constexpr int kTraceThreads = 128;
@@ -37,11 +39,19 @@ template <bool kShadow>
 int launch(const gbrt_bvh *b, const gbrt_ray *rays, uint32_t n, gbrt_hit *hits, int32_t *occ, cudaStream_t s)
 {
 	if(n == 0) return GBRT_OK;
-	int dev = 0, n_sm = 0, bps = 0;
-	GBRT_CK(cudaGetDevice(&dev));
-	GBRT_CK(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
-	GBRT_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace<kShadow>, kTraceThreads, 0));
-	if(bps < 1) bps = 1;
+	// SM count and resident blocks per SM, queried once per kernel
+	static std::atomic<int> cached_sm{0}, cached_bps{0};
+	int n_sm = cached_sm.load(std::memory_order_relaxed), bps = cached_bps.load(std::memory_order_relaxed);
+	if(n_sm == 0 || bps == 0)
+	{
+		int dev = 0;
+		GBRT_CK(cudaGetDevice(&dev));
+		GBRT_CK(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+		GBRT_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace<kShadow>, kTraceThreads, 0));
+		if(bps < 1) bps = 1;
+		cached_sm.store(n_sm, std::memory_order_relaxed);
+		cached_bps.store(bps, std::memory_order_relaxed);
+	}
 	const uint64_t warps_needed = (n + gbrt::kTraceChunk - 1) / gbrt::kTraceChunk;
 	const uint64_t warps_resident = static_cast<uint64_t>(n_sm) * bps * (kTraceThreads / 32);
 	const uint64_t warps = warps_needed < warps_resident ? warps_needed : warps_resident;
