@@ -255,7 +255,22 @@ typedef struct gbrt_pt_params {
 	uint32_t guide_max_vertex;  /* guide (and record) only vertices 0 .. guide_max_vertex - 1; 0 = all */
 	int32_t raydepth;           /* "raydepth": last ray level of the recursive glossy / specular split
 	                               (MonteCarloIntegrator::recursiveRaytrace); 0 = 5 */
+	/* Film filter (ImageFilm "filter_type", "AA_pixelwidth"; imagefilm.cc:231-264, 771-822).
+	 * GBRT_FILTER_PIXEL (0): each sample lands in its own pixel only and the
+	 * film holds plain sums (mean = sum / spp).  Any other type splats every
+	 * sample over the reference's filter footprint and adds the filter weights
+	 * to film_weight_dev (device, resx * resy floats, caller-zeroed); the
+	 * image is sum / weight per pixel, as ImageFilm::flush normalises. */
+	uint32_t filter_type;
+	float aa_pixel_width;       /* 0 = 1.5 (the reference's default) */
+	float *film_weight_dev;
 } gbrt_pt_params;
+
+#define GBRT_FILTER_PIXEL 0u
+#define GBRT_FILTER_BOX 1u
+#define GBRT_FILTER_GAUSS 2u
+#define GBRT_FILTER_MITCHELL 3u
+#define GBRT_FILTER_LANCZOS 4u
 
 typedef struct gbrt_pt_stats {
 	uint64_t camera_samples;

@@ -108,6 +108,13 @@ struct Params {
 	float pm_diffuse_paths, pm_caustic_paths;
 	float pm_lookup_r2;        // 4 diffuse_radius^2 (integrator_photon_mapping.h:90)
 	gbrt::PhotonGrid g_diffuse, g_caustic, g_radiance;
+	// film filter (ImageFilm::addSample): film_w = per-pixel weight sums, or
+	// NULL for the single-pixel splat whose weights are the sample counts
+	float *film_w;
+	const float *filter_tab;   // 16 x 16 filter table
+	float filter_width;        // filter_width_ (pixels)
+	float filter_scale;        // filter_table_scale_
+	int film_resx, film_resy;
 };
 
 struct Work {
@@ -1044,6 +1051,62 @@ __device__ __forceinline__ uint32_t pixel_offset(uint32_t pixel, int resx)
 	return gbrt::fnv32(y * gbrt::fnv32(x));      // integrator_tiled.cc:297
 }
 
+// ImageFilm::roundToIntWithBias (imagefilm.h:344-348): + (0.5 - 1.4e-11), truncated.
+__device__ __forceinline__ int round_bias(double v) { return static_cast<int>(v + (0.5 - 1.4e-11)); }
+
+// Sub-pixel position of camera sample si (TiledIntegrator::renderTile,
+// integrator_tiled.cc:316-323): pixel centre for one sample, else
+// ((0.5 + s) / n, riLp(s + pixel offset)).
+__device__ __forceinline__ void sample_pos(const Params &P, uint32_t pixel, uint32_t si, float &dx, float &dy)
+{
+	dx = 0.5f; dy = 0.5f;
+	if(P.spp > 1)
+	{
+		const uint32_t sample = si / static_cast<uint32_t>(P.path_samples);
+		dx = xm(xa(0.5f, static_cast<float>(sample)), P.d1);
+		dy = gbrt::ri_lp(sample + pixel_offset(pixel, P.film_resx));
+	}
+}
+
+// ImageFilm::addSample (imagefilm.cc:771-822): the filter footprint of a
+// sample (the reference's asymmetric rounding included), table indices from
+// |(i - (dx - 0.5)) x table scale| in double, and colour x weight into every
+// covered pixel; weight_only adds the filter weights (once per camera sample).
+__device__ void film_splat(const Params &P, float *film, double *film64, uint32_t pixel, uint32_t si, float r, float g, float b,
+                           bool weight_only)
+{
+	float dx, dy;
+	sample_pos(P, pixel, si, dx, dy);
+	const int x = static_cast<int>(pixel % static_cast<uint32_t>(P.film_resx));
+	const int y = static_cast<int>(pixel / static_cast<uint32_t>(P.film_resx));
+	const double fw = P.filter_width;
+	const int dx0 = max(-x, round_bias(static_cast<double>(dx) - fw));
+	const int dx1 = min(P.film_resx - 1 - x, round_bias(static_cast<double>(dx) + fw - 1.0));
+	const int dy0 = max(-y, round_bias(static_cast<double>(dy) - fw));
+	const int dy1 = min(P.film_resy - 1 - y, round_bias(static_cast<double>(dy) + fw - 1.0));
+	const double xo = static_cast<double>(dx) - 0.5, yo = static_cast<double>(dy) - 0.5;
+	const double sc = P.filter_scale;
+	for(int j = dy0; j <= dy1; ++j)
+	{
+		const int yi = min(15, static_cast<int>(floor(fabs((static_cast<double>(j) - yo) * sc))));
+		for(int i = dx0; i <= dx1; ++i)
+		{
+			const int xi = min(15, static_cast<int>(floor(fabs((static_cast<double>(i) - xo) * sc))));
+			const float w = __ldg(P.filter_tab + yi * 16 + xi);
+			const uint32_t q = static_cast<uint32_t>((y + j) * P.film_resx + (x + i));
+			if(weight_only) atomicAdd(P.film_w + q, w);
+			else film_add(film, film64, q, r * w, g * w, b * w);
+		}
+	}
+}
+
+// A contribution of camera sample si to the film.
+__device__ __forceinline__ void film_put(const Params &P, float *film, double *film64, uint32_t pixel, uint32_t si, float r, float g, float b)
+{
+	if(P.film_w) film_splat(P, film, film64, pixel, si, r, g, b, false);
+	else film_add(film, film64, pixel, r, g, b);
+}
+
 __global__ void __launch_bounds__(kThreads) k_camera(Camera cam, Params P, Work W)
 {
 	// sample-major order: a wave holds whole sample indices of every pixel,
@@ -1089,6 +1152,7 @@ __global__ void __launch_bounds__(kThreads) k_camera(Camera cam, Params P, Work 
 		W.q_ray[0][2ull * s] = make_float4(cam.from[0], cam.from[1], cam.from[2], 0.f);
 		W.q_ray[0][2ull * s + 1] = make_float4(d[0], d[1], d[2], -1.f);
 		W.q_path[0][s] = s;
+		if(P.film_w && sub == 0) film_splat(P, nullptr, nullptr, pixel, si, 0.f, 0.f, 0.f, true);
 	}
 	if(blockIdx.x == 0 && threadIdx.x == 0)
 	{
@@ -1196,7 +1260,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				{
 					// photonmapping adds it twice (integrator_photon_mapping.cc:686-687, 713-721)
 					const float em = P.pm == 1 ? 2.f : 1.f;
-					film_add(film, film64, pixel, xm(thr[0], e[0]) * em, xm(thr[1], e[1]) * em, xm(thr[2], e[2]) * em);
+					film_put(P, film, film64, pixel, si, xm(thr[0], e[0]) * em, xm(thr[1], e[1]) * em, xm(thr[2], e[2]) * em);
 					if(W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
 				}
 				do_nee_all = (s.m->flags & BF_DIFFUSE) && sub == 0;
@@ -1272,7 +1336,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 					{
 						float e[3];
 						if((mat1 & BF_EMIT) && mat_emit(s, wo, e)) for(int c = 0; c < 3; ++c) lcol[c] += e[c];
-						film_add(film, film64, pixel, lcol[0] * thr[0], lcol[1] * thr[1], lcol[2] * thr[2]);
+						film_put(P, film, film64, pixel, si, lcol[0] * thr[0], lcol[1] * thr[1], lcol[2] * thr[2]);
 					}
 					// next direction: All when close, else specular only (finalGathering :625-628)
 					const uint32_t offs = static_cast<uint32_t>(P.path_samples) * sample_ + offset_ + sub;
@@ -1303,7 +1367,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 					if(j >= 0) { const float4 c4 = __ldg(P.g_radiance.col + j); lcol[0] = c4.x; lcol[1] = c4.y; lcol[2] = c4.z; }
 					float e[3];
 					if((mat1 & BF_EMIT) && mat_emit(s, wo, e)) for(int c = 0; c < 3; ++c) lcol[c] += e[c];
-					film_add(film, film64, pixel, lcol[0] * thr[0], lcol[1] * thr[1], lcol[2] * thr[2]);
+					film_put(P, film, film64, pixel, si, lcol[0] * thr[0], lcol[1] * thr[1], lcol[2] * thr[2]);
 				}
 			}
 			else
@@ -1330,7 +1394,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 					if((k == 1 && (s.m->flags & BF_EMIT)) || (k >= 2 && (mat1 & BF_EMIT) && caustic))
 						if(mat_emit(s, wo, e))
 						{
-							film_add(film, film64, pixel, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
+							film_put(P, film, film64, pixel, si, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
 							if(W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
 						}
 				}
@@ -1503,7 +1567,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 	}
 }
 
-__global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Work W, uint32_t shadow_cap, float *film, double *film64)
+__global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Params P, Work W, uint32_t shadow_cap, float *film, double *film64)
 {
 	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
 	const uint32_t n = min(W.count[2], shadow_cap);
@@ -1521,7 +1585,7 @@ __global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Work W, u
 			if(h.prim < 0)
 			{
 				const float4 c = W.s_col[i];
-				film_add(film, film64, W.s_pix[i], c.x, c.y, c.z);
+				film_put(P, film, film64, W.s_pix[i], W.p_si[W.s_path[i]], c.x, c.y, c.z);
 				if(W.p_sum) path_sum_add(W, W.s_path[i], c.x, c.y, c.z);
 			}
 		});
@@ -1638,6 +1702,17 @@ __global__ void k_mean(const float *sum, const double *sum64, float *out, size_t
 {
 	for(size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
 		out[i] = sum64 ? static_cast<float>(sum64[i] * static_cast<double>(inv)) : sum[i] * inv;
+}
+
+// Rgba::normalized (color.h:538-542): sum / weight, 0 where the weight is 0.
+__global__ void k_normalize(const float *sum, const double *sum64, const float *w, float *out, size_t n)
+{
+	for(size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
+	{
+		const float wt = w[i / 3];
+		const float v = sum64 ? static_cast<float>(sum64[i]) : sum[i];
+		out[i] = wt != 0.f ? v / wt : 0.f;
+	}
 }
 
 // kind: 0 lowDiscrepancySampling(dim, x), 1 riVdC, 2 riLp, 3 riS, 4 fnv32ABuf,
@@ -1929,7 +2004,7 @@ __global__ void __launch_bounds__(kThreads) k_pm_root(SceneDev sc, Params P, Wor
 		if(est[0] != 0.f || est[1] != 0.f || est[2] != 0.f)
 		{
 			const float4 t4 = W.p_thr[path];
-			film_add(film, film64, W.p_pixel[path], est[0] * t4.x, est[1] * t4.y, est[2] * t4.z);
+			film_put(P, film, film64, W.p_pixel[path], W.p_si[path], est[0] * t4.x, est[1] * t4.y, est[2] * t4.z);
 		}
 	}
 }
@@ -2158,6 +2233,8 @@ struct gbrt_scene {
 	size_t spawn_cap = 0;
 	int spawn_levels = 0;
 	cudaEvent_t ev_last = nullptr;      // recorded after each render: the buffers' last use
+	float *filter_dev = nullptr;        // 16 x 16 film filter table of the current render
+	float filter_host[256];
 	std::mutex mu;
 };
 
@@ -2361,7 +2438,7 @@ struct DevBuf {
 		if(p) cudaFree(p);
 		p = nullptr;
 		const cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 16));
-		if(e != cudaSuccess) { p = nullptr; return gbrt_set_error(GBRT_ERR_OOM, "photon map buffers (%zu bytes): %s", bytes, cudaGetErrorString(e)); }
+		if(e != cudaSuccess) { p = nullptr; return gbrt_set_error(GBRT_ERR_OOM, "device buffers (%zu bytes): %s", bytes, cudaGetErrorString(e)); }
 		return GBRT_OK;
 	}
 };
@@ -2671,8 +2748,54 @@ int gbrt_scene_destroy(gbrt_scene *S)
 	void *ptrs[] = {S->prim_ng, S->mats, S->lights, S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off,
 	                S->lds_sfac_nd, S->work, S->spawn, S->spawn_count};
 	for(void *p : ptrs) if(p) cudaFree(p);
+	if(S->filter_dev) cudaFree(S->filter_dev);
 	if(S->ev_last) cudaEventDestroy(S->ev_last);
 	delete S;
+	return GBRT_OK;
+}
+
+// ImageFilm filter table (imagefilm.cc:231-264, math/filter.h): filter
+// width from AA_pixelwidth (x 2.6 Mitchell, x 2 Gauss, clamped to
+// [0.501, 4]), table[y][x] = f((x + 0.5) / 16, (y + 0.5) / 16), table scale
+// 0.9999 x 16 / width.  FAST_MATH exp and FAST_TRIG sin as the reference.
+static int film_filter_table(uint32_t type, float pixel_width, float table[256], float &width, float &scale)
+{
+	using gbrt::fmul; using gbrt::fadd; using gbrt::fsub;
+	width = (pixel_width > 0.f ? pixel_width : 1.5f) * 0.5f;
+	if(type == GBRT_FILTER_MITCHELL) width *= 2.6f;
+	else if(type == GBRT_FILTER_GAUSS) width *= 2.f;
+	else if(type != GBRT_FILTER_BOX && type != GBRT_FILTER_LANCZOS)
+		return gbrt_set_error(GBRT_ERR_INVALID, "film filter type %u unknown", type);
+	width = std::min(std::max(0.501f, width), 0.5f * 8.f);
+	for(int y = 0; y < 16; ++y)
+		for(int x = 0; x < 16; ++x)
+		{
+			const float dx = fmul(fadd(static_cast<float>(x), 0.5f), 1.f / 16.f), dy = fmul(fadd(static_cast<float>(y), 0.5f), 1.f / 16.f);
+			const float r2 = fadd(fmul(dx, dx), fmul(dy, dy));
+			float f = 1.f;
+			if(type == GBRT_FILTER_GAUSS)
+				f = std::max(0.f, fsub(gbrt::fast_exp2(fmul(1.4426950408889634f, fmul(-6.f, r2))), 0.00247875f));
+			else if(type == GBRT_FILTER_MITCHELL)
+			{
+				const float xx = fmul(2.f, std::sqrt(r2));
+				if(xx >= 2.f) f = 0.f;
+				else if(xx >= 1.f) f = fadd(fmul(xx, fsub(fmul(xx, fadd(fmul(xx, -0.38888889f), 2.0f)), 3.33333333f)), 1.77777778f);
+				else f = fadd(fmul(fmul(xx, xx), fsub(fmul(1.16666666f, xx), 2.0f)), 0.88888889f);
+			}
+			else if(type == GBRT_FILTER_LANCZOS)
+			{
+				const float xx = std::sqrt(r2);
+				if(xx == 0.f) f = 1.f;
+				else if(-2.f < xx && xx < 2.f)
+				{
+					const float a = fmul(3.14159265358979323846f, xx), b = fmul(1.57079632679489661923f, xx);
+					f = fmul(gbrt::fast_sin(a), gbrt::fast_sin(b)) / fmul(a, b);
+				}
+				else f = 0.f;
+			}
+			table[y * 16 + x] = f;
+		}
+	scale = fmul(0.9999f, 16.f) / width;
 	return GBRT_OK;
 }
 
@@ -2683,6 +2806,8 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
                          double *film64_dev, gbrt_pt_stats *stats, cudaStream_t s)
 {
 	gbrt_pt_params pp = pp_in;
+	// the scene's buffers and filter table: after its previous render, whatever stream that used
+	if(S->ev_last) GBRT_CK(cudaStreamWaitEvent(s, S->ev_last, 0));
 	if(pm)
 	{
 		// camera sample = one integrate(); with final gathering, fg_samples gather
@@ -2739,6 +2864,17 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	Params P{};
 	P.spp = pp.spp; P.path_samples = pp.path_samples; P.bounces = pp.bounces; P.rr_min = pp.russian_roulette_min_bounces;
 	P.raydepth = raydepth;
+	P.film_resx = camera->resx;
+	P.film_resy = camera->resy;
+	if(pp.filter_type != GBRT_FILTER_PIXEL)
+	{
+		if(!pp.film_weight_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: filter type %u needs film_weight_dev", pp.filter_type);
+		if(int rc = film_filter_table(pp.filter_type, pp.aa_pixel_width, S->filter_host, P.filter_width, P.filter_scale)) return rc;
+		if(!S->filter_dev) GBRT_CK(cudaMalloc(&S->filter_dev, sizeof(S->filter_host)));
+		GBRT_CK(cudaMemcpyAsync(S->filter_dev, S->filter_host, sizeof(S->filter_host), cudaMemcpyHostToDevice, s));
+		P.film_w = pp.film_weight_dev;
+		P.filter_tab = S->filter_dev;
+	}
 	if(pm)
 	{
 		P.pm = pm->pm; P.pm_fg = pm->pm_fg; P.pm_fg_bounces = pm->pm_fg_bounces; P.pm_gather_dist = pm->pm_gather_dist;
@@ -2784,7 +2920,7 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 			if(level_guided)
 				if(int rc = gbrt_guide_eval_queue(guide, Ww.hitpos, n, Ww.count + cur, Ww.lobes, s)) return rc;
 			k_shade<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, camera->resx, static_cast<uint32_t>(shadow_cap), film, film64_dev);
-			k_shadow<<<persistent_grid(k_shadow, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Ww, static_cast<uint32_t>(shadow_cap), film,
+			k_shadow<<<persistent_grid(k_shadow, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, static_cast<uint32_t>(shadow_cap), film,
 			                                                                             film64_dev);
 			cur ^= 1;
 		}
@@ -2897,34 +3033,34 @@ int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 }
 
 // Device film around a render call, per-pixel means copied to the host.
-static int render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
+static int render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params_in, const gbrt_pm_params *pm,
                        float *image_out, gbrt_pt_stats *stats, int kind)
 {
-	const size_t n = 3ull * camera->resx * camera->resy;
-	const bool fp64 = (params->flags & GBRT_PT_FP64_FILM) != 0;
-	void *sum = nullptr, *mean = nullptr;
-	GBRT_CK(cudaMalloc(&sum, n * (fp64 ? 8 : 4)));
-	cudaError_t e = cudaMalloc(&mean, n * 4);
-	if(e != cudaSuccess) { cudaFree(sum); return gbrt_set_error(GBRT_ERR_OOM, "gbrt_pt_render_host: %s", cudaGetErrorString(e)); }
-	int rc = GBRT_OK;
-	if((e = cudaMemset(sum, 0, n * (fp64 ? 8 : 4))) != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
-	if(!rc)
+	const size_t n_pix = static_cast<size_t>(camera->resx) * camera->resy, n = 3 * n_pix;
+	gbrt_pt_params params = *params_in;
+	const bool fp64 = (params.flags & GBRT_PT_FP64_FILM) != 0;
+	const bool filtered = params.filter_type != GBRT_FILTER_PIXEL;
+	DevBuf sum, mean, weight;
+	if(int rc = sum.alloc(n * (fp64 ? 8 : 4))) return rc;
+	if(int rc = mean.alloc(n * 4)) return rc;
+	if(filtered)
 	{
-		float *f32 = fp64 ? nullptr : static_cast<float *>(sum);
-		double *f64 = fp64 ? static_cast<double *>(sum) : nullptr;
-		rc = kind == 1 ? gbrt_pm_render(S, camera, params, pm, f32, f64, stats, nullptr)
-		   : kind == 2 ? gbrt_dl_render(S, camera, params, pm, f32, f64, stats, nullptr)
-		               : gbrt_pt_render(S, camera, params, f32, f64, stats, nullptr);
+		if(int rc = weight.alloc(n_pix * 4)) return rc;
+		GBRT_CK(cudaMemset(weight.p, 0, n_pix * 4));
+		params.film_weight_dev = weight.as<float>();
 	}
-	if(!rc)
-	{
-		k_mean<<<grid_for(n, S->n_sm), kThreads>>>(fp64 ? nullptr : static_cast<float *>(sum), fp64 ? static_cast<double *>(sum) : nullptr,
-		                                           static_cast<float *>(mean), n, 1.f / static_cast<float>(params->spp));
-		if((e = cudaMemcpy(image_out, mean, n * 4, cudaMemcpyDeviceToHost)) != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "copy: %s", cudaGetErrorString(e));
-	}
-	cudaFree(sum);
-	cudaFree(mean);
-	return rc;
+	GBRT_CK(cudaMemset(sum.p, 0, n * (fp64 ? 8 : 4)));
+	float *f32 = fp64 ? nullptr : sum.as<float>();
+	double *f64 = fp64 ? sum.as<double>() : nullptr;
+	const int rc = kind == 1 ? gbrt_pm_render(S, camera, &params, pm, f32, f64, stats, nullptr)
+	             : kind == 2 ? gbrt_dl_render(S, camera, &params, pm, f32, f64, stats, nullptr)
+	                         : gbrt_pt_render(S, camera, &params, f32, f64, stats, nullptr);
+	if(rc) return rc;
+	if(filtered) k_normalize<<<grid_for(n, S->n_sm), kThreads>>>(f32, f64, weight.as<float>(), mean.as<float>(), n);
+	else k_mean<<<grid_for(n, S->n_sm), kThreads>>>(f32, f64, mean.as<float>(), n, 1.f / static_cast<float>(params.spp));
+	GBRT_CK(cudaGetLastError());
+	GBRT_CK(cudaMemcpy(image_out, mean.p, n * 4, cudaMemcpyDeviceToHost));
+	return GBRT_OK;
 }
 
 int gbrt_pt_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, float *image_out, gbrt_pt_stats *stats)

@@ -60,7 +60,12 @@ class PtParams(ctypes.Structure):
                 ("russian_roulette_min_bounces", ctypes.c_int32), ("base_sampling_offset", ctypes.c_uint32),
                 ("seed", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("wave_paths", ctypes.c_uint32),
                 ("guide", ctypes.c_void_p), ("guide_alpha", ctypes.c_float), ("guide_train_steps", ctypes.c_uint32),
-                ("guide_batch", ctypes.c_uint32), ("guide_max_vertex", ctypes.c_uint32), ("raydepth", ctypes.c_int32)]
+                ("guide_batch", ctypes.c_uint32), ("guide_max_vertex", ctypes.c_uint32), ("raydepth", ctypes.c_int32),
+                ("filter_type", ctypes.c_uint32), ("aa_pixel_width", ctypes.c_float), ("film_weight_dev", ctypes.c_void_p)]
+
+
+# ImageFilm "filter_type" names -> gbrt_pt_params.filter_type ("pixel": single-pixel splat, plain sums)
+FILTERS = {"pixel": 0, "box": 1, "gauss": 2, "mitchell": 3, "lanczos": 4}
 
 
 class PmParams(ctypes.Structure):
@@ -395,12 +400,18 @@ class Renderer:
         return d
 
     def params(self, spp, base_offset=0, seed=1, fp64=False, wave_paths=0, guide=None, alpha=0.0, train_steps=0,
-               batch=0, max_vertex=0):
+               batch=0, max_vertex=0, weight_ptr=0):
+        """gbrt_pt_params; the film filter comes from the scene's optional
+        "film" entry ({"filter_type": ..., "AA_pixelwidth": ...}; default the
+        single-pixel splat)."""
         it = self.scene["integrator"]
+        film = self.scene.get("film", {})
         return PtParams(int(spp), int(it.get("path_samples", 1)), int(it.get("bounces", 5)),
                         int(it.get("russian_roulette_min_bounces", 0)), int(base_offset), int(seed),
                         PT_FP64_FILM if fp64 else 0, int(wave_paths), guide.handle if guide is not None else None,
-                        float(alpha), int(train_steps), int(batch), int(max_vertex), int(it.get("raydepth", 5)))
+                        float(alpha), int(train_steps), int(batch), int(max_vertex), int(it.get("raydepth", 5)),
+                        FILTERS[film.get("filter_type", "pixel")], float(film.get("AA_pixelwidth", 0.0)),
+                        int(weight_ptr) or None)
 
     def render(self, spp, base_offset=0, seed=1, fp64=False, guide=None, alpha=0.0, train_steps=0, batch=0,
                max_vertex=0):
@@ -419,11 +430,12 @@ class Renderer:
                      "shadow_rays": st.shadow_rays, "ms": st.ms}
 
     def render_device(self, spp, film_ptr, film64_ptr=0, base_offset=0, seed=1, stream=0, stats=False, wave_paths=0,
-                      guide=None, alpha=0.0, train_steps=0, batch=0, max_vertex=0, radiance_target=False):
-        """Adds sample sums into a device film (float or double RGB)."""
+                      guide=None, alpha=0.0, train_steps=0, batch=0, max_vertex=0, radiance_target=False, weight_ptr=0):
+        """Adds sample sums into a device film (float or double RGB); with a
+        filtered film (scene "film" entry) the filter weights go to weight_ptr."""
         cam = self.camera_desc()
         p = self.params(spp, base_offset, seed, bool(film64_ptr), wave_paths, guide, alpha, train_steps, batch,
-                        max_vertex)
+                        max_vertex, weight_ptr)
         if radiance_target:
             p.flags |= PT_GUIDE_RADIANCE
         st = PtStats()

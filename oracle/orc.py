@@ -170,6 +170,9 @@ def reference_scene_text(scene, spp, batches, threads=-1):
     integ = dict(scene["integrator"])
     t = integ.pop("type")
     out.append(f"integrator {t} " + " ".join(f"{k}={str(v).lower() if isinstance(v, bool) else v}" for k, v in integ.items()))
+    film = scene.get("film")
+    if film:
+        out.append(f"film {film['filter_type']} {float(film.get('AA_pixelwidth', 1.5))!r}")
     out.append(f"render {spp} {batches} {threads}")
     return "\n".join(out) + "\n"
 

@@ -2,8 +2,10 @@
 // its public C API (yafaray_c_api.h) and dumps the "combined" layer of K
 // independent batches (distinct adv_base_sampling_offset values,
 // imagefilm.h:194) so per-pixel means and standard errors can be formed.
-// Box filter of width 1 (imagefilm.cc:252) makes each sample land in its own
-// pixel, so a batch's pixel value is the plain mean of its spp samples.
+// The film defaults to a box filter of width 1 (imagefilm.cc:252), which
+// lands each sample in its own pixel (apart from samples within 0.001 of a
+// pixel edge), so a batch's pixel value is the mean of its spp samples; a
+// "film <filter_type> <AA_pixelwidth>" line selects another filter.
 // Only tests/golden/make_render_golden.py runs it.
 //
 // Input: a text scene, one statement per line (# comments):
@@ -82,6 +84,8 @@ int main(int argc, char **argv)
 	yafaray_SurfaceIntegrator *integrator = nullptr;
 	yafaray_ParamMap *camera = yafaray_createParamMap();
 	int resx = 0, resy = 0, spp = 1, batches = 1, threads = -1;
+	std::string filter_type = "box";
+	float pixel_width = 1.f;
 	std::string line;
 	while(std::getline(in, line))
 	{
@@ -198,6 +202,7 @@ int main(int argc, char **argv)
 			integrator = yafaray_createSurfaceIntegrator(logger, "integrator", pm);
 		}
 		else if(kw == "render") ss >> spp >> batches >> threads;
+		else if(kw == "film") ss >> filter_type >> pixel_width;
 	}
 	if(!integrator || resx <= 0 || resy <= 0) { fprintf(stderr, "scene lacks integrator or camera\n"); return 2; }
 	yafaray_clearParamMap(pm);
@@ -214,8 +219,8 @@ int main(int argc, char **argv)
 		yafaray_setParamMapInt(pm, "threads", threads);
 		yafaray_setParamMapInt(pm, "AA_passes", 1);
 		yafaray_setParamMapInt(pm, "AA_minsamples", spp);
-		yafaray_setParamMapString(pm, "filter_type", "box");
-		yafaray_setParamMapFloat(pm, "AA_pixelwidth", 1.0);
+		yafaray_setParamMapString(pm, "filter_type", filter_type.c_str());
+		yafaray_setParamMapFloat(pm, "AA_pixelwidth", pixel_width);
 		yafaray_setParamMapInt(pm, "adv_base_sampling_offset", k * spp);
 		yafaray_Film *film = yafaray_createFilm(logger, integrator, "film", pm);
 		yafaray_defineCamera(film, camera);

@@ -100,6 +100,21 @@ def hashgrid_golden():
     print(f"hashgrid.npz: {len(pos)} points, {len(cases)} cases")
 
 
+def film_golden(spp=16, batches=32):
+    """Cornell at 48x36 through the reference's default film filter (gauss,
+    AA_pixelwidth 1.5): each sample splats over neighbouring pixels."""
+    sc = scenes.cornell_scene(res=48)
+    sc["camera"]["resy"] = 36
+    sc["film"] = {"filter_type": "gauss", "AA_pixelwidth": 1.5}
+    rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
+    mean = rgb.mean(0)
+    se = rgb.std(0, ddof=1) / np.sqrt(batches)
+    name = "cornell_gauss_48x36_render.npz"
+    np.savez_compressed(os.path.join(OUT, name), mean=mean.astype(np.float32), se=se.astype(np.float32),
+                        batches=np.int32(batches), spp=np.int32(spp), seconds=secs)
+    print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
+
+
 def variant_golden(name, res=64, spp=16, batches=32, **kw):
     """Cornell variants: glass (glass + rough-glass spheres, the recursive
     split) and point (a pointlight instead of the area light)."""
@@ -216,5 +231,7 @@ if __name__ == "__main__":
         batch_golden()
     if "cornell_pm" in what:
         cornell_pm_golden()
+    if "film" in what:
+        film_golden()
     if "cornell_point" in what:
         variant_golden("cornell_point_64_render.npz", point_light=True)
