@@ -860,7 +860,10 @@ __global__ void __launch_bounds__(128) k_wide_level(int level, const uint2 *__re
 			eb[a] = e + 127;
 			scale[a] = ldexp(1.0, e);
 		}
-		// slots by octant: child nearest along octant s's diagonal goes to slot s
+		// slots by octant: child nearest along octant s's diagonal goes to slot
+		// s; up to 4 children use slots 0-3 only (ordered by the x / y signs),
+		// so the traversal can skip the empty upper half of the node
+		const int n_slots = n <= 4 ? 4 : 8;
 		float cost[8][8];
 		for(int k = 0; k < n; ++k)
 		{
@@ -880,7 +883,7 @@ __global__ void __launch_bounds__(128) k_wide_level(int level, const uint2 *__re
 			for(int k = 0; k < n; ++k)
 			{
 				if((placed >> k) & 1u) continue;
-				for(int sl = 0; sl < 8; ++sl)
+				for(int sl = 0; sl < n_slots; ++sl)
 					if(in_slot[sl] < 0 && (bk < 0 || cost[k][sl] < bc)) { bc = cost[k][sl]; bk = k; bs = sl; }
 			}
 			in_slot[bs] = bk;

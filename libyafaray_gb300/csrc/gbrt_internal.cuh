@@ -49,7 +49,8 @@ __host__ __device__ inline uint32_t gbrt_leaf_ref(uint32_t first, uint32_t count
 //       child_base + popc(imask below slot); leaf child (unary count << 5) |
 //       offset, primitives prim_base + offset .. + count - 1 (count 1..3).
 //       Children sit in slots by octant: the child nearest for rays whose
-//       direction signs are octant o is in slot o.
+//       direction signs are octant o is in slot o; nodes of up to 4
+//       children use slots 0-3 only (x / y signs), leaving slots 4-7 empty.
 //   wtris, wids: primitive records and IDs in wide-leaf order.
 struct gbrt_bvh {
 	int device = 0;

@@ -167,10 +167,13 @@ __device__ __forceinline__ void wide_node_test(const uint4 w0, const uint4 w1, c
 	GBRT_WIDE_CHILD(1, nx0, ny0, nz0, fx0, fy0, fz0, 1)
 	GBRT_WIDE_CHILD(2, nx0, ny0, nz0, fx0, fy0, fz0, 2)
 	GBRT_WIDE_CHILD(3, nx0, ny0, nz0, fx0, fy0, fz0, 3)
-	GBRT_WIDE_CHILD(0, nx1, ny1, nz1, fx1, fy1, fz1, 4)
-	GBRT_WIDE_CHILD(1, nx1, ny1, nz1, fx1, fy1, fz1, 5)
-	GBRT_WIDE_CHILD(2, nx1, ny1, nz1, fx1, fy1, fz1, 6)
-	GBRT_WIDE_CHILD(3, nx1, ny1, nz1, fx1, fy1, fz1, 7)
+	if(w1.w)   // nodes of up to 4 children leave slots 4-7 empty
+	{
+		GBRT_WIDE_CHILD(0, nx1, ny1, nz1, fx1, fy1, fz1, 4)
+		GBRT_WIDE_CHILD(1, nx1, ny1, nz1, fx1, fy1, fz1, 5)
+		GBRT_WIDE_CHILD(2, nx1, ny1, nz1, fx1, fy1, fz1, 6)
+		GBRT_WIDE_CHILD(3, nx1, ny1, nz1, fx1, fy1, fz1, 7)
+	}
 #undef GBRT_WIDE_CHILD
 	// Empty slots hold inverted boxes (missed except on a degenerate axis)
 	// and meta 0, so a stray hit on one adds no bits below.
