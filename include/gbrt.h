@@ -192,7 +192,9 @@ int gbrt_trace_shadow_host(const gbrt_bvh *bvh, const gbrt_ray *rays, uint32_t n
  * (imagefilm.cc:771-822). */
 
 enum {
-	GBRT_MAT_SHINYDIFFUSE = 0,   /* "shinydiffusemat": color, params[0] = diffuse_reflect (0 -> 1) */
+	GBRT_MAT_SHINYDIFFUSE = 0,   /* "shinydiffusemat": color, color2 (mirror_color; all 0 -> 1), power (emit),
+	                                params = {diffuse_reflect (0 -> 1), specular_reflect, transparency,
+	                                translucency, transmit_filter, -, fresnel_effect (0/1), IOR (0 -> 1.33)} */
 	GBRT_MAT_LIGHT = 1,          /* "light_mat": color, power, params[0] = double_sided (0/1) */
 	GBRT_MAT_GLOSSY = 2,         /* "glossy": color (glossy colour), color2 (diffuse_color), params =
 	                                {exponent, glossy_reflect, diffuse_reflect, as_diffuse (1)} */
@@ -213,7 +215,7 @@ typedef struct gbrt_material_desc {
 	float color[3];
 	float color2[3];
 	float power;
-	float params[6];
+	float params[8];
 } gbrt_material_desc;
 
 /* "arealight": corner, point1, point2, color, power, samples

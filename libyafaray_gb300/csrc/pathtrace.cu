@@ -51,14 +51,21 @@ enum : uint32_t {
 struct DevMaterial {
 	uint32_t type;
 	uint32_t flags;
-	float col[3];      // shinydiffuse: colour x diffuse strength; light_mat: colour x power; glossy: glossy colour;
+	float col[3];      // shinydiffuse: diffuse colour; light_mat: colour x power; glossy: glossy colour;
 	                   // glass, rough_glass: filter colour
-	float col2[3];     // glossy: diffuse colour; glass, rough_glass: mirror colour
+	float col2[3];     // shinydiffuse, glass, rough_glass: mirror colour; glossy: diffuse colour
 	float exponent, m_glossy, m_diffuse, p_diffuse;
 	uint32_t as_diffuse, with_diffuse, double_sided, addl_depth;
-	float ior, a2;     // glass, rough_glass: IOR; rough_glass: GGX alpha^2
-	float pad[2];
+	float ior, a2;     // glass, rough_glass: IOR; shinydiffuse: IOR^2; rough_glass: GGX alpha^2
+	uint32_t sd;       // shinydiffuse components present (SD_*)
+	float pad;
+	float sdc[4];      // shinydiffuse component strengths: mirror, transparency, translucency, diffuse
+	float tcol[3];     // shinydiffuse: transmit_filter x colour + (1 - transmit_filter)
+	float ecol[3];     // shinydiffuse: emit x colour
 };
+
+// ShinyDiffuseMaterial components (material_shiny_diffuse.cc:146-189)
+enum : uint32_t { SD_MIRROR = 1u, SD_TRANSPARENT = 2u, SD_TRANSLUCENT = 4u, SD_DIFFUSE = 8u, SD_FRESNEL = 16u };
 
 struct DevLight {
 	float c[3], tx[3], ty[3], nflip[3], col[3];   // area light (light_area.h:70-78); point light: c = from, col
@@ -647,17 +654,210 @@ __device__ __forceinline__ int rough_sample2(const Surface &s, const float wo[3]
 }
 
 
+// ---- ShinyDiffuseMaterial layers (material_shiny_diffuse.cc:205-619) -------
+// getFresnelKr (:205-217): Fresnel reflectance with the fresnel_effect, else 1.
+__device__ __forceinline__ float shiny_kr(const DevMaterial &m, const float wo[3], const float n[3])
+{
+	if(!(m.sd & SD_FRESNEL)) return 1.f;
+	float N[3] = {n[0], n[1], n[2]};
+	if(dot3(wo, n) < 0.f) { N[0] = -n[0]; N[1] = -n[1]; N[2] = -n[2]; }
+	const float c = dot3(wo, N);
+	float g = m.ior + c * c - 1.f;
+	if(g < 0.f) g = 0.f;
+	else g = sqrtf(g);
+	const float aux = c * (g + c);
+	return ((0.5f * (g - c) * (g - c)) / ((g + c) * (g + c))) * (1.f + ((aux - 1.f) * (aux - 1.f)) / ((aux + 1.f) * (aux + 1.f)));
+}
+
+// accumulate (:222-233): absolute component weights from the layer fractions.
+__device__ __forceinline__ void shiny_accum(const DevMaterial &m, float kr, float a[4])
+{
+	a[0] = m.sdc[0] * kr;
+	float acc = 1.f - a[0];
+	a[1] = m.sdc[1] * acc;
+	acc *= 1.f - m.sdc[1];
+	a[2] = m.sdc[2] * acc;
+	acc *= 1.f - m.sdc[2];
+	a[3] = m.sdc[3] * acc;
+}
+
+// Component order and flags (config, :146-189): mirror Specular|Reflect,
+// transparency Transmit|Filter, translucency Diffuse|Transmit, diffuse
+// Diffuse|Reflect.
+__device__ __forceinline__ uint32_t shiny_cflags(int i)
+{
+	return i == 0 ? (BF_SPECULAR | BF_REFLECT) : i == 1 ? (BF_TRANSMIT | BF_FILTER) : i == 2 ? (BF_DIFFUSE | BF_TRANSMIT) : (BF_DIFFUSE | BF_REFLECT);
+}
+
+// eval (:297-337) with bsdfs = All
+__device__ __forceinline__ void shiny_eval(const Surface &s, const float wo[3], const float wl[3], float out[3])
+{
+	const DevMaterial &m = *s.m;
+	out[0] = out[1] = out[2] = 0.f;
+	const float cos_ng_wo = dot3(s.ng, wo), cos_ng_wl = dot3(s.ng, wl);
+	float n[3];
+	face_forward(s, wo, n);
+	if(!(m.flags & BF_DIFFUSE)) return;
+	const float kr = shiny_kr(m, wo, n);
+	const float m_t = (1.f - kr * m.sdc[0]) * (1.f - m.sdc[1]);
+	if(xm(cos_ng_wo, cos_ng_wl) < 0.f && (m.sd & SD_TRANSLUCENT))
+	{
+		const float f = m.sdc[2] * m_t;
+		for(int k = 0; k < 3; ++k) out[k] = f * m.col[k];
+		return;
+	}
+	if(dot3(n, wl) < 0.f) return;
+	const float m_d = m_t * (1.f - m.sdc[2]) * m.sdc[3];
+	for(int k = 0; k < 3; ++k) out[k] = m_d * m.col[k];
+}
+
+// pdf (:443-484): the components whose flags share a bit with bsdfs add
+// their weights to the normalisation (mirror and transparency included).
+__device__ __forceinline__ float shiny_pdf(const Surface &s, const float wo[3], const float wi[3], uint32_t bsdfs)
+{
+	const DevMaterial &m = *s.m;
+	if(!(bsdfs & BF_DIFFUSE)) return 0.f;
+	const float cos_ng_wo = dot3(s.ng, wo);
+	float n[3];
+	face_forward(s, wo, n);
+	float a[4];
+	shiny_accum(m, shiny_kr(m, wo, n), a);
+	float sum = 0.f, pdf = 0.f;
+	int n_match = 0;
+	for(int i = 0; i < 4; ++i)
+	{
+		if(!((m.sd >> i) & 1u) || !(bsdfs & shiny_cflags(i))) continue;
+		const float width = a[i];
+		sum += width;
+		if(i == 2) { if(xm(cos_ng_wo, dot3(s.ng, wi)) < 0.f) pdf += fabsf(dot3(wi, n)) * width; }
+		else if(i == 3) pdf += fabsf(dot3(wi, n)) * width;
+		++n_match;
+	}
+	if(!n_match || sum < 0.00001f) return 0.f;
+	return pdf / sum;
+}
+
+// reflectDir (vector.h:391-396)
+__device__ __forceinline__ void reflect_dir(const float n[3], const float v[3], float out[3])
+{
+	const float vn = dot3(v, n);
+	if(vn < 0.f) { out[0] = -v[0]; out[1] = -v[1]; out[2] = -v[2]; return; }
+	for(int c = 0; c < 3; ++c) out[c] = 2.f * vn * n[c] - v[c];
+}
+
+// sample (:346-440): pick a component among those whose flags are all in
+// the request, by s1, then sample it; w = |wi . N| / (0.99 pdf + 0.01).
+__device__ __forceinline__ bool shiny_sample(const Surface &s, const float wo[3], float s1, float s2, uint32_t req, float wi[3], float col[3],
+                                             float &w, float &pdf, uint32_t &sampled)
+{
+	const DevMaterial &m = *s.m;
+	const float cos_ng_wo = dot3(s.ng, wo);
+	float n[3];
+	face_forward(s, wo, n);
+	const float kr = shiny_kr(m, wo, n);
+	float a[4];
+	shiny_accum(m, kr, a);
+	float sum = 0.f, val[4], width[4];
+	int choice[4], n_match = 0, pick = -1;
+	for(int i = 0; i < 4; ++i)
+	{
+		const uint32_t cf = shiny_cflags(i);
+		if(!((m.sd >> i) & 1u) || (req & cf) != cf) continue;
+		width[n_match] = a[i];
+		sum += width[n_match];
+		choice[n_match] = i;
+		val[n_match] = sum;
+		++n_match;
+	}
+	if(!n_match || sum < 0.00001f) { sampled = 0u; pdf = 0.f; return false; }
+	const float inv_sum = 1.f / sum;
+	for(int i = 0; i < n_match; ++i)
+	{
+		val[i] *= inv_sum;
+		width[i] *= inv_sum;
+		if(s1 <= val[i] && pick < 0) pick = i;
+	}
+	if(pick < 0) pick = n_match - 1;
+	const float s_1 = pick > 0 ? (s1 - val[pick - 1]) / width[pick] : s1 / width[pick];
+	const int c = choice[pick];
+	col[0] = col[1] = col[2] = 0.f;
+	if(c == 0)
+	{
+		reflect_dir(n, wo, wi);
+		pdf = width[pick];
+		const float f = 1.f / fmaxf(fabsf(dot3(s.n, wi)), 1.0e-6f);
+		for(int k = 0; k < 3; ++k) col[k] = (m.col2[k] * a[0]) * f;
+	}
+	else if(c == 1)
+	{
+		wi[0] = -wo[0]; wi[1] = -wo[1]; wi[2] = -wo[2];
+		for(int k = 0; k < 3; ++k) col[k] = a[1] * m.tcol[k];
+		pdf = fabsf(dot3(wi, n)) < 1e-6f ? 0.f : width[pick];
+	}
+	else if(c == 2)
+	{
+		const float nn[3] = {-n[0], -n[1], -n[2]};
+		cos_hemisphere(nn, s.u, s.v, s_1, s2, wi);
+		if(xm(cos_ng_wo, dot3(s.ng, wi)) < 0.f) for(int k = 0; k < 3; ++k) col[k] = a[2] * m.col[k];
+		pdf = fabsf(dot3(wi, n)) * width[pick];
+	}
+	else
+	{
+		cos_hemisphere(n, s.u, s.v, s_1, s2, wi);
+		if(xm(cos_ng_wo, dot3(s.ng, wi)) > 0.f) for(int k = 0; k < 3; ++k) col[k] = a[3] * m.col[k];
+		pdf = fabsf(dot3(wi, n)) * width[pick];
+	}
+	sampled = shiny_cflags(c);
+	w = __fdiv_rn(fabsf(dot3(wi, s.n)), xa(xm(pdf, 0.99f), 0.01f));
+	if(m.sd & SD_TRANSPARENT)
+	{
+		// getAlpha (:568-587): alpha = 1 - (1 - mirror kr) transparency, and
+		// sample() returns w alpha + (1 - alpha) for every component
+		const float alpha = 1.f - (1.f - m.sdc[0] * kr) * m.sdc[1];
+		w = xa(xm(w, alpha), 1.f - alpha);
+	}
+	return true;
+}
+
+// getSpecular (:490-533): transparency straight through, mirror reflection
+// lifted off the surface when it grazes (cos with Ng < 0.01).
+__device__ __forceinline__ void shiny_specular(const Surface &s, const float wo[3], bool &has_refract, float rdir[3], float rcol[3],
+                                               bool &has_reflect, float ldir[3], float lcol[3])
+{
+	const DevMaterial &m = *s.m;
+	const bool backface = dot3(wo, s.ng) < 0.f;
+	float n[3], ng[3];
+	for(int k = 0; k < 3; ++k) { n[k] = backface ? -s.n[k] : s.n[k]; ng[k] = backface ? -s.ng[k] : s.ng[k]; }
+	const float kr = shiny_kr(m, wo, n);
+	has_refract = (m.sd & SD_TRANSPARENT) != 0u;
+	has_reflect = (m.sd & SD_MIRROR) != 0u;
+	if(has_refract)
+	{
+		const float f = (1.f - m.sdc[0] * kr) * m.sdc[1];
+		for(int k = 0; k < 3; ++k) { rdir[k] = -wo[k]; rcol[k] = f * m.tcol[k]; }
+	}
+	if(has_reflect)
+	{
+		vec_reflect(wo, n, ldir);
+		const float cos_wi_ng = dot3(ldir, ng);
+		if(cos_wi_ng < 0.01f)
+		{
+			const float lift = 0.01f - cos_wi_ng;
+			for(int k = 0; k < 3; ++k) ldir[k] += lift * ng[k];
+			normalize3(ldir);
+		}
+		const float f = m.sdc[0] * kr;
+		for(int k = 0; k < 3; ++k) lcol[k] = m.col2[k] * f;
+	}
+}
+
 // Material::eval dispatch; ShinyDiffuseMaterial::eval diffuse component
 // (material_shiny_diffuse.cc:297-337).
 __device__ __forceinline__ void mat_eval(const Surface &s, const float wo[3], const float wl[3], float out[3])
 {
 	out[0] = out[1] = out[2] = 0.f;
 	if(s.m->type == GBRT_MAT_GLOSSY) { glossy_eval(s, wo, wl, BF_ALL, out); return; }
-	if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return;
-	float n[3];
-	face_forward(s, wo, n);
-	if(dot3(n, wl) < 0.f) return;
-	for(int k = 0; k < 3; ++k) out[k] = s.m->col[k];
+	if(s.m->type == GBRT_MAT_SHINYDIFFUSE) shiny_eval(s, wo, wl, out);
 }
 
 // Material::pdf dispatch; ShinyDiffuseMaterial::pdf lambertian part
@@ -667,9 +867,7 @@ __device__ __forceinline__ float mat_pdf(const Surface &s, const float wo[3], co
 {
 	if(s.m->type == GBRT_MAT_GLOSSY) return glossy_pdf(s, wo, wi, BF_GLOSSY | BF_DIFFUSE | BF_DISPERSIVE | BF_REFLECT | BF_TRANSMIT);
 	if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return 0.f;
-	float n[3];
-	face_forward(s, wo, n);
-	return fabsf(dot3(wi, n));
+	return shiny_pdf(s, wo, wi, BF_GLOSSY | BF_DIFFUSE | BF_DISPERSIVE | BF_REFLECT | BF_TRANSMIT);
 }
 
 // Material::sample dispatch; ShinyDiffuseMaterial::sample diffuse reflection
@@ -688,18 +886,7 @@ __device__ __forceinline__ bool mat_sample(const Surface &s, const float wo[3], 
 	if(s.m->type == GBRT_MAT_GLASS) return glass_sample(s, wo, s1, req_flags, wi, col, w, pdf, sampled);
 	if(s.m->type == GBRT_MAT_ROUGH_GLASS) return rough_sample(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
 	if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return false;
-	const uint32_t cflags = BF_DIFFUSE | BF_REFLECT;
-	if((req_flags & cflags) != cflags) return false;
-	float n[3];
-	face_forward(s, wo, n);
-	cos_hemisphere(n, s.u, s.v, s1, s2, wi);
-	const float cos_ng_wo = dot3(s.ng, wo);
-	if(xm(cos_ng_wo, dot3(s.ng, wi)) > 0.f)
-		for(int k = 0; k < 3; ++k) col[k] = s.m->col[k];
-	pdf = fabsf(dot3(wi, n));
-	w = __fdiv_rn(fabsf(dot3(wi, s.n)), xa(xm(pdf, 0.99f), 0.01f));
-	sampled = cflags;
-	return true;
+	return shiny_sample(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
 }
 
 // Sample colour x weight that Material::sample would return for a given
@@ -714,10 +901,11 @@ __device__ __forceinline__ void bsdf_eval_at(const Surface &s, const float wo[3]
 	const float cos_ng_wo = dot3(s.ng, wo), cos_ng_wi = dot3(s.ng, wi);
 	if(s.m->type == GBRT_MAT_SHINYDIFFUSE)
 	{
+		// guided only when the diffuse layer is the sole component (shiny_guidable)
 		if(!(xm(cos_ng_wo, cos_ng_wi) > 0.f)) return;
 		const float pdf = fabsf(dot3(wi, n));
 		const float w = __fdiv_rn(fabsf(dot3(wi, s.n)), xa(xm(pdf, 0.99f), 0.01f));
-		for(int k = 0; k < 3; ++k) fw[k] = xm(s.m->col[k], w);
+		for(int k = 0; k < 3; ++k) fw[k] = xm(s.m->sdc[3] * s.m->col[k], w);
 		return;
 	}
 	if(s.m->type != GBRT_MAT_GLOSSY || xm(cos_ng_wo, cos_ng_wi) < 0.f) return;
@@ -768,9 +956,16 @@ __device__ __forceinline__ float bsdf_true_pdf(const Surface &s, const float wo[
 	return pd * c * kInvPi + (1.f - pd) * pg;
 }
 
-// LightMaterial::emit (material_light.cc:82-87)
+// LightMaterial::emit (material_light.cc:82-87); ShinyDiffuseMaterial::emit
+// (material_shiny_diffuse.cc:342-347): emit x colour, both sides.
 __device__ __forceinline__ bool mat_emit(const Surface &s, const float wo[3], float out[3])
 {
+	if(s.m->type == GBRT_MAT_SHINYDIFFUSE)
+	{
+		if(!(s.m->flags & BF_EMIT)) return false;
+		for(int k = 0; k < 3; ++k) out[k] = s.m->ecol[k];
+		return true;
+	}
 	if(s.m->type != GBRT_MAT_LIGHT) return false;
 	if(dot3(wo, s.n) <= 0.f && !s.m->double_sided) return false;
 	for(int k = 0; k < 3; ++k) out[k] = s.m->col[k];
@@ -1035,11 +1230,12 @@ __device__ void spawn_children(const SceneDev &sc, const Params &P, const Surfac
 			}
 		}
 	}
-	if(do_spec && s.m->type == GBRT_MAT_GLASS)
+	if(do_spec && (s.m->type == GBRT_MAT_GLASS || s.m->type == GBRT_MAT_SHINYDIFFUSE))
 	{
 		bool hr, hl;
 		float rdir[3], rcol[3], ldir[3], lcol[3], wt[3];
-		glass_specular(s, wo, static_cast<int>(nl), hr, rdir, rcol, hl, ldir, lcol);
+		if(s.m->type == GBRT_MAT_GLASS) glass_specular(s, wo, static_cast<int>(nl), hr, rdir, rcol, hl, ldir, lcol);
+		else shiny_specular(s, wo, hr, rdir, rcol, hl, ldir, lcol);
 		if(hl) { for(int k = 0; k < 3; ++k) wt[k] = thr[k] * lcol[k]; emit(ldir, wt, division, branch, deco1, deco2); }
 		if(hr) { for(int k = 0; k < 3; ++k) wt[k] = thr[k] * rcol[k]; emit(rdir, wt, division, branch, deco1, deco2); }
 	}
@@ -1477,7 +1673,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				float wi[3], scol[3], w, pdf;
 				uint32_t sflags;
 				float mult[3], mpdf = 0.f, hf = 0.f;
-				const bool guidable = s.m->type == GBRT_MAT_SHINYDIFFUSE || s.m->type == GBRT_MAT_GLOSSY;
+				const bool guidable = (s.m->type == GBRT_MAT_SHINYDIFFUSE && s.m->sd == SD_DIFFUSE) || s.m->type == GBRT_MAT_GLOSSY;
 				if(P.guiding && guidable)
 				{
 					// one-sample MIS of the guide mixture q and the BSDF sampler
@@ -2604,9 +2800,54 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 		d.type = m.type;
 		if(m.type == GBRT_MAT_SHINYDIFFUSE)
 		{
-			const float strength = m.params[0] > 0.f ? m.params[0] : 1.f;   // diffuse_reflect
-			d.flags = strength * 1.f > 0.00001f ? (BF_DIFFUSE | BF_REFLECT) : 0u;
-			for(int k = 0; k < 3; ++k) d.col[k] = m.color[k] * strength;
+			// ShinyDiffuseMaterial ctor + config (material_shiny_diffuse.cc:133-189);
+			// ParamMap defaults: diffuse_reflect 1, mirror_color 1, IOR 1.33
+			const float diffuse_reflect = m.params[0] > 0.f ? m.params[0] : 1.f;
+			const float specular_reflect = m.params[1], transparency = m.params[2], translucency = m.params[3];
+			const float transmit_filter = m.params[4];
+			const bool fresnel = m.params[6] > 0.5f;
+			const float ior = m.params[7] > 0.f ? m.params[7] : 1.33f;
+			const bool mirror_set = m.color2[0] != 0.f || m.color2[1] != 0.f || m.color2[2] != 0.f;
+			float acc = 1.f;
+			d.flags = 0u;
+			d.sd = fresnel ? SD_FRESNEL : 0u;
+			if(specular_reflect > 0.00001f)
+			{
+				d.sd |= SD_MIRROR;
+				if(!fresnel) acc = 1.f - specular_reflect;
+				d.flags |= BF_SPECULAR | BF_REFLECT;
+			}
+			if(transparency * acc > 0.00001f)
+			{
+				d.sd |= SD_TRANSPARENT;
+				acc *= 1.f - transparency;
+				d.flags |= BF_TRANSMIT | BF_FILTER;
+			}
+			if(translucency * acc > 0.00001f)
+			{
+				d.sd |= SD_TRANSLUCENT;
+				acc *= 1.f - transparency;      // (sic) the reference's config
+				d.flags |= BF_DIFFUSE | BF_TRANSMIT;
+			}
+			if(diffuse_reflect * acc > 0.00001f)
+			{
+				d.sd |= SD_DIFFUSE;
+				d.flags |= BF_DIFFUSE | BF_REFLECT;
+			}
+			d.sdc[0] = (d.sd & SD_MIRROR) ? specular_reflect : 0.f;
+			d.sdc[1] = (d.sd & SD_TRANSPARENT) ? transparency : 0.f;
+			d.sdc[2] = (d.sd & SD_TRANSLUCENT) ? translucency : 0.f;
+			d.sdc[3] = (d.sd & SD_DIFFUSE) ? diffuse_reflect : 0.f;
+			d.ior = ior * ior;
+			const float emit = m.power;
+			if(emit > 0.f) d.flags |= BF_EMIT;
+			for(int k = 0; k < 3; ++k)
+			{
+				d.col[k] = m.color[k];
+				d.col2[k] = mirror_set ? m.color2[k] : 1.f;
+				d.tcol[k] = transmit_filter * m.color[k] + (1.f - transmit_filter);
+				d.ecol[k] = emit * m.color[k];
+			}
 		}
 		else if(m.type == GBRT_MAT_LIGHT)
 		{

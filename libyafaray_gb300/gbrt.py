@@ -41,7 +41,7 @@ class BvhInfo(ctypes.Structure):
 
 class MaterialDesc(ctypes.Structure):
     _fields_ = [("type", ctypes.c_uint32), ("color", ctypes.c_float * 3), ("color2", ctypes.c_float * 3),
-                ("power", ctypes.c_float), ("params", ctypes.c_float * 6)]
+                ("power", ctypes.c_float), ("params", ctypes.c_float * 8)]
 
 
 class LightDesc(ctypes.Structure):
@@ -292,7 +292,16 @@ def _material_desc(m):
     kind = m[0]
     d.type = MAT_TYPES[kind]
     if kind == "shinydiffusemat":
+        # ("shinydiffusemat", color[, {reference parameter name: value}])
         d.color[:] = [float(x) for x in m[1]]
+        opt = m[2] if len(m) > 2 else {}
+        d.color2[:] = [float(x) for x in opt.get("mirror_color", (1.0, 1.0, 1.0))]
+        d.power = float(opt.get("emit", 0.0))
+        d.params[:5] = [float(opt.get("diffuse_reflect", 1.0)), float(opt.get("specular_reflect", 0.0)),
+                        float(opt.get("transparency", 0.0)), float(opt.get("translucency", 0.0)),
+                        float(opt.get("transmit_filter", 1.0))]
+        d.params[6] = 1.0 if opt.get("fresnel_effect", False) else 0.0
+        d.params[7] = float(opt.get("IOR", 1.33))
     elif kind == "light_mat":
         d.color[:] = [float(x) for x in m[1]]
         d.power = float(m[2])

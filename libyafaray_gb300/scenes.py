@@ -227,7 +227,8 @@ def icosphere(center, radius, subdiv):
     return P.astype(np.float32), np.asarray(out, np.uint32)
 
 
-def cornell_scene(res=512, light_samples=4, bounces=5, rr_min=3, path_samples=1, glossy=False, glass=False, point_light=False):
+def cornell_scene(res=512, light_samples=4, bounces=5, rr_min=3, path_samples=1, glossy=False, glass=False, point_light=False,
+                  shiny=False):
     """The Cornell-box configuration: 34 triangles of walls and boxes
     (shinydiffuse, grey 0.75 / red / green), a 0.5 x 0.5 m ceiling area light
     of colour (17,12,4) at y = 1.999 with a 2-triangle light_mat emitter,
@@ -237,13 +238,34 @@ def cornell_scene(res=512, light_samples=4, bounces=5, rr_min=3, path_samples=1,
     short box and a rough-glass sphere (IOR 1.5, alpha 0.2, r 0.3) at the
     front left, both rendered through the recursive split.  point_light=True
     replaces the area light (and its emitter) by a pointlight at (0, 1.8, 0.2)
-    of power 3."""
+    of power 3.  shiny=True gives the shinydiffuse layers work: the tall box
+    a Fresnel mirror (specular_reflect 0.8, IOR 1.5), the short box
+    transparency 0.5 (transmit_filter 0.7) with translucency 0.3, the green
+    wall a plain 0.4 mirror over its diffuse layer, the red wall emit 0.3."""
     verts, faces, groups = cornell_mesh(as_quads=False)
     mats = {"grey": ("shinydiffusemat", (0.75, 0.75, 0.75)),
             "red": ("shinydiffusemat", (0.63, 0.065, 0.05)),
             "green": ("shinydiffusemat", (0.14, 0.45, 0.09)),
             "emitter": ("light_mat", (17.0, 12.0, 4.0), 1.0)}
     gmat = {0: "grey", 1: "red", 2: "green", 3: "grey", 4: "grey"}
+    if shiny:
+        feats = {"mirror", "fresnel", "transparent", "translucent", "emit"} if shiny is True else set(shiny)
+        if "emit" in feats:
+            mats["red"] = ("shinydiffusemat", (0.63, 0.065, 0.05), {"emit": 0.3})
+        if "mirror" in feats:
+            mats["green"] = ("shinydiffusemat", (0.14, 0.45, 0.09), {"specular_reflect": 0.4, "mirror_color": (0.8, 1.0, 0.8)})
+        if "fresnel" in feats:
+            mats["fresnel_box"] = ("shinydiffusemat", (0.75, 0.75, 0.75),
+                                   {"specular_reflect": 0.8, "fresnel_effect": True, "IOR": 1.5, "mirror_color": (0.9, 0.95, 1.0)})
+            gmat[4] = "fresnel_box"
+        clear = {}
+        if "transparent" in feats:
+            clear.update({"transparency": 0.5, "transmit_filter": 0.7})
+        if "translucent" in feats:
+            clear.update({"translucency": 0.3, "diffuse_reflect": 0.8})
+        if clear:
+            mats["clear_box"] = ("shinydiffusemat", (0.2, 0.6, 0.9), clear)
+            gmat[3] = "clear_box"
     if glossy:
         mats["glossy_box"] = glossy_material((0.75, 0.75, 0.75), exponent=100.0)
         mats["glossy_floor"] = glossy_material((0.75, 0.75, 0.75), exponent=20.0, glossy_reflect=0.4)

@@ -134,7 +134,15 @@ def reference_scene_text(scene, spp, batches, threads=-1):
     for name, m in scene["materials"].items():
         t = m[0]
         if t == "shinydiffusemat":
-            out.append(f"material {name} shinydiffusemat {m[1][0]!r} {m[1][1]!r} {m[1][2]!r}")
+            extra = ""
+            for k, v in (m[2] if len(m) > 2 else {}).items():
+                if isinstance(v, bool):
+                    extra += f" {k}={str(v).lower()}"
+                elif isinstance(v, (tuple, list)):
+                    extra += f" {k}=" + ",".join(repr(float(x)) for x in v)
+                else:
+                    extra += f" {k}={float(v)!r}"
+            out.append(f"material {name} shinydiffusemat {m[1][0]!r} {m[1][1]!r} {m[1][2]!r}{extra}")
         elif t == "light_mat":
             out.append(f"material {name} light_mat {m[1][0]!r} {m[1][1]!r} {m[1][2]!r} {m[2]!r}")
         elif t == "glossy":

@@ -121,6 +121,17 @@ int main(int argc, char **argv)
 				yafaray_setParamMapColor(pm, "filter_color", r, g, b, 1.0);
 				yafaray_setParamMapColor(pm, "mirror_color", mr, mg, mb, 1.0);
 			}
+			// optional key=value parameters (a colour as r,g,b)
+			std::string kv;
+			while(ss >> kv)
+			{
+				const size_t eq = kv.find('=');
+				if(eq == std::string::npos) continue;
+				const std::string key = kv.substr(0, eq), val = kv.substr(eq + 1);
+				double r, g, b;
+				if(std::sscanf(val.c_str(), "%lf,%lf,%lf", &r, &g, &b) == 3) yafaray_setParamMapColor(pm, key.c_str(), r, g, b, 1.0);
+				else setTyped(pm, key, val);
+			}
 			size_t id;
 			yafaray_createMaterial(scene, &id, name.c_str(), pm, pml);
 		}

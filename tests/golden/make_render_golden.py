@@ -233,5 +233,7 @@ if __name__ == "__main__":
         cornell_pm_golden()
     if "film" in what:
         film_golden()
+    if "cornell_shiny" in what:
+        variant_golden("cornell_shiny_64_render.npz", shiny=True)
     if "cornell_point" in what:
         variant_golden("cornell_point_64_render.npz", point_light=True)

@@ -107,6 +107,21 @@ def test_gpu_cornell_glass_matches_reference(cuda_device):
     assert frac >= 0.995
 
 
+def test_gpu_cornell_shiny_layers_match_reference(cuda_device):
+    """ShinyDiffuseMaterial's layers: a Fresnel mirror (specular_reflect 0.8,
+    IOR 1.5), transparency 0.5 with transmit_filter 0.7 and translucency 0.3,
+    a plain 0.4 mirror over a diffuse layer and an emissive wall, through the
+    recursive split (getSpecular) and the path loop (component sampling)."""
+    g = np.load(os.path.join(GOLD, "cornell_shiny_64_render.npz"))
+    sc = scenes.cornell_scene(res=64, shiny=True)
+    r = gbrt.Renderer(sc)
+    gb = batches(r, int(g["spp"]), int(g["batches"]))
+    frac, relmse, m = parity(gb, g["mean"], g["se"])
+    print(f"cornell shiny 64x64: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
+          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
+    assert frac >= 0.995
+
+
 def test_gpu_cornell_pointlight_matches_reference(cuda_device):
     """A pointlight (MonteCarloIntegrator::diracLight: one shadow ray, colour x
     power / d^2, no MIS) instead of the area light."""
