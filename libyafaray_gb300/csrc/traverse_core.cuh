@@ -242,7 +242,14 @@ __device__ __forceinline__ bool trace_init(TraceState &S, const BvhView &bv, flo
 	// accelerator_kdtree_common.h:139, accelerator.h:64
 	const float bias = xm(0.1f * 0.00005f, fabsf(xs(leave, enter)));
 	S.t_min = kShadow ? bias : fmaxf(tmin, bias);
+	// A zero (or denormal) direction component would make 1/d infinite and
+	// the node planes' t values infinite or NaN, which the min / max chains
+	// ignore: that axis would stop culling and the ray would walk most of
+	// the tree.  +-2^64 instead keeps every slab sign exact (power-of-two
+	// scaling) and puts planes outside the ray's slab far beyond any hit.
 	S.inv[0] = 1.f / dx; S.inv[1] = 1.f / dy; S.inv[2] = 1.f / dz;
+	for(int k = 0; k < 3; ++k)
+		if(isinf(S.inv[k])) S.inv[k] = copysignf(18446744073709551616.f, S.inv[k]);
 	S.oct = (dx < 0.f ? 1u : 0u) | (dy < 0.f ? 2u : 0u) | (dz < 0.f ? 4u : 0u);
 	// a virtual group whose only (internal) child, in slot 0, is the root
 	S.nbase = 0;
