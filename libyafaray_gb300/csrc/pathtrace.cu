@@ -3078,7 +3078,7 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	// at most W / path_samples + 2 such roots, a chunk of c spawned records at
 	// most c / n_min + 1, n_min = the fewest path samples a spawned call gets
 	// (the glossy split divides by up to 8)
-	constexpr uint64_t kSpawnCap = 1ull << 23;
+	constexpr uint64_t kSpawnCap = 1ull << 24;
 	const uint64_t ps = static_cast<uint64_t>(pp.path_samples);
 	const uint64_t n_min = std::max<uint64_t>(1, ps / (S->split_glossy ? 8u : 1u));
 	size_t spawn_cap = 0;
