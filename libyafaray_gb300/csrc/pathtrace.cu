@@ -690,7 +690,7 @@ __device__ __forceinline__ uint32_t shiny_cflags(int i)
 }
 
 // eval (:297-337) with bsdfs = All
-__device__ __forceinline__ void shiny_eval(const Surface &s, const float wo[3], const float wl[3], float out[3])
+__device__ __noinline__ void shiny_eval_layers(const Surface &s, const float wo[3], const float wl[3], float out[3])
 {
 	const DevMaterial &m = *s.m;
 	out[0] = out[1] = out[2] = 0.f;
@@ -713,7 +713,7 @@ __device__ __forceinline__ void shiny_eval(const Surface &s, const float wo[3], 
 
 // pdf (:443-484): the components whose flags share a bit with bsdfs add
 // their weights to the normalisation (mirror and transparency included).
-__device__ __forceinline__ float shiny_pdf(const Surface &s, const float wo[3], const float wi[3], uint32_t bsdfs)
+__device__ __noinline__ float shiny_pdf_layers(const Surface &s, const float wo[3], const float wi[3], uint32_t bsdfs)
 {
 	const DevMaterial &m = *s.m;
 	if(!(bsdfs & BF_DIFFUSE)) return 0.f;
@@ -747,8 +747,8 @@ __device__ __forceinline__ void reflect_dir(const float n[3], const float v[3], 
 
 // sample (:346-440): pick a component among those whose flags are all in
 // the request, by s1, then sample it; w = |wi . N| / (0.99 pdf + 0.01).
-__device__ __forceinline__ bool shiny_sample(const Surface &s, const float wo[3], float s1, float s2, uint32_t req, float wi[3], float col[3],
-                                             float &w, float &pdf, uint32_t &sampled)
+__device__ __noinline__ bool shiny_sample_layers(const Surface &s, const float wo[3], float s1, float s2, uint32_t req, float wi[3],
+                                                 float col[3], float &w, float &pdf, uint32_t &sampled)
 {
 	const DevMaterial &m = *s.m;
 	const float cos_ng_wo = dot3(s.ng, wo);
@@ -816,6 +816,50 @@ __device__ __forceinline__ bool shiny_sample(const Surface &s, const float wo[3]
 		const float alpha = 1.f - (1.f - m.sdc[0] * kr) * m.sdc[1];
 		w = xa(xm(w, alpha), 1.f - alpha);
 	}
+	return true;
+}
+
+// The diffuse layer alone (no mirror, transparency, translucency or
+// Fresnel): kr = 1 and the accumulated weight is the diffuse strength c, so
+// eval = c colour, pdf = |wi.n| c / c and sample picks the one component
+// with width c (1 / c) — the same float operations as the general code.
+__device__ __forceinline__ void shiny_eval(const Surface &s, const float wo[3], const float wl[3], float out[3])
+{
+	if(s.m->sd != SD_DIFFUSE) { shiny_eval_layers(s, wo, wl, out); return; }
+	out[0] = out[1] = out[2] = 0.f;
+	float n[3];
+	face_forward(s, wo, n);
+	if(dot3(n, wl) < 0.f) return;
+	const float m_d = s.m->sdc[3];
+	for(int k = 0; k < 3; ++k) out[k] = m_d * s.m->col[k];
+}
+
+__device__ __forceinline__ float shiny_pdf(const Surface &s, const float wo[3], const float wi[3], uint32_t bsdfs)
+{
+	if(s.m->sd != SD_DIFFUSE) return shiny_pdf_layers(s, wo, wi, bsdfs);
+	if(!(bsdfs & BF_DIFFUSE)) return 0.f;
+	const float c = s.m->sdc[3];
+	if(c < 0.00001f) return 0.f;
+	float n[3];
+	face_forward(s, wo, n);
+	return (fabsf(dot3(wi, n)) * c) / c;
+}
+
+__device__ __forceinline__ bool shiny_sample(const Surface &s, const float wo[3], float s1, float s2, uint32_t req, float wi[3], float col[3],
+                                             float &w, float &pdf, uint32_t &sampled)
+{
+	if(s.m->sd != SD_DIFFUSE) return shiny_sample_layers(s, wo, s1, s2, req, wi, col, w, pdf, sampled);
+	const float c = s.m->sdc[3];
+	if((req & (BF_DIFFUSE | BF_REFLECT)) != (BF_DIFFUSE | BF_REFLECT) || c < 0.00001f) { sampled = 0u; pdf = 0.f; return false; }
+	const float width = c * (1.f / c);
+	float n[3];
+	face_forward(s, wo, n);
+	cos_hemisphere(n, s.u, s.v, s1 / width, s2, wi);
+	col[0] = col[1] = col[2] = 0.f;
+	if(xm(dot3(s.ng, wo), dot3(s.ng, wi)) > 0.f) for(int k = 0; k < 3; ++k) col[k] = c * s.m->col[k];
+	pdf = fabsf(dot3(wi, n)) * width;
+	sampled = BF_DIFFUSE | BF_REFLECT;
+	w = __fdiv_rn(fabsf(dot3(wi, s.n)), xa(xm(pdf, 0.99f), 0.01f));
 	return true;
 }
 
@@ -1763,6 +1807,9 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 	}
 }
 
+// kFilm: the film has a filter (film_splat); the plain-sum variant keeps
+// the splat's registers out of this kernel.
+template <bool kFilm>
 __global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Params P, Work W, uint32_t shadow_cap, float *film, double *film64)
 {
 	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
@@ -1781,7 +1828,8 @@ __global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Params P,
 			if(h.prim < 0)
 			{
 				const float4 c = W.s_col[i];
-				film_put(P, film, film64, W.s_pix[i], W.p_si[W.s_path[i]], c.x, c.y, c.z);
+				if(kFilm) film_splat(P, film, film64, W.s_pix[i], W.p_si[W.s_path[i]], c.x, c.y, c.z, false);
+				else film_add(film, film64, W.s_pix[i], c.x, c.y, c.z);
 				if(W.p_sum) path_sum_add(W, W.s_path[i], c.x, c.y, c.z);
 			}
 		});
@@ -3161,8 +3209,12 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 			if(level_guided)
 				if(int rc = gbrt_guide_eval_queue(guide, Ww.hitpos, n, Ww.count + cur, Ww.lobes, s)) return rc;
 			k_shade<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, camera->resx, static_cast<uint32_t>(shadow_cap), film, film64_dev);
-			k_shadow<<<persistent_grid(k_shadow, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, static_cast<uint32_t>(shadow_cap), film,
-			                                                                             film64_dev);
+			if(Pw.film_w)
+				k_shadow<true><<<persistent_grid(k_shadow<true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, static_cast<uint32_t>(shadow_cap),
+				                                                                                         film, film64_dev);
+			else
+				k_shadow<false><<<persistent_grid(k_shadow<false>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, static_cast<uint32_t>(shadow_cap),
+				                                                                                           film, film64_dev);
 			cur ^= 1;
 		}
 		return GBRT_OK;
