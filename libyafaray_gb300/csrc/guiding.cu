@@ -46,7 +46,8 @@ GBRT_GHD void encode(const GuideGrid &g, const float *__restrict__ table, const 
 {
 	float x[3];
 	for(int a = 0; a < 3; ++a) x[a] = fminf(fmaxf((p[a] - g.lo[a]) * g.inv_ext[a], 0.f), 1.f);
-#pragma unroll 1
+	// 4 levels per round: 32 independent L2 gathers in flight per thread
+#pragma unroll 4
 	for(int l = 0; l < kGuideLevels; ++l)
 	{
 		const float r = g.res[l];
