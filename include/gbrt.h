@@ -268,6 +268,23 @@ typedef struct gbrt_pt_params {
 	float *film_weight_dev;
 } gbrt_pt_params;
 
+/* Adaptive anti-aliasing (ImageFilm / TiledIntegrator parameters with the
+ * reference's names and defaults in brackets). */
+typedef struct gbrt_aa_params {
+	int32_t passes;                          /* AA_passes [1] */
+	int32_t inc_samples;                     /* AA_inc_samples [1] */
+	float threshold;                         /* AA_threshold [0.05] */
+	float resampled_floor;                   /* AA_resampled_floor, percent of the pixels [0] */
+	float sample_multiplier_factor;          /* AA_sample_multiplier_factor [1] */
+	float light_sample_multiplier_factor;    /* AA_light_sample_multiplier_factor [1] */
+	float indirect_sample_multiplier_factor; /* AA_indirect_sample_multiplier_factor [1] (final gathering only) */
+	int32_t detect_color_noise;              /* AA_detect_color_noise [0] */
+	int32_t dark_detection_type;             /* AA_dark_detection_type: 0 none [default], 1 linear, 2 curve */
+	float dark_threshold_factor;             /* AA_dark_threshold_factor [0] */
+	int32_t variance_edge_size;              /* AA_variance_edge_size [10] */
+	int32_t variance_pixels;                 /* AA_variance_pixels [0] */
+} gbrt_aa_params;
+
 #define GBRT_FILTER_PIXEL 0u
 #define GBRT_FILTER_BOX 1u
 #define GBRT_FILTER_GAUSS 2u
@@ -309,10 +326,32 @@ int gbrt_pt_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const
                         float *image_out, gbrt_pt_stats *stats);
 
 
+/* TiledIntegrator::render with adaptive anti-aliasing (integrator_tiled.cc:
+ * 160-214, ImageFilm::nextPass imagefilm.cc:365-547): pass 0 renders every
+ * pixel with params->spp (AA_minsamples) samples; each later pass flags the
+ * pixels whose normalised colour differs from a neighbour's by the
+ * threshold (dark detection, variance window, threshold lowered below the
+ * resampled floor) and renders AA_inc_samples x multiplier more samples in
+ * those only.  With more than one pass, sample positions are riVdC / riS.
+ * pathtracing only.  params->filter_type must not be GBRT_FILTER_PIXEL and
+ * film_weight_dev is required (device, caller-zeroed, like film_dev);
+ * resampled (optional, aa->passes entries): pixels sampled per pass. */
+int gbrt_pt_render_aa(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params,
+                      const gbrt_aa_params *aa, float *film_dev, gbrt_pt_stats *stats, uint32_t *resampled, void *stream);
+/* Same into a host image of resx * resy * 3 floats (sum / weight); the film
+ * and weight buffers are allocated inside the call. */
+int gbrt_pt_render_aa_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params,
+                           const gbrt_aa_params *aa, float *image_out, gbrt_pt_stats *stats, uint32_t *resampled);
+/* Diagnostics: the pixels ImageFilm::nextPass would flag for resampling on a
+ * device film (sums, weights) at the given threshold; flags_dev = 1 byte per
+ * pixel.  Synchronises. */
+int gbrt_aa_flags(const float *film_dev, const float *weight_dev, int32_t resx, int32_t resy, const gbrt_aa_params *aa,
+                  float threshold, uint8_t *flags_dev, uint32_t *n_flagged);
+
 /* Renders n scenes (each with its camera, parameters and device float film),
  * up to `concurrency` at a time (0 = 8), each on its own stream from its own
  * host thread, freeing each scene's work buffers after its render; wave_paths
- * 0 means 1 Mi per scene here.  stats: NULL or n entries.  Returns the first
+ * 0 means 2 Mi per scene here.  stats: NULL or n entries.  Returns the first
  * error (its message names the scene). */
 int gbrt_pt_render_batch(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params, float *const *films,
                          uint32_t n, uint32_t concurrency, gbrt_pt_stats *stats);

@@ -122,6 +122,11 @@ struct Params {
 	float filter_width;        // filter_width_ (pixels)
 	float filter_scale;        // filter_table_scale_
 	int film_resx, film_resy;
+	// adaptive anti-aliasing (TiledIntegrator::render / renderTile)
+	float lmult;               // aa_light_sample_multiplier
+	int aa_multipass;          // AA_passes > 1: sample positions (riVdC, riS)
+	const uint32_t *pix_list;  // pixels of this pass (resampled ones), or NULL for all
+	uint32_t n_list;
 };
 
 struct Work {
@@ -1069,21 +1074,23 @@ struct ShadowWriter {
 // (areaLightSampleLight, :192-330) and num_samples BSDF samples that hit the
 // light (areaLightSampleMaterial, :332-415), power-heuristic MIS, Halton
 // bases 2/3 from offs = num_samples * sample + pixel offset + loffs * 4567.
-__device__ __forceinline__ int light_samples(const DevLight &L, uint32_t division)
+__device__ __forceinline__ int light_samples(const DevLight &L, uint32_t division, float lmult)
 {
 	if(L.type == GBRT_LIGHT_POINT) return 1;
-	return division > 1 ? max(1, L.samples / static_cast<int>(division)) : L.samples;   // integrator_montecarlo.cc:428-429
+	// integrator_montecarlo.cc:428-429
+	const int n = static_cast<int>(ceilf(static_cast<float>(L.samples) * lmult));
+	return division > 1 ? max(1, n / static_cast<int>(division)) : n;
 }
 
 // Shadow rays one light estimation writes: 2 per area-light sample, 1 for a point light.
-__device__ __forceinline__ uint32_t light_shadow_rays(const DevLight &L, uint32_t division)
+__device__ __forceinline__ uint32_t light_shadow_rays(const DevLight &L, uint32_t division, float lmult)
 {
-	return L.type == GBRT_LIGHT_POINT ? 1u : 2u * static_cast<uint32_t>(light_samples(L, division));
+	return L.type == GBRT_LIGHT_POINT ? 1u : 2u * static_cast<uint32_t>(light_samples(L, division, lmult));
 }
 
 __device__ void light_estimation(const SceneDev &sc, const Surface &s, const float wo[3], uint32_t li, uint32_t loffs,
                                  uint32_t sample_, uint32_t offset_, const float weight[3], uint32_t pixel, ShadowWriter &sw,
-                                 uint32_t division)
+                                 uint32_t division, float lmult)
 {
 	const DevLight &L = sc.lights[li];
 	if(L.type == GBRT_LIGHT_POINT)
@@ -1106,7 +1113,7 @@ __device__ void light_estimation(const SceneDev &sc, const Surface &s, const flo
 		if(c[0] != 0.f || c[1] != 0.f || c[2] != 0.f) sw.put(s.p, sbias, ldir, dist, pixel, c);
 		return;
 	}
-	const int ns = light_samples(L, division);
+	const int ns = light_samples(L, division, lmult);
 	const float inv_ns = __fdiv_rn(1.f, static_cast<float>(ns));
 	const uint32_t offs = static_cast<uint32_t>(ns) * sample_ + offset_ + loffs * 4567u;
 	const float plen = sqrtf(dot3(s.p, s.p));
@@ -1300,7 +1307,15 @@ __device__ __forceinline__ int round_bias(double v) { return static_cast<int>(v 
 __device__ __forceinline__ void sample_pos(const Params &P, uint32_t pixel, uint32_t si, float &dx, float &dy)
 {
 	dx = 0.5f; dy = 0.5f;
-	if(P.spp > 1)
+	if(P.aa_multipass)
+	{
+		// AA_passes > 1 (integrator_tiled.cc:316-319): sample index of the pass
+		const uint32_t sample_ = P.base_offset + si / static_cast<uint32_t>(P.path_samples);
+		const uint32_t off = pixel_offset(pixel, P.film_resx);
+		dx = gbrt::ri_vdc(sample_, off);
+		dy = gbrt::ri_s(sample_, off);
+	}
+	else if(P.spp > 1)
 	{
 		const uint32_t sample = si / static_cast<uint32_t>(P.path_samples);
 		dx = xm(xa(0.5f, static_cast<float>(sample)), P.d1);
@@ -1354,21 +1369,15 @@ __global__ void __launch_bounds__(kThreads) k_camera(Camera cam, Params P, Work 
 	// full image, and neighbouring threads shoot neighbouring pixels; the
 	// path samples of one camera sample are adjacent (so a wave of W paths
 	// holds at most W / path_samples + 2 integrate() roots)
-	const uint32_t n_pix = static_cast<uint32_t>(cam.resx) * static_cast<uint32_t>(cam.resy);
+	const uint32_t n_pix = P.pix_list ? P.n_list : static_cast<uint32_t>(cam.resx) * static_cast<uint32_t>(cam.resy);
 	const uint32_t ps = static_cast<uint32_t>(P.path_samples);
 	for(uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < P.wave_n; s += gridDim.x * blockDim.x)
 	{
 		const uint32_t g = P.wave_start + s;
 		const uint32_t rest = g / ps, sub = g % ps;
-		const uint32_t pixel = rest % n_pix, si = (rest / n_pix) * ps + sub;
-		const uint32_t sample = si / static_cast<uint32_t>(P.path_samples);
-		const uint32_t offset_ = pixel_offset(pixel, cam.resx);
-		float dx = 0.5f, dy = 0.5f;
-		if(P.spp > 1)
-		{
-			dx = xm(xa(0.5f, static_cast<float>(sample)), P.d1);
-			dy = gbrt::ri_lp(sample + offset_);
-		}
+		const uint32_t pixel = P.pix_list ? P.pix_list[rest % n_pix] : rest % n_pix, si = (rest / n_pix) * ps + sub;
+		float dx, dy;
+		sample_pos(P, pixel, si, dx, dy);
 		const float px = xa(static_cast<float>(pixel % static_cast<uint32_t>(cam.resx)), dx);
 		const float py = xa(static_cast<float>(pixel / static_cast<uint32_t>(cam.resx)), dy);
 		float d[3];
@@ -1506,7 +1515,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				do_nee_all = (s.m->flags & BF_DIFFUSE) && sub == 0;
 				for(int c = 0; c < 3; ++c) nee_weight[c] = thr[c];
 				if(do_nee_all)
-					for(uint32_t l = 0; l < P.n_lights; ++l) n_shadow += light_shadow_rays(sc.lights[l], division);
+					for(uint32_t l = 0; l < P.n_lights; ++l) n_shadow += light_shadow_rays(sc.lights[l], division, P.lmult);
 				// recursiveRaytrace at ray level + 1 (integrator_path_tracer.cc:287,
 				// integrator_montecarlo.cc:698-710)
 				addl = max(addl, s.m->addl_depth);
@@ -1562,7 +1571,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 								const float r = rng01(pixel, sample_ * 64u + sub, k, tseed ^ 0x9e3779b9u);
 								nee_light = min(static_cast<uint32_t>(r * static_cast<float>(P.n_lights)), P.n_lights - 1u);
 								for(int c = 0; c < 3; ++c) nee_weight[c] = thr[c] * static_cast<float>(P.n_lights);
-								n_shadow = light_shadow_rays(sc.lights[nee_light], division);
+								n_shadow = light_shadow_rays(sc.lights[nee_light], division, P.lmult);
 							}
 						}
 						else if(fg_caustic)
@@ -1628,7 +1637,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 						const float r = rng01(pixel, sample_ * 64u + sub, k, tseed ^ 0x9e3779b9u);
 						nee_light = min(static_cast<uint32_t>(r * static_cast<float>(P.n_lights)), P.n_lights - 1u);
 						for(int c = 0; c < 3; ++c) nee_weight[c] = xm(thr[c], static_cast<float>(P.n_lights));
-						n_shadow = light_shadow_rays(sc.lights[nee_light], division);
+						n_shadow = light_shadow_rays(sc.lights[nee_light], division, P.lmult);
 					}
 					float e[3];
 					if((k == 1 && (s.m->flags & BF_EMIT)) || (k >= 2 && (mat1 & BF_EMIT) && caustic))
@@ -1654,8 +1663,8 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 		ShadowWriter sw{W.s_ray, W.s_col, W.s_pix, W.s_path, path, wbase + incl - n_shadow, wbase + incl};
 		if(sw.end > shadow_cap) sw.end = sw.slot > shadow_cap ? sw.slot : shadow_cap;
 		if(do_nee_all)
-			for(uint32_t l = 0; l < P.n_lights; ++l) light_estimation(sc, s, wo, l, l, sample_, offset_, nee_weight, pixel, sw, division);
-		if(do_nee_one) light_estimation(sc, s, wo, nee_light, nee_light, sample_, offset_, nee_weight, pixel, sw, division);
+			for(uint32_t l = 0; l < P.n_lights; ++l) light_estimation(sc, s, wo, l, l, sample_, offset_, nee_weight, pixel, sw, division, P.lmult);
+		if(do_nee_one) light_estimation(sc, s, wo, nee_light, nee_light, sample_, offset_, nee_weight, pixel, sw, division, P.lmult);
 		sw.close();
 		// --- spawned integrate() calls of the recursive split ----------------
 		if(W.sp_out && __any_sync(0xffffffffu, n_spawn != 0u))
@@ -1948,14 +1957,123 @@ __global__ void k_mean(const float *sum, const double *sum64, float *out, size_t
 		out[i] = sum64 ? static_cast<float>(sum64[i] * static_cast<double>(inv)) : sum[i] * inv;
 }
 
-// Rgba::normalized (color.h:538-542): sum / weight, 0 where the weight is 0.
+// ---- adaptive anti-aliasing: ImageFilm::nextPass (imagefilm.cc:365-547) ----
+struct AaDev {
+	float threshold;
+	int color_noise, dark_type;
+	float dark_factor;
+	int var_half, var_pixels;
+};
+
+// Combined colour of a pixel normalised by its weight: Rgba::normalized and
+// operator / (color.h:294-298, 538-542) multiply by the reciprocal.  Every
+// camera sample here carries alpha 1 (no transparent background), so the
+// alpha sum equals the weight sum and alpha = w x (1 / w); 0 without samples.
+__device__ __forceinline__ float4 aa_color(const float *film, const float *w, int i)
+{
+	const float wt = w[i];
+	if(wt == 0.f) return make_float4(0.f, 0.f, 0.f, 0.f);
+	const float r = __fdiv_rn(1.f, wt);
+	return make_float4(xm(film[3 * i], r), xm(film[3 * i + 1], r), xm(film[3 * i + 2], r), xm(wt, r));
+}
+// Rgb::col2Bri (color.h:57), unfused like the reference's host build
+__device__ __forceinline__ float aa_bri(float4 c) { return xa(xa(xm(0.2126f, c.x), xm(0.7152f, c.y)), xm(0.0722f, c.z)); }
+
+// Rgba::colorDifference (color.h:434-452)
+__device__ __forceinline__ float aa_diff(float4 a, float4 b, int color_noise)
+{
+	float d = fabsf(xs(aa_bri(b), aa_bri(a)));
+	if(color_noise)
+	{
+		d = fmaxf(d, fabsf(xs(b.x, a.x))); d = fmaxf(d, fabsf(xs(b.y, a.y)));
+		d = fmaxf(d, fabsf(xs(b.z, a.z))); d = fmaxf(d, fabsf(xs(b.w, a.w)));
+	}
+	return d;
+}
+
+// ImageFilm::darkThresholdCurveInterpolate (imagefilm.cc:882-899)
+__device__ float aa_dark_curve(float b)
+{
+	// brightness knots and thresholds; between knots linear:
+	// t0 + (b - b0) x (t1 - t0) / (b1 - b0), each operation rounded in float
+	constexpr float kb[13] = {0.10f, 0.20f, 0.30f, 0.40f, 0.50f, 0.60f, 0.70f, 0.80f, 0.90f, 1.00f, 1.20f, 1.40f, 1.80f};
+	constexpr float kt[13] = {0.0001f, 0.0010f, 0.0020f, 0.0035f, 0.0055f, 0.0075f, 0.0100f, 0.0150f, 0.0250f, 0.0400f, 0.0800f, 0.0950f, 0.1000f};
+	constexpr float kw[13] = {0.f, 0.10f, 0.10f, 0.10f, 0.10f, 0.10f, 0.10f, 0.10f, 0.10f, 0.10f, 0.20f, 0.20f, 0.40f};
+	if(b <= kb[0]) return kt[0];
+	for(int k = 1; k < 13; ++k)
+		if(b <= kb[k]) return xa(kt[k - 1], __fdiv_rn(xm(xs(b, kb[k - 1]), kt[k] - kt[k - 1]), kw[k]));
+	return kt[12];
+}
+
+// Pixels without samples are flagged first, the rest cleared.
+__global__ void k_aa_init(const float *__restrict__ w, uint32_t n, uint8_t *__restrict__ flags)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) flags[i] = w[i] > 0.f ? 0u : 1u;
+}
+
+// One thread per pixel (x < W-1, y < H-1): neighbour differences set both
+// pixels' flags; the variance window flags a block around the pixel.
+// Every write stores 1, so concurrent writers agree.
+__global__ void k_aa_detect(const float *__restrict__ film, const float *__restrict__ w, int W, int H, AaDev a, uint8_t *flags)
+{
+	const uint32_t n = static_cast<uint32_t>(W - 1) * static_cast<uint32_t>(H - 1);
+	for(uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+	{
+		const int x = static_cast<int>(t % static_cast<uint32_t>(W - 1)), y = static_cast<int>(t / static_cast<uint32_t>(W - 1));
+		const int i = y * W + x;
+		const float4 c = aa_color(film, w, i);
+		const float bri = aa_bri(make_float4(fabsf(c.x), fabsf(c.y), fabsf(c.z), 0.f));  // Rgb::abscol2Bri (color.h:58)
+		float thr = a.threshold;
+		if(a.dark_type == 1 && a.dark_factor > 0.f) thr = xm(a.threshold, xa(xs(1.f, a.dark_factor), xm(bri, a.dark_factor)));
+		else if(a.dark_type == 2) thr = aa_dark_curve(bri);
+		if(aa_diff(c, aa_color(film, w, i + 1), a.color_noise) >= thr) { flags[i] = 1u; flags[i + 1] = 1u; }
+		if(aa_diff(c, aa_color(film, w, i + W), a.color_noise) >= thr) { flags[i] = 1u; flags[i + W] = 1u; }
+		if(aa_diff(c, aa_color(film, w, i + W + 1), a.color_noise) >= thr) { flags[i] = 1u; flags[i + W + 1] = 1u; }
+		if(x > 0 && aa_diff(c, aa_color(film, w, i + W - 1), a.color_noise) >= thr) { flags[i] = 1u; flags[i + W - 1] = 1u; }
+		if(a.var_pixels > 0)
+		{
+			int vx = 0, vy = 0;
+			for(int xd = -a.var_half; xd < a.var_half - 1; ++xd)
+			{
+				const int xi = min(max(x + xd, 0), W - 2);
+				if(aa_diff(aa_color(film, w, y * W + xi), aa_color(film, w, y * W + xi + 1), a.color_noise) >= thr) ++vx;
+			}
+			for(int yd = -a.var_half; yd < a.var_half - 1; ++yd)
+			{
+				const int yi = min(max(y + yd, 0), H - 2);
+				if(aa_diff(aa_color(film, w, yi * W + x), aa_color(film, w, (yi + 1) * W + x), a.color_noise) >= thr) ++vy;
+			}
+			if(vx + vy >= a.var_pixels)
+				for(int xd = -a.var_half; xd < a.var_half; ++xd)
+					for(int yd = -a.var_half; yd < a.var_half; ++yd)
+					{
+						const int xi = min(max(x + xd, 0), W - 1), yi = min(max(y + yd, 0), H - 1);
+						flags[yi * W + xi] = 1u;
+					}
+		}
+	}
+}
+
+// Flagged pixels -> list (order irrelevant: a pixel's samples depend only on
+// the pixel and the sample index); count only without a list.
+__global__ void k_aa_compact(const uint8_t *__restrict__ flags, uint32_t n, uint32_t *__restrict__ list, uint32_t *count)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		if(flags[i])
+		{
+			const uint32_t k = atomicAdd(count, 1u);
+			if(list) list[k] = i;
+		}
+}
+
+// Rgba::normalized (color.h:294-298, 538-542): sum x (1 / weight), 0 where the weight is 0.
 __global__ void k_normalize(const float *sum, const double *sum64, const float *w, float *out, size_t n)
 {
 	for(size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
 	{
 		const float wt = w[i / 3];
 		const float v = sum64 ? static_cast<float>(sum64[i]) : sum[i];
-		out[i] = wt != 0.f ? v / wt : 0.f;
+		out[i] = wt != 0.f ? v * (1.f / wt) : 0.f;
 	}
 }
 
@@ -3091,8 +3209,18 @@ static int film_filter_table(uint32_t type, float pixel_width, float table[256],
 // The wavefront render of gbrt_pt_render / gbrt_pm_render (scene lock held).
 // pm: photonmapping setup (the PM fields of Params and its photon grids), or
 // NULL for pathtracing.
+// One pass of an adaptive anti-aliasing render (TiledIntegrator::render /
+// renderPass): the pixels to sample (NULL: all), whether the render has
+// more than one pass (sample positions), the light sample multiplier.
+struct AaPass {
+	const uint32_t *list;
+	uint32_t n_list;
+	int multipass;
+	float lmult;
+};
+
 static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params &pp_in, const Params *pm, float *film_dev,
-                         double *film64_dev, gbrt_pt_stats *stats, cudaStream_t s)
+                         double *film64_dev, gbrt_pt_stats *stats, cudaStream_t s, const AaPass *aa = nullptr)
 {
 	gbrt_pt_params pp = pp_in;
 	// the scene's buffers and filter table: after its previous render, whatever stream that used
@@ -3109,7 +3237,9 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	}
 	if(camera->resx <= 0 || camera->resy <= 0 || pp.spp <= 0 || pp.path_samples <= 0 || pp.bounces < 0 || pp.path_samples > 64)
 		return gbrt_set_error(GBRT_ERR_INVALID, "render: bad resolution or sampling parameters");
-	const uint64_t total = static_cast<uint64_t>(camera->resx) * camera->resy * pp.spp * pp.path_samples;
+	const uint64_t n_pixels = (aa && aa->list) ? aa->n_list : static_cast<uint64_t>(camera->resx) * camera->resy;
+	const float lmult = aa ? aa->lmult : 1.f;
+	const uint64_t total = n_pixels * pp.spp * pp.path_samples;
 	if(total >= (1ull << 32)) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_pt_render: %llu paths exceed 2^32", static_cast<unsigned long long>(total));
 	gbrt_guide *guide = pp.guide;
 	if(pp.guide_batch > kMaxBatch) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_pt_render: guide_batch %u > %u", pp.guide_batch, kMaxBatch);
@@ -3142,7 +3272,12 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	uint32_t max_shadow = 0;
 	{
 		uint32_t all = 0, one = 0;
-		for(const auto &l : S->lights_host) { all += 2u * l.samples; one = std::max(one, 2u * static_cast<uint32_t>(l.samples)); }
+		for(const auto &l : S->lights_host)
+		{
+			const uint32_t n = 2u * static_cast<uint32_t>(std::ceil(static_cast<float>(l.samples) * lmult));
+			all += n;
+			one = std::max(one, n);
+		}
 		max_shadow = std::max(all, one);
 	}
 	const size_t shadow_cap = std::max<size_t>(1, wave * max_shadow);
@@ -3155,6 +3290,10 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	P.raydepth = raydepth;
 	P.film_resx = camera->resx;
 	P.film_resy = camera->resy;
+	P.lmult = lmult;
+	P.aa_multipass = aa ? aa->multipass : 0;
+	P.pix_list = aa ? aa->list : nullptr;
+	P.n_list = aa ? aa->n_list : 0u;
 	if(pp.filter_type != GBRT_FILTER_PIXEL)
 	{
 		if(!pp.film_weight_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: filter type %u needs film_weight_dev", pp.filter_type);
@@ -3374,6 +3513,162 @@ int gbrt_dl_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbr
 {
 	if(!S || !camera || !params || !image_out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_dl_render_host: NULL argument");
 	return render_host(S, camera, params, caustic, image_out, stats, 2);
+}
+
+// ---- adaptive anti-aliasing passes ----
+
+// ImageFilm::nextPass detection (imagefilm.cc:399-512): flags and the list of
+// flagged pixels on stream s; the number flagged on the host.
+static int aa_detect(const float *film, const float *w, int W, int H, const gbrt_aa_params &a, float thr, uint8_t *flags, uint32_t *list,
+                     uint32_t *d_count, uint32_t &n_flagged, int n_sm, cudaStream_t s)
+{
+	const uint32_t n = static_cast<uint32_t>(W) * static_cast<uint32_t>(H);
+	k_aa_init<<<grid_for(n, n_sm), kThreads, 0, s>>>(w, n, flags);
+	if(W > 1 && H > 1)
+	{
+		const AaDev d{thr, a.detect_color_noise != 0, a.dark_detection_type, a.dark_threshold_factor, a.variance_edge_size / 2, a.variance_pixels};
+		k_aa_detect<<<grid_for(static_cast<size_t>(W - 1) * (H - 1), n_sm), kThreads, 0, s>>>(film, w, W, H, d, flags);
+	}
+	GBRT_CK(cudaMemsetAsync(d_count, 0, 4, s));
+	k_aa_compact<<<grid_for(n, n_sm), kThreads, 0, s>>>(flags, n, list, d_count);
+	GBRT_CK(cudaGetLastError());
+	GBRT_CK(cudaMemcpyAsync(&n_flagged, d_count, 4, cudaMemcpyDeviceToHost, s));
+	GBRT_CK(cudaStreamSynchronize(s));
+	return GBRT_OK;
+}
+
+static int aa_check(const gbrt_aa_params &a, const char *who)
+{
+	if(a.passes < 1 || a.inc_samples < 0 || a.variance_edge_size < 0 || a.dark_detection_type < 0 || a.dark_detection_type > 2)
+		return gbrt_set_error(GBRT_ERR_INVALID, "%s: bad AA parameters (passes %d, inc_samples %d, variance_edge_size %d, dark_detection_type %d)",
+		                      who, a.passes, a.inc_samples, a.variance_edge_size, a.dark_detection_type);
+	return GBRT_OK;
+}
+
+// TiledIntegrator::render's pass loop (integrator_tiled.cc:160-214): pass 0
+// renders every pixel with AA_samples; pass i multiplies the sample and
+// light-sample multipliers, re-runs the detection (skipped once a pass
+// flagged nothing and the threshold stayed), renders ceil(inc_samples x
+// sample multiplier) more samples per flagged pixel (every pixel when the
+// threshold is <= 0, ImageFilm::doMoreSamples, imagefilm.cc:763-766) at
+// sample offset base + samples so far, and lowers the threshold by
+// 10 % x min(8, floor / flagged) while fewer than the floor were flagged.
+static int aa_render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params &pp, const gbrt_aa_params &a, float *film,
+                            gbrt_pt_stats *stats, uint32_t *resampled, cudaStream_t s)
+{
+	const int W = camera->resx, H = camera->resy;
+	if(W <= 0 || H <= 0) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_aa: bad resolution");
+	const uint32_t n_pix = static_cast<uint32_t>(W) * static_cast<uint32_t>(H);
+	DevBuf flags, list, count;
+	if(a.passes > 1)
+	{
+		if(int rc = flags.alloc(n_pix)) return rc;
+		if(int rc = list.alloc(4ull * n_pix)) return rc;
+		if(int rc = count.alloc(4)) return rc;
+	}
+	gbrt_pt_stats sum{}, one{};
+	auto add = [&]() {
+		sum.camera_samples += one.camera_samples; sum.extension_rays += one.extension_rays;
+		sum.shadow_rays += one.shadow_rays; sum.ms += one.ms;
+	};
+	const AaPass first{nullptr, 0, a.passes > 1 ? 1 : 0, 1.f};
+	if(int rc = render_locked(S, camera, pp, nullptr, film, nullptr, stats ? &one : nullptr, s, &first)) return rc;
+	add();
+	if(resampled) resampled[0] = n_pix;
+	float smult = 1.f, lmult = 1.f, thr = a.threshold;
+	bool thr_changed = true;
+	int64_t n_res = 0;
+	uint32_t acum = static_cast<uint32_t>(pp.spp);
+	const int floor_pix = static_cast<int>(floorf(a.resampled_floor * static_cast<float>(n_pix) / 100.f));
+	for(int i = 1; i < a.passes; ++i)
+	{
+		smult *= a.sample_multiplier_factor;
+		lmult *= a.light_sample_multiplier_factor;
+		const bool all = !(thr > 0.f);
+		if(n_res > 0 || thr_changed)
+		{
+			if(all) n_res = n_pix;
+			else
+			{
+				uint32_t nf = 0;
+				if(int rc = aa_detect(film, pp.film_weight_dev, W, H, a, thr, flags.as<uint8_t>(), list.as<uint32_t>(), count.as<uint32_t>(), nf, S->n_sm, s)) return rc;
+				n_res = nf;
+			}
+			thr_changed = false;
+		}
+		const int mult = static_cast<int>(ceilf(static_cast<float>(a.inc_samples) * smult));
+		if(n_res > 0 && mult > 0)
+		{
+			gbrt_pt_params q = pp;
+			q.spp = mult;
+			q.base_sampling_offset = pp.base_sampling_offset + acum;
+			const AaPass pass{all ? nullptr : list.as<uint32_t>(), all ? 0u : static_cast<uint32_t>(n_res), 1, lmult};
+			if(int rc = render_locked(S, camera, q, nullptr, film, nullptr, stats ? &one : nullptr, s, &pass)) return rc;
+			add();
+		}
+		if(resampled) resampled[i] = static_cast<uint32_t>(std::max<int64_t>(0, n_res));
+		acum += static_cast<uint32_t>(mult);
+		if(n_res < floor_pix)
+		{
+			const float ratio = std::min(8.f, static_cast<float>(floor_pix) / static_cast<float>(n_res));
+			thr = thr * (1.f - 0.1f * ratio);
+			if(a.threshold > 0.f) thr_changed = true;
+		}
+	}
+	if(stats) *stats = sum;
+	return GBRT_OK;
+}
+
+int gbrt_pt_render_aa(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_aa_params *aa, float *film_dev,
+                      gbrt_pt_stats *stats, uint32_t *resampled, void *stream)
+{
+	if(!S || !camera || !params || !aa || !film_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_aa: NULL argument");
+	if(int rc = aa_check(*aa, "gbrt_pt_render_aa")) return rc;
+	if(params->filter_type == GBRT_FILTER_PIXEL || !params->film_weight_dev)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_aa: adaptive AA needs a filtered film (filter_type != PIXEL, film_weight_dev)");
+	if(params->guide) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_aa: no path guide in adaptive AA renders");
+	std::lock_guard<std::mutex> lock(S->mu);
+	return aa_render_locked(S, camera, *params, *aa, film_dev, stats, resampled, static_cast<cudaStream_t>(stream));
+}
+
+int gbrt_pt_render_aa_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params_in, const gbrt_aa_params *aa,
+                           float *image_out, gbrt_pt_stats *stats, uint32_t *resampled)
+{
+	if(!S || !camera || !params_in || !aa || !image_out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_aa_host: NULL argument");
+	if(camera->resx <= 0 || camera->resy <= 0) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_aa_host: bad resolution");
+	if(params_in->filter_type == GBRT_FILTER_PIXEL)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_aa_host: adaptive AA needs a filtered film (filter_type != PIXEL)");
+	const size_t n_pix = static_cast<size_t>(camera->resx) * camera->resy, n = 3 * n_pix;
+	gbrt_pt_params params = *params_in;
+	DevBuf sum, mean, weight;
+	if(int rc = sum.alloc(n * 4)) return rc;
+	if(int rc = mean.alloc(n * 4)) return rc;
+	if(int rc = weight.alloc(n_pix * 4)) return rc;
+	GBRT_CK(cudaMemset(sum.p, 0, n * 4));
+	GBRT_CK(cudaMemset(weight.p, 0, n_pix * 4));
+	params.film_weight_dev = weight.as<float>();
+	if(int rc = gbrt_pt_render_aa(S, camera, &params, aa, sum.as<float>(), stats, resampled, nullptr)) return rc;
+	k_normalize<<<grid_for(n, S->n_sm), kThreads>>>(sum.as<float>(), nullptr, weight.as<float>(), mean.as<float>(), n);
+	GBRT_CK(cudaGetLastError());
+	GBRT_CK(cudaMemcpy(image_out, mean.p, n * 4, cudaMemcpyDeviceToHost));
+	return GBRT_OK;
+}
+
+int gbrt_aa_flags(const float *film_dev, const float *weight_dev, int32_t resx, int32_t resy, const gbrt_aa_params *aa, float threshold,
+                  uint8_t *flags_dev, uint32_t *n_flagged)
+{
+	if(!film_dev || !weight_dev || !aa || !flags_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_aa_flags: NULL argument");
+	if(resx <= 0 || resy <= 0) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_aa_flags: bad resolution");
+	if(int rc = aa_check(*aa, "gbrt_aa_flags")) return rc;
+	int dev = 0, n_sm = 0;
+	GBRT_CK(cudaGetDevice(&dev));
+	GBRT_CK(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+	DevBuf count;
+	if(int rc = count.alloc(4)) return rc;
+	uint32_t nf = 0;
+	if(int rc = aa_detect(film_dev, weight_dev, resx, resy, *aa, threshold, flags_dev, nullptr, count.as<uint32_t>(), nf, n_sm, nullptr)) return rc;
+	if(n_flagged) *n_flagged = nf;
+	return GBRT_OK;
 }
 
 // Diagnostics: evaluates one sampling primitive on n inputs, on the device

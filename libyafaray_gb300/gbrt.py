@@ -68,6 +68,34 @@ class PtParams(ctypes.Structure):
 FILTERS = {"pixel": 0, "box": 1, "gauss": 2, "mitchell": 3, "lanczos": 4}
 
 
+class AaParams(ctypes.Structure):
+    _fields_ = [("passes", ctypes.c_int32), ("inc_samples", ctypes.c_int32), ("threshold", ctypes.c_float),
+                ("resampled_floor", ctypes.c_float), ("sample_multiplier_factor", ctypes.c_float),
+                ("light_sample_multiplier_factor", ctypes.c_float), ("indirect_sample_multiplier_factor", ctypes.c_float),
+                ("detect_color_noise", ctypes.c_int32), ("dark_detection_type", ctypes.c_int32),
+                ("dark_threshold_factor", ctypes.c_float), ("variance_edge_size", ctypes.c_int32),
+                ("variance_pixels", ctypes.c_int32)]
+
+
+# AaNoiseParams::DarkDetectionType names (include/common/aa_noise_params.h:30-37)
+DARK_DETECTION = {"none": 0, "linear": 1, "curve": 2}
+
+
+def aa_params(film):
+    """gbrt_aa_params from a film dict with the reference's ImageFilm
+    parameter names and defaults (include/render/imagefilm.h:212-225)."""
+    film = film or {}
+    return AaParams(int(film.get("AA_passes", 1)), int(film.get("AA_inc_samples", 1)),
+                    float(film.get("AA_threshold", 0.05)), float(film.get("AA_resampled_floor", 0.0)),
+                    float(film.get("AA_sample_multiplier_factor", 1.0)),
+                    float(film.get("AA_light_sample_multiplier_factor", 1.0)),
+                    float(film.get("AA_indirect_sample_multiplier_factor", 1.0)),
+                    int(bool(film.get("AA_detect_color_noise", False))),
+                    DARK_DETECTION[film.get("AA_dark_detection_type", "none")],
+                    float(film.get("AA_dark_threshold_factor", 0.0)), int(film.get("AA_variance_edge_size", 10)),
+                    int(film.get("AA_variance_pixels", 0)))
+
+
 class PmParams(ctypes.Structure):
     _fields_ = [("diffuse_photons", ctypes.c_int32), ("caustic_photons", ctypes.c_int32), ("diffuse_radius", ctypes.c_float),
                 ("diffuse_search", ctypes.c_int32), ("caustic_radius", ctypes.c_float), ("caustic_mix", ctypes.c_int32),
@@ -159,6 +187,12 @@ SIGNATURES = {
                             ctypes.POINTER(PtStats), _VP]),
     "gbrt_pt_render_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP,
                                  ctypes.POINTER(PtStats)]),
+    "gbrt_pt_render_aa": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), ctypes.POINTER(AaParams), _VP,
+                               ctypes.POINTER(PtStats), _VP, _VP]),
+    "gbrt_pt_render_aa_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), ctypes.POINTER(AaParams),
+                                    _VP, ctypes.POINTER(PtStats), _VP]),
+    "gbrt_aa_flags": (_I, [_VP, _VP, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(AaParams), ctypes.c_float, _VP,
+                           ctypes.POINTER(ctypes.c_uint32)]),
 }
 
 _lib = None
@@ -438,6 +472,38 @@ class Renderer:
         return img, {"camera_samples": st.camera_samples, "extension_rays": st.extension_rays,
                      "shadow_rays": st.shadow_rays, "ms": st.ms}
 
+    def render_aa(self, spp=None, base_offset=0, seed=1):
+        """Adaptive anti-aliasing render (TiledIntegrator::render's passes)
+        with the scene's "film" AA parameters: (mean image [resy, resx, 3],
+        stats dict, pixels rendered per pass).  spp: AA_minsamples."""
+        if self.kind != "pathtracing":
+            raise ValueError("adaptive AA passes are implemented for the path tracer")
+        film = self.scene.get("film", {})
+        spp = int(film.get("AA_minsamples", 1)) if spp is None else int(spp)
+        aa = aa_params(film)
+        cam = self.camera_desc()
+        p = self.params(spp, base_offset, seed)
+        img = np.empty((cam.resy, cam.resx, 3), np.float32)
+        res = np.zeros(max(1, aa.passes), np.uint32)
+        st = PtStats()
+        check(load().gbrt_pt_render_aa_host(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.byref(aa), _ptr(img),
+                                            ctypes.byref(st), _ptr(res)))
+        return img, {"camera_samples": st.camera_samples, "extension_rays": st.extension_rays,
+                     "shadow_rays": st.shadow_rays, "ms": st.ms}, res.tolist()
+
+    def render_aa_device(self, film_ptr, weight_ptr, spp=None, base_offset=0, seed=1, stream=0):
+        """Adaptive AA passes into a device film (float RGB sums) and its
+        filter weights; returns the pixels rendered per pass."""
+        film = self.scene.get("film", {})
+        spp = int(film.get("AA_minsamples", 1)) if spp is None else int(spp)
+        aa = aa_params(film)
+        cam = self.camera_desc()
+        p = self.params(spp, base_offset, seed, weight_ptr=weight_ptr)
+        res = np.zeros(max(1, aa.passes), np.uint32)
+        check(load().gbrt_pt_render_aa(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.byref(aa),
+                                       ctypes.c_void_p(film_ptr), None, _ptr(res), ctypes.c_void_p(stream)))
+        return res.tolist()
+
     def render_device(self, spp, film_ptr, film64_ptr=0, base_offset=0, seed=1, stream=0, stats=False, wave_paths=0,
                       guide=None, alpha=0.0, train_steps=0, batch=0, max_vertex=0, radiance_target=False, weight_ptr=0):
         """Adds sample sums into a device film (float or double RGB); with a
@@ -465,6 +531,15 @@ class Renderer:
                            radiance_photons=st.radiance_photons, photon_ms=st.photon_ms)
             return out
         return None
+
+
+def aa_flags(film_ptr, weight_ptr, resx, resy, aa, threshold, flags_ptr):
+    """ImageFilm::nextPass's resample flags of a device film (float RGB sums
+    and filter weights) into a device uint8 buffer; returns the flagged count."""
+    n = ctypes.c_uint32()
+    check(load().gbrt_aa_flags(ctypes.c_void_p(film_ptr), ctypes.c_void_p(weight_ptr), int(resx), int(resy),
+                               ctypes.byref(aa), float(threshold), ctypes.c_void_p(flags_ptr), ctypes.byref(n)))
+    return n.value
 
 
 def sampler_eval(kind, dim, inputs, on_device):

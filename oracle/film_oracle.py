@@ -15,7 +15,12 @@ Follows
     (include/math/math.h:116-127, 200-206);
   * the splat: ImageFilm::addSample (imagefilm.cc:771-822) with
     roundToIntWithBias (include/render/imagefilm.h:344-348);
-  * normalisation: Rgba::normalized (include/color/color.h:538-542).
+  * normalisation: Rgba::normalized (include/color/color.h:538-542);
+  * adaptive anti-aliasing: the resample flags of ImageFilm::nextPass
+    (imagefilm.cc:399-512) with Rgba::colorDifference / col2Bri / abscol2Bri
+    (color.h:57-58, 434-452) and darkThresholdCurveInterpolate
+    (imagefilm.cc:882-899); multipass sample positions (riVdC, riS of
+    pass offset + sample, integrator_tiled.cc:316-319; sample.h:99-114).
 
 The sampler functions are pinned bit for bit against the reference's own
 values in tests/golden/sampler.npz (made by the compiled reference).
@@ -49,14 +54,42 @@ def ri_lp(values, r=0):
     return np.clip((acc.astype(np.float64) * 2.0 ** -32).astype(F32), F32(0), F32(1))
 
 
+def ri_vdc(values, r=0):
+    """sample::riVdC: bit-reversed radical inverse xor r, float32."""
+    b = np.asarray(values, np.uint32).astype(np.uint64)
+    rev = np.zeros_like(b)
+    for k in range(32):
+        rev |= ((b >> np.uint64(k)) & np.uint64(1)) << np.uint64(31 - k)
+    v = (rev ^ np.asarray(r, np.uint64)).astype(np.float64) * 2.0 ** -32
+    return np.clip(v.astype(F32), F32(0), F32(1))
+
+
+def ri_s(values, r=0):
+    """sample::riS: Sobol second dimension xor r, float32."""
+    i = np.asarray(values, np.uint32).astype(np.uint64).copy()
+    acc = (np.zeros(i.shape, np.uint64) + np.asarray(r, np.uint64)).astype(np.uint64)
+    v = np.full(i.shape, 1 << 31, np.uint64)
+    while (i != 0).any():
+        acc = np.where(i & np.uint64(1), acc ^ v, acc)
+        i >>= np.uint64(1)
+        v ^= v >> np.uint64(1)
+    return np.clip((acc.astype(np.float64) * 2.0 ** -32).astype(F32), F32(0), F32(1))
+
+
 def pixel_offset(x, y):
     """fnv32ABuf(y * fnv32ABuf(x)) (integrator_tiled.cc:297; x = column j, y = row i)."""
     inner = fnv32a(np.asarray(x, np.uint32))
     return fnv32a((np.asarray(y, np.uint64) * inner.astype(np.uint64)).astype(np.uint32))
 
 
-def sample_positions(x, y, sample, n_samples):
-    """(dx, dy) of camera sample `sample` of n in pixel (x, y)."""
+def sample_positions(x, y, sample, n_samples, multipass=False, pass_offset=0):
+    """(dx, dy) of camera sample `sample` of n in pixel (x, y); with AA_passes
+    > 1 every pass takes riVdC / riS of sample_ = pass offset + sample,
+    scrambled by the pixel offset."""
+    if multipass:
+        off = pixel_offset(x, y)
+        s_ = (np.asarray(sample, np.uint64) + np.uint64(pass_offset)).astype(np.uint32)
+        return ri_vdc(s_, off), ri_s(s_, off)
     if n_samples <= 1:
         z = np.full(np.shape(sample), F32(0.5))
         return z, z.copy()
@@ -127,14 +160,21 @@ def _round_bias(v):
     return np.trunc(np.asarray(v, np.float64) + (0.5 - 1.4e-11)).astype(np.int64)
 
 
-def splat_weights(resx, resy, n_samples, kind, pixel_width=1.5):
-    """Weight image [resy, resx] (float64 sums) of every camera sample of every pixel."""
+def splat_weights(resx, resy, n_samples, kind, pixel_width=1.5, multipass=False, pass_offset=0, pixels=None):
+    """Weight image [resy, resx] (float64 sums) of every camera sample of
+    every pixel (or of the pixels y resx + x listed in `pixels`)."""
     table, width, scale = filter_table(kind, pixel_width)
-    ys, xs = np.mgrid[0:resy, 0:resx]
-    xs = np.repeat(xs.ravel(), n_samples)
-    ys = np.repeat(ys.ravel(), n_samples)
-    ss = np.tile(np.arange(n_samples), resx * resy)
-    dx, dy = sample_positions(xs, ys, ss, n_samples)
+    if pixels is None:
+        ys, xs = np.mgrid[0:resy, 0:resx]
+        xs, ys = xs.ravel(), ys.ravel()
+    else:
+        pixels = np.asarray(pixels, np.int64)
+        xs, ys = pixels % resx, pixels // resx
+    npx = len(xs)
+    xs = np.repeat(xs, n_samples)
+    ys = np.repeat(ys, n_samples)
+    ss = np.tile(np.arange(n_samples), npx)
+    dx, dy = sample_positions(xs, ys, ss, n_samples, multipass, pass_offset)
     dx = dx.astype(np.float64)
     dy = dy.astype(np.float64)
     dx0 = np.maximum(-xs, _round_bias(dx - width))
@@ -153,3 +193,97 @@ def splat_weights(resx, resy, n_samples, kind, pixel_width=1.5):
             w = table[np.minimum(yi[ok], TABLE - 1), np.minimum(xi[ok], TABLE - 1)].astype(np.float64)
             np.add.at(out, (ys[ok] + j, xs[ok] + i), w)
     return out
+
+
+# ---- adaptive anti-aliasing: ImageFilm::nextPass ----
+
+def _bri(r, g, b):
+    """Rgb::col2Bri in float32, unfused, left to right."""
+    return ((F32(0.2126) * r + F32(0.7152) * g).astype(F32) + (F32(0.0722) * b)).astype(F32)
+
+
+_CURVE_B = np.array([0.10, 0.20, 0.30, 0.40, 0.50, 0.60, 0.70, 0.80, 0.90, 1.00, 1.20, 1.40, 1.80], F32)
+_CURVE_T = np.array([0.0001, 0.0010, 0.0020, 0.0035, 0.0055, 0.0075, 0.0100, 0.0150, 0.0250, 0.0400, 0.0800,
+                     0.0950, 0.1000], F32)
+_CURVE_W = np.array([0.0, 0.10, 0.10, 0.10, 0.10, 0.10, 0.10, 0.10, 0.10, 0.10, 0.20, 0.20, 0.40], F32)
+
+
+def dark_curve(b):
+    """darkThresholdCurveInterpolate: piecewise linear in brightness, float32."""
+    b = np.asarray(b, F32)
+    out = np.full(b.shape, _CURVE_T[-1], F32)
+    done = np.zeros(b.shape, bool)
+    m = b <= _CURVE_B[0]
+    out[m] = _CURVE_T[0]
+    done |= m
+    for k in range(1, len(_CURVE_B)):
+        m = ~done & (b <= _CURVE_B[k])
+        dt = F32(_CURVE_T[k] - _CURVE_T[k - 1])
+        seg = (((b - _CURVE_B[k - 1]).astype(F32) * dt).astype(F32) / _CURVE_W[k]).astype(F32)
+        out[m] = (_CURVE_T[k - 1] + seg[m]).astype(F32)
+        done |= m
+    return out
+
+
+def normalized(sums, weights):
+    """Rgba::normalized of film sums [H, W, 4] (rgba) by weights [H, W]: x (1 / w), 0 where w is 0."""
+    w = np.asarray(weights, F32)
+    nz = w != F32(0)
+    inv = np.where(nz, F32(1) / np.where(nz, w, F32(1)), F32(0)).astype(F32)
+    return (np.asarray(sums, F32) * inv[..., None]).astype(F32) * nz[..., None]
+
+
+def aa_flags(sums, weights, threshold, detect_color_noise=False, dark_detection="none", dark_threshold_factor=0.0,
+             variance_edge_size=10, variance_pixels=0):
+    """Resample flags [H, W] of one ImageFilm::nextPass with threshold > 0.
+
+    sums: combined-layer sums [H, W, 4] (rgba; with opaque samples a = the
+    weight sum), weights: filter weights [H, W]."""
+    w = np.asarray(weights, F32)
+    H, W = w.shape
+    c = normalized(sums, w)
+    flags = ~(w > F32(0))
+    if W < 2 or H < 2:
+        return flags
+    thr0 = F32(threshold)
+    core = c[:H - 1, :W - 1]
+    bri_abs = _bri(np.abs(core[..., 0]), np.abs(core[..., 1]), np.abs(core[..., 2]))
+    if dark_detection == "linear" and dark_threshold_factor > 0:
+        f = F32(dark_threshold_factor)
+        thr = (thr0 * ((F32(1) - f) + (bri_abs * f).astype(F32)).astype(F32)).astype(F32)
+    elif dark_detection == "curve":
+        thr = dark_curve(bri_abs)
+    else:
+        thr = np.full((H - 1, W - 1), thr0, F32)
+    bri = _bri(c[..., 0], c[..., 1], c[..., 2])
+
+    def diff(a_yx, b_yx):
+        d = np.abs((bri[b_yx] - bri[a_yx]).astype(F32))
+        if detect_color_noise:
+            for ch in range(4):
+                d = np.maximum(d, np.abs((c[b_yx][..., ch] - c[a_yx][..., ch]).astype(F32)))
+        return d
+
+    ys, xs = np.mgrid[0:H - 1, 0:W - 1]
+    here = (ys, xs)
+    for dy, dx in ((0, 1), (1, 0), (1, 1), (1, -1)):
+        ny, nx = ys + dy, xs + dx
+        ok = nx >= 0
+        nxc = np.maximum(nx, 0)
+        m = ok & (diff(here, (ny, nxc)) >= thr)
+        flags[ys[m], xs[m]] = True
+        flags[ny[m], nxc[m]] = True
+    if variance_pixels > 0:
+        h = variance_edge_size // 2
+        vx = np.zeros((H - 1, W - 1), np.int64)
+        vy = np.zeros((H - 1, W - 1), np.int64)
+        for d in range(-h, h - 1):
+            xi = np.clip(xs + d, 0, W - 2)
+            vx += diff((ys, xi), (ys, xi + 1)) >= thr
+            yi = np.clip(ys + d, 0, H - 2)
+            vy += diff((yi, xs), (yi + 1, xs)) >= thr
+        m = (vx + vy) >= variance_pixels
+        for ddx in range(-h, h):
+            for ddy in range(-h, h):
+                flags[np.clip(ys[m] + ddy, 0, H - 1), np.clip(xs[m] + ddx, 0, W - 1)] = True
+    return flags

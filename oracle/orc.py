@@ -128,7 +128,7 @@ def run_reference_kdtree(verts, faces, rays, mode=0, accel="yafaray-kdtree-origi
 REF_RENDER = os.path.join(HERE, "_ref", "render_dump")
 
 
-def reference_scene_text(scene, spp, batches, threads=-1):
+def reference_scene_text(scene, spp, batches, threads=-1, offset_stride=None):
     """Scene dict (libyafaray_gb300.scenes) -> render_dump input text."""
     out = []
     for name, m in scene["materials"].items():
@@ -181,8 +181,39 @@ def reference_scene_text(scene, spp, batches, threads=-1):
     film = scene.get("film")
     if film:
         out.append(f"film {film['filter_type']} {float(film.get('AA_pixelwidth', 1.5))!r}")
-    out.append(f"render {spp} {batches} {threads}")
+        aa = {k: v for k, v in film.items() if k.startswith("AA_") and k not in ("AA_pixelwidth", "AA_minsamples")}
+        if aa:
+            def fmt(v):
+                return str(v).lower() if isinstance(v, (bool, str)) else repr(v)
+            out.append("aa " + " ".join(f"{k}={fmt(v)}" for k, v in aa.items()))
+    out.append(f"render {spp} {batches} {threads}" + (f" {int(offset_stride)}" if offset_stride is not None else ""))
     return "\n".join(out) + "\n"
+
+
+def run_reference_aa(scene, spp, batches, offset_stride, threads=-1):
+    """Adaptive-AA renders with the compiled reference (the scene's "film"
+    AA_* entries): (rgb [K,H,W,3], seconds per batch, passes of batch 0 =
+    [{pass, threshold, sums [H,W,4], weights [H,W], flagged (y W + x)}])."""
+    text = reference_scene_text(scene, spp, batches, threads, offset_stride)
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout, faa = os.path.join(d, "scene.txt"), os.path.join(d, "out.bin"), os.path.join(d, "aa.bin")
+        open(fin, "w").write(text)
+        subprocess.run([REF_RENDER, fin, fout, faa], check=True, stdout=subprocess.DEVNULL)
+        raw = open(fout, "rb").read()
+        rawa = open(faa, "rb").read()
+    K, H, W = struct.unpack("<iii", raw[:12])
+    secs = np.frombuffer(raw[12:12 + 8 * K], np.float64).copy()
+    rgb = np.frombuffer(raw[12 + 8 * K:], np.float32).reshape(K, H, W, 3).copy()
+    passes = []
+    n_pass = struct.unpack("<i", rawa[:4])[0]
+    o = 4
+    for _ in range(n_pass):
+        pno, thr, n = struct.unpack("<ifi", rawa[o:o + 12]); o += 12
+        sums = np.frombuffer(rawa, np.float32, 4 * H * W, o).reshape(H, W, 4).copy(); o += 16 * H * W
+        w = np.frombuffer(rawa, np.float32, H * W, o).reshape(H, W).copy(); o += 4 * H * W
+        fl = np.frombuffer(rawa, np.int32, n, o).copy(); o += 4 * n
+        passes.append({"pass": pno, "threshold": thr, "sums": sums, "weights": w, "flagged": fl})
+    return rgb, secs, passes
 
 
 def run_reference_render(scene, spp, batches, threads=-1):

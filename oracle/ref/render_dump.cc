@@ -19,13 +19,20 @@
 //   pointlight X Y Z  R G B  POWER
 //   camera FX FY FZ  TX TY TZ  UX UY UZ  RESX RESY FOCAL
 //   integrator TYPE key=value ...      (ints/floats/bools/strings by key)
-//   render SPP BATCHES THREADS
+//   film FILTER_TYPE PIXEL_WIDTH
+//   aa key=value ...                   (ImageFilm AA_* parameters: adaptive passes)
+//   render SPP BATCHES THREADS [OFFSET_STRIDE]   (batch k: adv_base_sampling_offset k x stride, default SPP)
 // Output (binary): i32 K, H, W; f64 seconds[K]; f32 rgb[K][H][W][3]
-// Optional third argument (photonmapping only): after the first batch's
-// preprocess, the diffuse and caustic photon maps are written there:
+// Optional third argument: with photonmapping, the diffuse and caustic photon
+// maps after the first batch's preprocess:
 //   per map: i32 n_photons, i32 n_paths, f32 [n][9] (dir xyz, pos xyz, col rgb)
 // (the maps are private members of PhotonIntegrator, read by opening their
-// access for this file only).
+// access for this file only); with an "aa" line, the first batch's adaptive
+// passes instead, one record per ImageFilm::nextPass that flagged pixels:
+//   i32 pass, f32 threshold, i32 n_flagged, f32 sums[H][W][4] (combined layer
+//   before normalisation), f32 weights[H][W], i32 flagged[n] (y W + x)
+// read at the pass's first highlight-pixel callback, i.e. the film state the
+// detection ran on.
 #include "yafaray_c_api.h"
 #include <algorithm>
 #include <atomic>
@@ -45,6 +52,8 @@
 #define private public
 #define protected public
 #include "integrator/surface/integrator_photon_mapping.h"
+#include "render/imagefilm.h"
+#include "image/image_layers.h"
 #undef private
 #undef protected
 
@@ -58,6 +67,41 @@ void putPixel(const char *layer, int x, int y, float r, float g, float b, float 
 	if(std::strcmp(layer, "combined") != 0 || x < 0 || y < 0 || x >= f->w || y >= f->h) return;
 	float *p = &f->rgb[3ull * (static_cast<size_t>(y) * f->w + x)];
 	p[0] = r; p[1] = g; p[2] = b;
+}
+
+// Adaptive-pass records of one film (see the header).
+struct AaDump {
+	const yafaray::ImageFilm *film = nullptr;
+	bool on = false;
+	struct Pass { int pass; float thr; std::vector<float> sums, w; std::vector<int> flagged; };
+	std::vector<Pass> passes;
+};
+
+void highlightPixel(int x, int y, float, float, float, float, void *data)
+{
+	auto *d = static_cast<AaDump *>(data);
+	if(!d->on) return;
+	const yafaray::ImageFilm *f = d->film;
+	const int W = f->params_.width_, H = f->params_.height_;
+	if(d->passes.empty() || d->passes.back().pass != f->n_pass_)
+	{
+		AaDump::Pass p;
+		p.pass = f->n_pass_;
+		p.thr = f->getAaThresholdCalculated();
+		const auto &img = f->film_image_layers_(yafaray::LayerDef::Combined).image_;
+		p.sums.resize(4ull * W * H);
+		p.w.resize(1ull * W * H);
+		for(int yy = 0; yy < H; ++yy)
+			for(int xx = 0; xx < W; ++xx)
+			{
+				const yafaray::Rgba c = img->getColor({{xx, yy}});
+				float *q = &p.sums[4ull * (static_cast<size_t>(yy) * W + xx)];
+				q[0] = c.r_; q[1] = c.g_; q[2] = c.b_; q[3] = c.a_;
+				p.w[static_cast<size_t>(yy) * W + xx] = f->getWeight({{xx, yy}});
+			}
+		d->passes.push_back(std::move(p));
+	}
+	d->passes.back().flagged.push_back(y * W + x);
 }
 
 void setTyped(yafaray_ParamMap *pm, const std::string &key, const std::string &val)
@@ -86,6 +130,8 @@ int main(int argc, char **argv)
 	int resx = 0, resy = 0, spp = 1, batches = 1, threads = -1;
 	std::string filter_type = "box";
 	float pixel_width = 1.f;
+	int offset_stride = -1;
+	std::vector<std::pair<std::string, std::string>> aa_kv;
 	std::string line;
 	while(std::getline(in, line))
 	{
@@ -212,8 +258,17 @@ int main(int argc, char **argv)
 			}
 			integrator = yafaray_createSurfaceIntegrator(logger, "integrator", pm);
 		}
-		else if(kw == "render") ss >> spp >> batches >> threads;
+		else if(kw == "render") { ss >> spp >> batches >> threads; if(!(ss >> offset_stride)) offset_stride = -1; }
 		else if(kw == "film") ss >> filter_type >> pixel_width;
+		else if(kw == "aa")
+		{
+			std::string kv;
+			while(ss >> kv)
+			{
+				const auto eq = kv.find('=');
+				if(eq != std::string::npos) aa_kv.emplace_back(kv.substr(0, eq), kv.substr(eq + 1));
+			}
+		}
 	}
 	if(!integrator || resx <= 0 || resy <= 0) { fprintf(stderr, "scene lacks integrator or camera\n"); return 2; }
 	yafaray_clearParamMap(pm);
@@ -222,6 +277,7 @@ int main(int argc, char **argv)
 
 	std::vector<double> secs;
 	std::vector<float> all;
+	AaDump aa;
 	for(int k = 0; k < batches; ++k)
 	{
 		yafaray_clearParamMap(pm);
@@ -232,11 +288,15 @@ int main(int argc, char **argv)
 		yafaray_setParamMapInt(pm, "AA_minsamples", spp);
 		yafaray_setParamMapString(pm, "filter_type", filter_type.c_str());
 		yafaray_setParamMapFloat(pm, "AA_pixelwidth", pixel_width);
-		yafaray_setParamMapInt(pm, "adv_base_sampling_offset", k * spp);
+		yafaray_setParamMapInt(pm, "adv_base_sampling_offset", k * (offset_stride >= 0 ? offset_stride : spp));
+		for(const auto &kv : aa_kv) setTyped(pm, kv.first, kv.second);
 		yafaray_Film *film = yafaray_createFilm(logger, integrator, "film", pm);
 		yafaray_defineCamera(film, camera);
 		Film f; f.w = resx; f.h = resy; f.rgb.assign(3ull * resx * resy, 0.f);
 		yafaray_setPutPixelCallback(film, putPixel, &f);
+		aa.film = reinterpret_cast<const yafaray::ImageFilm *>(film);
+		aa.on = k == 0 && !aa_kv.empty();
+		yafaray_setHighlightPixelCallback(film, highlightPixel, &aa);
 		yafaray_RenderControl *rc = yafaray_createRenderControl();
 		yafaray_RenderMonitor *rm = yafaray_createRenderMonitor(nullptr, nullptr, YAFARAY_DISPLAY_CONSOLE_HIDDEN);
 		yafaray_setRenderControlForNormalStart(rc);
@@ -244,7 +304,7 @@ int main(int argc, char **argv)
 		const auto t0 = std::chrono::steady_clock::now();
 		yafaray_preprocessScene(scene, rc, flags);
 		yafaray_preprocessSurfaceIntegrator(rm, integrator, rc, scene);
-		if(k == 0 && argc > 3)
+		if(k == 0 && argc > 3 && aa_kv.empty())
 		{
 			auto *pmi = dynamic_cast<yafaray::PhotonIntegrator *>(reinterpret_cast<yafaray::SurfaceIntegrator *>(integrator));
 			if(!pmi) { fprintf(stderr, "photon dump needs the photonmapping integrator\n"); return 2; }
@@ -270,6 +330,22 @@ int main(int argc, char **argv)
 		yafaray_destroyRenderMonitor(rm);
 		yafaray_destroyRenderControl(rc);
 		yafaray_destroyFilm(film);
+	}
+	if(argc > 3 && !aa_kv.empty())
+	{
+		FILE *fa = fopen(argv[3], "wb");
+		if(!fa) { perror("aa"); return 2; }
+		const int np = static_cast<int>(aa.passes.size());
+		fwrite(&np, 4, 1, fa);
+		for(const auto &p : aa.passes)
+		{
+			const int n = static_cast<int>(p.flagged.size());
+			fwrite(&p.pass, 4, 1, fa); fwrite(&p.thr, 4, 1, fa); fwrite(&n, 4, 1, fa);
+			fwrite(p.sums.data(), 4, p.sums.size(), fa);
+			fwrite(p.w.data(), 4, p.w.size(), fa);
+			fwrite(p.flagged.data(), 4, p.flagged.size(), fa);
+		}
+		fclose(fa);
 	}
 	FILE *fo = fopen(argv[2], "wb");
 	if(!fo) { perror("out"); return 2; }

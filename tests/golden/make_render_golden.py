@@ -115,6 +115,64 @@ def film_golden(spp=16, batches=32):
     print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
 
 
+# Adaptive-AA cases: (resx, resy, focal scale, AA_minsamples, film AA_* entries)
+AA_CASES = [
+    (40, 30, 1.0, 16, dict(AA_threshold=0.15)),
+    (40, 30, 1.0, 16, dict(AA_threshold=0.2, AA_variance_pixels=4, AA_variance_edge_size=6, AA_detect_color_noise=True)),
+    (40, 30, 1.0, 16, dict(AA_threshold=0.12, AA_dark_detection_type="linear", AA_dark_threshold_factor=0.6,
+                           AA_resampled_floor=60.0)),
+    (40, 30, 1.0, 16, dict(AA_threshold=0.2, AA_resampled_floor=50.0, AA_sample_multiplier_factor=1.5,
+                           AA_light_sample_multiplier_factor=2.0)),
+    (24, 18, 6.0, 1024, dict(AA_threshold=0.05, AA_dark_detection_type="curve", AA_inc_samples=64)),
+]
+AA_RENDER = dict(AA_passes=4, AA_inc_samples=4, AA_threshold=0.2, AA_resampled_floor=50.0,
+                 AA_sample_multiplier_factor=1.5, AA_light_sample_multiplier_factor=2.0)
+
+
+def aa_scene(resx, resy, focal_scale, aa):
+    sc = scenes.cornell_scene(res=resx)
+    sc["camera"]["resy"] = resy
+    sc["camera"]["focal"] = sc["camera"]["focal"] * focal_scale
+    sc["film"] = {"filter_type": "gauss", "AA_pixelwidth": 1.5, "AA_passes": 3, "AA_inc_samples": 4, **aa}
+    return sc
+
+
+def aa_golden(batches=24, stride=4096):
+    """aa_flags.npz: the film state (combined sums, weights, threshold) of the
+    reference's adaptive passes and the pixels ImageFilm::nextPass flagged on
+    it, for every AA_CASES entry (first two detections each).
+    cornell_aa_48x36_render.npz: Cornell 48x36, gauss film, AA_RENDER passes
+    from 16 samples, `batches` renders at adv_base_sampling_offset k x stride:
+    mean, standard error and the pixels flagged per detection of batch 0."""
+    import json
+    out = {}
+    for i, (rx, ry, fs, spp, aa) in enumerate(AA_CASES):
+        sc = aa_scene(rx, ry, fs, aa)
+        _, _, passes = orc.run_reference_aa(sc, spp, 1, stride, threads=os.cpu_count() or 1)
+        out[f"c{i}_film"] = np.array(json.dumps(sc["film"]))
+        for j, p in enumerate(passes[:2]):
+            # opaque samples: the alpha sum is the weight sum
+            assert np.array_equal(p["sums"][..., 3], p["weights"])
+            mask = np.zeros(rx * ry, bool)
+            mask[p["flagged"]] = True
+            out[f"c{i}_p{j}_sums"] = p["sums"][..., :3].copy()
+            out[f"c{i}_p{j}_weights"] = p["weights"]
+            out[f"c{i}_p{j}_threshold"] = np.float32(p["threshold"])
+            out[f"c{i}_p{j}_flags"] = np.packbits(mask)
+        print(f"aa case {i}: flagged {[len(p['flagged']) for p in passes]}")
+    np.savez_compressed(os.path.join(OUT, "aa_flags.npz"), n_cases=np.int32(len(AA_CASES)), **out)
+    sc = aa_scene(48, 36, 1.0, AA_RENDER)
+    rgb, secs, passes = orc.run_reference_aa(sc, 16, batches, stride, threads=os.cpu_count() or 1)
+    mean = rgb.mean(0)
+    se = rgb.std(0, ddof=1) / np.sqrt(batches)
+    np.savez_compressed(os.path.join(OUT, "cornell_aa_48x36_render.npz"), mean=mean.astype(np.float32),
+                        se=se.astype(np.float32), batches=np.int32(batches), spp=np.int32(16), stride=np.int32(stride),
+                        film=np.array(json.dumps(sc["film"])), seconds=secs,
+                        flagged=np.array([len(p["flagged"]) for p in passes], np.int32))
+    print(f"cornell_aa_48x36_render.npz: mean {mean.mean(axis=(0, 1))}, flagged {[len(p['flagged']) for p in passes]}, "
+          f"{secs.sum():.1f} s of reference rendering")
+
+
 def variant_golden(name, res=64, spp=16, batches=32, **kw):
     """Cornell variants: glass (glass + rough-glass spheres, the recursive
     split) and point (a pointlight instead of the area light)."""
@@ -235,5 +293,7 @@ if __name__ == "__main__":
         film_golden()
     if "cornell_shiny" in what:
         variant_golden("cornell_shiny_64_render.npz", shiny=True)
+    if "aa" in what:
+        aa_golden()
     if "cornell_point" in what:
         variant_golden("cornell_point_64_render.npz", point_light=True)
