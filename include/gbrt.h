@@ -199,9 +199,9 @@ enum {
 	GBRT_MAT_GLOSSY = 2,         /* "glossy": color (glossy colour), color2 (diffuse_color), params =
 	                                {exponent, glossy_reflect, diffuse_reflect, as_diffuse (1)} */
 	GBRT_MAT_ROUGH_GLASS = 3,    /* "rough_glass": color (filter_color), color2 (mirror_color), params =
-	                                {IOR (0 -> 1.4), transmit_filter, alpha (0 -> 0.5)} */
+	                                {IOR (0 -> 1.4), transmit_filter, alpha (0 -> 0.5), fake_shadows (0/1)} */
 	GBRT_MAT_GLASS = 4           /* "glass": color (filter_color), color2 (mirror_color), params =
-	                                {IOR (0 -> 1.4), transmit_filter} */
+	                                {IOR (0 -> 1.4), transmit_filter, -, fake_shadows (0/1)} */
 };
 /* Every material: params[5] = additionaldepth (extra recursive ray levels). */
 enum { GBRT_LIGHT_AREA = 0, GBRT_LIGHT_POINT = 1 };   /* "pointlight": corner = from, color, power */
@@ -266,6 +266,14 @@ typedef struct gbrt_pt_params {
 	uint32_t filter_type;
 	float aa_pixel_width;       /* 0 = 1.5 (the reference's default) */
 	float *film_weight_dev;
+	/* Transparent shadows (MonteCarloIntegrator "transpShad", "shadowDepth";
+	 * Accelerator::isShadowedTransparentShadow, accelerator.h:113-169): shadow
+	 * rays pass transparent materials (shinydiffuse with transparency, glass /
+	 * rough_glass with fake_shadows) times their filter colour; more than
+	 * shadow_depth of them block.  shadow_depth is used as given (the
+	 * reference's default is 4). */
+	int32_t transparent_shadows;
+	int32_t shadow_depth;
 } gbrt_pt_params;
 
 /* Adaptive anti-aliasing (ImageFilm / TiledIntegrator parameters with the

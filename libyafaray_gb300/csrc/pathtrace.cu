@@ -32,6 +32,7 @@
 #include <atomic>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <functional>
 #include <mutex>
 #include <vector>
@@ -58,7 +59,7 @@ struct DevMaterial {
 	uint32_t as_diffuse, with_diffuse, double_sided, addl_depth;
 	float ior, a2;     // glass, rough_glass: IOR; shinydiffuse: IOR^2; rough_glass: GGX alpha^2
 	uint32_t sd;       // shinydiffuse components present (SD_*)
-	float pad;
+	uint32_t transparent;   // Material::isTransparent: shinydiffuse with a transparency layer, glass / rough_glass with fake_shadows
 	float sdc[4];      // shinydiffuse component strengths: mirror, transparency, translucency, diffuse
 	float tcol[3];     // shinydiffuse: transmit_filter x colour + (1 - transmit_filter)
 	float ecol[3];     // shinydiffuse: emit x colour
@@ -127,6 +128,10 @@ struct Params {
 	int aa_multipass;          // AA_passes > 1: sample positions (riVdC, riS)
 	const uint32_t *pix_list;  // pixels of this pass (resampled ones), or NULL for all
 	uint32_t n_list;
+	// transparent shadows (MonteCarloIntegrator "transpShad", "shadowDepth")
+	int tshadow, shadow_depth;
+	const DevMaterial *mats;
+	const float4 *prim_ng;
 };
 
 struct Work {
@@ -448,10 +453,12 @@ __device__ __forceinline__ bool glass_sample(const Surface &s, const float wo[3]
 		float kr, kt;
 		vec_fresnel(wo, n, m.ior, kr, kt);
 		const float p_kr = 0.01f + 0.99f * kr, p_kt = 0.01f + 0.99f * kt;
-		if(s1 < p_kt && (req & (BF_SPECULAR | BF_TRANSMIT)))
+		// transmit_flags_: Filter | Transmit with fake_shadows (material_glass.cc:147, 244-248)
+		const uint32_t tflags = m.transparent ? (BF_FILTER | BF_TRANSMIT) : (BF_SPECULAR | BF_TRANSMIT);
+		if(s1 < p_kt && (req & tflags))
 		{
 			for(int k = 0; k < 3; ++k) { wi[k] = refdir[k]; col[k] = m.col[k]; }
-			pdf = p_kt; w = 1.f; sampled = BF_SPECULAR | BF_TRANSMIT;
+			pdf = p_kt; w = 1.f; sampled = tflags;
 			return true;
 		}
 		if(req & (BF_SPECULAR | BF_REFLECT))
@@ -1816,16 +1823,79 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 	}
 }
 
+// Material::getTransparency of a shadow-ray hit, wo = the shadow ray's
+// direction, n = the flat normal face-forwarded (SurfacePoint::
+// normalFaceForward): ShinyDiffuseMaterial (material_shiny_diffuse.cc:541-563:
+// accum = 1 - kr x specular_reflect with a mirror layer, then
+// accum *= transparency x accum, times the transmit colour) and Glass /
+// RoughGlass (material_glass.cc:297-303, material_rough_glass.cc:349-355:
+// kt x filter colour).
+__device__ __forceinline__ void mat_transparency(const DevMaterial &m, const float ng[3], const float wo[3], float out[3])
+{
+	const bool flip = dot3(ng, wo) < 0.f;
+	const float n[3] = {flip ? -ng[0] : ng[0], flip ? -ng[1] : ng[1], flip ? -ng[2] : ng[2]};
+	if(m.type == GBRT_MAT_SHINYDIFFUSE)
+	{
+		const float kr = shiny_kr(m, wo, n);
+		float accum = 1.f;
+		if(m.sd & SD_MIRROR) accum = 1.f - kr * m.sdc[0];
+		accum *= m.sdc[1] * accum;
+		for(int k = 0; k < 3; ++k) out[k] = accum * m.tcol[k];
+	}
+	else
+	{
+		float kr, kt;
+		vec_fresnel(wo, n, m.ior, kr, kt);
+		for(int k = 0; k < 3; ++k) out[k] = kt * m.col[k];
+	}
+}
+
+// Accelerator::primitiveIntersectionTransparentShadow (accelerator.h:147-169):
+// an opaque material blocks; a transparent one multiplies the shadow colour
+// by its transparency, until more than shadowDepth transparent surfaces lie
+// on the ray (then it blocks too).
+struct TransparentHits {
+	static constexpr bool kTransparent = true;
+	const DevMaterial *mats;
+	const float4 *prim_ng;
+	int max_depth;
+	int depth;
+	float col[3];
+	__device__ __forceinline__ void reset() { depth = 0; col[0] = col[1] = col[2] = 1.f; }
+	__device__ __forceinline__ bool blocks(int32_t prim, float, const float *dir)
+	{
+		const float4 g = __ldg(prim_ng + prim);
+		const DevMaterial &m = mats[__float_as_uint(g.w)];
+		if(!m.transparent || depth >= max_depth) return true;
+		const float ng[3] = {g.x, g.y, g.z};
+		float tr[3];
+		mat_transparency(m, ng, dir, tr);
+		for(int k = 0; k < 3; ++k) col[k] *= tr[k];
+		++depth;
+		return false;
+	}
+};
+
 // kFilm: the film has a filter (film_splat); the plain-sum variant keeps
-// the splat's registers out of this kernel.
-template <bool kFilm>
+// the splat's registers out of this kernel.  kTransparent: transparent
+// shadows (the unoccluded colour times the filter colour of the transparent
+// surfaces passed).
+template <bool kFilm, bool kTransparent>
 __global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Params P, Work W, uint32_t shadow_cap, float *film, double *film64)
 {
 	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
 	const uint32_t n = min(W.count[2], shadow_cap);
 	uint32_t traced = 0;
-	gbrt::trace_persistent<true>(
-		bv, n, W.count + 5, stack + threadIdx.x, kThreads,
+	using Filter = typename std::conditional<kTransparent, TransparentHits, gbrt::OpaqueHits>::type;
+	Filter f;
+	if constexpr(kTransparent)
+	{
+		f.mats = P.mats;
+		f.prim_ng = P.prim_ng;
+		f.max_depth = P.shadow_depth;
+	}
+	gbrt::trace_persistent_filtered<true>(
+		bv, n, W.count + 5, stack + threadIdx.x, kThreads, f,
 		[&](uint32_t i, float r[8]) {
 			if(W.s_pix[i] == kDead) return false;
 			const float4 a = W.s_ray[2ull * i], b = W.s_ray[2ull * i + 1];
@@ -1836,7 +1906,8 @@ __global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Params P,
 		[&](uint32_t i, const gbrt::Hit &h) {
 			if(h.prim < 0)
 			{
-				const float4 c = W.s_col[i];
+				float4 c = W.s_col[i];
+				if constexpr(kTransparent) { c.x *= f.col[0]; c.y *= f.col[1]; c.z *= f.col[2]; }
 				if(kFilm) film_splat(P, film, film64, W.s_pix[i], W.p_si[W.s_path[i]], c.x, c.y, c.z, false);
 				else film_add(film, film64, W.s_pix[i], c.x, c.y, c.z);
 				if(W.p_sum) path_sum_add(W, W.s_path[i], c.x, c.y, c.z);
@@ -2986,6 +3057,7 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 			if(transparency * acc > 0.00001f)
 			{
 				d.sd |= SD_TRANSPARENT;
+				d.transparent = 1u;
 				acc *= 1.f - transparency;
 				d.flags |= BF_TRANSMIT | BF_FILTER;
 			}
@@ -3049,6 +3121,13 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 				const float a = std::max(1e-4f, std::min(alpha * 0.5f, 1.f));
 				d.a2 = a * a;
 				d.flags = BF_GLOSSY | BF_REFLECT | BF_TRANSMIT;
+			}
+			// fake_shadows: transparent to shadow rays, Filter in the BSDF flags
+			// (material_glass.cc:146, material_rough_glass.cc:148)
+			if(m.params[3] > 0.5f)
+			{
+				d.transparent = 1u;
+				d.flags |= BF_FILTER;
 			}
 		}
 		else return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_create: material %u has unsupported type %u", i, m.type);
@@ -3294,6 +3373,10 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	P.aa_multipass = aa ? aa->multipass : 0;
 	P.pix_list = aa ? aa->list : nullptr;
 	P.n_list = aa ? aa->n_list : 0u;
+	P.tshadow = pp.transparent_shadows ? 1 : 0;
+	P.shadow_depth = pp.shadow_depth;
+	P.mats = S->mats;
+	P.prim_ng = S->prim_ng;
 	if(pp.filter_type != GBRT_FILTER_PIXEL)
 	{
 		if(!pp.film_weight_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: filter type %u needs film_weight_dev", pp.filter_type);
@@ -3348,12 +3431,15 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 			if(level_guided)
 				if(int rc = gbrt_guide_eval_queue(guide, Ww.hitpos, n, Ww.count + cur, Ww.lobes, s)) return rc;
 			k_shade<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, camera->resx, static_cast<uint32_t>(shadow_cap), film, film64_dev);
-			if(Pw.film_w)
-				k_shadow<true><<<persistent_grid(k_shadow<true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, static_cast<uint32_t>(shadow_cap),
-				                                                                                         film, film64_dev);
+			const uint32_t scap = static_cast<uint32_t>(shadow_cap);
+			if(Pw.film_w && Pw.tshadow)
+				k_shadow<true, true><<<persistent_grid(k_shadow<true, true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, scap, film, film64_dev);
+			else if(Pw.film_w)
+				k_shadow<true, false><<<persistent_grid(k_shadow<true, false>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, scap, film, film64_dev);
+			else if(Pw.tshadow)
+				k_shadow<false, true><<<persistent_grid(k_shadow<false, true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, scap, film, film64_dev);
 			else
-				k_shadow<false><<<persistent_grid(k_shadow<false>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, static_cast<uint32_t>(shadow_cap),
-				                                                                                           film, film64_dev);
+				k_shadow<false, false><<<persistent_grid(k_shadow<false, false>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, scap, film, film64_dev);
 			cur ^= 1;
 		}
 		return GBRT_OK;

@@ -214,12 +214,26 @@ struct TraceState {
 	int sp;
 };
 
+// Hit filters of the shadow walk.  OpaqueHits: every hit in range blocks
+// (Accelerator::isShadowed).  A transparent-shadow filter
+// (isShadowedTransparentShadow, accelerator.h:113-120, 147-169) decides per
+// hit: blocks(prim, t, dir) true ends the walk as occluded, false lets the
+// ray pass (the filter keeps what it needs, e.g. the filter colour).  Its
+// kTransparent = true also selects the transparent walk's t_min,
+// max(tmin, bias) (accelerator_kdtree_common.h:139).  The hierarchy holds
+// every primitive once, so each is offered to the filter at most once.
+struct OpaqueHits {
+	static constexpr bool kTransparent = false;
+	__device__ __forceinline__ void reset() {}
+	__device__ __forceinline__ bool blocks(int32_t, float, const float *) { return true; }
+};
+
 // Ray set-up.  Closest hit follows Accelerator::intersect(ray, camera)
 // (accelerator.h:89-101); shadow follows Accelerator::isShadowed
 // (accelerator.h:103-111): origin advanced by tmin, t_max = tmax - 2 tmin,
-// bias-only t_min.  Returns false when the ray misses the tree bound (no
-// traversal).
-template <bool kShadow>
+// bias-only t_min (max(tmin, bias) for transparent shadows).  Returns false
+// when the ray misses the tree bound (no traversal).
+template <bool kShadow, bool kTransparent = false>
 __device__ __forceinline__ bool trace_init(TraceState &S, const BvhView &bv, float ox, float oy, float oz, float tmin, float dx, float dy,
                                            float dz, float tmax)
 {
@@ -241,7 +255,7 @@ __device__ __forceinline__ bool trace_init(TraceState &S, const BvhView &bv, flo
 	if(bv.n_prims == 0 || !bound_cross(bnd, S.from, S.dir, S.t_max, enter, leave)) return false;
 	// accelerator_kdtree_common.h:139, accelerator.h:64
 	const float bias = xm(0.1f * 0.00005f, fabsf(xs(leave, enter)));
-	S.t_min = kShadow ? bias : fmaxf(tmin, bias);
+	S.t_min = (kShadow && !kTransparent) ? bias : fmaxf(tmin, bias);
 	// A zero (or denormal) direction component would make 1/d infinite and
 	// the node planes' t values infinite or NaN, which the min / max chains
 	// ignore: that axis would stop culling and the ray would walk most of
@@ -264,10 +278,10 @@ __device__ __forceinline__ bool trace_init(TraceState &S, const BvhView &bv, flo
 // child of the current group by octant order (pushing the rest of the
 // group), test the opened node's primitive hits, pop when the group is
 // spent.  `sh` is this thread's column of a shared [kStackShared][stride]
-// uint2 array, `spill` a local array of kTraceStack - kStackShared entries.
-// Returns true when the query is answered.
-template <bool kShadow>
-__device__ __forceinline__ bool trace_step(TraceState &S, const BvhView &bv, uint2 *sh, int stride, uint2 *spill)
+// uint2 array, `spill` a local array of kTraceStack - kStackShared entries,
+// `f` the shadow walk's hit filter.  Returns true when the query is answered.
+template <bool kShadow, typename F = OpaqueHits>
+__device__ __forceinline__ bool trace_step(TraceState &S, const BvhView &bv, uint2 *sh, int stride, uint2 *spill, F &f)
 {
 	if(S.nhits & 0xFFu)
 	{
@@ -301,7 +315,11 @@ __device__ __forceinline__ bool trace_step(TraceState &S, const BvhView &bv, uin
 		const float t = mt_intersect(A, B, C, (id & GBRT_QUAD_BIT) != 0u, S.from, S.dir, u, v);
 		if(t <= 0.f || t < S.t_min || t >= S.t_max) continue;   // accelerator.h:125 / 137
 		const int32_t pid = static_cast<int32_t>(id & ~GBRT_QUAD_BIT);
-		if(kShadow) { S.h = Hit{pid, t, u, v}; return true; }
+		if(kShadow)
+		{
+			if(f.blocks(pid, t, S.dir)) { S.h = Hit{pid, t, u, v}; return true; }
+			continue;
+		}
 		if(t < S.h.t || (t == S.h.t && S.h.prim >= 0 && pid < S.h.prim)) S.h = Hit{pid, t, u, v};
 	}
 	if(!(S.nhits & 0xFFu))
@@ -330,7 +348,8 @@ __device__ __forceinline__ Hit trace_ray(const BvhView &bv, float ox, float oy, 
 	TraceState S;
 	if(!trace_init<kShadow>(S, bv, ox, oy, oz, tmin, dx, dy, dz, tmax)) return Hit{-1, 0.f, 0.f, 0.f};
 	uint2 spill[kTraceStack - kStackShared];
-	while(!trace_step<kShadow>(S, bv, sh, stride, spill)) { }
+	OpaqueHits f;
+	while(!trace_step<kShadow>(S, bv, sh, stride, spill, f)) { }
 	return trace_result(S);
 }
 
@@ -344,12 +363,14 @@ __device__ __forceinline__ Hit trace_ray(const BvhView &bv, float ox, float oy, 
 // every warp (the loop uses full-warp ballots) and a grid that fits on the
 // GPU at once.
 //   load(i, ray[8]) -> bool   false: entry i holds no query (skipped)
-//   store(i, const Hit &)     the answer of query i
+//   store(i, const Hit &)     the answer of query i (f still holds the
+//                             query's filter state)
+// f: the shadow walk's hit filter, reset before each query.
 constexpr uint32_t kTraceChunk = 32;
 
-template <bool kShadow, typename Load, typename Store>
-__device__ __forceinline__ void trace_persistent(const BvhView &bv, uint32_t n, uint32_t *counter, uint2 *sh, int stride, Load &&load,
-                                                 Store &&store)
+template <bool kShadow, typename F, typename Load, typename Store>
+__device__ __forceinline__ void trace_persistent_filtered(const BvhView &bv, uint32_t n, uint32_t *counter, uint2 *sh, int stride, F &f,
+                                                          Load &&load, Store &&store)
 {
 	uint2 spill[kTraceStack - kStackShared];
 	const uint32_t lane = threadIdx.x & 31u;
@@ -378,16 +399,25 @@ __device__ __forceinline__ void trace_persistent(const BvhView &bv, uint32_t n, 
 			if(!active && mine < end && load(mine, r))
 			{
 				idx = mine;
-				active = trace_init<kShadow>(S, bv, r[0], r[1], r[2], r[3], r[4], r[5], r[6], r[7]);
+				f.reset();
+				active = trace_init<kShadow, F::kTransparent>(S, bv, r[0], r[1], r[2], r[3], r[4], r[5], r[6], r[7]);
 				if(!active) store(idx, Hit{-1, 0.f, 0.f, 0.f});
 			}
 		}
-		if(active && trace_step<kShadow>(S, bv, sh, stride, spill))
+		if(active && trace_step<kShadow>(S, bv, sh, stride, spill, f))
 		{
 			store(idx, trace_result(S));
 			active = false;
 		}
 	}
+}
+
+template <bool kShadow, typename Load, typename Store>
+__device__ __forceinline__ void trace_persistent(const BvhView &bv, uint32_t n, uint32_t *counter, uint2 *sh, int stride, Load &&load,
+                                                 Store &&store)
+{
+	OpaqueHits f;
+	trace_persistent_filtered<kShadow>(bv, n, counter, sh, stride, f, load, store);
 }
 
 } // namespace gbrt

@@ -61,7 +61,8 @@ class PtParams(ctypes.Structure):
                 ("seed", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("wave_paths", ctypes.c_uint32),
                 ("guide", ctypes.c_void_p), ("guide_alpha", ctypes.c_float), ("guide_train_steps", ctypes.c_uint32),
                 ("guide_batch", ctypes.c_uint32), ("guide_max_vertex", ctypes.c_uint32), ("raydepth", ctypes.c_int32),
-                ("filter_type", ctypes.c_uint32), ("aa_pixel_width", ctypes.c_float), ("film_weight_dev", ctypes.c_void_p)]
+                ("filter_type", ctypes.c_uint32), ("aa_pixel_width", ctypes.c_float), ("film_weight_dev", ctypes.c_void_p),
+                ("transparent_shadows", ctypes.c_int32), ("shadow_depth", ctypes.c_int32)]
 
 
 # ImageFilm "filter_type" names -> gbrt_pt_params.filter_type ("pixel": single-pixel splat, plain sums)
@@ -345,16 +346,17 @@ def _material_desc(m):
         d.color2[:] = [float(x) for x in dc]
         d.params[:4] = [float(e), float(gr), float(dr), float(m[6]) if len(m) > 6 else 1.0]
     elif kind in ("glass", "rough_glass"):
-        # ("glass", IOR, filter_color, transmit_filter, mirror_color)
-        # ("rough_glass", IOR, alpha, filter_color, transmit_filter, mirror_color)
+        # ("glass", IOR, filter_color, transmit_filter, mirror_color[, {"fake_shadows": bool}])
+        # ("rough_glass", IOR, alpha, filter_color, transmit_filter, mirror_color[, {...}])
         ior, rest = float(m[1]), m[2:]
         alpha = 0.0
         if kind == "rough_glass":
             alpha, rest = float(rest[0]), rest[1:]
-        fc, tf, mc = rest
+        fc, tf, mc = rest[:3]
+        opt = rest[3] if len(rest) > 3 else {}
         d.color[:] = [float(x) for x in fc]
         d.color2[:] = [float(x) for x in mc]
-        d.params[:3] = [ior, float(tf), alpha]
+        d.params[:4] = [ior, float(tf), alpha, 1.0 if opt.get("fake_shadows", False) else 0.0]
     else:
         vals = [float(x) for x in m[1]]
         d.color[:] = vals[0:3]
@@ -454,7 +456,7 @@ class Renderer:
                         PT_FP64_FILM if fp64 else 0, int(wave_paths), guide.handle if guide is not None else None,
                         float(alpha), int(train_steps), int(batch), int(max_vertex), int(it.get("raydepth", 5)),
                         FILTERS[film.get("filter_type", "pixel")], float(film.get("AA_pixelwidth", 0.0)),
-                        int(weight_ptr) or None)
+                        int(weight_ptr) or None, int(bool(it.get("transpShad", False))), int(it.get("shadowDepth", 4)))
 
     def render(self, spp, base_offset=0, seed=1, fp64=False, guide=None, alpha=0.0, train_steps=0, batch=0,
                max_vertex=0):

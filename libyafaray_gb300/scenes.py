@@ -181,16 +181,21 @@ def glossy_material(diffuse_color, glossy_color=(0.9, 0.9, 0.9), exponent=100.0,
             float(diffuse_reflect))
 
 
-def glass_material(ior=1.5, filter_color=(1.0, 1.0, 1.0), transmit_filter=0.0, mirror_color=(1.0, 1.0, 1.0)):
+def glass_material(ior=1.5, filter_color=(1.0, 1.0, 1.0), transmit_filter=0.0, mirror_color=(1.0, 1.0, 1.0), fake_shadows=False):
     """A "glass" material tuple: (type, IOR, filter_color, transmit_filter,
-    mirror_color); the filter colour acts in proportion to transmit_filter."""
-    return ("glass", float(ior), tuple(filter_color), float(transmit_filter), tuple(mirror_color))
+    mirror_color[, {"fake_shadows": True}]); the filter colour acts in
+    proportion to transmit_filter; fake_shadows makes it transparent to
+    shadow rays of integrators with transpShad."""
+    m = ("glass", float(ior), tuple(filter_color), float(transmit_filter), tuple(mirror_color))
+    return m + ({"fake_shadows": True},) if fake_shadows else m
 
 
-def rough_glass_material(ior=1.5, alpha=0.1, filter_color=(1.0, 1.0, 1.0), transmit_filter=0.0, mirror_color=(1.0, 1.0, 1.0)):
+def rough_glass_material(ior=1.5, alpha=0.1, filter_color=(1.0, 1.0, 1.0), transmit_filter=0.0, mirror_color=(1.0, 1.0, 1.0),
+                         fake_shadows=False):
     """A "rough_glass" material tuple: (type, IOR, alpha, filter_color,
-    transmit_filter, mirror_color)."""
-    return ("rough_glass", float(ior), float(alpha), tuple(filter_color), float(transmit_filter), tuple(mirror_color))
+    transmit_filter, mirror_color[, {"fake_shadows": True}])."""
+    m = ("rough_glass", float(ior), float(alpha), tuple(filter_color), float(transmit_filter), tuple(mirror_color))
+    return m + ({"fake_shadows": True},) if fake_shadows else m
 
 
 def icosphere(center, radius, subdiv):
@@ -228,7 +233,7 @@ def icosphere(center, radius, subdiv):
 
 
 def cornell_scene(res=512, light_samples=4, bounces=5, rr_min=3, path_samples=1, glossy=False, glass=False, point_light=False,
-                  shiny=False):
+                  shiny=False, transparent_shadows=None):
     """The Cornell-box configuration: 34 triangles of walls and boxes
     (shinydiffuse, grey 0.75 / red / green), a 0.5 x 0.5 m ceiling area light
     of colour (17,12,4) at y = 1.999 with a 2-triangle light_mat emitter,
@@ -241,7 +246,11 @@ def cornell_scene(res=512, light_samples=4, bounces=5, rr_min=3, path_samples=1,
     of power 3.  shiny=True gives the shinydiffuse layers work: the tall box
     a Fresnel mirror (specular_reflect 0.8, IOR 1.5), the short box
     transparency 0.5 (transmit_filter 0.7) with translucency 0.3, the green
-    wall a plain 0.4 mirror over its diffuse layer, the red wall emit 0.3."""
+    wall a plain 0.4 mirror over its diffuse layer, the red wall emit 0.3.
+    transparent_shadows=D turns on the integrator's transparent shadows
+    ("transpShad", "shadowDepth" D); with glass the balls then take
+    fake_shadows (the glass ball tinted: filter colour (0.9, 0.7, 0.4),
+    transmit_filter 0.5)."""
     verts, faces, groups = cornell_mesh(as_quads=False)
     mats = {"grey": ("shinydiffusemat", (0.75, 0.75, 0.75)),
             "red": ("shinydiffusemat", (0.63, 0.065, 0.05)),
@@ -281,10 +290,18 @@ def cornell_scene(res=512, light_samples=4, bounces=5, rr_min=3, path_samples=1,
         used = np.unique(f[:, :3])
         remap = {int(u): i for i, u in enumerate(used)}
         ff = np.array([[remap[int(x)] for x in row[:3]] + [TRI] for row in f], np.uint32)
-        objects.append({"name": f"group{g}", "material": gmat[g], "vertices": verts[used], "faces": ff})
+        v = verts[used]
+        if g == 3 and transparent_shadows is not None:
+            # the short box 2 mm above the floor: its bottom face would be
+            # coplanar with the floor, and a camera path through the
+            # transparent box would then land on an exact closest-hit tie
+            v = v + np.array([0.0, 0.002, 0.0], v.dtype)
+        objects.append({"name": f"group{g}", "material": gmat[g], "vertices": v, "faces": ff})
     if glass:
-        mats["glass"] = glass_material(1.5)
-        mats["rough_glass"] = rough_glass_material(1.5, 0.2)
+        fake = transparent_shadows is not None
+        mats["glass"] = glass_material(1.5, filter_color=(0.9, 0.7, 0.4), transmit_filter=0.5 if fake else 0.0,
+                                       fake_shadows=fake) if fake else glass_material(1.5)
+        mats["rough_glass"] = rough_glass_material(1.5, 0.2, fake_shadows=fake)
         v, f = icosphere((0.35, 0.85, 0.25), 0.25, 2)
         objects.append({"name": "glass_ball", "material": "glass", "vertices": v, "faces": f})
         v, f = icosphere((-0.5, 0.3, 0.55), 0.3, 2)
@@ -305,6 +322,9 @@ def cornell_scene(res=512, light_samples=4, bounces=5, rr_min=3, path_samples=1,
               "resx": res, "resy": res, "focal": 1.3737}
     integ = {"type": "pathtracing", "path_samples": path_samples, "bounces": bounces,
              "russian_roulette_min_bounces": rr_min}
+    if transparent_shadows is not None:
+        # transparent_shadows = shadowDepth; the glass balls get fake_shadows
+        integ.update({"transpShad": True, "shadowDepth": int(transparent_shadows)})
     return {"materials": mats, "objects": objects, "lights": lights, "camera": camera, "integrator": integ}
 
 

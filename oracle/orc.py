@@ -150,13 +150,15 @@ def reference_scene_text(scene, spp, batches, threads=-1, offset_stride=None):
             vals = [*dc, *gc, e, gr, dr]
             out.append(f"material {name} glossy " + " ".join(repr(float(x)) for x in vals))
         elif t == "glass":
-            _, ior, fc, tf, mc = m
+            _, ior, fc, tf, mc = m[:5]
             vals = [ior, tf, *fc, *mc]
-            out.append(f"material {name} glass " + " ".join(repr(float(x)) for x in vals))
+            fake = " fake_shadows=true" if len(m) > 5 and m[5].get("fake_shadows") else ""
+            out.append(f"material {name} glass " + " ".join(repr(float(x)) for x in vals) + fake)
         elif t == "rough_glass":
-            _, ior, alpha, fc, tf, mc = m
+            _, ior, alpha, fc, tf, mc = m[:6]
             vals = [ior, alpha, tf, *fc, *mc]
-            out.append(f"material {name} rough_glass " + " ".join(repr(float(x)) for x in vals))
+            fake = " fake_shadows=true" if len(m) > 6 and m[6].get("fake_shadows") else ""
+            out.append(f"material {name} rough_glass " + " ".join(repr(float(x)) for x in vals) + fake)
         else:
             out.append(f"material {name} {t} " + " ".join(repr(float(x)) for x in m[1]))
     for o in scene["objects"]:

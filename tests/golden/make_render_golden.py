@@ -295,5 +295,12 @@ if __name__ == "__main__":
         variant_golden("cornell_shiny_64_render.npz", shiny=True)
     if "aa" in what:
         aa_golden()
+    if "cornell_tshadow" in what:
+        # transparent shadows: a transparent shinydiffuse box and fake_shadows
+        # glass balls, shadowDepth 4 (both balls pass) and 1 (a ball's second
+        # surface blocks)
+        variant_golden("cornell_tshadow_64_render.npz", shiny=("transparent",), glass=True, transparent_shadows=4)
+        variant_golden("cornell_tshadow1_48_render.npz", res=48, batches=24, shiny=("transparent",), glass=True,
+                       transparent_shadows=1)
     if "cornell_point" in what:
         variant_golden("cornell_point_64_render.npz", point_light=True)

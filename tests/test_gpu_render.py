@@ -107,6 +107,28 @@ def test_gpu_cornell_glass_matches_reference(cuda_device):
     assert frac >= 0.995
 
 
+@pytest.mark.parametrize("name,res,depth", [("cornell_tshadow_64_render.npz", 64, 4), ("cornell_tshadow1_48_render.npz", 48, 1)])
+def test_gpu_cornell_transparent_shadows_match_reference(cuda_device, name, res, depth):
+    """Transparent shadows (transpShad, shadowDepth): the transparent
+    shinydiffuse box and the fake_shadows glass balls let shadow rays pass
+    times their filter colour; with shadowDepth 1 a ball's second surface
+    blocks."""
+    g = np.load(os.path.join(GOLD, name))
+    sc = scenes.cornell_scene(res=res, shiny=("transparent",), glass=True, transparent_shadows=depth)
+    r = gbrt.Renderer(sc)
+    gb = batches(r, int(g["spp"]), int(g["batches"]))
+    frac, relmse, m = parity(gb, g["mean"], g["se"])
+    print(f"cornell transparent shadows (depth {depth}) {res}x{res}: {100 * frac:.2f}% of pixel channels within 3 SE, "
+          f"relMSE {relmse:.3g}, means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
+    assert frac >= 0.995
+    # the same scene with opaque shadows differs from the reference's
+    sc0 = scenes.cornell_scene(res=res, shiny=("transparent",), glass=True, transparent_shadows=depth)
+    sc0["integrator"]["transpShad"] = False
+    r0 = gbrt.Renderer(sc0)
+    f0, _, _ = parity(batches(r0, int(g["spp"]), int(g["batches"])), g["mean"], g["se"])
+    assert f0 < frac - 0.01
+
+
 def test_gpu_cornell_shiny_layers_match_reference(cuda_device):
     """ShinyDiffuseMaterial's layers: a Fresnel mirror (specular_reflect 0.8,
     IOR 1.5), transparency 0.5 with transmit_filter 0.7 and translucency 0.3,
