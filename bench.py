@@ -302,7 +302,7 @@ def render_sections(args):
         guide = r.make_guide()
         runs[frac] = convergence.time_to_relmse(r, ref, target=0.01, spp_pass=4, max_time=90, guide=guide,
                                                 alpha=0.6, train_fraction=frac, train_steps=16, batch=65536,
-                                                max_vertex=0, expected_time=plain["time_s"], spp_pass_after=16)
+                                                max_vertex=4, expected_time=plain["time_s"], spp_pass_after=16)
         del guide
     guided, short = runs[0.25], runs[0.1]
     ok = plain["reached"]
@@ -315,7 +315,7 @@ def render_sections(args):
         "guided": {k: guided[k] for k in ("time_s", "spp", "relmse", "reached")},
         "guided_settings": {"alpha": 0.6, "train_fraction_of_plain_time": 0.25, "adam_steps_per_wave": 16,
                             "batch": 65536, "spp_per_pass": "4 while training, then 16",
-                            "target": "incident radiance x BSDF cosine", "guided_vertices": "all"},
+                            "target": "incident radiance x BSDF cosine", "guided_vertices": "first 4 path vertices (camera hit and 3 bounces)"},
         "speedup_wall_time": plain["time_s"] / guided["time_s"] if guided["reached"] and ok else None,
         "speedup_samples": plain["spp"] / guided["spp"] if guided["reached"] and ok else None,
         "guided_training_10pct": {**{k: short[k] for k in ("time_s", "spp", "relmse", "reached")},

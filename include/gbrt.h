@@ -322,6 +322,48 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
                       const gbrt_light_desc *lights, uint32_t n_lights, gbrt_scene **out);
 int gbrt_scene_destroy(gbrt_scene *scene);
 
+/* ---- image textures on shinydiffuse diffuse colour ----------------------
+ * An ImageTexture (src/texture/texture_image.cc) over an in-memory float
+ * image, reached through a TextureMapperNode (src/shader/shader_node_texture.cc)
+ * set as a shinydiffuse material's "diffuse_shader": the texture's colour
+ * replaces the material's diffuse colour wherever the reference reads
+ * getShaderColor(Diffuse) (eval, sample, pdf weights, transmit filter,
+ * emission).  Parameter names and defaults [..] are the reference's. */
+enum { GBRT_TEXCO_GLOBAL = 0, GBRT_TEXCO_UV = 1 };                 /* "texco" ["global"] */
+enum { GBRT_MAPPING_PLAIN = 0, GBRT_MAPPING_CUBE = 1 };            /* "mapping" ["plain"] */
+enum { GBRT_CLIP_EXTEND = 0, GBRT_CLIP_CLIP = 1, GBRT_CLIP_CLIPCUBE = 2, GBRT_CLIP_REPEAT = 3 };   /* "clipping" ["repeat"] */
+enum { GBRT_INTERP_NONE = 0, GBRT_INTERP_BILINEAR = 1 };           /* "interpolate" ["bilinear"] */
+
+typedef struct gbrt_texture_desc {
+	int32_t width, height;
+	const float *rgba;          /* host, height rows of width RGBA floats (image x, y -> rgba[4 (y width + x)]),
+	                               linear colour (an Image with image_optimization "none") */
+	uint32_t interpolate;       /* GBRT_INTERP_* */
+	uint32_t clipping;          /* GBRT_CLIP_* */
+	int32_t xrepeat, yrepeat;   /* [1, 1] */
+	float crop[4];              /* cropmin_x, cropmin_y, cropmax_x, cropmax_y [0, 0, 1, 1] */
+	int32_t rot90;              /* [0] */
+	float adj_intensity, adj_contrast;     /* [1, 1] */
+	float adj_mult_factor[3];   /* red, green, blue [1, 1, 1] */
+	int32_t adj_clamp;          /* [0] */
+	/* the texture mapper node */
+	uint32_t texco;             /* GBRT_TEXCO_* */
+	uint32_t mapping;           /* GBRT_MAPPING_* */
+	float scale[3];             /* [1, 1, 1] */
+	float offset[3];            /* [0, 0, 0] */
+	int32_t proj[3];            /* proj_x, proj_y, proj_z: 0 zero, 1 x, 2 y, 3 z [1, 2, 3] */
+} gbrt_texture_desc;
+
+/* Texture coordinates and textures of a scene (replacing any set before).
+ * uv: n_uv (u, v) pairs (yafaray_addUv); face_uv: one uint32 quadruple per
+ * face of gbrt_scene_create, the uv indices of its vertices (the 4th unused
+ * for triangles), or NULL (no uvs: the implicit barycentric uv).
+ * material_diffuse_texture[m]: texture index driving material m's diffuse
+ * colour, -1 for none (n_materials entries; shinydiffuse materials only). */
+int gbrt_scene_set_textures(gbrt_scene *scene, const float *uv, uint32_t n_uv, const uint32_t *face_uv,
+                            const gbrt_texture_desc *textures, uint32_t n_textures,
+                            const int32_t *material_diffuse_texture, uint32_t n_materials);
+
 /* Renders spp samples per pixel and ADDS each pixel's sample sum (RGB,
  * resx*resy*3, row-major from the top-left) to film_dev (float) or
  * film64_dev (double, when not NULL).  Asynchronous on `stream` unless

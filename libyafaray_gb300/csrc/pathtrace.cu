@@ -63,10 +63,25 @@ struct DevMaterial {
 	float sdc[4];      // shinydiffuse component strengths: mirror, transparency, translucency, diffuse
 	float tcol[3];     // shinydiffuse: transmit_filter x colour + (1 - transmit_filter)
 	float ecol[3];     // shinydiffuse: emit x colour
+	int32_t dtex;      // shinydiffuse: texture driving the diffuse colour ("diffuse_shader"), -1 none
+	float tf, emit;    // shinydiffuse: transmit_filter, emit (for a textured diffuse colour)
 };
 
 // ShinyDiffuseMaterial components (material_shiny_diffuse.cc:146-189)
 enum : uint32_t { SD_MIRROR = 1u, SD_TRANSPARENT = 2u, SD_TRANSLUCENT = 4u, SD_DIFFUSE = 8u, SD_FRESNEL = 16u };
+
+// An image texture and its texture-mapper node (gbrt_texture_desc).
+struct DevTexture {
+	uint32_t off;               // first texel in the scene's texel array
+	int w, h;
+	uint32_t interp, clip, texco, mapping;
+	int xrep, yrep, rot90, crop_x, crop_y;
+	int adj, adj_ic, adj_clamp; // adjustments_set_, intensity / contrast set, adj_clamp
+	float crop[4];
+	float intensity, contrast, mult[3];
+	float scale[3], offset2[3]; // offset2 = 2 x offset (shader_node_texture.h:108)
+	int proj[3];
+};
 
 struct DevLight {
 	float c[3], tx[3], ty[3], nflip[3], col[3];   // area light (light_area.h:70-78); point light: c = from, col
@@ -130,8 +145,6 @@ struct Params {
 	uint32_t n_list;
 	// transparent shadows (MonteCarloIntegrator "transpShad", "shadowDepth")
 	int tshadow, shadow_depth;
-	const DevMaterial *mats;
-	const float4 *prim_ng;
 };
 
 struct Work {
@@ -172,6 +185,11 @@ struct SceneDev {
 	const DevMaterial *mats;
 	const DevLight *lights;
 	gbrt::LdsTables lds;
+	// textures (gbrt_scene_set_textures); null without
+	const DevTexture *tex;
+	const float4 *texels;
+	const float2 *uv;
+	const uint4 *face_uv;       // uv indices per face; x = kNoIdx: no uvs; w = kNoIdx: triangle
 };
 
 __device__ __forceinline__ float dot3(const float a[3], const float b[3]) { return xa(xa(xm(a[0], b[0]), xm(a[1], b[1])), xm(a[2], b[2])); }
@@ -217,6 +235,7 @@ __device__ __forceinline__ void cos_hemisphere(const float n[3], const float u[3
 
 struct Surface {
 	float p[3], ng[3], n[3], u[3], v[3];
+	float dcol[3];              // the diffuse colour here (the material's, or its texture's)
 	const DevMaterial *m;
 };
 
@@ -666,7 +685,161 @@ __device__ __forceinline__ int rough_sample2(const Surface &s, const float wo[3]
 }
 
 
+// ---- image textures (TextureMapperNode -> ImageTexture) --------------------
+constexpr uint32_t kNoIdx = 0xFFFFFFFFu;
+
+// Texture coordinates of a hit (PrimitivePolygon::getSurfacePolygon,
+// primitive_polygon.cc:70-101): a triangle's uvs at the barycentric weights
+// (1 - u - v, u, v), a quad's by ShapePolygon::interpolate (shape_polygon.h:
+// 94-100); a face without uvs takes the implicit (1 - u - v, u), a quad (u, v).
+__device__ __forceinline__ void hit_uv(const SceneDev &sc, int prim, float bu, float bv, float uv[2])
+{
+	const uint4 f = __ldg(sc.face_uv + prim);
+	const bool quad = f.w != kNoIdx;
+	const float w0 = xs(xs(1.f, bu), bv);
+	if(f.x == kNoIdx)
+	{
+		uv[0] = quad ? bu : w0;
+		uv[1] = quad ? bv : bu;
+		return;
+	}
+	const float2 a = __ldg(sc.uv + f.x), b = __ldg(sc.uv + f.y), c = __ldg(sc.uv + f.z);
+	if(!quad)
+	{
+		uv[0] = xa(xa(xm(w0, a.x), xm(bu, b.x)), xm(bv, c.x));
+		uv[1] = xa(xa(xm(w0, a.y), xm(bu, b.y)), xm(bv, c.y));
+		return;
+	}
+	const float2 d = __ldg(sc.uv + f.w);
+	const float iu = xs(1.f, bu), iv = xs(1.f, bv);
+	uv[0] = xa(xm(iv, xa(xm(iu, a.x), xm(bu, b.x))), xm(bv, xa(xm(iu, d.x), xm(bu, c.x))));
+	uv[1] = xa(xm(iv, xa(xm(iu, a.y), xm(bu, b.y))), xm(bv, xa(xm(iu, d.y), xm(bu, c.y))));
+}
+
+// ImageTexture::findTextureInterpolationCoordinates without mirroring
+// (texture_image.cc:264-341): the texel pair along one axis and the weight.
+__device__ __forceinline__ void tex_axis(float cf, int res, bool repeat, int &c1, int &c2, float &d)
+{
+	if(repeat)
+	{
+		c1 = static_cast<int>(cf) % res;
+		if(cf > 0.f) { c2 = (c1 + 1) % res; d = xs(cf, static_cast<float>(static_cast<int>(cf))); }
+		else { c2 = (res - 1) % res; d = -cf; }
+	}
+	else
+	{
+		c1 = max(0, min(res - 1, static_cast<int>(cf)));
+		c2 = cf > 0.f ? min(res - 1, c1 + 1) : 0;
+		d = xs(cf, floorf(cf));
+	}
+}
+
+// TextureMapperNode::getCoords / doMapping (shader_node_texture.cc:153-230),
+// ImageTexture::getColor / doMapping / noInterpolation /
+// bilinearInterpolation (texture_image.cc:180-262, 343-375) and
+// Texture::applyAdjustments (texture.cc:219-253): the texture's RGB at a hit.
+__device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p[3], const float ng[3], const float uv[2], float out[3])
+{
+	float q[3];
+	if(T.texco == GBRT_TEXCO_UV) { q[0] = xs(xm(2.f, uv[0]), 1.f); q[1] = xs(xm(2.f, uv[1]), 1.f); q[2] = 0.f; }
+	else { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+	const float tm[4] = {0.f, q[0], q[1], q[2]};
+	float t[3] = {tm[T.proj[0]], tm[T.proj[1]], tm[T.proj[2]]};
+	if(T.mapping == GBRT_MAPPING_CUBE)
+	{
+		// cubeMap: axis of the largest normal component (ties to z, then y)
+		const float ax = fabsf(ng[0]), ay = fabsf(ng[1]), az = fabsf(ng[2]);
+		float r[3];
+		if(az >= ax && az >= ay) { r[0] = t[0]; r[1] = t[1]; r[2] = t[2]; }
+		else if(ay >= ax && ay >= az) { r[0] = t[0]; r[1] = t[2]; r[2] = t[1]; }
+		else { r[0] = t[1]; r[1] = t[2]; r[2] = t[0]; }
+		t[0] = r[0]; t[1] = r[1]; t[2] = r[2];
+	}
+	for(int k = 0; k < 3; ++k) t[k] = xa(xm(t[k], T.scale[k]), T.offset2[k]);
+	// the image's own mapping of (x, -y, z)
+	float mx = xa(xm(0.5f, t[0]), 0.5f), my = xa(xm(0.5f, -t[1]), 0.5f);
+	const float mz = xa(xm(0.5f, t[2]), 0.5f);
+	if(T.clip == GBRT_CLIP_REPEAT)
+	{
+		if(T.xrep > 1) mx = xm(mx, static_cast<float>(T.xrep));
+		if(T.yrep > 1) my = xm(my, static_cast<float>(T.yrep));
+		if(mx > 1.f) mx = xs(mx, truncf(mx));
+		else if(mx < 0.f) mx = xa(mx, xs(1.f, truncf(mx)));
+		if(my > 1.f) my = xs(my, truncf(my));
+		else if(my < 0.f) my = xa(my, xs(1.f, truncf(my)));
+	}
+	if(T.crop_x) mx = xa(T.crop[0], xm(mx, xs(T.crop[2], T.crop[0])));
+	if(T.crop_y) my = xa(T.crop[1], xm(my, xs(T.crop[3], T.crop[1])));
+	if(T.rot90) { const float tmp = mx; mx = my; my = tmp; }
+	bool outside = false;
+	if(T.clip == GBRT_CLIP_CLIPCUBE) outside = mx < 0.f || mx > 1.f || my < 0.f || my > 1.f || mz < -1.f || mz > 1.f;
+	else if(T.clip == GBRT_CLIP_CLIP) outside = mx < 0.f || mx > 1.f || my < 0.f || my > 1.f;
+	else if(T.clip == GBRT_CLIP_EXTEND)
+	{
+		mx = mx > 0.99999f ? 0.99999f : (mx < 0.f ? 0.f : mx);
+		my = my > 0.99999f ? 0.99999f : (my < 0.f ? 0.f : my);
+	}
+	if(outside) { out[0] = out[1] = out[2] = 0.f; return; }
+	const bool rep = T.clip == GBRT_CLIP_REPEAT;
+	const float4 *tx = sc.texels + T.off;
+	float4 c;
+	if(T.interp == GBRT_INTERP_NONE)
+	{
+		const float xf = xm(static_cast<float>(T.w), xs(mx, floorf(mx)));
+		const float yf = xm(static_cast<float>(T.h), xs(my, floorf(my)));
+		int x1, x2, y1, y2;
+		float dx, dy;
+		tex_axis(xf, T.w, rep, x1, x2, dx);
+		tex_axis(yf, T.h, rep, y1, y2, dy);
+		c = __ldg(tx + y1 * T.w + x1);
+	}
+	else
+	{
+		const float xf = xs(xm(static_cast<float>(T.w), xs(mx, floorf(mx))), 0.5f);
+		const float yf = xs(xm(static_cast<float>(T.h), xs(my, floorf(my))), 0.5f);
+		int x1, x2, y1, y2;
+		float dx, dy;
+		tex_axis(xf, T.w, rep, x1, x2, dx);
+		tex_axis(yf, T.h, rep, y1, y2, dy);
+		const float4 c11 = __ldg(tx + y1 * T.w + x1), c21 = __ldg(tx + y1 * T.w + x2);
+		const float4 c12 = __ldg(tx + y2 * T.w + x1), c22 = __ldg(tx + y2 * T.w + x2);
+		const float w11 = xm(xs(1.f, dx), xs(1.f, dy)), w12 = xm(xs(1.f, dx), dy);
+		const float w21 = xm(dx, xs(1.f, dy)), w22 = xm(dx, dy);
+		c.x = xa(xa(xa(xm(w11, c11.x), xm(w12, c12.x)), xm(w21, c21.x)), xm(w22, c22.x));
+		c.y = xa(xa(xa(xm(w11, c11.y), xm(w12, c12.y)), xm(w21, c21.y)), xm(w22, c22.y));
+		c.z = xa(xa(xa(xm(w11, c11.z), xm(w12, c12.z)), xm(w21, c21.z)), xm(w22, c22.z));
+	}
+	float r[3] = {c.x, c.y, c.z};
+	if(T.adj)
+	{
+		if(T.adj_ic)
+			for(int k = 0; k < 3; ++k) r[k] = xs(xa(xm(xs(r[k], 0.5f), T.contrast), T.intensity), 0.5f);
+		if(T.adj_clamp) for(int k = 0; k < 3; ++k) r[k] = r[k] < 0.f ? 0.f : r[k];
+		for(int k = 0; k < 3; ++k) if(T.mult[k] != 1.f) r[k] = xm(r[k], T.mult[k]);
+		if(T.adj_clamp) for(int k = 0; k < 3; ++k) r[k] = r[k] < 0.f ? 0.f : r[k];
+	}
+	out[0] = r[0]; out[1] = r[1]; out[2] = r[2];
+}
+
+// The diffuse colour of a surface point (the material's, or its diffuse
+// shader's texture at the hit's coordinates).
+__device__ __forceinline__ void surface_color(const SceneDev &sc, Surface &s, int prim, float bu, float bv)
+{
+	const DevMaterial &m = *s.m;
+	if(m.dtex < 0) { s.dcol[0] = m.col[0]; s.dcol[1] = m.col[1]; s.dcol[2] = m.col[2]; return; }
+	float uv[2];
+	hit_uv(sc, prim, bu, bv, uv);
+	tex_color(sc, sc.tex[m.dtex], s.p, s.ng, uv, s.dcol);
+}
+
 // ---- ShinyDiffuseMaterial layers (material_shiny_diffuse.cc:205-619) -------
+// The transmit colour transmit_filter x diffuse colour + (1 - transmit_filter)
+// (:410, 517, 562), precomputed for an untextured diffuse colour.
+__device__ __forceinline__ float shiny_tcol(const Surface &s, int k)
+{
+	return s.m->dtex < 0 ? s.m->tcol[k] : s.m->tf * s.dcol[k] + (1.f - s.m->tf);
+}
+
 // getFresnelKr (:205-217): Fresnel reflectance with the fresnel_effect, else 1.
 __device__ __forceinline__ float shiny_kr(const DevMaterial &m, const float wo[3], const float n[3])
 {
@@ -715,12 +888,12 @@ __device__ __noinline__ void shiny_eval_layers(const Surface &s, const float wo[
 	if(xm(cos_ng_wo, cos_ng_wl) < 0.f && (m.sd & SD_TRANSLUCENT))
 	{
 		const float f = m.sdc[2] * m_t;
-		for(int k = 0; k < 3; ++k) out[k] = f * m.col[k];
+		for(int k = 0; k < 3; ++k) out[k] = f * s.dcol[k];
 		return;
 	}
 	if(dot3(n, wl) < 0.f) return;
 	const float m_d = m_t * (1.f - m.sdc[2]) * m.sdc[3];
-	for(int k = 0; k < 3; ++k) out[k] = m_d * m.col[k];
+	for(int k = 0; k < 3; ++k) out[k] = m_d * s.dcol[k];
 }
 
 // pdf (:443-484): the components whose flags share a bit with bsdfs add
@@ -803,20 +976,20 @@ __device__ __noinline__ bool shiny_sample_layers(const Surface &s, const float w
 	else if(c == 1)
 	{
 		wi[0] = -wo[0]; wi[1] = -wo[1]; wi[2] = -wo[2];
-		for(int k = 0; k < 3; ++k) col[k] = a[1] * m.tcol[k];
+		for(int k = 0; k < 3; ++k) col[k] = a[1] * shiny_tcol(s, k);
 		pdf = fabsf(dot3(wi, n)) < 1e-6f ? 0.f : width[pick];
 	}
 	else if(c == 2)
 	{
 		const float nn[3] = {-n[0], -n[1], -n[2]};
 		cos_hemisphere(nn, s.u, s.v, s_1, s2, wi);
-		if(xm(cos_ng_wo, dot3(s.ng, wi)) < 0.f) for(int k = 0; k < 3; ++k) col[k] = a[2] * m.col[k];
+		if(xm(cos_ng_wo, dot3(s.ng, wi)) < 0.f) for(int k = 0; k < 3; ++k) col[k] = a[2] * s.dcol[k];
 		pdf = fabsf(dot3(wi, n)) * width[pick];
 	}
 	else
 	{
 		cos_hemisphere(n, s.u, s.v, s_1, s2, wi);
-		if(xm(cos_ng_wo, dot3(s.ng, wi)) > 0.f) for(int k = 0; k < 3; ++k) col[k] = a[3] * m.col[k];
+		if(xm(cos_ng_wo, dot3(s.ng, wi)) > 0.f) for(int k = 0; k < 3; ++k) col[k] = a[3] * s.dcol[k];
 		pdf = fabsf(dot3(wi, n)) * width[pick];
 	}
 	sampled = shiny_cflags(c);
@@ -843,7 +1016,7 @@ __device__ __forceinline__ void shiny_eval(const Surface &s, const float wo[3], 
 	face_forward(s, wo, n);
 	if(dot3(n, wl) < 0.f) return;
 	const float m_d = s.m->sdc[3];
-	for(int k = 0; k < 3; ++k) out[k] = m_d * s.m->col[k];
+	for(int k = 0; k < 3; ++k) out[k] = m_d * s.dcol[k];
 }
 
 __device__ __forceinline__ float shiny_pdf(const Surface &s, const float wo[3], const float wi[3], uint32_t bsdfs)
@@ -868,7 +1041,7 @@ __device__ __forceinline__ bool shiny_sample(const Surface &s, const float wo[3]
 	face_forward(s, wo, n);
 	cos_hemisphere(n, s.u, s.v, s1 / width, s2, wi);
 	col[0] = col[1] = col[2] = 0.f;
-	if(xm(dot3(s.ng, wo), dot3(s.ng, wi)) > 0.f) for(int k = 0; k < 3; ++k) col[k] = c * s.m->col[k];
+	if(xm(dot3(s.ng, wo), dot3(s.ng, wi)) > 0.f) for(int k = 0; k < 3; ++k) col[k] = c * s.dcol[k];
 	pdf = fabsf(dot3(wi, n)) * width;
 	sampled = BF_DIFFUSE | BF_REFLECT;
 	w = __fdiv_rn(fabsf(dot3(wi, s.n)), xa(xm(pdf, 0.99f), 0.01f));
@@ -890,7 +1063,7 @@ __device__ __forceinline__ void shiny_specular(const Surface &s, const float wo[
 	if(has_refract)
 	{
 		const float f = (1.f - m.sdc[0] * kr) * m.sdc[1];
-		for(int k = 0; k < 3; ++k) { rdir[k] = -wo[k]; rcol[k] = f * m.tcol[k]; }
+		for(int k = 0; k < 3; ++k) { rdir[k] = -wo[k]; rcol[k] = f * shiny_tcol(s, k); }
 	}
 	if(has_reflect)
 	{
@@ -961,7 +1134,7 @@ __device__ __forceinline__ void bsdf_eval_at(const Surface &s, const float wo[3]
 		if(!(xm(cos_ng_wo, cos_ng_wi) > 0.f)) return;
 		const float pdf = fabsf(dot3(wi, n));
 		const float w = __fdiv_rn(fabsf(dot3(wi, s.n)), xa(xm(pdf, 0.99f), 0.01f));
-		for(int k = 0; k < 3; ++k) fw[k] = xm(s.m->sdc[3] * s.m->col[k], w);
+		for(int k = 0; k < 3; ++k) fw[k] = xm(s.m->sdc[3] * s.dcol[k], w);
 		return;
 	}
 	if(s.m->type != GBRT_MAT_GLOSSY || xm(cos_ng_wo, cos_ng_wi) < 0.f) return;
@@ -1019,7 +1192,7 @@ __device__ __forceinline__ bool mat_emit(const Surface &s, const float wo[3], fl
 	if(s.m->type == GBRT_MAT_SHINYDIFFUSE)
 	{
 		if(!(s.m->flags & BF_EMIT)) return false;
-		for(int k = 0; k < 3; ++k) out[k] = s.m->ecol[k];
+		for(int k = 0; k < 3; ++k) out[k] = s.m->dtex < 0 ? s.m->ecol[k] : s.dcol[k] * s.m->emit;
 		return true;
 	}
 	if(s.m->type != GBRT_MAT_LIGHT) return false;
@@ -1476,6 +1649,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				s.n[0] = ng.x; s.n[1] = ng.y; s.n[2] = ng.z;
 				s.m = sc.mats + __float_as_uint(ng.w);
 				coords_system(s.n, s.u, s.v);
+				surface_color(sc, s, prim, h.z, h.w);
 				wo[0] = -dir[0]; wo[1] = -dir[1]; wo[2] = -dir[2];
 				pixel = W.p_pixel[path];
 				si = W.p_si[path];
@@ -1830,7 +2004,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 // accum *= transparency x accum, times the transmit colour) and Glass /
 // RoughGlass (material_glass.cc:297-303, material_rough_glass.cc:349-355:
 // kt x filter colour).
-__device__ __forceinline__ void mat_transparency(const DevMaterial &m, const float ng[3], const float wo[3], float out[3])
+__device__ __forceinline__ void mat_transparency(const DevMaterial &m, const float ng[3], const float wo[3], const float *dcol, float out[3])
 {
 	const bool flip = dot3(ng, wo) < 0.f;
 	const float n[3] = {flip ? -ng[0] : ng[0], flip ? -ng[1] : ng[1], flip ? -ng[2] : ng[2]};
@@ -1840,7 +2014,7 @@ __device__ __forceinline__ void mat_transparency(const DevMaterial &m, const flo
 		float accum = 1.f;
 		if(m.sd & SD_MIRROR) accum = 1.f - kr * m.sdc[0];
 		accum *= m.sdc[1] * accum;
-		for(int k = 0; k < 3; ++k) out[k] = accum * m.tcol[k];
+		for(int k = 0; k < 3; ++k) out[k] = accum * (m.dtex < 0 ? m.tcol[k] : m.tf * dcol[k] + (1.f - m.tf));
 	}
 	else
 	{
@@ -1856,20 +2030,30 @@ __device__ __forceinline__ void mat_transparency(const DevMaterial &m, const flo
 // on the ray (then it blocks too).
 struct TransparentHits {
 	static constexpr bool kTransparent = true;
+	const SceneDev *sc;          // textures of a textured diffuse colour
 	const DevMaterial *mats;
 	const float4 *prim_ng;
 	int max_depth;
 	int depth;
 	float col[3];
 	__device__ __forceinline__ void reset() { depth = 0; col[0] = col[1] = col[2] = 1.f; }
-	__device__ __forceinline__ bool blocks(int32_t prim, float, const float *dir)
+	__device__ __forceinline__ bool blocks(int32_t prim, const float *from, const float *dir, float t, float u, float v)
 	{
 		const float4 g = __ldg(prim_ng + prim);
 		const DevMaterial &m = mats[__float_as_uint(g.w)];
 		if(!m.transparent || depth >= max_depth) return true;
 		const float ng[3] = {g.x, g.y, g.z};
+		float dcol[3] = {0.f, 0.f, 0.f};
+		if(m.dtex >= 0)
+		{
+			// the hit point as Accelerator::primitiveIntersectionTransparentShadow forms it (from + t dir)
+			const float p[3] = {xa(from[0], xm(t, dir[0])), xa(from[1], xm(t, dir[1])), xa(from[2], xm(t, dir[2]))};
+			float uv[2];
+			hit_uv(*sc, prim, u, v, uv);
+			tex_color(*sc, sc->tex[m.dtex], p, ng, uv, dcol);
+		}
 		float tr[3];
-		mat_transparency(m, ng, dir, tr);
+		mat_transparency(m, ng, dir, dcol, tr);
 		for(int k = 0; k < 3; ++k) col[k] *= tr[k];
 		++depth;
 		return false;
@@ -1881,8 +2065,9 @@ struct TransparentHits {
 // shadows (the unoccluded colour times the filter colour of the transparent
 // surfaces passed).
 template <bool kFilm, bool kTransparent>
-__global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Params P, Work W, uint32_t shadow_cap, float *film, double *film64)
+__global__ void __launch_bounds__(kThreads) k_shadow(SceneDev sc, Params P, Work W, uint32_t shadow_cap, float *film, double *film64)
 {
+	const gbrt::BvhView &bv = sc.bv;
 	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
 	const uint32_t n = min(W.count[2], shadow_cap);
 	uint32_t traced = 0;
@@ -1890,8 +2075,9 @@ __global__ void __launch_bounds__(kThreads) k_shadow(gbrt::BvhView bv, Params P,
 	Filter f;
 	if constexpr(kTransparent)
 	{
-		f.mats = P.mats;
-		f.prim_ng = P.prim_ng;
+		f.sc = &sc;
+		f.mats = sc.mats;
+		f.prim_ng = sc.prim_ng;
 		f.max_depth = P.shadow_depth;
 	}
 	gbrt::trace_persistent_filtered<true>(
@@ -2304,6 +2490,7 @@ __global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJo
 			s.n[0] = ng.x; s.n[1] = ng.y; s.n[2] = ng.z;
 			s.m = sc.mats + __float_as_uint(ng.w);
 			coords_system(s.n, s.u, s.v);
+			surface_color(sc, s, h.prim, h.u, h.v);
 			const float wi[3] = {-d[0], -d[1], -d[2]};
 			const uint32_t mf = s.m->flags;
 			const bool dep = J.caustic ? ((mf & (BF_DIFFUSE | BF_GLOSSY)) && caustic) : ((mf & BF_DIFFUSE) && !caustic);
@@ -2390,6 +2577,7 @@ __global__ void __launch_bounds__(kThreads) k_pm_root(SceneDev sc, Params P, Wor
 		s.ng[0] = ng.x; s.ng[1] = ng.y; s.ng[2] = ng.z;
 		s.n[0] = ng.x; s.n[1] = ng.y; s.n[2] = ng.z;
 		coords_system(s.n, s.u, s.v);
+		surface_color(sc, s, prim, h.z, h.w);
 		const float wo[3] = {-dir[0], -dir[1], -dir[2]};
 		float est[3] = {0.f, 0.f, 0.f};
 		uint32_t idx[gbrt::kMaxGather];
@@ -2668,6 +2856,13 @@ struct gbrt_scene {
 	cudaEvent_t ev_last = nullptr;      // recorded after each render: the buffers' last use
 	float *filter_dev = nullptr;        // 16 x 16 film filter table of the current render
 	float filter_host[256];
+	// textures (gbrt_scene_set_textures)
+	DevTexture *tex = nullptr;
+	float4 *texels = nullptr;
+	float2 *uv = nullptr;
+	uint4 *face_uv = nullptr;
+	std::vector<uint8_t> face_quad;     // per face: a quad (for the implicit uv)
+	std::vector<DevMaterial> mats_host;
 	std::mutex mu;
 };
 
@@ -3009,7 +3204,8 @@ int shoot_map(gbrt_scene *S, const SceneDev &sc, bool caustic, uint32_t n, int m
 
 SceneDev scene_dev(const gbrt_scene *S)
 {
-	return SceneDev{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off, S->lds_sfac_nd}};
+	return SceneDev{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off, S->lds_sfac_nd},
+	                S->tex, S->texels, S->uv, S->face_uv};
 }
 
 } // namespace
@@ -3035,6 +3231,7 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 		DevMaterial &d = mats[i];
 		std::memset(&d, 0, sizeof(d));
 		d.type = m.type;
+		d.dtex = -1;
 		if(m.type == GBRT_MAT_SHINYDIFFUSE)
 		{
 			// ShinyDiffuseMaterial ctor + config (material_shiny_diffuse.cc:133-189);
@@ -3079,6 +3276,8 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 			d.ior = ior * ior;
 			const float emit = m.power;
 			if(emit > 0.f) d.flags |= BF_EMIT;
+			d.tf = transmit_filter;
+			d.emit = emit;
 			for(int k = 0; k < 3; ++k)
 			{
 				d.col[k] = m.color[k];
@@ -3192,6 +3391,9 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 	gbrt_scene *S = new gbrt_scene();
 	S->bvh = bvh;
 	S->lights_host = ls;
+	S->mats_host = mats;
+	S->face_quad.resize(n_faces);
+	for(uint32_t i = 0; i < n_faces; ++i) S->face_quad[i] = faces[4ull * i + 3] != GBRT_TRIANGLE ? 1u : 0u;
 	for(const DevMaterial &d : mats)
 	{
 		if((d.flags & BF_GLOSSY) && (d.flags & BF_REFLECT)) { S->split_glossy = true; if(d.flags & BF_TRANSMIT) S->split_glossy_transmit = true; }
@@ -3228,12 +3430,96 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 	return GBRT_OK;
 }
 
+// Texture coordinates, image textures and the materials they drive.
+int gbrt_scene_set_textures(gbrt_scene *S, const float *uv, uint32_t n_uv, const uint32_t *face_uv, const gbrt_texture_desc *textures,
+                            uint32_t n_textures, const int32_t *material_diffuse_texture, uint32_t n_materials)
+{
+	if(!S) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: NULL scene");
+	if((n_uv && !uv) || (n_textures && !textures) || (n_materials && !material_diffuse_texture) || (face_uv && !n_uv))
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: NULL array");
+	if(n_materials != S->n_mats)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: %u material entries for %u materials", n_materials, S->n_mats);
+	std::vector<DevTexture> tex(std::max<uint32_t>(1, n_textures));
+	size_t n_texels = 0;
+	for(uint32_t i = 0; i < n_textures; ++i)
+	{
+		const gbrt_texture_desc &t = textures[i];
+		if(t.width <= 0 || t.height <= 0 || !t.rgba)
+			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u has no image (%d x %d)", i, t.width, t.height);
+		if(t.interpolate > GBRT_INTERP_BILINEAR || t.clipping > GBRT_CLIP_REPEAT || t.texco > GBRT_TEXCO_UV || t.mapping > GBRT_MAPPING_CUBE)
+			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u: unsupported interpolate / clipping / texco / mapping", i);
+		DevTexture &d = tex[i];
+		d.off = static_cast<uint32_t>(n_texels);
+		d.w = t.width; d.h = t.height;
+		d.interp = t.interpolate; d.clip = t.clipping; d.texco = t.texco; d.mapping = t.mapping;
+		d.xrep = t.xrepeat; d.yrep = t.yrepeat; d.rot90 = t.rot90 ? 1 : 0;
+		for(int k = 0; k < 4; ++k) d.crop[k] = t.crop[k];
+		d.crop_x = (t.crop[0] != 0.f || t.crop[2] != 1.f) ? 1 : 0;      // texture_image.h:104-105
+		d.crop_y = (t.crop[1] != 0.f || t.crop[3] != 1.f) ? 1 : 0;
+		d.intensity = t.adj_intensity; d.contrast = t.adj_contrast;
+		d.adj_ic = (t.adj_intensity != 1.f || t.adj_contrast != 1.f) ? 1 : 0;
+		d.adj_clamp = t.adj_clamp ? 1 : 0;
+		for(int k = 0; k < 3; ++k) d.mult[k] = t.adj_mult_factor[k];
+		d.adj = (d.adj_ic || d.adj_clamp || t.adj_mult_factor[0] != 1.f || t.adj_mult_factor[1] != 1.f || t.adj_mult_factor[2] != 1.f) ? 1 : 0;
+		for(int k = 0; k < 3; ++k)
+		{
+			if(t.proj[k] < 0 || t.proj[k] > 3) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u: proj %d", i, t.proj[k]);
+			d.proj[k] = t.proj[k];
+			d.scale[k] = t.scale[k];
+			d.offset2[k] = 2.f * t.offset[k];
+		}
+		n_texels += static_cast<size_t>(t.width) * t.height;
+		if(n_texels >= (1ull << 32)) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_scene_set_textures: more than 2^32 texels");
+	}
+	std::vector<float4> texels(std::max<size_t>(1, n_texels));
+	for(uint32_t i = 0; i < n_textures; ++i)
+		std::memcpy(&texels[tex[i].off], textures[i].rgba, sizeof(float4) * static_cast<size_t>(textures[i].width) * textures[i].height);
+	std::vector<uint4> fuv(std::max<uint32_t>(1, S->n_prims));
+	for(uint32_t f = 0; f < S->n_prims; ++f)
+	{
+		const bool quad = S->face_quad[f] != 0;
+		if(!face_uv) { fuv[f] = make_uint4(kNoIdx, kNoIdx, kNoIdx, quad ? 0u : kNoIdx); continue; }
+		const uint32_t *q = face_uv + 4ull * f;
+		for(int k = 0; k < (quad ? 4 : 3); ++k)
+			if(q[k] >= n_uv) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: face %u uses uv %u of %u", f, q[k], n_uv);
+		fuv[f] = make_uint4(q[0], q[1], q[2], quad ? q[3] : kNoIdx);
+	}
+	std::vector<DevMaterial> mats = S->mats_host;
+	for(uint32_t m = 0; m < n_materials; ++m)
+	{
+		const int32_t t = material_diffuse_texture[m];
+		if(t >= 0 && (static_cast<uint32_t>(t) >= n_textures || mats[m].type != GBRT_MAT_SHINYDIFFUSE))
+			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: material %u: texture %d (shinydiffuse only, %u textures)", m, t, n_textures);
+		mats[m].dtex = t >= 0 ? t : -1;
+	}
+	std::lock_guard<std::mutex> lock(S->mu);
+	if(S->ev_last) GBRT_CK(cudaEventSynchronize(S->ev_last));
+	for(void *p : {static_cast<void *>(S->tex), static_cast<void *>(S->texels), static_cast<void *>(S->uv), static_cast<void *>(S->face_uv)})
+		if(p) cudaFree(p);
+	S->tex = nullptr; S->texels = nullptr; S->uv = nullptr; S->face_uv = nullptr;
+	struct Up { void **dst; const void *src; size_t bytes; };
+	const Up ups[] = {{reinterpret_cast<void **>(&S->tex), tex.data(), tex.size() * sizeof(DevTexture)},
+	                  {reinterpret_cast<void **>(&S->texels), texels.data(), texels.size() * sizeof(float4)},
+	                  {reinterpret_cast<void **>(&S->uv), n_uv ? static_cast<const void *>(uv) : nullptr, std::max<size_t>(1, n_uv) * sizeof(float2)},
+	                  {reinterpret_cast<void **>(&S->face_uv), fuv.data(), fuv.size() * sizeof(uint4)}};
+	for(const Up &u : ups)
+	{
+		GBRT_CK(cudaMalloc(u.dst, u.bytes));
+		if(u.src) GBRT_CK(cudaMemcpy(*u.dst, u.src, u.bytes, cudaMemcpyHostToDevice));
+	}
+	GBRT_CK(cudaMemcpy(S->mats, mats.data(), mats.size() * sizeof(DevMaterial), cudaMemcpyHostToDevice));
+	S->mats_host = mats;
+	return GBRT_OK;
+}
+
 int gbrt_scene_destroy(gbrt_scene *S)
 {
 	if(!S) return GBRT_OK;
 	void *ptrs[] = {S->prim_ng, S->mats, S->lights, S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off,
 	                S->lds_sfac_nd, S->work, S->spawn, S->spawn_count};
 	for(void *p : ptrs) if(p) cudaFree(p);
+	for(void *p : {static_cast<void *>(S->tex), static_cast<void *>(S->texels), static_cast<void *>(S->uv), static_cast<void *>(S->face_uv)})
+		if(p) cudaFree(p);
 	if(S->filter_dev) cudaFree(S->filter_dev);
 	if(S->ev_last) cudaEventDestroy(S->ev_last);
 	delete S;
@@ -3363,7 +3649,7 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	const uint32_t stride = static_cast<uint32_t>(std::max(1, pp.bounces));
 	if(int rc = alloc_work(S, wave, shadow_cap, guide ? stride : 0, s)) return rc;
 	Camera cam = make_camera(*camera);
-	SceneDev sc{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off, S->lds_sfac_nd}};
+	const SceneDev sc = scene_dev(S);
 	Params P{};
 	P.spp = pp.spp; P.path_samples = pp.path_samples; P.bounces = pp.bounces; P.rr_min = pp.russian_roulette_min_bounces;
 	P.raydepth = raydepth;
@@ -3375,8 +3661,6 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	P.n_list = aa ? aa->n_list : 0u;
 	P.tshadow = pp.transparent_shadows ? 1 : 0;
 	P.shadow_depth = pp.shadow_depth;
-	P.mats = S->mats;
-	P.prim_ng = S->prim_ng;
 	if(pp.filter_type != GBRT_FILTER_PIXEL)
 	{
 		if(!pp.film_weight_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: filter type %u needs film_weight_dev", pp.filter_type);
@@ -3433,13 +3717,13 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 			k_shade<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, camera->resx, static_cast<uint32_t>(shadow_cap), film, film64_dev);
 			const uint32_t scap = static_cast<uint32_t>(shadow_cap);
 			if(Pw.film_w && Pw.tshadow)
-				k_shadow<true, true><<<persistent_grid(k_shadow<true, true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, scap, film, film64_dev);
+				k_shadow<true, true><<<persistent_grid(k_shadow<true, true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, scap, film, film64_dev);
 			else if(Pw.film_w)
-				k_shadow<true, false><<<persistent_grid(k_shadow<true, false>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, scap, film, film64_dev);
+				k_shadow<true, false><<<persistent_grid(k_shadow<true, false>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, scap, film, film64_dev);
 			else if(Pw.tshadow)
-				k_shadow<false, true><<<persistent_grid(k_shadow<false, true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, scap, film, film64_dev);
+				k_shadow<false, true><<<persistent_grid(k_shadow<false, true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, scap, film, film64_dev);
 			else
-				k_shadow<false, false><<<persistent_grid(k_shadow<false, false>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc.bv, Pw, Ww, scap, film, film64_dev);
+				k_shadow<false, false><<<persistent_grid(k_shadow<false, false>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, scap, film, film64_dev);
 			cur ^= 1;
 		}
 		return GBRT_OK;

@@ -217,7 +217,7 @@ struct TraceState {
 // Hit filters of the shadow walk.  OpaqueHits: every hit in range blocks
 // (Accelerator::isShadowed).  A transparent-shadow filter
 // (isShadowedTransparentShadow, accelerator.h:113-120, 147-169) decides per
-// hit: blocks(prim, t, dir) true ends the walk as occluded, false lets the
+// hit: blocks(prim, from, dir, t, u, v) true ends the walk as occluded, false lets the
 // ray pass (the filter keeps what it needs, e.g. the filter colour).  Its
 // kTransparent = true also selects the transparent walk's t_min,
 // max(tmin, bias) (accelerator_kdtree_common.h:139).  The hierarchy holds
@@ -225,7 +225,7 @@ struct TraceState {
 struct OpaqueHits {
 	static constexpr bool kTransparent = false;
 	__device__ __forceinline__ void reset() {}
-	__device__ __forceinline__ bool blocks(int32_t, float, const float *) { return true; }
+	__device__ __forceinline__ bool blocks(int32_t, const float *, const float *, float, float, float) { return true; }
 };
 
 // Ray set-up.  Closest hit follows Accelerator::intersect(ray, camera)
@@ -317,7 +317,7 @@ __device__ __forceinline__ bool trace_step(TraceState &S, const BvhView &bv, uin
 		const int32_t pid = static_cast<int32_t>(id & ~GBRT_QUAD_BIT);
 		if(kShadow)
 		{
-			if(f.blocks(pid, t, S.dir)) { S.h = Hit{pid, t, u, v}; return true; }
+			if(f.blocks(pid, S.from, S.dir, t, u, v)) { S.h = Hit{pid, t, u, v}; return true; }
 			continue;
 		}
 		if(t < S.h.t || (t == S.h.t && S.h.prim >= 0 && pid < S.h.prim)) S.h = Hit{pid, t, u, v};

@@ -78,6 +78,49 @@ class AaParams(ctypes.Structure):
                 ("variance_pixels", ctypes.c_int32)]
 
 
+class TextureDesc(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("rgba", ctypes.c_void_p),
+                ("interpolate", ctypes.c_uint32), ("clipping", ctypes.c_uint32), ("xrepeat", ctypes.c_int32),
+                ("yrepeat", ctypes.c_int32), ("crop", ctypes.c_float * 4), ("rot90", ctypes.c_int32),
+                ("adj_intensity", ctypes.c_float), ("adj_contrast", ctypes.c_float),
+                ("adj_mult_factor", ctypes.c_float * 3), ("adj_clamp", ctypes.c_int32), ("texco", ctypes.c_uint32),
+                ("mapping", ctypes.c_uint32), ("scale", ctypes.c_float * 3), ("offset", ctypes.c_float * 3),
+                ("proj", ctypes.c_int32 * 3)]
+
+
+# ImageTexture / TextureMapperNode enum names (texture_image.h, shader_node_texture.h)
+TEXCO = {"global": 0, "uv": 1}
+MAPPING = {"plain": 0, "cube": 1}
+CLIPPING = {"extend": 0, "clip": 1, "clipcube": 2, "repeat": 3}
+INTERPOLATE = {"none": 0, "bilinear": 1}
+
+
+def texture_desc(t):
+    """gbrt_texture_desc of a scene "textures" entry (image [h, w, 4] float32
+    plus the reference's texture and texture-mapper parameter names); the
+    image array must stay alive until the call that takes the desc."""
+    img = np.ascontiguousarray(t["image"], np.float32)
+    d = TextureDesc()
+    d.height, d.width = int(img.shape[0]), int(img.shape[1])
+    d.rgba = img.ctypes.data
+    d.interpolate = INTERPOLATE[t.get("interpolate", "bilinear")]
+    d.clipping = CLIPPING[t.get("clipping", "repeat")]
+    d.xrepeat, d.yrepeat = int(t.get("xrepeat", 1)), int(t.get("yrepeat", 1))
+    d.crop[:] = [float(t.get("cropmin_x", 0.0)), float(t.get("cropmin_y", 0.0)), float(t.get("cropmax_x", 1.0)),
+                 float(t.get("cropmax_y", 1.0))]
+    d.rot90 = int(bool(t.get("rot90", False)))
+    d.adj_intensity, d.adj_contrast = float(t.get("adj_intensity", 1.0)), float(t.get("adj_contrast", 1.0))
+    d.adj_mult_factor[:] = [float(t.get("adj_mult_factor_red", 1.0)), float(t.get("adj_mult_factor_green", 1.0)),
+                            float(t.get("adj_mult_factor_blue", 1.0))]
+    d.adj_clamp = int(bool(t.get("adj_clamp", False)))
+    d.texco = TEXCO[t.get("texco", "global")]
+    d.mapping = MAPPING[t.get("mapping", "plain")]
+    d.scale[:] = [float(x) for x in t.get("scale", (1.0, 1.0, 1.0))]
+    d.offset[:] = [float(x) for x in t.get("offset", (0.0, 0.0, 0.0))]
+    d.proj[:] = [int(x) for x in t.get("proj", (1, 2, 3))]
+    return d, img
+
+
 # AaNoiseParams::DarkDetectionType names (include/common/aa_noise_params.h:30-37)
 DARK_DETECTION = {"none": 0, "linear": 1, "curve": 2}
 
@@ -194,6 +237,7 @@ SIGNATURES = {
                                     _VP, ctypes.POINTER(PtStats), _VP]),
     "gbrt_aa_flags": (_I, [_VP, _VP, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(AaParams), ctypes.c_float, _VP,
                            ctypes.POINTER(ctypes.c_uint32)]),
+    "gbrt_scene_set_textures": (_I, [_VP, _VP, _U32, _VP, ctypes.POINTER(TextureDesc), _U32, _VP, _U32]),
 }
 
 _lib = None
@@ -400,6 +444,30 @@ class Renderer:
                                        len(self.faces), _ptr(fm), mats, len(self.mat_names), lights,
                                        len(scene["lights"]), ctypes.byref(h)))
         self._h = h
+        if scene.get("textures"):
+            self._set_textures()
+
+    def _set_textures(self):
+        """Image textures of the scene's "textures" entry on the shinydiffuse
+        materials whose options name one ("diffuse_texture")."""
+        from . import scenes as _scenes
+        names = list(self.scene["textures"].keys())
+        descs, keep = (TextureDesc * len(names))(), []
+        for i, n in enumerate(names):
+            d, img = texture_desc(self.scene["textures"][n])
+            descs[i] = d
+            keep.append(img)
+        mt = np.full(len(self.mat_names), -1, np.int32)
+        for i, n in enumerate(self.mat_names):
+            m = self.scene["materials"][n]
+            if m[0] == "shinydiffusemat" and len(m) > 2 and m[2].get("diffuse_texture"):
+                mt[i] = names.index(m[2]["diffuse_texture"])
+        uv, fuv = _scenes.flatten_uvs(self.scene)
+        if uv is not None:
+            uv = np.ascontiguousarray(uv, np.float32)
+            fuv = np.ascontiguousarray(fuv, np.uint32)
+        check(load().gbrt_scene_set_textures(self._h, _ptr(uv), 0 if uv is None else len(uv), _ptr(fuv), descs, len(names),
+                                             _ptr(mt), len(mt)))
 
     def close(self):
         if getattr(self, "_h", None):

@@ -347,6 +347,86 @@ def flatten(scene):
     return np.concatenate(V), np.concatenate(F), np.concatenate(M), names
 
 
+def flatten_uvs(scene):
+    """Texture coordinates of the flattened mesh: (uv [n, 2] float32, face uv
+    indices [faces, 4] uint32), or (None, None) when no object has "uvs".
+    An object's "face_uvs" index its own "uvs" (4th unused for triangles);
+    objects without uvs get their faces' first uv indices pointing at a
+    (0, 0) entry, which only an untextured material reads."""
+    if not any("uvs" in o for o in scene["objects"]):
+        return None, None
+    U, FU = [np.zeros((1, 2), np.float32)], []
+    base = 1
+    for o in scene["objects"]:
+        nf = len(o["faces"])
+        if "uvs" in o:
+            uv = np.asarray(o["uvs"], np.float32).reshape(-1, 2)
+            fu = np.asarray(o["face_uvs"], np.uint32).reshape(nf, 4).copy()
+            tri = np.asarray(o["faces"], np.uint32)[:, 3] == TRI
+            fu[:, :3] += base
+            fu[~tri, 3] += base
+            fu[tri, 3] = 0
+            U.append(uv)
+            FU.append(fu)
+            base += len(uv)
+        else:
+            FU.append(np.zeros((nf, 4), np.uint32))
+    return np.concatenate(U), np.concatenate(FU)
+
+
+def checker_image(w=16, h=16, c0=(0.9, 0.2, 0.1), c1=(0.1, 0.3, 0.8), seed=7):
+    """A w x h RGBA float32 image: a 4 x 4 checker of two colours with a
+    seeded per-texel tint (so the bilinear weights matter)."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w]
+    sel = ((x * 4 // w) + (y * 4 // h)) % 2 == 0
+    img = np.where(sel[..., None], np.asarray(c0, np.float32), np.asarray(c1, np.float32))
+    img = img * rng.uniform(0.7, 1.0, (h, w, 1)).astype(np.float32)
+    return np.concatenate([img, np.ones((h, w, 1), np.float32)], -1).astype(np.float32)
+
+
+def textured_cornell_scene(res=64, **kw):
+    """The Cornell box with image textures: the back wall carries uvs
+    (0..1 across it) and a UV-mapped checker texture (bilinear, repeat
+    x 2 / y 1); the tall box takes a second texture through global
+    coordinates with cube mapping (scale 2, offset, clip extend, no
+    interpolation).  Everything else is the plain Cornell box."""
+    sc = cornell_scene(res=res, **kw)
+    sc["textures"] = {
+        "checker": {"image": checker_image(16, 16), "interpolate": "bilinear", "clipping": "repeat",
+                    "xrepeat": 2, "yrepeat": 1, "texco": "uv", "mapping": "plain"},
+        "tiles": {"image": checker_image(8, 8, (0.8, 0.8, 0.3), (0.2, 0.7, 0.3), seed=11), "interpolate": "none",
+                  "clipping": "extend", "texco": "global", "mapping": "cube", "scale": (1.5, 1.5, 1.5),
+                  "offset": (0.1, 0.0, 0.2), "adj_intensity": 1.1, "adj_contrast": 0.9},
+    }
+    sc["materials"]["back_tex"] = ("shinydiffusemat", (0.75, 0.75, 0.75), {"diffuse_texture": "checker"})
+    sc["materials"]["box_tex"] = ("shinydiffusemat", (0.75, 0.75, 0.75), {"diffuse_texture": "tiles"})
+    objs = []
+    for o in sc["objects"]:
+        v = np.asarray(o["vertices"], np.float32)
+        f = np.asarray(o["faces"], np.uint32)
+        if o["name"] == "group0":
+            # the back wall's triangles (z = -1 plane) get their own textured object
+            back = np.all(np.abs(v[f[:, :3]][:, :, 2] + 1.0) < 1e-6, axis=1)
+            rest = f[~back]
+            fb = f[back]
+            used = np.unique(fb[:, :3])
+            remap = {int(u): i for i, u in enumerate(used)}
+            vb = v[used]
+            fbb = np.array([[remap[int(x)] for x in row[:3]] + [TRI] for row in fb], np.uint32)
+            uvs = np.stack([(vb[:, 0] + 1.0) * 0.5, vb[:, 1] * 0.5], -1).astype(np.float32)
+            fuv = np.concatenate([fbb[:, :3], np.zeros((len(fbb), 1), np.uint32)], 1)
+            objs.append({"name": "group0", "material": o["material"], "vertices": v, "faces": rest})
+            objs.append({"name": "back_wall", "material": "back_tex", "vertices": vb, "faces": fbb,
+                         "uvs": uvs, "face_uvs": fuv})
+        elif o["name"] == "group4":
+            objs.append({**o, "material": "box_tex"})
+        else:
+            objs.append(o)
+    sc["objects"] = objs
+    return sc
+
+
 def _box_tris(center, size, yaw, subdiv=1):
     """Triangles of a yawed box, each face subdivided into subdiv x subdiv
     quads (2 triangles each), outward-facing.  Returns (vertices, tri indices)."""

@@ -131,11 +131,39 @@ REF_RENDER = os.path.join(HERE, "_ref", "render_dump")
 def reference_scene_text(scene, spp, batches, threads=-1, offset_stride=None):
     """Scene dict (libyafaray_gb300.scenes) -> render_dump input text."""
     out = []
+    tex_keys = ("interpolate", "clipping", "xrepeat", "yrepeat", "cropmin_x", "cropmin_y", "cropmax_x", "cropmax_y",
+                "rot90", "adj_intensity", "adj_contrast", "adj_mult_factor_red", "adj_mult_factor_green",
+                "adj_mult_factor_blue", "adj_clamp")
+
+    def fmt(v):
+        if isinstance(v, bool):
+            return str(v).lower()
+        if isinstance(v, str):
+            return v
+        if isinstance(v, (tuple, list)):
+            return ",".join(repr(float(x)) for x in v)
+        return repr(v)
+    for tname, tx in scene.get("textures", {}).items():
+        img = np.asarray(tx["image"], np.float32)
+        h, w = img.shape[:2]
+        out.append(f"image {tname}_img {w} {h}")
+        out += [" ".join(repr(float(x)) for x in row.reshape(-1)) for row in img]
+        out.append(f"texture {tname} type=image image_name={tname}_img "
+                   + " ".join(f"{k}={fmt(tx[k])}" for k in tex_keys if k in tx))
     for name, m in scene["materials"].items():
         t = m[0]
         if t == "shinydiffusemat":
             extra = ""
             for k, v in (m[2] if len(m) > 2 else {}).items():
+                if k == "diffuse_texture":
+                    tx = scene["textures"][v]
+                    node = f"{name}_dtex"
+                    proj = tx.get("proj", (1, 2, 3))
+                    out.append(f"node name={node} type=texture_mapper texture={v} texco={tx.get('texco', 'global')} "
+                               f"mapping={tx.get('mapping', 'plain')} scale={fmt(tx.get('scale', (1.0, 1.0, 1.0)))} "
+                               f"offset={fmt(tx.get('offset', (0.0, 0.0, 0.0)))} proj_x={proj[0]} proj_y={proj[1]} proj_z={proj[2]}")
+                    extra += f" diffuse_shader={node}"
+                    continue
                 if isinstance(v, bool):
                     extra += f" {k}={str(v).lower()}"
                 elif isinstance(v, (tuple, list)):
@@ -164,6 +192,15 @@ def reference_scene_text(scene, spp, batches, threads=-1, offset_stride=None):
     for o in scene["objects"]:
         v = np.asarray(o["vertices"], np.float32)
         f = np.asarray(o["faces"], np.uint32)
+        if "uvs" in o:
+            uv = np.asarray(o["uvs"], np.float32).reshape(-1, 2)
+            fu = np.asarray(o["face_uvs"], np.uint32).reshape(len(f), 4)
+            out.append(f"object {o['name']} {o['material']} {len(v)} {len(f)} {len(uv)}")
+            out += [f"{float(a)!r} {float(b)!r} {float(c)!r}" for a, b, c in v]
+            out += [f"{float(a)!r} {float(b)!r}" for a, b in uv]
+            out += [" ".join(str(int(x)) for x in ((*row[:3], *fr[:3]) if row[3] == TRI_MARK else (*row, *fr)))
+                    for row, fr in zip(f, fu)]
+            continue
         out.append(f"object {o['name']} {o['material']} {len(v)} {len(f)}")
         out += [f"{float(a)!r} {float(b)!r} {float(c)!r}" for a, b, c in v]
         out += [" ".join(str(int(x)) for x in (row[:3] if row[3] == TRI_MARK else row)) for row in f]

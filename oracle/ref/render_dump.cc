@@ -14,7 +14,15 @@
 //   material NAME glossy R G B  SR SG SB  EXPONENT  GLOSSY_REFLECT  DIFFUSE_REFLECT
 //   material NAME rough_glass IOR ALPHA TRANSMIT_FILTER  FR FG FB  MR MG MB
 //   material NAME glass IOR TRANSMIT_FILTER  FR FG FB  MR MG MB
-//   object NAME MATERIAL NV NF   then NV lines "x y z", NF lines "a b c" or "a b c d"
+//   object NAME MATERIAL NV NF [NUV]   then NV lines "x y z", NUV lines "u v",
+//                                NF lines "a b c" / "a b c d" (with uvs also the
+//                                face's uv indices: "a b c ua ub uc")
+//   image NAME W H               then H lines of W x "r g b a" (an in-memory
+//                                ColorAlpha image, image_optimization none, LinearRGB)
+//   texture NAME key=value ...   (yafaray_createTexture: type=image image_name=...)
+//   node key=value ...           a shader node of the next material line
+//                                (e.g. name=tex0 type=texture_mapper texture=...);
+//                                the material names it (diffuse_shader=tex0)
 //   arealight CX CY CZ  P1X P1Y P1Z  P2X P2Y P2Z  R G B  POWER SAMPLES
 //   pointlight X Y Z  R G B  POWER
 //   camera FX FY FZ  TX TY TZ  UX UY UZ  RESX RESY FOCAL
@@ -131,6 +139,7 @@ int main(int argc, char **argv)
 	std::string filter_type = "box";
 	float pixel_width = 1.f;
 	int offset_stride = -1;
+	std::vector<yafaray_ParamMap *> pending_nodes;
 	std::vector<std::pair<std::string, std::string>> aa_kv;
 	std::string line;
 	while(std::getline(in, line))
@@ -179,12 +188,17 @@ int main(int argc, char **argv)
 				else setTyped(pm, key, val);
 			}
 			size_t id;
+			yafaray_clearParamMapList(pml);
+			for(yafaray_ParamMap *n : pending_nodes) yafaray_addParamMapToList(pml, n);
 			yafaray_createMaterial(scene, &id, name.c_str(), pm, pml);
+			for(yafaray_ParamMap *n : pending_nodes) yafaray_destroyParamMap(n);
+			pending_nodes.clear();
 		}
 		else if(kw == "object")
 		{
-			std::string name, mat; size_t nv, nf;
+			std::string name, mat; size_t nv, nf, nuv = 0;
 			ss >> name >> mat >> nv >> nf;
+			if(!(ss >> nuv)) nuv = 0;
 			size_t mat_id = 0;
 			yafaray_getMaterialId(scene, &mat_id, mat.c_str());
 			yafaray_setParamMapString(pm, "type", "mesh");
@@ -196,15 +210,63 @@ int main(int argc, char **argv)
 				double x, y, z; vs >> x >> y >> z;
 				yafaray_addVertex(scene, obj, x, y, z);
 			}
+			std::vector<size_t> uv_id;
+			for(size_t i = 0; i < nuv; ++i)
+			{
+				std::getline(in, line); std::istringstream us(line);
+				double u, v; us >> u >> v;
+				uv_id.push_back(yafaray_addUv(scene, obj, u, v));
+			}
 			for(size_t i = 0; i < nf; ++i)
 			{
 				std::getline(in, line); std::istringstream fs(line);
 				std::vector<size_t> ix; size_t k;
 				while(fs >> k) ix.push_back(k);
-				if(ix.size() == 3) yafaray_addTriangle(scene, obj, ix[0], ix[1], ix[2], mat_id);
+				if(nuv && ix.size() == 6) yafaray_addTriangleWithUv(scene, obj, ix[0], ix[1], ix[2], uv_id.at(ix[3]), uv_id.at(ix[4]), uv_id.at(ix[5]), mat_id);
+				else if(nuv && ix.size() == 8) yafaray_addQuadWithUv(scene, obj, ix[0], ix[1], ix[2], ix[3], uv_id.at(ix[4]), uv_id.at(ix[5]), uv_id.at(ix[6]), uv_id.at(ix[7]), mat_id);
+				else if(ix.size() == 3) yafaray_addTriangle(scene, obj, ix[0], ix[1], ix[2], mat_id);
 				else if(ix.size() == 4) yafaray_addQuad(scene, obj, ix[0], ix[1], ix[2], ix[3], mat_id);
 			}
 			yafaray_initObject(scene, obj, mat_id);
+		}
+		else if(kw == "image")
+		{
+			std::string name; int w, h;
+			ss >> name >> w >> h;
+			yafaray_setParamMapString(pm, "type", "ColorAlpha");
+			yafaray_setParamMapString(pm, "image_optimization", "none");
+			yafaray_setParamMapString(pm, "color_space", "LinearRGB");
+			yafaray_setParamMapInt(pm, "width", w);
+			yafaray_setParamMapInt(pm, "height", h);
+			size_t id = 0;
+			yafaray_createImage(scene, name.c_str(), &id, pm);
+			for(int y = 0; y < h; ++y)
+			{
+				std::getline(in, line); std::istringstream is(line);
+				for(int x = 0; x < w; ++x)
+				{
+					double r, g, b, a; is >> r >> g >> b >> a;
+					yafaray_setImageColor(scene, id, x, y, static_cast<float>(r), static_cast<float>(g), static_cast<float>(b), static_cast<float>(a));
+				}
+			}
+		}
+		else if(kw == "texture" || kw == "node")
+		{
+			std::string name;
+			if(kw == "texture") ss >> name;
+			yafaray_ParamMap *target = kw == "texture" ? pm : yafaray_createParamMap();
+			std::string kv;
+			while(ss >> kv)
+			{
+				const size_t eq = kv.find('=');
+				if(eq == std::string::npos) continue;
+				const std::string key = kv.substr(0, eq), val = kv.substr(eq + 1);
+				double a, b, c;
+				if(std::sscanf(val.c_str(), "%lf,%lf,%lf", &a, &b, &c) == 3) yafaray_setParamMapVector(target, key.c_str(), a, b, c);
+				else setTyped(target, key, val);
+			}
+			if(kw == "texture") yafaray_createTexture(scene, name.c_str(), pm);
+			else pending_nodes.push_back(target);
 		}
 		else if(kw == "arealight")
 		{

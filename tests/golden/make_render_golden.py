@@ -302,5 +302,14 @@ if __name__ == "__main__":
         variant_golden("cornell_tshadow_64_render.npz", shiny=("transparent",), glass=True, transparent_shadows=4)
         variant_golden("cornell_tshadow1_48_render.npz", res=48, batches=24, shiny=("transparent",), glass=True,
                        transparent_shadows=1)
+    if "cornell_textured" in what:
+        # image textures: a UV-mapped bilinear checker on the back wall and a
+        # cube-mapped global-coordinate texture on the tall box
+        sc = scenes.textured_cornell_scene(res=64)
+        rgb, secs = orc.run_reference_render(sc, 16, 32, threads=os.cpu_count() or 1)
+        np.savez_compressed(os.path.join(OUT, "cornell_textured_64_render.npz"), mean=rgb.mean(0).astype(np.float32),
+                            se=(rgb.std(0, ddof=1) / np.sqrt(32)).astype(np.float32), batches=np.int32(32),
+                            spp=np.int32(16), seconds=secs)
+        print(f"cornell_textured_64_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
     if "cornell_point" in what:
         variant_golden("cornell_point_64_render.npz", point_light=True)

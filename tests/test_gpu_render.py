@@ -129,6 +129,20 @@ def test_gpu_cornell_transparent_shadows_match_reference(cuda_device, name, res,
     assert f0 < frac - 0.01
 
 
+def test_gpu_cornell_textured_matches_reference(cuda_device):
+    """Image textures through texture-mapper nodes on shinydiffuse diffuse
+    colour: UV coordinates (bilinear, repeat x 2) on the back wall, global
+    coordinates with cube mapping, scale / offset, no interpolation, clip
+    extend and intensity / contrast adjustments on the tall box."""
+    g = np.load(os.path.join(GOLD, "cornell_textured_64_render.npz"))
+    r = gbrt.Renderer(scenes.textured_cornell_scene(res=64))
+    gb = batches(r, int(g["spp"]), int(g["batches"]))
+    frac, relmse, m = parity(gb, g["mean"], g["se"])
+    print(f"cornell textured 64x64: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
+          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
+    assert frac >= 0.995
+
+
 def test_gpu_cornell_shiny_layers_match_reference(cuda_device):
     """ShinyDiffuseMaterial's layers: a Fresnel mirror (specular_reflect 0.8,
     IOR 1.5), transparency 0.5 with transmit_filter 0.7 and translucency 0.3,
