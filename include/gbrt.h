@@ -453,6 +453,32 @@ int gbrt_dl_render(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt
                    float *film_dev, double *film64_dev, gbrt_pt_stats *stats, void *stream);
 int gbrt_dl_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *caustic,
                         float *image_out, gbrt_pt_stats *stats);
+
+/* ---- stochastic progressive photon mapping (the `SPPM` integrator) -------
+ * Replaces SppmIntegrator::render / prePass / photonWorker / traceGatherRay
+ * (src/integrator/surface/integrator_sppm.cc:99-1053).  Each of `passes`
+ * passes shoots `photons` photon paths (indirect deposits only, `bounces`
+ * deep), traces one eye sample per pixel at the multipass sample position of
+ * sample index base_sampling_offset + pass (emission, direct light at
+ * diffuse hits, the recursive glossy / specular split of traceGatherRay),
+ * gathers the caustic photons within each pixel's radius at diffuse hits,
+ * refines the radius (alpha 0.7) and adds acc_flux / (r^2 pi photons so far)
+ * + the eye sample's radiance to the film.  As in the reference, only the
+ * caustic map enters the estimate (its diffuse-map accumulation runs under
+ * debug logging only).  The initial radius comes from the scene bound and
+ * resolution (initializePpm); pmIRE is not built.  params: spp is ignored
+ * (one sample per pass), path_samples / bounces / russian roulette are not
+ * used; raydepth, transparent shadows and the film filter are. */
+typedef struct gbrt_sppm_params {
+	int32_t photons;            /* "photons" [500000] */
+	int32_t passes;             /* "passNums" [1000] */
+	int32_t bounces;            /* "bounces" [5] */
+} gbrt_sppm_params;
+
+int gbrt_sppm_render(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_sppm_params *sppm,
+                     float *film_dev, gbrt_pt_stats *stats, void *stream);
+int gbrt_sppm_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_sppm_params *sppm,
+                          float *image_out, gbrt_pt_stats *stats);
 /* Diagnostic: shoots one photon map (which = 0 diffuse, 1 caustic) and copies
  * its photons to host `out` [n][9] = (dir xyz, pos xyz, colour rgb) in
  * deposit order; n_photons and n_paths as PhotonMap::nPhotons / nPaths. */

@@ -145,6 +145,10 @@ struct Params {
 	uint32_t n_list;
 	// transparent shadows (MonteCarloIntegrator "transpShad", "shadowDepth")
 	int tshadow, shadow_depth;
+	// SPPM (pm == 3): per-pixel squared gather radius and this pass's
+	// photon flux (xyz) and photon count (w)
+	const float *sppm_r2;
+	float4 *sppm_pass;
 };
 
 struct Work {
@@ -2323,6 +2327,44 @@ __global__ void k_aa_compact(const uint8_t *__restrict__ flags, uint32_t n, uint
 		}
 }
 
+// ---- SPPM hit points (SppmIntegrator::HitPoint, integrator_sppm.h) ----
+__global__ void k_sppm_init(float4 *hp, float *r2, float4 *pass, uint32_t n, float r2_0)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	{
+		hp[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+		r2[i] = r2_0;
+		pass[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+	}
+}
+
+// Progressive refinement and the indirect estimate of one pass
+// (SppmIntegrator::renderTile, integrator_sppm.cc:278-292): with M photons
+// gathered, g = min((N + 0.7 M) / (N + M), 1), r^2 *= g, N += 0.7 M,
+// flux = (flux + pass flux) g; the pixel's sample adds flux / (r^2 pi
+// photons so far).  hp = {flux xyz, N}.
+__global__ void k_sppm_update(Params P, float4 *hp, float *r2, float4 *pass, uint32_t n, float total_photons, float *film)
+{
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	{
+		float4 h = hp[i];
+		float r = r2[i];
+		const float4 g4 = pass[i];
+		if(g4.w > 0.f)
+		{
+			const float g = fminf(__fdiv_rn(xa(h.w, xm(0.7f, g4.w)), xa(h.w, g4.w)), 1.f);
+			r = xm(r, g);
+			h.w = xa(h.w, xm(g4.w, 0.7f));
+			h.x = xm(xa(h.x, g4.x), g); h.y = xm(xa(h.y, g4.y), g); h.z = xm(xa(h.z, g4.z), g);
+			hp[i] = h;
+			r2[i] = r;
+		}
+		pass[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+		const float inv = __fdiv_rn(1.f, xm(xm(r, kPi), total_photons));
+		film_put(P, film, nullptr, i, 0u, xm(h.x, inv), xm(h.y, inv), xm(h.z, inv));
+	}
+}
+
 // Rgba::normalized (color.h:294-298, 538-542): sum x (1 / weight), 0 where the weight is 0.
 __global__ void k_normalize(const float *sum, const double *sum64, const float *w, float *out, size_t n)
 {
@@ -2389,6 +2431,12 @@ struct PhotonJob {
 	uint32_t *count;          // [0] photons, [1] radiance points
 	uint32_t cap, rp_cap;
 	float4 *rp_pos, *rp_nrm, *rp_refl, *rp_transm;
+	// SPPM (SppmIntegrator::photonWorker, integrator_sppm.cc:353-505): photon
+	// i of this pass is number base + i of the render; emission samples
+	// from Halton bases 2 / 3 / 5 / 7, scattering over every BSDF
+	// component, deposits only of indirect photons
+	int sppm;
+	uint32_t base;
 };
 
 // sample::sphere (include/sampler/sample.h:56-74), FAST_TRIG
@@ -2446,10 +2494,21 @@ __global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJo
 	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
 	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < J.n; i += gridDim.x * blockDim.x)
 	{
-		const float s1 = gbrt::ri_vdc(i);
-		const float s2 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 2, i));
-		const float s3 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 3, i));
-		const float s4 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 4, i));
+		const uint32_t pi = J.base + i;
+		float s1, s2, s3, s4;
+		if(J.sppm)
+		{
+			// hal_1_ .. hal_4_ {2, 0}, {3, 0}, {5, 0}, {7, 0}: the n-th getNext is index n
+			s1 = gbrt::radical_inverse(pi + 1u, 2); s2 = gbrt::radical_inverse(pi + 1u, 3);
+			s3 = gbrt::radical_inverse(pi + 1u, 5); s4 = gbrt::radical_inverse(pi + 1u, 7);
+		}
+		else
+		{
+			s1 = gbrt::ri_vdc(i);
+			s2 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 2, i));
+			s3 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 3, i));
+			s4 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 4, i));
+		}
 		const float s_l = J.caustic ? static_cast<float>(i) / static_cast<float>(J.n) : static_cast<float>(i) * J.inv_n;
 		uint32_t ln = 0;
 		if(s_l >= 1.f) ln = J.n_lights - 1u;
@@ -2493,7 +2552,7 @@ __global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJo
 			surface_color(sc, s, h.prim, h.u, h.v);
 			const float wi[3] = {-d[0], -d[1], -d[2]};
 			const uint32_t mf = s.m->flags;
-			const bool dep = J.caustic ? ((mf & (BF_DIFFUSE | BF_GLOSSY)) && caustic) : ((mf & BF_DIFFUSE) && !caustic);
+			const bool dep = (!J.sppm || !direct) && (J.caustic ? ((mf & (BF_DIFFUSE | BF_GLOSSY)) && caustic) : ((mf & BF_DIFFUSE) && !caustic));
 			const uint32_t slot = append_slot(J.count, dep);
 			if(dep && slot < J.cap)
 			{
@@ -2521,10 +2580,10 @@ __global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJo
 			if(nb == J.max_bounces) break;
 			// Material::scatterPhoton (src/material/material.cc:179-196)
 			const int d5 = 3 * nb + 5;
-			const float s5 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d5, i));
-			const float s6 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d5 + 1, i));
-			const float s7 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d5 + 2, i));
-			const uint32_t flags = J.caustic ? (BF_SPECULAR | BF_REFLECT | BF_TRANSMIT | BF_GLOSSY | BF_FILTER | BF_DISPERSIVE) : BF_ALL;
+			const float s5 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d5, pi));
+			const float s6 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d5 + 1, pi));
+			const float s7 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d5 + 2, pi));
+			const uint32_t flags = J.caustic && !J.sppm ? (BF_SPECULAR | BF_REFLECT | BF_TRANSMIT | BF_GLOSSY | BF_FILTER | BF_DISPERSIVE) : BF_ALL;
 			float wo[3], scol[3], w, pdf;
 			uint32_t sf;
 			mat_sample(s, wi, s5, s6, flags, wo, scol, w, pdf, sf);
@@ -2539,7 +2598,7 @@ __global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJo
 			caustic = ((sf & (BF_GLOSSY | BF_SPECULAR | BF_DISPERSIVE)) && direct) ||
 			          ((sf & (BF_GLOSSY | BF_SPECULAR | BF_FILTER | BF_DISPERSIVE)) && caustic);
 			direct = (sf & BF_FILTER) && direct;
-			if(J.caustic && !(caustic || direct)) break;
+			if(J.caustic && !J.sppm && !(caustic || direct)) break;
 			for(int k = 0; k < 3; ++k) { o[k] = s.p[k]; d[k] = wo[k]; }
 			tmin = kRayMinDist;
 		}
@@ -2579,6 +2638,34 @@ __global__ void __launch_bounds__(kThreads) k_pm_root(SceneDev sc, Params P, Wor
 		coords_system(s.n, s.u, s.v);
 		surface_color(sc, s, prim, h.z, h.w);
 		const float wo[3] = {-dir[0], -dir[1], -dir[2]};
+		if(P.pm == 3)
+		{
+			// SppmIntegrator::traceGatherRay (integrator_sppm.cc:727-748): every
+			// caustic photon within the pixel's radius, f(wo, photon dir) x
+			// photon colour; the count weighted 1 / (glossy split product)
+			if(!P.g_caustic.n) continue;
+			const uint32_t pixel = W.p_pixel[path];
+			const float r2 = P.sppm_r2[pixel];
+			float flux[3] = {0.f, 0.f, 0.f};
+			uint32_t cnt = 0;
+			gbrt::grid_range(P.g_caustic, s.p, r2, [&](uint32_t j) {
+				const float4 pd = __ldg(P.g_caustic.dir + j), pc = __ldg(P.g_caustic.col + j);
+				const float pdir[3] = {pd.x, pd.y, pd.z};
+				float sc3[3];
+				eval_flags(s, wo, pdir, BF_ALL, sc3);
+				flux[0] += sc3[0] * pc.x; flux[1] += sc3[1] * pc.y; flux[2] += sc3[2] * pc.z;
+				++cnt;
+			});
+			if(cnt)
+			{
+				const float4 t4 = W.p_thr[path];
+				const uint32_t division = max(1u, W.p_task[path].x >> 16);
+				float *acc = reinterpret_cast<float *>(P.sppm_pass + pixel);
+				atomicAdd(acc, flux[0] * t4.x); atomicAdd(acc + 1, flux[1] * t4.y); atomicAdd(acc + 2, flux[2] * t4.z);
+				atomicAdd(acc + 3, static_cast<float>(cnt) / static_cast<float>(division));
+			}
+			continue;
+		}
 		float est[3] = {0.f, 0.f, 0.f};
 		uint32_t idx[gbrt::kMaxGather];
 		float d2[gbrt::kMaxGather];
@@ -3149,7 +3236,7 @@ struct ShotMap {
 // One photon map: shoots n photon paths, keeps the deposits (and, for the
 // diffuse map with final gather, the radiance points).
 int shoot_map(gbrt_scene *S, const SceneDev &sc, bool caustic, uint32_t n, int max_bounces, bool radiance_points, uint32_t seed,
-              ShotMap &M, cudaStream_t s)
+              ShotMap &M, cudaStream_t s, bool sppm = false, uint32_t base = 0)
 {
 	M.paths = n;
 	M.n = M.n_rp = 0;
@@ -3187,6 +3274,8 @@ int shoot_map(gbrt_scene *S, const SceneDev &sc, bool caustic, uint32_t n, int m
 	J.light_cdf = dcdf.as<float>();
 	J.light_pdf = dpdf.as<float>();
 	J.seed = seed;
+	J.sppm = sppm ? 1 : 0;
+	J.base = base;
 	J.pos = M.pos.as<float4>(); J.dir = M.dir.as<float4>(); J.col = M.col.as<float4>();
 	J.count = M.count.as<uint32_t>();
 	J.cap = cap; J.rp_cap = rp_cap;
@@ -3577,6 +3666,19 @@ static int film_filter_table(uint32_t type, float pixel_width, float table[256],
 // One pass of an adaptive anti-aliasing render (TiledIntegrator::render /
 // renderPass): the pixels to sample (NULL: all), whether the render has
 // more than one pass (sample positions), the light sample multiplier.
+// The film filter of a render (ImageFilm's table and weights) into P.
+static int film_setup(gbrt_scene *S, const gbrt_pt_params &pp, Params &P, cudaStream_t s)
+{
+	if(pp.filter_type == GBRT_FILTER_PIXEL) return GBRT_OK;
+	if(!pp.film_weight_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: filter type %u needs film_weight_dev", pp.filter_type);
+	if(int rc = film_filter_table(pp.filter_type, pp.aa_pixel_width, S->filter_host, P.filter_width, P.filter_scale)) return rc;
+	if(!S->filter_dev) GBRT_CK(cudaMalloc(&S->filter_dev, sizeof(S->filter_host)));
+	GBRT_CK(cudaMemcpyAsync(S->filter_dev, S->filter_host, sizeof(S->filter_host), cudaMemcpyHostToDevice, s));
+	P.film_w = pp.film_weight_dev;
+	P.filter_tab = S->filter_dev;
+	return GBRT_OK;
+}
+
 struct AaPass {
 	const uint32_t *list;
 	uint32_t n_list;
@@ -3661,15 +3763,7 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	P.n_list = aa ? aa->n_list : 0u;
 	P.tshadow = pp.transparent_shadows ? 1 : 0;
 	P.shadow_depth = pp.shadow_depth;
-	if(pp.filter_type != GBRT_FILTER_PIXEL)
-	{
-		if(!pp.film_weight_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: filter type %u needs film_weight_dev", pp.filter_type);
-		if(int rc = film_filter_table(pp.filter_type, pp.aa_pixel_width, S->filter_host, P.filter_width, P.filter_scale)) return rc;
-		if(!S->filter_dev) GBRT_CK(cudaMalloc(&S->filter_dev, sizeof(S->filter_host)));
-		GBRT_CK(cudaMemcpyAsync(S->filter_dev, S->filter_host, sizeof(S->filter_host), cudaMemcpyHostToDevice, s));
-		P.film_w = pp.film_weight_dev;
-		P.filter_tab = S->filter_dev;
-	}
+	if(int rc = film_setup(S, pp, P, s)) return rc;
 	if(pm)
 	{
 		P.pm = pm->pm; P.pm_fg = pm->pm_fg; P.pm_fg_bounces = pm->pm_fg_bounces; P.pm_gather_dist = pm->pm_gather_dist;
@@ -3677,6 +3771,7 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 		P.pm_caustic_r2 = pm->pm_caustic_r2; P.pm_caustic_k = pm->pm_caustic_k; P.pm_diffuse_paths = pm->pm_diffuse_paths;
 		P.pm_caustic_paths = pm->pm_caustic_paths; P.pm_lookup_r2 = pm->pm_lookup_r2;
 		P.g_diffuse = pm->g_diffuse; P.g_caustic = pm->g_caustic; P.g_radiance = pm->g_radiance;
+		P.sppm_r2 = pm->sppm_r2; P.sppm_pass = pm->sppm_pass;
 	}
 	P.base_offset = pp.base_sampling_offset; P.seed = pp.seed;
 	P.d1 = 1.f / static_cast<float>(pp.spp);
@@ -4287,6 +4382,119 @@ int gbrt_pm_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 		stats->photon_ms = photon_ms;
 	}
 	return rc;
+}
+
+// SppmIntegrator::render (integrator_sppm.cc:99-201): initializePpm, then per
+// pass the photon pass (prePass: the caustic photons of this pass's photon
+// paths, gridded with cells of the initial radius, which bounds every later
+// one), one eye sample per pixel and the hit points' refinement.
+static int sppm_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params &pp, const gbrt_sppm_params &q, float *film,
+                       gbrt_pt_stats *stats, cudaStream_t s)
+{
+	const uint32_t n_pix = static_cast<uint32_t>(camera->resx) * static_cast<uint32_t>(camera->resy);
+	float bound[6];
+	if(int rc = gbrt_bvh_get_bound(S->bvh, bound)) return rc;
+	const float lo[3] = {bound[0], bound[1], bound[2]};
+	// initializePpm (:1054-1073): the scene bound's mean edge over the mean resolution, x 2, at most 1
+	float r0 = (((bound[3] - bound[0]) + (bound[4] - bound[1]) + (bound[5] - bound[2])) / 3.f) /
+	           (static_cast<float>(camera->resx + camera->resy) / 2.0f) * 2.f;
+	r0 = std::min(r0, 1.f);
+	DevBuf hp, r2, pass;
+	if(int rc = hp.alloc(16ull * n_pix)) return rc;
+	if(int rc = r2.alloc(4ull * n_pix)) return rc;
+	if(int rc = pass.alloc(16ull * n_pix)) return rc;
+	k_sppm_init<<<grid_for(n_pix, S->n_sm), kThreads, 0, s>>>(hp.as<float4>(), r2.as<float>(), pass.as<float4>(), n_pix, (r0 * 1.f) * (r0 * 1.f));
+	GBRT_CK(cudaGetLastError());
+	const SceneDev sc = scene_dev(S);
+	Params M{};
+	M.pm = 3;
+	M.pm_diffuse = 1;          // launches the root gather (k_pm_root)
+	M.pm_caustics = 1;
+	M.sppm_r2 = r2.as<float>();
+	M.sppm_pass = pass.as<float4>();
+	gbrt_pt_params e = pp;
+	e.spp = 1;
+	e.guide = nullptr; e.guide_alpha = 0.f; e.guide_train_steps = 0;
+	Params F{};                // the film view of the refinement kernel
+	F.spp = 1; F.path_samples = 1; F.d1 = 1.f;
+	F.film_resx = camera->resx; F.film_resy = camera->resy;
+	F.aa_multipass = 1;
+	if(int rc = film_setup(S, pp, F, s)) return rc;
+	const AaPass multipass{nullptr, 0, 1, 1.f};
+	gbrt_pt_stats sum{}, one{};
+	uint64_t total = 0, stored = 0;
+	const uint32_t n_ph = static_cast<uint32_t>(q.photons);
+	for(int i = 0; i < q.passes; ++i)
+	{
+		ShotMap C;
+		GridStore GC;
+		// photon paths of sample index base_sampling_offset + i: one render's
+		// passes use the Halton indices the reference's generators run through,
+		// renders at disjoint sample offsets disjoint photon paths
+		const uint64_t base = (static_cast<uint64_t>(pp.base_sampling_offset) + static_cast<uint64_t>(i)) * n_ph;
+		if(base + n_ph >= (1ull << 32)) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_sppm_render: more than 2^32 photon paths");
+		if(int rc = shoot_map(S, sc, true, n_ph, q.bounces, false, pp.seed, C, s, true, static_cast<uint32_t>(base))) return rc;
+		total += n_ph;
+		stored += C.n;
+		if(int rc = build_grid(C.pos.as<float4>(), C.dir.as<float4>(), C.col.as<float4>(), C.n, r0, lo, S->n_sm, GC, s)) return rc;
+		M.g_caustic = GC.g;
+		e.base_sampling_offset = pp.base_sampling_offset + static_cast<uint32_t>(i);
+		if(int rc = render_locked(S, camera, e, &M, film, nullptr, stats ? &one : nullptr, s, &multipass)) return rc;
+		F.base_offset = e.base_sampling_offset;
+		k_sppm_update<<<grid_for(n_pix, S->n_sm), kThreads, 0, s>>>(F, hp.as<float4>(), r2.as<float>(), pass.as<float4>(), n_pix,
+		                                                         static_cast<float>(total), film);
+		GBRT_CK(cudaGetLastError());
+		GBRT_CK(cudaStreamSynchronize(s));     // the pass's photon buffers are freed at the end of the iteration
+		if(stats)
+		{
+			sum.camera_samples += one.camera_samples; sum.extension_rays += one.extension_rays;
+			sum.shadow_rays += one.shadow_rays; sum.ms += one.ms;
+		}
+	}
+	if(stats)
+	{
+		*stats = sum;
+		stats->photon_paths = total;
+		stats->photons_stored = stored;
+	}
+	return GBRT_OK;
+}
+
+int gbrt_sppm_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_sppm_params *sppm,
+                     float *film_dev, gbrt_pt_stats *stats, void *stream)
+{
+	if(!S || !camera || !params || !sppm || !film_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_sppm_render: NULL argument");
+	if(sppm->photons < 1 || sppm->passes < 1 || sppm->bounces < 0 || camera->resx <= 0 || camera->resy <= 0)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_sppm_render: bad parameters (photons %d, passes %d, bounces %d)", sppm->photons,
+		                      sppm->passes, sppm->bounces);
+	std::lock_guard<std::mutex> lock(S->mu);
+	return sppm_locked(S, camera, *params, *sppm, film_dev, stats, static_cast<cudaStream_t>(stream));
+}
+
+int gbrt_sppm_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params_in, const gbrt_sppm_params *sppm,
+                          float *image_out, gbrt_pt_stats *stats)
+{
+	if(!S || !camera || !params_in || !sppm || !image_out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_sppm_render_host: NULL argument");
+	if(camera->resx <= 0 || camera->resy <= 0 || sppm->passes < 1) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_sppm_render_host: bad parameters");
+	const size_t n_pix = static_cast<size_t>(camera->resx) * camera->resy, n = 3 * n_pix;
+	gbrt_pt_params params = *params_in;
+	const bool filtered = params.filter_type != GBRT_FILTER_PIXEL;
+	DevBuf sum, mean, weight;
+	if(int rc = sum.alloc(n * 4)) return rc;
+	if(int rc = mean.alloc(n * 4)) return rc;
+	GBRT_CK(cudaMemset(sum.p, 0, n * 4));
+	if(filtered)
+	{
+		if(int rc = weight.alloc(n_pix * 4)) return rc;
+		GBRT_CK(cudaMemset(weight.p, 0, n_pix * 4));
+		params.film_weight_dev = weight.as<float>();
+	}
+	if(int rc = gbrt_sppm_render(S, camera, &params, sppm, sum.as<float>(), stats, nullptr)) return rc;
+	if(filtered) k_normalize<<<grid_for(n, S->n_sm), kThreads>>>(sum.as<float>(), nullptr, weight.as<float>(), mean.as<float>(), n);
+	else k_mean<<<grid_for(n, S->n_sm), kThreads>>>(sum.as<float>(), nullptr, mean.as<float>(), n, 1.f / static_cast<float>(sppm->passes));
+	GBRT_CK(cudaGetLastError());
+	GBRT_CK(cudaMemcpy(image_out, mean.p, n * 4, cudaMemcpyDeviceToHost));
+	return GBRT_OK;
 }
 
 int gbrt_pt_render_batch(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params, float *const *films,

@@ -126,6 +126,20 @@ __device__ __forceinline__ int knn_gather(const PhotonGrid &g, const float p[3],
 	return found;
 }
 
+// Every photon with d^2 < r2: f(index).
+template<typename F>
+__device__ __forceinline__ void grid_range(const PhotonGrid &g, const float p[3], float r2, F &&f)
+{
+	grid_visit(g, p, [&](uint32_t first, uint32_t end) {
+		for(uint32_t j = first; j < end; ++j)
+		{
+			const float4 q = __ldg(g.pos + j);
+			const float vx = q.x - p[0], vy = q.y - p[1], vz = q.z - p[2];
+			if(vx * vx + vy * vy + vz * vz < r2) f(j);
+		}
+	});
+}
+
 // Nearest photon with dir . n > 0 and d^2 < r2; -1 if none.
 __device__ __forceinline__ int find_nearest(const PhotonGrid &g, const float p[3], const float n[3], float r2)
 {

@@ -78,6 +78,16 @@ class AaParams(ctypes.Structure):
                 ("variance_pixels", ctypes.c_int32)]
 
 
+class SppmParams(ctypes.Structure):
+    _fields_ = [("photons", ctypes.c_int32), ("passes", ctypes.c_int32), ("bounces", ctypes.c_int32)]
+
+
+def sppm_params(it):
+    """gbrt_sppm_params from an "SPPM" integrator dict (SppmIntegrator's
+    parameter names and defaults, integrator_sppm.h:79-86)."""
+    return SppmParams(int(it.get("photons", 500000)), int(it.get("passNums", 1000)), int(it.get("bounces", 5)))
+
+
 class TextureDesc(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("rgba", ctypes.c_void_p),
                 ("interpolate", ctypes.c_uint32), ("clipping", ctypes.c_uint32), ("xrepeat", ctypes.c_int32),
@@ -238,6 +248,10 @@ SIGNATURES = {
     "gbrt_aa_flags": (_I, [_VP, _VP, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(AaParams), ctypes.c_float, _VP,
                            ctypes.POINTER(ctypes.c_uint32)]),
     "gbrt_scene_set_textures": (_I, [_VP, _VP, _U32, _VP, ctypes.POINTER(TextureDesc), _U32, _VP, _U32]),
+    "gbrt_sppm_render": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), ctypes.POINTER(SppmParams), _VP,
+                              ctypes.POINTER(PtStats), _VP]),
+    "gbrt_sppm_render_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), ctypes.POINTER(SppmParams), _VP,
+                                   ctypes.POINTER(PtStats)]),
 }
 
 _lib = None
@@ -537,6 +551,10 @@ class Renderer:
             pm = pm_params(self.scene["integrator"])
             fn = load().gbrt_pm_render_host if self.kind == "photonmapping" else load().gbrt_dl_render_host
             check(fn(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.byref(pm), _ptr(img), ctypes.byref(st)))
+        elif self.kind == "SPPM":
+            sp = sppm_params(self.scene["integrator"])
+            check(load().gbrt_sppm_render_host(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.byref(sp), _ptr(img),
+                                               ctypes.byref(st)))
         else:
             check(load().gbrt_pt_render_host(self._h, ctypes.byref(cam), ctypes.byref(p), _ptr(img), ctypes.byref(st)))
         return img, {"camera_samples": st.camera_samples, "extension_rays": st.extension_rays,

@@ -427,6 +427,16 @@ def textured_cornell_scene(res=64, **kw):
     return sc
 
 
+def cornell_sppm_scene(res=48, photons=100000, passes=8, bounces=5):
+    """The glass Cornell box (a glass and a rough-glass ball) rendered by the
+    "SPPM" integrator: caustics under the balls come from the photon
+    gathers, the rest from direct light and the specular split."""
+    sc = cornell_scene(res=res, glass=True)
+    sc["integrator"] = {"type": "SPPM", "photons": int(photons), "passNums": int(passes), "bounces": int(bounces),
+                        "raydepth": 5}
+    return sc
+
+
 def _box_tris(center, size, yaw, subdiv=1):
     """Triangles of a yawed box, each face subdivided into subdiv x subdiv
     quads (2 triangles each), outward-facing.  Returns (vertices, tri indices)."""

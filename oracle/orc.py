@@ -255,10 +255,11 @@ def run_reference_aa(scene, spp, batches, offset_stride, threads=-1):
     return rgb, secs, passes
 
 
-def run_reference_render(scene, spp, batches, threads=-1):
+def run_reference_render(scene, spp, batches, threads=-1, offset_stride=None):
     """Render with the compiled reference; returns (rgb [K,H,W,3] float32,
-    seconds per batch)."""
-    text = reference_scene_text(scene, spp, batches, threads)
+    seconds per batch).  Batch k renders at adv_base_sampling_offset
+    k x offset_stride (default spp)."""
+    text = reference_scene_text(scene, spp, batches, threads, offset_stride)
     with tempfile.TemporaryDirectory() as d:
         fin, fout = os.path.join(d, "scene.txt"), os.path.join(d, "out.bin")
         open(fin, "w").write(text)

@@ -62,6 +62,7 @@
 #include "integrator/surface/integrator_photon_mapping.h"
 #include "render/imagefilm.h"
 #include "image/image_layers.h"
+#include "integrator/surface/integrator_sppm.h"
 #undef private
 #undef protected
 
@@ -140,6 +141,16 @@ int main(int argc, char **argv)
 	float pixel_width = 1.f;
 	int offset_stride = -1;
 	std::vector<yafaray_ParamMap *> pending_nodes;
+	std::string integrator_type;
+	std::vector<std::pair<std::string, std::string>> integrator_kv;
+	auto make_integrator = [&]() {
+		yafaray_ParamMap *ip = yafaray_createParamMap();
+		yafaray_setParamMapString(ip, "type", integrator_type.c_str());
+		for(const auto &kv : integrator_kv) setTyped(ip, kv.first, kv.second);
+		yafaray_SurfaceIntegrator *si = yafaray_createSurfaceIntegrator(logger, "integrator", ip);
+		yafaray_destroyParamMap(ip);
+		return si;
+	};
 	std::vector<std::pair<std::string, std::string>> aa_kv;
 	std::string line;
 	while(std::getline(in, line))
@@ -310,15 +321,14 @@ int main(int argc, char **argv)
 		}
 		else if(kw == "integrator")
 		{
-			std::string type; ss >> type;
-			yafaray_setParamMapString(pm, "type", type.c_str());
+			ss >> integrator_type;
 			std::string kv;
 			while(ss >> kv)
 			{
 				const auto eq = kv.find('=');
-				if(eq != std::string::npos) setTyped(pm, kv.substr(0, eq), kv.substr(eq + 1));
+				if(eq != std::string::npos) integrator_kv.emplace_back(kv.substr(0, eq), kv.substr(eq + 1));
 			}
-			integrator = yafaray_createSurfaceIntegrator(logger, "integrator", pm);
+			integrator = make_integrator();
 		}
 		else if(kw == "render") { ss >> spp >> batches >> threads; if(!(ss >> offset_stride)) offset_stride = -1; }
 		else if(kw == "film") ss >> filter_type >> pixel_width;
@@ -342,6 +352,26 @@ int main(int argc, char **argv)
 	AaDump aa;
 	for(int k = 0; k < batches; ++k)
 	{
+		// SPPM keeps its hit points and photon count in the integrator
+		// (integrator_sppm.h:110-113) and appends new hit points per render:
+		// every batch gets a fresh one
+		if(k > 0 && integrator_type == "SPPM")
+		{
+			yafaray_destroySurfaceIntegrator(integrator);
+			integrator = make_integrator();
+		}
+		if(integrator_type == "SPPM")
+		{
+			// its photon emission samples (hal_1_ .. hal_4_) start where batch k's
+			// first pass (sample offset k x stride) begins, so batches shoot
+			// disjoint photon paths: photon p of pass j uses Halton index
+			// (k stride + j) photons + p + 1
+			auto *sppm = dynamic_cast<yafaray::SppmIntegrator *>(reinterpret_cast<yafaray::SurfaceIntegrator *>(integrator));
+			unsigned photons = 500000;
+			for(const auto &kv : integrator_kv) if(kv.first == "photons") photons = static_cast<unsigned>(std::stoul(kv.second));
+			const unsigned start = static_cast<unsigned>(k) * static_cast<unsigned>(offset_stride >= 0 ? offset_stride : spp) * photons;
+			if(sppm) { sppm->hal_1_.setStart(start); sppm->hal_2_.setStart(start); sppm->hal_3_.setStart(start); sppm->hal_4_.setStart(start); }
+		}
 		yafaray_clearParamMap(pm);
 		yafaray_setParamMapInt(pm, "width", resx);
 		yafaray_setParamMapInt(pm, "height", resy);

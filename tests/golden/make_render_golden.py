@@ -311,5 +311,14 @@ if __name__ == "__main__":
                             se=(rgb.std(0, ddof=1) / np.sqrt(32)).astype(np.float32), batches=np.int32(32),
                             spp=np.int32(16), seconds=secs)
         print(f"cornell_textured_64_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
+    if "cornell_sppm" in what:
+        # SPPM: the glass Cornell box, 100,000 photon paths x 8 passes; batch k
+        # at sample offsets 8k .. 8k + 7 (a fresh integrator per batch)
+        sc = scenes.cornell_sppm_scene(res=48, photons=100000, passes=8)
+        rgb, secs = orc.run_reference_render(sc, 1, 24, threads=os.cpu_count() or 1, offset_stride=8)
+        np.savez_compressed(os.path.join(OUT, "cornell_sppm_48_render.npz"), mean=rgb.mean(0).astype(np.float32),
+                            se=(rgb.std(0, ddof=1) / np.sqrt(24)).astype(np.float32), batches=np.int32(24), passes=np.int32(8),
+                            photons=np.int32(100000), seconds=secs)
+        print(f"cornell_sppm_48_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
     if "cornell_point" in what:
         variant_golden("cornell_point_64_render.npz", point_light=True)

@@ -143,6 +143,20 @@ def test_gpu_cornell_textured_matches_reference(cuda_device):
     assert frac >= 0.995
 
 
+def test_gpu_cornell_sppm_matches_reference(cuda_device):
+    """SPPM (SppmIntegrator): per pass a caustic photon map, one eye sample per
+    pixel with direct light and the specular / glossy split, the caustic
+    gather within each pixel's shrinking radius and the progressive update."""
+    g = np.load(os.path.join(GOLD, "cornell_sppm_48_render.npz"))
+    passes = int(g["passes"])
+    r = gbrt.Renderer(scenes.cornell_sppm_scene(res=48, photons=int(g["photons"]), passes=passes))
+    gb = np.stack([r.render(1, base_offset=b * passes, seed=1000 + b)[0] for b in range(int(g["batches"]))])
+    frac, relmse, m = parity(gb, g["mean"], g["se"])
+    print(f"cornell SPPM 48x48: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
+          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
+    assert frac >= 0.99
+
+
 def test_gpu_cornell_shiny_layers_match_reference(cuda_device):
     """ShinyDiffuseMaterial's layers: a Fresnel mirror (specular_reflect 0.8,
     IOR 1.5), transparency 0.5 with transmit_filter 0.7 and translucency 0.3,
