@@ -209,6 +209,63 @@ def coherent_traversal_section():
             "oracle_sample_agreement": agree, "oracle_sample": 20000}
 
 
+def next_rows_section():
+    """The rows built beyond the core path, each at 512x512 on the Cornell
+    box: adaptive anti-aliasing passes, transparent shadows, image textures
+    and SPPM; device time per frame beside the reference's CPU time for the
+    same configuration."""
+    import torch
+    from libyafaray_gb300 import gbrt, scenes
+    out = {}
+    ref_note = "reference: oracle/_ref render_dump, same configuration, 8 x86 cores (16 threads)"
+
+    def frame_ms(r, spp, reps=3):
+        film = torch.zeros(512 * 512 * 3, dtype=torch.float32, device="cuda")
+        r.render_device(spp, film.data_ptr())
+        return min(r.render_device(spp, film.data_ptr(), base_offset=spp * (k + 1), stats=True)["ms"] for k in range(reps))
+
+    # adaptive AA: gauss film, AA_passes 4 from 8 samples, inc 4, threshold 0.02
+    sc = scenes.cornell_scene(res=512)
+    sc["film"] = {"filter_type": "gauss", "AA_pixelwidth": 1.5, "AA_passes": 4, "AA_minsamples": 8, "AA_inc_samples": 4,
+                  "AA_threshold": 0.02}
+    r = gbrt.Renderer(sc)
+    film = torch.zeros(512 * 512 * 3, dtype=torch.float32, device="cuda")
+    w = torch.zeros(512 * 512, dtype=torch.float32, device="cuda")
+    r.render_aa_device(film.data_ptr(), w.data_ptr())
+    times, res = [], None
+    for k in range(3):
+        film.zero_(); w.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = r.render_aa_device(film.data_ptr(), w.data_ptr(), base_offset=1000 * (k + 1))
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    out["adaptive_aa_cornell"] = {"workload": "Cornell 512x512, gauss film 1.5, AA_passes 4, AA_minsamples 8, AA_inc_samples 4, "
+                                              "AA_threshold 0.02", "ms_per_frame": 1e3 * min(times), "pixels_per_pass": res,
+                                  "reference_s": 6.34, "reference_note": ref_note}
+    del r
+    r = gbrt.Renderer(scenes.cornell_scene(res=512, shiny=("transparent",), glass=True, transparent_shadows=4))
+    out["transparent_shadows_cornell"] = {"workload": "Cornell 512x512 16 spp, transparent box + fake_shadows glass balls, "
+                                                      "transpShad, shadowDepth 4", "ms_per_frame": frame_ms(r, 16),
+                                          "reference_s": 17.2, "reference_note": ref_note}
+    del r
+    r = gbrt.Renderer(scenes.textured_cornell_scene(res=512))
+    out["textured_cornell"] = {"workload": "Cornell 512x512 16 spp, UV-mapped bilinear checker + cube-mapped global texture",
+                               "ms_per_frame": frame_ms(r, 16), "reference_s": 4.39, "reference_note": ref_note}
+    del r
+    r = gbrt.Renderer(scenes.cornell_sppm_scene(res=512, photons=1_000_000, passes=16))
+    r.render(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, st = r.render(1, base_offset=16)
+    torch.cuda.synchronize()
+    out["sppm_glass_cornell"] = {"workload": "glass Cornell 512x512, SPPM 1,000,000 photon paths x 16 passes",
+                                 "ms_per_frame": 1e3 * (time.perf_counter() - t0), "reference_s": 19.8,
+                                 "reference_note": ref_note}
+    del r
+    return out
+
+
 def render_sections(args):
     """Cornell path tracing throughput and the guided-vs-plain time to
     relMSE 0.01 on the indoor scene (against an FP64-accumulated plain
@@ -439,6 +496,7 @@ def main():
     render = None if args.no_render else render_sections(args)
     if render is not None:
         render["traversal_coherent_2M"] = coherent_traversal_section()
+        render["beyond_core_path"] = next_rows_section()
 
     if rank != 0:
         if dist:
