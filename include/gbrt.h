@@ -352,7 +352,18 @@ typedef struct gbrt_texture_desc {
 	float scale[3];             /* [1, 1, 1] */
 	float offset[3];            /* [0, 0, 0] */
 	int32_t proj[3];            /* proj_x, proj_y, proj_z: 0 zero, 1 x, 2 y, 3 z [1, 2, 3] */
+	/* optional LayerNode over the mapper (src/shader/shader_node_layer.cc:110-193;
+	 * colour part, colour input, no upper layer): the material's diffuse
+	 * shader is then the layer */
+	int32_t layer;              /* 0: the mapper is the diffuse shader; 1: a layer node over it */
+	uint32_t blend_mode;        /* GBRT_BLEND_* ["mix"] */
+	float colfac;               /* [1] */
+	float upper_color[4];       /* [0, 0, 0, 0] (exporters pass the material colour, alpha 1) */
+	float def_col[3];           /* [1, 1, 1] */
+	int32_t negative, no_rgb, stencil;   /* "negative", "noRGB", "stencil" [0] */
 } gbrt_texture_desc;
+enum { GBRT_BLEND_MIX = 0, GBRT_BLEND_ADD = 1, GBRT_BLEND_MULTIPLY = 2, GBRT_BLEND_SUBTRACT = 3, GBRT_BLEND_SCREEN = 4,
+       GBRT_BLEND_DIVIDE = 5, GBRT_BLEND_DIFFERENCE = 6, GBRT_BLEND_DARKEN = 7, GBRT_BLEND_LIGHTEN = 8 };
 
 /* Texture coordinates and textures of a scene (replacing any set before).
  * uv: n_uv (u, v) pairs (yafaray_addUv); face_uv: one uint32 quadruple per

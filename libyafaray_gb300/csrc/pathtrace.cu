@@ -81,6 +81,8 @@ struct DevTexture {
 	float intensity, contrast, mult[3];
 	float scale[3], offset2[3]; // offset2 = 2 x offset (shader_node_texture.h:108)
 	int proj[3];
+	int layer, blend, negative, no_rgb, stencil;   // LayerNode over the mapper
+	float colfac, upper[4], def_col[3];
 };
 
 struct DevLight {
@@ -738,6 +740,52 @@ __device__ __forceinline__ void tex_axis(float cf, int res, bool repeat, int &c1
 	}
 }
 
+// LayerNode::eval, colour part (shader_node_layer.cc:110-171) with the
+// mapper's colour as input and no upper layer, and textureRgbBlend
+// (:264-316): rgb = the mapper's colour in, the layer's colour out.
+__device__ void tex_layer(const DevTexture &T, float ta, float rgb[3])
+{
+	if(!T.layer) return;
+	float tex[3] = {rgb[0], rgb[1], rgb[2]};
+	float stencil_tin = T.upper[3];
+	float tin = 0.f;
+	bool tex_rgb = true;
+	if(T.no_rgb) { tin = xa(xa(xm(0.2126f, tex[0]), xm(0.7152f, tex[1])), xm(0.0722f, tex[2])); tex_rgb = false; }
+	if(T.negative)
+	{
+		if(tex_rgb) for(int k = 0; k < 3; ++k) tex[k] = xs(1.f, tex[k]);
+		tin = xs(1.f, tin);
+	}
+	if(T.stencil)
+	{
+		if(tex_rgb) { const float f = ta; ta = xm(ta, stencil_tin); stencil_tin = xm(stencil_tin, f); }
+		else { const float f = tin; tin = xm(tin, stencil_tin); stencil_tin = xm(stencil_tin, f); }
+	}
+	if(!tex_rgb) for(int k = 0; k < 3; ++k) tex[k] = T.def_col[k];
+	else tin = ta;
+	const float tt = tin > 1.f ? 1.f : (tin < 0.f ? 0.f : tin);
+	const float facg = xm(stencil_tin, T.colfac);
+	const float fact = xm(tt, facg);
+	for(int k = 0; k < 3; ++k)
+	{
+		const float t = tex[k], o = T.upper[k];
+		float v;
+		switch(T.blend)
+		{
+			case GBRT_BLEND_MULTIPLY: v = xm(xa(xs(1.f, facg), xm(fact, t)), o); break;
+			case GBRT_BLEND_SCREEN: v = xs(1.f, xm(xa(xs(1.f, facg), xm(fact, xs(1.f, t))), xs(1.f, o))); break;
+			case GBRT_BLEND_SUBTRACT: v = xs(o, xm(fact, t)); break;
+			case GBRT_BLEND_ADD: v = xa(o, xm(fact, t)); break;
+			case GBRT_BLEND_DIVIDE: v = xa(xm(xs(1.f, fact), o), xm(xm(fact, o), t != 0.f ? __fdiv_rn(1.f, t) : 0.f)); break;
+			case GBRT_BLEND_DIFFERENCE: v = xa(xm(xs(1.f, fact), o), xm(fact, fabsf(xs(t, o)))); break;
+			case GBRT_BLEND_DARKEN: v = xm(fact, t) > o ? o : xm(fact, t); break;
+			case GBRT_BLEND_LIGHTEN: v = xm(fact, t) < o ? o : xm(fact, t); break;
+			default: v = xa(xm(fact, t), xm(xs(1.f, fact), o)); break;
+		}
+		rgb[k] = v < 0.f ? 0.f : v;
+	}
+}
+
 // TextureMapperNode::getCoords / doMapping (shader_node_texture.cc:153-230),
 // ImageTexture::getColor / doMapping / noInterpolation /
 // bilinearInterpolation (texture_image.cc:180-262, 343-375) and
@@ -783,7 +831,7 @@ __device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p
 		mx = mx > 0.99999f ? 0.99999f : (mx < 0.f ? 0.f : mx);
 		my = my > 0.99999f ? 0.99999f : (my < 0.f ? 0.f : my);
 	}
-	if(outside) { out[0] = out[1] = out[2] = 0.f; return; }
+	if(outside) { out[0] = out[1] = out[2] = 0.f; tex_layer(T, 0.f, out); return; }
 	const bool rep = T.clip == GBRT_CLIP_REPEAT;
 	const float4 *tx = sc.texels + T.off;
 	float4 c;
@@ -812,7 +860,9 @@ __device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p
 		c.x = xa(xa(xa(xm(w11, c11.x), xm(w12, c12.x)), xm(w21, c21.x)), xm(w22, c22.x));
 		c.y = xa(xa(xa(xm(w11, c11.y), xm(w12, c12.y)), xm(w21, c21.y)), xm(w22, c22.y));
 		c.z = xa(xa(xa(xm(w11, c11.z), xm(w12, c12.z)), xm(w21, c21.z)), xm(w22, c22.z));
+		c.w = xa(xa(xa(xm(w11, c11.w), xm(w12, c12.w)), xm(w21, c21.w)), xm(w22, c22.w));
 	}
+	const float alpha = c.w;
 	float r[3] = {c.x, c.y, c.z};
 	if(T.adj)
 	{
@@ -823,6 +873,7 @@ __device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p
 		if(T.adj_clamp) for(int k = 0; k < 3; ++k) r[k] = r[k] < 0.f ? 0.f : r[k];
 	}
 	out[0] = r[0]; out[1] = r[1]; out[2] = r[2];
+	tex_layer(T, alpha, out);
 }
 
 // The diffuse colour of a surface point (the material's, or its diffuse
@@ -3550,6 +3601,13 @@ int gbrt_scene_set_textures(gbrt_scene *S, const float *uv, uint32_t n_uv, const
 		d.adj_clamp = t.adj_clamp ? 1 : 0;
 		for(int k = 0; k < 3; ++k) d.mult[k] = t.adj_mult_factor[k];
 		d.adj = (d.adj_ic || d.adj_clamp || t.adj_mult_factor[0] != 1.f || t.adj_mult_factor[1] != 1.f || t.adj_mult_factor[2] != 1.f) ? 1 : 0;
+		d.layer = t.layer ? 1 : 0;
+		if(t.blend_mode > GBRT_BLEND_LIGHTEN) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u: blend mode %u", i, t.blend_mode);
+		d.blend = static_cast<int>(t.blend_mode);
+		d.negative = t.negative ? 1 : 0; d.no_rgb = t.no_rgb ? 1 : 0; d.stencil = t.stencil ? 1 : 0;
+		d.colfac = t.colfac;
+		for(int k = 0; k < 4; ++k) d.upper[k] = t.upper_color[k];
+		for(int k = 0; k < 3; ++k) d.def_col[k] = t.def_col[k];
 		for(int k = 0; k < 3; ++k)
 		{
 			if(t.proj[k] < 0 || t.proj[k] > 3) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u: proj %d", i, t.proj[k]);

@@ -95,7 +95,9 @@ class TextureDesc(ctypes.Structure):
                 ("adj_intensity", ctypes.c_float), ("adj_contrast", ctypes.c_float),
                 ("adj_mult_factor", ctypes.c_float * 3), ("adj_clamp", ctypes.c_int32), ("texco", ctypes.c_uint32),
                 ("mapping", ctypes.c_uint32), ("scale", ctypes.c_float * 3), ("offset", ctypes.c_float * 3),
-                ("proj", ctypes.c_int32 * 3)]
+                ("proj", ctypes.c_int32 * 3), ("layer", ctypes.c_int32), ("blend_mode", ctypes.c_uint32),
+                ("colfac", ctypes.c_float), ("upper_color", ctypes.c_float * 4), ("def_col", ctypes.c_float * 3),
+                ("negative", ctypes.c_int32), ("no_rgb", ctypes.c_int32), ("stencil", ctypes.c_int32)]
 
 
 # ImageTexture / TextureMapperNode enum names (texture_image.h, shader_node_texture.h)
@@ -103,6 +105,8 @@ TEXCO = {"global": 0, "uv": 1}
 MAPPING = {"plain": 0, "cube": 1}
 CLIPPING = {"extend": 0, "clip": 1, "clipcube": 2, "repeat": 3}
 INTERPOLATE = {"none": 0, "bilinear": 1}
+BLEND_MODES = {"mix": 0, "add": 1, "multiply": 2, "subtract": 3, "screen": 4, "divide": 5, "difference": 6, "darken": 7,
+               "lighten": 8}
 
 
 def texture_desc(t):
@@ -128,6 +132,14 @@ def texture_desc(t):
     d.scale[:] = [float(x) for x in t.get("scale", (1.0, 1.0, 1.0))]
     d.offset[:] = [float(x) for x in t.get("offset", (0.0, 0.0, 0.0))]
     d.proj[:] = [int(x) for x in t.get("proj", (1, 2, 3))]
+    lay = t.get("layer")
+    d.layer = int(lay is not None)
+    lay = lay or {}
+    d.blend_mode = BLEND_MODES[lay.get("blend_mode", "mix")]
+    d.colfac = float(lay.get("colfac", 1.0))
+    d.upper_color[:] = [float(x) for x in lay.get("upper_color", (0.0, 0.0, 0.0, 0.0))]
+    d.def_col[:] = [float(x) for x in lay.get("def_col", (1.0, 1.0, 1.0))]
+    d.negative, d.no_rgb, d.stencil = (int(bool(lay.get(k, False))) for k in ("negative", "noRGB", "stencil"))
     return d, img
 
 

@@ -162,6 +162,16 @@ def reference_scene_text(scene, spp, batches, threads=-1, offset_stride=None):
                     out.append(f"node name={node} type=texture_mapper texture={v} texco={tx.get('texco', 'global')} "
                                f"mapping={tx.get('mapping', 'plain')} scale={fmt(tx.get('scale', (1.0, 1.0, 1.0)))} "
                                f"offset={fmt(tx.get('offset', (0.0, 0.0, 0.0)))} proj_x={proj[0]} proj_y={proj[1]} proj_z={proj[2]}")
+                    lay = tx.get("layer")
+                    if lay is not None:
+                        layer = f"{name}_dlayer"
+                        up = lay.get("upper_color", (0.0, 0.0, 0.0, 0.0))
+                        dc = (*lay.get("def_col", (1.0, 1.0, 1.0)), 1.0)
+                        out.append(f"node name={layer} type=layer input={node} blend_mode={lay.get('blend_mode', 'mix')} "
+                                   f"colfac={float(lay.get('colfac', 1.0))!r} upper_color={fmt(up)} def_col={fmt(dc)} "
+                                   f"negative={fmt(bool(lay.get('negative', False)))} noRGB={fmt(bool(lay.get('noRGB', False)))} "
+                                   f"stencil={fmt(bool(lay.get('stencil', False)))} do_color=true color_input=true")
+                        node = layer
                     extra += f" diffuse_shader={node}"
                     continue
                 if isinstance(v, bool):

@@ -21,7 +21,8 @@
 //                                ColorAlpha image, image_optimization none, LinearRGB)
 //   texture NAME key=value ...   (yafaray_createTexture: type=image image_name=...)
 //   node key=value ...           a shader node of the next material line
-//                                (e.g. name=tex0 type=texture_mapper texture=...);
+//                                (e.g. name=tex0 type=texture_mapper texture=...;
+//                                "a,b,c" is a vector, "r,g,b,a" a colour);
 //                                the material names it (diffuse_shader=tex0)
 //   arealight CX CY CZ  P1X P1Y P1Z  P2X P2Y P2Z  R G B  POWER SAMPLES
 //   pointlight X Y Z  R G B  POWER
@@ -272,8 +273,9 @@ int main(int argc, char **argv)
 				const size_t eq = kv.find('=');
 				if(eq == std::string::npos) continue;
 				const std::string key = kv.substr(0, eq), val = kv.substr(eq + 1);
-				double a, b, c;
-				if(std::sscanf(val.c_str(), "%lf,%lf,%lf", &a, &b, &c) == 3) yafaray_setParamMapVector(target, key.c_str(), a, b, c);
+				double a, b, c, d;
+				if(std::sscanf(val.c_str(), "%lf,%lf,%lf,%lf", &a, &b, &c, &d) == 4) yafaray_setParamMapColor(target, key.c_str(), a, b, c, d);
+				else if(std::sscanf(val.c_str(), "%lf,%lf,%lf", &a, &b, &c) == 3) yafaray_setParamMapVector(target, key.c_str(), a, b, c);
 				else setTyped(target, key, val);
 			}
 			if(kw == "texture") yafaray_createTexture(scene, name.c_str(), pm);
