@@ -358,9 +358,35 @@ __device__ __forceinline__ void tc_layer(uint32_t d_tmem, uint32_t a_saddr, uint
 	tc::mma_commit(mbar);
 }
 
+// The hash-grid encoding of a queue of positions as BF16 rows of kGuideIn
+// features (64 B), one position per thread.  Kept apart from the tensor-core
+// kernel, whose TMEM and shared memory allow 4 CTAs per SM: here every SM
+// holds enough warps to keep its 128 gathers per position in flight.
+constexpr int kEncThreads = 256;
+__global__ void __launch_bounds__(kEncThreads) k_guide_encode(GuideGrid g, const float *__restrict__ table, const float *__restrict__ pos,
+                                                              uint32_t n, const uint32_t *__restrict__ n_dev, uint4 *__restrict__ enc)
+{
+	const uint32_t count = n_dev ? min(*n_dev, n) : n;
+	for(uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < count; s += gridDim.x * blockDim.x)
+	{
+		const float p[3] = {pos[3ull * s], pos[3ull * s + 1], pos[3ull * s + 2]};
+		float e[kGuideIn];
+		encode(g, table, p, e, nullptr, nullptr);
+		uint32_t w[kGuideIn / 2];
+		for(int i = 0; i < kGuideIn / 2; ++i)
+		{
+			const __nv_bfloat162 b = __floats2bfloat162_rn(e[2 * i], e[2 * i + 1]);
+			w[i] = *reinterpret_cast<const uint32_t *>(&b);
+		}
+		uint4 *row = enc + static_cast<size_t>(s) * (kGuideIn / 8);
+		for(int i = 0; i < kGuideIn / 8; ++i) row[i] = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
+	}
+}
+
+// enc: the positions' encodings (k_guide_encode), or null to encode here.
 __global__ void __launch_bounds__(kTcThreads) k_guide_eval_tc(GuideGrid g, const float *__restrict__ table, const float *__restrict__ mlp,
                                                               const float *__restrict__ pos, uint32_t n, const uint32_t *__restrict__ n_dev,
-                                                              float *__restrict__ lobes, uint32_t *__restrict__ err)
+                                                              float *__restrict__ lobes, uint32_t *__restrict__ err, const uint4 *__restrict__ enc)
 {
 	extern __shared__ __align__(1024) uint8_t smem[];
 	float *bias = reinterpret_cast<float *>(smem + kSmBias);
@@ -386,7 +412,22 @@ __global__ void __launch_bounds__(kTcThreads) k_guide_eval_tc(GuideGrid g, const
 		const uint32_t s = tile * 128u + t;
 		const bool live = s < count;
 		float v[kGuideOutPad];
-		if(live)
+		if(live && enc)
+		{
+			const uint4 *row = enc + static_cast<size_t>(s) * (kGuideIn / 8);
+			for(int i = 0; i < kGuideIn / 8; ++i)
+			{
+				const uint4 q = __ldg(row + i);
+				const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+				for(int k = 0; k < 4; ++k)
+				{
+					const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&w[k]));
+					v[8 * i + 2 * k] = f.x;
+					v[8 * i + 2 * k + 1] = f.y;
+				}
+			}
+		}
+		else if(live)
 		{
 			const float p[3] = {pos[3ull * s], pos[3ull * s + 1], pos[3ull * s + 2]};
 			encode(g, table, p, v, nullptr, nullptr);
@@ -797,6 +838,8 @@ struct gbrt_guide {
 	size_t partial_blocks = 0;
 	float *loss = nullptr;    // [0] loss, [1] record weight sum
 	uint32_t *tc_err = nullptr; // set by the tensor-core kernels when an MMA wait times out
+	uint4 *enc = nullptr;       // BF16 encodings of the eval queue (stream-ordered, grown on demand)
+	size_t enc_cap = 0;
 	int eval_mode = GBRT_GUIDE_EVAL_TENSOR;
 	int step = 0;
 	int n_sm = 0;
@@ -824,9 +867,19 @@ int launch_eval(gbrt_guide *G, const float *pos, uint32_t cap, const uint32_t *c
 	{
 		static bool attr = false;
 		if(!attr) { GBRT_CK(cudaFuncSetAttribute(k_guide_eval_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmTotal))); attr = true; }
+		if(cap > G->enc_cap)
+		{
+			if(G->enc) GBRT_CK(cudaFreeAsync(G->enc, s));
+			G->enc = nullptr;
+			GBRT_CK(cudaMallocAsync(reinterpret_cast<void **>(&G->enc), static_cast<size_t>(cap) * (kGuideIn * 2), s));
+			G->enc_cap = cap;
+		}
+		const unsigned egrid = static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>((static_cast<size_t>(cap) + kEncThreads - 1) / kEncThreads,
+		                                                                                static_cast<size_t>(G->n_sm) * 8)));
+		k_guide_encode<<<egrid, kEncThreads, 0, s>>>(G->grid, G->table, pos, cap, count_dev, G->enc);
 		const size_t tiles = (static_cast<size_t>(cap) + 127) / 128;
 		const unsigned grid = static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>(tiles, static_cast<size_t>(G->n_sm) * 4)));
-		k_guide_eval_tc<<<grid, kTcThreads, kSmTotal, s>>>(G->grid, G->table, G->mlp, pos, cap, count_dev, lobes, G->tc_err);
+		k_guide_eval_tc<<<grid, kTcThreads, kSmTotal, s>>>(G->grid, G->table, G->mlp, pos, cap, count_dev, lobes, G->tc_err, G->enc);
 	}
 	else
 	{
@@ -903,6 +956,7 @@ int gbrt_guide_destroy(gbrt_guide *G)
 {
 	if(!G) return GBRT_OK;
 	void *ptrs[] = {G->table, G->table_g, G->table_m, G->table_v, G->mlp, G->mlp_g, G->mlp_m, G->mlp_v, G->partial, G->loss, G->tc_err};
+	if(G->enc) { cudaDeviceSynchronize(); cudaFree(G->enc); }
 	for(void *p : ptrs) if(p) cudaFree(p);
 	delete G;
 	return GBRT_OK;
