@@ -394,7 +394,7 @@ int gbrt_pt_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const
  * threshold (dark detection, variance window, threshold lowered below the
  * resampled floor) and renders AA_inc_samples x multiplier more samples in
  * those only.  With more than one pass, sample positions are riVdC / riS.
- * pathtracing only.  params->filter_type must not be GBRT_FILTER_PIXEL and
+ * params->filter_type must not be GBRT_FILTER_PIXEL and
  * film_weight_dev is required (device, caller-zeroed, like film_dev);
  * resampled (optional, aa->passes entries): pixels sampled per pass. */
 int gbrt_pt_render_aa(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params,
@@ -464,6 +464,15 @@ int gbrt_dl_render(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt
                    float *film_dev, double *film64_dev, gbrt_pt_stats *stats, void *stream);
 int gbrt_dl_render_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *caustic,
                         float *image_out, gbrt_pt_stats *stats);
+/* The same passes for the photonmapping and directlighting integrators over
+ * photon maps built once (PhotonIntegrator::preprocess), with the host film
+ * of gbrt_pm_render_host / gbrt_dl_render_host.  With final gathering,
+ * AA_indirect_sample_multiplier_factor must be 1 (the multiplied gather
+ * counts are not built). */
+int gbrt_pm_render_aa_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
+                           const gbrt_aa_params *aa, float *image_out, gbrt_pt_stats *stats, uint32_t *resampled);
+int gbrt_dl_render_aa_host(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *caustic,
+                           const gbrt_aa_params *aa, float *image_out, gbrt_pt_stats *stats, uint32_t *resampled);
 
 /* ---- stochastic progressive photon mapping (the `SPPM` integrator) -------
  * Replaces SppmIntegrator::render / prePass / photonWorker / traceGatherRay

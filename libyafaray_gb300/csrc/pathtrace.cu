@@ -4077,7 +4077,7 @@ static int aa_check(const gbrt_aa_params &a, const char *who)
 // sample offset base + samples so far, and lowers the threshold by
 // 10 % x min(8, floor / flagged) while fewer than the floor were flagged.
 static int aa_render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params &pp, const gbrt_aa_params &a, float *film,
-                            gbrt_pt_stats *stats, uint32_t *resampled, cudaStream_t s)
+                            gbrt_pt_stats *stats, uint32_t *resampled, cudaStream_t s, const Params *pm = nullptr)
 {
 	const int W = camera->resx, H = camera->resy;
 	if(W <= 0 || H <= 0) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_aa: bad resolution");
@@ -4095,7 +4095,7 @@ static int aa_render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const
 		sum.shadow_rays += one.shadow_rays; sum.ms += one.ms;
 	};
 	const AaPass first{nullptr, 0, a.passes > 1 ? 1 : 0, 1.f};
-	if(int rc = render_locked(S, camera, pp, nullptr, film, nullptr, stats ? &one : nullptr, s, &first)) return rc;
+	if(int rc = render_locked(S, camera, pp, pm, film, nullptr, stats ? &one : nullptr, s, &first)) return rc;
 	add();
 	if(resampled) resampled[0] = n_pix;
 	float smult = 1.f, lmult = 1.f, thr = a.threshold;
@@ -4126,7 +4126,7 @@ static int aa_render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const
 			q.spp = mult;
 			q.base_sampling_offset = pp.base_sampling_offset + acum;
 			const AaPass pass{all ? nullptr : list.as<uint32_t>(), all ? 0u : static_cast<uint32_t>(n_res), 1, lmult};
-			if(int rc = render_locked(S, camera, q, nullptr, film, nullptr, stats ? &one : nullptr, s, &pass)) return rc;
+			if(int rc = render_locked(S, camera, q, pm, film, nullptr, stats ? &one : nullptr, s, &pass)) return rc;
 			add();
 		}
 		if(resampled) resampled[i] = static_cast<uint32_t>(std::max<int64_t>(0, n_res));
@@ -4324,8 +4324,11 @@ int gbrt_knn_gather(const float *points, uint32_t n, const float *queries, uint3
 	return GBRT_OK;
 }
 
-int gbrt_pm_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
-                   float *film_dev, double *film64_dev, gbrt_pt_stats *stats, void *stream)
+// photonmapping: the photon maps once (PhotonIntegrator::preprocess), then
+// one render, or the adaptive passes (aa) over them.
+static int pm_render_impl(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
+                          float *film_dev, double *film64_dev, gbrt_pt_stats *stats, void *stream, const gbrt_aa_params *aa,
+                          uint32_t *resampled)
 {
 	if(!S || !camera || !params || !pm) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pm_render: NULL argument");
 	if(!film_dev && !film64_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pm_render: no film buffer");
@@ -4430,7 +4433,10 @@ int gbrt_pm_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 		cudaEventElapsedTime(&photon_ms, p0, p1);
 		cudaEventDestroy(p0); cudaEventDestroy(p1);
 	}
-	const int rc = render_locked(S, camera, *params, &M, film_dev, film64_dev, stats, s);
+	if(aa && aa->indirect_sample_multiplier_factor != 1.f && fg)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pm_render_aa: AA_indirect_sample_multiplier_factor != 1 is not built");
+	const int rc = aa ? aa_render_locked(S, camera, *params, *aa, film_dev, stats, resampled, s, &M)
+	                  : render_locked(S, camera, *params, &M, film_dev, film64_dev, stats, s);
 	cudaStreamSynchronize(s);      // the photon buffers are freed on return
 	if(stats && !rc)
 	{
@@ -4555,6 +4561,12 @@ int gbrt_sppm_render_host(gbrt_scene *S, const gbrt_camera_desc *camera, const g
 	return GBRT_OK;
 }
 
+int gbrt_pm_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
+                   float *film_dev, double *film64_dev, gbrt_pt_stats *stats, void *stream)
+{
+	return pm_render_impl(S, camera, params, pm, film_dev, film64_dev, stats, stream, nullptr, nullptr);
+}
+
 int gbrt_pt_render_batch(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params, float *const *films,
                          uint32_t n, uint32_t concurrency, gbrt_pt_stats *stats)
 {
@@ -4605,8 +4617,9 @@ int gbrt_pt_render_batch(gbrt_scene *const *scenes, const gbrt_camera_desc *came
 	return GBRT_OK;
 }
 
-int gbrt_dl_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *caustic,
-                   float *film_dev, double *film64_dev, gbrt_pt_stats *stats, void *stream)
+static int dl_render_impl(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *caustic,
+                          float *film_dev, double *film64_dev, gbrt_pt_stats *stats, void *stream, const gbrt_aa_params *aa,
+                          uint32_t *resampled)
 {
 	if(!S || !camera || !params) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_dl_render: NULL argument");
 	if(!film_dev && !film64_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_dl_render: no film buffer");
@@ -4635,9 +4648,57 @@ int gbrt_dl_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 		M.pm_caustic_paths = static_cast<float>(C.paths);
 		M.g_caustic = GC.g;
 	}
-	const int rc = render_locked(S, camera, *params, &M, film_dev, film64_dev, stats, s);
+	const int rc = aa ? aa_render_locked(S, camera, *params, *aa, film_dev, stats, resampled, s, &M)
+	                  : render_locked(S, camera, *params, &M, film_dev, film64_dev, stats, s);
 	cudaStreamSynchronize(s);
 	return rc;
+}
+
+int gbrt_dl_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *caustic,
+                   float *film_dev, double *film64_dev, gbrt_pt_stats *stats, void *stream)
+{
+	return dl_render_impl(S, camera, params, caustic, film_dev, film64_dev, stats, stream, nullptr, nullptr);
+}
+
+// Adaptive passes of the photonmapping (kind 1) or directlighting (kind 2)
+// integrator over a device film built here; normalised image to the host.
+static int aa_host_other(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params_in, const gbrt_pm_params *pm,
+                         const gbrt_aa_params *aa, float *image_out, gbrt_pt_stats *stats, uint32_t *resampled, int kind)
+{
+	if(!S || !camera || !params_in || !aa || !image_out || (kind == 1 && !pm)) return gbrt_set_error(GBRT_ERR_INVALID, "render_aa_host: NULL argument");
+	if(int rc = aa_check(*aa, "render_aa_host")) return rc;
+	if(camera->resx <= 0 || camera->resy <= 0) return gbrt_set_error(GBRT_ERR_INVALID, "render_aa_host: bad resolution");
+	if(params_in->filter_type == GBRT_FILTER_PIXEL)
+		return gbrt_set_error(GBRT_ERR_INVALID, "render_aa_host: adaptive AA needs a filtered film (filter_type != PIXEL)");
+	const size_t n_pix = static_cast<size_t>(camera->resx) * camera->resy, n = 3 * n_pix;
+	gbrt_pt_params params = *params_in;
+	params.guide = nullptr;
+	DevBuf sum, mean, weight;
+	if(int rc = sum.alloc(n * 4)) return rc;
+	if(int rc = mean.alloc(n * 4)) return rc;
+	if(int rc = weight.alloc(n_pix * 4)) return rc;
+	GBRT_CK(cudaMemset(sum.p, 0, n * 4));
+	GBRT_CK(cudaMemset(weight.p, 0, n_pix * 4));
+	params.film_weight_dev = weight.as<float>();
+	const int rc = kind == 1 ? pm_render_impl(S, camera, &params, pm, sum.as<float>(), nullptr, stats, nullptr, aa, resampled)
+	                         : dl_render_impl(S, camera, &params, pm, sum.as<float>(), nullptr, stats, nullptr, aa, resampled);
+	if(rc) return rc;
+	k_normalize<<<grid_for(n, S->n_sm), kThreads>>>(sum.as<float>(), nullptr, weight.as<float>(), mean.as<float>(), n);
+	GBRT_CK(cudaGetLastError());
+	GBRT_CK(cudaMemcpy(image_out, mean.p, n * 4, cudaMemcpyDeviceToHost));
+	return GBRT_OK;
+}
+
+int gbrt_pm_render_aa_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *pm,
+                           const gbrt_aa_params *aa, float *image_out, gbrt_pt_stats *stats, uint32_t *resampled)
+{
+	return aa_host_other(S, camera, params, pm, aa, image_out, stats, resampled, 1);
+}
+
+int gbrt_dl_render_aa_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_pm_params *caustic,
+                           const gbrt_aa_params *aa, float *image_out, gbrt_pt_stats *stats, uint32_t *resampled)
+{
+	return aa_host_other(S, camera, params, caustic, aa, image_out, stats, resampled, 2);
 }
 
 int gbrt_grid_buckets(const float *points, uint32_t n, double cell_size, uint32_t grid_size, const float box_lo[3], uint32_t *bucket_out)

@@ -260,6 +260,10 @@ SIGNATURES = {
     "gbrt_aa_flags": (_I, [_VP, _VP, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(AaParams), ctypes.c_float, _VP,
                            ctypes.POINTER(ctypes.c_uint32)]),
     "gbrt_scene_set_textures": (_I, [_VP, _VP, _U32, _VP, ctypes.POINTER(TextureDesc), _U32, _VP, _U32]),
+    "gbrt_pm_render_aa_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP, ctypes.POINTER(AaParams),
+                                    _VP, ctypes.POINTER(PtStats), _VP]),
+    "gbrt_dl_render_aa_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP, ctypes.POINTER(AaParams),
+                                    _VP, ctypes.POINTER(PtStats), _VP]),
     "gbrt_sppm_render": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), ctypes.POINTER(SppmParams), _VP,
                               ctypes.POINTER(PtStats), _VP]),
     "gbrt_sppm_render_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), ctypes.POINTER(SppmParams), _VP,
@@ -576,8 +580,8 @@ class Renderer:
         """Adaptive anti-aliasing render (TiledIntegrator::render's passes)
         with the scene's "film" AA parameters: (mean image [resy, resx, 3],
         stats dict, pixels rendered per pass).  spp: AA_minsamples."""
-        if self.kind != "pathtracing":
-            raise ValueError("adaptive AA passes are implemented for the path tracer")
+        if self.kind not in ("pathtracing", "photonmapping", "directlighting"):
+            raise ValueError(f"adaptive AA passes are not built for the {self.kind} integrator")
         film = self.scene.get("film", {})
         spp = int(film.get("AA_minsamples", 1)) if spp is None else int(spp)
         aa = aa_params(film)
@@ -586,8 +590,14 @@ class Renderer:
         img = np.empty((cam.resy, cam.resx, 3), np.float32)
         res = np.zeros(max(1, aa.passes), np.uint32)
         st = PtStats()
-        check(load().gbrt_pt_render_aa_host(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.byref(aa), _ptr(img),
-                                            ctypes.byref(st), _ptr(res)))
+        if self.kind == "pathtracing":
+            check(load().gbrt_pt_render_aa_host(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.byref(aa), _ptr(img),
+                                                ctypes.byref(st), _ptr(res)))
+        else:
+            pm = pm_params(self.scene["integrator"])
+            fn = load().gbrt_pm_render_aa_host if self.kind == "photonmapping" else load().gbrt_dl_render_aa_host
+            check(fn(self._h, ctypes.byref(cam), ctypes.byref(p), ctypes.byref(pm), ctypes.byref(aa), _ptr(img),
+                     ctypes.byref(st), _ptr(res)))
         return img, {"camera_samples": st.camera_samples, "extension_rays": st.extension_rays,
                      "shadow_rays": st.shadow_rays, "ms": st.ms}, res.tolist()
 

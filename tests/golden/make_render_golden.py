@@ -320,5 +320,18 @@ if __name__ == "__main__":
                             se=(rgb.std(0, ddof=1) / np.sqrt(24)).astype(np.float32), batches=np.int32(24), passes=np.int32(8),
                             photons=np.int32(100000), seconds=secs)
         print(f"cornell_sppm_48_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
+    if "aa_pm" in what:
+        # adaptive AA passes of the photonmapping (direct estimate) and
+        # directlighting integrators
+        for name, sc in (("cornell_pm_aa_48_render.npz", scenes.cornell_pm_scene(48, False)),
+                         ("cornell_dl_aa_48_render.npz", scenes.cornell_dl_scene(48))):
+            sc["film"] = {"filter_type": "gauss", "AA_pixelwidth": 1.5, "AA_passes": 3, "AA_inc_samples": 2,
+                          "AA_threshold": 0.08}
+            rgb, secs, passes = orc.run_reference_aa(sc, 8, 24, 4096, threads=os.cpu_count() or 1)
+            np.savez_compressed(os.path.join(OUT, name), mean=rgb.mean(0).astype(np.float32),
+                                se=(rgb.std(0, ddof=1) / np.sqrt(24)).astype(np.float32), batches=np.int32(24), spp=np.int32(8),
+                                stride=np.int32(4096), film=np.array(__import__("json").dumps(sc["film"])), seconds=secs,
+                                flagged=np.array([len(p["flagged"]) for p in passes], np.int32))
+            print(f"{name}: mean {rgb.mean(axis=(0, 1, 2))}, flagged {[len(p['flagged']) for p in passes]}, {secs.sum():.1f} s")
     if "cornell_point" in what:
         variant_golden("cornell_point_64_render.npz", point_light=True)

@@ -108,3 +108,23 @@ def test_gpu_aa_needs_a_filtered_film(cuda_device):
     r2 = _cornell(16, 12, {"filter_type": "gauss", "AA_passes": 0})
     with pytest.raises(gbrt.GbrtError):
         r2.render_aa(spp=2)
+
+
+@pytest.mark.parametrize("name,kind", [("cornell_pm_aa_48_render.npz", "pm"), ("cornell_dl_aa_48_render.npz", "dl")])
+def test_gpu_aa_photon_integrators_vs_reference(cuda_device, name, kind):
+    """The adaptive passes over the photonmapping (direct estimate) and
+    directlighting integrators, photon maps built once per render."""
+    g = np.load(os.path.join(GOLD, name))
+    sc = scenes.cornell_pm_scene(48, False) if kind == "pm" else scenes.cornell_dl_scene(48)
+    sc["film"] = json.loads(str(g["film"]))
+    r = gbrt.Renderer(sc)
+    k, spp, stride = int(g["batches"]), int(g["spp"]), int(g["stride"])
+    imgs, flagged = [], []
+    for b in range(k):
+        img, _, res = r.render_aa(spp=spp, base_offset=b * stride, seed=1000 + b)
+        imgs.append(img)
+        flagged.append(res[1:])
+    frac, relmse, _ = parity(np.stack(imgs), g["mean"], g["se"])
+    print(f"{name}: {100 * frac:.2f}% within 3 SE, relMSE {relmse:.3g}; flagged {np.mean(flagged, 0).round(1).tolist()} "
+          f"(reference batch 0: {g['flagged'].tolist()})")
+    assert frac >= 0.99
