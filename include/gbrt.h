@@ -188,8 +188,8 @@ int gbrt_trace_shadow_host(const gbrt_bvh *bvh, const gbrt_ray *rays, uint32_t n
  * estimation (src/integrator/surface/integrator_path_tracer.cc:138-314,
  * integrator_montecarlo.cc:92-440) run per pixel sample by
  * TiledIntegrator::renderTile (integrator_tiled.cc:253-395), with the film
- * accumulation of ImageFilm::addSample for a box filter of width 1
- * (imagefilm.cc:771-822). */
+ * accumulation of ImageFilm::addSample (imagefilm.cc:771-822): single-pixel
+ * sums, or any of the reference's filters (gbrt_pt_params.filter_type). */
 
 enum {
 	GBRT_MAT_SHINYDIFFUSE = 0,   /* "shinydiffusemat": color, color2 (mirror_color; all 0 -> 1), power (emit),
