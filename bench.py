@@ -38,6 +38,32 @@ FALLBACK_HBM_GBS = 6800.0
 METRIC = "Mrays/s closest-hit (1M-triangle traversal micro-benchmark)"
 
 
+# ---- the multi-rank (replica) path: each rank traces its own seeded rays
+# over the replicated scene; the only exchange is the max of the ranks'
+# times (no collective on the data path) ----
+
+def rank_rays(n, rank):
+    """The n rays rank `rank` traces (its own seeded batch)."""
+    from libyafaray_gb300 import scenes
+    return scenes.random_rays(n, seed=2 + 1000 * rank)
+
+
+def max_over_ranks(x, dist, device=None):
+    """x reduced with MAX over the process group (x itself with no group)."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, seconds):
+    """Whole-job throughput in millions of units per second: every rank
+    processes units_per_rank in (at most) `seconds`."""
+    return units_per_rank * world / seconds / 1e6
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -415,7 +441,7 @@ def main():
     gbrt.load()
 
     verts, faces = scenes.random_triangles(args.tris, seed=1)
-    rays_np = scenes.random_rays(args.rays, seed=2 + 1000 * rank)
+    rays_np = rank_rays(args.rays, rank)
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
     v_d = torch.from_numpy(verts).cuda()
@@ -444,12 +470,9 @@ def main():
         torch.cuda.synchronize()
     launch_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     total_ms = ev[0].elapsed_time(ev[-1])
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dist, "cuda")
     per_step_s = total_ms / 1e3 / args.steps
-    value = args.rays * world / per_step_s / 1e6
+    value = whole_job_rate(args.rays, world, per_step_s)
     hits_np = hits_d[:, 0].cpu().numpy().view(np.int32)
     hit_frac = float((hits_np >= 0).mean())
 
@@ -484,12 +507,9 @@ def main():
         for _ in range(args.steps):
             e2e_step()
         e2e_s = (time.perf_counter() - t0) / args.steps
-        if dist:
-            t = torch.tensor([e2e_s], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, dist, "cuda")
         assert np.array_equal(hp[:, 0].view(np.int32), hits_np), "host path disagrees with device path"
-        e2e = {"value": args.rays * world / e2e_s / 1e6, "unit": "Mrays/s",
+        e2e = {"value": whole_job_rate(args.rays, world, e2e_s), "unit": "Mrays/s",
                "h2d_bytes_per_step": int(rp.nbytes), "d2h_bytes_per_step": int(hp.nbytes),
                "ms_per_step": e2e_s * 1e3, "gpu_launches_per_step": (args.rays + (1 << 21) - 1) >> 21}
 
