@@ -486,13 +486,20 @@ int gbrt_dl_render_aa_host(gbrt_scene *scene, const gbrt_camera_desc *camera, co
  * + the eye sample's radiance to the film.  As in the reference, only the
  * caustic map enters the estimate (its diffuse-map accumulation runs under
  * debug logging only).  The initial radius comes from the scene bound and
- * resolution (initializePpm); pmIRE is not built.  params: spp is ignored
+ * resolution (initializePpm).  params: spp is ignored
  * (one sample per pass), path_samples / bounces / russian roulette are not
  * used; raydepth, transparent shadows and the film filter are. */
 typedef struct gbrt_sppm_params {
 	int32_t photons;            /* "photons" [500000] */
 	int32_t passes;             /* "passNums" [1000] */
 	int32_t bounces;            /* "bounces" [5] */
+	/* initial radius estimate ("pmIRE", first pass only, traceGatherRay
+	 * :648-667): the first gather point of a pixel takes the smaller of the
+	 * radii of its searchNum nearest diffuse and caustic photons within
+	 * photonRadius */
+	int32_t pm_ire;             /* "pmIRE" [0] */
+	float photon_radius;        /* "photonRadius" [1] */
+	int32_t search_num;         /* "searchNum" [10], at most 64 */
 } gbrt_sppm_params;
 
 int gbrt_sppm_render(gbrt_scene *scene, const gbrt_camera_desc *camera, const gbrt_pt_params *params, const gbrt_sppm_params *sppm,

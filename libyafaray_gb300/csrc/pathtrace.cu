@@ -149,8 +149,11 @@ struct Params {
 	int tshadow, shadow_depth;
 	// SPPM (pm == 3): per-pixel squared gather radius and this pass's
 	// photon flux (xyz) and photon count (w)
-	const float *sppm_r2;
+	float *sppm_r2;
 	float4 *sppm_pass;
+	uint8_t *sppm_ire;         // pmIRE: per-pixel "radius set" flags, or null (no estimate this pass)
+	float sppm_ire_r2;         // photonRadius^2
+	int sppm_ire_k;            // searchNum
 };
 
 struct Work {
@@ -2680,7 +2683,7 @@ __global__ void __launch_bounds__(kThreads) k_pm_root(SceneDev sc, Params P, Wor
 		const float4 ng = __ldg(sc.prim_ng + prim);
 		Surface s;
 		s.m = sc.mats + __float_as_uint(ng.w);
-		if(!(s.m->flags & BF_DIFFUSE)) continue;
+		if(!(s.m->flags & BF_DIFFUSE) && !(P.pm == 3 && P.sppm_ire)) continue;
 		const float4 ra = W.q_ray[cur][2ull * q], rb = W.q_ray[cur][2ull * q + 1];
 		const float dir[3] = {rb.x, rb.y, rb.z};
 		s.p[0] = xa(ra.x, xm(h.y, dir[0])); s.p[1] = xa(ra.y, xm(h.y, dir[1])); s.p[2] = xa(ra.z, xm(h.y, dir[2]));
@@ -2694,8 +2697,22 @@ __global__ void __launch_bounds__(kThreads) k_pm_root(SceneDev sc, Params P, Wor
 			// SppmIntegrator::traceGatherRay (integrator_sppm.cc:727-748): every
 			// caustic photon within the pixel's radius, f(wo, photon dir) x
 			// photon colour; the count weighted 1 / (glossy split product)
-			if(!P.g_caustic.n) continue;
 			const uint32_t pixel = W.p_pixel[path];
+			if(P.sppm_ire && !P.sppm_ire[pixel])
+			{
+				// pmIRE at any material (:648-667): the smaller of the shrunk radii
+				uint32_t idx[gbrt::kMaxGather];
+				float d2[gbrt::kMaxGather];
+				float r1 = P.sppm_ire_r2, r2b = P.sppm_ire_r2;
+				const int n1 = P.g_diffuse.n ? gbrt::knn_gather(P.g_diffuse, s.p, P.sppm_ire_k, r1, idx, d2) : 0;
+				const int n2 = P.g_caustic.n ? gbrt::knn_gather(P.g_caustic, s.p, P.sppm_ire_k, r2b, idx, d2) : 0;
+				if(n1 > 0 || n2 > 0)
+				{
+					P.sppm_r2[pixel] = r1 < r2b ? r1 : r2b;
+					P.sppm_ire[pixel] = 1u;
+				}
+			}
+			if(!(s.m->flags & BF_DIFFUSE) || !P.g_caustic.n) continue;
 			const float r2 = P.sppm_r2[pixel];
 			float flux[3] = {0.f, 0.f, 0.f};
 			uint32_t cnt = 0;
@@ -3830,6 +3847,7 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 		P.pm_caustic_paths = pm->pm_caustic_paths; P.pm_lookup_r2 = pm->pm_lookup_r2;
 		P.g_diffuse = pm->g_diffuse; P.g_caustic = pm->g_caustic; P.g_radiance = pm->g_radiance;
 		P.sppm_r2 = pm->sppm_r2; P.sppm_pass = pm->sppm_pass;
+		P.sppm_ire = pm->sppm_ire; P.sppm_ire_r2 = pm->sppm_ire_r2; P.sppm_ire_k = pm->sppm_ire_k;
 	}
 	P.base_offset = pp.base_sampling_offset; P.seed = pp.seed;
 	P.d1 = 1.f / static_cast<float>(pp.spp);
@@ -4463,10 +4481,17 @@ static int sppm_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt
 	float r0 = (((bound[3] - bound[0]) + (bound[4] - bound[1]) + (bound[5] - bound[2])) / 3.f) /
 	           (static_cast<float>(camera->resx + camera->resy) / 2.0f) * 2.f;
 	r0 = std::min(r0, 1.f);
-	DevBuf hp, r2, pass;
+	DevBuf hp, r2, pass, ire;
 	if(int rc = hp.alloc(16ull * n_pix)) return rc;
 	if(int rc = r2.alloc(4ull * n_pix)) return rc;
 	if(int rc = pass.alloc(16ull * n_pix)) return rc;
+	if(q.pm_ire)
+	{
+		if(int rc = ire.alloc(n_pix)) return rc;
+		GBRT_CK(cudaMemsetAsync(ire.p, 0, n_pix, s));
+	}
+	// grid cells bound every query radius: the initial one, or photonRadius with pmIRE
+	const float cell = q.pm_ire ? std::max(r0, q.photon_radius) : r0;
 	k_sppm_init<<<grid_for(n_pix, S->n_sm), kThreads, 0, s>>>(hp.as<float4>(), r2.as<float>(), pass.as<float4>(), n_pix, (r0 * 1.f) * (r0 * 1.f));
 	GBRT_CK(cudaGetLastError());
 	const SceneDev sc = scene_dev(S);
@@ -4490,8 +4515,8 @@ static int sppm_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt
 	const uint32_t n_ph = static_cast<uint32_t>(q.photons);
 	for(int i = 0; i < q.passes; ++i)
 	{
-		ShotMap C;
-		GridStore GC;
+		ShotMap C, D;
+		GridStore GC, GD;
 		// photon paths of sample index base_sampling_offset + i: one render's
 		// passes use the Halton indices the reference's generators run through,
 		// renders at disjoint sample offsets disjoint photon paths
@@ -4500,8 +4525,20 @@ static int sppm_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt
 		if(int rc = shoot_map(S, sc, true, n_ph, q.bounces, false, pp.seed, C, s, true, static_cast<uint32_t>(base))) return rc;
 		total += n_ph;
 		stored += C.n;
-		if(int rc = build_grid(C.pos.as<float4>(), C.dir.as<float4>(), C.col.as<float4>(), C.n, r0, lo, S->n_sm, GC, s)) return rc;
+		if(int rc = build_grid(C.pos.as<float4>(), C.dir.as<float4>(), C.col.as<float4>(), C.n, cell, lo, S->n_sm, GC, s)) return rc;
 		M.g_caustic = GC.g;
+		M.sppm_ire = nullptr;
+		M.g_diffuse = gbrt::PhotonGrid{};
+		if(q.pm_ire && i == 0)
+		{
+			// the first pass's diffuse map (the same photon paths' non-caustic indirect deposits)
+			if(int rc = shoot_map(S, sc, false, n_ph, q.bounces, false, pp.seed, D, s, true, static_cast<uint32_t>(base))) return rc;
+			if(int rc = build_grid(D.pos.as<float4>(), D.dir.as<float4>(), D.col.as<float4>(), D.n, cell, lo, S->n_sm, GD, s)) return rc;
+			M.g_diffuse = GD.g;
+			M.sppm_ire = ire.as<uint8_t>();
+			M.sppm_ire_r2 = q.photon_radius * q.photon_radius;
+			M.sppm_ire_k = q.search_num;
+		}
 		e.base_sampling_offset = pp.base_sampling_offset + static_cast<uint32_t>(i);
 		if(int rc = render_locked(S, camera, e, &M, film, nullptr, stats ? &one : nullptr, s, &multipass)) return rc;
 		F.base_offset = e.base_sampling_offset;
@@ -4528,7 +4565,8 @@ int gbrt_sppm_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_p
                      float *film_dev, gbrt_pt_stats *stats, void *stream)
 {
 	if(!S || !camera || !params || !sppm || !film_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_sppm_render: NULL argument");
-	if(sppm->photons < 1 || sppm->passes < 1 || sppm->bounces < 0 || camera->resx <= 0 || camera->resy <= 0)
+	if(sppm->photons < 1 || sppm->passes < 1 || sppm->bounces < 0 || camera->resx <= 0 || camera->resy <= 0 ||
+	   (sppm->pm_ire && (sppm->search_num < 1 || sppm->search_num > gbrt::kMaxGather || !(sppm->photon_radius > 0.f))))
 		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_sppm_render: bad parameters (photons %d, passes %d, bounces %d)", sppm->photons,
 		                      sppm->passes, sppm->bounces);
 	std::lock_guard<std::mutex> lock(S->mu);

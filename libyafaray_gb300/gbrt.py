@@ -79,13 +79,15 @@ class AaParams(ctypes.Structure):
 
 
 class SppmParams(ctypes.Structure):
-    _fields_ = [("photons", ctypes.c_int32), ("passes", ctypes.c_int32), ("bounces", ctypes.c_int32)]
+    _fields_ = [("photons", ctypes.c_int32), ("passes", ctypes.c_int32), ("bounces", ctypes.c_int32),
+                ("pm_ire", ctypes.c_int32), ("photon_radius", ctypes.c_float), ("search_num", ctypes.c_int32)]
 
 
 def sppm_params(it):
     """gbrt_sppm_params from an "SPPM" integrator dict (SppmIntegrator's
     parameter names and defaults, integrator_sppm.h:79-86)."""
-    return SppmParams(int(it.get("photons", 500000)), int(it.get("passNums", 1000)), int(it.get("bounces", 5)))
+    return SppmParams(int(it.get("photons", 500000)), int(it.get("passNums", 1000)), int(it.get("bounces", 5)),
+                      int(bool(it.get("pmIRE", False))), float(it.get("photonRadius", 1.0)), int(it.get("searchNum", 10)))
 
 
 class TextureDesc(ctypes.Structure):

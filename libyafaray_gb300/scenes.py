@@ -429,13 +429,15 @@ def textured_cornell_scene(res=64, **kw):
     return sc
 
 
-def cornell_sppm_scene(res=48, photons=100000, passes=8, bounces=5):
+def cornell_sppm_scene(res=48, photons=100000, passes=8, bounces=5, pm_ire=False, photon_radius=0.1, search_num=10):
     """The glass Cornell box (a glass and a rough-glass ball) rendered by the
     "SPPM" integrator: caustics under the balls come from the photon
     gathers, the rest from direct light and the specular split."""
     sc = cornell_scene(res=res, glass=True)
     sc["integrator"] = {"type": "SPPM", "photons": int(photons), "passNums": int(passes), "bounces": int(bounces),
                         "raydepth": 5}
+    if pm_ire:
+        sc["integrator"].update({"pmIRE": True, "photonRadius": float(photon_radius), "searchNum": int(search_num)})
     return sc
 
 

@@ -320,6 +320,13 @@ if __name__ == "__main__":
                             se=(rgb.std(0, ddof=1) / np.sqrt(24)).astype(np.float32), batches=np.int32(24), passes=np.int32(8),
                             photons=np.int32(100000), seconds=secs)
         print(f"cornell_sppm_48_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
+        # the same with the initial radius estimate (pmIRE, photonRadius 0.1, searchNum 10)
+        sc = scenes.cornell_sppm_scene(res=48, photons=100000, passes=8, pm_ire=True)
+        rgb, secs = orc.run_reference_render(sc, 1, 24, threads=os.cpu_count() or 1, offset_stride=8)
+        np.savez_compressed(os.path.join(OUT, "cornell_sppm_ire_48_render.npz"), mean=rgb.mean(0).astype(np.float32),
+                            se=(rgb.std(0, ddof=1) / np.sqrt(24)).astype(np.float32), batches=np.int32(24), passes=np.int32(8),
+                            photons=np.int32(100000), seconds=secs)
+        print(f"cornell_sppm_ire_48_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
     if "aa_pm" in what:
         # adaptive AA passes of the photonmapping (direct estimate) and
         # directlighting integrators

@@ -143,16 +143,19 @@ def test_gpu_cornell_textured_matches_reference(cuda_device):
     assert frac >= 0.995
 
 
-def test_gpu_cornell_sppm_matches_reference(cuda_device):
+@pytest.mark.parametrize("name,ire", [("cornell_sppm_48_render.npz", False), ("cornell_sppm_ire_48_render.npz", True)])
+def test_gpu_cornell_sppm_matches_reference(cuda_device, name, ire):
     """SPPM (SppmIntegrator): per pass a caustic photon map, one eye sample per
     pixel with direct light and the specular / glossy split, the caustic
-    gather within each pixel's shrinking radius and the progressive update."""
-    g = np.load(os.path.join(GOLD, "cornell_sppm_48_render.npz"))
+    gather within each pixel's shrinking radius and the progressive update;
+    with pmIRE the first pass's radius estimate from the diffuse and caustic
+    maps."""
+    g = np.load(os.path.join(GOLD, name))
     passes = int(g["passes"])
-    r = gbrt.Renderer(scenes.cornell_sppm_scene(res=48, photons=int(g["photons"]), passes=passes))
+    r = gbrt.Renderer(scenes.cornell_sppm_scene(res=48, photons=int(g["photons"]), passes=passes, pm_ire=ire))
     gb = np.stack([r.render(1, base_offset=b * passes, seed=1000 + b)[0] for b in range(int(g["batches"]))])
     frac, relmse, m = parity(gb, g["mean"], g["se"])
-    print(f"cornell SPPM 48x48: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
+    print(f"{name}: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
           f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
     assert frac >= 0.99
 
