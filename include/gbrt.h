@@ -361,6 +361,7 @@ typedef struct gbrt_texture_desc {
 	float upper_color[4];       /* [0, 0, 0, 0] (exporters pass the material colour, alpha 1) */
 	float def_col[3];           /* [1, 1, 1] */
 	int32_t negative, no_rgb, stencil;   /* "negative", "noRGB", "stencil" [0] */
+	int32_t mirror_x, mirror_y; /* "mirror_x", "mirror_y" [0]: every other repeat mirrored (clipping repeat) */
 } gbrt_texture_desc;
 enum { GBRT_BLEND_MIX = 0, GBRT_BLEND_ADD = 1, GBRT_BLEND_MULTIPLY = 2, GBRT_BLEND_SUBTRACT = 3, GBRT_BLEND_SCREEN = 4,
        GBRT_BLEND_DIVIDE = 5, GBRT_BLEND_DIFFERENCE = 6, GBRT_BLEND_DARKEN = 7, GBRT_BLEND_LIGHTEN = 8 };

@@ -82,6 +82,7 @@ struct DevTexture {
 	float scale[3], offset2[3]; // offset2 = 2 x offset (shader_node_texture.h:108)
 	int proj[3];
 	int layer, blend, negative, no_rgb, stencil;   // LayerNode over the mapper
+	int mirror_x, mirror_y;
 	float colfac, upper[4], def_col[3];
 };
 
@@ -725,11 +726,23 @@ __device__ __forceinline__ void hit_uv(const SceneDev &sc, int prim, float bu, f
 	uv[1] = xa(xm(iv, xa(xm(iu, a.y), xm(bu, b.y))), xm(bv, xa(xm(iu, d.y), xm(bu, c.y))));
 }
 
-// ImageTexture::findTextureInterpolationCoordinates without mirroring
-// (texture_image.cc:264-341): the texel pair along one axis and the weight.
-__device__ __forceinline__ void tex_axis(float cf, int res, bool repeat, int &c1, int &c2, float &d)
+// ImageTexture::findTextureInterpolationCoordinates (texture_image.cc:
+// 264-341): the texel pair along one axis and the weight.
+__device__ __forceinline__ void tex_axis(float cf, int res, bool repeat, bool mirror, int &c1, int &c2, float &d)
 {
-	if(repeat)
+	if(repeat && mirror)
+	{
+		c1 = static_cast<int>(cf) % res;
+		if(cf < 0.f) { c2 = c1; d = -cf; }
+		else if(cf >= static_cast<float>(res - 1)) { c2 = c1; d = xs(cf, static_cast<float>(static_cast<int>(cf))); }
+		else
+		{
+			c2 = c1 + 1;
+			if(c2 >= res) c2 = (2 * res - c2) % res;
+			d = xs(cf, static_cast<float>(static_cast<int>(cf)));
+		}
+	}
+	else if(repeat)
 	{
 		c1 = static_cast<int>(cf) % res;
 		if(cf > 0.f) { c2 = (c1 + 1) % res; d = xs(cf, static_cast<float>(static_cast<int>(cf))); }
@@ -818,6 +831,8 @@ __device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p
 	{
 		if(T.xrep > 1) mx = xm(mx, static_cast<float>(T.xrep));
 		if(T.yrep > 1) my = xm(my, static_cast<float>(T.yrep));
+		if(T.mirror_x && static_cast<int>(ceilf(mx)) % 2 == 0) mx = -mx;
+		if(T.mirror_y && static_cast<int>(ceilf(my)) % 2 == 0) my = -my;
 		if(mx > 1.f) mx = xs(mx, truncf(mx));
 		else if(mx < 0.f) mx = xa(mx, xs(1.f, truncf(mx)));
 		if(my > 1.f) my = xs(my, truncf(my));
@@ -844,8 +859,8 @@ __device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p
 		const float yf = xm(static_cast<float>(T.h), xs(my, floorf(my)));
 		int x1, x2, y1, y2;
 		float dx, dy;
-		tex_axis(xf, T.w, rep, x1, x2, dx);
-		tex_axis(yf, T.h, rep, y1, y2, dy);
+		tex_axis(xf, T.w, rep, T.mirror_x != 0, x1, x2, dx);
+		tex_axis(yf, T.h, rep, T.mirror_y != 0, y1, y2, dy);
 		c = __ldg(tx + y1 * T.w + x1);
 	}
 	else
@@ -854,8 +869,8 @@ __device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p
 		const float yf = xs(xm(static_cast<float>(T.h), xs(my, floorf(my))), 0.5f);
 		int x1, x2, y1, y2;
 		float dx, dy;
-		tex_axis(xf, T.w, rep, x1, x2, dx);
-		tex_axis(yf, T.h, rep, y1, y2, dy);
+		tex_axis(xf, T.w, rep, T.mirror_x != 0, x1, x2, dx);
+		tex_axis(yf, T.h, rep, T.mirror_y != 0, y1, y2, dy);
 		const float4 c11 = __ldg(tx + y1 * T.w + x1), c21 = __ldg(tx + y1 * T.w + x2);
 		const float4 c12 = __ldg(tx + y2 * T.w + x1), c22 = __ldg(tx + y2 * T.w + x2);
 		const float w11 = xm(xs(1.f, dx), xs(1.f, dy)), w12 = xm(xs(1.f, dx), dy);
@@ -3622,6 +3637,7 @@ int gbrt_scene_set_textures(gbrt_scene *S, const float *uv, uint32_t n_uv, const
 		if(t.blend_mode > GBRT_BLEND_LIGHTEN) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u: blend mode %u", i, t.blend_mode);
 		d.blend = static_cast<int>(t.blend_mode);
 		d.negative = t.negative ? 1 : 0; d.no_rgb = t.no_rgb ? 1 : 0; d.stencil = t.stencil ? 1 : 0;
+		d.mirror_x = t.mirror_x ? 1 : 0; d.mirror_y = t.mirror_y ? 1 : 0;
 		d.colfac = t.colfac;
 		for(int k = 0; k < 4; ++k) d.upper[k] = t.upper_color[k];
 		for(int k = 0; k < 3; ++k) d.def_col[k] = t.def_col[k];

@@ -99,7 +99,8 @@ class TextureDesc(ctypes.Structure):
                 ("mapping", ctypes.c_uint32), ("scale", ctypes.c_float * 3), ("offset", ctypes.c_float * 3),
                 ("proj", ctypes.c_int32 * 3), ("layer", ctypes.c_int32), ("blend_mode", ctypes.c_uint32),
                 ("colfac", ctypes.c_float), ("upper_color", ctypes.c_float * 4), ("def_col", ctypes.c_float * 3),
-                ("negative", ctypes.c_int32), ("no_rgb", ctypes.c_int32), ("stencil", ctypes.c_int32)]
+                ("negative", ctypes.c_int32), ("no_rgb", ctypes.c_int32), ("stencil", ctypes.c_int32),
+                ("mirror_x", ctypes.c_int32), ("mirror_y", ctypes.c_int32)]
 
 
 # ImageTexture / TextureMapperNode enum names (texture_image.h, shader_node_texture.h)
@@ -125,6 +126,7 @@ def texture_desc(t):
     d.crop[:] = [float(t.get("cropmin_x", 0.0)), float(t.get("cropmin_y", 0.0)), float(t.get("cropmax_x", 1.0)),
                  float(t.get("cropmax_y", 1.0))]
     d.rot90 = int(bool(t.get("rot90", False)))
+    d.mirror_x, d.mirror_y = int(bool(t.get("mirror_x", False))), int(bool(t.get("mirror_y", False)))
     d.adj_intensity, d.adj_contrast = float(t.get("adj_intensity", 1.0)), float(t.get("adj_contrast", 1.0))
     d.adj_mult_factor[:] = [float(t.get("adj_mult_factor_red", 1.0)), float(t.get("adj_mult_factor_green", 1.0)),
                             float(t.get("adj_mult_factor_blue", 1.0))]

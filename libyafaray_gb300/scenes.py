@@ -388,14 +388,14 @@ def checker_image(w=16, h=16, c0=(0.9, 0.2, 0.1), c1=(0.1, 0.3, 0.8), seed=7):
 def textured_cornell_scene(res=64, **kw):
     """The Cornell box with image textures: the back wall carries uvs
     (0..1 across it) and a UV-mapped checker texture (bilinear, repeat
-    x 2 / y 1); the tall box takes a second texture through global
+    x 2 / y 1, mirror_x); the tall box takes a second texture through global
     coordinates with cube mapping (scale 1.5, offset, clip extend, no
     interpolation) through a layer node (multiply, colfac 0.8 over the
     material colour).  Everything else is the plain Cornell box."""
     sc = cornell_scene(res=res, **kw)
     sc["textures"] = {
         "checker": {"image": checker_image(16, 16), "interpolate": "bilinear", "clipping": "repeat",
-                    "xrepeat": 2, "yrepeat": 1, "texco": "uv", "mapping": "plain"},
+                    "xrepeat": 2, "yrepeat": 1, "mirror_x": True, "texco": "uv", "mapping": "plain"},
         "tiles": {"image": checker_image(8, 8, (0.8, 0.8, 0.3), (0.2, 0.7, 0.3), seed=11), "interpolate": "none",
                   "clipping": "extend", "texco": "global", "mapping": "cube", "scale": (1.5, 1.5, 1.5),
                   "offset": (0.1, 0.0, 0.2), "adj_intensity": 1.1, "adj_contrast": 0.9,
