@@ -331,7 +331,7 @@ int gbrt_scene_destroy(gbrt_scene *scene);
  * emission).  Parameter names and defaults [..] are the reference's. */
 enum { GBRT_TEXCO_GLOBAL = 0, GBRT_TEXCO_UV = 1 };                 /* "texco" ["global"] */
 enum { GBRT_MAPPING_PLAIN = 0, GBRT_MAPPING_CUBE = 1 };            /* "mapping" ["plain"] */
-enum { GBRT_CLIP_EXTEND = 0, GBRT_CLIP_CLIP = 1, GBRT_CLIP_CLIPCUBE = 2, GBRT_CLIP_REPEAT = 3 };   /* "clipping" ["repeat"] */
+enum { GBRT_CLIP_EXTEND = 0, GBRT_CLIP_CLIP = 1, GBRT_CLIP_CLIPCUBE = 2, GBRT_CLIP_REPEAT = 3, GBRT_CLIP_CHECKER = 4 };   /* "clipping" ["repeat"] */
 enum { GBRT_INTERP_NONE = 0, GBRT_INTERP_BILINEAR = 1 };           /* "interpolate" ["bilinear"] */
 
 typedef struct gbrt_texture_desc {
@@ -362,6 +362,8 @@ typedef struct gbrt_texture_desc {
 	float def_col[3];           /* [1, 1, 1] */
 	int32_t negative, no_rgb, stencil;   /* "negative", "noRGB", "stencil" [0] */
 	int32_t mirror_x, mirror_y; /* "mirror_x", "mirror_y" [0]: every other repeat mirrored (clipping repeat) */
+	int32_t even_tiles, odd_tiles;       /* clipping checker: "even_tiles" [0], "odd_tiles" [1] (set it: 0 hides those tiles) */
+	float checker_dist;         /* "checker_dist" [0]: tiles shrunk about their centres by 1 / (1 - checker_dist) */
 } gbrt_texture_desc;
 enum { GBRT_BLEND_MIX = 0, GBRT_BLEND_ADD = 1, GBRT_BLEND_MULTIPLY = 2, GBRT_BLEND_SUBTRACT = 3, GBRT_BLEND_SCREEN = 4,
        GBRT_BLEND_DIVIDE = 5, GBRT_BLEND_DIFFERENCE = 6, GBRT_BLEND_DARKEN = 7, GBRT_BLEND_LIGHTEN = 8 };

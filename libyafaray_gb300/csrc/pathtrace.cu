@@ -84,6 +84,8 @@ struct DevTexture {
 	int layer, blend, negative, no_rgb, stencil;   // LayerNode over the mapper
 	int mirror_x, mirror_y;
 	float colfac, upper[4], def_col[3];
+	int even_tiles, odd_tiles;  // clipping checker
+	float checker_dist;
 };
 
 struct DevLight {
@@ -843,6 +845,25 @@ __device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p
 	if(T.rot90) { const float tmp = mx; mx = my; my = tmp; }
 	bool outside = false;
 	if(T.clip == GBRT_CLIP_CLIPCUBE) outside = mx < 0.f || mx > 1.f || my < 0.f || my > 1.f || mz < -1.f || mz > 1.f;
+	else if(T.clip == GBRT_CLIP_CHECKER)
+	{
+		const float fx = floorf(mx), fy = floorf(my);
+		mx = xs(mx, fx);
+		my = xs(my, fy);
+		const bool odd = (static_cast<int>(xa(fx, fy)) & 1) != 0;
+		if(!T.odd_tiles && !odd) outside = true;
+		else if(!T.even_tiles && odd) outside = true;
+		else
+		{
+			// scaled about the tile centre, then the clip test
+			if(T.checker_dist < 1.f)
+			{
+				mx = xa(__fdiv_rn(xs(mx, 0.5f), xs(1.f, T.checker_dist)), 0.5f);
+				my = xa(__fdiv_rn(xs(my, 0.5f), xs(1.f, T.checker_dist)), 0.5f);
+			}
+			outside = mx < 0.f || mx > 1.f || my < 0.f || my > 1.f;
+		}
+	}
 	else if(T.clip == GBRT_CLIP_CLIP) outside = mx < 0.f || mx > 1.f || my < 0.f || my > 1.f;
 	else if(T.clip == GBRT_CLIP_EXTEND)
 	{
@@ -3618,7 +3639,7 @@ int gbrt_scene_set_textures(gbrt_scene *S, const float *uv, uint32_t n_uv, const
 		const gbrt_texture_desc &t = textures[i];
 		if(t.width <= 0 || t.height <= 0 || !t.rgba)
 			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u has no image (%d x %d)", i, t.width, t.height);
-		if(t.interpolate > GBRT_INTERP_BILINEAR || t.clipping > GBRT_CLIP_REPEAT || t.texco > GBRT_TEXCO_UV || t.mapping > GBRT_MAPPING_CUBE)
+		if(t.interpolate > GBRT_INTERP_BILINEAR || t.clipping > GBRT_CLIP_CHECKER || t.texco > GBRT_TEXCO_UV || t.mapping > GBRT_MAPPING_CUBE)
 			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u: unsupported interpolate / clipping / texco / mapping", i);
 		DevTexture &d = tex[i];
 		d.off = static_cast<uint32_t>(n_texels);
@@ -3638,6 +3659,8 @@ int gbrt_scene_set_textures(gbrt_scene *S, const float *uv, uint32_t n_uv, const
 		d.blend = static_cast<int>(t.blend_mode);
 		d.negative = t.negative ? 1 : 0; d.no_rgb = t.no_rgb ? 1 : 0; d.stencil = t.stencil ? 1 : 0;
 		d.mirror_x = t.mirror_x ? 1 : 0; d.mirror_y = t.mirror_y ? 1 : 0;
+		d.even_tiles = t.even_tiles ? 1 : 0; d.odd_tiles = t.odd_tiles ? 1 : 0;
+		d.checker_dist = t.checker_dist;
 		d.colfac = t.colfac;
 		for(int k = 0; k < 4; ++k) d.upper[k] = t.upper_color[k];
 		for(int k = 0; k < 3; ++k) d.def_col[k] = t.def_col[k];

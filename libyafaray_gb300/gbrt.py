@@ -100,13 +100,14 @@ class TextureDesc(ctypes.Structure):
                 ("proj", ctypes.c_int32 * 3), ("layer", ctypes.c_int32), ("blend_mode", ctypes.c_uint32),
                 ("colfac", ctypes.c_float), ("upper_color", ctypes.c_float * 4), ("def_col", ctypes.c_float * 3),
                 ("negative", ctypes.c_int32), ("no_rgb", ctypes.c_int32), ("stencil", ctypes.c_int32),
-                ("mirror_x", ctypes.c_int32), ("mirror_y", ctypes.c_int32)]
+                ("mirror_x", ctypes.c_int32), ("mirror_y", ctypes.c_int32), ("even_tiles", ctypes.c_int32),
+                ("odd_tiles", ctypes.c_int32), ("checker_dist", ctypes.c_float)]
 
 
 # ImageTexture / TextureMapperNode enum names (texture_image.h, shader_node_texture.h)
 TEXCO = {"global": 0, "uv": 1}
 MAPPING = {"plain": 0, "cube": 1}
-CLIPPING = {"extend": 0, "clip": 1, "clipcube": 2, "repeat": 3}
+CLIPPING = {"extend": 0, "clip": 1, "clipcube": 2, "repeat": 3, "checker": 4}
 INTERPOLATE = {"none": 0, "bilinear": 1}
 BLEND_MODES = {"mix": 0, "add": 1, "multiply": 2, "subtract": 3, "screen": 4, "divide": 5, "difference": 6, "darken": 7,
                "lighten": 8}
@@ -127,6 +128,8 @@ def texture_desc(t):
                  float(t.get("cropmax_y", 1.0))]
     d.rot90 = int(bool(t.get("rot90", False)))
     d.mirror_x, d.mirror_y = int(bool(t.get("mirror_x", False))), int(bool(t.get("mirror_y", False)))
+    d.even_tiles, d.odd_tiles = int(bool(t.get("even_tiles", False))), int(bool(t.get("odd_tiles", True)))
+    d.checker_dist = float(t.get("checker_dist", 0.0))
     d.adj_intensity, d.adj_contrast = float(t.get("adj_intensity", 1.0)), float(t.get("adj_contrast", 1.0))
     d.adj_mult_factor[:] = [float(t.get("adj_mult_factor_red", 1.0)), float(t.get("adj_mult_factor_green", 1.0)),
                             float(t.get("adj_mult_factor_blue", 1.0))]

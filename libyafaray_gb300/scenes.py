@@ -391,7 +391,9 @@ def textured_cornell_scene(res=64, **kw):
     x 2 / y 1, mirror_x); the tall box takes a second texture through global
     coordinates with cube mapping (scale 1.5, offset, clip extend, no
     interpolation) through a layer node (multiply, colfac 0.8 over the
-    material colour).  Everything else is the plain Cornell box."""
+    material colour); the short box a checker-clipped texture (odd tiles,
+    checker_dist 0.2) in global coordinates.  Everything else is the plain
+    Cornell box."""
     sc = cornell_scene(res=res, **kw)
     sc["textures"] = {
         "checker": {"image": checker_image(16, 16), "interpolate": "bilinear", "clipping": "repeat",
@@ -400,9 +402,13 @@ def textured_cornell_scene(res=64, **kw):
                   "clipping": "extend", "texco": "global", "mapping": "cube", "scale": (1.5, 1.5, 1.5),
                   "offset": (0.1, 0.0, 0.2), "adj_intensity": 1.1, "adj_contrast": 0.9,
                   "layer": {"blend_mode": "multiply", "colfac": 0.8, "upper_color": (0.75, 0.75, 0.75, 1.0)}},
+        "checks": {"image": checker_image(8, 8, (0.9, 0.5, 0.2), (0.3, 0.3, 0.9), seed=13), "interpolate": "bilinear",
+                   "clipping": "checker", "checker_dist": 0.2, "texco": "global", "mapping": "plain",
+                   "scale": (2.0, 2.0, 2.0)},
     }
     sc["materials"]["back_tex"] = ("shinydiffusemat", (0.75, 0.75, 0.75), {"diffuse_texture": "checker"})
     sc["materials"]["box_tex"] = ("shinydiffusemat", (0.75, 0.75, 0.75), {"diffuse_texture": "tiles"})
+    sc["materials"]["box2_tex"] = ("shinydiffusemat", (0.75, 0.75, 0.75), {"diffuse_texture": "checks"})
     objs = []
     for o in sc["objects"]:
         v = np.asarray(o["vertices"], np.float32)
@@ -423,6 +429,8 @@ def textured_cornell_scene(res=64, **kw):
                          "uvs": uvs, "face_uvs": fuv})
         elif o["name"] == "group4":
             objs.append({**o, "material": "box_tex"})
+        elif o["name"] == "group3":
+            objs.append({**o, "material": "box2_tex"})
         else:
             objs.append(o)
     sc["objects"] = objs

@@ -132,7 +132,7 @@ def reference_scene_text(scene, spp, batches, threads=-1, offset_stride=None):
     """Scene dict (libyafaray_gb300.scenes) -> render_dump input text."""
     out = []
     tex_keys = ("interpolate", "clipping", "xrepeat", "yrepeat", "cropmin_x", "cropmin_y", "cropmax_x", "cropmax_y",
-                "rot90", "mirror_x", "mirror_y", "adj_intensity", "adj_contrast", "adj_mult_factor_red", "adj_mult_factor_green",
+                "rot90", "mirror_x", "mirror_y", "even_tiles", "odd_tiles", "checker_dist", "adj_intensity", "adj_contrast", "adj_mult_factor_red", "adj_mult_factor_green",
                 "adj_mult_factor_blue", "adj_clamp")
 
     def fmt(v):
