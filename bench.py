@@ -276,7 +276,8 @@ def next_rows_section():
                                           "reference_s": 17.2, "reference_note": ref_note}
     del r
     r = gbrt.Renderer(scenes.textured_cornell_scene(res=512))
-    out["textured_cornell"] = {"workload": "Cornell 512x512 16 spp, UV-mapped bilinear checker + cube-mapped global texture",
+    out["textured_cornell"] = {"workload": "Cornell 512x512 16 spp, UV-mapped mirrored checker, cube-mapped global texture "
+                                                 "through a layer node, checker-clipped global texture",
                                "ms_per_frame": frame_ms(r, 16), "reference_s": 4.39, "reference_note": ref_note}
     del r
     r = gbrt.Renderer(scenes.cornell_sppm_scene(res=512, photons=1_000_000, passes=16))
