@@ -10,6 +10,14 @@ batch, 32 batches with distinct adv_base_sampling_offset; per-pixel mean and
 standard error of the batch means.
 sampler.npz: the reference's lowDiscrepancySampling / riVdC / riLp / riS /
 fnv32ABuf / Halton(2,3) / FAST_TRIG sin and cos on a fixed input grid.
+
+Other groups, by command-line name (python make_render_golden.py NAME ...):
+cornell_glossy, cornell_glass, cornell_point, cornell_shiny, indoor, pm,
+cornell_pm, dl, batch, hashgrid, film (gauss film), aa (adaptive-AA film
+states + flags and an adaptive render), aa_pm (adaptive passes of
+photonmapping / directlighting), cornell_tshadow (transparent shadows,
+shadowDepth 4 and 1), cornell_textured (image textures, mapper and layer
+nodes), cornell_sppm (SPPM with and without pmIRE).
 """
 import os
 import struct
