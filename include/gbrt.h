@@ -129,9 +129,11 @@ int gbrt_bvh_destroy(gbrt_bvh *bvh);
  * The build's temporary arrays live in one fixed device array inside the
  * library, sized for GBRT_STATIC_MAX_FACES faces (about 7 MB, held on every
  * GPU that loads the library until the process exits).  More faces return
- * GBRT_ERR_CAPACITY.  The first call on a device looks up that array's
- * device address (cudaGetSymbolAddress); make that first call before any
- * stream capture.  Every call, on every stream, shares the array: calls that
+ * GBRT_ERR_CAPACITY.  Every call looks up that array's device address in
+ * the current context (cudaGetSymbolAddress; the first call on a device also
+ * loads the library's module there), so a device reset or a new context is
+ * picked up; make the first call on a device before any stream capture.
+ * Every call, on every stream, shares the array: calls that
  * overlap on the GPU race and corrupt each other's result, so serialise
  * them.  Synchronises `stream` before returning. */
 int gbrt_bvh_build_static(const float *vertices_dev, uint32_t n_vertices,
@@ -322,6 +324,40 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
                       const gbrt_light_desc *lights, uint32_t n_lights, gbrt_scene **out);
 int gbrt_scene_destroy(gbrt_scene *scene);
 
+/* ---- per-vertex shading normals ------------------------------------------
+ * A face whose vertices carry normals shades with the barycentric (quads:
+ * bilinear) interpolation of them, normalised, instead of its geometric
+ * normal: the smooth branch of PrimitivePolygon::getSurfacePolygon
+ * (src/geometry/primitive/primitive_polygon.cc:49-56); a vertex without a
+ * normal (GBRT_NO_NORMAL) contributes the face's geometric normal
+ * (FacePrimitive::getVertexNormal, primitive_face.h:106-110). */
+#define GBRT_NO_NORMAL 0xFFFFFFFFu
+/* First index of a face that shades with its geometric normal (a face of a
+ * mesh without vertex normals, PrimitivePolygon's flat branch). */
+#define GBRT_FLAT_FACE 0xFFFFFFFEu
+
+/* The reference's yafaray_smoothObjectMesh(angle) on one mesh object
+ * (MeshObject::smoothVerticesNormals, src/geometry/object/object_mesh.cc:150-262),
+ * on the host: angle >= 180 averages every face at a vertex (weighted by the
+ * corner angle, one normal per vertex); 0.1 < angle < 180 smooths across
+ * faces whose normals lie within `angle` degrees (new normals appended after
+ * n_vertices zero entries); otherwise no normals.  Outputs: normals (3
+ * floats each, capacity normals_cap; NULL to query *n_normals only) and
+ * face_normals (4 indices per face, GBRT_NO_NORMAL where the face keeps its
+ * geometric normal).  At most n_vertices + 4 * n_faces normals. */
+int gbrt_mesh_smooth_normals(const float *vertices, uint32_t n_vertices, const uint32_t *faces, uint32_t n_faces,
+                             float angle, float *normals, uint32_t normals_cap, uint32_t *n_normals,
+                             uint32_t *face_normals);
+
+/* Shading normals of a scene's faces (replacing any set before): normals
+ * (n_normals x 3 floats, the vertex normals of yafaray_addNormal or
+ * gbrt_mesh_smooth_normals) and face_normals (4 indices per face of
+ * gbrt_scene_create, the 4th unused for triangles, GBRT_NO_NORMAL for a
+ * vertex without a normal, GBRT_FLAT_FACE first for a face of a mesh
+ * without vertex normals).  NULL face_normals returns every face to its
+ * geometric normal.  Fewer than 0xFFFFFFFD normals. */
+int gbrt_scene_set_normals(gbrt_scene *scene, const float *normals, uint32_t n_normals, const uint32_t *face_normals);
+
 /* ---- image textures on shinydiffuse diffuse colour ----------------------
  * An ImageTexture (src/texture/texture_image.cc) over an in-memory float
  * image, reached through a TextureMapperNode (src/shader/shader_node_texture.cc)
@@ -373,7 +409,9 @@ enum { GBRT_BLEND_MIX = 0, GBRT_BLEND_ADD = 1, GBRT_BLEND_MULTIPLY = 2, GBRT_BLE
  * face of gbrt_scene_create, the uv indices of its vertices (the 4th unused
  * for triangles), or NULL (no uvs: the implicit barycentric uv).
  * material_diffuse_texture[m]: texture index driving material m's diffuse
- * colour, -1 for none (n_materials entries; shinydiffuse materials only). */
+ * colour, -1 for none (n_materials entries; shinydiffuse materials only).
+ * Limits: fewer than 2^31 texels per texture and 2^32 in all (else
+ * GBRT_ERR_CAPACITY). */
 int gbrt_scene_set_textures(gbrt_scene *scene, const float *uv, uint32_t n_uv, const uint32_t *face_uv,
                             const gbrt_texture_desc *textures, uint32_t n_textures,
                             const int32_t *material_diffuse_texture, uint32_t n_materials);

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbrt.so")
 
-SOURCES = ["capi.cu", "bvh_build.cu", "traverse.cu", "pathtrace.cu", "guiding.cu"]
+SOURCES = ["capi.cu", "bvh_build.cu", "traverse.cu", "pathtrace.cu", "guiding.cu", "mesh.cu"]
 EXACT_FP = {"traverse.cu", "pathtrace.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -35,7 +35,6 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
-#include <mutex>
 
 namespace {
 
@@ -1244,25 +1243,18 @@ constexpr size_t kStaticScratchBytes = static_layout(GBRT_STATIC_MAX_FACES).tota
 // Shared by every call on a device; see gbrt_bvh_build_static in gbrt.h.
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_static_mu;
-unsigned char *g_static_addr[kMaxDevices] = {};
-
-// Device address of g_static_scratch on the current device, looked up once
-// per device (host code must not use the symbol itself as a pointer).
-int static_scratch_address(int dev, unsigned char **out)
+// Device address of g_static_scratch in the current device's context (host
+// code must not use the symbol itself as a pointer).  Looked up on every call,
+// not cached: after cudaDeviceReset, or in another context on the same
+// device, the module is loaded again at a new address.  Once the module is
+// loaded the lookup allocates nothing.
+int static_scratch_address(unsigned char **out)
 {
-	if(dev < 0 || dev >= kMaxDevices) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_bvh_build_static: device %d out of range", dev);
-	std::lock_guard<std::mutex> g(g_static_mu);
-	if(!g_static_addr[dev])
-	{
-		void *p = nullptr;
-		const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-		if(e != cudaSuccess || !p)
-			return gbrt_set_error(GBRT_ERR_CUDA, "gbrt_bvh_build_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-		g_static_addr[dev] = static_cast<unsigned char *>(p);
-	}
-	*out = g_static_addr[dev];
+	void *p = nullptr;
+	const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+	if(e != cudaSuccess || !p)
+		return gbrt_set_error(GBRT_ERR_CUDA, "gbrt_bvh_build_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+	*out = static_cast<unsigned char *>(p);
 	return GBRT_OK;
 }
 
@@ -1289,10 +1281,8 @@ extern "C" int gbrt_bvh_build_static(const float *verts, uint32_t nv, const uint
 	if(p.max_leaf_size > GBRT_LEAF_MAX_COUNT) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_bvh_build_static: max_leaf_size %u > %u", p.max_leaf_size, GBRT_LEAF_MAX_COUNT);
 	if(!(p.traversal_cost > 0.f)) p.traversal_cost = 1.f;
 	if(!(p.intersect_cost > 0.f)) p.intersect_cost = 1.f;
-	int dev = 0;
-	GBRT_CK(cudaGetDevice(&dev));
 	unsigned char *base = nullptr;
-	if(int rc = static_scratch_address(dev, &base)) return rc;
+	if(int rc = static_scratch_address(&base)) return rc;
 
 	const StaticLayout L = static_layout(nf);
 	float *meta = reinterpret_cast<float *>(base + L.meta);

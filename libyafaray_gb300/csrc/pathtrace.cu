@@ -202,6 +202,9 @@ struct SceneDev {
 	const float4 *texels;
 	const float2 *uv;
 	const uint4 *face_uv;       // uv indices per face; x = kNoIdx: no uvs; w = kNoIdx: triangle
+	// shading normals (gbrt_scene_set_normals); null without
+	const float4 *vnrm;         // vertex normals
+	const uint4 *face_nrm;      // normal indices per face; x = kFlatFace: geometric normal; w = kTriFace: triangle
 };
 
 __device__ __forceinline__ float dot3(const float a[3], const float b[3]) { return xa(xa(xm(a[0], b[0]), xm(a[1], b[1])), xm(a[2], b[2])); }
@@ -726,6 +729,46 @@ __device__ __forceinline__ void hit_uv(const SceneDev &sc, int prim, float bu, f
 	const float iu = xs(1.f, bu), iv = xs(1.f, bv);
 	uv[0] = xa(xm(iv, xa(xm(iu, a.x), xm(bu, b.x))), xm(bv, xa(xm(iu, d.x), xm(bu, c.x))));
 	uv[1] = xa(xm(iv, xa(xm(iu, a.y), xm(bu, b.y))), xm(bv, xa(xm(iu, d.y), xm(bu, c.y))));
+}
+
+// ---- shading normals --------------------------------------------------------
+constexpr uint32_t kFlatFace = 0xFFFFFFFEu;   // face_nrm.x: the face shades with its geometric normal
+constexpr uint32_t kTriFace = 0xFFFFFFFDu;    // face_nrm.w: the face is a triangle
+
+// Shading normal of a hit (PrimitivePolygon::getSurfacePolygon,
+// primitive_polygon.cc:49-56): a face of a mesh with vertex normals takes
+// its vertices' normals (a vertex without one contributes the geometric
+// normal, FacePrimitive::getVertexNormal, primitive_face.h:106-110) at the
+// barycentric weights (1 - u - v, u, v), a quad's by ShapePolygon::interpolate
+// (shape_polygon.h:94-100), normalised; other faces the geometric normal.
+__device__ __forceinline__ void shading_normal(const SceneDev &sc, int prim, float bu, float bv, const float ng[3], float n[3])
+{
+	n[0] = ng[0]; n[1] = ng[1]; n[2] = ng[2];
+	if(!sc.face_nrm) return;
+	const uint4 f = __ldg(sc.face_nrm + prim);
+	if(f.x == kFlatFace) return;
+	auto vn = [&](uint32_t i) {
+		if(i == GBRT_NO_NORMAL) return make_float3(ng[0], ng[1], ng[2]);
+		const float4 q = __ldg(sc.vnrm + i);
+		return make_float3(q.x, q.y, q.z);
+	};
+	const float3 a = vn(f.x), b = vn(f.y), c = vn(f.z);
+	if(f.w == kTriFace)
+	{
+		const float w0 = xs(xs(1.f, bu), bv);
+		n[0] = xa(xa(xm(w0, a.x), xm(bu, b.x)), xm(bv, c.x));
+		n[1] = xa(xa(xm(w0, a.y), xm(bu, b.y)), xm(bv, c.y));
+		n[2] = xa(xa(xm(w0, a.z), xm(bu, b.z)), xm(bv, c.z));
+	}
+	else
+	{
+		const float3 d = vn(f.w);
+		const float iu = xs(1.f, bu), iv = xs(1.f, bv);
+		n[0] = xa(xm(iv, xa(xm(iu, a.x), xm(bu, b.x))), xm(bv, xa(xm(iu, d.x), xm(bu, c.x))));
+		n[1] = xa(xm(iv, xa(xm(iu, a.y), xm(bu, b.y))), xm(bv, xa(xm(iu, d.y), xm(bu, c.y))));
+		n[2] = xa(xm(iv, xa(xm(iu, a.z), xm(bu, b.z))), xm(bv, xa(xm(iu, d.z), xm(bu, c.z))));
+	}
+	normalize3(n);
 }
 
 // ImageTexture::findTextureInterpolationCoordinates (texture_image.cc:
@@ -1740,7 +1783,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				s.p[0] = xa(ra.x, xm(h.y, dir[0])); s.p[1] = xa(ra.y, xm(h.y, dir[1])); s.p[2] = xa(ra.z, xm(h.y, dir[2]));
 				const float4 ng = __ldg(sc.prim_ng + prim);
 				s.ng[0] = ng.x; s.ng[1] = ng.y; s.ng[2] = ng.z;
-				s.n[0] = ng.x; s.n[1] = ng.y; s.n[2] = ng.z;
+				shading_normal(sc, prim, h.z, h.w, s.ng, s.n);
 				s.m = sc.mats + __float_as_uint(ng.w);
 				coords_system(s.n, s.u, s.v);
 				surface_color(sc, s, prim, h.z, h.w);
@@ -2092,16 +2135,17 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 }
 
 // Material::getTransparency of a shadow-ray hit, wo = the shadow ray's
-// direction, n = the flat normal face-forwarded (SurfacePoint::
-// normalFaceForward): ShinyDiffuseMaterial (material_shiny_diffuse.cc:541-563:
+// direction, n = the shading normal face-forwarded by the geometric one
+// (SurfacePoint::normalFaceForward): ShinyDiffuseMaterial (material_shiny_diffuse.cc:541-563:
 // accum = 1 - kr x specular_reflect with a mirror layer, then
 // accum *= transparency x accum, times the transmit colour) and Glass /
 // RoughGlass (material_glass.cc:297-303, material_rough_glass.cc:349-355:
 // kt x filter colour).
-__device__ __forceinline__ void mat_transparency(const DevMaterial &m, const float ng[3], const float wo[3], const float *dcol, float out[3])
+__device__ __forceinline__ void mat_transparency(const DevMaterial &m, const float ng[3], const float ns[3], const float wo[3], const float *dcol,
+                                                 float out[3])
 {
 	const bool flip = dot3(ng, wo) < 0.f;
-	const float n[3] = {flip ? -ng[0] : ng[0], flip ? -ng[1] : ng[1], flip ? -ng[2] : ng[2]};
+	const float n[3] = {flip ? -ns[0] : ns[0], flip ? -ns[1] : ns[1], flip ? -ns[2] : ns[2]};
 	if(m.type == GBRT_MAT_SHINYDIFFUSE)
 	{
 		const float kr = shiny_kr(m, wo, n);
@@ -2146,8 +2190,9 @@ struct TransparentHits {
 			hit_uv(*sc, prim, u, v, uv);
 			tex_color(*sc, sc->tex[m.dtex], p, ng, uv, dcol);
 		}
-		float tr[3];
-		mat_transparency(m, ng, dir, dcol, tr);
+		float ns[3], tr[3];
+		shading_normal(*sc, prim, u, v, ng, ns);
+		mat_transparency(m, ng, ns, dir, dcol, tr);
 		for(int k = 0; k < 3; ++k) col[k] *= tr[k];
 		++depth;
 		return false;
@@ -2636,7 +2681,7 @@ __global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJo
 			for(int k = 0; k < 3; ++k) s.p[k] = xa(o[k], xm(h.t, d[k]));
 			const float4 ng = __ldg(sc.prim_ng + h.prim);
 			s.ng[0] = ng.x; s.ng[1] = ng.y; s.ng[2] = ng.z;
-			s.n[0] = ng.x; s.n[1] = ng.y; s.n[2] = ng.z;
+			shading_normal(sc, h.prim, h.u, h.v, s.ng, s.n);
 			s.m = sc.mats + __float_as_uint(ng.w);
 			coords_system(s.n, s.u, s.v);
 			surface_color(sc, s, h.prim, h.u, h.v);
@@ -2724,7 +2769,7 @@ __global__ void __launch_bounds__(kThreads) k_pm_root(SceneDev sc, Params P, Wor
 		const float dir[3] = {rb.x, rb.y, rb.z};
 		s.p[0] = xa(ra.x, xm(h.y, dir[0])); s.p[1] = xa(ra.y, xm(h.y, dir[1])); s.p[2] = xa(ra.z, xm(h.y, dir[2]));
 		s.ng[0] = ng.x; s.ng[1] = ng.y; s.ng[2] = ng.z;
-		s.n[0] = ng.x; s.n[1] = ng.y; s.n[2] = ng.z;
+		shading_normal(sc, prim, h.z, h.w, s.ng, s.n);
 		coords_system(s.n, s.u, s.v);
 		surface_color(sc, s, prim, h.z, h.w);
 		const float wo[3] = {-dir[0], -dir[1], -dir[2]};
@@ -3053,6 +3098,9 @@ struct gbrt_scene {
 	float2 *uv = nullptr;
 	uint4 *face_uv = nullptr;
 	std::vector<uint8_t> face_quad;     // per face: a quad (for the implicit uv)
+	// shading normals (gbrt_scene_set_normals)
+	float4 *vnrm = nullptr;
+	uint4 *face_nrm = nullptr;
 	std::vector<DevMaterial> mats_host;
 	std::mutex mu;
 };
@@ -3398,7 +3446,7 @@ int shoot_map(gbrt_scene *S, const SceneDev &sc, bool caustic, uint32_t n, int m
 SceneDev scene_dev(const gbrt_scene *S)
 {
 	return SceneDev{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off, S->lds_sfac_nd},
-	                S->tex, S->texels, S->uv, S->face_uv};
+	                S->tex, S->texels, S->uv, S->face_uv, S->vnrm, S->face_nrm};
 }
 
 } // namespace
@@ -3639,6 +3687,10 @@ int gbrt_scene_set_textures(gbrt_scene *S, const float *uv, uint32_t n_uv, const
 		const gbrt_texture_desc &t = textures[i];
 		if(t.width <= 0 || t.height <= 0 || !t.rgba)
 			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u has no image (%d x %d)", i, t.width, t.height);
+		// the lookups index a texture's texels with 32-bit ints (y * w + x)
+		if(static_cast<uint64_t>(t.width) * static_cast<uint64_t>(t.height) >= (1ull << 31))
+			return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_scene_set_textures: texture %u has %d x %d texels (at most 2^31 - 1 per texture)",
+			                      i, t.width, t.height);
 		if(t.interpolate > GBRT_INTERP_BILINEAR || t.clipping > GBRT_CLIP_CHECKER || t.texco > GBRT_TEXCO_UV || t.mapping > GBRT_MAPPING_CUBE)
 			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u: unsupported interpolate / clipping / texco / mapping", i);
 		DevTexture &d = tex[i];
@@ -3715,13 +3767,49 @@ int gbrt_scene_set_textures(gbrt_scene *S, const float *uv, uint32_t n_uv, const
 	return GBRT_OK;
 }
 
+int gbrt_scene_set_normals(gbrt_scene *S, const float *normals, uint32_t n_normals, const uint32_t *face_normals)
+{
+	if(!S) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_normals: NULL scene");
+	if(n_normals && !normals) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_normals: NULL normals");
+	if(n_normals >= kTriFace) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_scene_set_normals: %u normals", n_normals);
+	std::vector<float4> vn(std::max<uint32_t>(1, n_normals), make_float4(0.f, 0.f, 0.f, 0.f));
+	for(uint32_t i = 0; i < n_normals; ++i) vn[i] = make_float4(normals[3ull * i], normals[3ull * i + 1], normals[3ull * i + 2], 0.f);
+	std::vector<uint4> fn;
+	if(face_normals)
+	{
+		fn.resize(std::max<uint32_t>(1, S->n_prims));
+		for(uint32_t f = 0; f < S->n_prims; ++f)
+		{
+			const uint32_t *q = face_normals + 4ull * f;
+			const bool quad = S->face_quad[f] != 0;
+			if(q[0] == GBRT_FLAT_FACE) { fn[f] = make_uint4(kFlatFace, kFlatFace, kFlatFace, quad ? kFlatFace : kTriFace); continue; }
+			for(int k = 0; k < (quad ? 4 : 3); ++k)
+				if(q[k] != GBRT_NO_NORMAL && q[k] >= n_normals)
+					return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_normals: face %u uses normal %u of %u", f, q[k], n_normals);
+			fn[f] = make_uint4(q[0], q[1], q[2], quad ? q[3] : kTriFace);
+		}
+	}
+	std::lock_guard<std::mutex> lock(S->mu);
+	if(S->ev_last) GBRT_CK(cudaEventSynchronize(S->ev_last));
+	for(void *p : {static_cast<void *>(S->vnrm), static_cast<void *>(S->face_nrm)})
+		if(p) cudaFree(p);
+	S->vnrm = nullptr; S->face_nrm = nullptr;
+	if(!face_normals) return GBRT_OK;
+	GBRT_CK(cudaMalloc(reinterpret_cast<void **>(&S->vnrm), vn.size() * sizeof(float4)));
+	GBRT_CK(cudaMemcpy(S->vnrm, vn.data(), vn.size() * sizeof(float4), cudaMemcpyHostToDevice));
+	GBRT_CK(cudaMalloc(reinterpret_cast<void **>(&S->face_nrm), fn.size() * sizeof(uint4)));
+	GBRT_CK(cudaMemcpy(S->face_nrm, fn.data(), fn.size() * sizeof(uint4), cudaMemcpyHostToDevice));
+	return GBRT_OK;
+}
+
 int gbrt_scene_destroy(gbrt_scene *S)
 {
 	if(!S) return GBRT_OK;
 	void *ptrs[] = {S->prim_ng, S->mats, S->lights, S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off,
 	                S->lds_sfac_nd, S->work, S->spawn, S->spawn_count};
 	for(void *p : ptrs) if(p) cudaFree(p);
-	for(void *p : {static_cast<void *>(S->tex), static_cast<void *>(S->texels), static_cast<void *>(S->uv), static_cast<void *>(S->face_uv)})
+	for(void *p : {static_cast<void *>(S->tex), static_cast<void *>(S->texels), static_cast<void *>(S->uv), static_cast<void *>(S->face_uv),
+	               static_cast<void *>(S->vnrm), static_cast<void *>(S->face_nrm)})
 		if(p) cudaFree(p);
 	if(S->filter_dev) cudaFree(S->filter_dev);
 	if(S->ev_last) cudaEventDestroy(S->ev_last);

@@ -267,6 +267,8 @@ SIGNATURES = {
     "gbrt_aa_flags": (_I, [_VP, _VP, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(AaParams), ctypes.c_float, _VP,
                            ctypes.POINTER(ctypes.c_uint32)]),
     "gbrt_scene_set_textures": (_I, [_VP, _VP, _U32, _VP, ctypes.POINTER(TextureDesc), _U32, _VP, _U32]),
+    "gbrt_mesh_smooth_normals": (_I, [_VP, _U32, _VP, _U32, ctypes.c_float, _VP, _U32, ctypes.POINTER(_U32), _VP]),
+    "gbrt_scene_set_normals": (_I, [_VP, _VP, _U32, _VP]),
     "gbrt_pm_render_aa_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP, ctypes.POINTER(AaParams),
                                     _VP, ctypes.POINTER(PtStats), _VP]),
     "gbrt_dl_render_aa_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP, ctypes.POINTER(AaParams),
@@ -445,6 +447,27 @@ def _material_desc(m):
     return d
 
 
+NO_NORMAL = 0xFFFFFFFF
+FLAT_FACE = 0xFFFFFFFE
+
+
+def smooth_normals(vertices, faces, angle):
+    """The reference's yafaray_smoothObjectMesh(angle) on one mesh object,
+    by gbrt_mesh_smooth_normals: (normals float32 [n, 3], face normal
+    indices uint32 [faces, 4], NO_NORMAL where a vertex keeps the face's
+    geometric normal)."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    f = np.ascontiguousarray(faces, np.uint32).reshape(-1, 4)
+    fn = np.empty((max(1, len(f)), 4), np.uint32)
+    n = _U32()
+    L = load()
+    check(L.gbrt_mesh_smooth_normals(_ptr(v), len(v), _ptr(f), len(f), float(angle), None, 0, ctypes.byref(n), _ptr(fn)))
+    out = np.empty((max(1, n.value), 3), np.float32)
+    check(L.gbrt_mesh_smooth_normals(_ptr(v), len(v), _ptr(f), len(f), float(angle), _ptr(out), len(out), ctypes.byref(n),
+                                     _ptr(fn)))
+    return out[:n.value], fn[:len(f)]
+
+
 class Renderer:
     """A scene dict (libyafaray_gb300.scenes) on the GPU: BVH + materials +
     lights, rendered by the wavefront path tracer (gbrt_pt_render)."""
@@ -483,6 +506,37 @@ class Renderer:
         self._h = h
         if scene.get("textures"):
             self._set_textures()
+        if any("smooth" in o or "normals" in o for o in scene["objects"]):
+            self._set_normals()
+
+    def _set_normals(self):
+        """Shading normals of the objects with "smooth" (an angle, as
+        yafaray_smoothObjectMesh) or explicit per-vertex "normals" (as
+        yafaray_addNormal, one per vertex); other objects stay flat."""
+        N, FN = [], []
+        base = 0
+        for o in self.scene["objects"]:
+            v = np.asarray(o["vertices"], np.float32)
+            f = np.asarray(o["faces"], np.uint32)
+            tri = f[:, 3] == TRIANGLE
+            if "normals" in o:
+                n = np.asarray(o["normals"], np.float32).reshape(-1, 3)
+                fn = f.copy()
+                fn[tri, 3] = NO_NORMAL
+            elif "smooth" in o:
+                n, fn = smooth_normals(v, f, float(o["smooth"]))
+            else:
+                FN.append(np.full((len(f), 4), FLAT_FACE, np.uint32))
+                continue
+            fn = fn.copy()
+            live = fn != NO_NORMAL
+            fn[live] += base
+            N.append(n)
+            FN.append(fn)
+            base += len(n)
+        normals = np.ascontiguousarray(np.concatenate(N) if N else np.zeros((0, 3), np.float32), np.float32)
+        face_normals = np.ascontiguousarray(np.concatenate(FN), np.uint32)
+        check(load().gbrt_scene_set_normals(self._h, _ptr(normals), len(normals), _ptr(face_normals)))
 
     def _set_textures(self):
         """Image textures of the scene's "textures" entry on the shinydiffuse

@@ -624,6 +624,38 @@ def torus(center, R, r, nu, nv):
     return P, F
 
 
+def torus_quads(center, R, r, nu, nv):
+    """Torus around +y as nu x nv quads (one primitive each)."""
+    P, F = torus(center, R, r, nu, nv)
+    T = F.reshape(-1, 2, 3)
+    Q = np.stack([T[:, 0, 0], T[:, 0, 1], T[:, 0, 2], T[:, 1, 2]], -1)   # (a, b, d, c)
+    return P.astype(np.float32), Q.astype(np.uint32)
+
+
+def smooth_cornell_scene(res=64, glass=True):
+    """The Cornell box with shading normals: a coarse shinydiffuse icosphere
+    (80 triangles) averaged at every vertex (smooth 181), a glossy torus of
+    quads smoothed across faces within 40 degrees, the short box smoothed at
+    30 degrees (its coplanar triangles share normals, its 90-degree edges stay
+    sharp) and, with glass, a glass icosphere (320 triangles, smooth 181) on
+    the short box through the recursive split."""
+    sc = cornell_scene(res=res)
+    sc["materials"]["ball"] = ("shinydiffusemat", (0.8, 0.7, 0.3))
+    sc["materials"]["ring"] = glossy_material((0.3, 0.5, 0.8), exponent=60.0, glossy_reflect=0.5)
+    v, f = icosphere((-0.45, 0.3, 0.45), 0.3, 1)
+    sc["objects"].insert(-1, {"name": "smooth_ball", "material": "ball", "vertices": v, "faces": f, "smooth": 181.0})
+    v, f = torus_quads((0.55, 0.08, 0.82), 0.2, 0.08, 16, 10)
+    sc["objects"].insert(-1, {"name": "ring", "material": "ring", "vertices": v, "faces": f, "smooth": 40.0})
+    for o in sc["objects"]:
+        if o["name"] == "group3":
+            o["smooth"] = 30.0
+    if glass:
+        sc["materials"]["glass"] = glass_material(1.5)
+        v, f = icosphere((0.35, 0.85, 0.25), 0.25, 2)
+        sc["objects"].insert(-1, {"name": "glass_ball", "material": "glass", "vertices": v, "faces": f, "smooth": 181.0})
+    return sc
+
+
 def batch_scene(i, res=None, spp_scale=1.0):
     """Scene i of the 64-scene batch (seed 1000 + i): about
     round(10^U[3, log10 2e6]) triangles of tessellated spheres and tori under

@@ -125,6 +125,28 @@ def run_reference_kdtree(verts, faces, rays, mode=0, accel="yafaray-kdtree-origi
     return bound, build_s, trace_s, rec["id"].copy(), rec["t"].copy(), rec["u"].copy(), rec["v"].copy()
 
 
+REF_NORMALS = os.path.join(HERE, "_ref", "normals_dump")
+
+
+def run_reference_normals(verts, faces, angle):
+    """The reference's yafaray_smoothObjectMesh(angle) on one mesh: per face
+    corner (4 per face) the normal index (-1 = none) and the normal."""
+    verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+    faces = np.ascontiguousarray(faces, dtype=np.uint32).reshape(-1, 4)
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
+        with open(fin, "wb") as f:
+            f.write(b"GBRTNM01")
+            f.write(struct.pack("<I", len(verts))); f.write(verts.tobytes())
+            f.write(struct.pack("<I", len(faces))); f.write(faces.tobytes())
+            f.write(struct.pack("<f", angle))
+        subprocess.run([REF_NORMALS, fin, fout], check=True, stdout=subprocess.DEVNULL)
+        raw = open(fout, "rb").read()
+    nf = struct.unpack("<I", raw[:4])[0]
+    rec = np.frombuffer(raw[4:], dtype=np.dtype([("idx", "<i4"), ("n", "<f4", 3)])).reshape(nf, 4)
+    return rec["idx"].copy(), rec["n"].copy()
+
+
 REF_RENDER = os.path.join(HERE, "_ref", "render_dump")
 
 
@@ -210,10 +232,12 @@ def reference_scene_text(scene, spp, batches, threads=-1, offset_stride=None):
             out += [f"{float(a)!r} {float(b)!r}" for a, b in uv]
             out += [" ".join(str(int(x)) for x in ((*row[:3], *fr[:3]) if row[3] == TRI_MARK else (*row, *fr)))
                     for row, fr in zip(f, fu)]
-            continue
-        out.append(f"object {o['name']} {o['material']} {len(v)} {len(f)}")
-        out += [f"{float(a)!r} {float(b)!r} {float(c)!r}" for a, b, c in v]
-        out += [" ".join(str(int(x)) for x in (row[:3] if row[3] == TRI_MARK else row)) for row in f]
+        else:
+            out.append(f"object {o['name']} {o['material']} {len(v)} {len(f)}")
+            out += [f"{float(a)!r} {float(b)!r} {float(c)!r}" for a, b, c in v]
+            out += [" ".join(str(int(x)) for x in (row[:3] if row[3] == TRI_MARK else row)) for row in f]
+        if "smooth" in o:
+            out.append(f"smooth {o['name']} {float(o['smooth'])!r}")
     for L in scene["lights"]:
         if L["type"] == "arealight":
             vals = [*L["corner"], *L["point1"], *L["point2"], *L["color"], L["power"]]

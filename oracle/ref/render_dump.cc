@@ -17,6 +17,7 @@
 //   object NAME MATERIAL NV NF [NUV]   then NV lines "x y z", NUV lines "u v",
 //                                NF lines "a b c" / "a b c d" (with uvs also the
 //                                face's uv indices: "a b c ua ub uc")
+//   smooth NAME ANGLE            yafaray_smoothObjectMesh on an object defined above
 //   image NAME W H               then H lines of W x "r g b a" (an in-memory
 //                                ColorAlpha image, image_optimization none, LinearRGB)
 //   texture NAME key=value ...   (yafaray_createTexture: type=image image_name=...)
@@ -142,6 +143,7 @@ int main(int argc, char **argv)
 	float pixel_width = 1.f;
 	int offset_stride = -1;
 	std::vector<yafaray_ParamMap *> pending_nodes;
+	std::map<std::string, size_t> object_ids;
 	std::string integrator_type;
 	std::vector<std::pair<std::string, std::string>> integrator_kv;
 	auto make_integrator = [&]() {
@@ -240,6 +242,13 @@ int main(int argc, char **argv)
 				else if(ix.size() == 4) yafaray_addQuad(scene, obj, ix[0], ix[1], ix[2], ix[3], mat_id);
 			}
 			yafaray_initObject(scene, obj, mat_id);
+			object_ids[name] = obj;
+		}
+		else if(kw == "smooth")
+		{
+			std::string name; double angle;
+			ss >> name >> angle;
+			yafaray_smoothObjectMesh(scene, object_ids.at(name), angle);
 		}
 		else if(kw == "image")
 		{

@@ -106,7 +106,46 @@ def main():
     cam = scenes.camera_rays(96, 54, (0.0, 0.6, 3.2), (0.0, 0.0, 0.0), seed=16)
     r = np.concatenate([cam, scenes.random_rays(2048, seed=17, lo=-1.5, hi=1.5), edge_rays(v, f, 512, seed=18)])
     run_case("perlin_sphere_16k", v, f, r)
+    normals_golden()
+
+
+def normals_golden():
+    """smooth_normals.npz: per face corner the normal index and normal the
+    reference's yafaray_smoothObjectMesh gives: a coarse icosphere at 181 /
+    100 / 30 / 0.05 degrees, a torus of quads at 40 and 181, the Cornell
+    short box at 30, and a noisy height field at 50 (many merges)."""
+    cases = {}
+    v, f = scenes.icosphere((0.1, 0.2, 0.3), 0.7, 1)
+    for a in (181.0, 100.0, 30.0, 0.05):
+        cases[f"ico_{a:g}"] = (v, f, a)
+    v, f = scenes.torus_quads((0.0, 0.1, 0.0), 0.5, 0.2, 12, 8)
+    for a in (40.0, 181.0):
+        cases[f"torus_{a:g}"] = (v, f, a)
+    sc = scenes.smooth_cornell_scene(res=8, glass=False)
+    box = [o for o in sc["objects"] if o["name"] == "group3"][0]
+    cases["box_30"] = (box["vertices"], box["faces"], 30.0)
+    rng = np.random.default_rng(21)
+    n = 9
+    gx, gz = np.meshgrid(np.linspace(0, 1, n), np.linspace(0, 1, n), indexing="ij")
+    hv = np.stack([gx, 0.15 * rng.random((n, n)), gz], -1).reshape(-1, 3).astype(np.float32)
+    quads = [[i * n + j, i * n + j + 1, (i + 1) * n + j + 1, (i + 1) * n + j] for i in range(n - 1) for j in range(n - 1)]
+    hf = np.array([[a, b, c, scenes.TRI] if k % 3 else [a, b, c, d] for k, (a, b, c, d) in enumerate(quads)], np.uint32)
+    cases["height_50"] = (hv, hf, 50.0)
+    out = {}
+    for name, (v, f, a) in cases.items():
+        idx, nrm = orc.run_reference_normals(v, f, a)
+        out[f"{name}_vertices"] = np.asarray(v, np.float32)
+        out[f"{name}_faces"] = np.asarray(f, np.uint32)
+        out[f"{name}_angle"] = np.float32(a)
+        out[f"{name}_index"] = idx
+        out[f"{name}_normal"] = nrm
+    out["cases"] = np.array(sorted(cases))
+    np.savez_compressed(os.path.join(OUT, "smooth_normals.npz"), **out)
+    print(f"smooth_normals.npz: {len(cases)} meshes")
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["normals"]:
+        normals_golden()
+    else:
+        main()

@@ -17,7 +17,8 @@ cornell_pm, dl, batch, hashgrid, film (gauss film), aa (adaptive-AA film
 states + flags and an adaptive render), aa_pm (adaptive passes of
 photonmapping / directlighting), cornell_tshadow (transparent shadows,
 shadowDepth 4 and 1), cornell_textured (image textures, mapper and layer
-nodes), cornell_sppm (SPPM with and without pmIRE).
+nodes), cornell_sppm (SPPM with and without pmIRE), cornell_smooth (smoothed
+vertex normals).
 """
 import os
 import struct
@@ -350,3 +351,21 @@ if __name__ == "__main__":
             print(f"{name}: mean {rgb.mean(axis=(0, 1, 2))}, flagged {[len(p['flagged']) for p in passes]}, {secs.sum():.1f} s")
     if "cornell_point" in what:
         variant_golden("cornell_point_64_render.npz", point_light=True)
+    if "cornell_smooth" in what:
+        # shading normals: yafaray_smoothObjectMesh at 181 (a coarse ball, a
+        # glass ball), 40 (a torus of quads) and 30 degrees (the short box)
+        sc = scenes.smooth_cornell_scene(res=64)
+        rgb, secs = orc.run_reference_render(sc, 16, 32, threads=os.cpu_count() or 1)
+        np.savez_compressed(os.path.join(OUT, "cornell_smooth_64_render.npz"), mean=rgb.mean(0).astype(np.float32),
+                            se=(rgb.std(0, ddof=1) / np.sqrt(32)).astype(np.float32), batches=np.int32(32),
+                            spp=np.int32(16), seconds=secs)
+        # the normals the reference's MeshObject::smoothVerticesNormals makes
+        # for the same objects are pinned by the render; the flat render of the
+        # same scene shows that the smoothing is visible
+        flat = scenes.smooth_cornell_scene(res=64)
+        for o in flat["objects"]:
+            o.pop("smooth", None)
+        rgb_f, _ = orc.run_reference_render(flat, 16, 8, threads=os.cpu_count() or 1)
+        np.savez_compressed(os.path.join(OUT, "cornell_smooth_flat_64_render.npz"), mean=rgb_f.mean(0).astype(np.float32),
+                            batches=np.int32(8), spp=np.int32(16))
+        print(f"cornell_smooth_64_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
