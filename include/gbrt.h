@@ -276,7 +276,31 @@ typedef struct gbrt_pt_params {
 	 * reference's default is 4). */
 	int32_t transparent_shadows;
 	int32_t shadow_depth;
+	/* PathIntegrator "caustic_type" (integrator_path_tracer.h:40-59): path
+	 * caustics (emission reached through specular / glossy / filter samples
+	 * after the first bounce), photon caustics (a caustic photon map,
+	 * CausticPhotonIntegrator::createCausticMap, estimated at the camera-path
+	 * root of diffuse surfaces), both or none.  GBRT_CAUSTIC_PATH (0) is the
+	 * reference's default. */
+	uint32_t caustic_type;
+	/* "no_recursive" [false]: the path loop starts at every first hit and
+	 * samples all BSDF components there (integrator_path_tracer.cc:177-200). */
+	int32_t no_recursive;
+	/* Caustic photon map of caustic_type photon / both: caustic_photons,
+	 * caustic_mix, caustic_radius, caustic_depth of a gbrt_pm_params, NULL =
+	 * the reference's defaults (500000, 50, 0.25, 10). */
+	const struct gbrt_pm_params *caustic;
+	/* ImageFilm "AA_clamp_indirect" [0 = off]: photon caustic estimates and
+	 * final-gather results brighter than this are scaled down to it
+	 * (Rgb::clampProportionalRgb; integrator_photon_caustic.cc:94,
+	 * integrator_photon_mapping.cc:727). */
+	float clamp_indirect;
 } gbrt_pt_params;
+
+#define GBRT_CAUSTIC_PATH 0u
+#define GBRT_CAUSTIC_NONE 1u
+#define GBRT_CAUSTIC_PHOTON 2u
+#define GBRT_CAUSTIC_BOTH 3u
 
 /* Adaptive anti-aliasing (ImageFilm / TiledIntegrator parameters with the
  * reference's names and defaults in brackets). */

@@ -157,6 +157,12 @@ struct Params {
 	uint8_t *sppm_ire;         // pmIRE: per-pixel "radius set" flags, or null (no estimate this pass)
 	float sppm_ire_r2;         // photonRadius^2
 	int sppm_ire_k;            // searchNum
+	// pathtracing (PathIntegrator): caustic_type has "path" (emission after
+	// specular / glossy / filter samples counts at later vertices), and
+	// no_recursive (the path loop starts at every first hit, all components)
+	int pt_caustic_path;
+	int no_recursive;
+	float clamp_indirect;      // AA_clamp_indirect (0: off)
 };
 
 struct Work {
@@ -2011,7 +2017,9 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 			uint32_t req = BF_ALL;
 			if(k == 0)
 			{
-				if((s.m->flags & BF_DIFFUSE) && (!P.pm || P.pm_fg))   // path_flags = Diffuse (integrator_path_tracer.cc:178-200)
+				// path_flags = Diffuse, or All with no_recursive (integrator_path_tracer.cc:177-200)
+				const uint32_t path_flags = (P.no_recursive && !P.pm) ? BF_ALL : BF_DIFFUSE;
+				if((s.m->flags & path_flags) && (!P.pm || P.pm_fg))
 				{
 					const uint32_t offs = static_cast<uint32_t>(P.path_samples) * sample_ + offset_ + sub;
 					s1 = gbrt::ri_vdc(offs);
@@ -2021,7 +2029,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 						s1 += deco1; if(s1 > 1.f) s1 -= 1.f;
 						s2 += deco2; if(s2 > 1.f) s2 -= 1.f;
 					}
-					req = BF_DIFFUSE | BF_REFLECT | BF_TRANSMIT;
+					req = path_flags | BF_DIFFUSE | BF_REFLECT | BF_TRANSMIT;
 				}
 			}
 			else if(static_cast<int>(k) < P.bounces)
@@ -2105,7 +2113,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 						W.r_thr[slot] = make_float4(nt[0], nt[1], nt[2], 0.f);
 						W.r_valid[slot] = 2u;     // waiting for the next vertex
 					}
-					caustic = (sflags & (BF_SPECULAR | BF_GLOSSY | BF_FILTER)) ? 1u : 0u;
+					caustic = (P.pt_caustic_path && (sflags & (BF_SPECULAR | BF_GLOSSY | BF_FILTER))) ? 1u : 0u;
 					if(P.pm) { caustic = 0u; W.p_pm[path] = make_float4(0.f, 0.f, 0.f, 0.f); }
 					W.p_thr[path] = make_float4(nt[0], nt[1], nt[2], 0.f);
 					W.p_state[path] = (k + 1u) | (mat1 << 8) | (caustic << 16);
@@ -2740,6 +2748,18 @@ __global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJo
 	}
 }
 
+// Rgb::clampProportionalRgb (include/color/color.h:399-432): the largest
+// component down to max_value, the others scaled by the same factor.
+__device__ __forceinline__ void clamp_proportional(float c[3], float max_value)
+{
+	const float m = fmaxf(c[0], fmaxf(c[1], c[2]));
+	const float adj = __fdiv_rn(max_value, m);
+	if(!(m > max_value)) return;
+	if(c[0] >= m) { c[0] = max_value; c[1] = xm(c[1], adj); c[2] = xm(c[2], adj); }
+	else if(c[1] >= m) { c[1] = max_value; c[0] = xm(c[0], adj); c[2] = xm(c[2], adj); }
+	else { c[2] = max_value; c[0] = xm(c[0], adj); c[1] = xm(c[1], adj); }
+}
+
 // Material::eval with explicit BSDF flags, for the photon estimates.
 __device__ __forceinline__ void eval_flags(const Surface &s, const float wo[3], const float wl[3], uint32_t flags, float out[3])
 {
@@ -2855,7 +2875,10 @@ __global__ void __launch_bounds__(kThreads) k_pm_root(SceneDev sc, Params P, Wor
 					sum[0] += sc3[0] * kk * pc.x; sum[1] += sc3[1] * kk * pc.y; sum[2] += sc3[2] * kk * pc.z;
 				}
 				const float inv = 1.f / P.pm_caustic_paths;
-				for(int c = 0; c < 3; ++c) est[c] += sum[c] * inv;
+				for(int c = 0; c < 3; ++c) sum[c] *= inv;
+				// CausticPhotonIntegrator::causticPhotons (integrator_photon_caustic.cc:91-100)
+				if(P.clamp_indirect > 0.f) clamp_proportional(sum, P.clamp_indirect);
+				for(int c = 0; c < 3; ++c) est[c] += sum[c];
 			}
 		}
 		if(est[0] != 0.f || est[1] != 0.f || est[2] != 0.f)
@@ -3894,7 +3917,7 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	gbrt_pt_params pp = pp_in;
 	// the scene's buffers and filter table: after its previous render, whatever stream that used
 	if(S->ev_last) GBRT_CK(cudaStreamWaitEvent(s, S->ev_last, 0));
-	if(pm)
+	if(pm && pm->pm)
 	{
 		// camera sample = one integrate(); with final gathering, fg_samples gather
 		// paths of fg_bounces + 1 vertices each (path_samples / bounces slots)
@@ -3977,6 +4000,9 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 		P.sppm_ire = pm->sppm_ire; P.sppm_ire_r2 = pm->sppm_ire_r2; P.sppm_ire_k = pm->sppm_ire_k;
 	}
 	P.base_offset = pp.base_sampling_offset; P.seed = pp.seed;
+	P.pt_caustic_path = (pp.caustic_type == GBRT_CAUSTIC_PATH || pp.caustic_type == GBRT_CAUSTIC_BOTH) ? 1 : 0;
+	P.no_recursive = pp.no_recursive ? 1 : 0;
+	P.clamp_indirect = pp.clamp_indirect;
 	P.d1 = 1.f / static_cast<float>(pp.spp);
 	P.n_lights = S->n_lights;
 	P.guiding = guiding ? 1 : 0;
@@ -4008,7 +4034,7 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 			k_reset<<<1, 1, 0, s>>>(Ww.count, cur ^ 1);
 			k_extend<<<persistent_grid(k_extend, n, S->n_sm), kThreads, 0, s>>>(sc.bv, Ww.q_ray[cur], Ww.count + cur, Ww.count + 4, Ww.hits,
 			                                                                     level_guided ? Ww.hitpos : nullptr);
-			if(vtx == 0 && Pw.pm && (Pw.pm_caustics || (Pw.pm_diffuse && !Pw.pm_fg)))
+			if(vtx == 0 && (Pw.pm_caustics || (Pw.pm && Pw.pm_diffuse && !Pw.pm_fg)))
 				k_pm_root<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, film, film64_dev);
 			if(level_guided)
 				if(int rc = gbrt_guide_eval_queue(guide, Ww.hitpos, n, Ww.count + cur, Ww.lobes, s)) return rc;
@@ -4123,13 +4149,54 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	return GBRT_OK;
 }
 
+// PathIntegrator::preprocess with caustic_type photon or both
+// (integrator_path_tracer.cc:100-103): the caustic photon map of
+// CausticPhotonIntegrator::createCausticMap, gridded for the estimate at the
+// roots of the camera paths (integrator_path_tracer.cc:164-171).
+struct PtCaustics {
+	Params M{};
+	ShotMap C;
+	GridStore G;
+	bool on = false;
+};
+
+static int pt_caustics(gbrt_scene *S, const gbrt_pt_params &pp, PtCaustics &K, cudaStream_t s)
+{
+	if(pp.caustic_type > GBRT_CAUSTIC_BOTH) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: caustic_type %u", pp.caustic_type);
+	if(pp.caustic_type != GBRT_CAUSTIC_PHOTON && pp.caustic_type != GBRT_CAUSTIC_BOTH) return GBRT_OK;
+	gbrt_pm_params d{};
+	gbrt_pm_default_params(&d);
+	const gbrt_pm_params &c = pp.caustic ? *pp.caustic : d;
+	if(c.caustic_mix < 1 || c.caustic_mix > gbrt::kMaxGather || !(c.caustic_radius > 0.f) || c.caustic_depth < 0 || c.caustic_photons < 0)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: bad caustic parameters (caustic_mix in [1, %d])", gbrt::kMaxGather);
+	float bound[6];
+	if(int rc = gbrt_bvh_get_bound(S->bvh, bound)) return rc;
+	const float lo[3] = {bound[0], bound[1], bound[2]};
+	const uint32_t seed = pp.seed * 0x9e3779b9u + pp.base_sampling_offset;
+	if(int rc = shoot_map(S, scene_dev(S), true, static_cast<uint32_t>(c.caustic_photons), c.caustic_depth, false, seed, K.C, s)) return rc;
+	if(int rc = build_grid(K.C.pos.as<float4>(), K.C.dir.as<float4>(), K.C.col.as<float4>(), K.C.n, c.caustic_radius, lo, S->n_sm, K.G, s))
+		return rc;
+	K.M.pm_caustics = 1;
+	K.M.pm_caustic_r2 = c.caustic_radius * c.caustic_radius;
+	K.M.pm_caustic_k = c.caustic_mix;
+	K.M.pm_caustic_paths = static_cast<float>(K.C.paths);
+	K.M.g_caustic = K.G.g;
+	K.on = true;
+	return GBRT_OK;
+}
+
 int gbrt_pt_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params, float *film_dev, double *film64_dev,
                    gbrt_pt_stats *stats, void *stream)
 {
 	if(!S || !camera || !params) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: NULL argument");
 	if(!film_dev && !film64_dev) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render: no film buffer");
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
 	std::lock_guard<std::mutex> lock(S->mu);
-	return render_locked(S, camera, *params, nullptr, film_dev, film64_dev, stats, static_cast<cudaStream_t>(stream));
+	PtCaustics K;
+	if(int rc = pt_caustics(S, *params, K, s)) return rc;
+	const int rc = render_locked(S, camera, *params, K.on ? &K.M : nullptr, film_dev, film64_dev, stats, s);
+	if(K.on) cudaStreamSynchronize(s);       // the caustic map is freed on return
+	return rc;
 }
 
 // Device film around a render call, per-pixel means copied to the host.
@@ -4295,8 +4362,13 @@ int gbrt_pt_render_aa(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_
 	if(params->filter_type == GBRT_FILTER_PIXEL || !params->film_weight_dev)
 		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_aa: adaptive AA needs a filtered film (filter_type != PIXEL, film_weight_dev)");
 	if(params->guide) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_aa: no path guide in adaptive AA renders");
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
 	std::lock_guard<std::mutex> lock(S->mu);
-	return aa_render_locked(S, camera, *params, *aa, film_dev, stats, resampled, static_cast<cudaStream_t>(stream));
+	PtCaustics K;
+	if(int rc = pt_caustics(S, *params, K, s)) return rc;
+	const int rc = aa_render_locked(S, camera, *params, *aa, film_dev, stats, resampled, s, K.on ? &K.M : nullptr);
+	if(K.on) cudaStreamSynchronize(s);
+	return rc;
 }
 
 int gbrt_pt_render_aa_host(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_params *params_in, const gbrt_aa_params *aa,

@@ -62,7 +62,13 @@ class PtParams(ctypes.Structure):
                 ("guide", ctypes.c_void_p), ("guide_alpha", ctypes.c_float), ("guide_train_steps", ctypes.c_uint32),
                 ("guide_batch", ctypes.c_uint32), ("guide_max_vertex", ctypes.c_uint32), ("raydepth", ctypes.c_int32),
                 ("filter_type", ctypes.c_uint32), ("aa_pixel_width", ctypes.c_float), ("film_weight_dev", ctypes.c_void_p),
-                ("transparent_shadows", ctypes.c_int32), ("shadow_depth", ctypes.c_int32)]
+                ("transparent_shadows", ctypes.c_int32), ("shadow_depth", ctypes.c_int32),
+                ("caustic_type", ctypes.c_uint32), ("no_recursive", ctypes.c_int32), ("caustic", ctypes.c_void_p),
+                ("clamp_indirect", ctypes.c_float)]
+
+
+# PathIntegrator "caustic_type" names -> gbrt_pt_params.caustic_type
+CAUSTIC_TYPES = {"path": 0, "none": 1, "photon": 2, "both": 3}
 
 
 # ImageFilm "filter_type" names -> gbrt_pt_params.filter_type ("pixel": single-pixel splat, plain sums)
@@ -610,12 +616,20 @@ class Renderer:
         single-pixel splat)."""
         it = self.scene["integrator"]
         film = self.scene.get("film", {})
-        return PtParams(int(spp), int(it.get("path_samples", 1)), int(it.get("bounces", 5)),
-                        int(it.get("russian_roulette_min_bounces", 0)), int(base_offset), int(seed),
-                        PT_FP64_FILM if fp64 else 0, int(wave_paths), guide.handle if guide is not None else None,
-                        float(alpha), int(train_steps), int(batch), int(max_vertex), int(it.get("raydepth", 5)),
-                        FILTERS[film.get("filter_type", "pixel")], float(film.get("AA_pixelwidth", 0.0)),
-                        int(weight_ptr) or None, int(bool(it.get("transpShad", False))), int(it.get("shadowDepth", 4)))
+        p = PtParams(int(spp), int(it.get("path_samples", 1)), int(it.get("bounces", 5)),
+                     int(it.get("russian_roulette_min_bounces", 0)), int(base_offset), int(seed),
+                     PT_FP64_FILM if fp64 else 0, int(wave_paths), guide.handle if guide is not None else None,
+                     float(alpha), int(train_steps), int(batch), int(max_vertex), int(it.get("raydepth", 5)),
+                     FILTERS[film.get("filter_type", "pixel")], float(film.get("AA_pixelwidth", 0.0)),
+                     int(weight_ptr) or None, int(bool(it.get("transpShad", False))), int(it.get("shadowDepth", 4)))
+        if self.kind == "pathtracing":
+            p.caustic_type = CAUSTIC_TYPES[it.get("caustic_type", "path")]
+            p.no_recursive = int(bool(it.get("no_recursive", False)))
+            if p.caustic_type in (2, 3):
+                self._caustic = pm_params(it)          # caustic_photons / _mix / _radius / _depth
+                p.caustic = ctypes.addressof(self._caustic)
+        p.clamp_indirect = float(film.get("AA_clamp_indirect", 0.0))
+        return p
 
     def render(self, spp, base_offset=0, seed=1, fp64=False, guide=None, alpha=0.0, train_steps=0, batch=0,
                max_vertex=0):

@@ -656,6 +656,26 @@ def smooth_cornell_scene(res=64, glass=True):
     return sc
 
 
+def cornell_pt_variant_scene(res=48, caustic_type="path", caustic_photons=100000, caustic_radius=0.08, caustic_mix=40,
+                             no_recursive=False, clamp_indirect=0.0):
+    """The glass Cornell box through `pathtracing` with the integrator's
+    caustic options: caustic_type path / photon / both / none (photon: a
+    caustic photon map of caustic_photons paths, estimated with caustic_mix
+    photons within caustic_radius at diffuse camera hits), no_recursive (the
+    path loop at every first hit), and the film's AA_clamp_indirect."""
+    sc = cornell_scene(res=res, glass=True)
+    it = sc["integrator"]
+    it["caustic_type"] = caustic_type
+    if caustic_type in ("photon", "both"):
+        it.update({"caustic_photons": int(caustic_photons), "caustic_radius": float(caustic_radius),
+                   "caustic_mix": int(caustic_mix)})
+    if no_recursive:
+        it["no_recursive"] = True
+    if clamp_indirect:
+        sc["film"] = {"filter_type": "pixel", "AA_clamp_indirect": float(clamp_indirect)}
+    return sc
+
+
 def batch_scene(i, res=None, spp_scale=1.0):
     """Scene i of the 64-scene batch (seed 1000 + i): about
     round(10^U[3, log10 2e6]) triangles of tessellated spheres and tori under

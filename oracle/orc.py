@@ -253,7 +253,10 @@ def reference_scene_text(scene, spp, batches, threads=-1, offset_stride=None):
     out.append(f"integrator {t} " + " ".join(f"{k}={str(v).lower() if isinstance(v, bool) else v}" for k, v in integ.items()))
     film = scene.get("film")
     if film:
-        out.append(f"film {film['filter_type']} {float(film.get('AA_pixelwidth', 1.5))!r}")
+        if film["filter_type"] == "pixel":      # the single-pixel splat: the reference's box filter of width 1
+            out.append("film box 1.0")
+        else:
+            out.append(f"film {film['filter_type']} {float(film.get('AA_pixelwidth', 1.5))!r}")
         aa = {k: v for k, v in film.items() if k.startswith("AA_") and k not in ("AA_pixelwidth", "AA_minsamples")}
         if aa:
             def fmt(v):

@@ -18,7 +18,7 @@ states + flags and an adaptive render), aa_pm (adaptive passes of
 photonmapping / directlighting), cornell_tshadow (transparent shadows,
 shadowDepth 4 and 1), cornell_textured (image textures, mapper and layer
 nodes), cornell_sppm (SPPM with and without pmIRE), cornell_smooth (smoothed
-vertex normals).
+vertex normals), cornell_pt_caustics (pathtracing caustic_type / no_recursive).
 """
 import os
 import struct
@@ -351,6 +351,18 @@ if __name__ == "__main__":
             print(f"{name}: mean {rgb.mean(axis=(0, 1, 2))}, flagged {[len(p['flagged']) for p in passes]}, {secs.sum():.1f} s")
     if "cornell_point" in what:
         variant_golden("cornell_point_64_render.npz", point_light=True)
+    if "cornell_pt_caustics" in what:
+        # pathtracing's caustic options on the glass Cornell box: photon
+        # caustics, both (path + photon) with AA_clamp_indirect, no_recursive
+        for name, kw in (("cornell_pt_photon_48_render.npz", dict(caustic_type="photon")),
+                         ("cornell_pt_both_clamp_48_render.npz", dict(caustic_type="both", clamp_indirect=0.3)),
+                         ("cornell_pt_norec_48_render.npz", dict(no_recursive=True))):
+            sc = scenes.cornell_pt_variant_scene(res=48, **kw)
+            rgb, secs = orc.run_reference_render(sc, 8, 24, threads=os.cpu_count() or 1)
+            np.savez_compressed(os.path.join(OUT, name), mean=rgb.mean(0).astype(np.float32),
+                                se=(rgb.std(0, ddof=1) / np.sqrt(24)).astype(np.float32), batches=np.int32(24),
+                                spp=np.int32(8), seconds=secs)
+            print(f"{name}: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
     if "cornell_smooth" in what:
         # shading normals: yafaray_smoothObjectMesh at 181 (a coarse ball, a
         # glass ball), 40 (a torus of quads) and 30 degrees (the short box)

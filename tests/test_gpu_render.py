@@ -183,6 +183,24 @@ def test_gpu_cornell_smooth_normals_match_reference(cuda_device):
     assert f0 < frac - 0.02
 
 
+@pytest.mark.parametrize("name,kw", [("cornell_pt_photon_48_render.npz", dict(caustic_type="photon")),
+                                     ("cornell_pt_both_clamp_48_render.npz", dict(caustic_type="both", clamp_indirect=0.3)),
+                                     ("cornell_pt_norec_48_render.npz", dict(no_recursive=True))])
+def test_gpu_pathtracing_caustic_options_match_reference(cuda_device, name, kw):
+    """PathIntegrator's caustic_type photon (a caustic photon map estimated at
+    diffuse camera hits, no path caustics after the first bounce), both (path
+    + photon, the photon estimate clamped by AA_clamp_indirect 0.3) and
+    no_recursive (the path loop at every first hit, all BSDF components) on
+    the glass Cornell box."""
+    g = np.load(os.path.join(GOLD, name))
+    r = gbrt.Renderer(scenes.cornell_pt_variant_scene(res=48, **kw))
+    gb = batches(r, int(g["spp"]), int(g["batches"]))
+    frac, relmse, m = parity(gb, g["mean"], g["se"])
+    print(f"{name}: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
+          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
+    assert frac >= 0.995
+
+
 def test_gpu_explicit_normals_equal_smoothing(cuda_device):
     """Vertex normals given per vertex (yafaray_addNormal: one normal per
     vertex, every face corner using its vertex's) render exactly like the
