@@ -648,7 +648,9 @@ int gbrt_guide_step(gbrt_guide *guide, const float *records_dev, uint32_t n, flo
  * Halton base 2/3 radical inverse of x (halton.h:59-85), 7 FAST_TRIG
  * math::sin (dim 0) or math::cos (dim 1) of the float with bits x
  * (math.h:228-265), 8 FAST_MATH math::pow(a, b) with a = float bits of x
- * and b = float bits of dim (math.h:116-146). */
+ * and b = float bits of dim (math.h:116-146), 9 / 10 kinds 0 / 6 rounded to
+ * float as the kernels form them (exact integer arithmetic, no FP64 except
+ * for inputs within a rounding margin). */
 int gbrt_sampler_eval(int kind, int dim, const uint32_t *input, uint32_t n, double *out, int on_device);
 
 #ifdef __cplusplus

@@ -1445,7 +1445,7 @@ __device__ void light_estimation(const SceneDev &sc, const Surface &s, const flo
 	for(int i = 0; i < ns; ++i)
 	{
 		const float s1 = gbrt::radical_inverse(offs + static_cast<uint32_t>(i), 2);
-		const float s2 = gbrt::radical_inverse(offs + static_cast<uint32_t>(i), 3);
+		const float s2 = gbrt::radical_inverse3_f(sc.lds, offs + static_cast<uint32_t>(i));
 		// light sample (AreaLight::illumSample, light_area.cc:99-124)
 		{
 			float lp[3], ldir[3];
@@ -1580,9 +1580,9 @@ __device__ void spawn_children(const SceneDev &sc, const Params &P, const Surfac
 		const float inv_rs = 1.f / static_cast<float>(rs);
 		for(uint32_t j = 0; j < rs; ++j)
 		{
-			const float d1 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 2 * static_cast<int>(nl) + 1, branch0 + j + offset_));
-			const float d2 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 2 * static_cast<int>(nl) + 2, branch0 + j + offset_));
-			const float s1 = gbrt::radical_inverse(offs + 1u + j, 2), s2 = gbrt::radical_inverse(offs + 1u + j, 3);
+			const float d1 = gbrt::low_discrepancy_f(sc.lds, 2 * static_cast<int>(nl) + 1, branch0 + j + offset_);
+			const float d2 = gbrt::low_discrepancy_f(sc.lds, 2 * static_cast<int>(nl) + 2, branch0 + j + offset_);
+			const float s1 = gbrt::radical_inverse(offs + 1u + j, 2), s2 = gbrt::radical_inverse3_f(sc.lds, offs + 1u + j);
 			if(s.m->flags & BF_TRANSMIT)
 			{
 				float dir[2][3], col[2][3], w[2];
@@ -1913,8 +1913,8 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 					}
 					// next direction: All when close, else specular only (finalGathering :625-628)
 					const uint32_t offs = static_cast<uint32_t>(P.path_samples) * sample_ + offset_ + sub;
-					float s1 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 4 * depth + 3, offs));
-					float s2 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 4 * depth + 4, offs));
+					float s1 = gbrt::low_discrepancy_f(sc.lds, 4 * depth + 3, offs);
+					float s2 = gbrt::low_discrepancy_f(sc.lds, 4 * depth + 4, offs);
 					if(division > 1) { s1 += deco1; if(s1 > 1.f) s1 -= 1.f; s2 += deco2; if(s2 > 1.f) s2 -= 1.f; }
 					const uint32_t fl = close ? BF_ALL : (BF_SPECULAR | BF_REFLECT | BF_TRANSMIT | BF_FILTER);
 					float wi[3], scol[3], w, pdf;
@@ -2023,7 +2023,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				{
 					const uint32_t offs = static_cast<uint32_t>(P.path_samples) * sample_ + offset_ + sub;
 					s1 = gbrt::ri_vdc(offs);
-					s2 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 2, offs));
+					s2 = gbrt::low_discrepancy_f(sc.lds, 2, offs);
 					if(division > 1)   // math::addMod1 with the split's decorrelation
 					{
 						s1 += deco1; if(s1 > 1.f) s1 -= 1.f;
@@ -2038,8 +2038,8 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 				const int d4 = 4 * static_cast<int>(k);
 				if(d4 + 4 < gbrt::kLdsDims)
 				{
-					s1 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d4 + 3, offs));
-					s2 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d4 + 4, offs));
+					s1 = gbrt::low_discrepancy_f(sc.lds, d4 + 3, offs);
+					s2 = gbrt::low_discrepancy_f(sc.lds, d4 + 4, offs);
 				}
 				else
 				{
@@ -2521,7 +2521,8 @@ __global__ void k_normalize(const float *sum, const double *sum64, const float *
 
 // kind: 0 lowDiscrepancySampling(dim, x), 1 riVdC, 2 riLp, 3 riS, 4 fnv32ABuf,
 // 5 radical inverse base 2, 6 radical inverse base 3, 7 FAST_TRIG sin and
-// cos of the float whose bits are x (sin in the value, cos via dim = 1).
+// cos of the float whose bits are x (sin in the value, cos via dim = 1),
+// 8 FAST_MATH pow, 9 / 10 the FP64-free float forms of kinds 0 / 6.
 __host__ __device__ inline double sampler_value(const gbrt::LdsTables &t, int kind, int dim, uint32_t x)
 {
 	switch(kind)
@@ -2533,6 +2534,8 @@ __host__ __device__ inline double sampler_value(const gbrt::LdsTables &t, int ki
 		case 4: return static_cast<double>(gbrt::fnv32(x));
 		case 5: return gbrt::radical_inverse(x, 2);
 		case 6: return gbrt::radical_inverse(x, 3);
+		case 9: return gbrt::low_discrepancy_f(t, dim, x);
+		case 10: return gbrt::radical_inverse3_f(t, x);
 		case 8:
 		{
 			// FAST_MATH pow: base = float bits of x, exponent = float bits of dim
@@ -2621,8 +2624,8 @@ __device__ void reflectivity(const SceneDev &sc, const Surface &s, uint32_t flag
 	{
 		const float s1 = 0.03125f + 0.0625f * static_cast<float>(i);
 		const float s2 = gbrt::ri_vdc(static_cast<uint32_t>(i));
-		const float s3 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 2, static_cast<uint32_t>(i)));
-		const float s4 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 3, static_cast<uint32_t>(i)));
+		const float s3 = gbrt::low_discrepancy_f(sc.lds, 2, static_cast<uint32_t>(i));
+		const float s4 = gbrt::low_discrepancy_f(sc.lds, 3, static_cast<uint32_t>(i));
 		float wo[3], wi[3], col[3], w, pdf;
 		uint32_t sf;
 		cos_hemisphere(s.n, s.u, s.v, s1, s2, wo);
@@ -2642,15 +2645,15 @@ __global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJo
 		if(J.sppm)
 		{
 			// hal_1_ .. hal_4_ {2, 0}, {3, 0}, {5, 0}, {7, 0}: the n-th getNext is index n
-			s1 = gbrt::radical_inverse(pi + 1u, 2); s2 = gbrt::radical_inverse(pi + 1u, 3);
+			s1 = gbrt::radical_inverse(pi + 1u, 2); s2 = gbrt::radical_inverse3_f(sc.lds, pi + 1u);
 			s3 = gbrt::radical_inverse(pi + 1u, 5); s4 = gbrt::radical_inverse(pi + 1u, 7);
 		}
 		else
 		{
 			s1 = gbrt::ri_vdc(i);
-			s2 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 2, i));
-			s3 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 3, i));
-			s4 = static_cast<float>(gbrt::low_discrepancy(sc.lds, 4, i));
+			s2 = gbrt::low_discrepancy_f(sc.lds, 2, i);
+			s3 = gbrt::low_discrepancy_f(sc.lds, 3, i);
+			s4 = gbrt::low_discrepancy_f(sc.lds, 4, i);
 		}
 		const float s_l = J.caustic ? static_cast<float>(i) / static_cast<float>(J.n) : static_cast<float>(i) * J.inv_n;
 		uint32_t ln = 0;
@@ -2723,9 +2726,9 @@ __global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJo
 			if(nb == J.max_bounces) break;
 			// Material::scatterPhoton (src/material/material.cc:179-196)
 			const int d5 = 3 * nb + 5;
-			const float s5 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d5, pi));
-			const float s6 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d5 + 1, pi));
-			const float s7 = static_cast<float>(gbrt::low_discrepancy(sc.lds, d5 + 2, pi));
+			const float s5 = gbrt::low_discrepancy_f(sc.lds, d5, pi);
+			const float s6 = gbrt::low_discrepancy_f(sc.lds, d5 + 1, pi);
+			const float s7 = gbrt::low_discrepancy_f(sc.lds, d5 + 2, pi);
 			const uint32_t flags = J.caustic && !J.sppm ? (BF_SPECULAR | BF_REFLECT | BF_TRANSMIT | BF_GLOSSY | BF_FILTER | BF_DISPERSIVE) : BF_ALL;
 			float wo[3], scol[3], w, pdf;
 			uint32_t sf;
@@ -3099,6 +3102,8 @@ struct gbrt_scene {
 	double *lds_inv = nullptr;
 	double *lds_sfac = nullptr;
 	uint32_t *lds_sfac_off = nullptr, *lds_sfac_nd = nullptr;
+	uint4 *lds_fx = nullptr;           // integer tables of the FP64-free sample streams
+	uint32_t lds_fx_dims = 0, lds_fx_rad3 = 0;
 	// materials that start the recursive split, for its buffer sizing
 	bool split_glossy = false, split_glossy_transmit = false, split_specular = false;
 	uint32_t max_addl = 0;
@@ -3468,7 +3473,8 @@ int shoot_map(gbrt_scene *S, const SceneDev &sc, bool caustic, uint32_t n, int m
 
 SceneDev scene_dev(const gbrt_scene *S)
 {
-	return SceneDev{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off, S->lds_sfac_nd},
+	return SceneDev{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off, S->lds_sfac_nd,
+	                                                                         S->lds_fx, S->lds_fx_dims, S->lds_fx_rad3},
 	                S->tex, S->texels, S->uv, S->face_uv, S->vnrm, S->face_nrm};
 }
 
@@ -3682,7 +3688,10 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 		{reinterpret_cast<void **>(&S->lds_sfac), T.sfac.data(), T.sfac.size() * sizeof(double)},
 		{reinterpret_cast<void **>(&S->lds_sfac_off), T.sfac_offset.data(), T.sfac_offset.size() * sizeof(uint32_t)},
 		{reinterpret_cast<void **>(&S->lds_sfac_nd), T.sfac_digits.data(), T.sfac_digits.size() * sizeof(uint32_t)},
+		{reinterpret_cast<void **>(&S->lds_fx), T.fx.data(), T.fx.size() * sizeof(uint4)},
 	};
+	S->lds_fx_dims = T.fx_dims;
+	S->lds_fx_rad3 = T.fx_rad3;
 	for(const Up &u : ups)
 	{
 		if((e = cudaMalloc(u.dst, u.bytes)) != cudaSuccess) return fail(gbrt_set_error(GBRT_ERR_OOM, "gbrt_scene_create: %s", cudaGetErrorString(e)));
@@ -3829,7 +3838,7 @@ int gbrt_scene_destroy(gbrt_scene *S)
 {
 	if(!S) return GBRT_OK;
 	void *ptrs[] = {S->prim_ng, S->mats, S->lights, S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off,
-	                S->lds_sfac_nd, S->work, S->spawn, S->spawn_count};
+	                S->lds_sfac_nd, S->lds_fx, S->work, S->spawn, S->spawn_count};
 	for(void *p : ptrs) if(p) cudaFree(p);
 	for(void *p : {static_cast<void *>(S->tex), static_cast<void *>(S->texels), static_cast<void *>(S->uv), static_cast<void *>(S->face_uv),
 	               static_cast<void *>(S->vnrm), static_cast<void *>(S->face_nrm)})
@@ -4416,7 +4425,7 @@ int gbrt_aa_flags(const float *film_dev, const float *weight_dev, int32_t resx, 
 int gbrt_sampler_eval(int kind, int dim, const uint32_t *input, uint32_t n, double *out, int on_device)
 {
 	if(!input || !out) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_sampler_eval: NULL buffer");
-	if(kind < 0 || kind > 8 || (kind == 0 && (dim < 1 || dim >= gbrt::kLdsDims)))
+	if(kind < 0 || kind > 10 || ((kind == 0 || kind == 9) && (dim < 1 || dim >= gbrt::kLdsDims)))
 		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_sampler_eval: bad kind %d / dim %d", kind, dim);
 	const auto T = gbrt::make_lds_tables();
 	if(!on_device)
@@ -4427,14 +4436,14 @@ int gbrt_sampler_eval(int kind, int dim, const uint32_t *input, uint32_t n, doub
 	}
 	if(n == 0) return GBRT_OK;
 	void *d_perm = nullptr, *d_off = nullptr, *d_base = nullptr, *d_inv = nullptr, *d_in = nullptr, *d_out = nullptr;
-	void *d_sf = nullptr, *d_sfo = nullptr, *d_sfd = nullptr;
+	void *d_sf = nullptr, *d_sfo = nullptr, *d_sfd = nullptr, *d_fx = nullptr;
 	int rc = GBRT_OK;
 	cudaError_t e = cudaSuccess;
 	struct Up { void **dst; const void *src; size_t bytes; };
 	const Up ups[] = {{&d_perm, T.perm.data(), T.perm.size() * 2}, {&d_off, T.offset.data(), T.offset.size() * 4},
 	                  {&d_base, T.base.data(), T.base.size() * 4}, {&d_inv, T.inv.data(), T.inv.size() * 8},
 	                  {&d_sf, T.sfac.data(), T.sfac.size() * 8}, {&d_sfo, T.sfac_offset.data(), T.sfac_offset.size() * 4},
-	                  {&d_sfd, T.sfac_digits.data(), T.sfac_digits.size() * 4},
+	                  {&d_sfd, T.sfac_digits.data(), T.sfac_digits.size() * 4}, {&d_fx, T.fx.data(), T.fx.size() * sizeof(uint4)},
 	                  {&d_in, input, 4ull * n}, {&d_out, nullptr, 8ull * n}};
 	for(const Up &u : ups)
 	{
@@ -4444,13 +4453,14 @@ int gbrt_sampler_eval(int kind, int dim, const uint32_t *input, uint32_t n, doub
 	if(e == cudaSuccess)
 	{
 		const gbrt::LdsTables t{static_cast<uint16_t *>(d_perm), static_cast<uint32_t *>(d_off), static_cast<uint32_t *>(d_base),
-		                        static_cast<double *>(d_inv), static_cast<double *>(d_sf), static_cast<uint32_t *>(d_sfo), static_cast<uint32_t *>(d_sfd)};
+		                        static_cast<double *>(d_inv), static_cast<double *>(d_sf), static_cast<uint32_t *>(d_sfo), static_cast<uint32_t *>(d_sfd),
+		                        static_cast<uint4 *>(d_fx), T.fx_dims, T.fx_rad3};
 		k_sampler<<<(n + 127) / 128, 128>>>(t, kind, dim, static_cast<const uint32_t *>(d_in), n, static_cast<double *>(d_out));
 		e = cudaGetLastError();
 		if(e == cudaSuccess) e = cudaMemcpy(out, d_out, 8ull * n, cudaMemcpyDeviceToHost);
 	}
 	if(e != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "gbrt_sampler_eval: %s", cudaGetErrorString(e));
-	for(void *p : {d_perm, d_off, d_base, d_inv, d_sf, d_sfo, d_sfd, d_in, d_out}) if(p) cudaFree(p);
+	for(void *p : {d_perm, d_off, d_base, d_inv, d_sf, d_sfo, d_sfd, d_fx, d_in, d_out}) if(p) cudaFree(p);
 	return rc;
 }
 

@@ -38,6 +38,13 @@ struct LdsTables {
 	const double *sfac;
 	const uint32_t *sfac_offset;       // [kLdsDims]
 	const uint32_t *sfac_digits;       // [kLdsDims] digits tabulated
+	// integer tables of the FP64-free evaluation (low_discrepancy_f,
+	// radical_inverse3_f): fixed-point terms at the sfac indices, then from
+	// fx_dims one entry per dimension {reciprocal of the base (64 bits),
+	// mantissa of inv (53 bits) with its exponent + 128 in the top byte},
+	// and from fx_rad3 the base-3 radical-inverse terms
+	const uint4 *fx;
+	uint32_t fx_dims, fx_rad3;
 };
 
 GBRT_HD float fmul(float a, float b)
@@ -216,6 +223,154 @@ GBRT_HD double low_discrepancy(const LdsTables &t, int dim, uint32_t n)
 	return value;
 }
 
+// ---- FP64-free evaluation of the same streams ------------------------------
+// The integrators use lowDiscrepancySampling and the base-3 radical inverse
+// as floats.  Here both are formed with integer arithmetic only: the digit
+// chain dn *= f with the double multiply's rounding emulated on 53-bit
+// mantissas (so every digit is the reference's), the digit terms (the
+// reference's double terms, converted exactly) summed in 128-bit fixed
+// point, then one rounding to float.  The reference's double sum differs
+// from the exact sum by at most one rounding per addition, so the float
+// equals (float) of the reference's double unless the exact sum lies within
+// K 2^-53 of a float rounding midpoint (K = terms added); those inputs,
+// about four in a million, take the double loop instead.
+
+// 128-bit fixed point: value = (hi 2^64 + lo) x 2^-127
+struct Fx128 {
+	uint64_t hi, lo;
+};
+
+GBRT_HD uint64_t mulhi64(uint64_t a, uint64_t b)
+{
+#if defined(__CUDA_ARCH__)
+	return __umul64hi(a, b);
+#else
+	return static_cast<uint64_t>((static_cast<unsigned __int128>(a) * b) >> 64);
+#endif
+}
+
+GBRT_HD int clz64(uint64_t x)
+{
+#if defined(__CUDA_ARCH__)
+	return __clzll(static_cast<long long>(x));
+#else
+	return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+GBRT_HD Fx128 fx_load(const uint4 &e) { return Fx128{(static_cast<uint64_t>(e.w) << 32) | e.z, (static_cast<uint64_t>(e.y) << 32) | e.x}; }
+GBRT_HD uint64_t fx_u64(uint32_t lo, uint32_t hi) { return (static_cast<uint64_t>(hi) << 32) | lo; }
+
+GBRT_HD void fx_add(Fx128 &a, const Fx128 &b)
+{
+	a.lo += b.lo;
+	a.hi += b.hi + (a.lo < b.lo ? 1u : 0u);
+}
+
+// The float nearest to the exact sum z, or false when the sum of k double
+// roundings could move the reference's value across a rounding midpoint.
+GBRT_HD bool fx_to_float(const Fx128 &z, uint32_t k, float &out)
+{
+	if(z.hi == 0 && z.lo == 0) { out = 0.f; return true; }
+	// every term is >= 2^-64 here, so the leading bit lies in hi
+	if(z.hi == 0) return false;
+	const int p = 127 - clz64(z.hi);           // leading bit index of the 128-bit integer
+	const int u = p - 23;                      // ulp bit index, >= 40
+	// the bits below the ulp, compared with half an ulp: bits u-1 .. 0
+	// (u > 64: all of lo and the low u - 64 bits of hi)
+	uint64_t rem_hi, rem_lo;                   // remainder as (rem_hi:rem_lo) with u bits
+	uint32_t mant;                             // the top 24 bits
+	if(u >= 64)
+	{
+		rem_hi = u > 64 ? (z.hi & ((1ull << (u - 64)) - 1ull)) : 0ull;
+		rem_lo = z.lo;
+		mant = static_cast<uint32_t>(z.hi >> (u - 64));
+	}
+	else
+	{
+		rem_hi = 0ull;
+		rem_lo = z.lo & ((1ull << u) - 1ull);
+		mant = static_cast<uint32_t>((z.hi << (64 - u)) | (z.lo >> u));
+	}
+	// |remainder - half| in units of 2^(u - 40): the tolerance k 2^-53 x 2^(p+1)
+	// = k 2^(u - 29) is k 2^11 such units
+	const int sh = u - 40;                     // >= 0
+	const uint64_t r40 = sh >= 64 ? (rem_hi >> (sh - 64)) : ((rem_hi << (64 - sh)) | (rem_lo >> sh));
+	const uint64_t half40 = 1ull << 39;
+	const uint64_t dist = r40 > half40 ? r40 - half40 : half40 - r40;
+	if(dist <= (static_cast<uint64_t>(k) << 11) + 1ull) return false;
+	const uint32_t m = mant + (r40 > half40 ? 1u : 0u);
+	// value = m x 2^(u - 127), m in [2^23, 2^24]: biased exponent u + 23
+	// (m = 2^24 carries into the exponent)
+	const uint32_t fb = (static_cast<uint32_t>(u + 23) << 23) + (m - (1u << 23));
+	std::memcpy(&out, &fb, 4);
+	return true;
+}
+
+GBRT_HD int clz32(uint32_t x)
+{
+#if defined(__CUDA_ARCH__)
+	return __clz(static_cast<int>(x));
+#else
+	return x ? __builtin_clz(x) : 32;
+#endif
+}
+
+GBRT_HD float low_discrepancy_f(const LdsTables &t, int dim, uint32_t n)
+{
+	const uint32_t b = t.base[dim];
+	if(b < 2 || n == 0) return 0.f;
+	const uint4 de = t.fx[t.fx_dims + dim];
+	const uint64_t recip = fx_u64(de.x, de.y);
+	const uint64_t mf = fx_u64(de.z, de.w & 0x1FFFFFu);           // f = mf 2^ef, mf in [2^52, 2^53)
+	const int ef = static_cast<int>(de.w >> 24) - 128;
+	const uint4 *term = t.fx + t.sfac_offset[dim];
+	const uint32_t nd = t.sfac_digits[dim];
+	// dn = (double)n = dm 2^dexp, then dn *= f rounded as the double multiply
+	// rounds (53-bit mantissas, product to nearest even): the reference's
+	// digit chain n_k = (unsigned)dn, exactly
+	const int msb = 31 - clz32(n);
+	uint64_t dm = static_cast<uint64_t>(n) << (52 - msb);
+	int dexp = msb - 52;
+	Fx128 z{0ull, 0ull};
+	uint32_t m = n, k = 0;
+	for(; m > 0; ++k)
+	{
+		if(k >= nd) return static_cast<float>(low_discrepancy(t, dim, n));   // not reached for 32-bit n
+		const uint32_t q = static_cast<uint32_t>(mulhi64(m, recip));      // floor(m / b)
+		fx_add(z, fx_load(term[k * b + (m - q * b)]));
+		const uint64_t plo = dm * mf, phi = mulhi64(dm, mf);               // 106-bit product
+		const int sh = 52 + static_cast<int>((phi >> 41) & 1u);            // its top bit is 104 or 105
+		uint64_t nm = (phi << (64 - sh)) | (plo >> sh);
+		const uint64_t rem = plo & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+		if(rem > half || (rem == half && (nm & 1ull))) ++nm;
+		dexp += ef + sh;
+		if(nm >> 53) { nm >>= 1; ++dexp; }
+		dm = nm;
+		m = -dexp >= 64 ? 0u : static_cast<uint32_t>(dm >> (-dexp));   // dn < 2^32, so dexp < -20
+	}
+	float out;
+	if(fx_to_float(z, k, out)) return out;
+	return static_cast<float>(low_discrepancy(t, dim, n));
+}
+
+// radical_inverse(n, 3) as a float, the same way (exact digits, exact sum).
+GBRT_HD float radical_inverse3_f(const LdsTables &t, uint32_t n)
+{
+	const uint4 *term = t.fx + t.fx_rad3;
+	Fx128 z{0ull, 0ull};
+	uint32_t k = 0, adds = 0;
+	for(uint32_t m = n; m > 0; ++k)
+	{
+		const uint32_t q = m / 3u, d = m - 3u * q;
+		if(d) { fx_add(z, fx_load(term[2 * k + (d - 1)])); ++adds; }
+		m = q;
+	}
+	float out;
+	if(fx_to_float(z, adds, out)) return clamp01(out);
+	return radical_inverse(n, 3);
+}
+
 // FAST_TRIG sine: wrap to [-pi, pi], parabola 4/pi x - 4/pi^2 x|x|, then the
 // 0.225 blend towards the squared parabola; clamped to [-1, 1].
 GBRT_HD float fast_sin(float x)
@@ -322,11 +477,31 @@ struct LdsHostTables {
 	std::vector<double> inv;
 	std::vector<double> sfac;
 	std::vector<uint32_t> sfac_offset, sfac_digits;
+	std::vector<uint4> fx;
+	uint32_t fx_dims = 0, fx_rad3 = 0;
 	LdsTables view() const
 	{
-		return LdsTables{perm.data(), offset.data(), base.data(), inv.data(), sfac.data(), sfac_offset.data(), sfac_digits.data()};
+		return LdsTables{perm.data(), offset.data(), base.data(), inv.data(), sfac.data(), sfac_offset.data(), sfac_digits.data(),
+		                 fx.data(), fx_dims, fx_rad3};
 	}
 };
+
+// A double in [0, 2) as 128-bit fixed point (units of 2^-127), exactly:
+// every tabulated term is at least 2^-74.
+inline uint4 fx_of_double(double t)
+{
+	uint4 e{0u, 0u, 0u, 0u};
+	if(t == 0.0) return e;
+	int ex = 0;
+	const double fr = std::frexp(t, &ex);                       // t = fr 2^ex, fr in [0.5, 1)
+	const uint64_t m53 = static_cast<uint64_t>(std::ldexp(fr, 53));
+	const int sh = ex + 74;                                     // t = m53 2^(ex - 53) = (m53 << (ex + 74)) 2^-127
+	const unsigned __int128 z = static_cast<unsigned __int128>(m53) << sh;
+	const uint64_t hi = static_cast<uint64_t>(z >> 64), lo = static_cast<uint64_t>(z);
+	e.x = static_cast<uint32_t>(lo); e.y = static_cast<uint32_t>(lo >> 32);
+	e.z = static_cast<uint32_t>(hi); e.w = static_cast<uint32_t>(hi >> 32);
+	return e;
+}
 
 inline LdsHostTables make_lds_tables()
 {
@@ -355,6 +530,34 @@ inline LdsHostTables make_lds_tables()
 				factor = factor * f;
 			}
 		}
+	}
+	// FP64-free tables: the terms at the sfac indices, per-dimension entries,
+	// base-3 radical-inverse terms
+	for(double v : t.sfac) t.fx.push_back(fx_of_double(v));
+	t.fx_dims = static_cast<uint32_t>(t.fx.size());
+	t.fx.resize(t.fx.size() + kLdsDims);
+	for(int d = 0; d < kLdsDims; ++d)
+	{
+		const uint32_t b = t.base[d];
+		uint4 &e = t.fx[t.fx_dims + d];
+		e = uint4{0u, 0u, 0u, 0u};
+		if(b < 2) continue;
+		// floor(2^64 / b) + 1: floor(m / b) = mulhi(m, this) for every m < 2^32
+		const uint64_t recip = static_cast<uint64_t>((~static_cast<unsigned __int128>(0) >> 64) / b) + 1u;
+		// f = mf 2^ef with a 53-bit mantissa
+		int ex = 0;
+		const double fr = std::frexp(t.inv[d], &ex);
+		const uint64_t mf = static_cast<uint64_t>(std::ldexp(fr, 53));
+		const int ef = ex - 53;
+		e.x = static_cast<uint32_t>(recip); e.y = static_cast<uint32_t>(recip >> 32);
+		e.z = static_cast<uint32_t>(mf);
+		e.w = static_cast<uint32_t>(mf >> 32) | (static_cast<uint32_t>(ef + 128) << 24);
+	}
+	t.fx_rad3 = static_cast<uint32_t>(t.fx.size());
+	for(int k = 0; k < 21; ++k)
+	{
+		t.fx.push_back(fx_of_double(h_inv3_pow[k]));
+		t.fx.push_back(fx_of_double(2.0 * h_inv3_pow[k]));
 	}
 	return t;
 }

@@ -46,4 +46,35 @@ def check_sampler(on_device):
         bad = int((got.view(np.uint32) != g["pow"][sel].view(np.uint32)).sum())
         if bad:
             mismatches[f"pow{e}"] = bad
+    mismatches.update(check_float_forms(on_device))
     return mismatches
+
+
+def check_float_forms(on_device, per_dim=20000, seed=11):
+    """The FP64-free float forms (kinds 9 and 10, what the kernels use) equal
+    the double loops rounded to float (kinds 0 and 6, pinned to the
+    reference above) on the reference's own indices, on random indices and
+    on the smallest and largest ones, for every dimension."""
+    g = np.load(GOLD)
+    rng = np.random.default_rng(seed)
+    bad = {}
+    n = g["lds"].shape[1]
+    for d in range(1, g["lds"].shape[0] + 1):
+        idx = (np.arange(n, dtype=np.uint64) * int(g["lds_index_mult"]) + d).astype(np.uint32)
+        idx = np.concatenate([idx, rng.integers(0, 2 ** 32, per_dim, dtype=np.uint64).astype(np.uint32),
+                              np.arange(2000, dtype=np.uint32), (2 ** 32 - 1 - np.arange(2000)).astype(np.uint32)])
+        ref = gbrt.sampler_eval(0, d, idx, on_device).astype(np.float32)
+        got = gbrt.sampler_eval(9, d, idx, on_device).astype(np.float32)
+        k = int((got.view(np.uint32) != ref.view(np.uint32)).sum())
+        if k:
+            bad[f"lds_f{d}"] = k
+    seq = np.concatenate([np.arange(1024, dtype=np.uint32) + np.uint32(g["halton_start"]) + 1,
+                          rng.integers(0, 2 ** 32, 20 * per_dim, dtype=np.uint64).astype(np.uint32)])
+    ref = gbrt.sampler_eval(6, 0, seq, on_device).astype(np.float32)
+    got = gbrt.sampler_eval(10, 0, seq, on_device).astype(np.float32)
+    k = int((got.view(np.uint32) != ref.view(np.uint32)).sum())
+    if k:
+        bad["h3_f"] = k
+    if (gbrt.sampler_eval(10, 0, seq[:1024], on_device).astype(np.float32) != g["h3"]).any():
+        bad["h3_f_golden"] = 1
+    return bad
