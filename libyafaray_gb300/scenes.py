@@ -549,9 +549,10 @@ def indoor_scene(n_boxes=463, subdiv=6, res=(960, 540), seed=5, bounces=12, rr_m
 
 
 def caustic_scene(res=(1024, 1024), subdiv=7, diffuse_photons=10_000_000, caustic_photons=10_000_000, final_gather=True,
-                  fg_samples=32, radius=0.02, search=50, fg_bounces=2, bounces=3):
+                  fg_samples=32, radius=0.02, search=50, fg_bounces=2, bounces=3, geodesic=None):
     """Photon-mapping configuration: a glass icosphere (r 0.5, IOR 1.5,
-    20 * 4**subdiv triangles: 327,680 at subdiv 7) resting on a 4 x 4 m
+    20 * 4**subdiv triangles; geodesic=freq instead makes a geodesic sphere
+    of 20 freq^2 triangles, 200,000 at freq 100) resting on a 4 x 4 m
     shinydiffuse plane (albedo 0.8), lit by a pointlight at (1, 3, 1) of power
     1000; `photonmapping` with caustics, diffuse_search = caustic_mix =
     search, diffuse_radius = caustic_radius = radius, finalGather."""
@@ -559,7 +560,7 @@ def caustic_scene(res=(1024, 1024), subdiv=7, diffuse_photons=10_000_000, causti
     plane = np.array([[-2, 0, -2], [2, 0, -2], [2, 0, 2], [-2, 0, 2]], np.float32)
     objects = [{"name": "floor", "material": "floor", "vertices": plane,
                 "faces": np.array([[0, 2, 1, TRI], [0, 3, 2, TRI]], np.uint32)}]
-    v, f = icosphere((0.0, 0.5, 0.0), 0.5, subdiv)
+    v, f = geodesic_sphere((0.0, 0.5, 0.0), 0.5, geodesic) if geodesic else icosphere((0.0, 0.5, 0.0), 0.5, subdiv)
     objects.append({"name": "ball", "material": "glass", "vertices": v, "faces": f})
     lights = [{"type": "pointlight", "from": (1.0, 3.0, 1.0), "color": (1.0, 1.0, 1.0), "power": 1000.0}]
     rx, ry = (res, res) if isinstance(res, int) else res
@@ -595,6 +596,52 @@ def cornell_pm_scene(res, final_gather, diffuse_photons=100000):
                         "finalGather": bool(final_gather), "fg_samples": 8, "fg_bounces": 2, "bounces": 3,
                         "threads_photons": 1}
     return sc
+
+
+def geodesic_sphere(center, radius, freq):
+    """Class-I geodesic sphere: every icosahedron face cut into freq^2
+    triangles (20 freq^2 in all: 200,000 at freq 100), vertices projected
+    onto the sphere and shared along the face edges, faces outward."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    V = np.array([(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+                  (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)], np.float64)
+    F = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6), (7, 1, 8),
+         (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    n = int(freq)
+    ii, jj = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    keep = ii + jj <= n
+    ii, jj = ii[keep], jj[keep]
+    local = {(int(a), int(b)): k for k, (a, b) in enumerate(zip(ii, jj))}
+    # the freq^2 triangles of one face in local vertex numbers
+    tris = []
+    for a in range(n):
+        for b in range(n - a):
+            tris.append((local[(a, b)], local[(a + 1, b)], local[(a, b + 1)]))
+            if a + b + 1 < n:
+                tris.append((local[(a + 1, b)], local[(a + 1, b + 1)], local[(a, b + 1)]))
+    tris = np.asarray(tris, np.int64)
+    P, T = [], []
+    for f, (A, B, C) in enumerate(F):
+        pts = V[A] + np.outer(ii / n, V[B] - V[A]) + np.outer(jj / n, V[C] - V[A])
+        P.append(pts / np.linalg.norm(pts, axis=1, keepdims=True))
+        T.append(tris + f * len(ii))
+    P, T = np.concatenate(P), np.concatenate(T)
+    # shared edge vertices: merge points that agree to 1e-9
+    key = np.round(P * 1e9).astype(np.int64)
+    _, first, inv = np.unique(key, axis=0, return_index=True, return_inverse=True)
+    order = np.argsort(first)
+    remap = np.empty(len(order), np.int64)
+    remap[order] = np.arange(len(order))
+    P = P[first[order]] * float(radius) + np.asarray(center, np.float64)
+    T = remap[inv.reshape(-1)][T]
+    # outward orientation
+    n_ = np.cross(P[T[:, 1]] - P[T[:, 0]], P[T[:, 2]] - P[T[:, 0]])
+    out = np.einsum("ij,ij->i", n_, P[T].mean(1) - np.asarray(center, np.float64)) >= 0
+    T[~out] = T[~out][:, [0, 2, 1]]
+    faces = np.empty((len(T), 4), np.uint32)
+    faces[:, :3] = T
+    faces[:, 3] = TRI
+    return P.astype(np.float32), faces
 
 
 def uv_sphere(center, radius, nu, nv):

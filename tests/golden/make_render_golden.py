@@ -18,7 +18,9 @@ states + flags and an adaptive render), aa_pm (adaptive passes of
 photonmapping / directlighting), cornell_tshadow (transparent shadows,
 shadowDepth 4 and 1), cornell_textured (image textures, mapper and layer
 nodes), cornell_sppm (SPPM with and without pmIRE), cornell_smooth (smoothed
-vertex normals), cornell_pt_caustics (pathtracing caustic_type / no_recursive).
+vertex normals), cornell_pt_caustics (pathtracing caustic_type / no_recursive),
+pm_full (config-5 photon maps at full size, as bucketed digests),
+cornell_512 (the Cornell configuration at 512x512).
 """
 import os
 import struct
@@ -33,6 +35,7 @@ sys.path.insert(0, ROOT)
 
 from oracle import orc  # noqa: E402
 from libyafaray_gb300 import scenes  # noqa: E402
+from tests.parity import photon_buckets  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 SAMPLER = os.path.join(ROOT, "oracle", "_ref", "sampler_dump")
@@ -194,6 +197,23 @@ def variant_golden(name, res=64, spp=16, batches=32, **kw):
     print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
 
 
+def pm_full_golden():
+    """pm_full_maps.npz: the photon maps of the photon-mapping configuration
+    at full size (200,000-triangle geodesic glass sphere, 10M diffuse + 10M
+    caustic photon paths, threads_photons 1) as bucketed digests (4096
+    buckets of count and hash sum per map) with the photon and path counts."""
+    sc = scenes.caustic_scene(res=32, geodesic=100, diffuse_photons=10_000_000, caustic_photons=10_000_000,
+                              final_gather=False, radius=0.02, search=50)
+    (d, dp), (c, cp) = orc.run_reference_photons(sc)
+    out = {}
+    for name, ph, paths in (("diffuse", d, dp), ("caustic", c, cp)):
+        counts, sums = photon_buckets(ph)
+        out.update({f"{name}_n": np.int64(len(ph)), f"{name}_paths": np.int64(paths), f"{name}_counts": counts,
+                    f"{name}_sums": sums})
+    np.savez_compressed(os.path.join(OUT, "pm_full_maps.npz"), **out)
+    print(f"pm_full_maps.npz: {len(d)} diffuse / {len(c)} caustic photons of {dp} / {cp} paths")
+
+
 def pm_golden(spp=8, batches=16):
     """photons_small.npz: diffuse and caustic photon maps of the reference
     (threads_photons 1, so photon path i uses Halton index i) for a 20k-path
@@ -290,6 +310,8 @@ if __name__ == "__main__":
         variant_golden("cornell_glass_64_render.npz", glass=True)
     if "pm" in what:
         pm_golden()
+    if "pm_full" in what:
+        pm_full_golden()
     if "hashgrid" in what:
         hashgrid_golden()
     if "dl" in what:
@@ -351,6 +373,15 @@ if __name__ == "__main__":
             print(f"{name}: mean {rgb.mean(axis=(0, 1, 2))}, flagged {[len(p['flagged']) for p in passes]}, {secs.sum():.1f} s")
     if "cornell_point" in what:
         variant_golden("cornell_point_64_render.npz", point_light=True)
+    if "cornell_512" in what:
+        # the Cornell-box configuration at its benchmark size: 512x512, 16 spp
+        # per batch, 16 batches; mean and standard error kept as float16
+        sc = scenes.cornell_scene(res=512)
+        rgb, secs = orc.run_reference_render(sc, 16, 16, threads=os.cpu_count() or 1)
+        np.savez_compressed(os.path.join(OUT, "cornell_512_render.npz"), mean=rgb.mean(0).astype(np.float16),
+                            se=(rgb.std(0, ddof=1) / np.sqrt(16)).astype(np.float16), batches=np.int32(16),
+                            spp=np.int32(16), seconds=secs)
+        print(f"cornell_512_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
     if "cornell_pt_caustics" in what:
         # pathtracing's caustic options on the glass Cornell box: photon
         # caustics, both (path + photon) with AA_clamp_indirect, no_recursive

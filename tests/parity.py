@@ -105,3 +105,26 @@ def compare_shadow(verts, faces, rays, got_occ, ref_hit):
     bad = [int(i) for i in mism if not _segment_edge_hit(verts, faces, rays[i])]
     return {"n": len(rays), "occluded": int(ref_hit.sum()), "mismatch": len(mism), "edge": len(mism) - len(bad),
             "bad": bad}
+
+
+def photon_hash(ph):
+    """64-bit hash of each photon row (dir, pos, colour: 9 float32 bits)."""
+    w = np.ascontiguousarray(ph, np.float32).view(np.uint32).astype(np.uint64)
+    h = np.full(len(w), 0x9E3779B97F4A7C15, np.uint64)
+    with np.errstate(over="ignore"):
+        for j in range(w.shape[1]):
+            h = (h ^ w[:, j]) * np.uint64(0xBF58476D1CE4E5B9)
+            h ^= h >> np.uint64(31)
+    return h
+
+
+def photon_buckets(ph, nb=4096):
+    """Order-free digest of a photon multiset: per hash bucket the photon
+    count and the wrapping sum of the photons' hashes."""
+    h = photon_hash(ph)
+    b = (h >> np.uint64(52)).astype(np.int64) % nb
+    counts = np.bincount(b, minlength=nb).astype(np.int64)
+    sums = np.zeros(nb, np.uint64)
+    with np.errstate(over="ignore"):
+        np.add.at(sums, b, h)
+    return counts, sums

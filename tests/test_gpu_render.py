@@ -51,6 +51,20 @@ def test_gpu_cornell_matches_reference(cuda_device):
     assert frac >= 0.995
 
 
+def test_gpu_cornell_512_benchmark_size_matches_reference(cuda_device):
+    """The Cornell-box configuration at the size the benchmark renders it
+    (512x512, 16 spp per batch): per-pixel means of 16 batches within 3
+    combined standard errors of the reference's on >= 99.5 % of pixel
+    channels."""
+    g = np.load(os.path.join(GOLD, "cornell_512_render.npz"))
+    r = gbrt.Renderer(scenes.cornell_scene(res=512))
+    gb = batches(r, int(g["spp"]), int(g["batches"]))
+    frac, relmse, m = parity(gb, g["mean"].astype(np.float32), g["se"].astype(np.float32))
+    print(f"cornell 512x512: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
+          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].astype(np.float32).mean(axis=(0, 1))}")
+    assert frac >= 0.995
+
+
 def test_gpu_render_accumulates_and_counts_rays(cuda_device):
     torch = pytest.importorskip("torch")
     sc = scenes.cornell_scene(res=32)

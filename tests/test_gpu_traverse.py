@@ -120,8 +120,12 @@ def test_gpu_invalid_input_is_an_error(dev):
 
 def test_gpu_full_size_properties(dev):
     """1,048,576 triangles x 16,777,216 rays (the traversal benchmark):
-    a seeded subset of rays is checked ray by ray against the oracle, and
-    closest/any-hit agree on every ray."""
+    every ray is checked against the oracle (oracle/traverse_oracle.c, all
+    host cores): the same primitive ID with a bit-identical t, or a
+    mismatch the parity rule explains (a shared edge or vertex within
+    1e-6, or an exact tie), counted and printed; closest and any-hit agree
+    on every ray, and the any-hit answer equals the oracle's on every ray
+    but the explained ones."""
     torch = pytest.importorskip("torch")
     v, f = scenes.random_triangles(1 << 20, seed=1)
     r = scenes.random_rays(1 << 24, seed=2)
@@ -138,9 +142,20 @@ def test_gpu_full_size_properties(dev):
     h = hits.cpu().numpy()
     prim = h[:, 0].view(np.int32)
     assert np.array_equal(prim >= 0, occ.cpu().numpy() >= 0)
-    sel = np.random.default_rng(3).choice(len(r), 200_000, replace=False)
-    exp = orc.OracleScene(v, f).trace(r[sel], 0)
-    assert np.array_equal(prim[sel], exp[0]) and np.array_equal(h[sel, 1], exp[1])
+    o = orc.OracleScene(v, f)
+    exp = o.trace(r, 0)
+    got = (prim, h[:, 1], h[:, 2], h[:, 3])
+    rep = parity.compare_closest(v, f, r, got, exp)
+    print(f"full size: {rep['n']} rays, {rep['hits']} hits, {rep['mismatch']} differ ({rep['edge']} shared edge, "
+          f"{rep['tie']} exact tie, {len(rep['bad'])} unexplained); t bit-identical where IDs match: {rep['t_exact']}")
+    assert rep["bad"] == [] and rep["t_exact"] and rep["uv_ok"]
+    # the rays are unbounded, so "occluded" is "has a closest hit": an any-hit
+    # difference must be one of the closest-hit differences explained above
+    exp_sh = o.trace(r, 1)
+    occ_h = occ.cpu().numpy()
+    sh_mis = np.nonzero((occ_h >= 0) != (exp_sh[0] >= 0))[0]
+    print(f"any-hit: {len(sh_mis)} of {len(r)} rays differ from the oracle")
+    assert np.isin(sh_mis, np.nonzero(prim != exp[0])[0]).all()
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
