@@ -233,8 +233,11 @@ def pm_golden(spp=8, batches=16):
         mean = rgb.mean(0)
         se = rgb.std(0, ddof=1) / np.sqrt(batches)
         name = f"pm_{'fg' if fg else 'direct'}_48_render.npz"
+        # the reference's photonmapping renders of these scenes are
+        # deterministic (Halton photon indices, batch-invariant sample
+        # positions): its first two batches are kept for a batch-by-batch check
         np.savez_compressed(os.path.join(OUT, name), mean=mean.astype(np.float32), se=se.astype(np.float32),
-                            batches=np.int32(batches), spp=np.int32(spp), seconds=secs)
+                            batches=np.int32(batches), spp=np.int32(spp), seconds=secs, batch01=rgb[:2].astype(np.float32))
         print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
 
 
@@ -250,7 +253,7 @@ def cornell_pm_golden(spp=8, batches=24):
         se = rgb.std(0, ddof=1) / np.sqrt(batches)
         name = f"cornell_pm_{'fg' if fg else 'direct'}_48_render.npz"
         np.savez_compressed(os.path.join(OUT, name), mean=mean.astype(np.float32), se=se.astype(np.float32),
-                            batches=np.int32(batches), spp=np.int32(spp), seconds=secs)
+                            batches=np.int32(batches), spp=np.int32(spp), seconds=secs, batch01=rgb[:2].astype(np.float32))
         print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
 
 

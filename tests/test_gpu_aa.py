@@ -96,7 +96,7 @@ def test_gpu_aa_render_vs_reference(cuda_device):
     frac, relmse, _ = parity(np.stack(imgs), g["mean"], g["se"])
     print(f"cornell adaptive AA 48x36: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}; "
           f"flagged per pass {np.mean(flagged, 0).round(1).tolist()} (reference batch 0: {g['flagged'].tolist()})")
-    assert frac >= 0.99
+    assert frac >= 0.995
     # the flagged counts of the reference's batch 0 against the mean of ours
     assert np.allclose(np.mean(flagged, 0), g["flagged"], rtol=0.15)
 
@@ -127,4 +127,4 @@ def test_gpu_aa_photon_integrators_vs_reference(cuda_device, name, kind):
     frac, relmse, _ = parity(np.stack(imgs), g["mean"], g["se"])
     print(f"{name}: {100 * frac:.2f}% within 3 SE, relMSE {relmse:.3g}; flagged {np.mean(flagged, 0).round(1).tolist()} "
           f"(reference batch 0: {g['flagged'].tolist()})")
-    assert frac >= 0.99
+    assert frac >= 0.995

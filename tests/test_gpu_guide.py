@@ -227,7 +227,7 @@ def _train(r, guide, passes=8, spp=4):
 
 def test_guided_render_is_unbiased(cuda_device):
     """Guided and plain converge to the same image: per-pixel means of 16
-    batches x 64 spp agree within 3 combined standard errors on >= 99 % of
+    batches x 64 spp agree within 3 combined standard errors on >= 99.5 % of
     pixel channels, and the image means within 1 %."""
     r = gbrt.Renderer(_indoor_small())
     guide = r.make_guide(log2_table=16, seed=2)
@@ -240,7 +240,7 @@ def test_guided_render_is_unbiased(cuda_device):
     frac = float(np.mean((z <= 3.0) | (se == 0)))
     rel = abs(mg.mean() - mp.mean()) / mp.mean()
     print(f"guided vs plain: {100 * frac:.2f}% within 3 SE, image means {mp.mean():.5f} / {mg.mean():.5f} ({100 * rel:.3f}%)")
-    assert frac >= 0.99 and rel < 0.01
+    assert frac >= 0.995 and rel < 0.01
 
 
 def test_trained_guide_lowers_error_at_equal_samples(cuda_device):

@@ -106,20 +106,38 @@ def test_full_size_photon_maps_match_reference(cuda_device):
         assert differ == 0
 
 
-def pm_parity(gpu_batches, ref_mean, ref_se, rel_floor=2e-5):
-    """Photon maps are the same in every batch (Halton photon indices), so
-    where the camera samples see a smooth photon estimate the per-pixel
-    standard errors fall to float rounding: a pixel channel agrees when it
-    is within 3 combined SE or within rel_floor relative (summation order
-    of the gathered photons).  Returns (fraction agreeing, relMSE, mean)."""
+# the reference renders these goldens through its box filter of width 1
+# (render_dump's film): a sample within 0.001 of a pixel edge also lands in
+# the neighbouring pixel, which the single-pixel GPU film does not do
+BOX_FILM = {"filter_type": "box", "AA_pixelwidth": 1.0}
+
+
+def pm_parity(gpu_batches, ref_mean, ref_se, rel_float=1e-5):
+    """Per-pixel means within 3 combined standard errors.  The photon maps
+    and the sample positions are the same in every batch, so where the
+    estimate is smooth a pixel's batch spread falls to float rounding; the
+    combined SE therefore carries a float term, rel_float x |mean| (the
+    photon terms of a gather, up to 64, and the 8 samples of a pixel are
+    summed in another order than the reference's).  Returns (fraction
+    agreeing, relMSE, mean, channels that agree only through the float
+    term)."""
     k = len(gpu_batches)
     m = gpu_batches.mean(0)
     se = gpu_batches.std(0, ddof=1) / np.sqrt(k)
-    comb = np.sqrt(se ** 2 + ref_se ** 2)
     d = np.abs(m - ref_mean)
-    ok = (d <= 3.0 * comb) | (d <= rel_floor * np.maximum(np.abs(ref_mean), 1e-3))
+    stat = np.sqrt(se ** 2 + ref_se ** 2)
+    comb = np.sqrt(stat ** 2 + (rel_float * np.abs(ref_mean)) ** 2)
+    ok = d <= 3.0 * comb
     relmse = float(np.mean((m - ref_mean) ** 2 / (ref_mean ** 2 + 1e-2)))
-    return float(np.mean(ok)), relmse, m
+    return float(np.mean(ok)), relmse, m, int(np.count_nonzero(ok & (d > 3.0 * stat)))
+
+
+def batch_agreement(gpu_batch, ref_batch, rel=1e-4):
+    """Fraction of pixel channels of one batch equal to the reference's same
+    batch within rel (relative, floor 1e-3), and the positions of the rest."""
+    d = np.abs(gpu_batch - ref_batch)
+    ok = d <= rel * np.maximum(np.abs(ref_batch), 1e-3)
+    return float(np.mean(ok)), np.argwhere(~ok)
 
 
 def render_batches(r, spp, k):
@@ -139,23 +157,32 @@ def test_area_light_photon_map_matches_reference(cuda_device):
     assert exact == 1.0
 
 
+def _pm_check(name, sc, fg):
+    g = np.load(os.path.join(GOLD, name))
+    sc["film"] = dict(BOX_FILM)
+    r = gbrt.Renderer(sc)
+    gb = render_batches(r, int(g["spp"]), int(g["batches"]))
+    frac, relmse, m, n_float = pm_parity(gb, g["mean"], g["se"])
+    print(f"{name}: {100 * frac:.2f}% of pixel channels within 3 SE ({n_float} through the float term), relMSE {relmse:.3g}, "
+          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
+    assert frac >= 0.995
+    if not fg:
+        # batch by batch: the same photon maps and sample positions give the
+        # reference's pixel values to float rounding
+        for b in range(2):
+            agree, rest = batch_agreement(gb[b], g["batch01"][b])
+            print(f"  batch {b}: {100 * agree:.3f}% of pixel channels equal the reference's within 1e-4; "
+                  f"others at {rest[:8].tolist()}")
+            assert agree >= 0.999
+
+
 @pytest.mark.parametrize("fg", [False, True])
 def test_photonmapping_caustic_scene_matches_reference(cuda_device, fg):
     """Glass ball on a plane under a pointlight: caustic map (kernel
     estimate), diffuse map (direct estimate or pre-gathered radiance map),
-    specular split through the ball.  Measured on a GB300: 99.4 % of pixel
-    channels agree to float precision; of the rest, two pixels differ by
-    1/8 (one of their 8 samples passes through a mesh vertex of the ball,
-    where the two implementations pick different, equally near triangles)
-    and about a dozen by 1e-4 .. 1e-2 (one photon entering or leaving a
-    gather of one sample).  Up to 1 % of pixel channels may differ."""
-    g = np.load(os.path.join(GOLD, f"pm_{'fg' if fg else 'direct'}_48_render.npz"))
-    r = gbrt.Renderer(scenes.caustic_scene_small(fg))
-    gb = render_batches(r, int(g["spp"]), int(g["batches"]))
-    frac, relmse, m = pm_parity(gb, g["mean"], g["se"])
-    print(f"photonmapping caustic scene, {'final gather' if fg else 'direct'} 48x48: {100 * frac:.2f}% agree, relMSE {relmse:.3g}, "
-          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
-    assert frac >= 0.99 and relmse < 1e-4
+    specular split through the ball.  Without final gather each batch also
+    equals the reference's same batch pixel by pixel."""
+    _pm_check(f"pm_{'fg' if fg else 'direct'}_48_render.npz", scenes.caustic_scene_small(fg), fg)
 
 
 @pytest.mark.parametrize("fg", [False, True])
@@ -163,13 +190,7 @@ def test_photonmapping_cornell_matches_reference(cuda_device, fg):
     """The Cornell box with photonmapping: area-light photons (unnormalised
     emission frame), emission counted twice, direct photon estimate or final
     gathering over the radiance map (thinned radiance points, pre-gather)."""
-    g = np.load(os.path.join(GOLD, f"cornell_pm_{'fg' if fg else 'direct'}_48_render.npz"))
-    r = gbrt.Renderer(scenes.cornell_pm_scene(48, fg))
-    gb = render_batches(r, int(g["spp"]), int(g["batches"]))
-    frac, relmse, m = pm_parity(gb, g["mean"], g["se"])
-    print(f"photonmapping cornell, {'final gather' if fg else 'direct'} 48x48: {100 * frac:.2f}% agree, relMSE {relmse:.3g}, "
-          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
-    assert frac >= 0.99 and relmse < 1e-3
+    _pm_check(f"cornell_pm_{'fg' if fg else 'direct'}_48_render.npz", scenes.cornell_pm_scene(48, fg), fg)
 
 
 def test_directlighting_caustics_matches_reference(cuda_device):
@@ -177,12 +198,14 @@ def test_directlighting_caustics_matches_reference(cuda_device):
     estimation, the recursive split through the glass and rough-glass balls,
     and the caustic photon map (glossy and specular photon paths)."""
     g = np.load(os.path.join(GOLD, "cornell_dl_48_render.npz"))
-    r = gbrt.Renderer(scenes.cornell_dl_scene(48))
+    sc = scenes.cornell_dl_scene(48)
+    sc["film"] = dict(BOX_FILM)
+    r = gbrt.Renderer(sc)
     gb = render_batches(r, int(g["spp"]), int(g["batches"]))
-    frac, relmse, m = pm_parity(gb, g["mean"], g["se"])
-    print(f"directlighting glass cornell 48x48: {100 * frac:.2f}% agree, relMSE {relmse:.3g}, "
+    frac, relmse, m, n_float = pm_parity(gb, g["mean"], g["se"])
+    print(f"directlighting glass cornell 48x48: {100 * frac:.2f}% agree ({n_float} through the float term), relMSE {relmse:.3g}, "
           f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
-    assert frac >= 0.99
+    assert frac >= 0.995
 
 
 def test_grid_cell_assignment_matches_reference_hashgrid(cuda_device):

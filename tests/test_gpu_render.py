@@ -171,7 +171,7 @@ def test_gpu_cornell_sppm_matches_reference(cuda_device, name, ire):
     frac, relmse, m = parity(gb, g["mean"], g["se"])
     print(f"{name}: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
           f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
-    assert frac >= 0.99
+    assert frac >= 0.995
 
 
 def test_gpu_cornell_smooth_normals_match_reference(cuda_device):
@@ -217,8 +217,8 @@ def test_gpu_pathtracing_caustic_options_match_reference(cuda_device, name, kw):
 
 def test_gpu_explicit_normals_equal_smoothing(cuda_device):
     """Vertex normals given per vertex (yafaray_addNormal: one normal per
-    vertex, every face corner using its vertex's) render exactly like the
-    same normals made by smoothing at 181 degrees."""
+    vertex, every face corner using its vertex's) render like the same
+    normals made by smoothing at 181 degrees."""
     sc = scenes.smooth_cornell_scene(res=32, glass=False)
     a = gbrt.Renderer(sc).render(4, base_offset=0, seed=5)[0]
     sc2 = scenes.smooth_cornell_scene(res=32, glass=False)
@@ -227,7 +227,8 @@ def test_gpu_explicit_normals_equal_smoothing(cuda_device):
             o["normals"], _ = gbrt.smooth_normals(o["vertices"], o["faces"], 181.0)
             del o["smooth"]
     b = gbrt.Renderer(sc2).render(4, base_offset=0, seed=5)[0]
-    assert np.array_equal(a, b)
+    # equal up to the film's float atomics (their order varies from run to run)
+    assert np.allclose(a, b, rtol=1e-5, atol=1e-6)
 
 
 def test_gpu_cornell_shiny_layers_match_reference(cuda_device):
