@@ -317,9 +317,9 @@ def render_sections(args):
         "msamples_s": best["camera_samples"] / best["ms"] / 1e3,
         "rays_per_frame": rays, "reference_cpu_note": "reference renders this frame in 3.37 s on 8 x86 threads"}
     del r
-    # photonmapping: glass ball (327,680 triangles) on a plane under a pointlight,
-    # 10M diffuse + 10M caustic photon paths, final gather 32, 1024x1024, 1 spp
-    sc = scenes.caustic_scene(res=1024, subdiv=7, diffuse_photons=10_000_000, caustic_photons=10_000_000,
+    # photonmapping: glass ball (200,000-triangle geodesic sphere) on a plane under
+    # a pointlight, 10M diffuse + 10M caustic photon paths, final gather 32, 1024x1024, 1 spp
+    sc = scenes.caustic_scene(res=1024, geodesic=100, diffuse_photons=10_000_000, caustic_photons=10_000_000,
                               final_gather=True, fg_samples=32, radius=0.02, search=50)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -339,7 +339,7 @@ def render_sections(args):
     best = min(frames, key=lambda x: x["wall_ms"])
     rays = best["extension_rays"] + best["shadow_rays"]
     out["photon_mapping"] = {
-        "workload": "glass icosphere r 0.5 (327,680 triangles, IOR 1.5) on a 4x4 m plane, pointlight power 1000; photonmapping "
+        "workload": "glass geodesic sphere r 0.5 (200,000 triangles, IOR 1.5) on a 4x4 m plane, pointlight power 1000; photonmapping "
                     "10M diffuse + 10M caustic photon paths, radius 0.02, search 50, final gather 32, 1024x1024, 1 spp",
         "scene_bvh_build_and_upload_s": build_s,
         "photon_paths": best["photon_paths"], "photons_stored": best["photons_stored"],
@@ -358,20 +358,31 @@ def render_sections(args):
     setup_s = time.perf_counter() - t0
     films = [torch.zeros(r.scene["camera"]["resx"] * r.scene["camera"]["resy"] * 3, dtype=torch.float32, device="cuda")
              for r in rs]
-    gbrt.render_batch(rs[:4], 1, [f.data_ptr() for f in films[:4]])        # warm-up
+    ptrs = [f.data_ptr() for f in films]
+    # the autotuner's trial renders (1 spp of the whole batch per candidate)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    st = gbrt.render_batch(rs, 64, [f.data_ptr() for f in films], concurrency=8)
+    _, tuning = gbrt.render_multi(rs, 1, ptrs)
+    torch.cuda.synchronize()
+    tune_wall_s = time.perf_counter() - t0
+    for f in films:
+        f.zero_()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st, _ = gbrt.render_multi(rs, 64, ptrs, tuning=tuning)
     torch.cuda.synchronize()
     batch_s = time.perf_counter() - t0
-    rays = sum(x["extension_rays"] + x["shadow_rays"] for x in st)
-    samples = sum(x["camera_samples"] for x in st)
+    rays = st["extension_rays"] + st["shadow_rays"]
+    samples = st["camera_samples"]
     out["batch_64_scenes"] = {
         "workload": "64 seeded scenes (seed 1000+i): round(10^U[3, log10 2e6]) triangles of spheres / tori on a plane, "
                     "50 % shinydiffuse, 30 % glossy, 20 % rough_glass, 1-4 area lights, 256/512/1024 square, 64 spp, bounces 8",
         "triangles": int(sum(len(r.faces) for r in rs)), "camera_samples": samples, "rays": rays,
-        "scene_setup_s": setup_s, "batch_wall_s": batch_s, "mrays_s": rays / batch_s / 1e6,
-        "msamples_s": samples / batch_s / 1e6, "concurrency": 8,
+        "scene_setup_s": setup_s, "batch_wall_s": batch_s, "batch_device_ms": st["ms"], "mrays_s": rays / batch_s / 1e6,
+        "msamples_s": samples / batch_s / 1e6,
+        "execution": "one wavefront over all 64 scenes (gbrt_pt_render_multi)",
+        "autotuned": {k: tuning[k] for k in ("wave_paths", "shade_block", "trace_blocks_per_sm")},
+        "autotune_wall_s": tune_wall_s, "autotune_device_ms": tuning["tune_ms"],
         "reference_cpu_note": "reference, extrapolated: 8 of the 64 scenes (every 8th) at 1 spp took 4.49 s on 8 x86 threads "
                               "(oracle/_ref render_dump, scene trees already built) -> about 2,300 s for 64 scenes x 64 spp"}
     del rs, films

@@ -474,11 +474,34 @@ int gbrt_pt_render_aa_host(gbrt_scene *scene, const gbrt_camera_desc *camera, co
 int gbrt_aa_flags(const float *film_dev, const float *weight_dev, int32_t resx, int32_t resy, const gbrt_aa_params *aa,
                   float threshold, uint8_t *flags_dev, uint32_t *n_flagged);
 
-/* Renders n scenes (each with its camera, parameters and device float film),
- * up to `concurrency` at a time (0 = 8), each on its own stream from its own
- * host thread, freeing each scene's work buffers after its render; wave_paths
- * 0 means 2 Mi per scene here.  stats: NULL or n entries.  Returns the first
- * error (its message names the scene). */
+/* ---- a batch of scenes in one wavefront ------------------------------------
+ * n scenes (each with its camera, parameters and device film) rendered
+ * together: every scene's camera samples form one index range, each wave of
+ * the wavefront takes a stretch of it across scenes, and every kernel of a
+ * vertex level serves all of them (the per-scene render loop of
+ * TiledIntegrator::render, integrator_tiled.cc:222-251, for many scenes at
+ * once).  pathtracing only: no guide and no photon caustics; the scenes must
+ * agree on film filtering and transparent shadows.  The first scene's work
+ * buffers serve the batch.  Synchronises `stream`.
+ *
+ * tuning: NULL, or in/out: a zero field is chosen by the autotuner (short
+ * device-timed trial renders of the whole batch at 1 sample per pixel into
+ * scratch films: the wave size, then the shading block size, then the
+ * residency of the persistent traversal grids), which writes back what it
+ * chose and the device time it spent; pass the result back to skip tuning.
+ * stats: NULL or one entry with the batch's totals. */
+typedef struct gbrt_batch_tuning {
+	uint32_t wave_paths;            /* paths per wave (the spawn buffers may cap it) */
+	uint32_t shade_block;           /* threads per block of the shading kernel, 32 .. 128 */
+	uint32_t trace_blocks_per_sm;   /* resident blocks per SM of the traversal grids */
+	float tune_ms;                  /* out: device time of the trial renders */
+} gbrt_batch_tuning;
+int gbrt_pt_render_multi(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params,
+                         float *const *films, uint32_t n, gbrt_batch_tuning *tuning, gbrt_pt_stats *stats, void *stream);
+
+/* gbrt_pt_render_multi with the autotuner on the default stream (concurrency
+ * is unused).  stats: NULL or n entries: each scene's camera samples, the
+ * batch's ray counts and device time in entry 0. */
 int gbrt_pt_render_batch(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params, float *const *films,
                          uint32_t n, uint32_t concurrency, gbrt_pt_stats *stats);
 

@@ -167,6 +167,7 @@ struct Params {
 
 struct Work {
 	uint32_t *p_pixel, *p_si, *p_state;
+	uint32_t *p_scene;          // batch renders: the path's entry of the scene table
 	float4 *p_thr;
 	uint4 *p_task;              // integrate() call of the path: {level | addl << 8 | division << 16, branch, deco1, deco2}
 	float4 *p_pm;               // final gathering: path length, colour of the last lookup
@@ -1518,6 +1519,7 @@ __device__ void light_estimation(const SceneDev &sc, const Surface &s, const flo
 struct SpawnWriter {
 	float4 *out;
 	uint32_t slot, end, cap;
+	uint32_t scene;               // the caller's entry of a batch's scene table (0 for one scene)
 	__device__ void put(const float o[3], const float d[3], const float wt[3], uint32_t pixel, uint32_t si, uint32_t tx, uint32_t branch,
 	                    float d1, float d2)
 	{
@@ -1529,7 +1531,7 @@ struct SpawnWriter {
 			r[1] = make_float4(d[0], d[1], d[2], -1.f);
 			r[2] = make_float4(wt[0], wt[1], wt[2], 0.f);
 			r[3] = make_float4(__uint_as_float(pixel), __uint_as_float(si), __uint_as_float(tx), __uint_as_float(branch));
-			r[4] = make_float4(d1, d2, 0.f, 0.f);
+			r[4] = make_float4(d1, d2, __uint_as_float(scene), 0.f);
 		}
 		++slot;
 	}
@@ -1685,47 +1687,50 @@ __device__ __forceinline__ void film_put(const Params &P, float *film, double *f
 	else film_add(film, film64, pixel, r, g, b);
 }
 
-__global__ void __launch_bounds__(kThreads) k_camera(Camera cam, Params P, Work W)
+// Camera sample g (an index into the render's sample-major path order) into
+// path slot s: sample-major order, so a wave holds whole sample indices of
+// every pixel, each wave (and each guide training batch drawn from it)
+// covers the full image, and neighbouring threads shoot neighbouring
+// pixels; the path samples of one camera sample are adjacent (so a wave of
+// W paths holds at most W / path_samples + 2 integrate() roots).
+__device__ __forceinline__ void camera_path(const Camera &cam, const Params &P, const Work &W, uint32_t s, uint32_t g)
 {
-	// sample-major order: a wave holds whole sample indices of every pixel,
-	// so each wave (and each guide training batch drawn from it) covers the
-	// full image, and neighbouring threads shoot neighbouring pixels; the
-	// path samples of one camera sample are adjacent (so a wave of W paths
-	// holds at most W / path_samples + 2 integrate() roots)
 	const uint32_t n_pix = P.pix_list ? P.n_list : static_cast<uint32_t>(cam.resx) * static_cast<uint32_t>(cam.resy);
 	const uint32_t ps = static_cast<uint32_t>(P.path_samples);
-	for(uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < P.wave_n; s += gridDim.x * blockDim.x)
+	const uint32_t rest = g / ps, sub = g % ps;
+	const uint32_t pixel = P.pix_list ? P.pix_list[rest % n_pix] : rest % n_pix, si = (rest / n_pix) * ps + sub;
+	float dx, dy;
+	sample_pos(P, pixel, si, dx, dy);
+	const float px = xa(static_cast<float>(pixel % static_cast<uint32_t>(cam.resx)), dx);
+	const float py = xa(static_cast<float>(pixel / static_cast<uint32_t>(cam.resx)), dy);
+	float d[3];
+	for(int k = 0; k < 3; ++k) d[k] = xa(xa(xm(cam.vright[k], px), xm(cam.vup[k], py)), cam.vto[k]);
+	const float l2 = dot3(d, d);
+	if(l2 != 0.f)
 	{
-		const uint32_t g = P.wave_start + s;
-		const uint32_t rest = g / ps, sub = g % ps;
-		const uint32_t pixel = P.pix_list ? P.pix_list[rest % n_pix] : rest % n_pix, si = (rest / n_pix) * ps + sub;
-		float dx, dy;
-		sample_pos(P, pixel, si, dx, dy);
-		const float px = xa(static_cast<float>(pixel % static_cast<uint32_t>(cam.resx)), dx);
-		const float py = xa(static_cast<float>(pixel / static_cast<uint32_t>(cam.resx)), dy);
-		float d[3];
-		for(int k = 0; k < 3; ++k) d[k] = xa(xa(xm(cam.vright[k], px), xm(cam.vup[k], py)), cam.vto[k]);
-		const float l2 = dot3(d, d);
-		if(l2 != 0.f)
-		{
-			const float inv = __fdiv_rn(1.f, sqrtf(l2));
-			for(int k = 0; k < 3; ++k) d[k] = xm(d[k], inv);
-		}
-		W.p_pixel[s] = pixel;
-		W.p_si[s] = si;
-		W.p_thr[s] = make_float4(1.f, 1.f, 1.f, 0.f);
-		W.p_state[s] = 0u;
-		W.p_task[s] = make_uint4(1u << 16, 0u, 0u, 0u);       // ray level 0, division 1
-		if(W.p_sum)
-		{
-			W.p_sum[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-			for(uint32_t k = 0; k < P.rec_stride; ++k) W.r_valid[static_cast<size_t>(s) * P.rec_stride + k] = 0u;
-		}
-		W.q_ray[0][2ull * s] = make_float4(cam.from[0], cam.from[1], cam.from[2], 0.f);
-		W.q_ray[0][2ull * s + 1] = make_float4(d[0], d[1], d[2], -1.f);
-		W.q_path[0][s] = s;
-		if(P.film_w && sub == 0) film_splat(P, nullptr, nullptr, pixel, si, 0.f, 0.f, 0.f, true);
+		const float inv = __fdiv_rn(1.f, sqrtf(l2));
+		for(int k = 0; k < 3; ++k) d[k] = xm(d[k], inv);
 	}
+	W.p_pixel[s] = pixel;
+	W.p_si[s] = si;
+	W.p_thr[s] = make_float4(1.f, 1.f, 1.f, 0.f);
+	W.p_state[s] = 0u;
+	W.p_task[s] = make_uint4(1u << 16, 0u, 0u, 0u);       // ray level 0, division 1
+	if(W.p_sum)
+	{
+		W.p_sum[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+		for(uint32_t k = 0; k < P.rec_stride; ++k) W.r_valid[static_cast<size_t>(s) * P.rec_stride + k] = 0u;
+	}
+	W.q_ray[0][2ull * s] = make_float4(cam.from[0], cam.from[1], cam.from[2], 0.f);
+	W.q_ray[0][2ull * s + 1] = make_float4(d[0], d[1], d[2], -1.f);
+	W.q_path[0][s] = s;
+	if(P.film_w && sub == 0) film_splat(P, nullptr, nullptr, pixel, si, 0.f, 0.f, 0.f, true);
+}
+
+__global__ void __launch_bounds__(kThreads) k_camera(Camera cam, Params P, Work W)
+{
+	for(uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < P.wave_n; s += gridDim.x * blockDim.x)
+		camera_path(cam, P, W, s, P.wave_start + s);
 	if(blockIdx.x == 0 && threadIdx.x == 0)
 	{
 		W.count[0] = P.wave_n;
@@ -1756,8 +1761,42 @@ __global__ void __launch_bounds__(kThreads) k_extend(gbrt::BvhView bv, const flo
 		});
 }
 
-__global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work W, int cur, int resx, uint32_t shadow_cap,
-                                                    float *film, double *film64)
+// One batch scene as the batch kernels read it: the scene, its render
+// parameters, camera and film, and its range of the batch's path indices.
+struct BatchScene {
+	SceneDev sc;
+	Params P;
+	Camera cam;
+	float *film;
+	uint32_t path_begin, paths;
+};
+
+// Where a queue entry's scene comes from: the launch's one scene (kernel
+// parameters), or the batch's scene table indexed by the path's scene.
+struct OneScene {
+	SceneDev sc;
+	Params P;
+	float *film;
+	double *film64;
+	__device__ __forceinline__ uint32_t id(const Work &, uint32_t) const { return 0u; }
+	__device__ __forceinline__ const SceneDev &scene(uint32_t) const { return sc; }
+	__device__ __forceinline__ const Params &params(uint32_t) const { return P; }
+	__device__ __forceinline__ float *film_of(uint32_t) const { return film; }
+	__device__ __forceinline__ double *film64_of(uint32_t) const { return film64; }
+};
+
+struct SceneTable {
+	const BatchScene *bs;
+	__device__ __forceinline__ uint32_t id(const Work &W, uint32_t path) const { return W.p_scene[path]; }
+	__device__ __forceinline__ const SceneDev &scene(uint32_t i) const { return bs[i].sc; }
+	__device__ __forceinline__ const Params &params(uint32_t i) const { return bs[i].P; }
+	__device__ __forceinline__ float *film_of(uint32_t i) const { return bs[i].film; }
+	__device__ __forceinline__ double *film64_of(uint32_t) const { return nullptr; }
+};
+
+// Shading of one vertex level of the wavefront (see the kernels below).
+template <typename Src>
+__device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uint32_t shadow_cap)
 {
 	const uint32_t n = W.count[cur];
 	const int nxt = cur ^ 1;
@@ -1767,6 +1806,13 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 	{
 		const uint32_t q = base + threadIdx.x;
 		const bool live = q < n;
+		const uint32_t path0 = live ? W.q_path[cur][q] : 0u;
+		const uint32_t sid = live ? src.id(W, path0) : 0u;
+		const SceneDev &sc = src.scene(sid);
+		const Params &P = src.params(sid);
+		float *const film = src.film_of(sid);
+		double *const film64 = src.film64_of(sid);
+		const int resx = P.film_resx;
 		bool cont = false;
 		float nray[8];
 		uint32_t path = 0, n_shadow = 0;
@@ -1778,7 +1824,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 		bool hit = false;
 		if(live)
 		{
-			path = W.q_path[cur][q];
+			path = path0;
 			const float4 h = W.hits[q];
 			const int32_t prim = __float_as_int(h.x);
 			if(prim >= 0)
@@ -2003,7 +2049,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 			uint32_t sbase = 0;
 			if(lane == 31) sbase = atomicAdd(W.sp_count, stotal);
 			sbase = __shfl_sync(0xffffffffu, sbase, 31);
-			SpawnWriter spw{W.sp_out, sbase + sincl - n_spawn, sbase + sincl, W.sp_cap};
+			SpawnWriter spw{W.sp_out, sbase + sincl - n_spawn, sbase + sincl, W.sp_cap, sid};
 			if(n_spawn)
 				spawn_children(sc, P, s, wo, thr, pixel, si, sample_, offset_, level + 1u, addl, division, branch, deco1, deco2,
 				               do_glossy, do_spec, spw);
@@ -2142,6 +2188,18 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneDev sc, Params P, Work 
 	}
 }
 
+__global__ void __launch_bounds__(kThreads, 1) k_shade(SceneDev sc, Params P, Work W, int cur, uint32_t shadow_cap, float *film,
+                                                    double *film64)
+{
+	shade_queue(OneScene{sc, P, film, film64}, W, cur, shadow_cap);
+}
+
+// The same for a batch of scenes: every path's scene from the table.
+__global__ void __launch_bounds__(kThreads, 1) k_shade_batch(const BatchScene *__restrict__ bs, Work W, int cur, uint32_t shadow_cap)
+{
+	shade_queue(SceneTable{bs}, W, cur, shadow_cap);
+}
+
 // Material::getTransparency of a shadow-ray hit, wo = the shadow ray's
 // direction, n = the shading normal face-forwarded by the geometric one
 // (SurfacePoint::normalFaceForward): ShinyDiffuseMaterial (material_shiny_diffuse.cc:541-563:
@@ -2250,6 +2308,92 @@ __global__ void __launch_bounds__(kThreads) k_shadow(SceneDev sc, Params P, Work
 	if((threadIdx.x & 31u) == 0 && traced) atomicAdd(W.stats + 1, static_cast<unsigned long long>(traced));
 }
 
+// ---- a batch of scenes in one wavefront --------------------------------------
+// The batch kernels run every scene's paths together: a wave is a range of
+// the batch's path indices (the scenes' sample-major orders back to back),
+// every path carries its scene's index, and each kernel reads the scene
+// (hierarchy, materials, lights, parameters, film) from the table.
+
+__global__ void __launch_bounds__(kThreads) k_camera_batch(const BatchScene *__restrict__ bs, uint32_t n_scenes, uint32_t wave_start,
+                                                           uint32_t wave_n, Work W)
+{
+	for(uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < wave_n; s += gridDim.x * blockDim.x)
+	{
+		const uint32_t g = wave_start + s;
+		uint32_t lo = 0, hi = n_scenes;            // the last scene whose range starts at or before g
+		while(hi - lo > 1)
+		{
+			const uint32_t mid = (lo + hi) >> 1;
+			if(bs[mid].path_begin <= g) lo = mid;
+			else hi = mid;
+		}
+		W.p_scene[s] = lo;
+		camera_path(bs[lo].cam, bs[lo].P, W, s, g - bs[lo].path_begin);
+	}
+	if(blockIdx.x == 0 && threadIdx.x == 0)
+	{
+		W.count[0] = wave_n;
+		atomicAdd(W.stats, static_cast<unsigned long long>(wave_n));
+	}
+}
+
+__global__ void __launch_bounds__(kThreads) k_extend_batch(const BatchScene *__restrict__ bs, Work W, int cur)
+{
+	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
+	const float4 *__restrict__ rays = W.q_ray[cur];
+	gbrt::OpaqueHits f;
+	gbrt::trace_persistent_filtered<false, true>(
+		bs[0].sc.bv, W.count[cur], W.count + 4, stack + threadIdx.x, kThreads, f,
+		[&](uint32_t i, float r[8], gbrt::BvhView &bv) {
+			const float4 a = rays[2ull * i], b = rays[2ull * i + 1];
+			r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w; r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+			bv = bs[W.p_scene[W.q_path[cur][i]]].sc.bv;
+			return true;
+		},
+		[&](uint32_t i, const gbrt::Hit &h) { W.hits[i] = make_float4(__int_as_float(h.prim), h.t, h.u, h.v); });
+}
+
+template <bool kFilm, bool kTransparent>
+__global__ void __launch_bounds__(kThreads) k_shadow_batch(const BatchScene *__restrict__ bs, Work W, uint32_t shadow_cap)
+{
+	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
+	const uint32_t n = min(W.count[2], shadow_cap);
+	uint32_t traced = 0;
+	using Filter = typename std::conditional<kTransparent, TransparentHits, gbrt::OpaqueHits>::type;
+	Filter f;
+	gbrt::trace_persistent_filtered<true, true>(
+		bs[0].sc.bv, n, W.count + 5, stack + threadIdx.x, kThreads, f,
+		[&](uint32_t i, float r[8], gbrt::BvhView &bv) {
+			if(W.s_pix[i] == kDead) return false;
+			const float4 a = W.s_ray[2ull * i], b = W.s_ray[2ull * i + 1];
+			r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w; r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+			const BatchScene &B = bs[W.p_scene[W.s_path[i]]];
+			bv = B.sc.bv;
+			if constexpr(kTransparent)
+			{
+				f.sc = &B.sc;
+				f.mats = B.sc.mats;
+				f.prim_ng = B.sc.prim_ng;
+				f.max_depth = B.P.shadow_depth;
+			}
+			++traced;
+			return true;
+		},
+		[&](uint32_t i, const gbrt::Hit &h) {
+			if(h.prim < 0)
+			{
+				const uint32_t path = W.s_path[i];
+				const BatchScene &B = bs[W.p_scene[path]];
+				float4 c = W.s_col[i];
+				if constexpr(kTransparent) { c.x *= f.col[0]; c.y *= f.col[1]; c.z *= f.col[2]; }
+				if(kFilm) film_splat(B.P, B.film, nullptr, W.s_pix[i], W.p_si[path], c.x, c.y, c.z, false);
+				else film_add(B.film, nullptr, W.s_pix[i], c.x, c.y, c.z);
+			}
+		});
+	for(int off = 16; off > 0; off >>= 1) traced += __shfl_xor_sync(0xffffffffu, traced, off);
+	if((threadIdx.x & 31u) == 0 && traced) atomicAdd(W.stats + 1, static_cast<unsigned long long>(traced));
+}
+
 // Records of a finished wave -> training records {pos, dir, c, 0} with
 // c = luminance(incident radiance) x h / mixture pdf, where h is the BSDF x
 // cosine factor of the estimator (the guide learns the product), incident
@@ -2348,6 +2492,7 @@ __global__ void __launch_bounds__(kThreads) k_spawn_init(Work W, const float4 *_
 			W.p_thr[slot] = make_float4(r2.x, r2.y, r2.z, 0.f);
 			W.p_state[slot] = 0u;
 			W.p_task[slot] = make_uint4(__float_as_uint(r3.z), __float_as_uint(r3.w), __float_as_uint(r4.x), __float_as_uint(r4.y));
+			if(W.p_scene) W.p_scene[slot] = __float_as_uint(r4.z);
 			W.q_ray[0][2ull * slot] = r0;
 			W.q_ray[0][2ull * slot + 1] = r1;
 			W.q_path[0][slot] = slot;
@@ -3166,7 +3311,7 @@ int alloc_work(gbrt_scene *S, size_t paths, size_t shadow, size_t stride, cudaSt
 	const size_t o_pix = carve(4 * paths), o_si = carve(4 * paths), o_st = carve(4 * paths), o_thr = carve(16 * paths);
 	const size_t o_task = carve(16 * paths), o_pm = carve(16 * paths);
 	const size_t o_qr0 = carve(32 * paths), o_qr1 = carve(32 * paths), o_qp0 = carve(4 * paths), o_qp1 = carve(4 * paths);
-	const size_t o_hit = carve(16 * paths);
+	const size_t o_hit = carve(16 * paths), o_scene = carve(4 * paths);
 	const size_t o_sr = carve(32 * shadow), o_sc = carve(16 * shadow), o_sp = carve(4 * shadow), o_spath = carve(4 * shadow);
 	const size_t o_cnt = carve(64), o_stats = carve(64);
 	size_t o_hp = 0, o_lob = 0, o_psum = 0, o_rpos = 0, o_rdir = 0, o_rthr = 0, o_rpre = 0, o_rval = 0, o_train = 0;
@@ -3193,6 +3338,7 @@ int alloc_work(gbrt_scene *S, size_t paths, size_t shadow, size_t stride, cudaSt
 	w.q_path[0] = reinterpret_cast<uint32_t *>(b + o_qp0);
 	w.q_path[1] = reinterpret_cast<uint32_t *>(b + o_qp1);
 	w.hits = reinterpret_cast<float4 *>(b + o_hit);
+	w.p_scene = reinterpret_cast<uint32_t *>(b + o_scene);
 	w.s_ray = reinterpret_cast<float4 *>(b + o_sr);
 	w.s_col = reinterpret_cast<float4 *>(b + o_sc);
 	w.s_pix = reinterpret_cast<uint32_t *>(b + o_sp);
@@ -4047,7 +4193,7 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 				k_pm_root<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, film, film64_dev);
 			if(level_guided)
 				if(int rc = gbrt_guide_eval_queue(guide, Ww.hitpos, n, Ww.count + cur, Ww.lobes, s)) return rc;
-			k_shade<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, camera->resx, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+			k_shade<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
 			const uint32_t scap = static_cast<uint32_t>(shadow_cap);
 			if(Pw.film_w && Pw.tshadow)
 				k_shadow<true, true><<<persistent_grid(k_shadow<true, true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, scap, film, film64_dev);
@@ -4814,53 +4960,349 @@ int gbrt_pm_render(gbrt_scene *S, const gbrt_camera_desc *camera, const gbrt_pt_
 	return pm_render_impl(S, camera, params, pm, film_dev, film64_dev, stats, stream, nullptr, nullptr);
 }
 
+// ---- a batch of scenes in one wavefront --------------------------------------
+// Every scene's camera samples form one index range (scene after scene, each
+// in its own sample-major order); a wave is a stretch of that range, so the
+// kernels of a vertex level serve all scenes at once (k_camera_batch,
+// k_extend_batch, k_shade_batch, k_shadow_batch) and the spawned calls of
+// the recursive split carry their scene along.  The first scene's work and
+// spawn buffers serve the batch.
+
+struct BatchPlan {
+	uint32_t wave;              // paths per wave
+	uint32_t shade_block;       // threads per block of k_shade_batch
+	uint32_t trace_bps;         // resident blocks per SM of the persistent traversal grids
+};
+
+// Resident blocks per SM of a persistent kernel at kThreads threads.
+static int max_blocks_per_sm(const void *kernel)
+{
+	int bps = 1;
+	if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, kThreads, 0) != cudaSuccess || bps < 1) bps = 1;
+	return bps;
+}
+
+static int batch_render_locked(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params,
+                               float *const *films, uint32_t n, const BatchPlan &plan, int spp_override, gbrt_pt_stats *stats,
+                               cudaStream_t s)
+{
+	gbrt_scene *S0 = scenes[0];
+	const bool tshadow = params[0].transparent_shadows != 0;
+	const bool filtered = params[0].filter_type != GBRT_FILTER_PIXEL;
+	std::vector<BatchScene> host(n);
+	uint64_t total = 0;
+	uint32_t fanout = 0, max_shadow = 0;
+	int split_levels = 0, bounces = 0;
+	uint64_t n_min = ~0ull;
+	for(uint32_t i = 0; i < n; ++i)
+	{
+		gbrt_scene *S = scenes[i];
+		gbrt_pt_params pp = params[i];
+		if(spp_override > 0) pp.spp = spp_override;
+		const gbrt_camera_desc &c = cameras[i];
+		if(S->device != S0->device) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_multi: scene %u is on another device", i);
+		if(pp.guide || (pp.caustic_type != GBRT_CAUSTIC_PATH && pp.caustic_type != GBRT_CAUSTIC_NONE))
+			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_multi: scene %u: no guide or photon caustics in a batch", i);
+		if((pp.transparent_shadows != 0) != tshadow || (pp.filter_type != GBRT_FILTER_PIXEL) != filtered)
+			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_multi: scene %u: film filtering and transparent shadows must agree", i);
+		if(c.resx <= 0 || c.resy <= 0 || pp.spp <= 0 || pp.path_samples <= 0 || pp.bounces < 0 || pp.path_samples > 64 || !films[i])
+			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_multi: scene %u: bad resolution, sampling parameters or film", i);
+		if(S->ev_last) GBRT_CK(cudaStreamWaitEvent(s, S->ev_last, 0));
+		BatchScene &B = host[i];
+		B.sc = scene_dev(S);
+		Params &P = B.P;
+		P = Params{};
+		P.spp = pp.spp; P.path_samples = pp.path_samples; P.bounces = pp.bounces; P.rr_min = pp.russian_roulette_min_bounces;
+		P.raydepth = pp.raydepth > 0 ? pp.raydepth : 5;
+		P.film_resx = c.resx; P.film_resy = c.resy;
+		P.lmult = 1.f;
+		P.tshadow = pp.transparent_shadows ? 1 : 0;
+		P.shadow_depth = pp.shadow_depth;
+		if(int rc = film_setup(S, pp, P, s)) return rc;
+		P.base_offset = pp.base_sampling_offset; P.seed = pp.seed;
+		P.pt_caustic_path = pp.caustic_type == GBRT_CAUSTIC_PATH ? 1 : 0;
+		P.no_recursive = pp.no_recursive ? 1 : 0;
+		P.clamp_indirect = pp.clamp_indirect;
+		P.d1 = 1.f / static_cast<float>(pp.spp);
+		P.n_lights = S->n_lights;
+		B.cam = make_camera(c);
+		B.film = films[i];
+		const uint64_t paths = static_cast<uint64_t>(c.resx) * c.resy * pp.spp * pp.path_samples;
+		B.path_begin = static_cast<uint32_t>(total);
+		B.paths = static_cast<uint32_t>(paths);
+		total += paths;
+		if(total >= (1ull << 32)) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_pt_render_multi: more than 2^32 paths in the batch");
+		const uint32_t f = split_fanout(S, pp.path_samples);
+		fanout = std::max(fanout, f);
+		if(f) split_levels = std::max(split_levels, std::min(19, P.raydepth + static_cast<int>(S->max_addl)));
+		n_min = std::min<uint64_t>(n_min, std::max<uint64_t>(1, static_cast<uint64_t>(pp.path_samples) / (S->split_glossy ? 8u : 1u)));
+		bounces = std::max(bounces, pp.bounces);
+		uint32_t all = 0, one = 0;
+		for(const auto &l : S->lights_host)
+		{
+			const uint32_t ns = 2u * static_cast<uint32_t>(std::ceil(static_cast<float>(l.samples)));
+			all += ns;
+			one = std::max(one, ns);
+		}
+		max_shadow = std::max(max_shadow, std::max(all, one));
+	}
+	// waves are cut so the spawned calls of one wave always fit
+	constexpr uint64_t kSpawnCap = 1ull << 24;
+	uint64_t wave = std::min<uint64_t>(total, std::max<uint32_t>(plan.wave, 256u));
+	size_t spawn_cap = 0;
+	uint64_t chunk = wave;
+	if(split_levels > 0)
+	{
+		const uint64_t roots = std::max<uint64_t>(1, kSpawnCap / fanout - 2);
+		wave = std::max<uint64_t>(1, std::min<uint64_t>(wave, roots));
+		spawn_cap = static_cast<size_t>((wave + 2) * fanout);
+		chunk = std::max<uint64_t>(1, std::min<uint64_t>(wave, (spawn_cap / fanout - 1) * n_min));
+		if(int rc = alloc_spawn(S0, spawn_cap, split_levels, s)) return rc;
+	}
+	const size_t shadow_cap = std::max<size_t>(1, wave * max_shadow);
+	if(int rc = alloc_work(S0, wave, shadow_cap, 0, s)) return rc;
+	BatchScene *table = nullptr;
+	GBRT_CK(cudaMallocAsync(reinterpret_cast<void **>(&table), sizeof(BatchScene) * n, s));
+	GBRT_CK(cudaMemcpyAsync(table, host.data(), sizeof(BatchScene) * n, cudaMemcpyHostToDevice, s));
+	Work W = S0->w;
+	const int n_sm = S0->n_sm;
+	const uint32_t scap = static_cast<uint32_t>(shadow_cap);
+	const uint32_t sblock = std::max(32u, std::min<uint32_t>(kThreads, plan.shade_block & ~31u));
+	auto trace_grid = [&](size_t nq, int bps_max) {
+		const int bps = std::max(1, std::min<int>(bps_max, plan.trace_bps ? static_cast<int>(plan.trace_bps) : bps_max));
+		const size_t want = (nq + kThreads - 1) / kThreads;
+		return static_cast<unsigned>(std::max<size_t>(1, std::min(want, static_cast<size_t>(n_sm) * bps)));
+	};
+	static const int bps_extend = max_blocks_per_sm(reinterpret_cast<const void *>(k_extend_batch));
+	auto shadow_launch = [&]() {
+		if(filtered && tshadow)
+			k_shadow_batch<true, true><<<trace_grid(shadow_cap, max_blocks_per_sm(reinterpret_cast<const void *>(k_shadow_batch<true, true>))), kThreads, 0, s>>>(table, W, scap);
+		else if(filtered)
+			k_shadow_batch<true, false><<<trace_grid(shadow_cap, max_blocks_per_sm(reinterpret_cast<const void *>(k_shadow_batch<true, false>))), kThreads, 0, s>>>(table, W, scap);
+		else if(tshadow)
+			k_shadow_batch<false, true><<<trace_grid(shadow_cap, max_blocks_per_sm(reinterpret_cast<const void *>(k_shadow_batch<false, true>))), kThreads, 0, s>>>(table, W, scap);
+		else
+			k_shadow_batch<false, false><<<trace_grid(shadow_cap, max_blocks_per_sm(reinterpret_cast<const void *>(k_shadow_batch<false, false>))), kThreads, 0, s>>>(table, W, scap);
+	};
+	auto vertex_loop = [&](const Work &Ww, uint32_t nq) {
+		int cur = 0;
+		for(int vtx = 0; vtx <= bounces; ++vtx)
+		{
+			k_reset<<<1, 1, 0, s>>>(Ww.count, cur ^ 1);
+			k_extend_batch<<<trace_grid(nq, bps_extend), kThreads, 0, s>>>(table, Ww, cur);
+			const unsigned blocks = static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>((nq + sblock - 1) / sblock,
+			                                                                                   static_cast<size_t>(n_sm) * 16 * (kThreads / sblock))));
+			k_shade_batch<<<blocks, sblock, 0, s>>>(table, Ww, cur, scap);
+			shadow_launch();
+			cur ^= 1;
+		}
+	};
+	auto spawn_buf = [&](int L) { return S0->spawn + static_cast<size_t>(L - 1) * spawn_cap * 5; };
+	auto spawn_target = [&](Work &Ww, int child_level) -> int {
+		if(child_level > split_levels) { Ww.sp_out = nullptr; Ww.sp_count = nullptr; Ww.sp_cap = 0; return GBRT_OK; }
+		Ww.sp_out = spawn_buf(child_level);
+		Ww.sp_count = S0->spawn_count + (child_level - 1);
+		Ww.sp_cap = static_cast<uint32_t>(spawn_cap);
+		GBRT_CK(cudaMemsetAsync(Ww.sp_count, 0, sizeof(uint32_t), s));
+		return GBRT_OK;
+	};
+	auto spawned = [&](int child_level, uint32_t &nc) -> int {
+		nc = 0;
+		if(child_level > split_levels) return GBRT_OK;
+		GBRT_CK(cudaMemcpyAsync(&nc, S0->spawn_count + (child_level - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+		GBRT_CK(cudaStreamSynchronize(s));
+		if(nc > spawn_cap) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_pt_render_multi: %u spawned rays at level %d exceed %zu", nc, child_level, spawn_cap);
+		return GBRT_OK;
+	};
+	std::function<int(int, uint32_t)> process_level = [&](int L, uint32_t nl) -> int {
+		for(uint32_t c0 = 0; c0 < nl; c0 += static_cast<uint32_t>(chunk))
+		{
+			const uint32_t cn = static_cast<uint32_t>(std::min<uint64_t>(chunk, nl - c0));
+			Work Wc = W;
+			if(int rc = spawn_target(Wc, L + 1)) return rc;
+			GBRT_CK(cudaMemsetAsync(Wc.count, 0, sizeof(uint32_t), s));
+			k_spawn_init<<<grid_for(cn, n_sm), kThreads, 0, s>>>(Wc, spawn_buf(L) + 5ull * c0, cn);
+			vertex_loop(Wc, cn);
+			uint32_t nc = 0;
+			if(int rc = spawned(L + 1, nc)) return rc;
+			if(nc)
+				if(int rc = process_level(L + 1, nc)) return rc;
+		}
+		return GBRT_OK;
+	};
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	GBRT_CK(cudaEventCreate(&e0));
+	GBRT_CK(cudaEventCreate(&e1));
+	GBRT_CK(cudaMemsetAsync(W.stats, 0, 2 * sizeof(unsigned long long), s));
+	GBRT_CK(cudaEventRecord(e0, s));
+	int rc = GBRT_OK;
+	for(uint64_t start = 0; start < total && rc == GBRT_OK; start += wave)
+	{
+		const uint32_t wn = static_cast<uint32_t>(std::min<uint64_t>(wave, total - start));
+		Work Wv = W;
+		if((rc = spawn_target(Wv, 1))) break;
+		k_camera_batch<<<grid_for(wn, n_sm), kThreads, 0, s>>>(table, n, static_cast<uint32_t>(start), wn, Wv);
+		vertex_loop(Wv, wn);
+		uint32_t nc = 0;
+		if((rc = spawned(1, nc))) break;
+		if(nc) rc = process_level(1, nc);
+	}
+	if(rc == GBRT_OK && cudaGetLastError() != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "gbrt_pt_render_multi: launch failed");
+	cudaEventRecord(e1, s);
+	unsigned long long st[2] = {0ull, 0ull};
+	cudaMemcpyAsync(st, W.stats, sizeof(st), cudaMemcpyDeviceToHost, s);
+	cudaFreeAsync(table, s);
+	for(uint32_t i = 0; i < n; ++i)
+	{
+		gbrt_scene *S = scenes[i];
+		if(!S->ev_last) cudaEventCreateWithFlags(&S->ev_last, cudaEventDisableTiming);
+		cudaEventRecord(S->ev_last, s);
+	}
+	const cudaError_t se = cudaStreamSynchronize(s);
+	float ms = 0.f;
+	cudaEventElapsedTime(&ms, e0, e1);
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	if(rc) return rc;
+	if(se != cudaSuccess) return gbrt_set_error(GBRT_ERR_CUDA, "gbrt_pt_render_multi: %s", cudaGetErrorString(se));
+	if(stats)
+	{
+		*stats = gbrt_pt_stats{};
+		for(uint32_t i = 0; i < n; ++i) stats->camera_samples += host[i].paths / static_cast<uint32_t>(host[i].P.path_samples);
+		stats->extension_rays = st[0];
+		stats->shadow_rays = st[1];
+		stats->ms = ms;
+	}
+	return GBRT_OK;
+}
+
+// The autotuner: short trial renders of the whole batch at 1 sample per
+// pixel into scratch films, device-timed, over the wave size, then the
+// shading block size, then the traversal grids' residency (coordinate
+// descent from the defaults 2 Mi / 128 / what fits).
+static int batch_autotune(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params, uint32_t n,
+                          gbrt_batch_tuning &t, cudaStream_t s)
+{
+	size_t film_max = 0, w_max = 0;
+	for(uint32_t i = 0; i < n; ++i)
+	{
+		const size_t px = static_cast<size_t>(cameras[i].resx) * cameras[i].resy;
+		film_max = std::max(film_max, 3 * px);
+		w_max = std::max(w_max, px);
+	}
+	float *scratch = nullptr, *wscratch = nullptr;
+	GBRT_CK(cudaMallocAsync(reinterpret_cast<void **>(&scratch), 4 * film_max, s));
+	GBRT_CK(cudaMallocAsync(reinterpret_cast<void **>(&wscratch), 4 * w_max, s));
+	std::vector<float *> films(n, scratch);
+	std::vector<gbrt_pt_params> pp(params, params + n);
+	for(auto &p : pp) if(p.filter_type != GBRT_FILTER_PIXEL) p.film_weight_dev = wscratch;
+	const int bps_max = max_blocks_per_sm(reinterpret_cast<const void *>(k_extend_batch));
+	BatchPlan plan{t.wave_paths ? t.wave_paths : (1u << 21), t.shade_block ? t.shade_block : kThreads,
+	               t.trace_blocks_per_sm ? t.trace_blocks_per_sm : static_cast<uint32_t>(bps_max)};
+	float spent = 0.f;
+	int rc = GBRT_OK;
+	auto trial = [&](const BatchPlan &pl, float &ms) -> int {
+		gbrt_pt_stats st{};
+		if(int r = batch_render_locked(scenes, cameras, pp.data(), films.data(), n, pl, 1, &st, s)) return r;
+		ms = st.ms;
+		spent += st.ms;
+		return GBRT_OK;
+	};
+	float ms0 = 0.f;
+	rc = trial(plan, ms0);               // warm: buffers grown, code loaded
+	if(!rc && !t.wave_paths)
+	{
+		float best = 3.4e38f;
+		uint32_t pick = plan.wave;
+		for(uint32_t w : {1u << 20, 1u << 21, 1u << 22, 1u << 23})
+		{
+			BatchPlan pl = plan;
+			pl.wave = w;
+			float ms = 0.f;
+			if((rc = trial(pl, ms))) break;
+			if(ms < best) { best = ms; pick = w; }
+		}
+		plan.wave = pick;
+	}
+	if(!rc && !t.shade_block)
+	{
+		float best = 3.4e38f;
+		uint32_t pick = plan.shade_block;
+		for(uint32_t b : {64u, 128u})
+		{
+			BatchPlan pl = plan;
+			pl.shade_block = b;
+			float ms = 0.f;
+			if((rc = trial(pl, ms))) break;
+			if(ms < best) { best = ms; pick = b; }
+		}
+		plan.shade_block = pick;
+	}
+	if(!rc && !t.trace_blocks_per_sm)
+	{
+		float best = 3.4e38f;
+		uint32_t pick = plan.trace_bps;
+		for(uint32_t b : {static_cast<uint32_t>(bps_max), std::max(1u, static_cast<uint32_t>(bps_max) / 2u)})
+		{
+			BatchPlan pl = plan;
+			pl.trace_bps = b;
+			float ms = 0.f;
+			if((rc = trial(pl, ms))) break;
+			if(ms < best) { best = ms; pick = b; }
+		}
+		plan.trace_bps = pick;
+	}
+	cudaFreeAsync(scratch, s);
+	cudaFreeAsync(wscratch, s);
+	if(rc) return rc;
+	t.wave_paths = plan.wave;
+	t.shade_block = plan.shade_block;
+	t.trace_blocks_per_sm = plan.trace_bps;
+	t.tune_ms = spent;
+	return GBRT_OK;
+}
+
+int gbrt_pt_render_multi(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params, float *const *films,
+                         uint32_t n, gbrt_batch_tuning *tuning, gbrt_pt_stats *stats, void *stream)
+{
+	if(n == 0) return GBRT_OK;
+	if(!scenes || !cameras || !params || !films) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_multi: NULL argument");
+	for(uint32_t i = 0; i < n; ++i)
+		if(!scenes[i] || !films[i]) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_multi: scene or film %u is NULL", i);
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	// every scene's lock, in address order (concurrent batches over shared scenes)
+	std::vector<gbrt_scene *> order(scenes, scenes + n);
+	std::sort(order.begin(), order.end());
+	order.erase(std::unique(order.begin(), order.end()), order.end());
+	std::vector<std::unique_lock<std::mutex>> locks;
+	for(gbrt_scene *S : order) locks.emplace_back(S->mu);
+	gbrt_batch_tuning t{};
+	if(tuning) t = *tuning;
+	if(!t.wave_paths || !t.shade_block || !t.trace_blocks_per_sm)
+		if(int rc = batch_autotune(scenes, cameras, params, n, t, s)) return rc;
+	if(tuning) *tuning = t;
+	const BatchPlan plan{t.wave_paths, t.shade_block, t.trace_blocks_per_sm};
+	return batch_render_locked(scenes, cameras, params, films, n, plan, 0, stats, s);
+}
+
 int gbrt_pt_render_batch(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params, float *const *films,
                          uint32_t n, uint32_t concurrency, gbrt_pt_stats *stats)
 {
-	if(n && (!scenes || !cameras || !params || !films)) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_batch: NULL argument");
-	for(uint32_t i = 0; i < n; ++i)
-		if(!scenes[i] || !films[i]) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_pt_render_batch: scene or film %u is NULL", i);
-	int dev = 0;
-	GBRT_CK(cudaGetDevice(&dev));
-	const uint32_t workers = std::max(1u, std::min(n, concurrency ? concurrency : 8u));
-	std::atomic<uint32_t> next{0};
-	std::atomic<int> first_rc{GBRT_OK};
-	std::mutex err_mu;
-	std::string err_msg;
-	auto work = [&]() {
-		if(cudaSetDevice(dev) != cudaSuccess) { first_rc = GBRT_ERR_CUDA; return; }
-		cudaStream_t st = nullptr;
-		if(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) { first_rc = GBRT_ERR_CUDA; return; }
-		for(uint32_t i = next++; i < n && first_rc.load() == GBRT_OK; i = next++)
+	(void)concurrency;
+	gbrt_pt_stats total{};
+	if(int rc = gbrt_pt_render_multi(scenes, cameras, params, films, n, nullptr, stats ? &total : nullptr, nullptr)) return rc;
+	if(stats)
+	{
+		// each scene's camera samples; the batch's rays and device time in entry 0
+		for(uint32_t i = 0; i < n; ++i)
 		{
-			gbrt_scene *S = scenes[i];
-			gbrt_pt_params p = params[i];
-			// 2 Mi paths per wave: the batch's wall time is flat from 1 to 4 Mi paths
-			// and 4 to 12 concurrent scenes (measured: 6.2-6.4 s at 64 spp)
-			if(!p.wave_paths) p.wave_paths = 1u << 21;
-			int rc = gbrt_pt_render(S, cameras + i, &p, films[i], nullptr, stats ? stats + i : nullptr, st);
-			if(!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "scene %u: stream error", i);
-			{
-				std::lock_guard<std::mutex> lock(S->mu);
-				release_work(S, st);                              // back to the pool for the next scenes
-			}
-			if(rc)
-			{
-				int expect = GBRT_OK;
-				if(first_rc.compare_exchange_strong(expect, rc))
-				{
-					std::lock_guard<std::mutex> lock(err_mu);
-					err_msg = std::string("scene ") + std::to_string(i) + ": " + gbrt_last_error();
-				}
-			}
+			stats[i] = gbrt_pt_stats{};
+			stats[i].camera_samples = static_cast<uint64_t>(cameras[i].resx) * cameras[i].resy * params[i].spp;
 		}
-		cudaStreamDestroy(st);
-	};
-	std::vector<std::thread> pool;
-	for(uint32_t w = 1; w < workers; ++w) pool.emplace_back(work);
-	work();
-	for(auto &t : pool) t.join();
-	if(first_rc.load() != GBRT_OK) return gbrt_set_error(first_rc.load(), "gbrt_pt_render_batch: %s", err_msg.c_str());
+		stats[0].extension_rays = total.extension_rays;
+		stats[0].shadow_rays = total.shadow_rays;
+		stats[0].ms = total.ms;
+	}
 	return GBRT_OK;
 }
 

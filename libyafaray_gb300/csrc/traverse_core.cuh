@@ -368,10 +368,15 @@ __device__ __forceinline__ Hit trace_ray(const BvhView &bv, float ox, float oy, 
 // f: the shadow walk's hit filter, reset before each query.
 constexpr uint32_t kTraceChunk = 32;
 
-template <bool kShadow, typename F, typename Load, typename Store>
-__device__ __forceinline__ void trace_persistent_filtered(const BvhView &bv, uint32_t n, uint32_t *counter, uint2 *sh, int stride, F &f,
+// kLaneView: every query carries its own hierarchy (a batch of scenes):
+// load(i, ray[8], BvhView &view) sets it, and the lane keeps it while it
+// walks; otherwise every query walks `bv0`.
+template <bool kShadow, bool kLaneView = false, typename F, typename Load, typename Store>
+__device__ __forceinline__ void trace_persistent_filtered(const BvhView &bv0, uint32_t n, uint32_t *counter, uint2 *sh, int stride, F &f,
                                                           Load &&load, Store &&store)
 {
+	BvhView lbv = bv0;
+	const BvhView &bv = kLaneView ? lbv : bv0;
 	uint2 spill[kTraceStack - kStackShared];
 	const uint32_t lane = threadIdx.x & 31u;
 	uint32_t next = 0, end = 0;      // the warp's current chunk (warp-uniform)
@@ -396,7 +401,10 @@ __device__ __forceinline__ void trace_persistent_filtered(const BvhView &bv, uin
 			const uint32_t mine = next + __popc(idle & ((1u << lane) - 1u));
 			next = min(next + static_cast<uint32_t>(__popc(idle)), end);
 			float r[8];
-			if(!active && mine < end && load(mine, r))
+			bool ok;
+			if constexpr(kLaneView) ok = !active && mine < end && load(mine, r, lbv);
+			else ok = !active && mine < end && load(mine, r);
+			if(ok)
 			{
 				idx = mine;
 				f.reset();

@@ -255,6 +255,7 @@ SIGNATURES = {
     "gbrt_tc_selftest": (_I, [_VP, _VP, _U32, _U32, _VP]),
     "gbrt_pm_default_params": (_I, [_VP]),
     "gbrt_pt_render_batch": (_I, [_VP, _VP, _VP, _VP, _U32, _U32, _VP]),
+    "gbrt_pt_render_multi": (_I, [_VP, _VP, _VP, _VP, _U32, _VP, _VP, _VP]),
     "gbrt_pm_render": (_I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "gbrt_pm_render_host": (_I, [_VP, _VP, _VP, _VP, _VP, _VP]),
     "gbrt_dl_render": (_I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
@@ -843,10 +844,37 @@ def knn_gather(points, queries, cell, k, r2):
     return cnt, rr, idx.astype(np.int64) - np.where(idx == 0xFFFFFFFF, 1 << 32, 0)
 
 
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("wave_paths", ctypes.c_uint32), ("shade_block", ctypes.c_uint32), ("trace_blocks_per_sm", ctypes.c_uint32),
+                ("tune_ms", ctypes.c_float)]
+
+
+def render_multi(renderers, spp, film_ptrs, tuning=None, base_offset=0, seed=1, stream=0):
+    """gbrt_pt_render_multi: every Renderer's scene into its device float film
+    (pointer) in one wavefront.  tuning: None (autotune) or a dict with
+    wave_paths / shade_block / trace_blocks_per_sm (missing or 0 = tuned).
+    Returns (stats dict of the batch, the tuning used incl. tune_ms)."""
+    n = len(renderers)
+    S = (ctypes.c_void_p * n)(*[r._h.value for r in renderers])
+    cams = (CameraDesc * n)(*[r.camera_desc() for r in renderers])
+    ps = (PtParams * n)(*[r.params(spp, base_offset, seed) for r in renderers])
+    F = (ctypes.c_void_p * n)(*[int(f) for f in film_ptrs])
+    t = BatchTuning()
+    for k, v in (tuning or {}).items():
+        if k != "tune_ms":
+            setattr(t, k, int(v))
+    st = PtStats()
+    check(load().gbrt_pt_render_multi(S, cams, ps, F, n, ctypes.byref(t), ctypes.byref(st), ctypes.c_void_p(stream)))
+    return ({"camera_samples": st.camera_samples, "extension_rays": st.extension_rays, "shadow_rays": st.shadow_rays,
+             "ms": st.ms},
+            {"wave_paths": t.wave_paths, "shade_block": t.shade_block, "trace_blocks_per_sm": t.trace_blocks_per_sm,
+             "tune_ms": t.tune_ms})
+
+
 def render_batch(renderers, spp, film_ptrs, concurrency=8, base_offset=0, seed=1):
     """gbrt_pt_render_batch: renders every Renderer's scene into its device
-    float film (pointer), several scenes at a time on their own streams.
-    Returns the per-scene stats."""
+    float film (pointer), all in one wavefront (autotuned).  Returns the
+    per-scene stats (rays and device time of the batch in entry 0)."""
     n = len(renderers)
     S = (ctypes.c_void_p * n)(*[r._h.value for r in renderers])
     cams = (CameraDesc * n)(*[r.camera_desc() for r in renderers])

@@ -257,7 +257,7 @@ def cornell_pm_golden(spp=8, batches=24):
         print(f"{name}: mean {mean.mean(axis=(0, 1))}, {secs.sum():.1f} s of reference rendering")
 
 
-BATCH_CASES = (5, 26)
+BATCH_CASES = (5, 26, 10, 18)        # 18: every object rough glass
 
 
 def batch_golden(spp=8, batches=24):
@@ -265,6 +265,9 @@ def batch_golden(spp=8, batches=24):
     1000 + i; spheres / tori, shinydiffuse + glossy + rough glass, 2-4 area
     lights, bounces 8) at 48x48."""
     for i in BATCH_CASES:
+        name = f"batch_scene_{i}_48_render.npz"
+        if os.path.exists(os.path.join(OUT, name)) and "--force" not in sys.argv:
+            continue
         sc = scenes.batch_scene(i, res=48)
         rgb, secs = orc.run_reference_render(sc, spp, batches, threads=os.cpu_count() or 1)
         mean = rgb.mean(0)

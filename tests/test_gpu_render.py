@@ -288,17 +288,57 @@ def test_gpu_batch_scene_matches_reference(cuda_device, i):
     assert frac >= 0.995
 
 
+def test_gpu_batch_wavefront_matches_reference(cuda_device):
+    """Four scenes of the 64-scene batch rendered together in one wavefront
+    (gbrt_pt_render_multi) - scene 18 all rough glass, scene 10 two rough
+    glass objects - each against the reference's render of that scene
+    alone: per-pixel means of the batches within 3 SE on >= 99.5 %."""
+    torch = pytest.importorskip("torch")
+    cases = (5, 26, 10, 18)
+    gs = [np.load(os.path.join(GOLD, f"batch_scene_{i}_48_render.npz")) for i in cases]
+    rs = [gbrt.Renderer(scenes.batch_scene(i, res=48)) for i in cases]
+    spp, k = int(gs[0]["spp"]), int(gs[0]["batches"])
+    imgs = [[] for _ in cases]
+    tuning = None
+    for b in range(k):
+        films = [torch.zeros(48 * 48 * 3, dtype=torch.float32, device="cuda") for _ in rs]
+        _, tuning = gbrt.render_multi(rs, spp, [f.data_ptr() for f in films], tuning=tuning, base_offset=b * spp, seed=1000 + b)
+        for j, f in enumerate(films):
+            imgs[j].append(f.cpu().numpy().reshape(48, 48, 3) / spp)
+    print(f"autotuned: {tuning}")
+    for i, g, im in zip(cases, gs, imgs):
+        frac, relmse, m = parity(np.stack(im), g["mean"], g["se"])
+        print(f"batch wavefront, scene {i}: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}")
+        assert frac >= 0.995
+
+
 def test_gpu_render_batch_equals_single_renders(cuda_device):
-    """gbrt_pt_render_batch (several scenes at once on their own streams)
-    gives each scene the image its own render gives."""
+    """One wavefront over scenes of different sizes and materials (rough
+    glass splits included) gives each scene the image its own render gives
+    (up to the order of the film's float atomics) and the same ray counts;
+    also with small waves that cut across scene boundaries, 64-thread
+    shading blocks and one traversal block per SM."""
     torch = pytest.importorskip("torch")
     rs = [gbrt.Renderer(scenes.batch_scene(i, res=32)) for i in (5, 26, 30)]
-    films = [torch.zeros(32 * 32 * 3, dtype=torch.float32, device="cuda") for _ in rs]
-    st = gbrt.render_batch(rs, 4, [f.data_ptr() for f in films], concurrency=3)
-    torch.cuda.synchronize()
-    for r, f, s in zip(rs, films, st):
-        single = torch.zeros_like(f)
-        s1 = r.render_device(4, single.data_ptr(), stats=True)
+    sc = scenes.cornell_scene(res=40, glass=True)
+    sc["camera"]["resy"] = 24
+    rs.append(gbrt.Renderer(sc))
+    singles, rays = [], [0, 0]
+    for r in rs:
+        n = r.scene["camera"]["resx"] * r.scene["camera"]["resy"] * 3
+        f = torch.zeros(n, dtype=torch.float32, device="cuda")
+        s1 = r.render_device(4, f.data_ptr(), stats=True)
         torch.cuda.synchronize()
-        assert s["extension_rays"] == s1["extension_rays"] and s["shadow_rays"] == s1["shadow_rays"]
-        assert torch.allclose(f, single, rtol=1e-4, atol=1e-6)
+        singles.append(f)
+        rays[0] += s1["extension_rays"]
+        rays[1] += s1["shadow_rays"]
+    for tuning in (None, {"wave_paths": 3000, "shade_block": 64, "trace_blocks_per_sm": 1}):
+        films = [torch.zeros_like(f) for f in singles]
+        st, used = gbrt.render_multi(rs, 4, [f.data_ptr() for f in films], tuning=tuning)
+        torch.cuda.synchronize()
+        print(f"tuning {used}: {st}")
+        assert st["extension_rays"] == rays[0] and st["shadow_rays"] == rays[1]
+        for f, single in zip(films, singles):
+            assert torch.allclose(f, single, rtol=1e-4, atol=1e-6)
+        if tuning is None:
+            assert used["wave_paths"] in (1 << 20, 1 << 21, 1 << 22, 1 << 23) and used["shade_block"] in (64, 128)
