@@ -381,7 +381,7 @@ def render_sections(args):
         "scene_setup_s": setup_s, "batch_wall_s": batch_s, "batch_device_ms": st["ms"], "mrays_s": rays / batch_s / 1e6,
         "msamples_s": samples / batch_s / 1e6,
         "execution": "one wavefront over all 64 scenes (gbrt_pt_render_multi)",
-        "autotuned": {k: tuning[k] for k in ("wave_paths", "shade_block", "trace_blocks_per_sm")},
+        "autotuned": {k: tuning[k] for k in ("wave_paths", "shade_block", "trace_blocks_per_sm", "streams")},
         "autotune_wall_s": tune_wall_s, "autotune_device_ms": tuning["tune_ms"],
         "reference_cpu_note": "reference, extrapolated: 8 of the 64 scenes (every 8th) at 1 spp took 4.49 s on 8 x86 threads "
                               "(oracle/_ref render_dump, scene trees already built) -> about 2,300 s for 64 scenes x 64 spp"}

@@ -481,19 +481,23 @@ int gbrt_aa_flags(const float *film_dev, const float *weight_dev, int32_t resx, 
  * vertex level serves all of them (the per-scene render loop of
  * TiledIntegrator::render, integrator_tiled.cc:222-251, for many scenes at
  * once).  pathtracing only: no guide and no photon caustics; the scenes must
- * agree on film filtering and transparent shadows.  The first scene's work
- * buffers serve the batch.  Synchronises `stream`.
+ * agree on film filtering and transparent shadows.  Several waves may be in
+ * flight at once, each on its own stream in the work buffers of one of the
+ * batch's scenes (released after the call).  Synchronises `stream`.
  *
  * tuning: NULL, or in/out: a zero field is chosen by the autotuner (short
  * device-timed trial renders of the whole batch at 1 sample per pixel into
- * scratch films: the wave size, then the shading block size, then the
- * residency of the persistent traversal grids), which writes back what it
- * chose and the device time it spent; pass the result back to skip tuning.
+ * scratch films: the waves in flight, the wave size, the shading block
+ * size, then the residency of the persistent traversal grids), which writes
+ * back what it chose and the device time it spent; pass the result back to
+ * skip tuning.
  * stats: NULL or one entry with the batch's totals. */
 typedef struct gbrt_batch_tuning {
 	uint32_t wave_paths;            /* paths per wave (the spawn buffers may cap it) */
 	uint32_t shade_block;           /* threads per block of the shading kernel, 32 .. 128 */
 	uint32_t trace_blocks_per_sm;   /* resident blocks per SM of the traversal grids */
+	uint32_t streams;               /* waves in flight, each on its own stream (and host thread),
+	                                   in the buffers of scenes 0 .. streams - 1 */
 	float tune_ms;                  /* out: device time of the trial renders */
 } gbrt_batch_tuning;
 int gbrt_pt_render_multi(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params,

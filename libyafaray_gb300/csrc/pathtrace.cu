@@ -246,11 +246,18 @@ __device__ __forceinline__ void coords_system(const float n[3], float u[3], floa
 }
 
 // sample::cosHemisphere (include/sampler/sample.h:43-52) with FAST_TRIG.
+// kExact: the accurate sine and cosine, so the directions follow the cosine
+// density exactly (guided vertices: the one-sample MIS weights need the true
+// density of the BSDF technique; the FAST_TRIG parabola bends the azimuth by
+// up to about 1 %).
+template <bool kExact = false>
 __device__ __forceinline__ void cos_hemisphere(const float n[3], const float u[3], const float v[3], float s1, float s2, float out[3])
 {
 	if(s1 >= 1.f) { out[0] = n[0]; out[1] = n[1]; out[2] = n[2]; return; }
 	const float z2 = xm(s2, 6.28318530717958647692f);
-	const float cz = gbrt::fast_cos(z2), sz = gbrt::fast_sin(z2);
+	float cz, sz;
+	if constexpr(kExact) sincosf(z2, &sz, &cz);
+	else { cz = gbrt::fast_cos(z2); sz = gbrt::fast_sin(z2); }
 	const float a = sqrtf(xs(1.f, s1)), b = sqrtf(s1);
 	for(int k = 0; k < 3; ++k) out[k] = xa(xm(xa(xm(u[k], cz), xm(v[k], sz)), a), xm(n[k], b));
 }
@@ -348,6 +355,9 @@ __device__ __forceinline__ float glossy_pdf(const Surface &s, const float wo[3],
 }
 
 // GlossyMaterial::sample (material_glossy.cc:245-402), isotropic Blinn.
+// kExact: the directions drawn with the accurate pow / sine / cosine (see
+// cos_hemisphere); the sample weight is the same function of the direction.
+template <bool kExact = false>
 __device__ __forceinline__ void glossy_sample(const Surface &s, const float wo[3], float s1, float s2, uint32_t flags,
                                               float wi[3], float col[3], float &w, float &pdf, uint32_t &sampled)
 {
@@ -370,7 +380,7 @@ __device__ __forceinline__ void glossy_sample(const Surface &s, const float wo[3
 		if(s1 < s_pd)
 		{
 			s1 = __fdiv_rn(s1, s_pd);
-			cos_hemisphere(n, s.u, s.v, s1, s2, wi);
+			cos_hemisphere<kExact>(n, s.u, s.v, s1, s2, wi);
 			if(xm(dot3(s.ng, wi), cos_ng_wo) < 0.f) { w = 0.f; return; }
 			wi_n = fabsf(dot3(wi, n));
 			pdf = wi_n;
@@ -395,10 +405,14 @@ __device__ __forceinline__ void glossy_sample(const Surface &s, const float wo[3
 	if(use_glossy)
 	{
 		// microfacet::blinnSample (material_utils_microfacet.h:96-104)
-		const float cos_theta = gbrt::fast_pow(xs(1.f, s2), __fdiv_rn(1.f, xa(m.exponent, 1.f)));
+		const float e1 = __fdiv_rn(1.f, xa(m.exponent, 1.f));
+		const float cos_theta = kExact ? powf(xs(1.f, s2), e1) : gbrt::fast_pow(xs(1.f, s2), e1);
 		const float sin_theta = sqrtf(xs(1.f, xm(cos_theta, cos_theta)));
 		const float phi = xm(s1, 6.28318530717958647692f);
-		const float hs[3] = {xm(sin_theta, gbrt::fast_cos(phi)), xm(sin_theta, gbrt::fast_sin(phi)), cos_theta};
+		float cphi, sphi;
+		if constexpr(kExact) sincosf(phi, &sphi, &cphi);
+		else { cphi = gbrt::fast_cos(phi); sphi = gbrt::fast_sin(phi); }
+		const float hs[3] = {xm(sin_theta, cphi), xm(sin_theta, sphi), cos_theta};
 		float h[3];
 		for(int k = 0; k < 3; ++k) h[k] = xa(xa(xm(hs[0], s.u[k]), xm(hs[1], s.v[k])), xm(hs[2], n[k]));
 		float cos_wo_h = dot3(wo, h);
@@ -1174,6 +1188,7 @@ __device__ __forceinline__ float shiny_pdf(const Surface &s, const float wo[3], 
 	return (fabsf(dot3(wi, n)) * c) / c;
 }
 
+template <bool kExact = false>
 __device__ __forceinline__ bool shiny_sample(const Surface &s, const float wo[3], float s1, float s2, uint32_t req, float wi[3], float col[3],
                                              float &w, float &pdf, uint32_t &sampled)
 {
@@ -1183,7 +1198,7 @@ __device__ __forceinline__ bool shiny_sample(const Surface &s, const float wo[3]
 	const float width = c * (1.f / c);
 	float n[3];
 	face_forward(s, wo, n);
-	cos_hemisphere(n, s.u, s.v, s1 / width, s2, wi);
+	cos_hemisphere<kExact>(n, s.u, s.v, s1 / width, s2, wi);
 	col[0] = col[1] = col[2] = 0.f;
 	if(xm(dot3(s.ng, wo), dot3(s.ng, wi)) > 0.f) for(int k = 0; k < 3; ++k) col[k] = c * s.dcol[k];
 	pdf = fabsf(dot3(wi, n)) * width;
@@ -1246,6 +1261,7 @@ __device__ __forceinline__ float mat_pdf(const Surface &s, const float wo[3], co
 // Material::sample dispatch; ShinyDiffuseMaterial::sample diffuse reflection
 // branch (material_shiny_diffuse.cc:346-440); light_mat returns pdf 0
 // (material_light.cc:75-80).
+template <bool kExact = false>
 __device__ __forceinline__ bool mat_sample(const Surface &s, const float wo[3], float s1, float s2, uint32_t req_flags,
                                            float wi[3], float col[3], float &w, float &pdf, uint32_t &sampled)
 {
@@ -1253,13 +1269,13 @@ __device__ __forceinline__ bool mat_sample(const Surface &s, const float wo[3], 
 	w = 0.f; pdf = 0.f; sampled = 0u;
 	if(s.m->type == GBRT_MAT_GLOSSY)
 	{
-		glossy_sample(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
+		glossy_sample<kExact>(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
 		return sampled != 0u;
 	}
 	if(s.m->type == GBRT_MAT_GLASS) return glass_sample(s, wo, s1, req_flags, wi, col, w, pdf, sampled);
 	if(s.m->type == GBRT_MAT_ROUGH_GLASS) return rough_sample(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
 	if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return false;
-	return shiny_sample(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
+	return shiny_sample<kExact>(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
 }
 
 // Sample colour x weight that Material::sample would return for a given
@@ -2119,7 +2135,9 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 					}
 					else
 					{
-						mat_sample(s, wo, s1, s2, req, wi, scol, w, pdf, sflags);
+						// the BSDF technique drawn exactly, so its density is ptrue
+						mat_sample<true>(s, wo, s1, s2, req, wi, scol, w, pdf, sflags);
+						normalize3(wi);
 						for(int c = 0; c < 3; ++c) fw[c] = xm(scol[c], w);
 						ptrue = bsdf_true_pdf(s, wo, wi, req);
 					}
@@ -2188,14 +2206,14 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 	}
 }
 
-__global__ void __launch_bounds__(kThreads, 1) k_shade(SceneDev sc, Params P, Work W, int cur, uint32_t shadow_cap, float *film,
+__global__ void __launch_bounds__(kThreads, 4) k_shade(SceneDev sc, Params P, Work W, int cur, uint32_t shadow_cap, float *film,
                                                     double *film64)
 {
 	shade_queue(OneScene{sc, P, film, film64}, W, cur, shadow_cap);
 }
 
 // The same for a batch of scenes: every path's scene from the table.
-__global__ void __launch_bounds__(kThreads, 1) k_shade_batch(const BatchScene *__restrict__ bs, Work W, int cur, uint32_t shadow_cap)
+__global__ void __launch_bounds__(kThreads, 4) k_shade_batch(const BatchScene *__restrict__ bs, Work W, int cur, uint32_t shadow_cap)
 {
 	shade_queue(SceneTable{bs}, W, cur, shadow_cap);
 }
@@ -4972,6 +4990,7 @@ struct BatchPlan {
 	uint32_t wave;              // paths per wave
 	uint32_t shade_block;       // threads per block of k_shade_batch
 	uint32_t trace_bps;         // resident blocks per SM of the persistent traversal grids
+	uint32_t streams;           // waves in flight: one stream (and host thread) each
 };
 
 // Resident blocks per SM of a persistent kernel at kThreads threads.
@@ -4981,6 +5000,9 @@ static int max_blocks_per_sm(const void *kernel)
 	if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, kThreads, 0) != cudaSuccess || bps < 1) bps = 1;
 	return bps;
 }
+
+// Spawn records a batch wave may leave per ray level (80 bytes each).
+constexpr uint64_t kBatchSpawnCap = 1ull << 24;
 
 static int batch_render_locked(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params,
                                float *const *films, uint32_t n, const BatchPlan &plan, int spp_override, gbrt_pt_stats *stats,
@@ -5047,110 +5069,153 @@ static int batch_render_locked(gbrt_scene *const *scenes, const gbrt_camera_desc
 		max_shadow = std::max(max_shadow, std::max(all, one));
 	}
 	// waves are cut so the spawned calls of one wave always fit
-	constexpr uint64_t kSpawnCap = 1ull << 24;
 	uint64_t wave = std::min<uint64_t>(total, std::max<uint32_t>(plan.wave, 256u));
 	size_t spawn_cap = 0;
 	uint64_t chunk = wave;
 	if(split_levels > 0)
 	{
-		const uint64_t roots = std::max<uint64_t>(1, kSpawnCap / fanout - 2);
+		const uint64_t roots = std::max<uint64_t>(1, kBatchSpawnCap / fanout - 2);
 		wave = std::max<uint64_t>(1, std::min<uint64_t>(wave, roots));
 		spawn_cap = static_cast<size_t>((wave + 2) * fanout);
 		chunk = std::max<uint64_t>(1, std::min<uint64_t>(wave, (spawn_cap / fanout - 1) * n_min));
-		if(int rc = alloc_spawn(S0, spawn_cap, split_levels, s)) return rc;
 	}
 	const size_t shadow_cap = std::max<size_t>(1, wave * max_shadow);
-	if(int rc = alloc_work(S0, wave, shadow_cap, 0, s)) return rc;
+	const uint64_t n_waves = (total + wave - 1) / wave;
+	// every stream works in its own scene's buffers (the scenes are locked)
+	const uint32_t n_streams = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>({plan.streams ? plan.streams : 1u, n, n_waves})));
 	BatchScene *table = nullptr;
 	GBRT_CK(cudaMallocAsync(reinterpret_cast<void **>(&table), sizeof(BatchScene) * n, s));
 	GBRT_CK(cudaMemcpyAsync(table, host.data(), sizeof(BatchScene) * n, cudaMemcpyHostToDevice, s));
-	Work W = S0->w;
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	GBRT_CK(cudaEventCreate(&e0));
+	GBRT_CK(cudaEventCreate(&e1));
+	GBRT_CK(cudaEventRecord(e0, s));
 	const int n_sm = S0->n_sm;
 	const uint32_t scap = static_cast<uint32_t>(shadow_cap);
 	const uint32_t sblock = std::max(32u, std::min<uint32_t>(kThreads, plan.shade_block & ~31u));
+	static const int bps_extend = max_blocks_per_sm(reinterpret_cast<const void *>(k_extend_batch));
+	static const int bps_shadow[4] = {max_blocks_per_sm(reinterpret_cast<const void *>(k_shadow_batch<false, false>)),
+	                                  max_blocks_per_sm(reinterpret_cast<const void *>(k_shadow_batch<false, true>)),
+	                                  max_blocks_per_sm(reinterpret_cast<const void *>(k_shadow_batch<true, false>)),
+	                                  max_blocks_per_sm(reinterpret_cast<const void *>(k_shadow_batch<true, true>))};
 	auto trace_grid = [&](size_t nq, int bps_max) {
 		const int bps = std::max(1, std::min<int>(bps_max, plan.trace_bps ? static_cast<int>(plan.trace_bps) : bps_max));
 		const size_t want = (nq + kThreads - 1) / kThreads;
 		return static_cast<unsigned>(std::max<size_t>(1, std::min(want, static_cast<size_t>(n_sm) * bps)));
 	};
-	static const int bps_extend = max_blocks_per_sm(reinterpret_cast<const void *>(k_extend_batch));
-	auto shadow_launch = [&]() {
-		if(filtered && tshadow)
-			k_shadow_batch<true, true><<<trace_grid(shadow_cap, max_blocks_per_sm(reinterpret_cast<const void *>(k_shadow_batch<true, true>))), kThreads, 0, s>>>(table, W, scap);
-		else if(filtered)
-			k_shadow_batch<true, false><<<trace_grid(shadow_cap, max_blocks_per_sm(reinterpret_cast<const void *>(k_shadow_batch<true, false>))), kThreads, 0, s>>>(table, W, scap);
-		else if(tshadow)
-			k_shadow_batch<false, true><<<trace_grid(shadow_cap, max_blocks_per_sm(reinterpret_cast<const void *>(k_shadow_batch<false, true>))), kThreads, 0, s>>>(table, W, scap);
-		else
-			k_shadow_batch<false, false><<<trace_grid(shadow_cap, max_blocks_per_sm(reinterpret_cast<const void *>(k_shadow_batch<false, false>))), kThreads, 0, s>>>(table, W, scap);
-	};
-	auto vertex_loop = [&](const Work &Ww, uint32_t nq) {
-		int cur = 0;
-		for(int vtx = 0; vtx <= bounces; ++vtx)
+	std::atomic<uint64_t> next_wave{0};
+	std::atomic<int> first_rc{GBRT_OK};
+	std::mutex err_mu;
+	std::string err_msg;
+	std::vector<unsigned long long> rays(2ull * n_streams, 0ull);
+	std::vector<cudaEvent_t> done(n_streams, nullptr);
+	auto fail = [&](int rc) {
+		int expect = GBRT_OK;
+		if(first_rc.compare_exchange_strong(expect, rc))
 		{
-			k_reset<<<1, 1, 0, s>>>(Ww.count, cur ^ 1);
-			k_extend_batch<<<trace_grid(nq, bps_extend), kThreads, 0, s>>>(table, Ww, cur);
-			const unsigned blocks = static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>((nq + sblock - 1) / sblock,
-			                                                                                   static_cast<size_t>(n_sm) * 16 * (kThreads / sblock))));
-			k_shade_batch<<<blocks, sblock, 0, s>>>(table, Ww, cur, scap);
-			shadow_launch();
-			cur ^= 1;
+			std::lock_guard<std::mutex> g(err_mu);
+			err_msg = gbrt_last_error();
 		}
+		return rc;
 	};
-	auto spawn_buf = [&](int L) { return S0->spawn + static_cast<size_t>(L - 1) * spawn_cap * 5; };
-	auto spawn_target = [&](Work &Ww, int child_level) -> int {
-		if(child_level > split_levels) { Ww.sp_out = nullptr; Ww.sp_count = nullptr; Ww.sp_cap = 0; return GBRT_OK; }
-		Ww.sp_out = spawn_buf(child_level);
-		Ww.sp_count = S0->spawn_count + (child_level - 1);
-		Ww.sp_cap = static_cast<uint32_t>(spawn_cap);
-		GBRT_CK(cudaMemsetAsync(Ww.sp_count, 0, sizeof(uint32_t), s));
-		return GBRT_OK;
-	};
-	auto spawned = [&](int child_level, uint32_t &nc) -> int {
-		nc = 0;
-		if(child_level > split_levels) return GBRT_OK;
-		GBRT_CK(cudaMemcpyAsync(&nc, S0->spawn_count + (child_level - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-		GBRT_CK(cudaStreamSynchronize(s));
-		if(nc > spawn_cap) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_pt_render_multi: %u spawned rays at level %d exceed %zu", nc, child_level, spawn_cap);
-		return GBRT_OK;
-	};
-	std::function<int(int, uint32_t)> process_level = [&](int L, uint32_t nl) -> int {
-		for(uint32_t c0 = 0; c0 < nl; c0 += static_cast<uint32_t>(chunk))
+	// one stream's share of the waves
+	auto worker = [&](uint32_t k) -> int {
+		if(cudaSetDevice(S0->device) != cudaSuccess) return fail(gbrt_set_error(GBRT_ERR_CUDA, "gbrt_pt_render_multi: cudaSetDevice"));
+		gbrt_scene *H = scenes[k];                 // the buffers this stream works in
+		cudaStream_t st = s;
+		if(k > 0 && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+			return fail(gbrt_set_error(GBRT_ERR_CUDA, "gbrt_pt_render_multi: stream creation"));
+		if(k > 0) cudaStreamWaitEvent(st, e0, 0);
+		int rc = GBRT_OK;
+		if(split_levels > 0) rc = alloc_spawn(H, spawn_cap, split_levels, st);
+		if(!rc) rc = alloc_work(H, wave, shadow_cap, 0, st);
+		Work W = H->w;
+		if(!rc && cudaMemsetAsync(W.stats, 0, 2 * sizeof(unsigned long long), st) != cudaSuccess)
+			rc = gbrt_set_error(GBRT_ERR_CUDA, "gbrt_pt_render_multi: memset");
+		auto vertex_loop = [&](const Work &Ww, uint32_t nq) {
+			int cur = 0;
+			for(int vtx = 0; vtx <= bounces; ++vtx)
+			{
+				k_reset<<<1, 1, 0, st>>>(Ww.count, cur ^ 1);
+				k_extend_batch<<<trace_grid(nq, bps_extend), kThreads, 0, st>>>(table, Ww, cur);
+				const unsigned blocks = static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>((nq + sblock - 1) / sblock,
+				                                                                                   static_cast<size_t>(n_sm) * 16 * (kThreads / sblock))));
+				k_shade_batch<<<blocks, sblock, 0, st>>>(table, Ww, cur, scap);
+				const unsigned sg = trace_grid(shadow_cap, bps_shadow[(filtered ? 2 : 0) + (tshadow ? 1 : 0)]);
+				if(filtered && tshadow) k_shadow_batch<true, true><<<sg, kThreads, 0, st>>>(table, Ww, scap);
+				else if(filtered) k_shadow_batch<true, false><<<sg, kThreads, 0, st>>>(table, Ww, scap);
+				else if(tshadow) k_shadow_batch<false, true><<<sg, kThreads, 0, st>>>(table, Ww, scap);
+				else k_shadow_batch<false, false><<<sg, kThreads, 0, st>>>(table, Ww, scap);
+				cur ^= 1;
+			}
+		};
+		auto spawn_buf = [&](int L) { return H->spawn + static_cast<size_t>(L - 1) * spawn_cap * 5; };
+		auto spawn_target = [&](Work &Ww, int child_level) -> int {
+			if(child_level > split_levels) { Ww.sp_out = nullptr; Ww.sp_count = nullptr; Ww.sp_cap = 0; return GBRT_OK; }
+			Ww.sp_out = spawn_buf(child_level);
+			Ww.sp_count = H->spawn_count + (child_level - 1);
+			Ww.sp_cap = static_cast<uint32_t>(spawn_cap);
+			GBRT_CK(cudaMemsetAsync(Ww.sp_count, 0, sizeof(uint32_t), st));
+			return GBRT_OK;
+		};
+		auto spawned = [&](int child_level, uint32_t &nc) -> int {
+			nc = 0;
+			if(child_level > split_levels) return GBRT_OK;
+			GBRT_CK(cudaMemcpyAsync(&nc, H->spawn_count + (child_level - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+			GBRT_CK(cudaStreamSynchronize(st));
+			if(nc > spawn_cap)
+				return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_pt_render_multi: %u spawned rays at level %d exceed %zu", nc, child_level, spawn_cap);
+			return GBRT_OK;
+		};
+		std::function<int(int, uint32_t)> process_level = [&](int L, uint32_t nl) -> int {
+			for(uint32_t c0 = 0; c0 < nl; c0 += static_cast<uint32_t>(chunk))
+			{
+				const uint32_t cn = static_cast<uint32_t>(std::min<uint64_t>(chunk, nl - c0));
+				Work Wc = W;
+				if(int r = spawn_target(Wc, L + 1)) return r;
+				GBRT_CK(cudaMemsetAsync(Wc.count, 0, sizeof(uint32_t), st));
+				k_spawn_init<<<grid_for(cn, n_sm), kThreads, 0, st>>>(Wc, spawn_buf(L) + 5ull * c0, cn);
+				vertex_loop(Wc, cn);
+				uint32_t nc = 0;
+				if(int r = spawned(L + 1, nc)) return r;
+				if(nc)
+					if(int r = process_level(L + 1, nc)) return r;
+			}
+			return GBRT_OK;
+		};
+		while(!rc && first_rc.load() == GBRT_OK)
 		{
-			const uint32_t cn = static_cast<uint32_t>(std::min<uint64_t>(chunk, nl - c0));
-			Work Wc = W;
-			if(int rc = spawn_target(Wc, L + 1)) return rc;
-			GBRT_CK(cudaMemsetAsync(Wc.count, 0, sizeof(uint32_t), s));
-			k_spawn_init<<<grid_for(cn, n_sm), kThreads, 0, s>>>(Wc, spawn_buf(L) + 5ull * c0, cn);
-			vertex_loop(Wc, cn);
+			const uint64_t wv = next_wave.fetch_add(1);
+			if(wv >= n_waves) break;
+			const uint64_t start = wv * wave;
+			const uint32_t wn = static_cast<uint32_t>(std::min<uint64_t>(wave, total - start));
+			Work Wv = W;
+			if((rc = spawn_target(Wv, 1))) break;
+			k_camera_batch<<<grid_for(wn, n_sm), kThreads, 0, st>>>(table, n, static_cast<uint32_t>(start), wn, Wv);
+			vertex_loop(Wv, wn);
 			uint32_t nc = 0;
-			if(int rc = spawned(L + 1, nc)) return rc;
-			if(nc)
-				if(int rc = process_level(L + 1, nc)) return rc;
+			if((rc = spawned(1, nc))) break;
+			if(nc) rc = process_level(1, nc);
 		}
-		return GBRT_OK;
+		if(!rc && cudaGetLastError() != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "gbrt_pt_render_multi: launch failed");
+		if(!rc) cudaMemcpyAsync(&rays[2 * k], W.stats, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+		release_work(H, st);                    // back to the pool
+		if(k > 0)
+		{
+			cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming);
+			cudaEventRecord(done[k], st);
+			if(cudaStreamSynchronize(st) != cudaSuccess && !rc) rc = gbrt_set_error(GBRT_ERR_CUDA, "gbrt_pt_render_multi: stream error");
+			cudaStreamDestroy(st);
+		}
+		return rc ? fail(rc) : GBRT_OK;
 	};
-	cudaEvent_t e0 = nullptr, e1 = nullptr;
-	GBRT_CK(cudaEventCreate(&e0));
-	GBRT_CK(cudaEventCreate(&e1));
-	GBRT_CK(cudaMemsetAsync(W.stats, 0, 2 * sizeof(unsigned long long), s));
-	GBRT_CK(cudaEventRecord(e0, s));
-	int rc = GBRT_OK;
-	for(uint64_t start = 0; start < total && rc == GBRT_OK; start += wave)
-	{
-		const uint32_t wn = static_cast<uint32_t>(std::min<uint64_t>(wave, total - start));
-		Work Wv = W;
-		if((rc = spawn_target(Wv, 1))) break;
-		k_camera_batch<<<grid_for(wn, n_sm), kThreads, 0, s>>>(table, n, static_cast<uint32_t>(start), wn, Wv);
-		vertex_loop(Wv, wn);
-		uint32_t nc = 0;
-		if((rc = spawned(1, nc))) break;
-		if(nc) rc = process_level(1, nc);
-	}
-	if(rc == GBRT_OK && cudaGetLastError() != cudaSuccess) rc = gbrt_set_error(GBRT_ERR_CUDA, "gbrt_pt_render_multi: launch failed");
+	std::vector<std::thread> pool;
+	for(uint32_t k = 1; k < n_streams; ++k) pool.emplace_back(worker, k);
+	worker(0);
+	for(auto &t : pool) t.join();
+	for(uint32_t k = 1; k < n_streams; ++k)
+		if(done[k]) { cudaStreamWaitEvent(s, done[k], 0); cudaEventDestroy(done[k]); }
 	cudaEventRecord(e1, s);
-	unsigned long long st[2] = {0ull, 0ull};
-	cudaMemcpyAsync(st, W.stats, sizeof(st), cudaMemcpyDeviceToHost, s);
 	cudaFreeAsync(table, s);
 	for(uint32_t i = 0; i < n; ++i)
 	{
@@ -5163,14 +5228,13 @@ static int batch_render_locked(gbrt_scene *const *scenes, const gbrt_camera_desc
 	cudaEventElapsedTime(&ms, e0, e1);
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
-	if(rc) return rc;
+	if(first_rc.load() != GBRT_OK) return gbrt_set_error(first_rc.load(), "%s", err_msg.c_str());
 	if(se != cudaSuccess) return gbrt_set_error(GBRT_ERR_CUDA, "gbrt_pt_render_multi: %s", cudaGetErrorString(se));
 	if(stats)
 	{
 		*stats = gbrt_pt_stats{};
 		for(uint32_t i = 0; i < n; ++i) stats->camera_samples += host[i].paths / static_cast<uint32_t>(host[i].P.path_samples);
-		stats->extension_rays = st[0];
-		stats->shadow_rays = st[1];
+		for(uint32_t k = 0; k < n_streams; ++k) { stats->extension_rays += rays[2 * k]; stats->shadow_rays += rays[2 * k + 1]; }
 		stats->ms = ms;
 	}
 	return GBRT_OK;
@@ -5197,8 +5261,8 @@ static int batch_autotune(gbrt_scene *const *scenes, const gbrt_camera_desc *cam
 	std::vector<gbrt_pt_params> pp(params, params + n);
 	for(auto &p : pp) if(p.filter_type != GBRT_FILTER_PIXEL) p.film_weight_dev = wscratch;
 	const int bps_max = max_blocks_per_sm(reinterpret_cast<const void *>(k_extend_batch));
-	BatchPlan plan{t.wave_paths ? t.wave_paths : (1u << 21), t.shade_block ? t.shade_block : kThreads,
-	               t.trace_blocks_per_sm ? t.trace_blocks_per_sm : static_cast<uint32_t>(bps_max)};
+	BatchPlan plan{t.wave_paths ? t.wave_paths : (1u << 20), t.shade_block ? t.shade_block : kThreads,
+	               t.trace_blocks_per_sm ? t.trace_blocks_per_sm : static_cast<uint32_t>(bps_max), t.streams ? t.streams : 4u};
 	float spent = 0.f;
 	int rc = GBRT_OK;
 	auto trial = [&](const BatchPlan &pl, float &ms) -> int {
@@ -5210,11 +5274,25 @@ static int batch_autotune(gbrt_scene *const *scenes, const gbrt_camera_desc *cam
 	};
 	float ms0 = 0.f;
 	rc = trial(plan, ms0);               // warm: buffers grown, code loaded
+	if(!rc && !t.streams)
+	{
+		float best = 3.4e38f;
+		uint32_t pick = plan.streams;
+		for(uint32_t k : {1u, 2u, 4u, 8u})
+		{
+			BatchPlan pl = plan;
+			pl.streams = k;
+			float ms = 0.f;
+			if((rc = trial(pl, ms))) break;
+			if(ms < best) { best = ms; pick = k; }
+		}
+		plan.streams = pick;
+	}
 	if(!rc && !t.wave_paths)
 	{
 		float best = 3.4e38f;
 		uint32_t pick = plan.wave;
-		for(uint32_t w : {1u << 20, 1u << 21, 1u << 22, 1u << 23})
+		for(uint32_t w : {1u << 19, 1u << 20, 1u << 21, 1u << 22})
 		{
 			BatchPlan pl = plan;
 			pl.wave = w;
@@ -5258,6 +5336,7 @@ static int batch_autotune(gbrt_scene *const *scenes, const gbrt_camera_desc *cam
 	t.wave_paths = plan.wave;
 	t.shade_block = plan.shade_block;
 	t.trace_blocks_per_sm = plan.trace_bps;
+	t.streams = plan.streams;
 	t.tune_ms = spent;
 	return GBRT_OK;
 }
@@ -5278,10 +5357,10 @@ int gbrt_pt_render_multi(gbrt_scene *const *scenes, const gbrt_camera_desc *came
 	for(gbrt_scene *S : order) locks.emplace_back(S->mu);
 	gbrt_batch_tuning t{};
 	if(tuning) t = *tuning;
-	if(!t.wave_paths || !t.shade_block || !t.trace_blocks_per_sm)
+	if(!t.wave_paths || !t.shade_block || !t.trace_blocks_per_sm || !t.streams)
 		if(int rc = batch_autotune(scenes, cameras, params, n, t, s)) return rc;
 	if(tuning) *tuning = t;
-	const BatchPlan plan{t.wave_paths, t.shade_block, t.trace_blocks_per_sm};
+	const BatchPlan plan{t.wave_paths, t.shade_block, t.trace_blocks_per_sm, t.streams};
 	return batch_render_locked(scenes, cameras, params, films, n, plan, 0, stats, s);
 }
 

@@ -846,7 +846,7 @@ def knn_gather(points, queries, cell, k, r2):
 
 class BatchTuning(ctypes.Structure):
     _fields_ = [("wave_paths", ctypes.c_uint32), ("shade_block", ctypes.c_uint32), ("trace_blocks_per_sm", ctypes.c_uint32),
-                ("tune_ms", ctypes.c_float)]
+                ("streams", ctypes.c_uint32), ("tune_ms", ctypes.c_float)]
 
 
 def render_multi(renderers, spp, film_ptrs, tuning=None, base_offset=0, seed=1, stream=0):
@@ -868,7 +868,7 @@ def render_multi(renderers, spp, film_ptrs, tuning=None, base_offset=0, seed=1, 
     return ({"camera_samples": st.camera_samples, "extension_rays": st.extension_rays, "shadow_rays": st.shadow_rays,
              "ms": st.ms},
             {"wave_paths": t.wave_paths, "shade_block": t.shade_block, "trace_blocks_per_sm": t.trace_blocks_per_sm,
-             "tune_ms": t.tune_ms})
+             "streams": t.streams, "tune_ms": t.tune_ms})
 
 
 def render_batch(renderers, spp, film_ptrs, concurrency=8, base_offset=0, seed=1):

@@ -247,12 +247,10 @@ def test_trained_guide_lowers_error_at_equal_samples(cuda_device):
     """What the trained network gains: relMSE at 64 spp against an 8192-spp
     plain reference, guided (after online training) vs plain.  relMSE of a
     64-spp image of this scene is heavy-tailed (rare long paths through the
-    door gap), so the comparison is of medians over 24 independent images.
-    Training is not deterministic (gradient atomics); after 48 passes the
-    gain measured 1.2-1.4x over three guide seeds, after 24 passes 1.0-1.2x.
-    One of about fifteen runs trained into a worse guide (0.73x), so a second
-    guide is trained with another seed before the test fails: a network
-    that never gains still fails it."""
+    door gap), so each estimate is the median over 24 independent images.
+    Training is not deterministic (gradient atomics), so three guides are
+    trained (seeds 4, 5, 6) and the median of their gains must reach 1.1x;
+    every seed's gain is printed (the worst one included)."""
     r = gbrt.Renderer(_indoor_small())
     ref = np.mean([r.render(1024, base_offset=10_000_000 + b * 1024, seed=900 + b)[0] for b in range(8)], axis=0)
 
@@ -260,12 +258,11 @@ def test_trained_guide_lowers_error_at_equal_samples(cuda_device):
         return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
     ep = np.median([relmse(r.render(64, base_offset=b * 64, seed=70 + b)[0]) for b in range(24)])
     gains = []
-    for seed in (4, 5):
+    for seed in (4, 5, 6):
         guide = r.make_guide(log2_table=16, seed=seed)
         _train(r, guide, passes=48)
         eg = np.median([relmse(r.render(64, base_offset=b * 64, seed=70 + b, guide=guide, alpha=0.5)[0]) for b in range(24)])
         gains.append(ep / eg)
         print(f"median relMSE at 64 spp: plain {ep:.4g}, guided (seed {seed}) {eg:.4g} (x{ep / eg:.2f})")
-        if eg < ep:
-            break
-    assert gains[-1] > 1.0, gains
+    print(f"gains {[round(g, 3) for g in gains]}, median {np.median(gains):.3f}, worst {min(gains):.3f}")
+    assert np.median(gains) >= 1.1, gains

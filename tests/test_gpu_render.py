@@ -332,7 +332,7 @@ def test_gpu_render_batch_equals_single_renders(cuda_device):
         singles.append(f)
         rays[0] += s1["extension_rays"]
         rays[1] += s1["shadow_rays"]
-    for tuning in (None, {"wave_paths": 3000, "shade_block": 64, "trace_blocks_per_sm": 1}):
+    for tuning in (None, {"wave_paths": 3000, "shade_block": 64, "trace_blocks_per_sm": 1, "streams": 3}):
         films = [torch.zeros_like(f) for f in singles]
         st, used = gbrt.render_multi(rs, 4, [f.data_ptr() for f in films], tuning=tuning)
         torch.cuda.synchronize()
