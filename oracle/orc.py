@@ -323,3 +323,59 @@ def run_reference_photons(scene):
         ph = np.frombuffer(raw, np.float32, 9 * n, o).reshape(n, 9).copy(); o += 36 * n
         out.append((ph, paths))
     return out
+
+
+REF_BINDING = os.path.join(HERE, "_ref", "binding_dump")
+
+
+def binding_available():
+    return os.path.exists(REF_BINDING)
+
+
+def run_reference_translation(scene, spp=1):
+    """The scene as the reference-side binding (oracle/ref/gb300_binding.cc)
+    hands it to the GPU library: gb300::translate of the reference's own
+    Scene and camera, gb300::pt_params of the integrator's ParamMap and
+    gb300::film_params of the film's.  Returns a dict of numpy arrays and
+    ctypes structures (libyafaray_gb300.gbrt layouts), with "ok" and
+    "error" for a scene the binding refuses."""
+    from libyafaray_gb300 import gbrt
+    text = reference_scene_text(scene, spp, 1)
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout, ftr = os.path.join(d, "scene.txt"), os.path.join(d, "out.bin"), os.path.join(d, "tr.bin")
+        open(fin, "w").write(text)
+        env = {k: v for k, v in os.environ.items() if k != "GB300_INTEGRATOR"}
+        # the render itself is the reference's own (a short one): only the translation is read
+        subprocess.run([REF_BINDING, fin, fout, ftr], check=True, stdout=subprocess.DEVNULL, env=env)
+        raw = open(ftr, "rb").read()
+    nv, nf, nm, nl, nn, hn = struct.unpack("<6i", raw[:24])
+    o = 24
+
+    def take(dtype, count, shape):
+        nonlocal o
+        a = np.frombuffer(raw, dtype, count, o).reshape(shape).copy()
+        o += a.nbytes
+        return a
+
+    def take_struct(cls, count):
+        nonlocal o
+        arr = (cls * max(1, count))()
+        n = ctypes.sizeof(cls) * count
+        ctypes.memmove(arr, raw[o:o + n], n)
+        o += n
+        return arr[:count]
+
+    out = {"vertices": take(np.float32, 3 * nv, (nv, 3)), "faces": take(np.uint32, 4 * nf, (nf, 4)),
+           "face_material": take(np.int32, nf, (nf,))}
+    out["materials"] = take_struct(gbrt.MaterialDesc, nm)
+    out["lights"] = take_struct(gbrt.LightDesc, nl)
+    if hn:
+        out["normals"] = take(np.float32, 3 * nn, (nn, 3))
+        out["face_normals"] = take(np.uint32, 4 * nf, (nf, 4))
+    out["camera"] = take_struct(gbrt.CameraDesc, 1)[0]
+    out["params"] = take_struct(gbrt.PtParams, 1)[0]
+    out["aa"] = take_struct(gbrt.AaParams, 1)[0]
+    out["caustic"] = take_struct(gbrt.PmParams, 1)[0]
+    out["ok"] = struct.unpack("<i", raw[o:o + 4])[0] == 0
+    out["error"] = raw[o + 4:].decode()
+    return out

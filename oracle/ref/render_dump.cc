@@ -67,6 +67,12 @@
 #include "integrator/surface/integrator_sppm.h"
 #undef private
 #undef protected
+#ifdef GB300_BINDING
+#include "gb300_binding.h"
+#include "common/logger.h"
+#include "param/param_result.h"
+#include <cstdlib>
+#endif
 
 namespace {
 struct Film { int w = 0, h = 0; std::vector<float> rgb; };
@@ -150,6 +156,17 @@ int main(int argc, char **argv)
 		yafaray_ParamMap *ip = yafaray_createParamMap();
 		yafaray_setParamMapString(ip, "type", integrator_type.c_str());
 		for(const auto &kv : integrator_kv) setTyped(ip, kv.first, kv.second);
+#ifdef GB300_BINDING
+		if(std::getenv("GB300_INTEGRATOR") && integrator_type == "pathtracing")
+		{
+			// the GPU pathtracing integrator in place of the factory's
+			yafaray::ParamResult pr;
+			yafaray::SurfaceIntegrator *gpu = new gb300::PathIntegratorGb300(*reinterpret_cast<yafaray::Logger *>(logger), pr, "integrator",
+			                                                                  *reinterpret_cast<yafaray::ParamMap *>(ip));
+			yafaray_destroyParamMap(ip);
+			return reinterpret_cast<yafaray_SurfaceIntegrator *>(gpu);
+		}
+#endif
 		yafaray_SurfaceIntegrator *si = yafaray_createSurfaceIntegrator(logger, "integrator", ip);
 		yafaray_destroyParamMap(ip);
 		return si;
@@ -407,7 +424,57 @@ int main(int argc, char **argv)
 		const auto t0 = std::chrono::steady_clock::now();
 		yafaray_preprocessScene(scene, rc, flags);
 		yafaray_preprocessSurfaceIntegrator(rm, integrator, rc, scene);
+#ifdef GB300_BINDING
+		// the third argument takes the scene as the GPU path receives it
+		// (gb300::translate and gb300::pt_params / film_params):
+		//   i32 n_vertices, n_faces, n_materials, n_lights, n_normals, has_normals,
+		//   f32 vertices[n_vertices][3], u32 faces[n_faces][4], i32 face_material[n_faces],
+		//   gbrt_material_desc[n_materials], gbrt_light_desc[n_lights],
+		//   f32 normals[n_normals][3], u32 face_normals[n_faces][4] (has_normals only),
+		//   gbrt_camera_desc, gbrt_pt_params, gbrt_aa_params, gbrt_pm_params (caustic map),
+		//   i32 status, error text
+		if(k == 0 && argc > 3)
+		{
+			gb300::SceneDesc desc;
+			std::string error;
+			const auto *image_film = reinterpret_cast<const yafaray::ImageFilm *>(film);
+			bool ok = gb300::translate(*reinterpret_cast<const yafaray::Scene *>(scene), *image_film->getCamera(), desc, error);
+			yafaray::ParamMap ip;
+			ip.setParam("type", integrator_type);
+			for(const auto &kv : integrator_kv) setTyped(reinterpret_cast<yafaray_ParamMap *>(&ip), kv.first, kv.second);
+			gbrt_pm_params caustic{};
+			gbrt_pt_params ptp = gb300::pt_params(ip, spp, image_film->getBaseSamplingOffset(), caustic);
+			gbrt_aa_params aap{};
+			ok = ok && gb300::film_params(image_film->getAsParamMap(false), ptp, aap, error);
+			FILE *ft = fopen(argv[3], "wb");
+			if(!ft) { perror("translation"); return 2; }
+			const int hdr6[6] = {static_cast<int>(desc.vertices.size() / 3), static_cast<int>(desc.face_material.size()),
+			                     static_cast<int>(desc.materials.size()), static_cast<int>(desc.lights.size()),
+			                     static_cast<int>(desc.normals.size() / 3), desc.has_normals ? 1 : 0};
+			fwrite(hdr6, 4, 6, ft);
+			fwrite(desc.vertices.data(), 4, desc.vertices.size(), ft);
+			fwrite(desc.faces.data(), 4, desc.faces.size(), ft);
+			fwrite(desc.face_material.data(), 4, desc.face_material.size(), ft);
+			fwrite(desc.materials.data(), sizeof(gbrt_material_desc), desc.materials.size(), ft);
+			fwrite(desc.lights.data(), sizeof(gbrt_light_desc), desc.lights.size(), ft);
+			if(desc.has_normals)
+			{
+				fwrite(desc.normals.data(), 4, desc.normals.size(), ft);
+				fwrite(desc.face_normals.data(), 4, desc.face_normals.size(), ft);
+			}
+			fwrite(&desc.camera, sizeof desc.camera, 1, ft);
+			fwrite(&ptp, sizeof ptp, 1, ft);
+			fwrite(&aap, sizeof aap, 1, ft);
+			fwrite(&caustic, sizeof caustic, 1, ft);
+			const int status = ok ? 0 : 1;
+			fwrite(&status, 4, 1, ft);
+			fwrite(error.data(), 1, error.size(), ft);
+			fclose(ft);
+		}
+		if(false)
+#else
 		if(k == 0 && argc > 3 && aa_kv.empty())
+#endif
 		{
 			auto *pmi = dynamic_cast<yafaray::PhotonIntegrator *>(reinterpret_cast<yafaray::SurfaceIntegrator *>(integrator));
 			if(!pmi) { fprintf(stderr, "photon dump needs the photonmapping integrator\n"); return 2; }
@@ -434,7 +501,11 @@ int main(int argc, char **argv)
 		yafaray_destroyRenderControl(rc);
 		yafaray_destroyFilm(film);
 	}
+#ifdef GB300_BINDING
+	if(false)
+#else
 	if(argc > 3 && !aa_kv.empty())
+#endif
 	{
 		FILE *fa = fopen(argv[3], "wb");
 		if(!fa) { perror("aa"); return 2; }

@@ -7,6 +7,13 @@ reference sources by oracle/ref/Makefile) ray by ray.
 Each file holds the scene (vertices, faces), the rays, and what the reference
 returned: closest hit (Accelerator::intersect) prim/t/u/v and shadow
 occlusion (Accelerator::isShadowed) as a hit flag, plus the tree bound.
+
+    python tests/golden/make_golden.py normals   # smooth_normals.npz only
+    python tests/golden/make_golden.py binding   # binding_translation.npz only
+
+smooth_normals.npz holds the reference's yafaray_smoothObjectMesh results;
+binding_translation.npz the scenes the reference-side binding
+(oracle/ref/gb300_binding.cc) translates for the GPU library.
 """
 import os
 import sys
@@ -144,8 +151,39 @@ def normals_golden():
     print(f"smooth_normals.npz: {len(cases)} meshes")
 
 
+BINDING_CASES = {
+    # the glass Cornell box with smoothed meshes (shading normals per corner)
+    "smooth": lambda: scenes.smooth_cornell_scene(res=48),
+    # pathtracing with a caustic photon map and the film's AA_clamp_indirect
+    "pt_photon": lambda: scenes.cornell_pt_variant_scene(res=48, caustic_type="both", clamp_indirect=2.0),
+}
+
+
+def binding_golden():
+    """binding_translation.npz: the scenes of BINDING_CASES as the
+    reference-side binding (oracle/ref/gb300_binding.cc, run by
+    oracle/_ref/binding_dump) hands them to the GPU library: arrays, and the
+    descriptor structures as raw bytes (gbrt.h layouts)."""
+    out = {}
+    for name, make in BINDING_CASES.items():
+        tr = orc.run_reference_translation(make(), spp=8)
+        assert tr["ok"], tr["error"]
+        for k in ("vertices", "faces", "face_material", "normals", "face_normals"):
+            if k in tr:
+                out[f"{name}_{k}"] = tr[k]
+        for k in ("materials", "lights"):
+            out[f"{name}_{k}"] = np.frombuffer(b"".join(bytes(x) for x in tr[k]), np.uint8)
+        for k in ("camera", "params", "aa", "caustic"):
+            out[f"{name}_{k}"] = np.frombuffer(bytes(tr[k]), np.uint8)
+    out["cases"] = np.array(sorted(BINDING_CASES))
+    np.savez_compressed(os.path.join(OUT, "binding_translation.npz"), **out)
+    print(f"binding_translation.npz: {len(BINDING_CASES)} scenes")
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["normals"]:
         normals_golden()
+    elif sys.argv[1:] == ["binding"]:
+        binding_golden()
     else:
         main()
