@@ -5241,9 +5241,11 @@ static int batch_render_locked(gbrt_scene *const *scenes, const gbrt_camera_desc
 }
 
 // The autotuner: short trial renders of the whole batch at 1 sample per
-// pixel into scratch films, device-timed, over the wave size, then the
-// shading block size, then the traversal grids' residency (coordinate
-// descent from the defaults 2 Mi / 128 / what fits).
+// pixel into scratch films, device-timed, coordinate descent over the
+// number of waves in flight, then the wave size, then the shading block
+// size, then the traversal grids' residency (from the defaults 4 streams,
+// 1 Mi paths, 128 threads, what fits; residency tried at what fits and
+// half of it).
 static int batch_autotune(gbrt_scene *const *scenes, const gbrt_camera_desc *cameras, const gbrt_pt_params *params, uint32_t n,
                           gbrt_batch_tuning &t, cudaStream_t s)
 {

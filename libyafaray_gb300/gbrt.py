@@ -852,7 +852,8 @@ class BatchTuning(ctypes.Structure):
 def render_multi(renderers, spp, film_ptrs, tuning=None, base_offset=0, seed=1, stream=0):
     """gbrt_pt_render_multi: every Renderer's scene into its device float film
     (pointer) in one wavefront.  tuning: None (autotune) or a dict with
-    wave_paths / shade_block / trace_blocks_per_sm (missing or 0 = tuned).
+    wave_paths / shade_block / trace_blocks_per_sm / streams (missing or 0 =
+    tuned).
     Returns (stats dict of the batch, the tuning used incl. tune_ms)."""
     n = len(renderers)
     S = (ctypes.c_void_p * n)(*[r._h.value for r in renderers])
