@@ -382,17 +382,78 @@ int gbrt_mesh_smooth_normals(const float *vertices, uint32_t n_vertices, const u
  * geometric normal.  Fewer than 0xFFFFFFFD normals. */
 int gbrt_scene_set_normals(gbrt_scene *scene, const float *normals, uint32_t n_normals, const uint32_t *face_normals);
 
-/* ---- image textures on shinydiffuse diffuse colour ----------------------
+/* ---- textures on shinydiffuse diffuse colour -----------------------------
  * An ImageTexture (src/texture/texture_image.cc) over an in-memory float
- * image, reached through a TextureMapperNode (src/shader/shader_node_texture.cc)
- * set as a shinydiffuse material's "diffuse_shader": the texture's colour
- * replaces the material's diffuse colour wherever the reference reads
+ * image, or a procedural texture (blend, clouds, marble, wood, voronoi,
+ * musgrave, distorted_noise, rgb_cube: src/texture/texture_*.cc), reached
+ * through a TextureMapperNode (src/shader/shader_node_texture.cc) set as a
+ * shinydiffuse material's "diffuse_shader": the texture's colour replaces
+ * the material's diffuse colour wherever the reference reads
  * getShaderColor(Diffuse) (eval, sample, pdf weights, transmit filter,
  * emission).  Parameter names and defaults [..] are the reference's. */
 enum { GBRT_TEXCO_GLOBAL = 0, GBRT_TEXCO_UV = 1 };                 /* "texco" ["global"] */
-enum { GBRT_MAPPING_PLAIN = 0, GBRT_MAPPING_CUBE = 1 };            /* "mapping" ["plain"] */
+enum { GBRT_MAPPING_PLAIN = 0, GBRT_MAPPING_CUBE = 1, GBRT_MAPPING_TUBE = 2, GBRT_MAPPING_SPHERE = 3 };   /* "mapping" ["plain"] */
 enum { GBRT_CLIP_EXTEND = 0, GBRT_CLIP_CLIP = 1, GBRT_CLIP_CLIPCUBE = 2, GBRT_CLIP_REPEAT = 3, GBRT_CLIP_CHECKER = 4 };   /* "clipping" ["repeat"] */
 enum { GBRT_INTERP_NONE = 0, GBRT_INTERP_BILINEAR = 1 };           /* "interpolate" ["bilinear"] */
+
+/* Texture "type" (Texture::Type, include/texture/texture.h:70-84). */
+enum { GBRT_TEX_IMAGE = 0, GBRT_TEX_BLEND = 1, GBRT_TEX_CLOUDS = 2, GBRT_TEX_MARBLE = 3, GBRT_TEX_WOOD = 4, GBRT_TEX_VORONOI = 5,
+       GBRT_TEX_MUSGRAVE = 6, GBRT_TEX_DISTORTED_NOISE = 7, GBRT_TEX_RGB_CUBE = 8 };
+/* "noise_type" (NoiseGenerator::NoiseType, include/noise/noise_generator.h:32-45) ["newperlin"] */
+enum { GBRT_NOISE_BLENDER = 0, GBRT_NOISE_STDPERLIN = 1, GBRT_NOISE_NEWPERLIN = 2, GBRT_NOISE_CELL = 3, GBRT_NOISE_VORONOI_F1 = 4,
+       GBRT_NOISE_VORONOI_F2 = 5, GBRT_NOISE_VORONOI_F3 = 6, GBRT_NOISE_VORONOI_F4 = 7, GBRT_NOISE_VORONOI_F2F1 = 8,
+       GBRT_NOISE_VORONOI_CRACKLE = 9 };
+/* voronoi "distance_metric" ["real"] */
+enum { GBRT_DIST_REAL = 0, GBRT_DIST_SQUARED = 1, GBRT_DIST_MANHATTAN = 2, GBRT_DIST_CHEBYCHEV = 3, GBRT_DIST_MINKOVSKY_HALF = 4,
+       GBRT_DIST_MINKOVSKY_FOUR = 5, GBRT_DIST_MINKOVSKY = 6 };
+/* blend "blend_type" ["linear"] */
+enum { GBRT_PROGRESSION_LINEAR = 0, GBRT_PROGRESSION_QUADRATIC = 1, GBRT_PROGRESSION_EASING = 2, GBRT_PROGRESSION_DIAGONAL = 3,
+       GBRT_PROGRESSION_SPHERE = 4, GBRT_PROGRESSION_QUAD_SPHERE = 5, GBRT_PROGRESSION_RADIAL = 6 };
+enum { GBRT_BIAS_NONE = 0, GBRT_BIAS_POSITIVE = 1, GBRT_BIAS_NEGATIVE = 2 };          /* clouds "bias" ["none"] */
+enum { GBRT_SHAPE_SIN = 0, GBRT_SHAPE_SAW = 1, GBRT_SHAPE_TRI = 2 };                  /* marble / wood "shape" ["sin"] */
+enum { GBRT_WOOD_BANDS = 0, GBRT_WOOD_RINGS = 1 };                                    /* wood "wood_type" ["bands"] */
+/* voronoi "color_mode" ["intensity-without-color"] */
+enum { GBRT_VORONOI_INTENSITY = 0, GBRT_VORONOI_POSITION = 1, GBRT_VORONOI_POSITION_OUTLINE = 2,
+       GBRT_VORONOI_POSITION_OUTLINE_INTENSITY = 3 };
+/* musgrave "musgrave_type" ["fBm"] */
+enum { GBRT_MUSGRAVE_FBM = 0, GBRT_MUSGRAVE_MULTIFRACTAL = 1, GBRT_MUSGRAVE_HETERO = 2, GBRT_MUSGRAVE_HYBRID = 3,
+       GBRT_MUSGRAVE_RIDGED = 4 };
+/* colour ramp "ramp_color_mode" ["RGB"], "ramp_interpolation" ["LINEAR"],
+ * "ramp_hue_interpolation" ["NEAR"] (include/color/color_ramp.h:50-80) */
+enum { GBRT_RAMP_RGB = 0, GBRT_RAMP_HSV = 1, GBRT_RAMP_HSL = 2 };
+enum { GBRT_RAMP_LINEAR = 0, GBRT_RAMP_CONSTANT = 1 };
+enum { GBRT_HUE_NEAR = 0, GBRT_HUE_FAR = 1, GBRT_HUE_CLOCKWISE = 2, GBRT_HUE_COUNTERCLOCKWISE = 3 };
+#define GBRT_RAMP_MAX 16
+
+/* The parameters of a procedural texture (reference names and defaults). */
+typedef struct gbrt_procedural_desc {
+	uint32_t noise_type;        /* "noise_type" (distorted_noise: "noise_type1") [GBRT_NOISE_NEWPERLIN] */
+	uint32_t noise_type2;       /* distorted_noise "noise_type2" [GBRT_NOISE_NEWPERLIN] */
+	float color1[3], color2[3]; /* "color1" [0, 0, 0], "color2" [1, 1, 1] */
+	float size;                 /* "size" [1] */
+	int32_t depth;              /* clouds / marble / wood "depth" [2] */
+	int32_t hard;               /* "hard" [0] */
+	uint32_t bias;              /* clouds GBRT_BIAS_* */
+	uint32_t shape;             /* marble / wood GBRT_SHAPE_* */
+	uint32_t wood_type;         /* GBRT_WOOD_* */
+	uint32_t blend_type;        /* blend GBRT_PROGRESSION_* */
+	int32_t use_flip_axis;      /* blend "use_flip_axis" [0] */
+	float sharpness;            /* marble "sharpness" [1] */
+	float turbulence;           /* marble / wood "turbulence" [1] */
+	uint32_t distance_metric;   /* voronoi GBRT_DIST_* */
+	uint32_t color_mode;        /* voronoi GBRT_VORONOI_* */
+	float weight[4];            /* voronoi "weight1" .. "weight4" [1, 0, 0, 0] */
+	float mk_exponent;          /* voronoi "mk_exponent" [2.5] */
+	float intensity;            /* voronoi / musgrave "intensity" [1] */
+	uint32_t musgrave_type;     /* GBRT_MUSGRAVE_* */
+	float h, lacunarity, octaves, offset, gain;   /* musgrave "H" [1], "lacunarity" [2], "octaves" [2], "offset" [1], "gain" [1] */
+	float distort;              /* distorted_noise "distort" [1] */
+	int32_t ramp_n;             /* "ramp_num_items" [0]: no ramp; at most GBRT_RAMP_MAX */
+	uint32_t ramp_mode, ramp_interpolation, ramp_hue_interpolation;
+	float ramp[GBRT_RAMP_MAX][5];   /* "ramp_item_<i>_color" RGBA and "_position", any order */
+} gbrt_procedural_desc;
+/* Zero-initialised descriptor with the reference's defaults. */
+void gbrt_procedural_defaults(gbrt_procedural_desc *d);
 
 typedef struct gbrt_texture_desc {
 	int32_t width, height;
@@ -424,7 +485,33 @@ typedef struct gbrt_texture_desc {
 	int32_t mirror_x, mirror_y; /* "mirror_x", "mirror_y" [0]: every other repeat mirrored (clipping repeat) */
 	int32_t even_tiles, odd_tiles;       /* clipping checker: "even_tiles" [0], "odd_tiles" [1] (set it: 0 hides those tiles) */
 	float checker_dist;         /* "checker_dist" [0]: tiles shrunk about their centres by 1 / (1 - checker_dist) */
+	uint32_t kind;              /* GBRT_TEX_* [GBRT_TEX_IMAGE]; procedural textures ignore the image fields
+	                               (width, height, rgba, interpolate, clipping, repeats, crop, rot90, mirror, tiles) */
+	float adj_saturation, adj_hue;   /* "adj_saturation" [1], "adj_hue" (degrees) [0]: a zeroed descriptor has
+	                                    saturation 0, so set them */
+	gbrt_procedural_desc proc;  /* kind != GBRT_TEX_IMAGE */
 } gbrt_texture_desc;
+
+/* libYafaRay's noise tables (NoiseGenerator::hash_ / hashpntf_,
+ * BlenderNoiseGenerator::hashvectf_, StdPerlinNoiseGenerator::stdp_p_ /
+ * stdp_g_): the procedural textures index them, and the library carries
+ * no copy, so the host hands them over (512 bytes, 768 floats, 768 floats,
+ * 514 bytes, 514 x 3 floats). */
+typedef struct gbrt_noise_tables {
+	const uint8_t *hash;
+	const float *hashpntf;
+	const float *hashvectf;
+	const uint8_t *stdp_p;
+	const float *stdp_g;
+} gbrt_noise_tables;
+/* The scene's noise tables, required before gbrt_scene_set_textures takes
+ * a procedural texture. */
+int gbrt_scene_set_noise_tables(gbrt_scene *scene, const gbrt_noise_tables *tables);
+/* Diagnostics: a texture's getColor (RGBA) and getFloat at n texture-space
+ * points (xyz, after the mapper) on the host or, on_device != 0, in a
+ * kernel (host buffers either way; synchronises).  Procedural kinds only. */
+int gbrt_texture_eval(const gbrt_texture_desc *texture, const gbrt_noise_tables *tables, const float *points, uint32_t n,
+                      float *rgba, float *value, int on_device);
 enum { GBRT_BLEND_MIX = 0, GBRT_BLEND_ADD = 1, GBRT_BLEND_MULTIPLY = 2, GBRT_BLEND_SUBTRACT = 3, GBRT_BLEND_SCREEN = 4,
        GBRT_BLEND_DIVIDE = 5, GBRT_BLEND_DIFFERENCE = 6, GBRT_BLEND_DARKEN = 7, GBRT_BLEND_LIGHTEN = 8 };
 

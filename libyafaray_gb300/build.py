@@ -17,8 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbrt.so")
 
-SOURCES = ["capi.cu", "bvh_build.cu", "traverse.cu", "pathtrace.cu", "guiding.cu", "mesh.cu"]
-EXACT_FP = {"traverse.cu", "pathtrace.cu"}
+SOURCES = ["capi.cu", "bvh_build.cu", "traverse.cu", "pathtrace.cu", "guiding.cu", "mesh.cu", "texture_eval.cu"]
+EXACT_FP = {"traverse.cu", "pathtrace.cu", "texture_eval.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -23,6 +23,7 @@
 // (material_shiny_diffuse.cc:432).
 #include "traverse_core.cuh"
 #include "sampling.cuh"
+#include "procedural.cuh"
 #include "guide_device.cuh"
 #include "photon_map.cuh"
 
@@ -86,6 +87,9 @@ struct DevTexture {
 	float colfac, upper[4], def_col[3];
 	int even_tiles, odd_tiles;  // clipping checker
 	float checker_dist;
+	float saturation, hue6;     // adj_saturation, adj_hue / 60 (HSV adjustment when either is set)
+	uint32_t kind;              // GBRT_TEX_*: image, or a procedural texture in proc
+	gbrt::ProcTex proc;
 };
 
 struct DevLight {
@@ -212,6 +216,7 @@ struct SceneDev {
 	// shading normals (gbrt_scene_set_normals); null without
 	const float4 *vnrm;         // vertex normals
 	const uint4 *face_nrm;      // normal indices per face; x = kFlatFace: geometric normal; w = kTriFace: triangle
+	gbrt::NoiseTables nt;       // the host's noise tables (gbrt_scene_set_noise_tables); null without
 };
 
 __device__ __forceinline__ float dot3(const float a[3], const float b[3]) { return xa(xa(xm(a[0], b[0]), xm(a[1], b[1])), xm(a[2], b[2])); }
@@ -868,6 +873,13 @@ __device__ void tex_layer(const DevTexture &T, float ta, float rgb[3])
 	}
 }
 
+// A procedural texture's colour, out of line so the shading kernels keep
+// their registers for the common path.
+__device__ __noinline__ void tex_procedural(const SceneDev &sc, const DevTexture &T, const float p[3], float c4[4])
+{
+	gbrt::proc_color(sc.nt, T.proc, p, c4);
+}
+
 // TextureMapperNode::getCoords / doMapping (shader_node_texture.cc:153-230),
 // ImageTexture::getColor / doMapping / noInterpolation /
 // bilinearInterpolation (texture_image.cc:180-262, 343-375) and
@@ -889,7 +901,41 @@ __device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p
 		else { r[0] = t[1]; r[1] = t[2]; r[2] = t[0]; }
 		t[0] = r[0]; t[1] = r[1]; t[2] = r[2];
 	}
+	else if(T.mapping == GBRT_MAPPING_TUBE)
+	{
+		// TextureMapperNode::tubeMap (shader_node_texture.cc:125-137)
+		float r[3];
+		r[1] = t[2];
+		const float d = xa(xm(t[0], t[0]), xm(t[1], t[1]));
+		if(d > 0.f) { r[2] = __fdiv_rn(1.f, sqrtf(d)); r[0] = xm(-atan2f(t[0], t[1]), kInvPi); }
+		else r[0] = r[2] = 0.f;
+		t[0] = r[0]; t[1] = r[1]; t[2] = r[2];
+	}
+	else if(T.mapping == GBRT_MAPPING_SPHERE)
+	{
+		// TextureMapperNode::sphereMap (:139-151) with math::acos's clamp
+		float r[3] = {0.f, 0.f, 0.f};
+		const float d = xa(xa(xm(t[0], t[0]), xm(t[1], t[1])), xm(t[2], t[2]));
+		if(d > 0.f)
+		{
+			r[2] = sqrtf(d);
+			if(t[0] != 0.f && t[1] != 0.f) r[0] = xm(-atan2f(t[0], t[1]), kInvPi);
+			const float c = __fdiv_rn(t[2], r[2]);
+			const float ac = c <= -1.f ? kPi : (c >= 1.f ? 0.f : acosf(c));
+			r[1] = xs(1.f, xm(2.f, xm(ac, kInvPi)));
+		}
+		t[0] = r[0]; t[1] = r[1]; t[2] = r[2];
+	}
 	for(int k = 0; k < 3; ++k) t[k] = xa(xm(t[k], T.scale[k]), T.offset2[k]);
+	if(T.kind != GBRT_TEX_IMAGE)
+	{
+		// a procedural texture's getColor at the mapped point
+		float c4[4];
+		tex_procedural(sc, T, t, c4);
+		out[0] = c4[0]; out[1] = c4[1]; out[2] = c4[2];
+		tex_layer(T, c4[3], out);
+		return;
+	}
 	// the image's own mapping of (x, -y, z)
 	float mx = xa(xm(0.5f, t[0]), 0.5f), my = xa(xm(0.5f, -t[1]), 0.5f);
 	const float mz = xa(xm(0.5f, t[2]), 0.5f);
@@ -974,6 +1020,18 @@ __device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p
 		if(T.adj_clamp) for(int k = 0; k < 3; ++k) r[k] = r[k] < 0.f ? 0.f : r[k];
 		for(int k = 0; k < 3; ++k) if(T.mult[k] != 1.f) r[k] = xm(r[k], T.mult[k]);
 		if(T.adj_clamp) for(int k = 0; k < 3; ++k) r[k] = r[k] < 0.f ? 0.f : r[k];
+		if(T.saturation != 1.f || T.hue6 != 0.f)
+		{
+			// the HSV step of Texture::applyColorAdjustments (texture.cc:260-269)
+			float h = 0.f, sat = 0.f, v = 0.f;
+			gbrt::rgb_to_hsv(r, h, sat, v);
+			sat = xm(sat, T.saturation);
+			h = xa(h, T.hue6);
+			if(h < 0.f) h = xa(h, 6.f);
+			else if(h > 6.f) h = xs(h, 6.f);
+			gbrt::hsv_to_rgb(h, sat, v, r);
+			if(T.adj_clamp) for(int k = 0; k < 3; ++k) r[k] = r[k] < 0.f ? 0.f : r[k];
+		}
 	}
 	out[0] = r[0]; out[1] = r[1]; out[2] = r[2];
 	tex_layer(T, alpha, out);
@@ -1166,9 +1224,11 @@ __device__ __noinline__ bool shiny_sample_layers(const Surface &s, const float w
 // Fresnel): kr = 1 and the accumulated weight is the diffuse strength c, so
 // eval = c colour, pdf = |wi.n| c / c and sample picks the one component
 // with width c (1 / c) — the same float operations as the general code.
+// kPlain: the caller knows the material is the diffuse layer alone.
+template <bool kPlain = false>
 __device__ __forceinline__ void shiny_eval(const Surface &s, const float wo[3], const float wl[3], float out[3])
 {
-	if(s.m->sd != SD_DIFFUSE) { shiny_eval_layers(s, wo, wl, out); return; }
+	if(!kPlain && s.m->sd != SD_DIFFUSE) { shiny_eval_layers(s, wo, wl, out); return; }
 	out[0] = out[1] = out[2] = 0.f;
 	float n[3];
 	face_forward(s, wo, n);
@@ -1177,9 +1237,10 @@ __device__ __forceinline__ void shiny_eval(const Surface &s, const float wo[3], 
 	for(int k = 0; k < 3; ++k) out[k] = m_d * s.dcol[k];
 }
 
+template <bool kPlain = false>
 __device__ __forceinline__ float shiny_pdf(const Surface &s, const float wo[3], const float wi[3], uint32_t bsdfs)
 {
-	if(s.m->sd != SD_DIFFUSE) return shiny_pdf_layers(s, wo, wi, bsdfs);
+	if(!kPlain && s.m->sd != SD_DIFFUSE) return shiny_pdf_layers(s, wo, wi, bsdfs);
 	if(!(bsdfs & BF_DIFFUSE)) return 0.f;
 	const float c = s.m->sdc[3];
 	if(c < 0.00001f) return 0.f;
@@ -1188,11 +1249,11 @@ __device__ __forceinline__ float shiny_pdf(const Surface &s, const float wo[3], 
 	return (fabsf(dot3(wi, n)) * c) / c;
 }
 
-template <bool kExact = false>
+template <bool kExact = false, bool kPlain = false>
 __device__ __forceinline__ bool shiny_sample(const Surface &s, const float wo[3], float s1, float s2, uint32_t req, float wi[3], float col[3],
                                              float &w, float &pdf, uint32_t &sampled)
 {
-	if(s.m->sd != SD_DIFFUSE) return shiny_sample_layers(s, wo, s1, s2, req, wi, col, w, pdf, sampled);
+	if(!kPlain && s.m->sd != SD_DIFFUSE) return shiny_sample_layers(s, wo, s1, s2, req, wi, col, w, pdf, sampled);
 	const float c = s.m->sdc[3];
 	if((req & (BF_DIFFUSE | BF_REFLECT)) != (BF_DIFFUSE | BF_REFLECT) || c < 0.00001f) { sampled = 0u; pdf = 0.f; return false; }
 	const float width = c * (1.f / c);
@@ -1276,6 +1337,45 @@ __device__ __forceinline__ bool mat_sample(const Surface &s, const float wo[3], 
 	if(s.m->type == GBRT_MAT_ROUGH_GLASS) return rough_sample(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
 	if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return false;
 	return shiny_sample<kExact>(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
+}
+
+// The dispatch for scenes whose materials are all plain: shinydiffuse with
+// the diffuse layer alone and an untextured colour, or light_mat
+// (kLean); the same float operations as the general dispatch for those.
+template <bool kLean>
+__device__ __forceinline__ void mat_eval_l(const Surface &s, const float wo[3], const float wl[3], float out[3])
+{
+	if constexpr(kLean)
+	{
+		out[0] = out[1] = out[2] = 0.f;
+		if(s.m->type == GBRT_MAT_SHINYDIFFUSE) shiny_eval<true>(s, wo, wl, out);
+	}
+	else mat_eval(s, wo, wl, out);
+}
+
+template <bool kLean>
+__device__ __forceinline__ float mat_pdf_l(const Surface &s, const float wo[3], const float wi[3])
+{
+	if constexpr(kLean)
+	{
+		if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return 0.f;
+		return shiny_pdf<true>(s, wo, wi, BF_GLOSSY | BF_DIFFUSE | BF_DISPERSIVE | BF_REFLECT | BF_TRANSMIT);
+	}
+	else return mat_pdf(s, wo, wi);
+}
+
+template <bool kLean>
+__device__ __forceinline__ bool mat_sample_l(const Surface &s, const float wo[3], float s1, float s2, uint32_t req_flags, float wi[3],
+                                             float col[3], float &w, float &pdf, uint32_t &sampled)
+{
+	if constexpr(kLean)
+	{
+		col[0] = col[1] = col[2] = 0.f;
+		w = 0.f; pdf = 0.f; sampled = 0u;
+		if(s.m->type != GBRT_MAT_SHINYDIFFUSE) return false;
+		return shiny_sample<false, true>(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
+	}
+	else return mat_sample(s, wo, s1, s2, req_flags, wi, col, w, pdf, sampled);
 }
 
 // Sample colour x weight that Material::sample would return for a given
@@ -1428,6 +1528,7 @@ __device__ __forceinline__ uint32_t light_shadow_rays(const DevLight &L, uint32_
 	return L.type == GBRT_LIGHT_POINT ? 1u : 2u * static_cast<uint32_t>(light_samples(L, division, lmult));
 }
 
+template <bool kLean = false>
 __device__ void light_estimation(const SceneDev &sc, const Surface &s, const float wo[3], uint32_t li, uint32_t loffs,
                                  uint32_t sample_, uint32_t offset_, const float weight[3], uint32_t pixel, ShadowWriter &sw,
                                  uint32_t division, float lmult)
@@ -1446,7 +1547,7 @@ __device__ void light_estimation(const SceneDev &sc, const Surface &s, const flo
 		for(int k = 0; k < 3; ++k) ldir[k] *= inv;
 		const float sbias = kShadowBias * fmaxf(1.f, sqrtf(dot3(s.p, s.p)));
 		float surf[3];
-		mat_eval(s, wo, ldir, surf);
+		mat_eval_l<kLean>(s, wo, ldir, surf);
 		const float angle = fabsf(dot3(s.n, ldir));
 		float c[3];
 		for(int k = 0; k < 3; ++k) c[k] = surf[k] * (L.col[k] * idist_sqr) * angle * weight[k];
@@ -1481,10 +1582,10 @@ __device__ void light_estimation(const SceneDev &sc, const Surface &s, const flo
 					if(pdf > 1e-6f)
 					{
 						float surf[3];
-						mat_eval(s, wo, ldir, surf);
+						mat_eval_l<kLean>(s, wo, ldir, surf);
 						const float angle = fabsf(dot3(s.n, ldir));
 						float w = 1.f;
-						const float m_pdf = mat_pdf(s, wo, ldir);
+						const float m_pdf = mat_pdf_l<kLean>(s, wo, ldir);
 						if(m_pdf > 1e-6f)
 						{
 							const float l2 = xm(pdf, pdf), m2 = xm(m_pdf, m_pdf);
@@ -1502,7 +1603,7 @@ __device__ void light_estimation(const SceneDev &sc, const Surface &s, const flo
 		{
 			float wi[3], scol[3], W, spdf;
 			uint32_t sflags;
-			mat_sample(s, wo, s1, s2, BF_GLOSSY | BF_DIFFUSE | BF_DISPERSIVE | BF_REFLECT | BF_TRANSMIT, wi, scol, W, spdf, sflags);
+			mat_sample_l<kLean>(s, wo, s1, s2, BF_GLOSSY | BF_DIFFUSE | BF_DISPERSIVE | BF_REFLECT | BF_TRANSMIT, wi, scol, W, spdf, sflags);
 			const float cos_angle = dot3(wi, L.nflip);
 			if(cos_angle > 0.f && spdf > 1e-6f)
 			{
@@ -1811,7 +1912,12 @@ struct SceneTable {
 };
 
 // Shading of one vertex level of the wavefront (see the kernels below).
-template <typename Src>
+// kLean: a pathtracing render without guiding, records or photon maps of a
+// scene whose materials are all plain (mat_eval_l) and flat-shaded: the
+// photonmapping, guiding, recording, recursive-split, texture and
+// shading-normal code is compiled out, which roughly halves the kernel's
+// registers and lets twice the warps stay resident.
+template <typename Src, bool kLean = false>
 __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uint32_t shadow_cap)
 {
 	const uint32_t n = W.count[cur];
@@ -1851,10 +1957,19 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 				s.p[0] = xa(ra.x, xm(h.y, dir[0])); s.p[1] = xa(ra.y, xm(h.y, dir[1])); s.p[2] = xa(ra.z, xm(h.y, dir[2]));
 				const float4 ng = __ldg(sc.prim_ng + prim);
 				s.ng[0] = ng.x; s.ng[1] = ng.y; s.ng[2] = ng.z;
-				shading_normal(sc, prim, h.z, h.w, s.ng, s.n);
 				s.m = sc.mats + __float_as_uint(ng.w);
-				coords_system(s.n, s.u, s.v);
-				surface_color(sc, s, prim, h.z, h.w);
+				if constexpr(kLean)
+				{
+					s.n[0] = ng.x; s.n[1] = ng.y; s.n[2] = ng.z;
+					s.dcol[0] = s.m->col[0]; s.dcol[1] = s.m->col[1]; s.dcol[2] = s.m->col[2];
+					coords_system(s.n, s.u, s.v);
+				}
+				else
+				{
+					shading_normal(sc, prim, h.z, h.w, s.ng, s.n);
+					coords_system(s.n, s.u, s.v);
+					surface_color(sc, s, prim, h.z, h.w);
+				}
 				wo[0] = -dir[0]; wo[1] = -dir[1]; wo[2] = -dir[2];
 				pixel = W.p_pixel[path];
 				si = W.p_si[path];
@@ -1874,7 +1989,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 		}
 		// the previous vertex's record: incident radiance along its sampled
 		// direction = what the path adds from here on
-		if(hit && W.p_sum && k >= 1 && k - 1 < P.rec_stride && W.r_valid[static_cast<size_t>(path) * P.rec_stride + (k - 1)] == 2u)
+		if(!kLean && hit && W.p_sum && k >= 1 && k - 1 < P.rec_stride && W.r_valid[static_cast<size_t>(path) * P.rec_stride + (k - 1)] == 2u)
 		{
 			const size_t slot = static_cast<size_t>(path) * P.rec_stride + (k - 1);
 			W.r_pre[slot] = W.p_sum[path];
@@ -1896,7 +2011,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 					// photonmapping adds it twice (integrator_photon_mapping.cc:686-687, 713-721)
 					const float em = P.pm == 1 ? 2.f : 1.f;
 					film_put(P, film, film64, pixel, si, xm(thr[0], e[0]) * em, xm(thr[1], e[1]) * em, xm(thr[2], e[2]) * em);
-					if(W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
+					if(!kLean && W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
 				}
 				do_nee_all = (s.m->flags & BF_DIFFUSE) && sub == 0;
 				for(int c = 0; c < 3; ++c) nee_weight[c] = thr[c];
@@ -1906,7 +2021,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 				// integrator_montecarlo.cc:698-710)
 				addl = max(addl, s.m->addl_depth);
 				const uint32_t nl = level + 1u;
-				if(sub == 0 && W.sp_out && nl <= static_cast<uint32_t>(P.raydepth) + addl && nl < 20u)
+				if(!kLean && sub == 0 && W.sp_out && nl <= static_cast<uint32_t>(P.raydepth) + addl && nl < 20u)
 				{
 					const uint32_t f = s.m->flags;
 					do_glossy = (f & BF_GLOSSY) && (f & BF_REFLECT);
@@ -1914,7 +2029,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 					n_spawn = spawn_bound(f, do_glossy, do_spec, division, static_cast<uint32_t>(P.path_samples));
 				}
 			}
-			else if(P.pm)
+			else if(!kLean && P.pm)
 			{
 				// PhotonIntegrator::finalGathering (integrator_photon_mapping.cc:547-668)
 				// after its zero'th bounce: vertex k is the loop's depth k - 1
@@ -2030,7 +2145,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 						if(mat_emit(s, wo, e))
 						{
 							film_put(P, film, film64, pixel, si, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
-							if(W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
+							if(!kLean && W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
 						}
 				}
 			}
@@ -2049,11 +2164,12 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 		ShadowWriter sw{W.s_ray, W.s_col, W.s_pix, W.s_path, path, wbase + incl - n_shadow, wbase + incl};
 		if(sw.end > shadow_cap) sw.end = sw.slot > shadow_cap ? sw.slot : shadow_cap;
 		if(do_nee_all)
-			for(uint32_t l = 0; l < P.n_lights; ++l) light_estimation(sc, s, wo, l, l, sample_, offset_, nee_weight, pixel, sw, division, P.lmult);
-		if(do_nee_one) light_estimation(sc, s, wo, nee_light, nee_light, sample_, offset_, nee_weight, pixel, sw, division, P.lmult);
+			for(uint32_t l = 0; l < P.n_lights; ++l)
+				light_estimation<kLean>(sc, s, wo, l, l, sample_, offset_, nee_weight, pixel, sw, division, P.lmult);
+		if(do_nee_one) light_estimation<kLean>(sc, s, wo, nee_light, nee_light, sample_, offset_, nee_weight, pixel, sw, division, P.lmult);
 		sw.close();
 		// --- spawned integrate() calls of the recursive split ----------------
-		if(W.sp_out && __any_sync(0xffffffffu, n_spawn != 0u))
+		if(!kLean && W.sp_out && __any_sync(0xffffffffu, n_spawn != 0u))
 		{
 			uint32_t sincl = n_spawn;
 			for(int off = 1; off < 32; off <<= 1)
@@ -2073,7 +2189,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 		}
 		// --- continuation ray ----------------------------------------------
 		// (photonmapping: only the zero'th final-gather bounce comes here)
-		if(hit && !rr_dead && !(P.pm && k >= 1))
+		if(hit && !rr_dead && !(!kLean && P.pm && k >= 1))
 		{
 			float s1 = -1.f, s2 = 0.f;
 			uint32_t req = BF_ALL;
@@ -2115,7 +2231,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 				uint32_t sflags;
 				float mult[3], mpdf = 0.f, hf = 0.f;
 				const bool guidable = (s.m->type == GBRT_MAT_SHINYDIFFUSE && s.m->sd == SD_DIFFUSE) || s.m->type == GBRT_MAT_GLOSSY;
-				if(P.guiding && guidable)
+				if(!kLean && P.guiding && guidable)
 				{
 					// one-sample MIS of the guide mixture q and the BSDF sampler
 					// (true density p): weight = h(w) / (alpha q(w) + (1 - alpha) p(w)),
@@ -2149,9 +2265,9 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 				}
 				else
 				{
-					mat_sample(s, wo, s1, s2, req, wi, scol, w, pdf, sflags);
+					mat_sample_l<kLean>(s, wo, s1, s2, req, wi, scol, w, pdf, sflags);
 					for(int c = 0; c < 3; ++c) mult[c] = xm(scol[c], w);
-					if(P.record && guidable)
+					if(!kLean && P.record && guidable)
 					{
 						mpdf = bsdf_true_pdf(s, wo, wi, req);
 						hf = (0.2126f * mult[0] + 0.7152f * mult[1] + 0.0722f * mult[2]) * mpdf;
@@ -2169,7 +2285,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 				if(nt[0] != 0.f || nt[1] != 0.f || nt[2] != 0.f)
 				{
 					cont = true;
-					if(P.record && mpdf > 0.f && k < P.rec_stride)
+					if(!kLean && P.record && mpdf > 0.f && k < P.rec_stride)
 					{
 						const size_t slot = static_cast<size_t>(path) * P.rec_stride + k;
 						W.r_pos[slot] = make_float4(s.p[0], s.p[1], s.p[2], mpdf);
@@ -2178,7 +2294,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 						W.r_valid[slot] = 2u;     // waiting for the next vertex
 					}
 					caustic = (P.pt_caustic_path && (sflags & (BF_SPECULAR | BF_GLOSSY | BF_FILTER))) ? 1u : 0u;
-					if(P.pm) { caustic = 0u; W.p_pm[path] = make_float4(0.f, 0.f, 0.f, 0.f); }
+					if(!kLean && P.pm) { caustic = 0u; W.p_pm[path] = make_float4(0.f, 0.f, 0.f, 0.f); }
 					W.p_thr[path] = make_float4(nt[0], nt[1], nt[2], 0.f);
 					W.p_state[path] = (k + 1u) | (mat1 << 8) | (caustic << 16);
 					nray[0] = s.p[0]; nray[1] = s.p[1]; nray[2] = s.p[2]; nray[3] = kRayMinDist;
@@ -2210,6 +2326,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_shade(SceneDev sc, Params P, Wo
                                                     double *film64)
 {
 	shade_queue(OneScene{sc, P, film, film64}, W, cur, shadow_cap);
+}
+
+// The same for plain scenes (shade_queue kLean).
+__global__ void __launch_bounds__(kThreads, 6) k_shade_plain(SceneDev sc, Params P, Work W, int cur, uint32_t shadow_cap, float *film,
+                                                          double *film64)
+{
+	shade_queue<OneScene, true>(OneScene{sc, P, film, film64}, W, cur, shadow_cap);
 }
 
 // The same for a batch of scenes: every path's scene from the table.
@@ -3252,6 +3375,9 @@ __global__ void k_knn_test(gbrt::PhotonGrid g, const float *__restrict__ q, uint
 
 } // namespace
 
+struct gbrt_scene;
+static bool plain_scene(const gbrt_scene *S);
+
 struct gbrt_scene {
 	const gbrt_bvh *bvh = nullptr;
 	int device = 0;
@@ -3292,9 +3418,26 @@ struct gbrt_scene {
 	// shading normals (gbrt_scene_set_normals)
 	float4 *vnrm = nullptr;
 	uint4 *face_nrm = nullptr;
+	// noise tables of the procedural textures (gbrt_scene_set_noise_tables)
+	uint8_t *noise_dev = nullptr;
 	std::vector<DevMaterial> mats_host;
 	std::mutex mu;
 };
+
+// Every material plain (the diffuse layer of shinydiffuse alone, an
+// untextured colour, or light_mat) and no shading normals: the scenes
+// k_shade_plain serves.
+static bool plain_scene(const gbrt_scene *S)
+{
+	if(S->face_nrm) return false;
+	for(const DevMaterial &m : S->mats_host)
+	{
+		if(m.type == GBRT_MAT_LIGHT) continue;
+		if(m.type == GBRT_MAT_SHINYDIFFUSE && m.sd == SD_DIFFUSE && m.dtex < 0) continue;
+		return false;
+	}
+	return true;
+}
 
 namespace {
 
@@ -3635,11 +3778,23 @@ int shoot_map(gbrt_scene *S, const SceneDev &sc, bool caustic, uint32_t n, int m
 	return GBRT_OK;
 }
 
+// Device views of the scene's noise tables (one allocation: hash 512 B,
+// stdp_p 514 B padded to 1,032 B, then the float tables).
+constexpr size_t kNoiseHash = 0, kNoiseStdpP = 512, kNoiseFloats = 1040;
+constexpr size_t kNoiseBytes = kNoiseFloats + 4 * (768 + 768 + 514 * 3);
+gbrt::NoiseTables noise_view(const gbrt_scene *S)
+{
+	if(!S->noise_dev) return gbrt::NoiseTables{nullptr, nullptr, nullptr, nullptr, nullptr};
+	const uint8_t *b = S->noise_dev;
+	const float *f = reinterpret_cast<const float *>(b + kNoiseFloats);
+	return gbrt::NoiseTables{b + kNoiseHash, f, f + 768, b + kNoiseStdpP, f + 1536};
+}
+
 SceneDev scene_dev(const gbrt_scene *S)
 {
 	return SceneDev{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off, S->lds_sfac_nd,
 	                                                                         S->lds_fx, S->lds_fx_dims, S->lds_fx_rad3},
-	                S->tex, S->texels, S->uv, S->face_uv, S->vnrm, S->face_nrm};
+	                S->tex, S->texels, S->uv, S->face_uv, S->vnrm, S->face_nrm, noise_view(S)};
 }
 
 } // namespace
@@ -3881,17 +4036,34 @@ int gbrt_scene_set_textures(gbrt_scene *S, const float *uv, uint32_t n_uv, const
 	for(uint32_t i = 0; i < n_textures; ++i)
 	{
 		const gbrt_texture_desc &t = textures[i];
-		if(t.width <= 0 || t.height <= 0 || !t.rgba)
+		const bool image = t.kind == GBRT_TEX_IMAGE;
+		if(t.kind > GBRT_TEX_RGB_CUBE) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u: kind %u", i, t.kind);
+		if(image && (t.width <= 0 || t.height <= 0 || !t.rgba))
 			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u has no image (%d x %d)", i, t.width, t.height);
 		// the lookups index a texture's texels with 32-bit ints (y * w + x)
-		if(static_cast<uint64_t>(t.width) * static_cast<uint64_t>(t.height) >= (1ull << 31))
+		if(image && static_cast<uint64_t>(t.width) * static_cast<uint64_t>(t.height) >= (1ull << 31))
 			return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_scene_set_textures: texture %u has %d x %d texels (at most 2^31 - 1 per texture)",
 			                      i, t.width, t.height);
-		if(t.interpolate > GBRT_INTERP_BILINEAR || t.clipping > GBRT_CLIP_CHECKER || t.texco > GBRT_TEXCO_UV || t.mapping > GBRT_MAPPING_CUBE)
+		if(t.interpolate > GBRT_INTERP_BILINEAR || t.clipping > GBRT_CLIP_CHECKER || t.texco > GBRT_TEXCO_UV || t.mapping > GBRT_MAPPING_SPHERE)
 			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u: unsupported interpolate / clipping / texco / mapping", i);
 		DevTexture &d = tex[i];
+		d.kind = t.kind;
+		if(!image)
+		{
+			if(!S->noise_dev)
+				return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u is procedural: set the noise tables first", i);
+			const gbrt_procedural_desc &q = t.proc;
+			if(q.noise_type > GBRT_NOISE_VORONOI_CRACKLE || q.noise_type2 > GBRT_NOISE_VORONOI_CRACKLE || q.distance_metric > GBRT_DIST_MINKOVSKY ||
+			   q.bias > GBRT_BIAS_NEGATIVE || q.shape > GBRT_SHAPE_TRI || q.wood_type > GBRT_WOOD_RINGS ||
+			   q.blend_type > GBRT_PROGRESSION_RADIAL || q.color_mode > GBRT_VORONOI_POSITION_OUTLINE_INTENSITY ||
+			   q.musgrave_type > GBRT_MUSGRAVE_RIDGED || q.ramp_mode > GBRT_RAMP_HSL || q.ramp_interpolation > GBRT_RAMP_CONSTANT ||
+			   q.ramp_hue_interpolation > GBRT_HUE_COUNTERCLOCKWISE || q.depth < 0 || q.depth > 30)
+				return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u: procedural parameter out of range", i);
+			if(!gbrt::proc_from_desc(t, d.proc))
+				return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u: %d ramp items (at most %d)", i, q.ramp_n, GBRT_RAMP_MAX);
+		}
 		d.off = static_cast<uint32_t>(n_texels);
-		d.w = t.width; d.h = t.height;
+		d.w = image ? t.width : 0; d.h = image ? t.height : 0;
 		d.interp = t.interpolate; d.clip = t.clipping; d.texco = t.texco; d.mapping = t.mapping;
 		d.xrep = t.xrepeat; d.yrep = t.yrepeat; d.rot90 = t.rot90 ? 1 : 0;
 		for(int k = 0; k < 4; ++k) d.crop[k] = t.crop[k];
@@ -3901,7 +4073,10 @@ int gbrt_scene_set_textures(gbrt_scene *S, const float *uv, uint32_t n_uv, const
 		d.adj_ic = (t.adj_intensity != 1.f || t.adj_contrast != 1.f) ? 1 : 0;
 		d.adj_clamp = t.adj_clamp ? 1 : 0;
 		for(int k = 0; k < 3; ++k) d.mult[k] = t.adj_mult_factor[k];
-		d.adj = (d.adj_ic || d.adj_clamp || t.adj_mult_factor[0] != 1.f || t.adj_mult_factor[1] != 1.f || t.adj_mult_factor[2] != 1.f) ? 1 : 0;
+		d.saturation = t.adj_saturation;
+		d.hue6 = t.adj_hue / 60.f;
+		d.adj = (d.adj_ic || d.adj_clamp || t.adj_mult_factor[0] != 1.f || t.adj_mult_factor[1] != 1.f || t.adj_mult_factor[2] != 1.f ||
+		         t.adj_saturation != 1.f || t.adj_hue != 0.f) ? 1 : 0;
 		d.layer = t.layer ? 1 : 0;
 		if(t.blend_mode > GBRT_BLEND_LIGHTEN) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u: blend mode %u", i, t.blend_mode);
 		d.blend = static_cast<int>(t.blend_mode);
@@ -3919,12 +4094,13 @@ int gbrt_scene_set_textures(gbrt_scene *S, const float *uv, uint32_t n_uv, const
 			d.scale[k] = t.scale[k];
 			d.offset2[k] = 2.f * t.offset[k];
 		}
-		n_texels += static_cast<size_t>(t.width) * t.height;
+		if(image) n_texels += static_cast<size_t>(t.width) * t.height;
 		if(n_texels >= (1ull << 32)) return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_scene_set_textures: more than 2^32 texels");
 	}
 	std::vector<float4> texels(std::max<size_t>(1, n_texels));
 	for(uint32_t i = 0; i < n_textures; ++i)
-		std::memcpy(&texels[tex[i].off], textures[i].rgba, sizeof(float4) * static_cast<size_t>(textures[i].width) * textures[i].height);
+		if(textures[i].kind == GBRT_TEX_IMAGE)
+			std::memcpy(&texels[tex[i].off], textures[i].rgba, sizeof(float4) * static_cast<size_t>(textures[i].width) * textures[i].height);
 	std::vector<uint4> fuv(std::max<uint32_t>(1, S->n_prims));
 	for(uint32_t f = 0; f < S->n_prims; ++f)
 	{
@@ -3960,6 +4136,24 @@ int gbrt_scene_set_textures(gbrt_scene *S, const float *uv, uint32_t n_uv, const
 	}
 	GBRT_CK(cudaMemcpy(S->mats, mats.data(), mats.size() * sizeof(DevMaterial), cudaMemcpyHostToDevice));
 	S->mats_host = mats;
+	return GBRT_OK;
+}
+
+int gbrt_scene_set_noise_tables(gbrt_scene *S, const gbrt_noise_tables *t)
+{
+	if(!S || !t || !t->hash || !t->hashpntf || !t->hashvectf || !t->stdp_p || !t->stdp_g)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_noise_tables: NULL argument");
+	std::vector<uint8_t> b(kNoiseBytes, 0);
+	std::memcpy(b.data() + kNoiseHash, t->hash, 512);
+	std::memcpy(b.data() + kNoiseStdpP, t->stdp_p, 514);
+	float *f = reinterpret_cast<float *>(b.data() + kNoiseFloats);
+	std::memcpy(f, t->hashpntf, 4 * 768);
+	std::memcpy(f + 768, t->hashvectf, 4 * 768);
+	std::memcpy(f + 1536, t->stdp_g, 4 * 514 * 3);
+	std::lock_guard<std::mutex> lock(S->mu);
+	if(S->ev_last) GBRT_CK(cudaEventSynchronize(S->ev_last));
+	if(!S->noise_dev) GBRT_CK(cudaMalloc(reinterpret_cast<void **>(&S->noise_dev), kNoiseBytes));
+	GBRT_CK(cudaMemcpy(S->noise_dev, b.data(), kNoiseBytes, cudaMemcpyHostToDevice));
 	return GBRT_OK;
 }
 
@@ -4005,7 +4199,7 @@ int gbrt_scene_destroy(gbrt_scene *S)
 	                S->lds_sfac_nd, S->lds_fx, S->work, S->spawn, S->spawn_count};
 	for(void *p : ptrs) if(p) cudaFree(p);
 	for(void *p : {static_cast<void *>(S->tex), static_cast<void *>(S->texels), static_cast<void *>(S->uv), static_cast<void *>(S->face_uv),
-	               static_cast<void *>(S->vnrm), static_cast<void *>(S->face_nrm)})
+	               static_cast<void *>(S->vnrm), static_cast<void *>(S->face_nrm), static_cast<void *>(S->noise_dev)})
 		if(p) cudaFree(p);
 	if(S->filter_dev) cudaFree(S->filter_dev);
 	if(S->ev_last) cudaEventDestroy(S->ev_last);
@@ -4185,6 +4379,8 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	Work W = S->w;
 	if(!record) W.p_sum = nullptr;
 	float *film = film64_dev ? nullptr : film_dev;
+	// the lean shading kernel serves pathtracing over plain scenes
+	const bool plain = !pm && plain_scene(S);
 	cudaEvent_t e0 = nullptr, e1 = nullptr;
 	if(stats)
 	{
@@ -4211,7 +4407,10 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 				k_pm_root<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, film, film64_dev);
 			if(level_guided)
 				if(int rc = gbrt_guide_eval_queue(guide, Ww.hitpos, n, Ww.count + cur, Ww.lobes, s)) return rc;
-			k_shade<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+			if(plain && !Pw.guiding && !Pw.record)
+				k_shade_plain<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+			else
+				k_shade<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
 			const uint32_t scap = static_cast<uint32_t>(shadow_cap);
 			if(Pw.film_w && Pw.tshadow)
 				k_shadow<true, true><<<persistent_grid(k_shadow<true, true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, scap, film, film64_dev);

@@ -96,6 +96,27 @@ def sppm_params(it):
                       int(bool(it.get("pmIRE", False))), float(it.get("photonRadius", 1.0)), int(it.get("searchNum", 10)))
 
 
+RAMP_MAX = 16
+
+
+class ProceduralDesc(ctypes.Structure):
+    _fields_ = [("noise_type", ctypes.c_uint32), ("noise_type2", ctypes.c_uint32), ("color1", ctypes.c_float * 3),
+                ("color2", ctypes.c_float * 3), ("size", ctypes.c_float), ("depth", ctypes.c_int32), ("hard", ctypes.c_int32),
+                ("bias", ctypes.c_uint32), ("shape", ctypes.c_uint32), ("wood_type", ctypes.c_uint32),
+                ("blend_type", ctypes.c_uint32), ("use_flip_axis", ctypes.c_int32), ("sharpness", ctypes.c_float),
+                ("turbulence", ctypes.c_float), ("distance_metric", ctypes.c_uint32), ("color_mode", ctypes.c_uint32),
+                ("weight", ctypes.c_float * 4), ("mk_exponent", ctypes.c_float), ("intensity", ctypes.c_float),
+                ("musgrave_type", ctypes.c_uint32), ("h", ctypes.c_float), ("lacunarity", ctypes.c_float),
+                ("octaves", ctypes.c_float), ("offset", ctypes.c_float), ("gain", ctypes.c_float), ("distort", ctypes.c_float),
+                ("ramp_n", ctypes.c_int32), ("ramp_mode", ctypes.c_uint32), ("ramp_interpolation", ctypes.c_uint32),
+                ("ramp_hue_interpolation", ctypes.c_uint32), ("ramp", (ctypes.c_float * 5) * RAMP_MAX)]
+
+
+class NoiseTablesDesc(ctypes.Structure):
+    _fields_ = [("hash", ctypes.c_void_p), ("hashpntf", ctypes.c_void_p), ("hashvectf", ctypes.c_void_p),
+                ("stdp_p", ctypes.c_void_p), ("stdp_g", ctypes.c_void_p)]
+
+
 class TextureDesc(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("rgba", ctypes.c_void_p),
                 ("interpolate", ctypes.c_uint32), ("clipping", ctypes.c_uint32), ("xrepeat", ctypes.c_int32),
@@ -107,26 +128,104 @@ class TextureDesc(ctypes.Structure):
                 ("colfac", ctypes.c_float), ("upper_color", ctypes.c_float * 4), ("def_col", ctypes.c_float * 3),
                 ("negative", ctypes.c_int32), ("no_rgb", ctypes.c_int32), ("stencil", ctypes.c_int32),
                 ("mirror_x", ctypes.c_int32), ("mirror_y", ctypes.c_int32), ("even_tiles", ctypes.c_int32),
-                ("odd_tiles", ctypes.c_int32), ("checker_dist", ctypes.c_float)]
+                ("odd_tiles", ctypes.c_int32), ("checker_dist", ctypes.c_float), ("kind", ctypes.c_uint32),
+                ("adj_saturation", ctypes.c_float), ("adj_hue", ctypes.c_float), ("proc", ProceduralDesc)]
 
 
 # ImageTexture / TextureMapperNode enum names (texture_image.h, shader_node_texture.h)
 TEXCO = {"global": 0, "uv": 1}
-MAPPING = {"plain": 0, "cube": 1}
+MAPPING = {"plain": 0, "cube": 1, "tube": 2, "sphere": 3}
+# Texture::Type and the procedural textures' enum names (include/texture/*.h,
+# include/noise/*.h, include/color/color_ramp.h)
+TEX_KINDS = {"image": 0, "blend": 1, "clouds": 2, "marble": 3, "wood": 4, "voronoi": 5, "musgrave": 6, "distorted_noise": 7,
+             "rgb_cube": 8}
+NOISE_TYPES = {"blender": 0, "stdperlin": 1, "newperlin": 2, "cellnoise": 3, "voronoi_f1": 4, "voronoi_f2": 5, "voronoi_f3": 6,
+               "voronoi_f4": 7, "voronoi_f2f1": 8, "voronoi_crackle": 9}
+DISTANCE_METRICS = {"real": 0, "squared": 1, "manhattan": 2, "chebychev": 3, "minkovsky_half": 4, "minkovsky_four": 5,
+                    "minkovsky": 6}
+PROGRESSIONS = {"linear": 0, "quadratic": 1, "easing": 2, "diagonal": 3, "sphere": 4, "quad_sphere": 5, "radial": 6}
+BIASES = {"none": 0, "positive": 1, "negative": 2}
+SHAPES = {"sin": 0, "saw": 1, "tri": 2}
+WOOD_TYPES = {"bands": 0, "rings": 1}
+VORONOI_COLOR_MODES = {"intensity-without-color": 0, "position": 1, "position-outline": 2, "position-outline-intensity": 3}
+MUSGRAVE_TYPES = {"fBm": 0, "multifractal": 1, "heteroterrain": 2, "hybridmf": 3, "ridgedmf": 4}
+RAMP_MODES = {"RGB": 0, "HSV": 1, "HSL": 2}
+RAMP_INTERPOLATIONS = {"LINEAR": 0, "CONSTANT": 1}
+HUE_INTERPOLATIONS = {"NEAR": 0, "FAR": 1, "CW": 2, "CCW": 3}
+
+
+def procedural_desc(t):
+    """gbrt_procedural_desc of a procedural texture dict (the reference's
+    parameter names; missing ones take its defaults)."""
+    p = ProceduralDesc()
+    load().gbrt_procedural_defaults(ctypes.byref(p))
+    kind = t["type"]
+    p.noise_type = NOISE_TYPES[t.get("noise_type1" if kind == "distorted_noise" else "noise_type", "newperlin")]
+    p.noise_type2 = NOISE_TYPES[t.get("noise_type2", "newperlin")]
+    p.color1[:] = [float(x) for x in t.get("color1", (0.0, 0.0, 0.0))][:3]
+    p.color2[:] = [float(x) for x in t.get("color2", (1.0, 1.0, 1.0))][:3]
+    p.size = float(t.get("size", 1.0))
+    p.depth = int(t.get("depth", 2))
+    p.hard = int(bool(t.get("hard", False)))
+    p.bias = BIASES[t.get("bias", "none")]
+    p.shape = SHAPES[t.get("shape", "sin")]
+    p.wood_type = WOOD_TYPES[t.get("wood_type", "bands")]
+    p.blend_type = PROGRESSIONS[t.get("blend_type", "linear")]
+    p.use_flip_axis = int(bool(t.get("use_flip_axis", False)))
+    p.sharpness = float(t.get("sharpness", 1.0))
+    p.turbulence = float(t.get("turbulence", 1.0))
+    p.distance_metric = DISTANCE_METRICS[t.get("distance_metric", "real")]
+    p.color_mode = VORONOI_COLOR_MODES[t.get("color_mode", "intensity-without-color")]
+    p.weight[:] = [float(t.get(f"weight{i}", 1.0 if i == 1 else 0.0)) for i in range(1, 5)]
+    p.mk_exponent = float(t.get("mk_exponent", 2.5))
+    p.intensity = float(t.get("intensity", 1.0))
+    p.musgrave_type = MUSGRAVE_TYPES[t.get("musgrave_type", "fBm")]
+    p.h, p.lacunarity, p.octaves = float(t.get("H", 1.0)), float(t.get("lacunarity", 2.0)), float(t.get("octaves", 2.0))
+    p.offset, p.gain = float(t.get("offset", 1.0)), float(t.get("gain", 1.0))
+    p.distort = float(t.get("distort", 1.0))
+    n = int(t.get("ramp_num_items", 0))
+    if n > RAMP_MAX:
+        raise ValueError(f"at most {RAMP_MAX} ramp items")
+    p.ramp_n = n
+    p.ramp_mode = RAMP_MODES[t.get("ramp_color_mode", "RGB")]
+    p.ramp_interpolation = RAMP_INTERPOLATIONS[t.get("ramp_interpolation", "LINEAR")]
+    p.ramp_hue_interpolation = HUE_INTERPOLATIONS[t.get("ramp_hue_interpolation", "NEAR")]
+    for i in range(n):
+        c = [float(x) for x in t.get(f"ramp_item_{i}_color", (0.0, 0.0, 0.0, 1.0))]
+        p.ramp[i][:] = [*c[:4], float(t.get(f"ramp_item_{i}_position", 0.0))]
+    return p
 CLIPPING = {"extend": 0, "clip": 1, "clipcube": 2, "repeat": 3, "checker": 4}
 INTERPOLATE = {"none": 0, "bilinear": 1}
 BLEND_MODES = {"mix": 0, "add": 1, "multiply": 2, "subtract": 3, "screen": 4, "divide": 5, "difference": 6, "darken": 7,
                "lighten": 8}
 
 
+def mapper_of(t):
+    """The texture-mapper node parameters of a scene texture entry (texco,
+    mapping, scale, offset, proj): its "mapper" dict, or, for an image
+    texture, the entry itself (musgrave's own "offset" would clash)."""
+    if "mapper" in t:
+        return t["mapper"]
+    return t if t.get("type", "image") == "image" else {}
+
+
 def texture_desc(t):
     """gbrt_texture_desc of a scene "textures" entry (image [h, w, 4] float32
     plus the reference's texture and texture-mapper parameter names); the
-    image array must stay alive until the call that takes the desc."""
-    img = np.ascontiguousarray(t["image"], np.float32)
+    image array must stay alive until the call that takes the desc.  A
+    procedural texture ("type" other than "image", no image) carries its
+    parameters in the desc's proc part (procedural_desc)."""
     d = TextureDesc()
-    d.height, d.width = int(img.shape[0]), int(img.shape[1])
-    d.rgba = img.ctypes.data
+    kind = t.get("type", "image")
+    d.kind = TEX_KINDS[kind]
+    d.adj_saturation, d.adj_hue = float(t.get("adj_saturation", 1.0)), float(t.get("adj_hue", 0.0))
+    if kind == "image":
+        img = np.ascontiguousarray(t["image"], np.float32)
+        d.height, d.width = int(img.shape[0]), int(img.shape[1])
+        d.rgba = img.ctypes.data
+    else:
+        img = None
+        d.proc = procedural_desc(t)
     d.interpolate = INTERPOLATE[t.get("interpolate", "bilinear")]
     d.clipping = CLIPPING[t.get("clipping", "repeat")]
     d.xrepeat, d.yrepeat = int(t.get("xrepeat", 1)), int(t.get("yrepeat", 1))
@@ -140,11 +239,12 @@ def texture_desc(t):
     d.adj_mult_factor[:] = [float(t.get("adj_mult_factor_red", 1.0)), float(t.get("adj_mult_factor_green", 1.0)),
                             float(t.get("adj_mult_factor_blue", 1.0))]
     d.adj_clamp = int(bool(t.get("adj_clamp", False)))
-    d.texco = TEXCO[t.get("texco", "global")]
-    d.mapping = MAPPING[t.get("mapping", "plain")]
-    d.scale[:] = [float(x) for x in t.get("scale", (1.0, 1.0, 1.0))]
-    d.offset[:] = [float(x) for x in t.get("offset", (0.0, 0.0, 0.0))]
-    d.proj[:] = [int(x) for x in t.get("proj", (1, 2, 3))]
+    mp = mapper_of(t)
+    d.texco = TEXCO[mp.get("texco", "global")]
+    d.mapping = MAPPING[mp.get("mapping", "plain")]
+    d.scale[:] = [float(x) for x in mp.get("scale", (1.0, 1.0, 1.0))]
+    d.offset[:] = [float(x) for x in mp.get("offset", (0.0, 0.0, 0.0))]
+    d.proj[:] = [int(x) for x in mp.get("proj", (1, 2, 3))]
     lay = t.get("layer")
     d.layer = int(lay is not None)
     lay = lay or {}
@@ -276,6 +376,9 @@ SIGNATURES = {
     "gbrt_scene_set_textures": (_I, [_VP, _VP, _U32, _VP, ctypes.POINTER(TextureDesc), _U32, _VP, _U32]),
     "gbrt_mesh_smooth_normals": (_I, [_VP, _U32, _VP, _U32, ctypes.c_float, _VP, _U32, ctypes.POINTER(_U32), _VP]),
     "gbrt_scene_set_normals": (_I, [_VP, _VP, _U32, _VP]),
+    "gbrt_procedural_defaults": (None, [ctypes.POINTER(ProceduralDesc)]),
+    "gbrt_scene_set_noise_tables": (_I, [_VP, ctypes.POINTER(NoiseTablesDesc)]),
+    "gbrt_texture_eval": (_I, [ctypes.POINTER(TextureDesc), ctypes.POINTER(NoiseTablesDesc), _VP, _U32, _VP, _VP, ctypes.c_int]),
     "gbrt_pm_render_aa_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP, ctypes.POINTER(AaParams),
                                     _VP, ctypes.POINTER(PtStats), _VP]),
     "gbrt_dl_render_aa_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP, ctypes.POINTER(AaParams),
@@ -458,6 +561,30 @@ NO_NORMAL = 0xFFFFFFFF
 FLAT_FACE = 0xFFFFFFFE
 
 
+def noise_tables(tables):
+    """gbrt_noise_tables of a dict of the reference's noise tables (hash
+    uint8 [512], hashpntf float32 [768], hashvectf float32 [768], stdp_p
+    uint8 [514], stdp_g float32 [514, 3]); returns (desc, arrays to keep)."""
+    keep = [np.ascontiguousarray(tables["hash"], np.uint8).reshape(512),
+            np.ascontiguousarray(tables["hashpntf"], np.float32).reshape(768),
+            np.ascontiguousarray(tables["hashvectf"], np.float32).reshape(768),
+            np.ascontiguousarray(tables["stdp_p"], np.uint8).reshape(514),
+            np.ascontiguousarray(tables["stdp_g"], np.float32).reshape(514 * 3)]
+    return NoiseTablesDesc(*[a.ctypes.data for a in keep]), keep
+
+
+def texture_eval(texture, tables, points, on_device=False):
+    """gbrt_texture_eval: a procedural texture dict's getColor (RGBA [n, 4])
+    and getFloat ([n]) at texture-space points [n, 3]."""
+    d, _ = texture_desc(texture)
+    nt, keep = noise_tables(tables)
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    rgba = np.empty((max(1, len(pts)), 4), np.float32)
+    val = np.empty(max(1, len(pts)), np.float32)
+    check(load().gbrt_texture_eval(ctypes.byref(d), ctypes.byref(nt), _ptr(pts), len(pts), _ptr(rgba), _ptr(val), int(bool(on_device))))
+    return rgba[:len(pts)], val[:len(pts)]
+
+
 def smooth_normals(vertices, faces, angle):
     """The reference's yafaray_smoothObjectMesh(angle) on one mesh object,
     by gbrt_mesh_smooth_normals: (normals float32 [n, 3], face normal
@@ -546,10 +673,15 @@ class Renderer:
         check(load().gbrt_scene_set_normals(self._h, _ptr(normals), len(normals), _ptr(face_normals)))
 
     def _set_textures(self):
-        """Image textures of the scene's "textures" entry on the shinydiffuse
-        materials whose options name one ("diffuse_texture")."""
+        """Image and procedural textures of the scene's "textures" entry on
+        the shinydiffuse materials whose options name one
+        ("diffuse_texture"); procedural textures need the scene's
+        "noise_tables" (the reference's NoiseGenerator tables)."""
         from . import scenes as _scenes
         names = list(self.scene["textures"].keys())
+        if any(self.scene["textures"][n].get("type", "image") != "image" for n in names):
+            nt, self._noise_keep = noise_tables(self.scene["noise_tables"])
+            check(load().gbrt_scene_set_noise_tables(self._h, ctypes.byref(nt)))
         descs, keep = (TextureDesc * len(names))(), []
         for i, n in enumerate(names):
             d, img = texture_desc(self.scene["textures"][n])

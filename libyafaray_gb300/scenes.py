@@ -437,6 +437,49 @@ def textured_cornell_scene(res=64, **kw):
     return sc
 
 
+def procedural_cornell_scene(noise_tables, res=64, **kw):
+    """The Cornell box with procedural textures on every surface
+    (noise_tables: the reference's noise tables, as gbrt.noise_tables
+    takes them): marble over the floor / ceiling / back wall (global
+    coordinates, scale 2), blender-noise clouds through an HSV colour ramp
+    on the red wall, voronoi position-outline colour cells on the green
+    wall, wood rings (saw) on the short box through a multiply layer node
+    over the material colour, a ridged Musgrave fractal on the tall box
+    through tube mapping with colour adjustments, and distorted noise on
+    the light's emitter surround.  Everything else is the plain Cornell
+    box."""
+    sc = cornell_scene(res=res, **kw)
+    sc["noise_tables"] = noise_tables
+    sc["textures"] = {
+        "marble": {"type": "marble", "noise_type": "newperlin", "depth": 3, "turbulence": 4.0, "sharpness": 2.0,
+                   "color1": (0.85, 0.82, 0.75), "color2": (0.35, 0.3, 0.28), "mapper": {"scale": (2.0, 2.0, 2.0)}},
+        "clouds": {"type": "clouds", "noise_type": "blender", "depth": 3, "size": 0.6, "hard": True,
+                   "ramp_num_items": 3, "ramp_color_mode": "HSV", "ramp_item_0_color": (0.7, 0.05, 0.05, 1.0),
+                   "ramp_item_0_position": 0.2, "ramp_item_1_color": (0.9, 0.5, 0.1, 1.0), "ramp_item_1_position": 0.5,
+                   "ramp_item_2_color": (0.5, 0.1, 0.4, 1.0), "ramp_item_2_position": 0.8},
+        "cells": {"type": "voronoi", "color_mode": "position-outline", "distance_metric": "manhattan", "size": 4.0,
+                  "weight1": 1.0, "weight2": -0.4, "adj_mult_factor_green": 1.2, "adj_saturation": 0.7},
+        "wood": {"type": "wood", "wood_type": "rings", "shape": "saw", "noise_type": "stdperlin", "turbulence": 0.4,
+                 "depth": 2, "color1": (0.6, 0.35, 0.15), "color2": (0.95, 0.75, 0.45), "mapper": {"scale": (3.0, 3.0, 3.0)},
+                 "layer": {"blend_mode": "multiply", "colfac": 0.9, "upper_color": (0.75, 0.75, 0.75, 1.0)}},
+        "fractal": {"type": "musgrave", "musgrave_type": "ridgedmf", "noise_type": "newperlin", "octaves": 3.5, "H": 0.9,
+                    "lacunarity": 2.1, "offset": 1.0, "gain": 1.6, "intensity": 0.55, "size": 1.7,
+                    "color1": (0.2, 0.3, 0.6), "color2": (0.95, 0.95, 0.8), "adj_contrast": 1.2, "adj_clamp": True,
+                    "mapper": {"mapping": "tube", "scale": (1.0, 1.0, 1.0), "offset": (0.1, 0.0, 0.0)}},
+    }
+    for name, tex in (("grey", "marble"), ("red", "clouds"), ("green", "cells")):
+        m = sc["materials"][name]
+        sc["materials"][name] = ("shinydiffusemat", m[1], {"diffuse_texture": tex})
+    sc["materials"]["short_tex"] = ("shinydiffusemat", (0.75, 0.75, 0.75), {"diffuse_texture": "wood"})
+    sc["materials"]["tall_tex"] = ("shinydiffusemat", (0.75, 0.75, 0.75), {"diffuse_texture": "fractal"})
+    for o in sc["objects"]:
+        if o["name"] == "group3":
+            o["material"] = "short_tex"
+        elif o["name"] == "group4":
+            o["material"] = "tall_tex"
+    return sc
+
+
 def cornell_sppm_scene(res=48, photons=100000, passes=8, bounces=5, pm_ire=False, photon_radius=0.1, search_num=10):
     """The glass Cornell box (a glass and a rough-glass ball) rendered by the
     "SPPM" integrator: caustics under the balls come from the photon

@@ -166,6 +166,9 @@ def reference_scene_text(scene, spp, batches, threads=-1, offset_stride=None):
             return ",".join(repr(float(x)) for x in v)
         return repr(v)
     for tname, tx in scene.get("textures", {}).items():
+        if tx.get("type", "image") != "image":
+            out.append(f"texture {tname} {texture_spec({k: v for k, v in tx.items() if k != 'mapper'})}")
+            continue
         img = np.asarray(tx["image"], np.float32)
         h, w = img.shape[:2]
         out.append(f"image {tname}_img {w} {h}")
@@ -179,11 +182,12 @@ def reference_scene_text(scene, spp, batches, threads=-1, offset_stride=None):
             for k, v in (m[2] if len(m) > 2 else {}).items():
                 if k == "diffuse_texture":
                     tx = scene["textures"][v]
+                    mp = tx.get("mapper", tx if tx.get("type", "image") == "image" else {})
                     node = f"{name}_dtex"
-                    proj = tx.get("proj", (1, 2, 3))
-                    out.append(f"node name={node} type=texture_mapper texture={v} texco={tx.get('texco', 'global')} "
-                               f"mapping={tx.get('mapping', 'plain')} scale={fmt(tx.get('scale', (1.0, 1.0, 1.0)))} "
-                               f"offset={fmt(tx.get('offset', (0.0, 0.0, 0.0)))} proj_x={proj[0]} proj_y={proj[1]} proj_z={proj[2]}")
+                    proj = mp.get("proj", (1, 2, 3))
+                    out.append(f"node name={node} type=texture_mapper texture={v} texco={mp.get('texco', 'global')} "
+                               f"mapping={mp.get('mapping', 'plain')} scale={fmt(mp.get('scale', (1.0, 1.0, 1.0)))} "
+                               f"offset={fmt(mp.get('offset', (0.0, 0.0, 0.0)))} proj_x={proj[0]} proj_y={proj[1]} proj_z={proj[2]}")
                     lay = tx.get("layer")
                     if lay is not None:
                         layer = f"{name}_dlayer"
@@ -379,3 +383,63 @@ def run_reference_translation(scene, spp=1):
     out["ok"] = struct.unpack("<i", raw[o:o + 4])[0] == 0
     out["error"] = raw[o + 4:].decode()
     return out
+
+
+REF_NOISE = os.path.join(HERE, "_ref", "noise_dump")
+
+
+def _tex_value(k, v):
+    if isinstance(v, bool):
+        return str(v).lower()
+    if isinstance(v, str):
+        return v
+    if isinstance(v, (tuple, list)):
+        vals = [float(x) for x in v]
+        if k in ("color1", "color2") and len(vals) == 3:
+            vals.append(1.0)                      # a colour parameter, not a vector
+        return ",".join(repr(x) for x in vals)
+    return repr(v)
+
+
+def texture_spec(t):
+    """A procedural texture dict as a noise_dump / render_dump "texture"
+    statement's key=value list."""
+    return " ".join(f"{k}={_tex_value(k, v)}" for k, v in t.items() if k not in ("mapper", "layer"))
+
+
+def run_reference_textures(textures, points, noises=(), turbulences=()):
+    """The reference's noise tables, and its procedural textures evaluated at
+    texture-space points (oracle/_ref/noise_dump): returns (tables dict,
+    [(status, rgba [n, 4], value [n]) per texture], [noise values [n] per
+    noise type], [turbulence values [n] per (type, oct, size, hard)])."""
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    lines = [f"points {len(pts)}"] + [f"{float(a)!r} {float(b)!r} {float(c)!r}" for a, b, c in pts] + ["tables"]
+    lines += [f"noise {n}" for n in noises]
+    lines += [f"turbulence {n} {int(o)} {float(s)!r} {int(h)}" for n, o, s, h in turbulences]
+    lines += [f"texture {texture_spec(t)}" for t in textures]
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout = os.path.join(d, "spec.txt"), os.path.join(d, "out.bin")
+        open(fin, "w").write("\n".join(lines) + "\n")
+        subprocess.run([REF_NOISE, fin, fout], check=True, stdout=subprocess.DEVNULL)
+        raw = open(fout, "rb").read()
+    n = len(pts)
+    o = 0
+    tables = {}
+    for key, dt, cnt in (("hash", np.uint8, 512), ("hashpntf", np.float32, 768), ("hashvectf", np.float32, 768),
+                         ("stdp_p", np.uint8, 514), ("stdp_g", np.float32, 514 * 3)):
+        a = np.frombuffer(raw, dt, cnt, o).copy()
+        o += a.nbytes
+        tables[key] = a
+    nz = []
+    for _ in noises:
+        nz.append(np.frombuffer(raw, np.float32, n, o).copy()); o += 4 * n
+    tb = []
+    for _ in turbulences:
+        tb.append(np.frombuffer(raw, np.float32, n, o).copy()); o += 4 * n
+    tex = []
+    for _ in textures:
+        status = struct.unpack("<i", raw[o:o + 4])[0]; o += 4
+        rgba = np.frombuffer(raw, np.float32, 4 * n, o).reshape(n, 4).copy(); o += 16 * n
+        val = np.frombuffer(raw, np.float32, n, o).copy(); o += 4 * n
+        tex.append((status, rgba, val))
+    return tables, tex, nz, tb

@@ -10,10 +10,13 @@ occlusion (Accelerator::isShadowed) as a hit flag, plus the tree bound.
 
     python tests/golden/make_golden.py normals   # smooth_normals.npz only
     python tests/golden/make_golden.py binding   # binding_translation.npz only
+    python tests/golden/make_golden.py procedural   # procedural.npz only
 
 smooth_normals.npz holds the reference's yafaray_smoothObjectMesh results;
 binding_translation.npz the scenes the reference-side binding
-(oracle/ref/gb300_binding.cc) translates for the GPU library.
+(oracle/ref/gb300_binding.cc) translates for the GPU library;
+procedural.npz the reference's noise tables and procedural textures
+evaluated at seeded points (oracle/_ref/noise_dump).
 """
 import os
 import sys
@@ -180,10 +183,83 @@ def binding_golden():
     print(f"binding_translation.npz: {len(BINDING_CASES)} scenes")
 
 
+def procedural_cases():
+    """The procedural textures the golden covers: every texture type, every
+    noise generator, every voronoi metric and colour mode, every Musgrave
+    type, every blend progression, colour ramps in each mode and hue
+    interpolation, and the colour adjustments."""
+    ramp3 = {"ramp_num_items": 3, "ramp_item_0_color": (1.0, 0.1, 0.0, 1.0), "ramp_item_0_position": 0.15,
+             "ramp_item_1_color": (0.1, 0.9, 0.2, 0.5), "ramp_item_1_position": 0.55,
+             "ramp_item_2_color": (0.2, 0.1, 1.0, 0.8), "ramp_item_2_position": 0.85}
+    cases = []
+    noises = ["blender", "stdperlin", "newperlin", "cellnoise", "voronoi_f1", "voronoi_f2", "voronoi_f3", "voronoi_f4",
+              "voronoi_f2f1", "voronoi_crackle"]
+    for i, n in enumerate(noises):
+        cases.append({"type": "clouds", "noise_type": n, "depth": i % 4, "size": 0.6 + 0.1 * i, "hard": i % 2 == 1,
+                      "color1": (0.1, 0.2, 0.3), "color2": (0.9, 0.7, 0.4)})
+    cases += [{"type": "clouds", "noise_type": "blender", "bias": "positive", "depth": 3},
+              {"type": "clouds", "noise_type": "stdperlin", "bias": "negative", "depth": 2, "hard": True}]
+    for i, (shape, n) in enumerate([("sin", "newperlin"), ("saw", "blender"), ("tri", "voronoi_f1")]):
+        cases.append({"type": "marble", "shape": shape, "noise_type": n, "sharpness": 1.0 + 1.5 * i, "turbulence": 2.0 + i,
+                      "depth": 1 + i, "hard": i == 1})
+        cases.append({"type": "wood", "shape": shape, "noise_type": n, "wood_type": "rings" if i % 2 else "bands",
+                      "turbulence": 0.0 if i == 2 else 0.7, "depth": i, "size": 0.8})
+    metrics = ["real", "squared", "manhattan", "chebychev", "minkovsky_half", "minkovsky_four", "minkovsky"]
+    modes = ["intensity-without-color", "position", "position-outline", "position-outline-intensity"]
+    for i, m in enumerate(metrics):
+        cases.append({"type": "voronoi", "distance_metric": m, "color_mode": modes[i % 4], "mk_exponent": 1.7, "size": 1.3,
+                      "weight1": 1.0, "weight2": -0.5 if i % 2 else 0.3, "weight3": 0.2 * (i % 3), "weight4": 0.1,
+                      "intensity": 0.9})
+    for i, (mt, n) in enumerate([("fBm", "newperlin"), ("multifractal", "blender"), ("heteroterrain", "stdperlin"),
+                                 ("hybridmf", "voronoi_crackle"), ("ridgedmf", "newperlin")]):
+        cases.append({"type": "musgrave", "musgrave_type": mt, "noise_type": n, "octaves": 2.0 + 0.75 * i, "H": 0.6 + 0.1 * i,
+                      "lacunarity": 2.2, "offset": 0.9 + 0.1 * i, "gain": 1.3, "intensity": 0.8, "size": 0.7})
+    cases += [{"type": "distorted_noise", "noise_type1": "blender", "noise_type2": "voronoi_f2f1", "distort": 1.5, "size": 0.8},
+              {"type": "distorted_noise", "noise_type1": "stdperlin", "noise_type2": "cellnoise", "distort": 0.4}]
+    for bt in ["linear", "quadratic", "easing", "diagonal", "sphere", "quad_sphere", "radial"]:
+        cases.append({"type": "blend", "blend_type": bt, "use_flip_axis": bt in ("easing", "diagonal")})
+    cases.append({"type": "rgb_cube"})
+    cases.append({"type": "rgb_cube", "adj_contrast": 1.4, "adj_clamp": True})
+    for mode, interp, hue in [("RGB", "LINEAR", "NEAR"), ("RGB", "CONSTANT", "NEAR"), ("HSV", "LINEAR", "NEAR"),
+                              ("HSV", "LINEAR", "FAR"), ("HSV", "LINEAR", "CW"), ("HSL", "LINEAR", "CCW")]:
+        cases.append({"type": "clouds", "noise_type": "newperlin", "depth": 2, **ramp3, "ramp_color_mode": mode,
+                      "ramp_interpolation": interp, "ramp_hue_interpolation": hue})
+    cases.append({"type": "voronoi", "color_mode": "position", **ramp3})
+    cases.append({"type": "blend", "blend_type": "sphere", **ramp3, "ramp_color_mode": "HSV"})
+    cases += [{"type": "clouds", "adj_intensity": 1.2, "adj_contrast": 0.8, "adj_saturation": 0.5, "adj_hue": 30.0,
+               "adj_mult_factor_red": 1.3, "color1": (0.2, 0.4, 0.1), "color2": (0.9, 0.3, 0.6)},
+              {"type": "marble", "adj_mult_factor_green": 0.5, "adj_hue": -50.0, "adj_clamp": True, "color1": (0.9, 0.2, 0.1)},
+              {"type": "voronoi", "color_mode": "position-outline-intensity", "adj_intensity": 0.7, "adj_saturation": 1.6}]
+    return cases
+
+
+def procedural_golden():
+    """procedural.npz: the reference's noise tables and, at 768 seeded
+    texture-space points, each case of procedural_cases: getColor RGBA and
+    getFloat (oracle/_ref/noise_dump)."""
+    import json
+    rng = np.random.default_rng(31)
+    pts = np.concatenate([rng.uniform(-3.0, 3.0, (512, 3)), rng.uniform(-0.5, 0.5, (192, 3)),
+                          np.round(rng.uniform(-4, 4, (64, 3))) + rng.choice([0.0, 1e-4, -1e-4, 0.5], (64, 3))]).astype(np.float32)
+    cases = procedural_cases()
+    tables, tex, _, _ = orc.run_reference_textures(cases, pts)
+    out = {f"table_{k}": v for k, v in tables.items()}
+    out["points"] = pts
+    out["cases"] = np.array(json.dumps(cases))
+    for i, (status, rgba, val) in enumerate(tex):
+        assert status == 0, cases[i]
+        out[f"rgba_{i}"] = rgba
+        out[f"value_{i}"] = val
+    np.savez_compressed(os.path.join(OUT, "procedural.npz"), **out)
+    print(f"procedural.npz: {len(cases)} textures at {len(pts)} points")
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["normals"]:
         normals_golden()
     elif sys.argv[1:] == ["binding"]:
         binding_golden()
+    elif sys.argv[1:] == ["procedural"]:
+        procedural_golden()
     else:
         main()
