@@ -507,6 +507,47 @@ typedef struct gbrt_noise_tables {
 /* The scene's noise tables, required before gbrt_scene_set_textures takes
  * a procedural texture. */
 int gbrt_scene_set_noise_tables(gbrt_scene *scene, const gbrt_noise_tables *tables);
+/* ---- shader node trees on material colour slots -------------------------
+ * The reference's shader nodes (src/shader/: texture_mapper, value, mix
+ * with its nine blend modes, layer) as a node array; every material colour
+ * slot may name a root node, whose tree (the root and every node it reads,
+ * all at lower indices) is evaluated per surface point as the reference's
+ * Material::evalNodes does.  A texture_mapper node reads a texture of
+ * gbrt_scene_set_textures (its texco / mapping / scale / offset / proj are
+ * the mapper's; the texture's own layer fields are not used here).
+ * Parameter names and defaults [..] are the reference's. */
+enum { GBRT_NODE_TEXTURE = 0, GBRT_NODE_VALUE = 1, GBRT_NODE_MIX = 2, GBRT_NODE_LAYER = 3 };
+/* mix "blend_mode" (shader_node_mix.h:51-66) ["mix"]; layer nodes take GBRT_BLEND_* */
+enum { GBRT_MIX_MIX = 0, GBRT_MIX_ADD = 1, GBRT_MIX_MULTIPLY = 2, GBRT_MIX_SUBTRACT = 3, GBRT_MIX_SCREEN = 4, GBRT_MIX_DIFFERENCE = 5,
+       GBRT_MIX_DARKEN = 6, GBRT_MIX_LIGHTEN = 7, GBRT_MIX_OVERLAY = 8 };
+/* material slots: shinydiffuse / glossy "diffuse_shader", glossy
+ * "glossy_shader", shinydiffuse / glass / rough_glass "mirror_color_shader",
+ * glass / rough_glass "filter_color_shader", "bump_shader" */
+enum { GBRT_SLOT_DIFFUSE = 0, GBRT_SLOT_GLOSSY = 1, GBRT_SLOT_MIRROR_COLOR = 2, GBRT_SLOT_FILTER_COLOR = 3, GBRT_SLOT_BUMP = 4,
+       GBRT_SLOTS = 5 };
+#define GBRT_TREE_MAX 16          /* index span from a root back to the lowest node it reads */
+typedef struct gbrt_shader_node {
+	uint32_t type;              /* GBRT_NODE_* */
+	int32_t texture;            /* texture_mapper: texture index */
+	int32_t do_scalar;          /* texture_mapper "do_scalar" [1]; layer "do_scalar" [0] */
+	/* mix: "input1", "input2", "input_factor"; layer: input1 = "input", input2 = "upper_layer"
+	 * (node indices below this node's, or -1) */
+	int32_t input1, input2, input_factor;
+	float color1[4], color2[4]; /* mix "color1", "color2" [0]; value: color1 = "color" + "alpha" [1, 1];
+	                               layer: color1 = "upper_color" [0] */
+	float value1, value2;       /* mix "value1", "value2" [0]; value: value1 = "scalar" [1]; layer: value1 = "upper_value" [0] */
+	float factor;               /* mix "cfactor" [0.5] */
+	uint32_t mode;              /* mix GBRT_MIX_*; layer "blend_mode" GBRT_BLEND_* */
+	float def_col[4];           /* layer "def_col" [1] */
+	float def_val, colfac, valfac;   /* layer "def_val" [1], "colfac" [1], "valfac" [1] */
+	int32_t do_color, color_input, use_alpha, no_rgb, stencil, negative;   /* layer [1, 1, 0, 0, 0, 0] */
+	float bump_strength;        /* texture_mapper "bump_strength" [1] (bump slot) */
+} gbrt_shader_node;
+/* The scene's node trees (replacing any set before; textures first).
+ * material_slots: n_materials x GBRT_SLOTS root node indices, -1 for none. */
+int gbrt_scene_set_shader_nodes(gbrt_scene *scene, const gbrt_shader_node *nodes, uint32_t n_nodes, const int32_t *material_slots,
+                                uint32_t n_materials);
+
 /* Diagnostics: a texture's getColor (RGBA) and getFloat at n texture-space
  * points (xyz, after the mapper) on the host or, on_device != 0, in a
  * kernel (host buffers either way; synchronises).  Procedural kinds only. */

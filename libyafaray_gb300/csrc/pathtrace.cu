@@ -66,6 +66,11 @@ struct DevMaterial {
 	float ecol[3];     // shinydiffuse: emit x colour
 	int32_t dtex;      // shinydiffuse: texture driving the diffuse colour ("diffuse_shader"), -1 none
 	float tf, emit;    // shinydiffuse: transmit_filter, emit (for a textured diffuse colour)
+	// shader node trees of the colour slots (gbrt_scene_set_shader_nodes):
+	// root node and the lowest node index of its tree, -1 for none
+	int32_t nroot[GBRT_SLOTS], nfirst[GBRT_SLOTS];
+	uint32_t nmask[GBRT_SLOTS];   // the nodes of the tree (bit i: node nfirst + i)
+	uint32_t has_nodes;
 };
 
 // ShinyDiffuseMaterial components (material_shiny_diffuse.cc:146-189)
@@ -217,6 +222,7 @@ struct SceneDev {
 	const float4 *vnrm;         // vertex normals
 	const uint4 *face_nrm;      // normal indices per face; x = kFlatFace: geometric normal; w = kTriFace: triangle
 	gbrt::NoiseTables nt;       // the host's noise tables (gbrt_scene_set_noise_tables); null without
+	const gbrt_shader_node *nodes;   // shader node trees (gbrt_scene_set_shader_nodes); null without
 };
 
 __device__ __forceinline__ float dot3(const float a[3], const float b[3]) { return xa(xa(xm(a[0], b[0]), xm(a[1], b[1])), xm(a[2], b[2])); }
@@ -875,16 +881,31 @@ __device__ void tex_layer(const DevTexture &T, float ta, float rgb[3])
 
 // A procedural texture's colour, out of line so the shading kernels keep
 // their registers for the common path.
-__device__ __noinline__ void tex_procedural(const SceneDev &sc, const DevTexture &T, const float p[3], float c4[4])
+__device__ __noinline__ void tex_procedural(const SceneDev &sc, const DevTexture &T, const float p[3], float c4[4], float *scalar)
 {
 	gbrt::proc_color(sc.nt, T.proc, p, c4);
+	if(scalar) *scalar = gbrt::proc_float(sc.nt, T.proc, p);
+}
+
+// Texture::applyIntensityContrastAdjustments(float) of an image texture
+// (texture.cc:272-287).
+__device__ __forceinline__ float image_adjust_float(const DevTexture &T, float v)
+{
+	if(!T.adj) return v;
+	float r = v;
+	if(T.adj_ic) r = xs(xa(xm(xs(v, 0.5f), T.contrast), T.intensity), 0.5f);
+	if(T.adj_clamp) r = r < 0.f ? 0.f : (r > 1.f ? 1.f : r);
+	return r;
 }
 
 // TextureMapperNode::getCoords / doMapping (shader_node_texture.cc:153-230),
 // ImageTexture::getColor / doMapping / noInterpolation /
 // bilinearInterpolation (texture_image.cc:180-262, 343-375) and
-// Texture::applyAdjustments (texture.cc:219-253): the texture's RGB at a hit.
-__device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p[3], const float ng[3], const float uv[2], float out[3])
+// Texture::applyAdjustments (texture.cc:219-253): the texture's RGBA at a
+// hit (getColor); with scalar, also its getFloat (for an image,
+// applyIntensityContrastAdjustments of the colour's brightness, texture.h:52).
+__device__ void tex_eval(const SceneDev &sc, const DevTexture &T, const float p[3], const float ng[3], const float uv[2], float out[4],
+                         float *scalar)
 {
 	float q[3];
 	if(T.texco == GBRT_TEXCO_UV) { q[0] = xs(xm(2.f, uv[0]), 1.f); q[1] = xs(xm(2.f, uv[1]), 1.f); q[2] = 0.f; }
@@ -929,11 +950,8 @@ __device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p
 	for(int k = 0; k < 3; ++k) t[k] = xa(xm(t[k], T.scale[k]), T.offset2[k]);
 	if(T.kind != GBRT_TEX_IMAGE)
 	{
-		// a procedural texture's getColor at the mapped point
-		float c4[4];
-		tex_procedural(sc, T, t, c4);
-		out[0] = c4[0]; out[1] = c4[1]; out[2] = c4[2];
-		tex_layer(T, c4[3], out);
+		// a procedural texture at the mapped point
+		tex_procedural(sc, T, t, out, scalar);
 		return;
 	}
 	// the image's own mapping of (x, -y, z)
@@ -980,7 +998,12 @@ __device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p
 		mx = mx > 0.99999f ? 0.99999f : (mx < 0.f ? 0.f : mx);
 		my = my > 0.99999f ? 0.99999f : (my < 0.f ? 0.f : my);
 	}
-	if(outside) { out[0] = out[1] = out[2] = 0.f; tex_layer(T, 0.f, out); return; }
+	if(outside)
+	{
+		out[0] = out[1] = out[2] = out[3] = 0.f;
+		if(scalar) *scalar = image_adjust_float(T, 0.f);
+		return;
+	}
 	const bool rep = T.clip == GBRT_CLIP_REPEAT;
 	const float4 *tx = sc.texels + T.off;
 	float4 c;
@@ -1033,19 +1056,245 @@ __device__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p
 			if(T.adj_clamp) for(int k = 0; k < 3; ++k) r[k] = r[k] < 0.f ? 0.f : r[k];
 		}
 	}
-	out[0] = r[0]; out[1] = r[1]; out[2] = r[2];
-	tex_layer(T, alpha, out);
+	out[0] = r[0]; out[1] = r[1]; out[2] = r[2]; out[3] = alpha;
+	if(scalar) *scalar = image_adjust_float(T, xa(xa(xm(0.2126f, r[0]), xm(0.7152f, r[1])), xm(0.0722f, r[2])));
+}
+
+// A diffuse shader of gbrt_scene_set_textures: the texture through its
+// mapper and optional layer node.
+__device__ __noinline__ void tex_color(const SceneDev &sc, const DevTexture &T, const float p[3], const float ng[3], const float uv[2],
+                                       float out[3])
+{
+	float c4[4];
+	tex_eval(sc, T, p, ng, uv, c4, nullptr);
+	out[0] = c4[0]; out[1] = c4[1]; out[2] = c4[2];
+	tex_layer(T, c4[3], out);
+}
+
+// Evaluates the shader node tree [first, root] at a surface point
+// (Material::evalNodes over the nodes of src/shader/): every node's colour
+// (RGBA) and scalar, in index order (each reads only lower indices); returns
+// the root's.
+__device__ __noinline__ void node_tree(const SceneDev &sc, int first, int root, uint32_t mask, const float p[3], const float ng[3],
+                                       const float uv[2], float out[4], float &scalar)
+{
+	float R[GBRT_TREE_MAX][5];
+	for(int i = first; i <= root; ++i)
+	{
+		if(!((mask >> (i - first)) & 1u)) continue;      // a node the root does not read
+		const gbrt_shader_node &N = sc.nodes[i];
+		float *r = R[i - first];
+		auto col_of = [&](int j, const float def[4], float c[4]) {
+			for(int k = 0; k < 4; ++k) c[k] = j >= 0 ? R[j - first][k] : def[k];
+		};
+		auto val_of = [&](int j, float def) { return j >= 0 ? R[j - first][4] : def; };
+		switch(N.type)
+		{
+			case GBRT_NODE_TEXTURE:
+			{
+				// TextureMapperNode::eval (shader_node_texture.cc:232-251)
+				float f = 0.f;
+				tex_eval(sc, sc.tex[N.texture], p, ng, uv, r, N.do_scalar ? &f : nullptr);
+				r[4] = f;
+				break;
+			}
+			case GBRT_NODE_VALUE:
+				// ValueNode::eval (shader_node_value.cc:71-74): colour with its alpha, scalar
+				for(int k = 0; k < 4; ++k) r[k] = N.color1[k];
+				r[4] = N.value1;
+				break;
+			case GBRT_NODE_MIX:
+			{
+				// MixNode::getInputs / eval and the blend-mode nodes (shader_node_mix.cc:143-175, mix/*.h)
+				const float f = val_of(N.input_factor, N.factor);
+				float c1[4], c2[4];
+				col_of(N.input1, N.color1, c1);
+				col_of(N.input2, N.color2, c2);
+				float f1 = val_of(N.input1, N.value1), f2 = val_of(N.input2, N.value2);
+				switch(N.mode)
+				{
+					case GBRT_MIX_ADD:
+						for(int k = 0; k < 4; ++k) c1[k] = xa(c1[k], xm(f, c2[k]));
+						f1 = xa(f1, xm(f, f2));
+						break;
+					case GBRT_MIX_MULTIPLY:
+						for(int k = 0; k < 4; ++k) c1[k] = xm(c1[k], xa(xm(1.f, xs(1.f, f)), xm(c2[k], f)));
+						f1 = xm(f1, xa(xm(1.f, xs(1.f, f)), xm(f2, f)));
+						break;
+					case GBRT_MIX_SUBTRACT:
+						for(int k = 0; k < 4; ++k) c1[k] = xs(c1[k], xm(f, c2[k]));
+						f1 = xs(f1, xm(f, f2));
+						break;
+					case GBRT_MIX_SCREEN:
+					{
+						const float fr = xs(1.f, f);
+						for(int k = 0; k < 4; ++k) c1[k] = xs(1.f, xm(xa(fr, xm(f, xs(1.f, c2[k]))), xs(1.f, c1[k])));
+						f1 = xs(1.f, xm(xa(fr, xm(f, xs(1.f, f2))), xs(1.f, f1)));
+						break;
+					}
+					case GBRT_MIX_DIFFERENCE:
+						for(int k = 0; k < 4; ++k) c1[k] = xa(xm(c1[k], xs(1.f, f)), xm(fabsf(xs(c1[k], c2[k])), f));
+						f1 = xa(xm(f1, xs(1.f, f)), xm(fabsf(xs(f1, f2)), f));
+						break;
+					case GBRT_MIX_DARKEN:
+					case GBRT_MIX_LIGHTEN:
+					{
+						const bool dark = N.mode == GBRT_MIX_DARKEN;
+						for(int k = 0; k < 4; ++k)
+						{
+							const float v = xm(c2[k], f);
+							if(dark ? v < c1[k] : v > c1[k]) c1[k] = v;
+						}
+						const float v = xm(f2, f);
+						if(dark ? v < f1 : v > f1) f1 = v;
+						break;
+					}
+					case GBRT_MIX_OVERLAY:
+					{
+						auto ov = [&](float a, float b) {
+							if(a < 0.5f) return xm(a, xa(xs(1.f, f), xm(xm(2.f, f), b)));
+							return xs(1.f, xm(xa(xs(1.f, f), xm(xm(2.f, f), xs(1.f, b))), xs(1.f, a)));
+						};
+						for(int k = 0; k < 4; ++k) c1[k] = ov(c1[k], c2[k]);
+						f1 = ov(f1, f2);
+						break;
+					}
+					default:   // mix: math::lerp
+						for(int k = 0; k < 4; ++k) c1[k] = xa(xm(c1[k], xs(1.f, f)), xm(c2[k], f));
+						f1 = xa(xm(f1, xs(1.f, f)), xm(f2, f));
+						break;
+				}
+				for(int k = 0; k < 4; ++k) r[k] = c1[k];
+				r[4] = f1;
+				break;
+			}
+			default:
+			{
+				// LayerNode::eval (shader_node_layer.cc:110-194) with textureRgbBlend /
+				// textureValueBlend (:264-366)
+				float rcol[4], tex[4] = {0.f, 0.f, 0.f, 1.f};
+				col_of(N.input2, N.color1, rcol);
+				float rval = val_of(N.input2, N.value1);
+				float stencil_tin = rcol[3];
+				float tin = 0.f, ta = 1.f;
+				bool tex_rgb = N.color_input != 0;
+				if(N.color_input) { for(int k = 0; k < 4; ++k) tex[k] = R[N.input1 - first][k]; ta = tex[3]; }
+				else tin = R[N.input1 - first][4];
+				if(N.no_rgb) { tin = xa(xa(xm(0.2126f, tex[0]), xm(0.7152f, tex[1])), xm(0.0722f, tex[2])); tex_rgb = false; }
+				if(N.negative)
+				{
+					if(tex_rgb) for(int k = 0; k < 4; ++k) tex[k] = xs(1.f, tex[k]);
+					tin = xs(1.f, tin);
+				}
+				if(N.stencil)
+				{
+					if(tex_rgb) { const float fact = ta; ta = xm(ta, stencil_tin); stencil_tin = xm(stencil_tin, fact); }
+					else { const float fact = tin; tin = xm(tin, stencil_tin); stencil_tin = xm(stencil_tin, fact); }
+				}
+				if(N.do_color)
+				{
+					if(!tex_rgb) for(int k = 0; k < 4; ++k) tex[k] = N.def_col[k];
+					else tin = ta;
+					const float tt = tin > 1.f ? 1.f : (tin < 0.f ? 0.f : tin);
+					const float facg = xm(stencil_tin, N.colfac);
+					const float fact = xm(tt, facg);
+					for(int k = 0; k < 3; ++k)
+					{
+						const float t = tex[k], o = rcol[k];
+						float v;
+						switch(N.mode)
+						{
+							case GBRT_BLEND_MULTIPLY: v = xm(xa(xs(1.f, facg), xm(fact, t)), o); break;
+							case GBRT_BLEND_SCREEN: v = xs(1.f, xm(xa(xs(1.f, facg), xm(fact, xs(1.f, t))), xs(1.f, o))); break;
+							case GBRT_BLEND_SUBTRACT: v = xs(o, xm(fact, t)); break;
+							case GBRT_BLEND_ADD: v = xa(o, xm(fact, t)); break;
+							case GBRT_BLEND_DIVIDE: v = xa(xm(xs(1.f, fact), o), xm(xm(fact, o), t != 0.f ? __fdiv_rn(1.f, t) : 0.f)); break;
+							case GBRT_BLEND_DIFFERENCE: v = xa(xm(xs(1.f, fact), o), xm(fact, fabsf(xs(t, o)))); break;
+							case GBRT_BLEND_DARKEN: v = xm(fact, t) > o ? o : xm(fact, t); break;
+							case GBRT_BLEND_LIGHTEN: v = xm(fact, t) < o ? o : xm(fact, t); break;
+							default: v = xa(xm(fact, t), xm(xs(1.f, fact), o)); break;
+						}
+						rcol[k] = v < 0.f ? 0.f : v;
+					}
+				}
+				if(N.do_scalar)
+				{
+					if(tex_rgb)
+					{
+						if(N.use_alpha) { tin = ta; if(N.negative) tin = xs(1.f, tin); }
+						else tin = xa(xa(xm(0.2126f, tex[0]), xm(0.7152f, tex[1])), xm(0.0722f, tex[2]));
+					}
+					const float facg = xm(stencil_tin, N.valfac);
+					float fact = xm(tin, facg);
+					float facm = xs(1.f, fact);
+					const float t = N.def_val, o = rval;
+					float v;
+					switch(N.mode)
+					{
+						case GBRT_BLEND_MULTIPLY: facm = xs(1.f, facg); v = xm(xa(facm, xm(fact, t)), o); break;
+						case GBRT_BLEND_SCREEN: facm = xs(1.f, facg); v = xs(1.f, xm(xa(facm, xm(fact, xs(1.f, t))), xs(1.f, o))); break;
+						case GBRT_BLEND_SUBTRACT: v = xs(o, xm(fact, t)); break;
+						case GBRT_BLEND_ADD: v = xa(o, xm(fact, t)); break;
+						case GBRT_BLEND_DIVIDE: v = t == 0.f ? 0.f : xa(xm(facm, o), __fdiv_rn(xm(fact, o), t)); break;
+						case GBRT_BLEND_DIFFERENCE: v = xa(xm(facm, o), xm(fact, fabsf(xs(t, o)))); break;
+						case GBRT_BLEND_DARKEN: { const float c = xm(fact, t); v = c < o ? c : o; break; }
+						case GBRT_BLEND_LIGHTEN: { const float c = xm(fact, t); v = c > o ? c : o; break; }
+						default: v = xa(xm(fact, t), xm(facm, o)); break;
+					}
+					rval = v < 0.f ? 0.f : v;
+				}
+				rcol[3] = stencil_tin;
+				for(int k = 0; k < 4; ++k) r[k] = rcol[k];
+				r[4] = rval;
+				break;
+			}
+		}
+	}
+	for(int k = 0; k < 4; ++k) out[k] = R[root - first][k];
+	scalar = R[root - first][4];
 }
 
 // The diffuse colour of a surface point (the material's, or its diffuse
 // shader's texture at the hit's coordinates).
-__device__ __forceinline__ void surface_color(const SceneDev &sc, Surface &s, int prim, float bu, float bv)
+// With shader node trees on its slots the material is copied to mloc with
+// the slot colours of this point (the reference's getShaderColor of each
+// slot) and s.m points there: the diffuse colour of shinydiffuse (s.dcol)
+// and glossy, the glossy colour, the mirror colour, the glass filter colour.
+__device__ __noinline__ void surface_nodes(const SceneDev &sc, Surface &s, int prim, float bu, float bv, DevMaterial &mloc)
 {
-	const DevMaterial &m = *s.m;
-	if(m.dtex < 0) { s.dcol[0] = m.col[0]; s.dcol[1] = m.col[1]; s.dcol[2] = m.col[2]; return; }
+	mloc = *s.m;
 	float uv[2];
 	hit_uv(sc, prim, bu, bv, uv);
-	tex_color(sc, sc.tex[m.dtex], s.p, s.ng, uv, s.dcol);
+	for(int slot = 0; slot < GBRT_SLOT_BUMP; ++slot)
+	{
+		if(mloc.nroot[slot] < 0) continue;
+		float c[4], f;
+		node_tree(sc, mloc.nfirst[slot], mloc.nroot[slot], mloc.nmask[slot], s.p, s.ng, uv, c, f);
+		if(slot == GBRT_SLOT_DIFFUSE)
+		{
+			if(mloc.type == GBRT_MAT_SHINYDIFFUSE) { s.dcol[0] = c[0]; s.dcol[1] = c[1]; s.dcol[2] = c[2]; mloc.dtex = 0; }
+			else for(int k = 0; k < 3; ++k) mloc.col2[k] = c[k];
+		}
+		else if(slot == GBRT_SLOT_MIRROR_COLOR) for(int k = 0; k < 3; ++k) mloc.col2[k] = c[k];
+		else for(int k = 0; k < 3; ++k) mloc.col[k] = c[k];    // glossy colour, glass filter colour
+	}
+	s.m = &mloc;
+}
+
+// kTex false: the scene has no textured material and no node trees (the
+// kernels instantiated so carry none of the texture code).
+template <bool kTex = true>
+__device__ __forceinline__ void surface_color(const SceneDev &sc, Surface &s, int prim, float bu, float bv, DevMaterial &mloc)
+{
+	const DevMaterial &m = *s.m;
+	if(!kTex || m.dtex < 0) { s.dcol[0] = m.col[0]; s.dcol[1] = m.col[1]; s.dcol[2] = m.col[2]; }
+	else
+	{
+		float uv[2];
+		hit_uv(sc, prim, bu, bv, uv);
+		tex_color(sc, sc.tex[m.dtex], s.p, s.ng, uv, s.dcol);
+	}
+	if(kTex && m.has_nodes) surface_nodes(sc, s, prim, bu, bv, mloc);
 }
 
 // ---- ShinyDiffuseMaterial layers (material_shiny_diffuse.cc:205-619) -------
@@ -1917,7 +2166,7 @@ struct SceneTable {
 // photonmapping, guiding, recording, recursive-split, texture and
 // shading-normal code is compiled out, which roughly halves the kernel's
 // registers and lets twice the warps stay resident.
-template <typename Src, bool kLean = false>
+template <typename Src, bool kLean = false, bool kTex = true>
 __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uint32_t shadow_cap)
 {
 	const uint32_t n = W.count[cur];
@@ -1939,6 +2188,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 		float nray[8];
 		uint32_t path = 0, n_shadow = 0;
 		Surface s;
+		DevMaterial mloc;           // the material with node-tree slot colours, when it has node trees
 		float wo[3] = {0.f, 0.f, 0.f}, thr[3] = {0.f, 0.f, 0.f};
 		uint32_t pixel = 0, sample_ = 0, offset_ = 0, sub = 0, k = 0, mat1 = 0, caustic = 0;
 		uint32_t level = 0, addl = 0, division = 1, branch = 0, si = 0, tseed = P.seed;
@@ -1968,7 +2218,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 				{
 					shading_normal(sc, prim, h.z, h.w, s.ng, s.n);
 					coords_system(s.n, s.u, s.v);
-					surface_color(sc, s, prim, h.z, h.w);
+					surface_color<kTex>(sc, s, prim, h.z, h.w, mloc);
 				}
 				wo[0] = -dir[0]; wo[1] = -dir[1]; wo[2] = -dir[2];
 				pixel = W.p_pixel[path];
@@ -2322,10 +2572,11 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 	}
 }
 
+template <bool kTex>
 __global__ void __launch_bounds__(kThreads, 4) k_shade(SceneDev sc, Params P, Work W, int cur, uint32_t shadow_cap, float *film,
                                                     double *film64)
 {
-	shade_queue(OneScene{sc, P, film, film64}, W, cur, shadow_cap);
+	shade_queue<OneScene, false, kTex>(OneScene{sc, P, film, film64}, W, cur, shadow_cap);
 }
 
 // The same for plain scenes (shade_queue kLean).
@@ -2336,9 +2587,10 @@ __global__ void __launch_bounds__(kThreads, 6) k_shade_plain(SceneDev sc, Params
 }
 
 // The same for a batch of scenes: every path's scene from the table.
+template <bool kTex>
 __global__ void __launch_bounds__(kThreads, 4) k_shade_batch(const BatchScene *__restrict__ bs, Work W, int cur, uint32_t shadow_cap)
 {
-	shade_queue(SceneTable{bs}, W, cur, shadow_cap);
+	shade_queue<SceneTable, false, kTex>(SceneTable{bs}, W, cur, shadow_cap);
 }
 
 // Material::getTransparency of a shadow-ray hit, wo = the shadow ray's
@@ -2369,10 +2621,41 @@ __device__ __forceinline__ void mat_transparency(const DevMaterial &m, const flo
 	}
 }
 
+// A transparent surface's filter colour with what varies over it: a
+// textured diffuse colour, node-tree slot colours, a shading normal (out of
+// line: the shadow walk keeps its registers for the traversal).
+__device__ __noinline__ void shaded_transparency(const SceneDev &sc, const DevMaterial &m, int32_t prim, const float *from, const float *dir,
+                                                 float t, float u, float v, const float ng[3], float tr[3])
+{
+	// the hit point as Accelerator::primitiveIntersectionTransparentShadow forms it (from + t dir)
+	const float p[3] = {xa(from[0], xm(t, dir[0])), xa(from[1], xm(t, dir[1])), xa(from[2], xm(t, dir[2]))};
+	float dcol[3] = {0.f, 0.f, 0.f};
+	if(m.dtex >= 0)
+	{
+		float uv[2];
+		hit_uv(sc, prim, u, v, uv);
+		tex_color(sc, sc.tex[m.dtex], p, ng, uv, dcol);
+	}
+	float ns[3];
+	shading_normal(sc, prim, u, v, ng, ns);
+	if(m.has_nodes)
+	{
+		// the slot colours of this point (diffuse and filter colour)
+		Surface s;
+		for(int k = 0; k < 3; ++k) { s.p[k] = p[k]; s.ng[k] = ng[k]; s.dcol[k] = dcol[k]; }
+		s.m = &m;
+		DevMaterial ml;
+		surface_nodes(sc, s, prim, u, v, ml);
+		mat_transparency(ml, ng, ns, dir, s.dcol, tr);
+	}
+	else mat_transparency(m, ng, ns, dir, dcol, tr);
+}
+
 // Accelerator::primitiveIntersectionTransparentShadow (accelerator.h:147-169):
 // an opaque material blocks; a transparent one multiplies the shadow colour
 // by its transparency, until more than shadowDepth transparent surfaces lie
 // on the ray (then it blocks too).
+template <bool kTex>
 struct TransparentHits {
 	static constexpr bool kTransparent = true;
 	const SceneDev *sc;          // textures of a textured diffuse colour
@@ -2388,18 +2671,15 @@ struct TransparentHits {
 		const DevMaterial &m = mats[__float_as_uint(g.w)];
 		if(!m.transparent || depth >= max_depth) return true;
 		const float ng[3] = {g.x, g.y, g.z};
-		float dcol[3] = {0.f, 0.f, 0.f};
-		if(m.dtex >= 0)
+		float tr[3];
+		if(kTex && (m.dtex >= 0 || m.has_nodes)) shaded_transparency(*sc, m, prim, from, dir, t, u, v, ng, tr);
+		else
 		{
-			// the hit point as Accelerator::primitiveIntersectionTransparentShadow forms it (from + t dir)
-			const float p[3] = {xa(from[0], xm(t, dir[0])), xa(from[1], xm(t, dir[1])), xa(from[2], xm(t, dir[2]))};
-			float uv[2];
-			hit_uv(*sc, prim, u, v, uv);
-			tex_color(*sc, sc->tex[m.dtex], p, ng, uv, dcol);
+			const float dcol[3] = {0.f, 0.f, 0.f};
+			float ns[3];
+			shading_normal(*sc, prim, u, v, ng, ns);
+			mat_transparency(m, ng, ns, dir, dcol, tr);
 		}
-		float ns[3], tr[3];
-		shading_normal(*sc, prim, u, v, ng, ns);
-		mat_transparency(m, ng, ns, dir, dcol, tr);
 		for(int k = 0; k < 3; ++k) col[k] *= tr[k];
 		++depth;
 		return false;
@@ -2410,14 +2690,14 @@ struct TransparentHits {
 // the splat's registers out of this kernel.  kTransparent: transparent
 // shadows (the unoccluded colour times the filter colour of the transparent
 // surfaces passed).
-template <bool kFilm, bool kTransparent>
+template <bool kFilm, bool kTransparent, bool kTex = false>
 __global__ void __launch_bounds__(kThreads) k_shadow(SceneDev sc, Params P, Work W, uint32_t shadow_cap, float *film, double *film64)
 {
 	const gbrt::BvhView &bv = sc.bv;
 	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
 	const uint32_t n = min(W.count[2], shadow_cap);
 	uint32_t traced = 0;
-	using Filter = typename std::conditional<kTransparent, TransparentHits, gbrt::OpaqueHits>::type;
+	using Filter = typename std::conditional<kTransparent, TransparentHits<kTex>, gbrt::OpaqueHits>::type;
 	Filter f;
 	if constexpr(kTransparent)
 	{
@@ -2494,13 +2774,13 @@ __global__ void __launch_bounds__(kThreads) k_extend_batch(const BatchScene *__r
 		[&](uint32_t i, const gbrt::Hit &h) { W.hits[i] = make_float4(__int_as_float(h.prim), h.t, h.u, h.v); });
 }
 
-template <bool kFilm, bool kTransparent>
+template <bool kFilm, bool kTransparent, bool kTex = false>
 __global__ void __launch_bounds__(kThreads) k_shadow_batch(const BatchScene *__restrict__ bs, Work W, uint32_t shadow_cap)
 {
 	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
 	const uint32_t n = min(W.count[2], shadow_cap);
 	uint32_t traced = 0;
-	using Filter = typename std::conditional<kTransparent, TransparentHits, gbrt::OpaqueHits>::type;
+	using Filter = typename std::conditional<kTransparent, TransparentHits<kTex>, gbrt::OpaqueHits>::type;
 	Filter f;
 	gbrt::trace_persistent_filtered<true, true>(
 		bs[0].sc.bv, n, W.count + 5, stack + threadIdx.x, kThreads, f,
@@ -2921,6 +3201,7 @@ __device__ void reflectivity(const SceneDev &sc, const Surface &s, uint32_t flag
 	for(int k = 0; k < 3; ++k) out[k] *= 0.0625f;
 }
 
+template <bool kTex>
 __global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJob J)
 {
 	__shared__ uint2 stack[gbrt::kStackShared * kThreads];
@@ -2981,7 +3262,8 @@ __global__ void __launch_bounds__(kThreads) k_photon_shoot(SceneDev sc, PhotonJo
 			shading_normal(sc, h.prim, h.u, h.v, s.ng, s.n);
 			s.m = sc.mats + __float_as_uint(ng.w);
 			coords_system(s.n, s.u, s.v);
-			surface_color(sc, s, h.prim, h.u, h.v);
+			DevMaterial mloc;
+			surface_color<kTex>(sc, s, h.prim, h.u, h.v, mloc);
 			const float wi[3] = {-d[0], -d[1], -d[2]};
 			const uint32_t mf = s.m->flags;
 			const bool dep = (!J.sppm || !direct) && (J.caustic ? ((mf & (BF_DIFFUSE | BF_GLOSSY)) && caustic) : ((mf & BF_DIFFUSE) && !caustic));
@@ -3060,6 +3342,7 @@ __device__ __forceinline__ void eval_flags(const Surface &s, const float wo[3], 
 // Photon estimates at the roots of integrate() calls (vertex level 0 of a
 // wave), PhotonIntegrator::integrate (integrator_photon_mapping.cc:762-793)
 // and CausticPhotonIntegrator::estimateCausticPhotons (integrator_photon_caustic.cc:284-304).
+template <bool kTex>
 __global__ void __launch_bounds__(kThreads) k_pm_root(SceneDev sc, Params P, Work W, int cur, float *film, double *film64)
 {
 	const uint32_t n = W.count[cur];
@@ -3080,7 +3363,8 @@ __global__ void __launch_bounds__(kThreads) k_pm_root(SceneDev sc, Params P, Wor
 		s.ng[0] = ng.x; s.ng[1] = ng.y; s.ng[2] = ng.z;
 		shading_normal(sc, prim, h.z, h.w, s.ng, s.n);
 		coords_system(s.n, s.u, s.v);
-		surface_color(sc, s, prim, h.z, h.w);
+		DevMaterial mloc;
+		surface_color<kTex>(sc, s, prim, h.z, h.w, mloc);
 		const float wo[3] = {-dir[0], -dir[1], -dir[2]};
 		if(P.pm == 3)
 		{
@@ -3377,6 +3661,7 @@ __global__ void k_knn_test(gbrt::PhotonGrid g, const float *__restrict__ q, uint
 
 struct gbrt_scene;
 static bool plain_scene(const gbrt_scene *S);
+static bool textured_scene(const gbrt_scene *S);
 
 struct gbrt_scene {
 	const gbrt_bvh *bvh = nullptr;
@@ -3420,6 +3705,9 @@ struct gbrt_scene {
 	uint4 *face_nrm = nullptr;
 	// noise tables of the procedural textures (gbrt_scene_set_noise_tables)
 	uint8_t *noise_dev = nullptr;
+	// shader node trees (gbrt_scene_set_shader_nodes)
+	gbrt_shader_node *nodes = nullptr;
+	uint32_t n_tex = 0;
 	std::vector<DevMaterial> mats_host;
 	std::mutex mu;
 };
@@ -3427,13 +3715,20 @@ struct gbrt_scene {
 // Every material plain (the diffuse layer of shinydiffuse alone, an
 // untextured colour, or light_mat) and no shading normals: the scenes
 // k_shade_plain serves.
+static bool textured_scene(const gbrt_scene *S)
+{
+	for(const DevMaterial &m : S->mats_host)
+		if(m.dtex >= 0 || m.has_nodes) return true;
+	return false;
+}
+
 static bool plain_scene(const gbrt_scene *S)
 {
 	if(S->face_nrm) return false;
 	for(const DevMaterial &m : S->mats_host)
 	{
 		if(m.type == GBRT_MAT_LIGHT) continue;
-		if(m.type == GBRT_MAT_SHINYDIFFUSE && m.sd == SD_DIFFUSE && m.dtex < 0) continue;
+		if(m.type == GBRT_MAT_SHINYDIFFUSE && m.sd == SD_DIFFUSE && m.dtex < 0 && !m.has_nodes) continue;
 		return false;
 	}
 	return true;
@@ -3767,7 +4062,8 @@ int shoot_map(gbrt_scene *S, const SceneDev &sc, bool caustic, uint32_t n, int m
 	J.count = M.count.as<uint32_t>();
 	J.cap = cap; J.rp_cap = rp_cap;
 	J.rp_pos = M.rp_pos.as<float4>(); J.rp_nrm = M.rp_nrm.as<float4>(); J.rp_refl = M.rp_refl.as<float4>(); J.rp_transm = M.rp_transm.as<float4>();
-	k_photon_shoot<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, J);
+	if(textured_scene(S)) k_photon_shoot<true><<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, J);
+	else k_photon_shoot<false><<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, J);
 	GBRT_CK(cudaGetLastError());
 	uint32_t cnt[2];
 	GBRT_CK(cudaMemcpyAsync(cnt, M.count.p, 8, cudaMemcpyDeviceToHost, s));
@@ -3794,7 +4090,7 @@ SceneDev scene_dev(const gbrt_scene *S)
 {
 	return SceneDev{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off, S->lds_sfac_nd,
 	                                                                         S->lds_fx, S->lds_fx_dims, S->lds_fx_rad3},
-	                S->tex, S->texels, S->uv, S->face_uv, S->vnrm, S->face_nrm, noise_view(S)};
+	                S->tex, S->texels, S->uv, S->face_uv, S->vnrm, S->face_nrm, noise_view(S), S->nodes};
 }
 
 } // namespace
@@ -3821,6 +4117,7 @@ int gbrt_scene_create(const gbrt_bvh *bvh, const float *vertices, uint32_t n_ver
 		std::memset(&d, 0, sizeof(d));
 		d.type = m.type;
 		d.dtex = -1;
+		for(int k = 0; k < GBRT_SLOTS; ++k) d.nroot[k] = d.nfirst[k] = -1;
 		if(m.type == GBRT_MAT_SHINYDIFFUSE)
 		{
 			// ShinyDiffuseMaterial ctor + config (material_shiny_diffuse.cc:133-189);
@@ -4136,6 +4433,78 @@ int gbrt_scene_set_textures(gbrt_scene *S, const float *uv, uint32_t n_uv, const
 	}
 	GBRT_CK(cudaMemcpy(S->mats, mats.data(), mats.size() * sizeof(DevMaterial), cudaMemcpyHostToDevice));
 	S->mats_host = mats;
+	S->n_tex = n_textures;
+	return GBRT_OK;
+}
+
+int gbrt_scene_set_shader_nodes(gbrt_scene *S, const gbrt_shader_node *nodes, uint32_t n_nodes, const int32_t *slots, uint32_t n_materials)
+{
+	if(!S || (n_nodes && !nodes) || (n_materials && !slots)) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_shader_nodes: NULL argument");
+	if(n_materials != S->n_mats)
+		return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_shader_nodes: %u material entries for %u materials", n_materials, S->n_mats);
+	for(uint32_t i = 0; i < n_nodes; ++i)
+	{
+		const gbrt_shader_node &N = nodes[i];
+		const int32_t ii = static_cast<int32_t>(i);
+		auto bad_input = [&](int32_t j) { return j >= ii || j < -1; };
+		if(N.type > GBRT_NODE_LAYER || bad_input(N.input1) || bad_input(N.input2) || bad_input(N.input_factor))
+			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_shader_nodes: node %u: type %u or an input not below it", i, N.type);
+		if(N.type == GBRT_NODE_TEXTURE && (N.texture < 0 || static_cast<uint32_t>(N.texture) >= S->n_tex))
+			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_shader_nodes: node %u: texture %d of %u (set the textures first)", i,
+			                      N.texture, S->n_tex);
+		if(N.type == GBRT_NODE_MIX && N.mode > GBRT_MIX_OVERLAY)
+			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_shader_nodes: node %u: mix mode %u", i, N.mode);
+		if(N.type == GBRT_NODE_LAYER && (N.input1 < 0 || N.mode > GBRT_BLEND_LIGHTEN))
+			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_shader_nodes: node %u: a layer needs an input and a blend mode", i);
+	}
+	std::vector<DevMaterial> mats = S->mats_host;
+	for(uint32_t m = 0; m < n_materials; ++m)
+	{
+		DevMaterial &d = mats[m];
+		d.has_nodes = 0u;
+		for(int k = 0; k < GBRT_SLOTS; ++k)
+		{
+			const int32_t root = slots[static_cast<size_t>(m) * GBRT_SLOTS + k];
+			d.nroot[k] = d.nfirst[k] = -1;
+			d.nmask[k] = 0u;
+			if(root < 0) continue;
+			if(static_cast<uint32_t>(root) >= n_nodes)
+				return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_shader_nodes: material %u slot %d: node %d of %u", m, k, root, n_nodes);
+			const bool ok = (k == GBRT_SLOT_DIFFUSE && (d.type == GBRT_MAT_SHINYDIFFUSE || d.type == GBRT_MAT_GLOSSY)) ||
+			                (k == GBRT_SLOT_GLOSSY && d.type == GBRT_MAT_GLOSSY) ||
+			                (k == GBRT_SLOT_MIRROR_COLOR && (d.type == GBRT_MAT_SHINYDIFFUSE || d.type == GBRT_MAT_GLASS || d.type == GBRT_MAT_ROUGH_GLASS)) ||
+			                (k == GBRT_SLOT_FILTER_COLOR && (d.type == GBRT_MAT_GLASS || d.type == GBRT_MAT_ROUGH_GLASS));
+			if(!ok)
+				return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_shader_nodes: material %u (type %u) has no slot %d", m, d.type, k);
+			// the nodes the root reads, through its inputs, and the lowest of them
+			int32_t first = root;
+			std::vector<int32_t> todo{root}, tree;
+			while(!todo.empty())
+			{
+				const int32_t j = todo.back();
+				todo.pop_back();
+				first = std::min(first, j);
+				tree.push_back(j);
+				for(int32_t q : {nodes[j].input1, nodes[j].input2, nodes[j].input_factor})
+					if(q >= 0) todo.push_back(q);
+			}
+			if(root - first + 1 > GBRT_TREE_MAX)
+				return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_scene_set_shader_nodes: material %u slot %d: a tree spanning %d nodes (at most %d)",
+				                      m, k, root - first + 1, GBRT_TREE_MAX);
+			d.nroot[k] = root;
+			d.nfirst[k] = first;
+			for(int32_t j : tree) d.nmask[k] |= 1u << (j - first);
+			d.has_nodes = 1u;
+		}
+	}
+	std::lock_guard<std::mutex> lock(S->mu);
+	if(S->ev_last) GBRT_CK(cudaEventSynchronize(S->ev_last));
+	if(S->nodes) cudaFree(S->nodes);
+	S->nodes = nullptr;
+	GBRT_CK(cudaMalloc(reinterpret_cast<void **>(&S->nodes), std::max<uint32_t>(1, n_nodes) * sizeof(gbrt_shader_node)));
+	if(n_nodes) GBRT_CK(cudaMemcpy(S->nodes, nodes, n_nodes * sizeof(gbrt_shader_node), cudaMemcpyHostToDevice));
+	GBRT_CK(cudaMemcpy(S->mats, mats.data(), mats.size() * sizeof(DevMaterial), cudaMemcpyHostToDevice));
+	S->mats_host = mats;
 	return GBRT_OK;
 }
 
@@ -4199,7 +4568,7 @@ int gbrt_scene_destroy(gbrt_scene *S)
 	                S->lds_sfac_nd, S->lds_fx, S->work, S->spawn, S->spawn_count};
 	for(void *p : ptrs) if(p) cudaFree(p);
 	for(void *p : {static_cast<void *>(S->tex), static_cast<void *>(S->texels), static_cast<void *>(S->uv), static_cast<void *>(S->face_uv),
-	               static_cast<void *>(S->vnrm), static_cast<void *>(S->face_nrm), static_cast<void *>(S->noise_dev)})
+	               static_cast<void *>(S->vnrm), static_cast<void *>(S->face_nrm), static_cast<void *>(S->noise_dev), static_cast<void *>(S->nodes)})
 		if(p) cudaFree(p);
 	if(S->filter_dev) cudaFree(S->filter_dev);
 	if(S->ev_last) cudaEventDestroy(S->ev_last);
@@ -4379,8 +4748,10 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 	Work W = S->w;
 	if(!record) W.p_sum = nullptr;
 	float *film = film64_dev ? nullptr : film_dev;
-	// the lean shading kernel serves pathtracing over plain scenes
+	// the lean shading kernel serves pathtracing over plain scenes; kernels
+	// with the texture and node-tree code only serve scenes that use them
 	const bool plain = !pm && plain_scene(S);
+	const bool tex = textured_scene(S);
 	cudaEvent_t e0 = nullptr, e1 = nullptr;
 	if(stats)
 	{
@@ -4404,15 +4775,26 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 			k_extend<<<persistent_grid(k_extend, n, S->n_sm), kThreads, 0, s>>>(sc.bv, Ww.q_ray[cur], Ww.count + cur, Ww.count + 4, Ww.hits,
 			                                                                     level_guided ? Ww.hitpos : nullptr);
 			if(vtx == 0 && (Pw.pm_caustics || (Pw.pm && Pw.pm_diffuse && !Pw.pm_fg)))
-				k_pm_root<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, film, film64_dev);
+			{
+				if(tex) k_pm_root<true><<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, film, film64_dev);
+				else k_pm_root<false><<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, film, film64_dev);
+			}
 			if(level_guided)
 				if(int rc = gbrt_guide_eval_queue(guide, Ww.hitpos, n, Ww.count + cur, Ww.lobes, s)) return rc;
 			if(plain && !Pw.guiding && !Pw.record)
 				k_shade_plain<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+			else if(tex)
+				k_shade<true><<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
 			else
-				k_shade<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+				k_shade<false><<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
 			const uint32_t scap = static_cast<uint32_t>(shadow_cap);
-			if(Pw.film_w && Pw.tshadow)
+			if(Pw.film_w && Pw.tshadow && tex)
+				k_shadow<true, true, true><<<persistent_grid(k_shadow<true, true, true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, scap, film,
+				                                                                                                          film64_dev);
+			else if(Pw.tshadow && tex)
+				k_shadow<false, true, true><<<persistent_grid(k_shadow<false, true, true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, scap, film,
+				                                                                                                            film64_dev);
+			else if(Pw.film_w && Pw.tshadow)
 				k_shadow<true, true><<<persistent_grid(k_shadow<true, true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, scap, film, film64_dev);
 			else if(Pw.film_w)
 				k_shadow<true, false><<<persistent_grid(k_shadow<true, false>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, scap, film, film64_dev);
@@ -5210,6 +5592,8 @@ static int batch_render_locked(gbrt_scene *const *scenes, const gbrt_camera_desc
 	gbrt_scene *S0 = scenes[0];
 	const bool tshadow = params[0].transparent_shadows != 0;
 	const bool filtered = params[0].filter_type != GBRT_FILTER_PIXEL;
+	bool tex = false;
+	for(uint32_t i = 0; i < n; ++i) tex = tex || textured_scene(scenes[i]);
 	std::vector<BatchScene> host(n);
 	uint64_t total = 0;
 	uint32_t fanout = 0, max_shadow = 0;
@@ -5339,9 +5723,12 @@ static int batch_render_locked(gbrt_scene *const *scenes, const gbrt_camera_desc
 				k_extend_batch<<<trace_grid(nq, bps_extend), kThreads, 0, st>>>(table, Ww, cur);
 				const unsigned blocks = static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>((nq + sblock - 1) / sblock,
 				                                                                                   static_cast<size_t>(n_sm) * 16 * (kThreads / sblock))));
-				k_shade_batch<<<blocks, sblock, 0, st>>>(table, Ww, cur, scap);
+				if(tex) k_shade_batch<true><<<blocks, sblock, 0, st>>>(table, Ww, cur, scap);
+				else k_shade_batch<false><<<blocks, sblock, 0, st>>>(table, Ww, cur, scap);
 				const unsigned sg = trace_grid(shadow_cap, bps_shadow[(filtered ? 2 : 0) + (tshadow ? 1 : 0)]);
-				if(filtered && tshadow) k_shadow_batch<true, true><<<sg, kThreads, 0, st>>>(table, Ww, scap);
+				if(filtered && tshadow && tex) k_shadow_batch<true, true, true><<<sg, kThreads, 0, st>>>(table, Ww, scap);
+				else if(tshadow && tex) k_shadow_batch<false, true, true><<<sg, kThreads, 0, st>>>(table, Ww, scap);
+				else if(filtered && tshadow) k_shadow_batch<true, true><<<sg, kThreads, 0, st>>>(table, Ww, scap);
 				else if(filtered) k_shadow_batch<true, false><<<sg, kThreads, 0, st>>>(table, Ww, scap);
 				else if(tshadow) k_shadow_batch<false, true><<<sg, kThreads, 0, st>>>(table, Ww, scap);
 				else k_shadow_batch<false, false><<<sg, kThreads, 0, st>>>(table, Ww, scap);

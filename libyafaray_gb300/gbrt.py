@@ -117,6 +117,95 @@ class NoiseTablesDesc(ctypes.Structure):
                 ("stdp_p", ctypes.c_void_p), ("stdp_g", ctypes.c_void_p)]
 
 
+class ShaderNode(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_uint32), ("texture", ctypes.c_int32), ("do_scalar", ctypes.c_int32), ("input1", ctypes.c_int32),
+                ("input2", ctypes.c_int32), ("input_factor", ctypes.c_int32), ("color1", ctypes.c_float * 4),
+                ("color2", ctypes.c_float * 4), ("value1", ctypes.c_float), ("value2", ctypes.c_float), ("factor", ctypes.c_float),
+                ("mode", ctypes.c_uint32), ("def_col", ctypes.c_float * 4), ("def_val", ctypes.c_float), ("colfac", ctypes.c_float),
+                ("valfac", ctypes.c_float), ("do_color", ctypes.c_int32), ("color_input", ctypes.c_int32), ("use_alpha", ctypes.c_int32),
+                ("no_rgb", ctypes.c_int32), ("stencil", ctypes.c_int32), ("negative", ctypes.c_int32), ("bump_strength", ctypes.c_float)]
+
+
+NODE_TYPES = {"texture_mapper": 0, "value": 1, "mix": 2, "layer": 3}
+MIX_MODES = {"mix": 0, "add": 1, "multiply": 2, "subtract": 3, "screen": 4, "difference": 5, "darken": 6, "lighten": 7, "overlay": 8}
+SLOTS = {"diffuse_shader": 0, "glossy_shader": 1, "mirror_color_shader": 2, "filter_color_shader": 3, "bump_shader": 4}
+N_SLOTS = 5
+
+
+def _rgba(v, alpha=1.0):
+    v = [float(x) for x in v]
+    return v + [alpha] if len(v) == 3 else v[:4]
+
+
+def shader_nodes(scene):
+    """The scene's shader node trees ("nodes": name -> node dict with the
+    reference's parameter names; "material_shaders": material name ->
+    {slot parameter name: node name}) as gbrt_shader_node entries in an
+    order where every node follows its inputs, the textures their
+    texture_mapper nodes read (texture dict + the node's mapper
+    parameters), and per material the GBRT_SLOTS root indices."""
+    nodes = scene.get("nodes", {})
+    order, seen = [], set()
+
+    def visit(name):
+        if name in seen:
+            return
+        seen.add(name)
+        nd = nodes[name]
+        for k in ("input1", "input2", "input_factor", "input", "upper_layer"):
+            if nd.get(k):
+                visit(nd[k])
+        order.append(name)
+
+    for name in nodes:
+        visit(name)
+    index = {n: i for i, n in enumerate(order)}
+    arr = (ShaderNode * max(1, len(order)))()
+    textures = []
+    for i, name in enumerate(order):
+        nd = nodes[name]
+        d = arr[i]
+        d.type = NODE_TYPES[nd["type"]]
+        d.texture = -1
+        d.input1 = d.input2 = d.input_factor = -1
+        d.bump_strength = float(nd.get("bump_strength", 1.0))
+        if nd["type"] == "texture_mapper":
+            tx = dict(scene["textures"][nd["texture"]])
+            mp = {k: nd[k] for k in ("texco", "mapping", "scale", "offset") if k in nd}
+            mp["proj"] = tuple(int(nd.get(f"proj_{a}", d0)) for a, d0 in (("x", 1), ("y", 2), ("z", 3)))
+            tx["mapper"] = mp
+            tx.pop("layer", None)
+            d.texture = len(textures)
+            textures.append(tx)
+            d.do_scalar = int(bool(nd.get("do_scalar", True)))
+        elif nd["type"] == "value":
+            d.color1[:] = [*[float(x) for x in nd.get("color", (1.0, 1.0, 1.0))][:3], float(nd.get("alpha", 1.0))]
+            d.value1 = float(nd.get("scalar", 1.0))
+        elif nd["type"] == "mix":
+            d.input1 = index[nd["input1"]] if nd.get("input1") else -1
+            d.input2 = index[nd["input2"]] if nd.get("input2") else -1
+            d.input_factor = index[nd["input_factor"]] if nd.get("input_factor") else -1
+            d.color1[:] = _rgba(nd.get("color1", (0.0, 0.0, 0.0, 0.0)), 0.0)
+            d.color2[:] = _rgba(nd.get("color2", (0.0, 0.0, 0.0, 0.0)), 0.0)
+            d.value1, d.value2 = float(nd.get("value1", 0.0)), float(nd.get("value2", 0.0))
+            d.factor = float(nd.get("cfactor", 0.5))
+            d.mode = MIX_MODES[nd.get("blend_mode", "mix")]
+        else:
+            d.input1 = index[nd["input"]]
+            d.input2 = index[nd["upper_layer"]] if nd.get("upper_layer") else -1
+            d.color1[:] = _rgba(nd.get("upper_color", (0.0, 0.0, 0.0, 0.0)), 0.0)
+            d.value1 = float(nd.get("upper_value", 0.0))
+            d.def_col[:] = _rgba(nd.get("def_col", (1.0, 1.0, 1.0, 1.0)), 1.0)
+            d.def_val, d.colfac, d.valfac = float(nd.get("def_val", 1.0)), float(nd.get("colfac", 1.0)), float(nd.get("valfac", 1.0))
+            d.do_color = int(bool(nd.get("do_color", True)))
+            d.do_scalar = int(bool(nd.get("do_scalar", False)))
+            d.color_input = int(bool(nd.get("color_input", True)))
+            d.use_alpha = int(bool(nd.get("use_alpha", False)))
+            d.no_rgb, d.stencil, d.negative = (int(bool(nd.get(k, False))) for k in ("noRGB", "stencil", "negative"))
+            d.mode = BLEND_MODES[nd.get("blend_mode", "mix")]
+    return arr, len(order), textures, index
+
+
 class TextureDesc(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("rgba", ctypes.c_void_p),
                 ("interpolate", ctypes.c_uint32), ("clipping", ctypes.c_uint32), ("xrepeat", ctypes.c_int32),
@@ -378,6 +467,7 @@ SIGNATURES = {
     "gbrt_scene_set_normals": (_I, [_VP, _VP, _U32, _VP]),
     "gbrt_procedural_defaults": (None, [ctypes.POINTER(ProceduralDesc)]),
     "gbrt_scene_set_noise_tables": (_I, [_VP, ctypes.POINTER(NoiseTablesDesc)]),
+    "gbrt_scene_set_shader_nodes": (_I, [_VP, ctypes.POINTER(ShaderNode), _U32, _VP, _U32]),
     "gbrt_texture_eval": (_I, [ctypes.POINTER(TextureDesc), ctypes.POINTER(NoiseTablesDesc), _VP, _U32, _VP, _VP, ctypes.c_int]),
     "gbrt_pm_render_aa_host": (_I, [_VP, ctypes.POINTER(CameraDesc), ctypes.POINTER(PtParams), _VP, ctypes.POINTER(AaParams),
                                     _VP, ctypes.POINTER(PtStats), _VP]),
@@ -638,7 +728,7 @@ class Renderer:
                                        len(self.faces), _ptr(fm), mats, len(self.mat_names), lights,
                                        len(scene["lights"]), ctypes.byref(h)))
         self._h = h
-        if scene.get("textures"):
+        if scene.get("textures") or scene.get("nodes"):
             self._set_textures()
         if any("smooth" in o or "normals" in o for o in scene["objects"]):
             self._set_normals()
@@ -675,16 +765,19 @@ class Renderer:
     def _set_textures(self):
         """Image and procedural textures of the scene's "textures" entry on
         the shinydiffuse materials whose options name one
-        ("diffuse_texture"); procedural textures need the scene's
-        "noise_tables" (the reference's NoiseGenerator tables)."""
+        ("diffuse_texture"), then the shader node trees ("nodes",
+        "material_shaders"; shader_nodes); procedural textures need the
+        scene's "noise_tables" (the reference's NoiseGenerator tables)."""
         from . import scenes as _scenes
-        names = list(self.scene["textures"].keys())
-        if any(self.scene["textures"][n].get("type", "image") != "image" for n in names):
+        names = list(self.scene.get("textures", {}).keys())
+        nodes, n_nodes, node_tex, _ = shader_nodes(self.scene)
+        all_tex = [self.scene["textures"][n] for n in names] + node_tex
+        if any(t.get("type", "image") != "image" for t in all_tex):
             nt, self._noise_keep = noise_tables(self.scene["noise_tables"])
             check(load().gbrt_scene_set_noise_tables(self._h, ctypes.byref(nt)))
-        descs, keep = (TextureDesc * len(names))(), []
-        for i, n in enumerate(names):
-            d, img = texture_desc(self.scene["textures"][n])
+        descs, keep = (TextureDesc * max(1, len(all_tex)))(), []
+        for i, t in enumerate(all_tex):
+            d, img = texture_desc(t)
             descs[i] = d
             keep.append(img)
         mt = np.full(len(self.mat_names), -1, np.int32)
@@ -696,8 +789,15 @@ class Renderer:
         if uv is not None:
             uv = np.ascontiguousarray(uv, np.float32)
             fuv = np.ascontiguousarray(fuv, np.uint32)
-        check(load().gbrt_scene_set_textures(self._h, _ptr(uv), 0 if uv is None else len(uv), _ptr(fuv), descs, len(names),
+        check(load().gbrt_scene_set_textures(self._h, _ptr(uv), 0 if uv is None else len(uv), _ptr(fuv), descs, len(all_tex),
                                              _ptr(mt), len(mt)))
+        if n_nodes:
+            _, _, _, index = shader_nodes(self.scene)
+            slots = np.full((len(self.mat_names), N_SLOTS), -1, np.int32)
+            for i, n in enumerate(self.mat_names):
+                for key, node in self.scene.get("material_shaders", {}).get(n, {}).items():
+                    slots[i, SLOTS[key]] = index[node]
+            check(load().gbrt_scene_set_shader_nodes(self._h, nodes, n_nodes, _ptr(slots), len(self.mat_names)))
 
     def close(self):
         if getattr(self, "_h", None):

@@ -480,6 +480,55 @@ def procedural_cornell_scene(noise_tables, res=64, **kw):
     return sc
 
 
+def node_cornell_scene(noise_tables, res=64, **kw):
+    """The glass and glossy Cornell box with shader node trees on every
+    colour slot: mix nodes in each blend mode (multiply with a texture's
+    scalar as factor, overlay, darken, lighten, screen, subtract,
+    difference, add), value nodes, a chain of two layer nodes (the second
+    stencilled over the first through upper_layer), texture mappers over
+    procedural and image textures; slots: shinydiffuse and glossy diffuse,
+    glossy colour, glass and rough-glass filter and mirror colours."""
+    sc = cornell_scene(res=res, glass=True, glossy=True, **kw)
+    sc["noise_tables"] = noise_tables
+    sc["textures"] = {
+        "marble": {"type": "marble", "noise_type": "newperlin", "depth": 2, "turbulence": 3.0, "color1": (0.9, 0.85, 0.8),
+                   "color2": (0.3, 0.25, 0.2)},
+        "clouds": {"type": "clouds", "noise_type": "blender", "depth": 3, "size": 0.7, "color1": (0.2, 0.3, 0.5),
+                   "color2": (0.9, 0.8, 0.6)},
+        "cells": {"type": "voronoi", "color_mode": "position", "size": 3.0, "weight1": 1.0, "weight2": -0.3},
+        "checker": {"image": checker_image(8, 8, (0.9, 0.9, 0.2), (0.2, 0.4, 0.9), seed=17), "interpolate": "bilinear",
+                    "clipping": "repeat"},
+    }
+    sc["nodes"] = {
+        "m_marble": {"type": "texture_mapper", "texture": "marble", "scale": (2.0, 2.0, 2.0)},
+        "m_clouds": {"type": "texture_mapper", "texture": "clouds"},
+        "m_cells": {"type": "texture_mapper", "texture": "cells", "scale": (1.5, 1.5, 1.5)},
+        "m_check": {"type": "texture_mapper", "texture": "checker", "mapping": "cube", "scale": (1.5, 1.5, 1.5)},
+        "v_tint": {"type": "value", "color": (0.9, 0.6, 0.3), "alpha": 0.8, "scalar": 0.4},
+        "mix_grey": {"type": "mix", "blend_mode": "multiply", "input1": "m_marble", "input2": "v_tint", "input_factor": "m_clouds"},
+        "lay1": {"type": "layer", "input": "m_cells", "upper_color": (0.63, 0.065, 0.05, 1.0), "blend_mode": "mix", "colfac": 0.7},
+        "lay2": {"type": "layer", "input": "m_check", "upper_layer": "lay1", "blend_mode": "difference", "colfac": 0.5,
+                 "stencil": True},
+        "ov": {"type": "mix", "blend_mode": "overlay", "input1": "m_clouds", "color2": (0.2, 0.5, 0.9, 1.0), "cfactor": 0.6},
+        "dk": {"type": "mix", "blend_mode": "darken", "input1": "m_cells", "input2": "v_tint", "cfactor": 0.8},
+        "lt": {"type": "mix", "blend_mode": "lighten", "input1": "v_tint", "input2": "m_cells", "cfactor": 0.7},
+        "scr": {"type": "mix", "blend_mode": "screen", "color1": (0.9, 0.9, 1.0, 1.0), "input2": "m_marble", "cfactor": 0.3},
+        "sub": {"type": "mix", "blend_mode": "subtract", "color1": (1.0, 1.0, 1.0, 1.0), "input2": "m_clouds", "cfactor": 0.25},
+        "diff": {"type": "mix", "blend_mode": "difference", "input1": "m_check", "input2": "m_cells", "cfactor": 0.5},
+        "add": {"type": "mix", "blend_mode": "add", "input1": "v_tint", "input2": "m_marble", "cfactor": 0.2},
+    }
+    sc["material_shaders"] = {
+        "grey": {"diffuse_shader": "mix_grey"},
+        "red": {"diffuse_shader": "lay2"},
+        "green": {"diffuse_shader": "lt"},
+        "glossy_box": {"diffuse_shader": "m_clouds", "glossy_shader": "ov"},
+        "glossy_floor": {"diffuse_shader": "diff"},
+        "glass": {"filter_color_shader": "scr", "mirror_color_shader": "dk"},
+        "rough_glass": {"filter_color_shader": "sub", "mirror_color_shader": "add"},
+    }
+    return sc
+
+
 def cornell_sppm_scene(res=48, photons=100000, passes=8, bounces=5, pm_ire=False, photon_radius=0.1, search_num=10):
     """The glass Cornell box (a glass and a rough-glass ball) rendered by the
     "SPPM" integrator: caustics under the balls come from the photon

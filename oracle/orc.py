@@ -175,8 +175,32 @@ def reference_scene_text(scene, spp, batches, threads=-1, offset_stride=None):
         out += [" ".join(repr(float(x)) for x in row.reshape(-1)) for row in img]
         out.append(f"texture {tname} type=image image_name={tname}_img "
                    + " ".join(f"{k}={fmt(tx[k])}" for k in tex_keys if k in tx))
+    shaders = scene.get("material_shaders", {})
     for name, m in scene["materials"].items():
         t = m[0]
+        slot_extra = ""
+        if name in shaders:
+            # the material's node trees: every node its slots read, then the slots
+            nodes = scene["nodes"]
+            need, todo = [], list(shaders[name].values())
+            while todo:
+                n = todo.pop()
+                if n in need:
+                    continue
+                need.append(n)
+                todo += [nodes[n][k] for k in ("input1", "input2", "input_factor", "input", "upper_layer") if nodes[n].get(k)]
+            for n in need:
+                nd = dict(nodes[n])
+                kv = [f"name={n}", f"type={nd.pop('type')}"]
+                for k, v in nd.items():
+                    if k in ("color", "color1", "color2", "upper_color", "def_col") and isinstance(v, (tuple, list)):
+                        v = [float(x) for x in v]
+                        v = v + [1.0 if k in ("color", "def_col") else 0.0] if len(v) == 3 else v
+                        kv.append(f"{k}=" + ",".join(repr(x) for x in v[:4]))
+                    else:
+                        kv.append(f"{k}={fmt(v)}")
+                out.append("node " + " ".join(kv))
+            slot_extra = "".join(f" {k}={v}" for k, v in shaders[name].items())
         if t == "shinydiffusemat":
             extra = ""
             for k, v in (m[2] if len(m) > 2 else {}).items():
@@ -206,25 +230,25 @@ def reference_scene_text(scene, spp, batches, threads=-1, offset_stride=None):
                     extra += f" {k}=" + ",".join(repr(float(x)) for x in v)
                 else:
                     extra += f" {k}={float(v)!r}"
-            out.append(f"material {name} shinydiffusemat {m[1][0]!r} {m[1][1]!r} {m[1][2]!r}{extra}")
+            out.append(f"material {name} shinydiffusemat {m[1][0]!r} {m[1][1]!r} {m[1][2]!r}{extra}" + slot_extra)
         elif t == "light_mat":
-            out.append(f"material {name} light_mat {m[1][0]!r} {m[1][1]!r} {m[1][2]!r} {m[2]!r}")
+            out.append(f"material {name} light_mat {m[1][0]!r} {m[1][1]!r} {m[1][2]!r} {m[2]!r}" + slot_extra)
         elif t == "glossy":
             _, dc, gc, e, gr, dr = m
             vals = [*dc, *gc, e, gr, dr]
-            out.append(f"material {name} glossy " + " ".join(repr(float(x)) for x in vals))
+            out.append(f"material {name} glossy " + " ".join(repr(float(x)) for x in vals) + slot_extra)
         elif t == "glass":
             _, ior, fc, tf, mc = m[:5]
             vals = [ior, tf, *fc, *mc]
             fake = " fake_shadows=true" if len(m) > 5 and m[5].get("fake_shadows") else ""
-            out.append(f"material {name} glass " + " ".join(repr(float(x)) for x in vals) + fake)
+            out.append(f"material {name} glass " + " ".join(repr(float(x)) for x in vals) + fake + slot_extra)
         elif t == "rough_glass":
             _, ior, alpha, fc, tf, mc = m[:6]
             vals = [ior, alpha, tf, *fc, *mc]
             fake = " fake_shadows=true" if len(m) > 6 and m[6].get("fake_shadows") else ""
-            out.append(f"material {name} rough_glass " + " ".join(repr(float(x)) for x in vals) + fake)
+            out.append(f"material {name} rough_glass " + " ".join(repr(float(x)) for x in vals) + fake + slot_extra)
         else:
-            out.append(f"material {name} {t} " + " ".join(repr(float(x)) for x in m[1]))
+            out.append(f"material {name} {t} " + " ".join(repr(float(x)) for x in m[1]) + slot_extra)
     for o in scene["objects"]:
         v = np.asarray(o["vertices"], np.float32)
         f = np.asarray(o["faces"], np.uint32)

@@ -69,3 +69,31 @@ def test_gpu_procedural_texture_needs_noise_tables(cuda_device):
     gbrt.check(gbrt.load().gbrt_scene_set_textures(r._h, None, 0, None, descs, 1, gbrt._ptr(mt), len(mt)))
     img, _ = r.render(2)
     assert np.isfinite(img).all()
+
+
+@pytest.mark.gpu
+def test_gpu_cornell_shader_nodes_match_reference(cuda_device):
+    """Shader node trees on every colour slot: mix nodes in the multiply
+    (with a texture's scalar as factor), overlay, darken, lighten, screen,
+    subtract, difference and add modes, a value node, two chained layer
+    nodes (stencil, upper_layer), texture mappers over procedural and image
+    textures; on shinydiffuse and glossy diffuse, glossy colour, glass and
+    rough-glass filter and mirror colours."""
+    _, tables, _ = golden()
+    g = np.load(os.path.join(GOLD, "cornell_nodes_64_render.npz"))
+    r = gbrt.Renderer(scenes.node_cornell_scene(tables, res=64))
+    gb = batches(r, int(g["spp"]), int(g["batches"]))
+    frac, relmse, m = parity(gb, g["mean"], g["se"])
+    print(f"cornell shader nodes 64x64: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
+          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
+    assert frac >= 0.995
+
+
+@pytest.mark.gpu
+def test_gpu_shader_nodes_reject_bad_trees(cuda_device):
+    """Inputs must lie below a node, slots must exist on the material type."""
+    _, tables, _ = golden()
+    sc = scenes.node_cornell_scene(tables, res=8)
+    sc["material_shaders"]["grey"] = {"glossy_shader": "m_clouds"}     # shinydiffuse has no glossy slot
+    with pytest.raises(gbrt.GbrtError):
+        gbrt.Renderer(sc)
