@@ -223,6 +223,7 @@ struct SceneDev {
 	const uint4 *face_nrm;      // normal indices per face; x = kFlatFace: geometric normal; w = kTriFace: triangle
 	gbrt::NoiseTables nt;       // the host's noise tables (gbrt_scene_set_noise_tables); null without
 	const gbrt_shader_node *nodes;   // shader node trees (gbrt_scene_set_shader_nodes); null without
+	const uint32_t *prim_slot;  // primitive -> its record in the BVH's leaf order (bump mapping); null without
 };
 
 __device__ __forceinline__ float dot3(const float a[3], const float b[3]) { return xa(xa(xm(a[0], b[0]), xm(a[1], b[1])), xm(a[2], b[2])); }
@@ -904,14 +905,13 @@ __device__ __forceinline__ float image_adjust_float(const DevTexture &T, float v
 // Texture::applyAdjustments (texture.cc:219-253): the texture's RGBA at a
 // hit (getColor); with scalar, also its getFloat (for an image,
 // applyIntensityContrastAdjustments of the colour's brightness, texture.h:52).
-__device__ void tex_eval(const SceneDev &sc, const DevTexture &T, const float p[3], const float ng[3], const float uv[2], float out[4],
-                         float *scalar)
+__device__ void tex_domap(const DevTexture &T, const float c[3], const float ng[3], float t[3])
 {
 	float q[3];
-	if(T.texco == GBRT_TEXCO_UV) { q[0] = xs(xm(2.f, uv[0]), 1.f); q[1] = xs(xm(2.f, uv[1]), 1.f); q[2] = 0.f; }
-	else { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+	if(T.texco == GBRT_TEXCO_UV) { q[0] = xs(xm(2.f, c[0]), 1.f); q[1] = xs(xm(2.f, c[1]), 1.f); q[2] = c[2]; }
+	else { q[0] = c[0]; q[1] = c[1]; q[2] = c[2]; }
 	const float tm[4] = {0.f, q[0], q[1], q[2]};
-	float t[3] = {tm[T.proj[0]], tm[T.proj[1]], tm[T.proj[2]]};
+	t[0] = tm[T.proj[0]]; t[1] = tm[T.proj[1]]; t[2] = tm[T.proj[2]];
 	if(T.mapping == GBRT_MAPPING_CUBE)
 	{
 		// cubeMap: axis of the largest normal component (ties to z, then y)
@@ -948,6 +948,19 @@ __device__ void tex_eval(const SceneDev &sc, const DevTexture &T, const float p[
 		t[0] = r[0]; t[1] = r[1]; t[2] = r[2];
 	}
 	for(int k = 0; k < 3; ++k) t[k] = xa(xm(t[k], T.scale[k]), T.offset2[k]);
+}
+
+// TextureMapperNode::getCoords (shader_node_texture.cc:203-230): the hit
+// position, or (u, v, 0) for uv coordinates.
+__device__ __forceinline__ void tex_coords(const DevTexture &T, const float p[3], const float uv[2], float c[3])
+{
+	if(T.texco == GBRT_TEXCO_UV) { c[0] = uv[0]; c[1] = uv[1]; c[2] = 0.f; }
+	else { c[0] = p[0]; c[1] = p[1]; c[2] = p[2]; }
+}
+
+// The texture's getColor and (with scalar) getFloat at a texture-space point.
+__device__ void tex_eval_at(const SceneDev &sc, const DevTexture &T, const float t[3], float out[4], float *scalar)
+{
 	if(T.kind != GBRT_TEX_IMAGE)
 	{
 		// a procedural texture at the mapped point
@@ -1058,6 +1071,15 @@ __device__ void tex_eval(const SceneDev &sc, const DevTexture &T, const float p[
 	}
 	out[0] = r[0]; out[1] = r[1]; out[2] = r[2]; out[3] = alpha;
 	if(scalar) *scalar = image_adjust_float(T, xa(xa(xm(0.2126f, r[0]), xm(0.7152f, r[1])), xm(0.0722f, r[2])));
+}
+
+__device__ void tex_eval(const SceneDev &sc, const DevTexture &T, const float p[3], const float ng[3], const float uv[2], float out[4],
+                         float *scalar)
+{
+	float c[3], t[3];
+	tex_coords(T, p, uv, c);
+	tex_domap(T, c, ng, t);
+	tex_eval_at(sc, T, t, out, scalar);
 }
 
 // A diffuse shader of gbrt_scene_set_textures: the texture through its
@@ -1256,6 +1278,121 @@ __device__ __noinline__ void node_tree(const SceneDev &sc, int first, int root, 
 
 // The diffuse colour of a surface point (the material's, or its diffuse
 // shader's texture at the hit's coordinates).
+// TextureMapperNode::evalDerivative (shader_node_texture.cc:255-355) of a
+// texture node: the texture's getFloat differences along the surface frame
+// (s.u, s.v: createCoordsSystem of the shading normal) around the point, or,
+// for an image through uv coordinates of a uv-mapped mesh, its slopes in
+// texture space carried into shading space by dP/du, dP/dv
+// (PrimitivePolygon::getSurfacePolygon, primitive_polygon.cc:70-114).
+__device__ void tex_derivative(const SceneDev &sc, const DevTexture &T, float bump_strength, const Surface &s, int prim, const float uv[2],
+                               float &du, float &dv)
+{
+	const bool image = T.kind == GBRT_TEX_IMAGE;
+	const float d_u = image ? __fdiv_rn(1.f, static_cast<float>(T.w)) : 0.0002f;
+	const float d_v = image ? __fdiv_rn(1.f, static_cast<float>(T.h)) : 0.0002f;
+	// bump_strength / |scale| / 100 (the mapper's constructor)
+	const float len = sqrtf(xa(xa(xm(T.scale[0], T.scale[0]), xm(T.scale[1], T.scale[1])), xm(T.scale[2], T.scale[2])));
+	const float bs = __fdiv_rn(__fdiv_rn(bump_strength, len), 100.f);
+	const uint4 fu = __ldg(sc.face_uv + prim);
+	float c[3], f0, f1, g0, g1, col[4];
+	tex_coords(T, s.p, uv, c);
+	if(image && fu.x != kNoIdx && T.texco == GBRT_TEXCO_UV)
+	{
+		float t[3], q[3];
+		tex_domap(T, c, s.ng, t);
+		q[0] = xs(t[0], d_u); q[1] = t[1]; q[2] = t[2]; tex_eval_at(sc, T, q, col, &f0);
+		q[0] = xa(t[0], d_u); tex_eval_at(sc, T, q, col, &f1);
+		q[0] = t[0]; q[1] = xs(t[1], d_v); tex_eval_at(sc, T, q, col, &g0);
+		q[1] = xa(t[1], d_v); tex_eval_at(sc, T, q, col, &g1);
+		const float dfdu = __fdiv_rn(xs(f0, f1), d_u), dfdv = __fdiv_rn(xs(g0, g1), d_v);
+		// dP/du, dP/dv of the face from its first three corners and uvs
+		const uint32_t slot = __ldg(sc.prim_slot + prim);
+		const float4 B = __ldg(sc.bv.tris + 3ull * slot + 1), C = __ldg(sc.bv.tris + 3ull * slot + 2);
+		const float e1[3] = {B.x, B.y, B.z}, e2[3] = {C.x, C.y, C.z};
+		const float2 a = __ldg(sc.uv + fu.x), b = __ldg(sc.uv + fu.y), cc = __ldg(sc.uv + fu.z);
+		const float d1u = xs(b.x, a.x), d1v = xs(b.y, a.y), d2u = xs(cc.x, a.x), d2v = xs(cc.y, a.y);
+		const float det = xs(xm(d1u, d2v), xm(d1v, d2u));
+		float dpu[3], dpv[3];
+		if(fabsf(det) > 1e-30f)
+		{
+			const float inv = __fdiv_rn(1.f, det);
+			for(int k = 0; k < 3; ++k)
+			{
+				dpu[k] = xm(xs(xm(d2v, e1[k]), xm(d1v, e2[k])), inv);
+				dpv[k] = xm(xs(xm(d1u, e2[k]), xm(d2u, e1[k])), inv);
+			}
+		}
+		else for(int k = 0; k < 3; ++k) { dpu[k] = e1[k]; dpv[k] = e2[k]; }
+		normalize3(dpu);
+		normalize3(dpv);
+		float vu[3] = {dot3(s.u, dpu), dot3(s.v, dpu), dfdu};
+		float vv[3] = {dot3(s.u, dpv), dot3(s.v, dpv), dfdv};
+		float nrm[3] = {xs(xm(vu[1], vv[2]), xm(vu[2], vv[1])), xs(xm(vu[2], vv[0]), xm(vu[0], vv[2])), xs(xm(vu[0], vv[1]), xm(vu[1], vv[0]))};
+		normalize3(nrm);
+		if(fabsf(nrm[2]) > 1e-30f)
+		{
+			const float nf = xm(__fdiv_rn(1.f, nrm[2]), bs);
+			du = xm(nrm[0], nf);
+			dv = xm(nrm[1], nf);
+		}
+		else du = dv = 0.f;
+		return;
+	}
+	float q[3], t[3];
+	for(int k = 0; k < 3; ++k) q[k] = xs(c[k], xm(d_u, s.u[k]));
+	tex_domap(T, q, s.ng, t); tex_eval_at(sc, T, t, col, &f0);
+	for(int k = 0; k < 3; ++k) q[k] = xa(c[k], xm(d_u, s.u[k]));
+	tex_domap(T, q, s.ng, t); tex_eval_at(sc, T, t, col, &f1);
+	for(int k = 0; k < 3; ++k) q[k] = xs(c[k], xm(d_v, s.v[k]));
+	tex_domap(T, q, s.ng, t); tex_eval_at(sc, T, t, col, &g0);
+	for(int k = 0; k < 3; ++k) q[k] = xa(c[k], xm(d_v, s.v[k]));
+	tex_domap(T, q, s.ng, t); tex_eval_at(sc, T, t, col, &g1);
+	du = xm(__fdiv_rn(xs(f0, f1), d_u), bs);
+	dv = xm(__fdiv_rn(xs(g0, g1), d_v), bs);
+	if(T.texco != GBRT_TEXCO_UV) { du = -du; dv = -dv; }
+}
+
+// NodeMaterial::evalBump (material_node.cc:95-100): the bump tree's
+// evalDerivative results (texture nodes above; LayerNode::evalDerivative,
+// shader_node_layer.cc:196-225; other nodes zero) and Material::applyBump
+// (material.cc:218-225) on the shading frame.
+__device__ __noinline__ void surface_bump(const SceneDev &sc, Surface &s, int first, int root, uint32_t mask, int prim, const float uv[2])
+{
+	float R[GBRT_TREE_MAX][4];
+	for(int i = first; i <= root; ++i)
+	{
+		if(!((mask >> (i - first)) & 1u)) continue;
+		const gbrt_shader_node &N = sc.nodes[i];
+		float *r = R[i - first];
+		if(N.type == GBRT_NODE_TEXTURE)
+		{
+			tex_derivative(sc, sc.tex[N.texture], N.bump_strength, s, prim, uv, r[0], r[1]);
+			r[2] = 0.f; r[3] = 0.f;
+		}
+		else if(N.type == GBRT_NODE_LAYER)
+		{
+			float rdu = 0.f, rdv = 0.f, stencil = 1.f;
+			if(N.input2 >= 0) { const float *u = R[N.input2 - first]; rdu = u[0]; rdv = u[1]; stencil = u[3]; }
+			const float *t = R[N.input1 - first];
+			float tdu = t[0], tdv = t[1];
+			if(N.negative) { tdu = -tdu; tdv = -tdv; }
+			r[0] = xa(rdu, tdu); r[1] = xa(rdv, tdv); r[2] = 0.f; r[3] = stencil;
+		}
+		else { r[0] = r[1] = r[2] = 0.f; r[3] = 1.f; }
+	}
+	const float du = R[root - first][0], dv = R[root - first][1];
+	for(int k = 0; k < 3; ++k) { s.u[k] = xa(s.u[k], xm(du, s.n[k])); s.v[k] = xa(s.v[k], xm(dv, s.n[k])); }
+	s.n[0] = xs(xm(s.u[1], s.v[2]), xm(s.u[2], s.v[1]));
+	s.n[1] = xs(xm(s.u[2], s.v[0]), xm(s.u[0], s.v[2]));
+	s.n[2] = xs(xm(s.u[0], s.v[1]), xm(s.u[1], s.v[0]));
+	normalize3(s.n);
+	normalize3(s.u);
+	s.v[0] = xs(xm(s.n[1], s.u[2]), xm(s.n[2], s.u[1]));
+	s.v[1] = xs(xm(s.n[2], s.u[0]), xm(s.n[0], s.u[2]));
+	s.v[2] = xs(xm(s.n[0], s.u[1]), xm(s.n[1], s.u[0]));
+	normalize3(s.v);
+}
+
 // With shader node trees on its slots the material is copied to mloc with
 // the slot colours of this point (the reference's getShaderColor of each
 // slot) and s.m points there: the diffuse colour of shinydiffuse (s.dcol)
@@ -1265,6 +1402,9 @@ __device__ __noinline__ void surface_nodes(const SceneDev &sc, Surface &s, int p
 	mloc = *s.m;
 	float uv[2];
 	hit_uv(sc, prim, bu, bv, uv);
+	// the bump first: the colour nodes see the bumped surface (initBsdf)
+	if(mloc.nroot[GBRT_SLOT_BUMP] >= 0)
+		surface_bump(sc, s, mloc.nfirst[GBRT_SLOT_BUMP], mloc.nroot[GBRT_SLOT_BUMP], mloc.nmask[GBRT_SLOT_BUMP], prim, uv);
 	for(int slot = 0; slot < GBRT_SLOT_BUMP; ++slot)
 	{
 		if(mloc.nroot[slot] < 0) continue;
@@ -2640,13 +2780,14 @@ __device__ __noinline__ void shaded_transparency(const SceneDev &sc, const DevMa
 	shading_normal(sc, prim, u, v, ng, ns);
 	if(m.has_nodes)
 	{
-		// the slot colours of this point (diffuse and filter colour)
+		// the slot colours (diffuse, filter) and the bumped normal of this point
 		Surface s;
-		for(int k = 0; k < 3; ++k) { s.p[k] = p[k]; s.ng[k] = ng[k]; s.dcol[k] = dcol[k]; }
+		for(int k = 0; k < 3; ++k) { s.p[k] = p[k]; s.ng[k] = ng[k]; s.dcol[k] = dcol[k]; s.n[k] = ns[k]; }
+		coords_system(s.n, s.u, s.v);
 		s.m = &m;
 		DevMaterial ml;
 		surface_nodes(sc, s, prim, u, v, ml);
-		mat_transparency(ml, ng, ns, dir, s.dcol, tr);
+		mat_transparency(ml, ng, s.n, dir, s.dcol, tr);
 	}
 	else mat_transparency(m, ng, ns, dir, dcol, tr);
 }
@@ -3707,10 +3848,21 @@ struct gbrt_scene {
 	uint8_t *noise_dev = nullptr;
 	// shader node trees (gbrt_scene_set_shader_nodes)
 	gbrt_shader_node *nodes = nullptr;
+	uint32_t *prim_slot = nullptr;      // primitive -> BVH leaf-order record (bump mapping)
 	uint32_t n_tex = 0;
 	std::vector<DevMaterial> mats_host;
 	std::mutex mu;
 };
+
+// prim_slot[ids[i] without the quad bit] = i: each primitive's record in
+// the BVH's leaf order.
+__global__ void k_prim_slot(const uint32_t *__restrict__ ids, uint32_t n, uint32_t *__restrict__ slot)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	const uint32_t p = ids[i] & ~GBRT_QUAD_BIT;
+	if(p < n) slot[p] = i;
+}
 
 // Every material plain (the diffuse layer of shinydiffuse alone, an
 // untextured colour, or light_mat) and no shading normals: the scenes
@@ -4090,7 +4242,7 @@ SceneDev scene_dev(const gbrt_scene *S)
 {
 	return SceneDev{gbrt::view_of(S->bvh), S->prim_ng, S->mats, S->lights, {S->lds_perm, S->lds_off, S->lds_base, S->lds_inv, S->lds_sfac, S->lds_sfac_off, S->lds_sfac_nd,
 	                                                                         S->lds_fx, S->lds_fx_dims, S->lds_fx_rad3},
-	                S->tex, S->texels, S->uv, S->face_uv, S->vnrm, S->face_nrm, noise_view(S), S->nodes};
+	                S->tex, S->texels, S->uv, S->face_uv, S->vnrm, S->face_nrm, noise_view(S), S->nodes, S->prim_slot};
 }
 
 } // namespace
@@ -4470,7 +4622,8 @@ int gbrt_scene_set_shader_nodes(gbrt_scene *S, const gbrt_shader_node *nodes, ui
 			if(root < 0) continue;
 			if(static_cast<uint32_t>(root) >= n_nodes)
 				return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_shader_nodes: material %u slot %d: node %d of %u", m, k, root, n_nodes);
-			const bool ok = (k == GBRT_SLOT_DIFFUSE && (d.type == GBRT_MAT_SHINYDIFFUSE || d.type == GBRT_MAT_GLOSSY)) ||
+			const bool ok = (k == GBRT_SLOT_BUMP && d.type != GBRT_MAT_LIGHT) ||
+			                (k == GBRT_SLOT_DIFFUSE && (d.type == GBRT_MAT_SHINYDIFFUSE || d.type == GBRT_MAT_GLOSSY)) ||
 			                (k == GBRT_SLOT_GLOSSY && d.type == GBRT_MAT_GLOSSY) ||
 			                (k == GBRT_SLOT_MIRROR_COLOR && (d.type == GBRT_MAT_SHINYDIFFUSE || d.type == GBRT_MAT_GLASS || d.type == GBRT_MAT_ROUGH_GLASS)) ||
 			                (k == GBRT_SLOT_FILTER_COLOR && (d.type == GBRT_MAT_GLASS || d.type == GBRT_MAT_ROUGH_GLASS));
@@ -4497,10 +4650,20 @@ int gbrt_scene_set_shader_nodes(gbrt_scene *S, const gbrt_shader_node *nodes, ui
 			d.has_nodes = 1u;
 		}
 	}
+	bool bump = false;
+	for(const DevMaterial &d : mats) bump = bump || d.nroot[GBRT_SLOT_BUMP] >= 0;
 	std::lock_guard<std::mutex> lock(S->mu);
 	if(S->ev_last) GBRT_CK(cudaEventSynchronize(S->ev_last));
 	if(S->nodes) cudaFree(S->nodes);
 	S->nodes = nullptr;
+	if(bump && !S->prim_slot && S->n_prims)
+	{
+		// the inverse of the BVH's leaf order, for the faces' edge vectors
+		GBRT_CK(cudaMalloc(reinterpret_cast<void **>(&S->prim_slot), S->n_prims * sizeof(uint32_t)));
+		k_prim_slot<<<(S->n_prims + 255) / 256, 256>>>(S->bvh->wids, S->n_prims, S->prim_slot);
+		GBRT_CK(cudaGetLastError());
+		GBRT_CK(cudaDeviceSynchronize());
+	}
 	GBRT_CK(cudaMalloc(reinterpret_cast<void **>(&S->nodes), std::max<uint32_t>(1, n_nodes) * sizeof(gbrt_shader_node)));
 	if(n_nodes) GBRT_CK(cudaMemcpy(S->nodes, nodes, n_nodes * sizeof(gbrt_shader_node), cudaMemcpyHostToDevice));
 	GBRT_CK(cudaMemcpy(S->mats, mats.data(), mats.size() * sizeof(DevMaterial), cudaMemcpyHostToDevice));
@@ -4568,7 +4731,8 @@ int gbrt_scene_destroy(gbrt_scene *S)
 	                S->lds_sfac_nd, S->lds_fx, S->work, S->spawn, S->spawn_count};
 	for(void *p : ptrs) if(p) cudaFree(p);
 	for(void *p : {static_cast<void *>(S->tex), static_cast<void *>(S->texels), static_cast<void *>(S->uv), static_cast<void *>(S->face_uv),
-	               static_cast<void *>(S->vnrm), static_cast<void *>(S->face_nrm), static_cast<void *>(S->noise_dev), static_cast<void *>(S->nodes)})
+	               static_cast<void *>(S->vnrm), static_cast<void *>(S->face_nrm), static_cast<void *>(S->noise_dev), static_cast<void *>(S->nodes),
+	               static_cast<void *>(S->prim_slot)})
 		if(p) cudaFree(p);
 	if(S->filter_dev) cudaFree(S->filter_dev);
 	if(S->ev_last) cudaEventDestroy(S->ev_last);

@@ -137,13 +137,14 @@ def _rgba(v, alpha=1.0):
     return v + [alpha] if len(v) == 3 else v[:4]
 
 
-def shader_nodes(scene):
+def shader_nodes(scene, texture_base=0):
     """The scene's shader node trees ("nodes": name -> node dict with the
     reference's parameter names; "material_shaders": material name ->
     {slot parameter name: node name}) as gbrt_shader_node entries in an
     order where every node follows its inputs, the textures their
     texture_mapper nodes read (texture dict + the node's mapper
-    parameters), and per material the GBRT_SLOTS root indices."""
+    parameters; their texture indices start at texture_base), and the node
+    index of each name."""
     nodes = scene.get("nodes", {})
     order, seen = [], set()
 
@@ -175,7 +176,7 @@ def shader_nodes(scene):
             mp["proj"] = tuple(int(nd.get(f"proj_{a}", d0)) for a, d0 in (("x", 1), ("y", 2), ("z", 3)))
             tx["mapper"] = mp
             tx.pop("layer", None)
-            d.texture = len(textures)
+            d.texture = texture_base + len(textures)
             textures.append(tx)
             d.do_scalar = int(bool(nd.get("do_scalar", True)))
         elif nd["type"] == "value":
@@ -770,7 +771,7 @@ class Renderer:
         scene's "noise_tables" (the reference's NoiseGenerator tables)."""
         from . import scenes as _scenes
         names = list(self.scene.get("textures", {}).keys())
-        nodes, n_nodes, node_tex, _ = shader_nodes(self.scene)
+        nodes, n_nodes, node_tex, index = shader_nodes(self.scene, len(names))
         all_tex = [self.scene["textures"][n] for n in names] + node_tex
         if any(t.get("type", "image") != "image" for t in all_tex):
             nt, self._noise_keep = noise_tables(self.scene["noise_tables"])
@@ -792,7 +793,6 @@ class Renderer:
         check(load().gbrt_scene_set_textures(self._h, _ptr(uv), 0 if uv is None else len(uv), _ptr(fuv), descs, len(all_tex),
                                              _ptr(mt), len(mt)))
         if n_nodes:
-            _, _, _, index = shader_nodes(self.scene)
             slots = np.full((len(self.mat_names), N_SLOTS), -1, np.int32)
             for i, n in enumerate(self.mat_names):
                 for key, node in self.scene.get("material_shaders", {}).get(n, {}).items():

@@ -529,6 +529,50 @@ def node_cornell_scene(noise_tables, res=64, **kw):
     return sc
 
 
+def bump_cornell_scene(noise_tables, res=64, **kw):
+    """Bump mapping (bump_shader): the back wall (uv-mapped) bumped by a
+    noisy image through uv coordinates (the image branch of the mapper's
+    derivative: slopes in texture space through dP/du, dP/dv), the short box
+    by a marble texture in global coordinates, the tall box, glossy, by a
+    stencilled, negated layer over clouds with a voronoi upper layer, and
+    the glass ball by blender-noise clouds; the floor, ceiling and side
+    walls stay flat."""
+    sc = textured_cornell_scene(res=res, **kw)
+    sc["noise_tables"] = noise_tables
+    rng = np.random.default_rng(23)
+    bumps = rng.random((16, 16, 1)).astype(np.float32)
+    img = np.concatenate([bumps, bumps, bumps, np.ones((16, 16, 1), np.float32)], -1)
+    sc["textures"] = {
+        "bumps": {"image": img, "interpolate": "bilinear", "clipping": "repeat"},
+        "marble": {"type": "marble", "noise_type": "newperlin", "depth": 2, "turbulence": 2.0},
+        "clouds": {"type": "clouds", "noise_type": "newperlin", "depth": 3, "size": 0.5},
+        "cells": {"type": "voronoi", "size": 2.0},
+        "noise": {"type": "clouds", "noise_type": "blender", "depth": 2, "size": 0.3},
+    }
+    sc["nodes"] = {
+        "b_img": {"type": "texture_mapper", "texture": "bumps", "texco": "uv", "bump_strength": 2.0},
+        "b_marble": {"type": "texture_mapper", "texture": "marble", "scale": (3.0, 3.0, 3.0), "bump_strength": 4.0},
+        "b_clouds": {"type": "texture_mapper", "texture": "clouds", "bump_strength": 3.0},
+        "b_cells": {"type": "texture_mapper", "texture": "cells", "bump_strength": 1.5},
+        "b_up": {"type": "layer", "input": "b_cells"},
+        "b_layer": {"type": "layer", "input": "b_clouds", "upper_layer": "b_up", "negative": True, "stencil": True},
+        "b_noise": {"type": "texture_mapper", "texture": "noise", "bump_strength": 2.5},
+    }
+    sc["materials"]["back_tex"] = ("shinydiffusemat", (0.75, 0.75, 0.75))
+    sc["materials"]["box2_tex"] = ("shinydiffusemat", (0.8, 0.7, 0.4))
+    sc["materials"]["box_tex"] = glossy_material((0.6, 0.65, 0.75), exponent=80.0, glossy_reflect=0.6)
+    sc["materials"]["glass"] = glass_material(1.5)
+    v, f = icosphere((0.35, 0.85, 0.25), 0.25, 2)
+    sc["objects"].insert(-1, {"name": "glass_ball", "material": "glass", "vertices": v, "faces": f})
+    sc["material_shaders"] = {
+        "back_tex": {"bump_shader": "b_img"},
+        "box2_tex": {"bump_shader": "b_marble"},
+        "box_tex": {"bump_shader": "b_layer"},
+        "glass": {"bump_shader": "b_noise"},
+    }
+    return sc
+
+
 def cornell_sppm_scene(res=48, photons=100000, passes=8, bounces=5, pm_ire=False, photon_radius=0.1, search_num=10):
     """The glass Cornell box (a glass and a rough-glass ball) rendered by the
     "SPPM" integrator: caustics under the balls come from the photon

@@ -22,7 +22,8 @@ vertex normals), cornell_pt_caustics (pathtracing caustic_type / no_recursive),
 pm_full (config-5 photon maps at full size, as bucketed digests),
 cornell_512 (the Cornell configuration at 512x512), cornell_procedural
 (procedural textures; needs procedural.npz from make_golden.py procedural),
-cornell_nodes (shader node trees on every colour slot; the same tables).
+cornell_nodes (shader node trees on every colour slot; the same tables),
+cornell_bump (bump mapping; the same tables).
 """
 import os
 import struct
@@ -373,6 +374,17 @@ if __name__ == "__main__":
                             se=(rgb.std(0, ddof=1) / np.sqrt(32)).astype(np.float32), batches=np.int32(32),
                             spp=np.int32(16), seconds=secs)
         print(f"cornell_nodes_64_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
+    if "cornell_bump" in what:
+        # bump mapping: an image through uvs, marble in global coordinates, a
+        # layer chain over clouds and voronoi, blender noise on glass
+        g = np.load(os.path.join(OUT, "procedural.npz"))
+        tables = {k[len("table_"):]: g[k] for k in g.files if k.startswith("table_")}
+        sc = scenes.bump_cornell_scene(tables, res=64)
+        rgb, secs = orc.run_reference_render(sc, 16, 32, threads=os.cpu_count() or 1)
+        np.savez_compressed(os.path.join(OUT, "cornell_bump_64_render.npz"), mean=rgb.mean(0).astype(np.float32),
+                            se=(rgb.std(0, ddof=1) / np.sqrt(32)).astype(np.float32), batches=np.int32(32),
+                            spp=np.int32(16), seconds=secs)
+        print(f"cornell_bump_64_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
     if "cornell_sppm" in what:
         # SPPM: the glass Cornell box, 100,000 photon paths x 8 passes; batch k
         # at sample offsets 8k .. 8k + 7 (a fresh integrator per batch)

@@ -97,3 +97,19 @@ def test_gpu_shader_nodes_reject_bad_trees(cuda_device):
     sc["material_shaders"]["grey"] = {"glossy_shader": "m_clouds"}     # shinydiffuse has no glossy slot
     with pytest.raises(gbrt.GbrtError):
         gbrt.Renderer(sc)
+
+
+@pytest.mark.gpu
+def test_gpu_cornell_bump_matches_reference(cuda_device):
+    """Bump mapping on four materials: an image bump map through uv
+    coordinates (the texture-space slope branch), marble in global
+    coordinates (shinydiffuse), a negated, stencilled layer over clouds with
+    a voronoi upper layer (glossy), blender-noise clouds (glass)."""
+    _, tables, _ = golden()
+    g = np.load(os.path.join(GOLD, "cornell_bump_64_render.npz"))
+    r = gbrt.Renderer(scenes.bump_cornell_scene(tables, res=64))
+    gb = batches(r, int(g["spp"]), int(g["batches"]))
+    frac, relmse, m = parity(gb, g["mean"], g["se"])
+    print(f"cornell bump 64x64: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g}, "
+          f"means gpu {m.mean(axis=(0, 1))} ref {g['mean'].mean(axis=(0, 1))}")
+    assert frac >= 0.995

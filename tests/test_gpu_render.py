@@ -341,4 +341,4 @@ def test_gpu_render_batch_equals_single_renders(cuda_device):
         for f, single in zip(films, singles):
             assert torch.allclose(f, single, rtol=1e-4, atol=1e-6)
         if tuning is None:
-            assert used["wave_paths"] in (1 << 20, 1 << 21, 1 << 22, 1 << 23) and used["shade_block"] in (64, 128)
+            assert used["wave_paths"] in (1 << 19, 1 << 20, 1 << 21, 1 << 22) and used["shade_block"] in (64, 128)
