@@ -1,6 +1,8 @@
 // extern "C" entry points of libgbrt (declared in include/gbrt.h).
 #include "gbrt_internal.cuh"
 
+#include <cuda.h>
+
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -29,10 +31,46 @@ namespace {
 std::mutex g_stage_init_mu;
 constexpr uint32_t kStageRays = 1u << 21;  // 2 Mi rays = 64 MiB per slot
 
-// Pipelined host path: chunk k's upload, trace and download run on stream
-// k % 2, so the copies of one chunk overlap the traversal of the other.  With
-// pinned host buffers every copy is asynchronous; pageable buffers still work
-// (the runtime stages them).
+// Whether [p, p + bytes) lies inside one page-locked host allocation the
+// device can address (pinned memory under unified addressing): the pointer's
+// attributes say host memory with a device mapping, and the driver's range
+// of the allocation (cuPointerGetAttribute RANGE_START_ADDR / RANGE_SIZE)
+// covers the whole span.  Anything else - pageable memory, a failed query -
+// answers false.
+bool mapped_host_range(const void *p, size_t bytes, void **dev)
+{
+	cudaPointerAttributes a{};
+	if(cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+	if(a.type != cudaMemoryTypeHost || !a.devicePointer || a.devicePointer != p) return false;
+	using GetAttr = CUresult (*)(void *, CUpointer_attribute, CUdeviceptr);
+	static GetAttr get_attr = [] {
+		void *fn = nullptr;
+		cudaDriverEntryPointQueryResult q{};
+		if(cudaGetDriverEntryPoint("cuPointerGetAttribute", &fn, cudaEnableDefault, &q) != cudaSuccess || q != cudaDriverEntryPointSuccess)
+		{
+			cudaGetLastError();
+			return static_cast<GetAttr>(nullptr);
+		}
+		return reinterpret_cast<GetAttr>(fn);
+	}();
+	if(!get_attr) return false;
+	CUdeviceptr start = 0;
+	size_t size = 0;
+	if(get_attr(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, reinterpret_cast<CUdeviceptr>(p)) != CUDA_SUCCESS ||
+	   get_attr(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, reinterpret_cast<CUdeviceptr>(p)) != CUDA_SUCCESS)
+		return false;
+	const uintptr_t lo = static_cast<uintptr_t>(start), q = reinterpret_cast<uintptr_t>(p);
+	if(q < lo || q - lo > size || bytes > size - (q - lo)) return false;
+	*dev = a.devicePointer;
+	return true;
+}
+
+// Host path.  Rays and results in page-locked host memory that the device
+// maps are read and written by the traversal kernel itself, over the
+// host-device link, in one launch (no staging copies).  Otherwise the
+// pipelined path: chunk k's upload, trace and download run on stream k % 2,
+// so the copies of one chunk overlap the traversal of the other (pageable
+// buffers still work: the runtime stages them).
 int stage_and_trace(gbrt_bvh *b, const gbrt_ray *rays, uint32_t n, void *out, size_t out_rec, bool shadow)
 {
 	{
@@ -51,6 +89,19 @@ int stage_and_trace(gbrt_bvh *b, const gbrt_ray *rays, uint32_t n, void *out, si
 	}
 	// gbrt_bvh_build synchronised its stream, so the hierarchy is complete.
 	int rc = GBRT_OK;
+	void *rays_dev = nullptr, *out_dev = nullptr;
+	// the kernel loads rays and stores hits as 16-byte vectors (4-byte occluder IDs)
+	const bool aligned = (reinterpret_cast<uintptr_t>(rays) & 15u) == 0 && (reinterpret_cast<uintptr_t>(out) & (shadow ? 3u : 15u)) == 0;
+	if(aligned && mapped_host_range(rays, sizeof(gbrt_ray) * static_cast<size_t>(n), &rays_dev) &&
+	   mapped_host_range(out, out_rec * static_cast<size_t>(n), &out_dev))
+	{
+		cudaStream_t st = b->stage_stream[0];
+		rc = shadow ? gbrt_launch_shadow(b, static_cast<const gbrt_ray *>(rays_dev), n, static_cast<int32_t *>(out_dev), st)
+		            : gbrt_launch_closest(b, static_cast<const gbrt_ray *>(rays_dev), n, static_cast<gbrt_hit *>(out_dev), st);
+		GBRT_CK(cudaStreamSynchronize(st));
+		if(dev != b->device) cudaSetDevice(dev);
+		return rc;
+	}
 	uint32_t chunk = 0;
 	for(uint64_t off = 0; off < n; off += kStageRays, ++chunk)
 	{

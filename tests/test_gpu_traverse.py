@@ -92,6 +92,40 @@ def test_gpu_device_pointer_path_matches_host_path(dev):
     assert np.array_equal(occ.cpu().numpy() >= 0, p2 >= 0)
 
 
+def test_gpu_pinned_host_buffers_direct_path(dev):
+    """gbrt_trace_closest_host / _shadow_host with page-locked buffers (the
+    kernel reads rays from and writes results to host memory directly),
+    with a pinned buffer offset by 4 bytes (misaligned: the staged path),
+    and with pageable buffers: every form equals the device-pointer path."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    v, f = scenes.random_triangles(50_000, seed=43)
+    r = scenes.random_rays(300_000, seed=44)
+    bvh = gbrt.Bvh.build_host(v, f)
+    rt = torch.from_numpy(r).cuda()
+    hits = torch.empty((len(r), 4), dtype=torch.float32, device="cuda")
+    occ = torch.empty(len(r), dtype=torch.int32, device="cuda")
+    bvh.trace_closest_device(rt.data_ptr(), len(r), hits.data_ptr())
+    bvh.trace_shadow_device(rt.data_ptr(), len(r), occ.data_ptr())
+    torch.cuda.synchronize()
+    ref_h, ref_o = hits.cpu().numpy(), occ.cpu().numpy()
+    L = gbrt.load()
+    rp = torch.from_numpy(r).pin_memory()
+    hp = torch.empty((len(r), 4), dtype=torch.float32).pin_memory()
+    op = torch.empty(len(r), dtype=torch.int32).pin_memory()
+    gbrt.check(L.gbrt_trace_closest_host(bvh.handle, ctypes.c_void_p(rp.data_ptr()), len(r), ctypes.c_void_p(hp.data_ptr())))
+    gbrt.check(L.gbrt_trace_shadow_host(bvh.handle, ctypes.c_void_p(rp.data_ptr()), len(r), ctypes.c_void_p(op.data_ptr())))
+    assert np.array_equal(hp.numpy().view(np.uint32), ref_h.view(np.uint32))
+    assert np.array_equal(op.numpy(), ref_o)
+    # misaligned result buffer inside a pinned allocation: the staged path
+    big = torch.empty(len(r) * 4 + 1, dtype=torch.float32).pin_memory()
+    gbrt.check(L.gbrt_trace_closest_host(bvh.handle, ctypes.c_void_p(rp.data_ptr()), len(r), ctypes.c_void_p(big.data_ptr() + 4)))
+    assert np.array_equal(big.numpy()[1:].reshape(-1, 4).view(np.uint32), ref_h.view(np.uint32))
+    # pageable buffers
+    p2, t2, _, _ = bvh.trace_closest_host(r)
+    assert np.array_equal(p2, ref_h[:, 0].view(np.int32)) and np.array_equal(t2, ref_h[:, 1])
+
+
 def test_gpu_empty_and_single(dev):
     r = scenes.random_rays(1000, seed=51)
     bvh = gbrt.Bvh.build_host(np.zeros((0, 3), np.float32), np.zeros((0, 4), np.uint32))
