@@ -110,6 +110,7 @@ constexpr uint32_t kDead = 0xFFFFFFFFu;
 constexpr uint32_t kMaxBatch = 1u << 18;   // largest guide training batch
 constexpr float kRayMinDist = 0.00005f;   // Accelerator::min_raydist_ (accelerator.h:85)
 constexpr float kShadowBias = 0.0005f;    // Accelerator::shadow_bias_ (accelerator.h:86)
+constexpr uint32_t kSppmMaxGather = 1000u; // SppmIntegrator::n_max_gather_ (integrator_sppm.h:118)
 constexpr float kPi = 3.14159265358979323846f;
 constexpr float kInvPi = 0.31830988618379067154f;
 
@@ -3529,9 +3530,42 @@ __global__ void __launch_bounds__(kThreads) k_pm_root(SceneDev sc, Params P, Wor
 			}
 			if(!(s.m->flags & BF_DIFFUSE) || !P.g_caustic.n) continue;
 			const float r2 = P.sppm_r2[pixel];
+			// the reference gathers at most n_max_gather_ = 1000 photons, the
+			// nearest (integrator_sppm.h:118, PhotonMap::gather): beyond that
+			// many within the radius, the 1000th smallest squared distance
+			// (bisection over its float bits) bounds the sum
+			uint32_t within = 0;
+			gbrt::grid_range(P.g_caustic, s.p, r2, [&](uint32_t) { ++within; });
+			float cap = r2;
+			bool capped = false;
+			if(within > kSppmMaxGather)
+			{
+				uint32_t lo = 0u, hi = __float_as_uint(r2);        // count(d2 <= lo) < 1000 <= count(d2 <= hi)
+				for(int it = 0; it < 32 && hi - lo > 1u; ++it)
+				{
+					const uint32_t mid = lo + (hi - lo) / 2u;
+					const float x = __uint_as_float(mid);
+					uint32_t c = 0;
+					gbrt::grid_range(P.g_caustic, s.p, r2, [&](uint32_t j) {
+						const float4 q = __ldg(P.g_caustic.pos + j);
+						const float vx = q.x - s.p[0], vy = q.y - s.p[1], vz = q.z - s.p[2];
+						if(vx * vx + vy * vy + vz * vz <= x) ++c;
+					});
+					if(c >= kSppmMaxGather) hi = mid;
+					else lo = mid;
+				}
+				cap = __uint_as_float(hi);
+				capped = true;
+			}
 			float flux[3] = {0.f, 0.f, 0.f};
 			uint32_t cnt = 0;
 			gbrt::grid_range(P.g_caustic, s.p, r2, [&](uint32_t j) {
+				if(capped)
+				{
+					const float4 q = __ldg(P.g_caustic.pos + j);
+					const float vx = q.x - s.p[0], vy = q.y - s.p[1], vz = q.z - s.p[2];
+					if(!(vx * vx + vy * vy + vz * vz <= cap)) return;
+				}
 				const float4 pd = __ldg(P.g_caustic.dir + j), pc = __ldg(P.g_caustic.col + j);
 				const float pdir[3] = {pd.x, pd.y, pd.z};
 				float sc3[3];

@@ -385,6 +385,16 @@ if __name__ == "__main__":
                             se=(rgb.std(0, ddof=1) / np.sqrt(32)).astype(np.float32), batches=np.int32(32),
                             spp=np.int32(16), seconds=secs)
         print(f"cornell_bump_64_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
+    if "cornell_sppm_dense" in what:
+        # SPPM with 1,000,000 photon paths x 2 passes: in the glass ball's
+        # caustic thousands of photons lie within the initial radius, so the
+        # reference's 1,000-photon gather cap decides those pixels
+        sc = scenes.cornell_sppm_scene(res=48, photons=1000000, passes=2)
+        rgb, secs = orc.run_reference_render(sc, 1, 24, threads=os.cpu_count() or 1, offset_stride=2)
+        np.savez_compressed(os.path.join(OUT, "cornell_sppm_dense_48_render.npz"), mean=rgb.mean(0).astype(np.float32),
+                            se=(rgb.std(0, ddof=1) / np.sqrt(24)).astype(np.float32), batches=np.int32(24), passes=np.int32(2),
+                            photons=np.int32(1000000), seconds=secs)
+        print(f"cornell_sppm_dense_48_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
     if "cornell_sppm" in what:
         # SPPM: the glass Cornell box, 100,000 photon paths x 8 passes; batch k
         # at sample offsets 8k .. 8k + 7 (a fresh integrator per batch)

@@ -157,13 +157,15 @@ def test_gpu_cornell_textured_matches_reference(cuda_device):
     assert frac >= 0.995
 
 
-@pytest.mark.parametrize("name,ire", [("cornell_sppm_48_render.npz", False), ("cornell_sppm_ire_48_render.npz", True)])
+@pytest.mark.parametrize("name,ire", [("cornell_sppm_48_render.npz", False), ("cornell_sppm_ire_48_render.npz", True),
+                                      ("cornell_sppm_dense_48_render.npz", False)])
 def test_gpu_cornell_sppm_matches_reference(cuda_device, name, ire):
     """SPPM (SppmIntegrator): per pass a caustic photon map, one eye sample per
     pixel with direct light and the specular / glossy split, the caustic
     gather within each pixel's shrinking radius and the progressive update;
     with pmIRE the first pass's radius estimate from the diffuse and caustic
-    maps."""
+    maps; with 1,000,000 photon paths per pass the gather keeps the 1,000
+    nearest photons where more lie within the radius."""
     g = np.load(os.path.join(GOLD, name))
     passes = int(g["passes"])
     r = gbrt.Renderer(scenes.cornell_sppm_scene(res=48, photons=int(g["photons"]), passes=passes, pm_ire=ire))
