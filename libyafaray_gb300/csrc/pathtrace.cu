@@ -3534,11 +3534,28 @@ __global__ void __launch_bounds__(kThreads) k_pm_root(SceneDev sc, Params P, Wor
 			// nearest (integrator_sppm.h:118, PhotonMap::gather): beyond that
 			// many within the radius, the 1000th smallest squared distance
 			// (bisection over its float bits) bounds the sum
-			uint32_t within = 0;
-			gbrt::grid_range(P.g_caustic, s.p, r2, [&](uint32_t) { ++within; });
-			float cap = r2;
-			bool capped = false;
-			if(within > kSppmMaxGather)
+			float flux[3] = {0.f, 0.f, 0.f};
+			uint32_t cnt = 0;
+			auto gather = [&](bool capped, float cap) {
+				flux[0] = flux[1] = flux[2] = 0.f;
+				cnt = 0;
+				gbrt::grid_range(P.g_caustic, s.p, r2, [&](uint32_t j) {
+					if(capped)
+					{
+						const float4 q = __ldg(P.g_caustic.pos + j);
+						const float vx = q.x - s.p[0], vy = q.y - s.p[1], vz = q.z - s.p[2];
+						if(!(vx * vx + vy * vy + vz * vz <= cap)) return;
+					}
+					const float4 pd = __ldg(P.g_caustic.dir + j), pc = __ldg(P.g_caustic.col + j);
+					const float pdir[3] = {pd.x, pd.y, pd.z};
+					float sc3[3];
+					eval_flags(s, wo, pdir, BF_ALL, sc3);
+					flux[0] += sc3[0] * pc.x; flux[1] += sc3[1] * pc.y; flux[2] += sc3[2] * pc.z;
+					++cnt;
+				});
+			};
+			gather(false, r2);
+			if(cnt > kSppmMaxGather)
 			{
 				uint32_t lo = 0u, hi = __float_as_uint(r2);        // count(d2 <= lo) < 1000 <= count(d2 <= hi)
 				for(int it = 0; it < 32 && hi - lo > 1u; ++it)
@@ -3554,25 +3571,8 @@ __global__ void __launch_bounds__(kThreads) k_pm_root(SceneDev sc, Params P, Wor
 					if(c >= kSppmMaxGather) hi = mid;
 					else lo = mid;
 				}
-				cap = __uint_as_float(hi);
-				capped = true;
+				gather(true, __uint_as_float(hi));
 			}
-			float flux[3] = {0.f, 0.f, 0.f};
-			uint32_t cnt = 0;
-			gbrt::grid_range(P.g_caustic, s.p, r2, [&](uint32_t j) {
-				if(capped)
-				{
-					const float4 q = __ldg(P.g_caustic.pos + j);
-					const float vx = q.x - s.p[0], vy = q.y - s.p[1], vz = q.z - s.p[2];
-					if(!(vx * vx + vy * vy + vz * vz <= cap)) return;
-				}
-				const float4 pd = __ldg(P.g_caustic.dir + j), pc = __ldg(P.g_caustic.col + j);
-				const float pdir[3] = {pd.x, pd.y, pd.z};
-				float sc3[3];
-				eval_flags(s, wo, pdir, BF_ALL, sc3);
-				flux[0] += sc3[0] * pc.x; flux[1] += sc3[1] * pc.y; flux[2] += sc3[2] * pc.z;
-				++cnt;
-			});
 			if(cnt)
 			{
 				const float4 t4 = W.p_thr[path];
