@@ -2307,7 +2307,9 @@ struct SceneTable {
 // photonmapping, guiding, recording, recursive-split, texture and
 // shading-normal code is compiled out, which roughly halves the kernel's
 // registers and lets twice the warps stay resident.
-template <typename Src, bool kLean = false, bool kTex = true>
+// kGuide: a render with a path guide attached (guided sampling, training
+// records); without it that code is compiled out.
+template <typename Src, bool kLean = false, bool kTex = true, bool kGuide = false>
 __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uint32_t shadow_cap)
 {
 	const uint32_t n = W.count[cur];
@@ -2380,7 +2382,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 		}
 		// the previous vertex's record: incident radiance along its sampled
 		// direction = what the path adds from here on
-		if(!kLean && hit && W.p_sum && k >= 1 && k - 1 < P.rec_stride && W.r_valid[static_cast<size_t>(path) * P.rec_stride + (k - 1)] == 2u)
+		if(kGuide && hit && W.p_sum && k >= 1 && k - 1 < P.rec_stride && W.r_valid[static_cast<size_t>(path) * P.rec_stride + (k - 1)] == 2u)
 		{
 			const size_t slot = static_cast<size_t>(path) * P.rec_stride + (k - 1);
 			W.r_pre[slot] = W.p_sum[path];
@@ -2402,7 +2404,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 					// photonmapping adds it twice (integrator_photon_mapping.cc:686-687, 713-721)
 					const float em = P.pm == 1 ? 2.f : 1.f;
 					film_put(P, film, film64, pixel, si, xm(thr[0], e[0]) * em, xm(thr[1], e[1]) * em, xm(thr[2], e[2]) * em);
-					if(!kLean && W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
+					if(kGuide && W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
 				}
 				do_nee_all = (s.m->flags & BF_DIFFUSE) && sub == 0;
 				for(int c = 0; c < 3; ++c) nee_weight[c] = thr[c];
@@ -2536,7 +2538,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 						if(mat_emit(s, wo, e))
 						{
 							film_put(P, film, film64, pixel, si, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
-							if(!kLean && W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
+							if(kGuide && W.p_sum) path_sum_add(W, path, xm(thr[0], e[0]), xm(thr[1], e[1]), xm(thr[2], e[2]));
 						}
 				}
 			}
@@ -2622,7 +2624,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 				uint32_t sflags;
 				float mult[3], mpdf = 0.f, hf = 0.f;
 				const bool guidable = (s.m->type == GBRT_MAT_SHINYDIFFUSE && s.m->sd == SD_DIFFUSE) || s.m->type == GBRT_MAT_GLOSSY;
-				if(!kLean && P.guiding && guidable)
+				if(kGuide && P.guiding && guidable)
 				{
 					// one-sample MIS of the guide mixture q and the BSDF sampler
 					// (true density p): weight = h(w) / (alpha q(w) + (1 - alpha) p(w)),
@@ -2658,7 +2660,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 				{
 					mat_sample_l<kLean>(s, wo, s1, s2, req, wi, scol, w, pdf, sflags);
 					for(int c = 0; c < 3; ++c) mult[c] = xm(scol[c], w);
-					if(!kLean && P.record && guidable)
+					if(kGuide && P.record && guidable)
 					{
 						mpdf = bsdf_true_pdf(s, wo, wi, req);
 						hf = (0.2126f * mult[0] + 0.7152f * mult[1] + 0.0722f * mult[2]) * mpdf;
@@ -2676,7 +2678,7 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 				if(nt[0] != 0.f || nt[1] != 0.f || nt[2] != 0.f)
 				{
 					cont = true;
-					if(!kLean && P.record && mpdf > 0.f && k < P.rec_stride)
+					if(kGuide && P.record && mpdf > 0.f && k < P.rec_stride)
 					{
 						const size_t slot = static_cast<size_t>(path) * P.rec_stride + k;
 						W.r_pos[slot] = make_float4(s.p[0], s.p[1], s.p[2], mpdf);
@@ -2713,11 +2715,11 @@ __device__ __forceinline__ void shade_queue(const Src &src, Work W, int cur, uin
 	}
 }
 
-template <bool kTex>
+template <bool kTex, bool kGuide>
 __global__ void __launch_bounds__(kThreads, 4) k_shade(SceneDev sc, Params P, Work W, int cur, uint32_t shadow_cap, float *film,
                                                     double *film64)
 {
-	shade_queue<OneScene, false, kTex>(OneScene{sc, P, film, film64}, W, cur, shadow_cap);
+	shade_queue<OneScene, false, kTex, kGuide>(OneScene{sc, P, film, film64}, W, cur, shadow_cap);
 }
 
 // The same for plain scenes (shade_queue kLean).
@@ -4981,10 +4983,16 @@ static int render_locked(gbrt_scene *S, const gbrt_camera_desc *camera, const gb
 				if(int rc = gbrt_guide_eval_queue(guide, Ww.hitpos, n, Ww.count + cur, Ww.lobes, s)) return rc;
 			if(plain && !Pw.guiding && !Pw.record)
 				k_shade_plain<<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+			else if(guide)
+			{
+				// the guided instances also serve the vertex levels past guide_max_vertex (no guiding, no records there)
+				if(tex) k_shade<true, true><<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+				else k_shade<false, true><<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+			}
 			else if(tex)
-				k_shade<true><<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+				k_shade<true, false><<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
 			else
-				k_shade<false><<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
+				k_shade<false, false><<<grid_for(n, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, cur, static_cast<uint32_t>(shadow_cap), film, film64_dev);
 			const uint32_t scap = static_cast<uint32_t>(shadow_cap);
 			if(Pw.film_w && Pw.tshadow && tex)
 				k_shadow<true, true, true><<<persistent_grid(k_shadow<true, true, true>, shadow_cap, S->n_sm), kThreads, 0, s>>>(sc, Pw, Ww, scap, film,
