@@ -554,7 +554,7 @@ def main():
                                "U[-0.01,0.01]), 16,777,216 incoherent rays (origins U[-0.2,1.2]^3, directions "
                                "uniform on S^2), closest hit",
                    "triangles": args.tris, "rays_per_gpu": args.rays, "l2": "inputs (512 MiB rays) larger than L2; no flush",
-                   "max_leaf_size": 4, "hit_fraction": hit_frac, "bvh_build_s": build_s,
+                   "max_leaf_size": 4, "sah_intersect_cost": 2.0, "hit_fraction": hit_frac, "bvh_build_s": build_s,
                    "bvh_nodes": info["n_nodes"], "bvh_depth": info["max_depth"], "bvh_sah": info["sah_cost"]},
         "gpu_launches": args.steps,
         "anyhit_mrays_s": anyhit_mrays,

@@ -67,7 +67,7 @@ typedef struct gbrt_hit {
 typedef struct gbrt_build_params {
 	uint32_t max_leaf_size;   /* 1..16; 0 = default (4) */
 	float traversal_cost;     /* SAH cost of a node visit; 0 = default (1.0) */
-	float intersect_cost;     /* SAH cost of a primitive test; 0 = default (1.0) */
+	float intersect_cost;     /* SAH cost of a primitive test; 0 = default (2.0: leaves of one triangle, mostly) */
 	uint32_t flags;           /* GBRT_BUILD_* bits; 0 = default */
 } gbrt_build_params;
 

@@ -36,6 +36,14 @@
 #include <cmath>
 #include <cstring>
 
+// SAH cost of a primitive test relative to a node visit when the caller
+// gives none.  The 8-wide node test is cheaper than the reference's exact
+// Moller-Trumbore test, so at 2 nearly every leaf holds one triangle;
+// measured on a GB300 (1,048,576-triangle soup, 16.8M incoherent rays),
+// cost 1 / 2 / 3: closest hit 2,322 / 2,467 / 2,472 Mrays/s, any hit
+// 3,377 / 3,555 / 3,556 (leaf sizes 2-16 at cost 2: within 0.1 %).
+constexpr float kDefaultIntersectCost = 2.f;
+
 namespace {
 
 constexpr int kSortThreads = 256;
@@ -1098,7 +1106,7 @@ int gbrt_build_impl(const float *verts, uint32_t nv, const uint32_t *faces, uint
 	if(p.max_leaf_size == 0) p.max_leaf_size = 4;
 	if(p.max_leaf_size > GBRT_LEAF_MAX_COUNT) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_bvh_build: max_leaf_size %u > %u", p.max_leaf_size, GBRT_LEAF_MAX_COUNT);
 	if(!(p.traversal_cost > 0.f)) p.traversal_cost = 1.f;
-	if(!(p.intersect_cost > 0.f)) p.intersect_cost = 1.f;
+	if(!(p.intersect_cost > 0.f)) p.intersect_cost = kDefaultIntersectCost;
 
 	gbrt_bvh *b = new gbrt_bvh();
 	b->params = p;
@@ -1280,7 +1288,7 @@ extern "C" int gbrt_bvh_build_static(const float *verts, uint32_t nv, const uint
 	if(p.max_leaf_size == 0) p.max_leaf_size = 4;
 	if(p.max_leaf_size > GBRT_LEAF_MAX_COUNT) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_bvh_build_static: max_leaf_size %u > %u", p.max_leaf_size, GBRT_LEAF_MAX_COUNT);
 	if(!(p.traversal_cost > 0.f)) p.traversal_cost = 1.f;
-	if(!(p.intersect_cost > 0.f)) p.intersect_cost = 1.f;
+	if(!(p.intersect_cost > 0.f)) p.intersect_cost = kDefaultIntersectCost;
 	unsigned char *base = nullptr;
 	if(int rc = static_scratch_address(&base)) return rc;
 
