@@ -1,6 +1,6 @@
-// Path-guiding network (no counterpart in the reference; the benchmark spec's
-// learned part): hash-grid encoding + MLP + 8-lobe vMF mixture head, trained
-// online on the tracer's own radiance samples.
+// Path-guiding network (no counterpart in the reference): hash-grid
+// encoding + MLP + 8-lobe vMF mixture head, trained online on the tracer's
+// own radiance samples.
 //
 //   k_guide_eval   position -> mixture parameters (mu, kappa, weight per lobe)
 //   k_guide_grad   forward + KL-divergence gradient + backward for a batch of
