@@ -74,6 +74,10 @@ typedef struct gbrt_build_params {
 /* gbrt_build_params.flags: skip the treelet restructuring passes (plain
  * LBVH topology; for comparisons). */
 #define GBRT_BUILD_NO_TREELETS 1u
+/* Collapse the binary hierarchy into the 8-wide one greedily (open the
+ * largest-area child until 8) instead of by the SAH dynamic programme
+ * (for comparisons). */
+#define GBRT_BUILD_GREEDY_WIDE 2u
 
 typedef struct gbrt_bvh_info {
 	uint32_t n_prims;

@@ -23,13 +23,16 @@
 //                    primitives contiguous after restructuring)
 //   9. k_emit_nodes  64-byte binary nodes holding both children's boxes
 //  10. k_emit_prims  48-byte primitive records in leaf order
-//  11. k_wide_level  8-wide compressed hierarchy for the traversal, one
+//  11. k_wide_cost   SAH dynamic programme over the binary tree choosing
+//                    which subtrees become the children of each 8-wide node
+//  12. k_wide_level  8-wide compressed hierarchy for the traversal, one
 //                    launch per level (layout in gbrt_internal.cuh), after
 //                    Ylitie, Karras & Laine, "Efficient incoherent ray
 //                    traversal on GPUs through compressed wide BVHs", HPG
-//                    2017: greedy collapse of the binary tree (open the
-//                    largest-area child until 8), 8-bit child planes on a
-//                    per-node power-of-two grid, slots by ray octant
+//                    2017: the children k_wide_cost chose (or, with
+//                    GBRT_BUILD_GREEDY_WIDE, the largest-area child opened
+//                    until 8), 8-bit child planes on a per-node
+//                    power-of-two grid, slots by ray octant
 #include "gbrt_internal.cuh"
 
 #include <cfloat>
@@ -778,12 +781,85 @@ struct WideSrc {
 	const uint32_t *ids;
 	uint32_t n_node_cap;           // wide node slots (= task buffer entries)
 	uint32_t n_prims;
+	const uint8_t *choice;         // SAH collapse decisions (k_wide_cost), or null for the greedy collapse
 };
 
 __device__ __forceinline__ bool wide_leaf(uint32_t ref, const WideSrc &W)
 {
 	if(ref & GBRT_LEAF_BIT) return true;
+	if(W.choice) return W.choice[8ull * ref + 7] != 0u;
 	return W.collapse[ref] && __float_as_uint(W.node_hi[ref].w) <= kWideLeafMax;
+}
+
+// SAH-optimal collapse of the binary hierarchy into 8-wide nodes, after
+// Ylitie, Karras & Laine (HPG 2017, section 3.1), bottom up as k_refit.
+// For a binary node n with children L, R, area A and p primitives:
+//   D(n, 1)   = min(leaf: ci A p if p <= 3, wide node: ct A + min_k D(L, k) + D(R, 8 - k))
+//   D(n, j)   = min(D(n, j - 1), min_k D(L, k) + D(R, j - k))      j = 2..7
+// D(n, j) is the cheapest way to hand subtree n to its parent wide node as at
+// most j children; a primitive (binary leaf) costs ci A for every j.
+// cost[7 n + j - 1] = D(n, j); choice[8 n]: the k of the wide node (R gets
+// 8 - k); choice[8 n + j - 1], j = 2..7: 0 = D(n, j - 1), else its k;
+// choice[8 n + 7]: 1 = n is a leaf child.
+__global__ void k_wide_cost(const uint32_t *__restrict__ vals, int n, const float4 *__restrict__ box_lo, const float4 *__restrict__ box_hi,
+                            const uint2 *__restrict__ child, const uint32_t *__restrict__ parent_int, const uint32_t *__restrict__ parent_leaf,
+                            const float4 *__restrict__ node_lo, const float4 *__restrict__ node_hi, uint32_t *flags, float *cost,
+                            uint8_t *choice, float ct, float ci, float *meta)
+{
+	const int j0 = blockIdx.x * blockDim.x + threadIdx.x;
+	if(j0 >= n) return;
+	uint32_t p = __ldcg(parent_leaf + j0);
+	for(int walk = 0; p != kNoParent; ++walk)
+	{
+		if(walk == kMaxWalk) { raise_err(meta, kErrWalk); return; }
+		__threadfence();
+		if(atomicAdd(&flags[p], 1u) == 0u) return;
+		__threadfence();
+		const uint2 c = __ldcg(child + p);
+		const uint32_t cc[2] = {c.x, c.y};
+		float d[2][8];
+		for(int k = 0; k < 2; ++k)
+		{
+			if(cc[k] & GBRT_LEAF_BIT)
+			{
+				const uint32_t prim = vals[cc[k] & ~GBRT_LEAF_BIT];
+				const float v = ci * half_area(box_lo[prim], box_hi[prim]);
+				for(int jj = 1; jj <= 7; ++jj) d[k][jj] = v;
+			}
+			else
+				for(int jj = 1; jj <= 7; ++jj) d[k][jj] = __ldcg(cost + 7ull * cc[k] + jj - 1);
+		}
+		const float area = half_area(node_lo[p], node_hi[p]);
+		const uint32_t cnt = __float_as_uint(node_hi[p].w);
+		uint8_t ch[8];
+		float best = FLT_MAX;
+		ch[0] = 1;
+		for(int k = 1; k <= 7; ++k)
+		{
+			const float v = d[0][k] + d[1][8 - k];
+			if(v < best) { best = v; ch[0] = static_cast<uint8_t>(k); }
+		}
+		const float c_wide = ct * area + best;
+		const float c_leaf = cnt <= kWideLeafMax ? ci * area * static_cast<float>(cnt) : FLT_MAX;
+		float dn[8];
+		dn[1] = fminf(c_leaf, c_wide);
+		ch[7] = c_leaf <= c_wide ? 1 : 0;
+		for(int jj = 2; jj <= 7; ++jj)
+		{
+			float b = dn[jj - 1];
+			uint8_t kk = 0;
+			for(int k = 1; k < jj; ++k)
+			{
+				const float v = d[0][k] + d[1][jj - k];
+				if(v < b) { b = v; kk = static_cast<uint8_t>(k); }
+			}
+			dn[jj] = b;
+			ch[jj - 1] = kk;
+		}
+		for(int jj = 1; jj <= 7; ++jj) __stcg(cost + 7ull * p + jj - 1, dn[jj]);
+		for(int k = 0; k < 8; ++k) choice[8ull * p + k] = ch[k];
+		p = __ldcg(parent_int + p);
+	}
 }
 
 __device__ __forceinline__ void ref_box(uint32_t ref, const WideSrc &W, float4 &lo, float4 &hi)
@@ -830,7 +906,49 @@ __global__ void __launch_bounds__(128) k_wide_level(int level, const uint2 *__re
 			ref_box(c[0], W, lo[0], hi[0]);
 			ref_box(c[1], W, lo[1], hi[1]);
 		}
-		while(n < 8)
+		if(W.choice)
+		{
+			// the children the SAH collapse chose: forests of (node, at most j roots)
+			uint32_t st_ref[16], st_j[16];
+			int sp = 0;
+			const uint32_t k8 = W.choice[8ull * task.x];
+			st_ref[sp] = c[1]; st_j[sp++] = 8u - k8;
+			st_ref[sp] = c[0]; st_j[sp++] = k8;
+			n = 0;
+			bool bad = false;
+			// at most 8 children and 7 splits, each entry stepping down j at most 6 times
+			for(int it = 0; sp > 0 && it < 256; ++it)
+			{
+				const uint32_t r = st_ref[--sp], jj = st_j[sp];
+				uint32_t k = 0;
+				if(!(r & GBRT_LEAF_BIT) && jj >= 2u && jj <= 7u) k = W.choice[8ull * r + jj - 1];
+				if((r & GBRT_LEAF_BIT) || jj <= 1u || jj > 7u) k = 0xFFu;    // one child
+				if(k == 0xFFu)
+				{
+					if(n >= 8) { bad = true; break; }
+					c[n] = r;
+					ref_box(r, W, lo[n], hi[n]);
+					++n;
+				}
+				else if(k == 0u)
+				{
+					st_ref[sp] = r; st_j[sp++] = jj - 1u;
+				}
+				else
+				{
+					if(sp + 2 > 16 || k >= jj) { bad = true; break; }
+					const uint2 rc = W.child[r];
+					st_ref[sp] = rc.y; st_j[sp++] = jj - k;
+					st_ref[sp] = rc.x; st_j[sp++] = k;
+				}
+			}
+			if(bad || sp > 0 || n < 2)
+			{
+				raise_err(meta, kErrWide);
+				continue;
+			}
+		}
+		while(!W.choice && n < 8)
 		{
 			int best = -1;
 			float ba = -1.f;
@@ -1152,6 +1270,8 @@ int gbrt_build_impl(const float *verts, uint32_t nv, const uint32_t *faces, uint
 	const size_t o_nlo = carve(16ull * n_int), o_nhi = carve(16ull * n_int);
 	const size_t o_flags = carve(4ull * n_int), o_coll = carve(n_int);
 	const size_t o_task0 = carve(8ull * n_int), o_task1 = carve(8ull * n_int), o_counts = carve(4ull * (GBRT_WIDE_MAX_LEVELS + 1));
+	const bool sah_wide = !(p.flags & GBRT_BUILD_GREEDY_WIDE);
+	const size_t o_wcost = sah_wide ? carve(28ull * n_int) : 0, o_wchoice = sah_wide ? carve(8ull * n_int) : 0;
 	Scratch sc(s);
 	if((e = cudaMallocAsync(&sc.p, off, s)) != cudaSuccess)
 		return fail(gbrt_set_error(GBRT_ERR_OOM, "gbrt_bvh_build: scratch allocation of %zu bytes failed: %s", off, cudaGetErrorString(e)));
@@ -1185,7 +1305,17 @@ int gbrt_build_impl(const float *verts, uint32_t nv, const uint32_t *faces, uint
 		if((e = cudaMemsetAsync(counts, 0, 4ull * (GBRT_WIDE_MAX_LEVELS + 1), s)) != cudaSuccess)
 			return fail(gbrt_set_error(GBRT_ERR_CUDA, "memset: %s", cudaGetErrorString(e)));
 		k_wide_init<<<1, 1, 0, s>>>(b->meta, task[0], counts);
-		WideSrc W{B.child, B.vals, B.blo, B.bhi, B.nlo, B.nhi, B.coll, B.pos_leaf, B.first_int, b->tris, b->ids, n_int, nf};
+		uint8_t *wchoice = nullptr;
+		if(sah_wide)
+		{
+			float *wcost = reinterpret_cast<float *>(base + o_wcost);
+			wchoice = reinterpret_cast<uint8_t *>(base + o_wchoice);
+			if((e = cudaMemsetAsync(B.flags, 0, 4ull * n_int, s)) != cudaSuccess)
+				return fail(gbrt_set_error(GBRT_ERR_CUDA, "memset: %s", cudaGetErrorString(e)));
+			k_wide_cost<<<blocks_for(nf, 256), 256, 0, s>>>(B.vals, static_cast<int>(nf), B.blo, B.bhi, B.child, B.pint, B.pleaf, B.nlo, B.nhi,
+			                                               B.flags, wcost, wchoice, p.traversal_cost, p.intersect_cost, b->meta);
+		}
+		WideSrc W{B.child, B.vals, B.blo, B.bhi, B.nlo, B.nhi, B.coll, B.pos_leaf, B.first_int, b->tris, b->ids, n_int, nf, wchoice};
 		int n_sm = 0;
 		GBRT_CK(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, b->device));
 		const unsigned wgrid = std::max(1u, std::min(blocks_for(n_int, 128), static_cast<unsigned>(n_sm) * 8u));

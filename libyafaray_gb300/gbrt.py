@@ -26,6 +26,11 @@ class GbrtError(RuntimeError):
 
 
 BUILD_NO_TREELETS = 1
+BUILD_GREEDY_WIDE = 2
+
+
+def _build_flags(treelets, greedy_wide):
+    return (0 if treelets else BUILD_NO_TREELETS) | (BUILD_GREEDY_WIDE if greedy_wide else 0)
 
 
 class BuildParams(ctypes.Structure):
@@ -516,18 +521,19 @@ class Bvh:
         self._h = handle
 
     @classmethod
-    def build_host(cls, vertices, faces, max_leaf_size=0, traversal_cost=0.0, intersect_cost=0.0, treelets=True):
+    def build_host(cls, vertices, faces, max_leaf_size=0, traversal_cost=0.0, intersect_cost=0.0, treelets=True,
+                   greedy_wide=False):
         v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
         f = np.ascontiguousarray(faces, np.uint32).reshape(-1, 4)
-        p = BuildParams(max_leaf_size, traversal_cost, intersect_cost, 0 if treelets else BUILD_NO_TREELETS)
+        p = BuildParams(max_leaf_size, traversal_cost, intersect_cost, _build_flags(treelets, greedy_wide))
         h = ctypes.c_void_p()
         check(load().gbrt_bvh_build_host(_ptr(v), len(v), _ptr(f), len(f), ctypes.byref(p), ctypes.byref(h)))
         return cls(h)
 
     @classmethod
     def build_device(cls, vertices_ptr, n_vertices, faces_ptr, n_faces, stream=0, max_leaf_size=0,
-                     traversal_cost=0.0, intersect_cost=0.0, treelets=True):
-        p = BuildParams(max_leaf_size, traversal_cost, intersect_cost, 0 if treelets else BUILD_NO_TREELETS)
+                     traversal_cost=0.0, intersect_cost=0.0, treelets=True, greedy_wide=False):
+        p = BuildParams(max_leaf_size, traversal_cost, intersect_cost, _build_flags(treelets, greedy_wide))
         h = ctypes.c_void_p()
         check(load().gbrt_bvh_build(ctypes.c_void_p(vertices_ptr), n_vertices, ctypes.c_void_p(faces_ptr), n_faces,
                                     ctypes.byref(p), ctypes.c_void_p(stream), ctypes.byref(h)))

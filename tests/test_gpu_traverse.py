@@ -230,6 +230,28 @@ def test_gpu_wide_structure_random(dev):
             assert len(nodes) < len(f) // 2 and depth < 30
 
 
+def test_gpu_sah_wide_collapse_matches_greedy(dev):
+    """The SAH dynamic-programme collapse into 8-wide nodes (the default) and
+    the greedy largest-area collapse both give valid wide hierarchies, and
+    every closest-hit and any-hit answer is the same; the programme's tree
+    has no more wide nodes than 8-wide packing needs."""
+    from tests.bvh_check import check_wide
+    v, f = scenes.random_triangles(200_000, seed=65, spread=0.02)
+    r = scenes.random_rays(300_000, seed=66)
+    out = {}
+    for greedy in (False, True):
+        for leaf in (1, 4):
+            bvh = gbrt.Bvh.build_host(v, f, max_leaf_size=leaf, greedy_wide=greedy)
+            nodes, prims, ids, depth = bvh.export_wide()
+            assert check_wide(nodes, prims, ids, v, f, depth) == [], (greedy, leaf)
+            assert len(nodes) < len(f) // 2 and depth < 30
+            out[(greedy, leaf)] = (bvh.trace_closest_host(r), bvh.trace_shadow_host(r) >= 0)
+    a = out[(False, 1)]
+    for key, b in out.items():
+        assert np.array_equal(a[0][0], b[0][0]) and np.array_equal(a[0][1].view(np.uint32), b[0][1].view(np.uint32)), key
+        assert np.array_equal(a[1], b[1]), key
+
+
 def test_gpu_treelets_lower_sah_and_keep_results(dev):
     """Treelet restructuring lowers the hierarchy's SAH cost; the binary
     export stays a valid hierarchy and every query answer is unchanged."""
