@@ -521,9 +521,13 @@ def main():
         e2e_s = (time.perf_counter() - t0) / args.steps
         e2e_s = max_over_ranks(e2e_s, dist, "cuda")
         assert np.array_equal(hp[:, 0].view(np.int32), hits_np), "host path disagrees with device path"
+        direct = gbrt.host_path_direct(rp.ctypes.data, args.rays, hp.ctypes.data)
         e2e = {"value": whole_job_rate(args.rays, world, e2e_s), "unit": "Mrays/s",
                "h2d_bytes_per_step": int(rp.nbytes), "d2h_bytes_per_step": int(hp.nbytes),
-               "ms_per_step": e2e_s * 1e3, "gpu_launches_per_step": (args.rays + (1 << 21) - 1) >> 21}
+               "ms_per_step": e2e_s * 1e3,
+               "host_path": "direct: the kernel reads the pinned rays and writes the pinned hits in place" if direct
+               else "staged: 2,097,152-ray chunks copied through device buffers on two streams",
+               "gpu_launches_per_step": 1 if direct else (args.rays + (1 << 21) - 1) >> 21}
 
     render = None if args.no_render else render_sections(args)
     if render is not None:

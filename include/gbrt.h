@@ -187,6 +187,12 @@ int gbrt_trace_shadow(const gbrt_bvh *bvh, const gbrt_ray *rays_dev, uint32_t n,
  * These are what a host Accelerator::intersect batch path binds. */
 int gbrt_trace_closest_host(const gbrt_bvh *bvh, const gbrt_ray *rays, uint32_t n, gbrt_hit *hits);
 int gbrt_trace_shadow_host(const gbrt_bvh *bvh, const gbrt_ray *rays, uint32_t n, int32_t *occluder);
+/* Which way the two calls above would move these buffers: *direct = 1 when
+ * the rays and the results (gbrt_hit records, or occluder IDs if shadow)
+ * are aligned and each lies in one page-locked allocation the device maps,
+ * so the kernel reads and writes them in place in one launch; 0 when they
+ * are staged through device buffers in chunks of 2,097,152 rays. */
+int gbrt_host_path(const gbrt_ray *rays, uint32_t n, const void *out, int shadow, int *direct);
 
 
 /* ---- wavefront path tracer (the `pathtracing` integrator) ---------------

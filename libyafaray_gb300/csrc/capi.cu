@@ -65,6 +65,16 @@ bool mapped_host_range(const void *p, size_t bytes, void **dev)
 	return true;
 }
 
+// Whether host buffers take the direct path: rays 16-byte aligned, results
+// 16-byte aligned (4 for occluder IDs), each inside one page-locked
+// allocation the device maps.
+bool direct_host_path(const void *rays, uint32_t n, const void *out, size_t out_rec, bool shadow, void **rays_dev, void **out_dev)
+{
+	const bool aligned = (reinterpret_cast<uintptr_t>(rays) & 15u) == 0 && (reinterpret_cast<uintptr_t>(out) & (shadow ? 3u : 15u)) == 0;
+	return aligned && mapped_host_range(rays, sizeof(gbrt_ray) * static_cast<size_t>(n), rays_dev) &&
+	       mapped_host_range(out, out_rec * static_cast<size_t>(n), out_dev);
+}
+
 // Host path.  Rays and results in page-locked host memory that the device
 // maps are read and written by the traversal kernel itself, over the
 // host-device link, in one launch (no staging copies).  Otherwise the
@@ -91,9 +101,7 @@ int stage_and_trace(gbrt_bvh *b, const gbrt_ray *rays, uint32_t n, void *out, si
 	int rc = GBRT_OK;
 	void *rays_dev = nullptr, *out_dev = nullptr;
 	// the kernel loads rays and stores hits as 16-byte vectors (4-byte occluder IDs)
-	const bool aligned = (reinterpret_cast<uintptr_t>(rays) & 15u) == 0 && (reinterpret_cast<uintptr_t>(out) & (shadow ? 3u : 15u)) == 0;
-	if(aligned && mapped_host_range(rays, sizeof(gbrt_ray) * static_cast<size_t>(n), &rays_dev) &&
-	   mapped_host_range(out, out_rec * static_cast<size_t>(n), &out_dev))
+	if(direct_host_path(rays, n, out, out_rec, shadow, &rays_dev, &out_dev))
 	{
 		cudaStream_t st = b->stage_stream[0];
 		rc = shadow ? gbrt_launch_shadow(b, static_cast<const gbrt_ray *>(rays_dev), n, static_cast<int32_t *>(out_dev), st)
@@ -316,6 +324,16 @@ int gbrt_trace_closest_host(const gbrt_bvh *b, const gbrt_ray *rays, uint32_t n,
 	if(n == 0) return GBRT_OK;
 	if(!rays || !hits) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_trace_closest_host: NULL buffer");
 	return stage_and_trace(const_cast<gbrt_bvh *>(b), rays, n, hits, sizeof(gbrt_hit), false);
+}
+
+int gbrt_host_path(const gbrt_ray *rays, uint32_t n, const void *out, int shadow, int *direct)
+{
+	if(!direct) return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_host_path: NULL result");
+	*direct = 0;
+	if(n == 0 || !rays || !out) return GBRT_OK;
+	void *rd = nullptr, *od = nullptr;
+	*direct = direct_host_path(rays, n, out, shadow ? sizeof(int32_t) : sizeof(gbrt_hit), shadow != 0, &rd, &od) ? 1 : 0;
+	return GBRT_OK;
 }
 
 int gbrt_trace_shadow_host(const gbrt_bvh *b, const gbrt_ray *rays, uint32_t n, int32_t *occ)

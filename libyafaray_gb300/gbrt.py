@@ -431,6 +431,7 @@ SIGNATURES = {
     "gbrt_trace_shadow": (_I, [_VP, _VP, _U32, _VP, _VP]),
     "gbrt_trace_closest_host": (_I, [_VP, _VP, _U32, _VP]),
     "gbrt_trace_shadow_host": (_I, [_VP, _VP, _U32, _VP]),
+    "gbrt_host_path": (_I, [_VP, _U32, _VP, ctypes.c_int, _VP]),
     "gbrt_scene_create": (_I, [_VP, _VP, _U32, _VP, _U32, _VP, ctypes.POINTER(MaterialDesc), _U32,
                                ctypes.POINTER(LightDesc), _U32, ctypes.POINTER(_VP)]),
     "gbrt_scene_destroy": (_I, [_VP]),
@@ -955,6 +956,14 @@ class Renderer:
                            radiance_photons=st.radiance_photons, photon_ms=st.photon_ms)
             return out
         return None
+
+
+def host_path_direct(rays_ptr, n, out_ptr, shadow=False):
+    """True when gbrt_trace_*_host would trace these host buffers in place
+    (one launch), False when it would stage them in chunks."""
+    d = ctypes.c_int(0)
+    check(load().gbrt_host_path(ctypes.c_void_p(rays_ptr), int(n), ctypes.c_void_p(out_ptr), 1 if shadow else 0, ctypes.byref(d)))
+    return bool(d.value)
 
 
 def aa_flags(film_ptr, weight_ptr, resx, resy, aa, threshold, flags_ptr):

@@ -113,12 +113,15 @@ def test_gpu_pinned_host_buffers_direct_path(dev):
     rp = torch.from_numpy(r).pin_memory()
     hp = torch.empty((len(r), 4), dtype=torch.float32).pin_memory()
     op = torch.empty(len(r), dtype=torch.int32).pin_memory()
+    assert gbrt.host_path_direct(rp.data_ptr(), len(r), hp.data_ptr())
+    assert gbrt.host_path_direct(rp.data_ptr(), len(r), op.data_ptr(), shadow=True)
     gbrt.check(L.gbrt_trace_closest_host(bvh.handle, ctypes.c_void_p(rp.data_ptr()), len(r), ctypes.c_void_p(hp.data_ptr())))
     gbrt.check(L.gbrt_trace_shadow_host(bvh.handle, ctypes.c_void_p(rp.data_ptr()), len(r), ctypes.c_void_p(op.data_ptr())))
     assert np.array_equal(hp.numpy().view(np.uint32), ref_h.view(np.uint32))
     assert np.array_equal(op.numpy(), ref_o)
     # misaligned result buffer inside a pinned allocation: the staged path
     big = torch.empty(len(r) * 4 + 1, dtype=torch.float32).pin_memory()
+    assert not gbrt.host_path_direct(rp.data_ptr(), len(r), big.data_ptr() + 4)
     gbrt.check(L.gbrt_trace_closest_host(bvh.handle, ctypes.c_void_p(rp.data_ptr()), len(r), ctypes.c_void_p(big.data_ptr() + 4)))
     assert np.array_equal(big.numpy()[1:].reshape(-1, 4).view(np.uint32), ref_h.view(np.uint32))
     # pageable buffers
