@@ -404,7 +404,7 @@ int gbrt_scene_set_normals(gbrt_scene *scene, const float *normals, uint32_t n_n
 enum { GBRT_TEXCO_GLOBAL = 0, GBRT_TEXCO_UV = 1 };                 /* "texco" ["global"] */
 enum { GBRT_MAPPING_PLAIN = 0, GBRT_MAPPING_CUBE = 1, GBRT_MAPPING_TUBE = 2, GBRT_MAPPING_SPHERE = 3 };   /* "mapping" ["plain"] */
 enum { GBRT_CLIP_EXTEND = 0, GBRT_CLIP_CLIP = 1, GBRT_CLIP_CLIPCUBE = 2, GBRT_CLIP_REPEAT = 3, GBRT_CLIP_CHECKER = 4 };   /* "clipping" ["repeat"] */
-enum { GBRT_INTERP_NONE = 0, GBRT_INTERP_BILINEAR = 1 };           /* "interpolate" ["bilinear"] */
+enum { GBRT_INTERP_NONE = 0, GBRT_INTERP_BILINEAR = 1, GBRT_INTERP_BICUBIC = 2 };   /* "interpolate" ["bilinear"] */
 
 /* Texture "type" (Texture::Type, include/texture/texture.h:70-84). */
 enum { GBRT_TEX_IMAGE = 0, GBRT_TEX_BLEND = 1, GBRT_TEX_CLOUDS = 2, GBRT_TEX_MARBLE = 3, GBRT_TEX_WOOD = 4, GBRT_TEX_VORONOI = 5,

@@ -807,32 +807,60 @@ __device__ __forceinline__ void shading_normal(const SceneDev &sc, int prim, flo
 
 // ImageTexture::findTextureInterpolationCoordinates (texture_image.cc:
 // 264-341): the texel pair along one axis and the weight.
-__device__ __forceinline__ void tex_axis(float cf, int res, bool repeat, bool mirror, int &c1, int &c2, float &d)
+__device__ __forceinline__ void tex_axis(float cf, int res, bool repeat, bool mirror, int &c1, int &c2, float &d, int *c0 = nullptr,
+                                         int *c3 = nullptr)
 {
+	int o0, o3;
 	if(repeat && mirror)
 	{
 		c1 = static_cast<int>(cf) % res;
-		if(cf < 0.f) { c2 = c1; d = -cf; }
-		else if(cf >= static_cast<float>(res - 1)) { c2 = c1; d = xs(cf, static_cast<float>(static_cast<int>(cf))); }
+		if(cf < 0.f) { o0 = 1 % res; c2 = c1; o3 = o0; d = -cf; }
+		else if(cf >= static_cast<float>(res - 1))
+		{
+			o0 = (2 * res - 1) % res; c2 = c1; o3 = o0;
+			d = xs(cf, static_cast<float>(static_cast<int>(cf)));
+		}
 		else
 		{
+			o0 = (res + c1 - 1) % res;
 			c2 = c1 + 1;
 			if(c2 >= res) c2 = (2 * res - c2) % res;
+			o3 = c1 + 2;
+			if(o3 >= res) o3 = (2 * res - o3) % res;
 			d = xs(cf, static_cast<float>(static_cast<int>(cf)));
 		}
 	}
 	else if(repeat)
 	{
 		c1 = static_cast<int>(cf) % res;
-		if(cf > 0.f) { c2 = (c1 + 1) % res; d = xs(cf, static_cast<float>(static_cast<int>(cf))); }
-		else { c2 = (res - 1) % res; d = -cf; }
+		if(cf > 0.f)
+		{
+			o0 = (res + c1 - 1) % res; c2 = (c1 + 1) % res; o3 = (c1 + 2) % res;
+			d = xs(cf, static_cast<float>(static_cast<int>(cf)));
+		}
+		else { o0 = 1 % res; c2 = (res - 1) % res; o3 = (res - 2) % res; d = -cf; }
 	}
 	else
 	{
 		c1 = max(0, min(res - 1, static_cast<int>(cf)));
 		c2 = cf > 0.f ? min(res - 1, c1 + 1) : 0;
+		o0 = max(0, c1 - 1);
+		o3 = min(res - 1, c2 + 1);
 		d = xs(cf, floorf(cf));
 	}
+	if(c0) *c0 = o0;
+	if(c3) *c3 = o3;
+}
+
+// math::cubicInterpolate (include/math/interpolation.h:70-80) on one channel,
+// the reference's operation order.
+__device__ __forceinline__ float cubic_interp(float y0, float y1, float y2, float y3, float x)
+{
+	const float x2 = xm(x, x), x3 = xm(x, x2);
+	const float a0 = xa(xs(xs(y3, y2), y0), y1);
+	const float a1 = xs(xs(y0, y1), a0);
+	const float a2 = xs(y2, y0);
+	return xa(xa(xa(xm(a0, x3), xm(a1, x2)), xm(a2, x)), y1);
 }
 
 // LayerNode::eval, colour part (shader_node_layer.cc:110-171) with the
@@ -902,7 +930,8 @@ __device__ __forceinline__ float image_adjust_float(const DevTexture &T, float v
 
 // TextureMapperNode::getCoords / doMapping (shader_node_texture.cc:153-230),
 // ImageTexture::getColor / doMapping / noInterpolation /
-// bilinearInterpolation (texture_image.cc:180-262, 343-375) and
+// bilinearInterpolation / bicubicInterpolation (texture_image.cc:180-262,
+// 343-427) and
 // Texture::applyAdjustments (texture.cc:219-253): the texture's RGBA at a
 // hit (getColor); with scalar, also its getFloat (for an image,
 // applyIntensityContrastAdjustments of the colour's brightness, texture.h:52).
@@ -1030,6 +1059,27 @@ __device__ void tex_eval_at(const SceneDev &sc, const DevTexture &T, const float
 		tex_axis(xf, T.w, rep, T.mirror_x != 0, x1, x2, dx);
 		tex_axis(yf, T.h, rep, T.mirror_y != 0, y1, y2, dy);
 		c = __ldg(tx + y1 * T.w + x1);
+	}
+	else if(T.interp == GBRT_INTERP_BICUBIC)
+	{
+		// ImageTexture::bicubicInterpolation (texture_image.cc:387-427): rows
+		// along x first, then the four row results along y
+		const float xf = xs(xm(static_cast<float>(T.w), xs(mx, floorf(mx))), 0.5f);
+		const float yf = xs(xm(static_cast<float>(T.h), xs(my, floorf(my))), 0.5f);
+		int xs4[4], ys4[4];
+		float dx, dy;
+		tex_axis(xf, T.w, rep, T.mirror_x != 0, xs4[1], xs4[2], dx, &xs4[0], &xs4[3]);
+		tex_axis(yf, T.h, rep, T.mirror_y != 0, ys4[1], ys4[2], dy, &ys4[0], &ys4[3]);
+		float4 row[4];
+		for(int j = 0; j < 4; ++j)
+		{
+			const float4 *t = tx + static_cast<size_t>(ys4[j]) * T.w;
+			const float4 a = __ldg(t + xs4[0]), b = __ldg(t + xs4[1]), cc = __ldg(t + xs4[2]), e = __ldg(t + xs4[3]);
+			row[j] = make_float4(cubic_interp(a.x, b.x, cc.x, e.x, dx), cubic_interp(a.y, b.y, cc.y, e.y, dx),
+			                     cubic_interp(a.z, b.z, cc.z, e.z, dx), cubic_interp(a.w, b.w, cc.w, e.w, dx));
+		}
+		c = make_float4(cubic_interp(row[0].x, row[1].x, row[2].x, row[3].x, dy), cubic_interp(row[0].y, row[1].y, row[2].y, row[3].y, dy),
+		                cubic_interp(row[0].z, row[1].z, row[2].z, row[3].z, dy), cubic_interp(row[0].w, row[1].w, row[2].w, row[3].w, dy));
 	}
 	else
 	{
@@ -4529,7 +4579,7 @@ int gbrt_scene_set_textures(gbrt_scene *S, const float *uv, uint32_t n_uv, const
 		if(image && static_cast<uint64_t>(t.width) * static_cast<uint64_t>(t.height) >= (1ull << 31))
 			return gbrt_set_error(GBRT_ERR_CAPACITY, "gbrt_scene_set_textures: texture %u has %d x %d texels (at most 2^31 - 1 per texture)",
 			                      i, t.width, t.height);
-		if(t.interpolate > GBRT_INTERP_BILINEAR || t.clipping > GBRT_CLIP_CHECKER || t.texco > GBRT_TEXCO_UV || t.mapping > GBRT_MAPPING_SPHERE)
+		if(t.interpolate > GBRT_INTERP_BICUBIC || t.clipping > GBRT_CLIP_CHECKER || t.texco > GBRT_TEXCO_UV || t.mapping > GBRT_MAPPING_SPHERE)
 			return gbrt_set_error(GBRT_ERR_INVALID, "gbrt_scene_set_textures: texture %u: unsupported interpolate / clipping / texco / mapping", i);
 		DevTexture &d = tex[i];
 		d.kind = t.kind;

@@ -290,7 +290,7 @@ def procedural_desc(t):
         p.ramp[i][:] = [*c[:4], float(t.get(f"ramp_item_{i}_position", 0.0))]
     return p
 CLIPPING = {"extend": 0, "clip": 1, "clipcube": 2, "repeat": 3, "checker": 4}
-INTERPOLATE = {"none": 0, "bilinear": 1}
+INTERPOLATE = {"none": 0, "bilinear": 1, "bicubic": 2}
 BLEND_MODES = {"mix": 0, "add": 1, "multiply": 2, "subtract": 3, "screen": 4, "divide": 5, "difference": 6, "darken": 7,
                "lighten": 8}
 

@@ -393,7 +393,9 @@ def textured_cornell_scene(res=64, **kw):
     interpolation) through a layer node (multiply, colfac 0.8 over the
     material colour); the short box a checker-clipped texture (odd tiles,
     checker_dist 0.2) in global coordinates.  Everything else is the plain
-    Cornell box."""
+    Cornell box.  interpolate (e.g. "bicubic") replaces the interpolation
+    of all three textures."""
+    interpolate = kw.pop("interpolate", None)
     sc = cornell_scene(res=res, **kw)
     sc["textures"] = {
         "checker": {"image": checker_image(16, 16), "interpolate": "bilinear", "clipping": "repeat",
@@ -406,6 +408,9 @@ def textured_cornell_scene(res=64, **kw):
                    "clipping": "checker", "checker_dist": 0.2, "texco": "global", "mapping": "plain",
                    "scale": (2.0, 2.0, 2.0)},
     }
+    if interpolate:
+        for t in sc["textures"].values():
+            t["interpolate"] = interpolate
     sc["materials"]["back_tex"] = ("shinydiffusemat", (0.75, 0.75, 0.75), {"diffuse_texture": "checker"})
     sc["materials"]["box_tex"] = ("shinydiffusemat", (0.75, 0.75, 0.75), {"diffuse_texture": "tiles"})
     sc["materials"]["box2_tex"] = ("shinydiffusemat", (0.75, 0.75, 0.75), {"diffuse_texture": "checks"})

@@ -17,7 +17,8 @@ cornell_pm, dl, batch, hashgrid, film (gauss film), aa (adaptive-AA film
 states + flags and an adaptive render), aa_pm (adaptive passes of
 photonmapping / directlighting), cornell_tshadow (transparent shadows,
 shadowDepth 4 and 1), cornell_textured (image textures, mapper and layer
-nodes), cornell_sppm (SPPM with and without pmIRE), cornell_smooth (smoothed
+nodes), cornell_bicubic (the same textures with bicubic interpolation),
+cornell_sppm (SPPM with and without pmIRE), cornell_smooth (smoothed
 vertex normals), cornell_pt_caustics (pathtracing caustic_type / no_recursive),
 pm_full (config-5 photon maps at full size, as bucketed digests),
 cornell_512 (the Cornell configuration at 512x512), cornell_procedural
@@ -351,6 +352,15 @@ if __name__ == "__main__":
                             se=(rgb.std(0, ddof=1) / np.sqrt(32)).astype(np.float32), batches=np.int32(32),
                             spp=np.int32(16), seconds=secs)
         print(f"cornell_textured_64_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
+    if "cornell_bicubic" in what:
+        # the same textures with bicubic interpolation (repeat + mirror, extend
+        # and checker-clipped lookups)
+        sc = scenes.textured_cornell_scene(res=48, interpolate="bicubic")
+        rgb, secs = orc.run_reference_render(sc, 16, 24, threads=os.cpu_count() or 1)
+        np.savez_compressed(os.path.join(OUT, "cornell_bicubic_48_render.npz"), mean=rgb.mean(0).astype(np.float32),
+                            se=(rgb.std(0, ddof=1) / np.sqrt(24)).astype(np.float32), batches=np.int32(24),
+                            spp=np.int32(16), seconds=secs)
+        print(f"cornell_bicubic_48_render.npz: mean {rgb.mean(axis=(0, 1, 2))}, {secs.sum():.1f} s")
     if "cornell_procedural" in what:
         # procedural textures (marble, clouds with an HSV ramp, voronoi cells,
         # wood rings under a layer node, a tube-mapped ridged Musgrave fractal);

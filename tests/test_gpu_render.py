@@ -157,6 +157,23 @@ def test_gpu_cornell_textured_matches_reference(cuda_device):
     assert frac >= 0.995
 
 
+def test_gpu_cornell_bicubic_matches_reference(cuda_device):
+    """The textured Cornell box with bicubic image interpolation on all three
+    textures (ImageTexture::bicubicInterpolation: the repeat + mirror lookup
+    of the back wall, the extend and checker-clipped lookups of the boxes).
+    The same scene with bilinear lookups is scored against the bicubic
+    golden for comparison (printed)."""
+    g = np.load(os.path.join(GOLD, "cornell_bicubic_48_render.npz"))
+    r = gbrt.Renderer(scenes.textured_cornell_scene(res=48, interpolate="bicubic"))
+    gb = batches(r, int(g["spp"]), int(g["batches"]))
+    frac, relmse, m = parity(gb, g["mean"], g["se"])
+    rl = gbrt.Renderer(scenes.textured_cornell_scene(res=48, interpolate="bilinear"))
+    fl, rel_l, _ = parity(batches(rl, int(g["spp"]), int(g["batches"])), g["mean"], g["se"])
+    print(f"cornell bicubic 48x48: {100 * frac:.2f}% of pixel channels within 3 SE, relMSE {relmse:.3g} "
+          f"(bilinear lookups against the same golden: {100 * fl:.2f}%, relMSE {rel_l:.3g})")
+    assert frac >= 0.995
+
+
 @pytest.mark.parametrize("name,ire", [("cornell_sppm_48_render.npz", False), ("cornell_sppm_ire_48_render.npz", True),
                                       ("cornell_sppm_dense_48_render.npz", False)])
 def test_gpu_cornell_sppm_matches_reference(cuda_device, name, ire):
